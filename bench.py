@@ -1,0 +1,420 @@
+"""Benchmark: converged POIs/s of the 2D subset-DIC hot path on one GB300 (per rank).
+
+Workload (BASELINE configuration 2): a 2048 x 2048 uint8 synthetic speckle pair (24000 blobs,
+u = 0.5 sin(2 pi x / 256), v = 0.3 cos(2 pi y / 192), noise 1), first-order ZNSSD ICGN, bicubic
+B-spline, subset radius 15, POI step 5 (410 x 410 grid, 163,216 interior POIs), threshold 1e-3,
+20 iterations, seed from the reference initializer.
+
+One step = the hot path over one image pair with the inputs resident in HBM: image conversion
+and B-spline prefilter (K1), then the frontier-wave propagation over every grid POI (K3), with
+device outputs.  ``value`` = converged POIs (valid, strictly converged, accepted) / step time.
+``e2e`` = the same through the public API ``subset.compute`` with pinned host images: upload,
+seed selection, prefilter, propagation and the device->host result dict, every step.
+L2 (129 MB) is flushed with a 256 MB write between timed steps.
+
+``--impl reference`` times the reference algorithm's CPU implementation (the FP64 C++ port in
+oracle/, the reference itself does not build without Eigen) on a bounded sample of the same
+workload: reliability-guided heap propagation, single thread as the reference runs.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+import __graft_entry__  # noqa: E402
+
+__graft_entry__.load_package()
+
+METRIC = "converged POIs/s, 2048^2 r=15 (FP32 vs FP64, <=1e-3 px)"
+UNIT = "POI/s"
+WORKLOAD = {
+    "workload": "synthetic speckle 2048x2048 uint8, sinusoidal u/v, radius 15, POI step 5 (BASELINE config 2)",
+    "image": [2048, 2048], "dtype_in": "uint8", "subset_radius": 15, "poi_step": 5, "grid": [410, 410],
+    "bspline_degree": 3, "threshold": 1e-3, "max_iterations": 20, "shape_function": "first_order",
+    "optimizer": "icgn", "propagation": "frontier waves", "l2": "flushed (256 MB write) between timed steps",
+}
+CONFIG = {
+    "subset": {"radius": 15},
+    "optimization": {"max_iterations": 20, "convergence_threshold": 1e-3},
+    "interpolation": {"degree": 3},
+    "initialization": {"method": "integer_search",
+                       "integer_search": {"subset_radius": 10, "search_radius": 20, "sift_enabled": False,
+                                          "pyramid_enabled": True},
+                       "subpixel_refinement": {"enabled": True, "subset_radius": 15, "max_iterations": 20,
+                                               "convergence_threshold": 1e-3}},
+    "seed_selection": {"seed_count": 64, "max_znssd": 0.3, "min_texture_std": 0.02},
+    "reliability_propagation": {"spacing": 4, "max_znssd": 0.5},
+}
+
+
+def icgn_flops(iterations: np.ndarray, n_samples: int) -> float:
+    """Algorithmic FP32 flops of the ICGN solves (FMA = 2): per POI 52 N setup + per iteration
+    (94 N + 150)."""
+    it = iterations.astype(np.float64)
+    solved = it > 0
+    return float(np.sum(solved * 52.0 * n_samples + it * (94.0 * n_samples + 150.0)))
+
+
+def n_samples(r: int) -> int:
+    return sum(1 for dy in range(-r, r + 1) for dx in range(-r, r + 1) if dx * dx + dy * dy <= r * r)
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self, device: int = 0) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9 or parts[0] != str(device):
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+def fp32_peak_tflops(torch) -> float:
+    """Measured FP32 CUDA-core throughput: cuBLAS SGEMM 8192^3 with TF32 disabled, best of 5."""
+    torch.backends.cuda.matmul.allow_tf32 = False
+    a = torch.randn(8192, 8192, device="cuda", dtype=torch.float32)
+    b = torch.randn(8192, 8192, device="cuda", dtype=torch.float32)
+    for _ in range(2):
+        a @ b
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        a @ b
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e) / 1e3)
+    del a, b
+    return 2.0 * 8192 ** 3 / best / 1e12
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v: float) -> float:
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, v: float) -> float:
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------------------
+def run_reference(args, world, rank, pg):
+    """Reference arm: the FP64 C++ port of the reference path on the host cores (rank 0)."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from traditional_dic_gb300 import subset as S, synthetic
+    pair = synthetic.workload(1)
+    cfg = O.as_config(S.config_from_dict(CONFIG))
+    cfg.propagation_mode = 1  # reliability-guided heap order: the reference's own visit order
+    t0 = time.perf_counter()
+    seed, _ = O.select_seed(pair.reference, pair.deformed, cfg)
+    t_seed = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    coef = O.prefilter(pair.deformed, 3, 3, True)
+    grads = O.reference_gradient(pair.reference)
+    t_pre = time.perf_counter() - t0
+    budget = args.ref_solves
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        O.propagate(pair.reference, coef, cfg, seed, gradients=grads, max_solves=min(200, budget))
+    rates, solved, conv_total, t_total = [], 0, 0, 0.0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        r = O.propagate(pair.reference, coef, cfg, seed, gradients=grads, max_solves=budget)
+        dt = time.perf_counter() - t0
+        conv = int(np.sum(r["valid"] & r["converged"]))
+        rates.append(conv / dt)
+        solved += r["solves"]
+        conv_total += conv
+        t_total += dt
+    value = conv_total / t_total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": dict(WORKLOAD, propagation="reliability-guided heap (serial, reference order)"),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"first {budget} heap-order solves of the 2048^2 workload per step "
+                                   f"(seed selection {t_seed:.2f} s and prefilter+gradients {t_pre:.2f} s "
+                                   f"untimed, once)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local, pg):
+    import torch
+    from traditional_dic_gb300 import subset as S, synthetic, _lib as L
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ctx = S.Context(local)
+    pair_np = synthetic.workload(1)
+    h, w = pair_np.reference.shape
+    cfg = S.config_from_dict(CONFIG)
+    cfg.precision = L.FP64 if args.precision == "fp64" else L.FP32_MIXED
+    r = cfg.subset_radius
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+    ref_d = torch.from_numpy(pair_np.reference).to(dev)
+    def_d = torch.from_numpy(pair_np.deformed).to(dev)
+    gw, gh = L.grid_dims(w, h, cfg.propagation_spacing)
+    n = gw * gh
+    outs = {k: torch.empty(n, dtype=torch.float64, device=dev) for k in
+            ("x", "y", "u", "v", "du_dx", "du_dy", "dv_dx", "dv_dy", "correlation", "zncc")}
+    outs["valid"] = torch.empty(n, dtype=torch.uint8, device=dev)
+    outs["status"] = torch.empty(n, dtype=torch.int8, device=dev)
+    outs["iterations"] = torch.empty(n, dtype=torch.int32, device=dev)
+    outs["converged"] = torch.empty(n, dtype=torch.uint8, device=dev)
+    grid = L.GridOut(**{k: outs[k].data_ptr() for k in L.GRID_FIELDS})
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    # Seed from the reference initializer (tdic_select_seed), once, untimed: it is an input of
+    # the hot path.  The e2e leg below re-runs it every step.
+    _, seed = S.compute(pair_np.reference, pair_np.deformed, dict(CONFIG, gpu={"precision": args.precision}),
+                        context=ctx, return_seed=True)
+    assert seed.found, "no seed found"
+    pair = S.Pair(ctx, ref_d, def_d, degree=3, precision=cfg.precision, stream=stream)
+    pc = __import__("ctypes").c_int32()
+
+    def step():
+        pair.update(ref_d, def_d, stream=stream)
+        ctx.check(ctx.lib.tdic_propagate(ctx.handle, pair.handle, __import__("ctypes").byref(cfg),
+                                         __import__("ctypes").byref(seed), None, __import__("ctypes").byref(grid),
+                                         L.DEVICE, __import__("ctypes").byref(pc), sptr))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = Clocks()
+    barrier(pg)
+    torch.cuda.synchronize()
+    clocks.start()
+    times, prop_times = [], []
+    conv_counts = []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
+            pair.update(ref_d, def_d, stream=stream)
+            e1.record(stream)
+            ctx.check(ctx.lib.tdic_propagate(ctx.handle, pair.handle, __import__("ctypes").byref(cfg),
+                                             __import__("ctypes").byref(seed), None, __import__("ctypes").byref(grid),
+                                             L.DEVICE, __import__("ctypes").byref(pc), sptr))
+            e2.record(stream)
+        e2.synchronize()
+        times.append(e0.elapsed_time(e2) / 1e3)
+        prop_times.append(e1.elapsed_time(e2) / 1e3)
+        conv_counts.append(int(((outs["valid"] != 0) & (outs["converged"] != 0)).sum().item()))
+    torch.cuda.synchronize()
+    barrier(pg)
+    clk = clocks.stop(local)
+    t_step = max_over_ranks(pg, sum(times) / len(times))
+    conv = conv_counts[-1]
+    total_conv = sum_over_ranks(pg, float(conv))
+    value = total_conv / t_step
+
+    iters = outs["iterations"].cpu().numpy()
+    flops = icgn_flops(iters, n_samples(r))
+    t_prop = statistics.median(prop_times)
+    peaks = measured_peaks()
+    fp32_peak = fp32_peak_tflops(torch)
+    roofline = {"kernel": "propagate_kernel (ICGN, FP32 mixed)", "bound": "fp32",
+                "achieved": flops / t_prop / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": flops / t_prop / 1e12 / fp32_peak,
+                "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, TF32 off (MEASURED_PEAKS.json holds "
+                               "HBM and bf16 only)",
+                "algorithmic_flops_per_launch": flops, "traffic": None,
+                "hbm_peak_gbs": peaks.get("hbm_gbs")}
+
+    # FP64 GPU path on the same configuration, for the precision comparison.
+    res32 = {k: outs[k].cpu().numpy().copy() for k in ("u", "v", "valid", "converged", "zncc")}
+    fp64 = None
+    if args.precision == "fp32" and not args.skip_fp64:
+        cfg64 = S.config_from_dict(CONFIG)
+        cfg64.precision = L.FP64
+        pair64 = S.Pair(ctx, ref_d, def_d, degree=3, precision=L.FP64, stream=stream)
+        t64 = []
+        for i in range(2):
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            pair64.update(ref_d, def_d, stream=stream)
+            ctx.check(ctx.lib.tdic_propagate(ctx.handle, pair64.handle, __import__("ctypes").byref(cfg64),
+                                             __import__("ctypes").byref(seed), None, __import__("ctypes").byref(grid),
+                                             L.DEVICE, __import__("ctypes").byref(pc), sptr))
+            b.record(stream)
+            b.synchronize()
+            if i:
+                t64.append(a.elapsed_time(b) / 1e3)
+        v64 = outs["valid"].cpu().numpy() != 0
+        c64 = outs["converged"].cpu().numpy() != 0
+        both = v64 & (res32["valid"] != 0)
+        du = np.abs(outs["u"].cpu().numpy()[both] - res32["u"][both])
+        dv = np.abs(outs["v"].cpu().numpy()[both] - res32["v"][both])
+        dz = np.abs(outs["zncc"].cpu().numpy()[both] - res32["zncc"][both])
+        fp64 = {"value": float(np.sum(v64 & c64)) / t64[0], "ms_per_step": 1e3 * t64[0],
+                "speedup_fp32_over_fp64": value / (float(np.sum(v64 & c64)) / t64[0]),
+                "fp32_vs_fp64": {"max_abs_u_px": float(du.max()), "max_abs_v_px": float(dv.max()),
+                                 "p99_abs_u_px": float(np.quantile(du, 0.99)), "max_abs_zncc": float(dz.max()),
+                                 "flag_agreement": float(np.mean(v64 == (res32["valid"] != 0))),
+                                 "within_1e-3_px": float(np.mean((du <= 1e-3) & (dv <= 1e-3)))}}
+        pair64.close()
+
+    # e2e through the public API with pinned host images.
+    ref_pin = torch.from_numpy(pair_np.reference).pin_memory()
+    def_pin = torch.from_numpy(pair_np.deformed).pin_memory()
+    ref_h, def_h = ref_pin.numpy(), def_pin.numpy()
+    e2e_cfg = dict(CONFIG, gpu={"precision": args.precision})
+    S.compute(ref_h, def_h, e2e_cfg, context=ctx)
+    barrier(pg)
+    t0 = time.perf_counter()
+    e2e_conv = 0
+    for _ in range(args.steps):
+        res = S.compute(ref_h, def_h, e2e_cfg, context=ctx)
+        e2e_conv = int(np.sum(res["valid"] & res["converged"]))
+    t_e2e = max_over_ranks(pg, (time.perf_counter() - t0) / args.steps)
+    e2e_value = sum_over_ranks(pg, float(e2e_conv)) / t_e2e
+    d2h = n * (10 * 8 + 1 + 1 + 4 + 1)
+
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        ocfg = O.as_config(cfg)
+        ocfg.propagation_mode = 1
+        coef = O.prefilter(pair_np.deformed, 3, 3, True)
+        grads = O.reference_gradient(pair_np.reference)
+        oseed = O.make_seed(seed.x, seed.y, list(seed.p), seed.correlation)
+        t0 = time.perf_counter()
+        rr = O.propagate(pair_np.reference, coef, ocfg, oseed, gradients=grads, max_solves=args.ref_solves)
+        dt = time.perf_counter() - t0
+        cpu = {"value": float(np.sum(rr["valid"] & rr["converged"])) / dt, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"first {rr['solves']} heap-order solves of the same 2048^2 workload "
+                         f"({dt:.1f} s, FP64 C++ port of the reference path, 1 thread)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64 (mixed)" if args.precision == "fp32" else "f64",
+            "data": "synthetic", "config": dict(WORKLOAD, precision=args.precision,
+                                                  parallelism=f"replicas x{world}" if world > 1 else "1 GPU"),
+            "converged_pois_per_step": conv,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(2 * h * w),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * t_e2e,
+                    "includes": "H2D of both images (pinned), seed selection, prefilter, propagation, D2H of the "
+                                "result dict"},
+            "fp64_path": fp64,
+            "gpu_launches": 5 * args.steps,
+            "clocks": clk,
+            "stages_ms": {"prefilter_and_convert": 1e3 * (statistics.median(times) - t_prop),
+                          "propagate": 1e3 * t_prop},
+        }
+        print(json.dumps(line), flush=True)
+    pair.close()
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--ref-solves", type=int, default=20000)
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-fp64", action="store_true")
+    args = ap.parse_args()
+    world, rank, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank, pg)
+    else:
+        __graft_entry__.build()
+        run_ours(args, world, rank, local, pg)
+
+
+if __name__ == "__main__":
+    main()

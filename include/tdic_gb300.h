@@ -1,0 +1,209 @@
+/*
+ * tdic_gb300.h -- C ABI of the GB300 (sm_103a) 2D subset-DIC hot path.
+ *
+ * Drop-in boundary for lbd-hfut/Traditional-DIC.  The reference has no C ABI; its seams are
+ *   - the per-POI virtual call SubsetSolver::solve_with_interpolators
+ *     (include/dic/subset/solver/subset_solver.hpp:39-65), called inside the propagation heap
+ *     loop of ReliabilityPropagation::propagate (src/subset/seed/reliability_propagation.cpp:283-389);
+ *   - the pybind entry _traditional_dic.subset.compute(reference, deformed, config, roi)
+ *     (bindings/python/bind_subset.cpp:253-356) that wraps SubsetDIC::compute
+ *     (src/subset/subset_dic.cpp:39-105).
+ * Every entry point below names the reference interface it replaces.  Plain C types only:
+ * pointers, sizes, POD structs.  Nothing throws across this boundary; every call returns a
+ * tdic_status and tdic_last_error() holds the message of the last failure on the context.
+ *
+ * Threading: a context is internally locked (one call at a time per context); use one
+ * context per host thread for concurrency.  Streams are passed as void* (cudaStream_t);
+ * NULL means the context's own stream.
+ */
+#ifndef TDIC_GB300_H
+#define TDIC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum tdic_status {
+    TDIC_OK = 0,
+    TDIC_INVALID_ARG = 1,   /* reference: std::invalid_argument / pybind TypeError, ValueError */
+    TDIC_OOM = 2,           /* device allocation or admission refused */
+    TDIC_CUDA_ERROR = 3,    /* a CUDA runtime error (message in tdic_last_error) */
+    TDIC_TIMEOUT = 4,       /* a bounded device-side wait ran out */
+    TDIC_UNSUPPORTED = 5    /* second-order / SSD / masked routes: not on this path */
+} tdic_status;
+
+typedef enum tdic_dtype { TDIC_U8 = 0, TDIC_U16 = 1, TDIC_F32 = 2, TDIC_F64 = 3 } tdic_dtype;
+
+typedef enum tdic_memory { TDIC_HOST = 0, TDIC_DEVICE = 1 } tdic_memory;
+
+typedef enum tdic_precision { TDIC_FP32_MIXED = 0, TDIC_FP64 = 1 } tdic_precision;
+
+/* Per-POI status ordinals = dic::SolverStatus (include/dic/core/types.hpp:35-40). */
+enum { TDIC_SUCCESS = 0, TDIC_NOT_CONVERGED = 1, TDIC_INVALID_INPUT = 2, TDIC_NUMERICAL_FAILURE = 3 };
+
+/* The knobs of dic::SubsetConfig reachable from the pybind config dict
+ * (include/dic/subset/subset_config.hpp:33-50, include/dic/initialization/seed_config.hpp:32-68,
+ * include/dic/interpolation/bspline.hpp:42-67), C++ defaults from tdic_config_default().
+ * propagation_mode and precision are GPU-only knobs (the reference has neither). */
+typedef struct tdic_config {
+    int32_t subset_radius;             /* subset.radius                               15 */
+    int32_t max_iterations;            /* optimization.max_iterations                 30 */
+    double convergence_threshold;      /* optimization.convergence_threshold        1e-3 */
+    int32_t optimizer;                 /* optimization.method: 0 icgn, 1 fgn           0 */
+    int32_t shape_order;               /* shape_function.order                          1 */
+    int32_t criterion;                 /* correlation.criterion: 1 znssd, 0 ssd         1 */
+    int32_t degree;                    /* interpolation.degree (1, 3; else 5)           5 */
+    int32_t border;                    /* B-spline border (>= 3)                        3 */
+    int32_t propagation_spacing;       /* reliability_propagation.spacing (gap count)   5 */
+    double propagation_max_znssd;      /* reliability_propagation.max_znssd           0.5 */
+    int32_t is_subset_radius;          /* initialization.integer_search.subset_radius  10 */
+    int32_t is_search_radius;          /* initialization.integer_search.search_radius  30 */
+    int32_t sift_enabled;              /* initialization.integer_search.sift_enabled    0 */
+    int32_t pyramid_enabled;           /* ....pyramid_enabled                           1 */
+    int32_t pyramid_scale;             /* ....pyramid_scale                             4 */
+    int32_t pyramid_refinement_radius; /* ....pyramid_refinement_radius                 4 */
+    int32_t sp_enabled;                /* initialization.subpixel_refinement.enabled    1 */
+    int32_t sp_subset_radius;          /* ....subset_radius                            15 */
+    int32_t sp_max_iterations;         /* ....max_iterations                           30 */
+    int32_t precision;                 /* tdic_precision (GPU only)         FP32_MIXED */
+    double sp_convergence_threshold;   /* ....convergence_threshold                  1e-3 */
+    int32_t seed_count;                /* seed_selection.seed_count                   256 */
+    int32_t kmeans_iterations;         /* seed_selection.kmeans_iterations             20 */
+    double seed_max_znssd;             /* seed_selection.max_znssd                    0.2 */
+    double min_displacement_norm;      /* seed_selection.min_displacement_norm          0 */
+    double min_texture_std;            /* seed_selection.min_texture_std                0 */
+    int32_t kmeans_sample_limit;       /* seed_selection.kmeans_sample_limit        20000 */
+    int32_t propagation_mode;          /* 0 = frontier waves (GPU only)                 0 */
+} tdic_config;
+
+/* One POI for a batched solve: centre (rounded to the nearest pixel as icgn.cpp:472-473),
+ * initial guess u, v, du_dx, du_dy, dv_dx, dv_dy and initial.confidence. */
+typedef struct tdic_poi_in {
+    double x, y;
+    double p0[6];
+    double confidence;
+} tdic_poi_in;
+
+/* dic::Displacement2D (include/dic/core/result.hpp:32-51, first-order part) plus additive
+ * fields: zncc = clamp(1 - correlation / 2, -1, 1), iterations (loop bodies entered),
+ * converged (strict |dp| < threshold; the reference's `valid` is also true when the loop ran
+ * out with a finite correlation, icgn.cpp:620-625). */
+typedef struct tdic_poi_out {
+    double p[6];
+    double correlation;
+    double zncc;
+    int32_t iterations;
+    int8_t status;
+    int8_t valid;
+    int8_t converged;
+    int8_t pad_;
+} tdic_poi_out;
+
+/* The propagation seed (PropagationSeed, reliability_propagation.hpp:35-39). */
+typedef struct tdic_seed {
+    double x, y;
+    double p[6];
+    double correlation;
+    int32_t found;
+    int32_t pad_;
+} tdic_seed;
+
+/* Structure-of-arrays grid result, one entry per grid point i = gy * grid_w + gx
+ * (reliability_propagation.cpp:159-176); keys of results_to_dict (bind_subset.cpp:102-153)
+ * plus zncc / iterations / converged / status.  Any pointer may be NULL (not written). */
+typedef struct tdic_grid_out {
+    double* x; double* y; double* u; double* v;
+    double* du_dx; double* du_dy; double* dv_dx; double* dv_dy;
+    double* correlation; double* zncc;
+    uint8_t* valid; int8_t* status; int32_t* iterations; uint8_t* converged;
+} tdic_grid_out;
+
+typedef struct tdic_ctx tdic_ctx;
+typedef struct tdic_pair tdic_pair;
+
+/* Defaults of dic::SubsetConfig{} (subset_config.hpp:33-50). */
+void tdic_config_default(tdic_config* cfg);
+
+/* Output grid size: ceil(W / stride) x ceil(H / stride), stride = spacing + 1
+ * (reliability_propagation.cpp:154-160). */
+void tdic_grid_dims(int32_t width, int32_t height, int32_t spacing, int32_t* grid_w, int32_t* grid_h);
+
+/* Context: one device, one stream, a caching device-memory pool and per-radius sample tables.
+ * (No reference counterpart: the reference builds its state per call.) */
+tdic_status tdic_ctx_create(int32_t device, tdic_ctx** out);
+void tdic_ctx_destroy(tdic_ctx* ctx);
+const char* tdic_last_error(const tdic_ctx* ctx);
+/* Bytes the pool holds on the device (allocated, live + cached). */
+size_t tdic_ctx_device_bytes(const tdic_ctx* ctx);
+
+/* Image pair on the device: the reference image (float32, as dic::Image stores it,
+ * image.hpp:58-81) and the deformed image's B-spline coefficients of `degree` with `border`
+ * (BSplineImagePreprocessor::compute, bspline.cpp:270-300 / form_coefficients :369-392;
+ * exact_prefilter = 0 gives the clamp-padded, non-deconvolved coefficients of compute_lazy
+ * used by seed refinement, seed_selector.cpp:166-173).  `reference`/`deformed` are host or
+ * device pointers of `dtype` per `memory`, row-major H x W with row stride `pitch` elements
+ * (0 = width).  Runs kernels K1 (prefilter) and the image conversion; async on `stream`. */
+tdic_status tdic_pair_create(tdic_ctx* ctx, const void* reference, const void* deformed,
+                             int32_t width, int32_t height, int32_t pitch, tdic_dtype dtype,
+                             tdic_memory memory, int32_t degree, int32_t border,
+                             int32_t exact_prefilter, int32_t precision, void* stream,
+                             tdic_pair** out);
+/* Recompute an existing pair from new images of the same shape (no allocation). */
+tdic_status tdic_pair_update(tdic_pair* pair, const void* reference, const void* deformed,
+                             int32_t pitch, tdic_dtype dtype, tdic_memory memory, void* stream);
+void tdic_pair_destroy(tdic_pair* pair);
+/* Copy the coefficient image ((H+2B) x (W+2B), float32 or float64 per the pair's precision)
+ * into a host buffer of `bytes` bytes; for tests. */
+tdic_status tdic_pair_coefficients(tdic_pair* pair, void* host_out, size_t bytes);
+
+/* Reference-image gradients, kernel K2 (build_reference_gradient_cache,
+ * reliability_propagation.cpp:84-112): central differences on raw pixels, one-sided at the
+ * border.  gx/gy are host float64 arrays of H*W. */
+tdic_status tdic_reference_gradient(tdic_pair* pair, double* gx, double* gy);
+
+/* Batched per-POI solve: replaces SubsetSolver::solve_with_interpolators (subset_solver.hpp:
+ * 39-65 -> icgn.cpp:384-405 -> icgn.cpp:446-627, or forward_gauss_newton.cpp:188-399 when
+ * cfg->optimizer == 1) for n POIs at once.  in/out are host or device pointers per `memory`.
+ * Only first-order ZNSSD routes are on this path (others: TDIC_UNSUPPORTED). */
+tdic_status tdic_solve_pois(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cfg,
+                            const tdic_poi_in* in, int32_t n, tdic_poi_out* out,
+                            tdic_memory memory, void* stream);
+
+/* Propagation over the POI grid from one seed: replaces the heap loop of
+ * ReliabilityPropagation::propagate (reliability_propagation.cpp:130-394).  The grid
+ * geometry, seed alignment (:201-264), neighbour admission (:303-323), guess extrapolation
+ * (:326-329) and acceptance rule (:359-368) are the reference's; the visit order is the
+ * frontier-wave rule (every admissible neighbour of wave w's accepted set is solved in wave
+ * w+1 from the parent with the lowest ZNSSD, ties to the lowest parent index).
+ * roi: host uint8 H x W mask (NULL = all valid).  out: host or device arrays per `memory`
+ * of grid_w*grid_h entries.  *points_computed = accepted points including the seed (0 means
+ * the seed could not be placed: SubsetDIC::compute then returns the empty result). */
+tdic_status tdic_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cfg,
+                           const tdic_seed* seed, const uint8_t* roi, tdic_grid_out* out,
+                           tdic_memory memory, int32_t* points_computed, void* stream);
+
+/* Seed selection: SeedSelector::select_best_seed (seed_selector.cpp:146-205) with k-means
+ * candidates (:207-317), integer search (integer_search.cpp:333-432, kernel K5) and subpixel
+ * ICGN refinement on the non-prefiltered spline (subset_initializer.cpp:152-204).  `lazy` is
+ * a pair created with exact_prefilter = 0 over the same images; reference_host is the host
+ * float32 reference (texture statistics).  seed->found = 0 when no candidate passes. */
+tdic_status tdic_select_seed(tdic_ctx* ctx, tdic_pair* lazy, const float* reference_host,
+                             const uint8_t* roi, const tdic_config* cfg, tdic_seed* seed,
+                             void* stream);
+
+/* Whole pybind path: _traditional_dic.subset.compute (bind_subset.cpp:253-315) ->
+ * SubsetDIC::compute (subset_dic.cpp:39-105).  Host images of `dtype`, host roi (NULL = full
+ * image), host outputs of grid_w*grid_h entries.  *n_points = grid_w*grid_h, or 0 for the
+ * reference's empty result (no seed found, or nothing computed). */
+tdic_status tdic_subset_compute(tdic_ctx* ctx, const void* reference, const void* deformed,
+                                int32_t width, int32_t height, tdic_dtype dtype,
+                                const uint8_t* roi, const tdic_config* cfg, tdic_grid_out* out,
+                                int32_t* n_points, tdic_seed* seed_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TDIC_GB300_H */

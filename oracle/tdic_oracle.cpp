@@ -1,0 +1,1118 @@
+/*
+ * tdic_oracle.cpp -- FP64 CPU restatement of the Traditional-DIC 2D subset-DIC hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY (parity checker and CPU baseline); see tdic_oracle.h for what
+ * pins it.  Plain C++17, no Eigen.  Each function cites the reference file:line it follows.
+ * Two deliberate, documented differences in mechanism (not in result):
+ *   - the periodic deconvolution of bspline.cpp:191-244 (Eigen::FFT / kissfft) is computed
+ *     with the exact periodic recursive filter (poles of the sampled B-spline kernel, causal
+ *     and anti-causal passes with closed-form periodic initial values); both are the exact
+ *     inverse of the same circulant system, so they agree to rounding (~1e-13);
+ *   - the 6x6 LDLT of Eigen (icgn.cpp:538, forward_gauss_newton.cpp:355) is restated as
+ *     symmetric diagonal pivoting LDLT with the same success / positivity semantics.
+ * The "frontier" propagation mode is not a reference behaviour: it is the deterministic wave
+ * rule that the GPU path uses, restated here so the GPU can be checked mode-for-mode.
+ */
+#include "tdic_oracle.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <numeric>
+#include <queue>
+#include <vector>
+
+namespace {
+
+constexpr double kEps = 1e-12;  // icgn.cpp:13, forward_gauss_newton.cpp:11, integer_search.cpp:10
+constexpr double kInf = std::numeric_limits<double>::infinity();
+constexpr double kNaN = std::numeric_limits<double>::quiet_NaN();
+
+enum Status : int8_t { kSuccess = 0, kNotConverged = 1, kInvalidInput = 2, kNumericalFailure = 3 };
+
+int factorial(int n) { int v = 1; for (int i = 2; i <= n; ++i) v *= i; return v; }
+int combination(int n, int k) {
+    if (k < 0 || k > n) return 0;
+    return factorial(n) / (factorial(k) * factorial(n - k));
+}
+double plus_power(double x, int p) { return x > 0.0 ? std::pow(x, p) : 0.0; }  // bspline.cpp:68-71
+int clamp_index(int v, int lo, int hi) { return std::max(lo, std::min(v, hi)); }  // bspline.cpp:73-76
+int symmetric_index(int v, int size) {  // bspline.cpp:78-89
+    if (size <= 0) return 0;
+    const int period = 2 * size;
+    int w = v % period;
+    if (w < 0) w += period;
+    return w < size ? w : period - 1 - w;
+}
+
+double basis(double x, int r, int d) {  // bspline.cpp:342-367
+    if (r < 0 || r > d) return 0.0;
+    const int dfac = factorial(d) / factorial(d - r);
+    double sum = 0.0;
+    for (int k = 0; k <= d + 1; ++k) {
+        const double sign = k % 2 == 0 ? 1.0 : -1.0;
+        const double coef = sign * static_cast<double>(combination(d + 1, k));
+        const double shift = static_cast<double>(d + 1) / 2.0 - static_cast<double>(k);
+        sum += coef * static_cast<double>(dfac) * plus_power(x + shift, d - r);
+    }
+    return sum / static_cast<double>(factorial(d));
+}
+
+bool valid_degree(int d) { return d == 1 || d == 3 || d == 5; }
+
+void build_qk(int d, double* qk) {  // bspline.cpp:320-340
+    const int n = d + 1, off = d / 2;
+    for (int r = 0; r < n; ++r)
+        for (int c = 0; c < n; ++c) {
+            const double x = static_cast<double>(-off + c);
+            const double sign = r % 2 == 0 ? 1.0 : -1.0;
+            qk[r * n + c] = sign * basis(x, r, d) / static_cast<double>(factorial(r));
+        }
+}
+
+// ---------------------------------------------------------------------------------------
+// Exact periodic deconvolution by the sampled B-spline kernel (restates the result of
+// bspline.cpp:177-244).  Poles: cubic z = sqrt(3) - 2; quintic z = roots of
+// z^4 + 26 z^3 + 66 z^2 + 26 z + 1 with |z| < 1 (w = z + 1/z solves w^2 + 26 w + 64 = 0).
+// Gain prod (1 - z)^2 makes the DC response 1.
+// ---------------------------------------------------------------------------------------
+int spline_poles(int d, double* z) {
+    if (d == 3) { z[0] = std::sqrt(3.0) - 2.0; return 1; }
+    if (d == 5) {
+        const double s = std::sqrt(105.0);
+        const double w1 = -13.0 + s, w2 = -13.0 - s;
+        z[0] = 0.5 * (w1 + std::sqrt(w1 * w1 - 4.0));
+        z[1] = 0.5 * (w2 + std::sqrt(w2 * w2 - 4.0));
+        return 2;
+    }
+    return 0;
+}
+
+void deconvolve_periodic(double* s, int L, std::ptrdiff_t stride, int d, std::vector<double>& tmp) {
+    double z[2];
+    const int np = spline_poles(d, z);
+    if (np == 0) return;
+    tmp.resize(static_cast<std::size_t>(L));
+    double gain = 1.0;
+    for (int k = 0; k < np; ++k) gain *= (1.0 - z[k]) * (1.0 - z[k]);
+    for (int i = 0; i < L; ++i) tmp[i] = s[i * stride] * gain;
+    for (int k = 0; k < np; ++k) {
+        const double zk = z[k];
+        const double zl = std::pow(zk, L);
+        // causal: y[0] = sum_{j<L} z^j x[-j mod L] / (1 - z^L)
+        double acc = 0.0, zj = 1.0;
+        for (int j = 0; j < L; ++j) {
+            acc += zj * tmp[(L - j) % L];
+            zj *= zk;
+            if (std::fabs(zj) < 1e-300) break;
+        }
+        tmp[0] = acc / (1.0 - zl);
+        for (int i = 1; i < L; ++i) tmp[i] += zk * tmp[i - 1];
+        // anti-causal: c[L-1] = sum_{j<L} z^j y[(L-1+j) mod L] / (1 - z^L)
+        acc = 0.0; zj = 1.0;
+        for (int j = 0; j < L; ++j) {
+            acc += zj * tmp[(L - 1 + j) % L];
+            zj *= zk;
+            if (std::fabs(zj) < 1e-300) break;
+        }
+        tmp[L - 1] = acc / (1.0 - zl);
+        for (int i = L - 2; i >= 0; --i) tmp[i] += zk * tmp[i + 1];
+    }
+    for (int i = 0; i < L; ++i) s[i * stride] = tmp[i];
+}
+
+// ---------------------------------------------------------------------------------------
+// Interpolation through the local polynomial block qk * C * qk^T (bspline.cpp:153-175,
+// 418-424) evaluated as in evaluate_polynomial{,_dx,_dy} (bspline.cpp:96-151).
+// ---------------------------------------------------------------------------------------
+struct Spline {
+    const double* c = nullptr;
+    int w = 0, h = 0, d = 3, border = 3, cw = 0, ch = 0;
+    double qk[36];
+    void init(const double* coeffs, int w_, int h_, int d_, int b_) {
+        c = coeffs; w = w_; h = h_; d = d_; border = std::max(3, b_);
+        cw = w + 2 * border; ch = h + 2 * border;
+        build_qk(d, qk);
+    }
+    void block(int ix, int iy, double* out) const {  // bspline.cpp:153-175
+        const int n = d + 1, off = d / 2;
+        const int top = iy + border - off, left = ix + border - off;
+        double cb[36], t[36];
+        for (int r = 0; r < n; ++r) {
+            const int sy = clamp_index(top + r, 0, ch - 1);
+            for (int q = 0; q < n; ++q) cb[r * n + q] = c[static_cast<std::size_t>(sy) * cw + clamp_index(left + q, 0, cw - 1)];
+        }
+        for (int i = 0; i < n; ++i)  // t = qk * cb
+            for (int j = 0; j < n; ++j) {
+                double s = 0.0;
+                for (int k = 0; k < n; ++k) s += qk[i * n + k] * cb[k * n + j];
+                t[i * n + j] = s;
+            }
+        for (int i = 0; i < n; ++i)  // out = t * qk^T
+            for (int j = 0; j < n; ++j) {
+                double s = 0.0;
+                for (int k = 0; k < n; ++k) s += t[i * n + k] * qk[j * n + k];
+                out[i * n + j] = s;
+            }
+    }
+    void locate(double x, double y, int& ix, int& iy, double& dx, double& dy) const {  // bspline.cpp:465-468
+        ix = clamp_index(static_cast<int>(std::floor(x)), 0, w - 1);
+        iy = clamp_index(static_cast<int>(std::floor(y)), 0, h - 1);
+        dx = x - static_cast<double>(ix);
+        dy = y - static_cast<double>(iy);
+    }
+    double value(double x, double y) const {  // bspline.cpp:458-474, 96-113
+        int ix, iy; double dx, dy;
+        locate(x, y, ix, iy, dx, dy);
+        double b[36];
+        block(ix, iy, b);
+        const int n = d + 1;
+        double v = 0.0, yp = 1.0;
+        for (int r = 0; r < n; ++r) {
+            double xp = 1.0;
+            for (int q = 0; q < n; ++q) { v += b[r * n + q] * yp * xp; xp *= dx; }
+            yp *= dy;
+        }
+        return v;
+    }
+    void gradient(double x, double y, double& gx, double& gy) const {  // bspline.cpp:476-500, 115-151
+        int ix, iy; double dx, dy;
+        locate(x, y, ix, iy, dx, dy);
+        double b[36];
+        block(ix, iy, b);
+        const int n = d + 1;
+        double vx = 0.0, yp = 1.0;
+        for (int r = 0; r < n; ++r) {
+            double xp = 1.0;
+            for (int q = 1; q < n; ++q) { vx += static_cast<double>(q) * b[r * n + q] * yp * xp; xp *= dx; }
+            yp *= dy;
+        }
+        double vy = 0.0;
+        yp = 1.0;
+        for (int r = 1; r < n; ++r) {
+            double xp = 1.0;
+            for (int q = 0; q < n; ++q) { vy += static_cast<double>(r) * b[r * n + q] * yp * xp; xp *= dx; }
+            yp *= dy;
+        }
+        gx = vx; gy = vy;
+    }
+};
+
+void form_coefficients(const float* img, int w, int h, int d, int border, bool exact, double* out) {
+    // bspline.cpp:369-392
+    border = std::max(3, border);
+    const int cw = w + 2 * border, ch = h + 2 * border;
+    for (int y = 0; y < ch; ++y) {
+        const int sy = exact ? symmetric_index(y - border, h) : clamp_index(y - border, 0, h - 1);
+        for (int x = 0; x < cw; ++x) {
+            const int sx = exact ? symmetric_index(x - border, w) : clamp_index(x - border, 0, w - 1);
+            out[static_cast<std::size_t>(y) * cw + x] = static_cast<double>(img[static_cast<std::size_t>(sy) * w + sx]);
+        }
+    }
+    if (exact) {
+        std::vector<double> tmp;
+        for (int y = 0; y < ch; ++y) deconvolve_periodic(out + static_cast<std::size_t>(y) * cw, cw, 1, d, tmp);
+        for (int x = 0; x < cw; ++x) deconvolve_periodic(out + x, ch, cw, d, tmp);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// 6x6 LDLT with symmetric diagonal pivoting and sign tracking: restates the factorisation
+// semantics relied on by icgn.cpp:538-542 / forward_gauss_newton.cpp:354-358
+// (info() == Success, isPositive()) and the pseudo-inverse solve of D.
+// ---------------------------------------------------------------------------------------
+struct Ldlt6 {
+    double m[6][6];
+    int t[6];
+    enum { kZero, kPosSemi, kNegSemi, kIndef } sign = kZero;
+    bool ok = true;
+
+    void factor(const double a[6][6]) {
+        for (int i = 0; i < 6; ++i) for (int j = 0; j < 6; ++j) m[i][j] = a[i][j];
+        sign = kZero;
+        ok = true;
+        bool found_zero = false;
+        double temp[6];
+        for (int k = 0; k < 6; ++k) {
+            int big = k;
+            double bigv = std::fabs(m[k][k]);
+            for (int i = k + 1; i < 6; ++i) if (std::fabs(m[i][i]) > bigv) { bigv = std::fabs(m[i][i]); big = i; }
+            t[k] = big;
+            if (big != k) {
+                for (int j = 0; j < k; ++j) std::swap(m[k][j], m[big][j]);
+                for (int i = big + 1; i < 6; ++i) std::swap(m[i][k], m[i][big]);
+                std::swap(m[k][k], m[big][big]);
+                for (int i = k + 1; i < big; ++i) { const double tmp = m[i][k]; m[i][k] = m[big][i]; m[big][i] = tmp; }
+            }
+            if (k > 0) {
+                for (int j = 0; j < k; ++j) temp[j] = m[j][j] * m[k][j];
+                double s = 0.0;
+                for (int j = 0; j < k; ++j) s += m[k][j] * temp[j];
+                m[k][k] -= s;
+                for (int i = k + 1; i < 6; ++i) {
+                    double si = 0.0;
+                    for (int j = 0; j < k; ++j) si += m[i][j] * temp[j];
+                    m[i][k] -= si;
+                }
+            }
+            const double akk = m[k][k];
+            const bool pivot_valid = std::fabs(akk) > 0.0;
+            if (k == 0 && !pivot_valid) {
+                sign = kZero;
+                for (int j = 0; j < 6; ++j) { t[j] = j; for (int i = 0; i < 6; ++i) m[i][j] = 0.0; }
+                ok = true;
+                return;
+            }
+            if (pivot_valid) {
+                for (int i = k + 1; i < 6; ++i) m[i][k] /= akk;
+            } else {
+                for (int i = k + 1; i < 6; ++i) ok = ok && (m[i][k] == 0.0);
+            }
+            if (found_zero && pivot_valid) ok = false;
+            else if (!pivot_valid) found_zero = true;
+            if (sign == kPosSemi) { if (akk < 0.0) sign = kIndef; }
+            else if (sign == kNegSemi) { if (akk > 0.0) sign = kIndef; }
+            else if (sign == kZero) { if (akk > 0.0) sign = kPosSemi; else if (akk < 0.0) sign = kNegSemi; }
+        }
+    }
+    bool success() const { return ok; }
+    bool positive() const { return sign == kPosSemi || sign == kZero; }
+    void solve(const double b[6], double x[6]) const {
+        for (int i = 0; i < 6; ++i) x[i] = b[i];
+        for (int k = 0; k < 6; ++k) std::swap(x[k], x[t[k]]);
+        for (int i = 0; i < 6; ++i) { double s = x[i]; for (int j = 0; j < i; ++j) s -= m[i][j] * x[j]; x[i] = s; }
+        for (int i = 0; i < 6; ++i) { const double dd = m[i][i]; x[i] = std::fabs(dd) > DBL_MIN ? x[i] / dd : 0.0; }
+        for (int i = 5; i >= 0; --i) { double s = x[i]; for (int j = i + 1; j < 6; ++j) s -= m[j][i] * x[j]; x[i] = s; }
+        for (int k = 5; k >= 0; --k) std::swap(x[k], x[t[k]]);
+    }
+};
+
+bool finite6(const double* p) { for (int i = 0; i < 6; ++i) if (!std::isfinite(p[i])) return false; return true; }
+
+// icgn.cpp:83-120
+void ic_update(const double* p, const double* dp, double* out) {
+    const double du = p[0], dv = p[1], dudx = p[2], dudy = p[3], dvdx = p[4], dvdy = p[5];
+    const double dp0 = dp[0], dp1 = dp[1], dp2 = dp[2], dp3 = dp[3], dp4 = dp[4], dp5 = dp[5];
+    const double den = dp2 + dp5 + dp2 * dp5 - dp3 * dp4 + 1.0;
+    if (std::fabs(den) <= kEps) { for (int i = 0; i < 6; ++i) out[i] = kNaN; return; }
+    out[0] = du - ((dudx + 1.0) * (dp0 + dp0 * dp5 - dp1 * dp3)) / den - (dudy * (dp1 - dp0 * dp4 + dp1 * dp2)) / den;
+    out[1] = dv - ((dvdy + 1.0) * (dp1 - dp0 * dp4 + dp1 * dp2)) / den - (dvdx * (dp0 + dp0 * dp5 - dp1 * dp3)) / den;
+    out[2] = ((dp5 + 1.0) * (dudx + 1.0)) / den - (dp4 * dudy) / den - 1.0;
+    out[3] = (dudy * (dp2 + 1.0)) / den - (dp3 * (dudx + 1.0)) / den;
+    out[4] = (dvdx * (dp5 + 1.0)) / den - (dp4 * (dvdy + 1.0)) / den;
+    out[5] = ((dp2 + 1.0) * (dvdy + 1.0)) / den - (dp3 * dvdx) / den - 1.0;
+}
+
+// forward_gauss_newton.cpp:64-76
+void compose_warp(const double* p, const double* dp, double* pn) {
+    pn[0] = dp[0] + p[0] + p[2] * dp[0] + p[3] * dp[1];
+    pn[1] = dp[1] + p[1] + p[4] * dp[0] + p[5] * dp[1];
+    pn[2] = dp[2] + p[2] * (1.0 + dp[2]) + p[3] * dp[4];
+    pn[3] = dp[3] + p[2] * dp[3] + p[3] * (1.0 + dp[5]);
+    pn[4] = dp[4] + p[4] * (1.0 + dp[2]) + p[5] * dp[4];
+    pn[5] = dp[5] + p[4] * dp[3] + p[5] * (1.0 + dp[5]);
+}
+
+struct GradSource {  // reference_gradient_at, icgn.cpp:55-71 / central difference icgn.cpp:42-53
+    const float* img; int w, h;
+    const double* gx; const double* gy;
+    void at(int x, int y, double& ox, double& oy) const {
+        if (gx && gy) { ox = gx[static_cast<std::size_t>(y) * w + x]; oy = gy[static_cast<std::size_t>(y) * w + x]; return; }
+        const int xm = std::max(0, x - 1), xp = std::min(w - 1, x + 1);
+        const int ym = std::max(0, y - 1), yp = std::min(h - 1, y + 1);
+        ox = (static_cast<double>(img[static_cast<std::size_t>(y) * w + xp]) - static_cast<double>(img[static_cast<std::size_t>(y) * w + xm])) / static_cast<double>(std::max(1, xp - xm));
+        oy = (static_cast<double>(img[static_cast<std::size_t>(yp) * w + x]) - static_cast<double>(img[static_cast<std::size_t>(ym) * w + x])) / static_cast<double>(std::max(1, yp - ym));
+    }
+};
+
+struct SolverCfg { int radius; int max_iter; double thr; int optimizer; };
+
+void init_result(orc_poi_result& r, const double* p0, double conf) {
+    // icgn.cpp:454-462: u, v from the initial guess, gradients default to zero.
+    for (int i = 0; i < 6; ++i) r.p[i] = 0.0;
+    r.p[0] = p0[0]; r.p[1] = p0[1];
+    r.correlation = conf;
+    r.iterations = 0; r.status = kInvalidInput; r.valid = 0; r.converged = 0; r.pad_ = 0;
+}
+
+struct Sample { double lx, ly, ref, refn, sd[6]; };
+
+// icgn.cpp:446-627
+orc_poi_result solve_icgn(const float* ref, int w, int h, const GradSource& gs, const Spline& sp,
+                          const SolverCfg& cfg, double px, double py, const double* p0, double conf) {
+    orc_poi_result res;
+    init_result(res, p0, conf);
+    if (w <= 0 || h <= 0 || cfg.radius < 1 || cfg.max_iter < 0) return res;
+    const int cx = static_cast<int>(std::round(px)), cy = static_cast<int>(std::round(py));
+    const int r = cfg.radius;
+    if (cx - r < 0 || cy - r < 0 || cx + r >= w || cy + r >= h) return res;
+    std::vector<Sample> s;
+    s.reserve(static_cast<std::size_t>((2 * r + 1) * (2 * r + 1)));
+    double mean = 0.0;
+    for (int dy = -r; dy <= r; ++dy)
+        for (int dx = -r; dx <= r; ++dx) {
+            if (dx * dx + dy * dy > r * r) continue;
+            Sample q;
+            q.lx = dx; q.ly = dy;
+            q.ref = static_cast<double>(ref[static_cast<std::size_t>(cy + dy) * w + cx + dx]);
+            double gx, gy;
+            gs.at(cx + dx, cy + dy, gx, gy);
+            q.sd[0] = gx; q.sd[1] = gy; q.sd[2] = gx * q.lx; q.sd[3] = gx * q.ly; q.sd[4] = gy * q.lx; q.sd[5] = gy * q.ly;
+            mean += q.ref;
+            s.push_back(q);
+        }
+    if (s.size() < 6) return res;
+    const double N = static_cast<double>(s.size());
+    mean /= N;
+    double norm = 0.0;
+    for (const auto& q : s) { const double df = q.ref - mean; norm += df * df; }
+    norm = std::sqrt(norm);
+    if (norm <= kEps) { res.status = kNumericalFailure; return res; }
+    for (auto& q : s) q.refn = (q.ref - mean) / norm;
+    double H[6][6] = {};
+    for (const auto& q : s) for (int i = 0; i < 6; ++i) for (int j = 0; j < 6; ++j) H[i][j] += q.sd[i] * q.sd[j];
+    const double hs = 2.0 / (norm * norm);
+    for (int i = 0; i < 6; ++i) for (int j = 0; j < 6; ++j) H[i][j] *= hs;
+    Ldlt6 f;
+    f.factor(H);
+    if (!f.success() || !f.positive()) { res.status = kNumericalFailure; return res; }
+    double p[6];
+    for (int i = 0; i < 6; ++i) p[i] = p0[i];
+    double corr = kInf;
+    bool converged = false;
+    std::vector<double> g(s.size());
+    int it = 0;
+    for (; it < cfg.max_iter; ++it) {
+        res.iterations = it + 1;
+        double gm = 0.0;
+        for (std::size_t i = 0; i < s.size(); ++i) {
+            const double wx = static_cast<double>(cx) + s[i].lx + p[0] + p[2] * s[i].lx + p[3] * s[i].ly;
+            const double wy = static_cast<double>(cy) + s[i].ly + p[1] + p[4] * s[i].lx + p[5] * s[i].ly;
+            if (!(wx >= 0.0 && wy >= 0.0 && wx <= static_cast<double>(w - 1) && wy <= static_cast<double>(h - 1))) {
+                res.status = kInvalidInput;
+                return res;
+            }
+            g[i] = sp.value(wx, wy);
+            gm += g[i];
+        }
+        gm /= N;
+        double gn = 0.0;
+        for (double v : g) { const double df = v - gm; gn += df * df; }
+        gn = std::sqrt(gn);
+        if (gn <= kEps) { res.status = kNumericalFailure; return res; }
+        double grad[6] = {0, 0, 0, 0, 0, 0};
+        corr = 0.0;
+        for (std::size_t i = 0; i < s.size(); ++i) {
+            const double nd = s[i].refn - (g[i] - gm) / gn;
+            for (int k = 0; k < 6; ++k) grad[k] += nd * s[i].sd[k];
+            corr += nd * nd;
+        }
+        for (int k = 0; k < 6; ++k) grad[k] *= 2.0 / norm;
+        double dp[6];
+        f.solve(grad, dp);
+        for (int k = 0; k < 6; ++k) dp[k] = -dp[k];
+        if (!finite6(dp)) { res.status = kNumericalFailure; return res; }
+        double dn = 0.0;
+        for (int k = 0; k < 6; ++k) dn += dp[k] * dp[k];
+        dn = std::sqrt(dn);
+        double pn[6];
+        ic_update(p, dp, pn);
+        for (int k = 0; k < 6; ++k) p[k] = pn[k];
+        if (!finite6(p)) { res.status = kNumericalFailure; return res; }
+        if (dn < cfg.thr) { converged = true; break; }
+    }
+    for (int k = 0; k < 6; ++k) res.p[k] = p[k];
+    res.correlation = corr;
+    res.converged = converged ? 1 : 0;
+    if (!converged && std::isfinite(corr)) converged = true;
+    res.status = converged ? kSuccess : kNotConverged;
+    res.valid = converged ? 1 : 0;
+    return res;
+}
+
+// forward_gauss_newton.cpp:188-399 (sd: 44-60, compose: 64-76)
+orc_poi_result solve_fgn(const float* ref, int w, int h, const Spline& sp, const SolverCfg& cfg,
+                         double px, double py, const double* p0, double conf) {
+    orc_poi_result res;
+    init_result(res, p0, conf);
+    if (w <= 0 || h <= 0 || cfg.radius < 1 || cfg.max_iter < 0) return res;
+    const int cx = static_cast<int>(std::round(px)), cy = static_cast<int>(std::round(py));
+    const int r = cfg.radius;
+    if (cx - r < 0 || cy - r < 0 || cx + r >= w || cy + r >= h) return res;
+    std::vector<Sample> s;
+    double mean = 0.0;
+    for (int dy = -r; dy <= r; ++dy)
+        for (int dx = -r; dx <= r; ++dx) {
+            if (dx * dx + dy * dy > r * r) continue;
+            Sample q;
+            q.lx = dx; q.ly = dy;
+            q.ref = static_cast<double>(ref[static_cast<std::size_t>(cy + dy) * w + cx + dx]);
+            mean += q.ref;
+            s.push_back(q);
+        }
+    if (s.size() < 6) return res;
+    const double N = static_cast<double>(s.size());
+    mean /= N;
+    double norm = 0.0;
+    for (const auto& q : s) { const double df = q.ref - mean; norm += df * df; }
+    norm = std::sqrt(norm);
+    if (norm <= kEps) { res.status = kNumericalFailure; return res; }
+    for (auto& q : s) q.refn = (q.ref - mean) / norm;
+    double p[6];
+    for (int i = 0; i < 6; ++i) p[i] = p0[i];
+    double corr = kInf;
+    bool converged = false;
+    std::vector<double> g(s.size());
+    for (int it = 0; it < cfg.max_iter; ++it) {
+        res.iterations = it + 1;
+        double gm = 0.0;
+        for (std::size_t i = 0; i < s.size(); ++i) {
+            const double wx = static_cast<double>(cx) + s[i].lx + p[0] + p[2] * s[i].lx + p[3] * s[i].ly;
+            const double wy = static_cast<double>(cy) + s[i].ly + p[1] + p[4] * s[i].lx + p[5] * s[i].ly;
+            if (!(wx >= 0.0 && wy >= 0.0 && wx <= static_cast<double>(w - 1) && wy <= static_cast<double>(h - 1))) {
+                res.status = kInvalidInput;
+                return res;
+            }
+            g[i] = sp.value(wx, wy);
+            gm += g[i];
+        }
+        gm /= N;
+        double gn = 0.0;
+        for (double v : g) { const double df = v - gm; gn += df * df; }
+        gn = std::sqrt(gn);
+        if (gn <= kEps) { res.status = kNumericalFailure; return res; }
+        double H[6][6] = {};
+        double grad[6] = {0, 0, 0, 0, 0, 0};
+        corr = 0.0;
+        for (std::size_t i = 0; i < s.size(); ++i) {
+            const double wx = static_cast<double>(cx) + s[i].lx + p[0] + p[2] * s[i].lx + p[3] * s[i].ly;
+            const double wy = static_cast<double>(cy) + s[i].ly + p[1] + p[4] * s[i].lx + p[5] * s[i].ly;
+            double gx, gy;
+            sp.gradient(wx, wy, gx, gy);
+            const double gxe = gx * (1.0 + p[2]) + gy * p[4];
+            const double gye = gx * p[3] + gy * (1.0 + p[5]);
+            const double sd[6] = {gxe, gye, gxe * s[i].lx, gxe * s[i].ly, gye * s[i].lx, gye * s[i].ly};
+            const double nd = s[i].refn - (g[i] - gm) / gn;
+            for (int a = 0; a < 6; ++a) { for (int b = 0; b < 6; ++b) H[a][b] += sd[a] * sd[b]; grad[a] += nd * sd[a]; }
+            corr += nd * nd;
+        }
+        const double hs = 2.0 / (norm * norm);
+        for (int a = 0; a < 6; ++a) for (int b = 0; b < 6; ++b) H[a][b] *= hs;
+        for (int a = 0; a < 6; ++a) grad[a] *= 2.0 / norm;
+        Ldlt6 f;
+        f.factor(H);
+        if (!f.success() || !f.positive()) { res.status = kNumericalFailure; return res; }
+        double dp[6];
+        f.solve(grad, dp);
+        if (!finite6(dp)) { res.status = kNumericalFailure; return res; }
+        double dn = 0.0;
+        for (int k = 0; k < 6; ++k) dn += dp[k] * dp[k];
+        dn = std::sqrt(dn);
+        if (dn > 0.5) {  // forward_gauss_newton.cpp:367-371
+            for (int k = 0; k < 6; ++k) dp[k] *= 0.5 / dn;
+            dn = 0.5;
+        }
+        double pn[6];
+        compose_warp(p, dp, pn);
+        for (int k = 0; k < 6; ++k) p[k] = pn[k];
+        if (!finite6(p)) { res.status = kNumericalFailure; return res; }
+        if (dn < cfg.thr) { converged = true; break; }
+    }
+    for (int k = 0; k < 6; ++k) res.p[k] = p[k];
+    res.correlation = corr;
+    res.converged = converged ? 1 : 0;
+    if (!converged && std::isfinite(corr)) converged = true;
+    res.status = converged ? kSuccess : kNotConverged;
+    res.valid = converged ? 1 : 0;
+    return res;
+}
+
+orc_poi_result solve_one(const float* ref, int w, int h, const GradSource& gs, const Spline& sp,
+                         const SolverCfg& cfg, double px, double py, const double* p0, double conf) {
+    if (cfg.optimizer == 1) return solve_fgn(ref, w, h, sp, cfg, px, py, p0, conf);
+    return solve_icgn(ref, w, h, gs, sp, cfg, px, py, p0, conf);
+}
+
+bool all_finite7(const orc_poi_result& r) {  // reliability_propagation.cpp:67-75
+    return finite6(r.p) && std::isfinite(r.correlation);
+}
+
+struct QueueItem {  // reliability_propagation.cpp:44-53
+    double corrcoef;
+    int gx, gy;
+    double p[6];
+    bool operator<(const QueueItem& o) const { return corrcoef > o.corrcoef; }
+};
+
+void clear_grid(orc_grid_out* out, int gw, int gh, int step) {
+    const int n = gw * gh;
+    for (int i = 0; i < n; ++i) {
+        out->x[i] = static_cast<double>((i % gw) * step);
+        out->y[i] = static_cast<double>((i / gw) * step);
+        out->u[i] = out->v[i] = out->du_dx[i] = out->du_dy[i] = out->dv_dx[i] = out->dv_dy[i] = 0.0;
+        out->correlation[i] = 0.0;
+        out->valid[i] = 0;
+        out->status[i] = kInvalidInput;
+        out->iterations[i] = 0;
+        out->converged[i] = 0;
+    }
+}
+
+void store(orc_grid_out* out, int idx, const orc_poi_result& r) {
+    out->u[idx] = r.p[0]; out->v[idx] = r.p[1];
+    out->du_dx[idx] = r.p[2]; out->du_dy[idx] = r.p[3]; out->dv_dx[idx] = r.p[4]; out->dv_dy[idx] = r.p[5];
+    out->correlation[idx] = r.correlation;
+    out->valid[idx] = r.valid;
+    out->status[idx] = r.status;
+    out->iterations[idx] = r.iterations;
+    out->converged[idx] = r.converged;
+}
+
+bool roi_valid(const uint8_t* roi, int w, int h, int x, int y) {
+    if (x < 0 || y < 0 || x >= w || y >= h) return false;
+    return roi == nullptr || roi[static_cast<std::size_t>(y) * w + x] != 0;
+}
+
+int nearest_grid_index(int c, int step, int limit) {  // reliability_propagation.cpp:77-82
+    const int idx = static_cast<int>(std::llround(static_cast<double>(c) / static_cast<double>(step)));
+    return std::clamp(idx, 0, limit - 1);
+}
+
+float corr_key(double c) { return static_cast<float>(c); }
+
+// reliability_propagation.cpp:130-394 (mode 1, heap order) and the frontier-wave rule (mode 0).
+int propagate(const float* ref, int w, int h, const uint8_t* roi, const GradSource& gs, const Spline& sp,
+              const orc_config& c, const orc_seed& seed, int max_solves, orc_grid_out* out, int* solves_done) {
+    int solves = 0;
+    if (solves_done) *solves_done = 0;
+    const int spacing = std::max(0, c.propagation_spacing);
+    if (w <= 0 || h <= 0 || c.subset_radius < 1) return 0;
+    const int step = spacing + 1;
+    const int gw = (w + step - 1) / step, gh = (h + step - 1) / step;
+    clear_grid(out, gw, gh, step);
+    const int radius = c.subset_radius;
+    const SolverCfg scfg{c.subset_radius, c.max_iterations, c.convergence_threshold, c.optimizer};
+    std::vector<uint8_t> calc(static_cast<std::size_t>(gw) * gh, 0);
+    const double cutoff_corr = c.propagation_max_znssd, cutoff_disp = static_cast<double>(step);
+    int computed = 0;
+
+    const int sxr = static_cast<int>(std::round(seed.x)), syr = static_cast<int>(std::round(seed.y));
+    if (sxr < 0 || syr < 0 || sxr >= w || syr >= h) return 0;
+    if (!roi_valid(roi, w, h, sxr, syr)) return 0;
+    const int gxs = nearest_grid_index(sxr, step, gw), gys = nearest_grid_index(syr, step, gh);
+    const int sx = gxs * step, sy = gys * step;
+    if (sx < 0 || sy < 0 || sx >= w || sy >= h) return 0;
+    if (!roi_valid(roi, w, h, sx, sy)) return 0;
+    const int sidx = gys * gw + gxs;
+    orc_poi_result aligned;
+    for (int k = 0; k < 6; ++k) aligned.p[k] = seed.p[k];
+    aligned.correlation = seed.correlation;
+    aligned.iterations = 0; aligned.status = kSuccess; aligned.valid = 1; aligned.converged = 0;
+    if (sx != sxr || sy != syr) {
+        aligned = solve_one(ref, w, h, gs, sp, scfg, sx, sy, seed.p, seed.correlation);
+        ++solves;
+        if (!aligned.valid || aligned.status != kSuccess || !all_finite7(aligned)) { if (solves_done) *solves_done = solves; return 0; }
+    }
+    calc[sidx] = 1;
+    store(out, sidx, aligned);
+    out->valid[sidx] = 1;
+    out->status[sidx] = kSuccess;
+    ++computed;
+
+    auto try_neighbor = [&](int popx, int popy, int n, int& nx, int& ny, int& nidx) -> bool {
+        const int offs[4][2] = {{0, -step}, {step, 0}, {0, step}, {-step, 0}};  // up, right, down, left
+        nx = popx + offs[n][0]; ny = popy + offs[n][1];
+        if (nx < 0 || ny < 0 || nx >= w || ny >= h) return false;
+        const int gnx = nx / step, gny = ny / step;
+        if (gnx < 0 || gny < 0 || gnx >= gw || gny >= gh) return false;
+        nidx = gny * gw + gnx;
+        if (calc[nidx]) return false;
+        if (!roi_valid(roi, w, h, nx, ny)) { calc[nidx] = 1; return false; }
+        if (nx - radius < 0 || ny - radius < 0 || nx + radius >= w || ny + radius >= h) { calc[nidx] = 1; return false; }
+        return true;
+    };
+    auto accept = [&](const orc_poi_result& r, double iu, double iv) {  // :359-368
+        return r.valid && r.status == kSuccess && r.correlation < cutoff_corr &&
+               std::fabs(iu - r.p[0]) < cutoff_disp && std::fabs(iv - r.p[1]) < cutoff_disp && all_finite7(r);
+    };
+
+    if (c.propagation_mode == 1) {
+        std::priority_queue<QueueItem> q;
+        QueueItem si;
+        si.corrcoef = std::max(0.0, aligned.correlation);
+        si.gx = gxs; si.gy = gys;
+        for (int k = 0; k < 6; ++k) si.p[k] = aligned.p[k];
+        q.push(si);
+        while (!q.empty()) {
+            const QueueItem it = q.top();
+            q.pop();
+            const int popx = it.gx * step, popy = it.gy * step;
+            for (int n = 0; n < 4; ++n) {
+                if (max_solves >= 0 && solves >= max_solves) { if (solves_done) *solves_done = solves; return computed; }
+                int nx, ny, nidx;
+                if (!try_neighbor(popx, popy, n, nx, ny, nidx)) continue;
+                const double ddx = nx - popx, ddy = ny - popy;
+                double p0[6];
+                p0[0] = it.p[0] + it.p[2] * ddx + it.p[3] * ddy;
+                p0[1] = it.p[1] + it.p[4] * ddx + it.p[5] * ddy;
+                p0[2] = it.p[2]; p0[3] = it.p[3]; p0[4] = it.p[4]; p0[5] = it.p[5];
+                const orc_poi_result r = solve_one(ref, w, h, gs, sp, scfg, nx, ny, p0, 0.0);
+                ++solves;
+                calc[nidx] = 1;
+                if (accept(r, p0[0], p0[1])) {
+                    store(out, nidx, r);
+                    ++computed;
+                    QueueItem nxt;
+                    nxt.corrcoef = r.correlation;
+                    nxt.gx = nx / step; nxt.gy = ny / step;
+                    for (int k = 0; k < 6; ++k) nxt.p[k] = r.p[k];
+                    q.push(nxt);
+                }
+            }
+        }
+    } else {
+        // Frontier waves: every unclaimed, admissible 4-neighbour of the wave-w accepted set
+        // is solved in wave w+1 from the parent with the lowest (float) ZNSSD, ties to the
+        // lowest parent grid index.
+        std::vector<int> frontier{sidx};
+        std::vector<double> fcorr{std::max(0.0, aligned.correlation)};
+        std::vector<int> best_parent(static_cast<std::size_t>(gw) * gh, -1);
+        std::vector<float> best_key(static_cast<std::size_t>(gw) * gh, 0.0f);
+        std::vector<double> pp(static_cast<std::size_t>(gw) * gh * 6, 0.0);
+        for (int k = 0; k < 6; ++k) pp[static_cast<std::size_t>(sidx) * 6 + k] = aligned.p[k];
+        while (!frontier.empty()) {
+            std::vector<int> next;
+            for (std::size_t fi = 0; fi < frontier.size(); ++fi) {
+                const int pidx = frontier[fi];
+                const int popx = (pidx % gw) * step, popy = (pidx / gw) * step;
+                const float key = corr_key(fcorr[fi]);
+                for (int n = 0; n < 4; ++n) {
+                    int nx, ny, nidx;
+                    const int offs[4][2] = {{0, -step}, {step, 0}, {0, step}, {-step, 0}};
+                    nx = popx + offs[n][0]; ny = popy + offs[n][1];
+                    if (nx < 0 || ny < 0 || nx >= w || ny >= h) continue;
+                    nidx = (ny / step) * gw + nx / step;
+                    if (best_parent[nidx] >= 0) {  // already a candidate of this wave
+                        if (key < best_key[nidx] || (key == best_key[nidx] && pidx < best_parent[nidx])) {
+                            best_key[nidx] = key; best_parent[nidx] = pidx;
+                        }
+                        continue;
+                    }
+                    if (!try_neighbor(popx, popy, n, nx, ny, nidx)) continue;
+                    best_parent[nidx] = pidx; best_key[nidx] = key;
+                    next.push_back(nidx);
+                }
+            }
+            std::vector<int> acc;
+            std::vector<double> acorr;
+            for (int nidx : next) {
+                calc[nidx] = 1;
+                if (max_solves >= 0 && solves >= max_solves) continue;
+                const int pidx = best_parent[nidx];
+                const double* pp0 = &pp[static_cast<std::size_t>(pidx) * 6];
+                const int nx = (nidx % gw) * step, ny = (nidx / gw) * step;
+                const double ddx = nx - (pidx % gw) * step, ddy = ny - (pidx / gw) * step;
+                double p0[6];
+                p0[0] = pp0[0] + pp0[2] * ddx + pp0[3] * ddy;
+                p0[1] = pp0[1] + pp0[4] * ddx + pp0[5] * ddy;
+                p0[2] = pp0[2]; p0[3] = pp0[3]; p0[4] = pp0[4]; p0[5] = pp0[5];
+                const orc_poi_result r = solve_one(ref, w, h, gs, sp, scfg, nx, ny, p0, 0.0);
+                ++solves;
+                if (accept(r, p0[0], p0[1])) {
+                    store(out, nidx, r);
+                    ++computed;
+                    for (int k = 0; k < 6; ++k) pp[static_cast<std::size_t>(nidx) * 6 + k] = r.p[k];
+                    acc.push_back(nidx);
+                    acorr.push_back(r.correlation);
+                }
+            }
+            for (int nidx : next) best_parent[nidx] = -2;  // resolved; never a candidate again
+            frontier.swap(acc);
+            fcorr.swap(acorr);
+        }
+    }
+    if (solves_done) *solves_done = solves;
+    return computed;
+}
+
+// ---------------------------------------------------------------------------------------
+// Integer search (integer_search.cpp:129-280, 333-432).
+// ---------------------------------------------------------------------------------------
+struct ISample { int dx, dy; double v; };
+struct Cand { int u = 0, v = 0; double zncc = -kInf; };
+
+std::vector<ISample> circ_samples(const float* ref, int w, int cx, int cy, int r, int step) {  // :60-80
+    step = std::max(1, step);
+    std::vector<ISample> s;
+    for (int dy = -r; dy <= r; dy += step)
+        for (int dx = -r; dx <= r; dx += step) {
+            if (dx * dx + dy * dy > r * r) continue;
+            s.push_back({dx, dy, static_cast<double>(ref[static_cast<std::size_t>(cy + dy) * w + cx + dx])});
+        }
+    return s;
+}
+double s_mean(const std::vector<ISample>& s) { double m = 0; for (auto& q : s) m += q.v; return s.empty() ? 0.0 : m / static_cast<double>(s.size()); }
+double s_norm(const std::vector<ISample>& s, double m) { double n = 0; for (auto& q : s) { const double d = q.v - m; n += d * d; } return n; }
+
+double circ_zncc(const float* def, int w, int h, const std::vector<ISample>& s, double rm, double rn, int cx, int cy, int u, int v) {  // :129-166
+    if (s.empty() || rn <= kEps) return -kInf;
+    double dm = 0.0;
+    for (auto& q : s) {
+        const int x = cx + u + q.dx, y = cy + v + q.dy;
+        if (x < 0 || y < 0 || x >= w || y >= h) return -kInf;
+        dm += static_cast<double>(def[static_cast<std::size_t>(y) * w + x]);
+    }
+    dm /= static_cast<double>(s.size());
+    double num = 0.0, dn = 0.0;
+    for (auto& q : s) {
+        const double rd = q.v - rm;
+        const double dd = static_cast<double>(def[static_cast<std::size_t>(cy + v + q.dy) * w + cx + u + q.dx]) - dm;
+        num += rd * dd;
+        dn += dd * dd;
+    }
+    if (dn <= kEps) return -kInf;
+    return num / std::sqrt(rn * dn);
+}
+
+Cand search_disp(const float* def, int w, int h, const std::vector<ISample>& s, double rm, double rn,
+                 int cx, int cy, int r, int minu, int maxu, int minv, int maxv, int step) {  // :168-206
+    Cand best;
+    step = std::max(1, step);
+    for (int v = minv; v <= maxv; v += step)
+        for (int u = minu; u <= maxu; u += step) {
+            const int x = cx + u, y = cy + v;
+            if (!(x - r >= 0 && y - r >= 0 && x + r < w && y + r < h)) continue;
+            const double z = circ_zncc(def, w, h, s, rm, rn, cx, cy, u, v);
+            if (z > best.zncc) { best.u = u; best.v = v; best.zncc = z; }
+        }
+    return best;
+}
+
+bool integer_search(const float* ref, const float* def, int w, int h, const orc_config& c,
+                    double px, double py, double& ou, double& ov, double& oz) {
+    const int cx = static_cast<int>(std::round(px)), cy = static_cast<int>(std::round(py));
+    const int r = std::max(1, c.is_subset_radius);
+    if (!(cx - r >= 0 && cy - r >= 0 && cx + r < w && cy + r < h)) return false;
+    const auto s = circ_samples(ref, w, cx, cy, r, 1);
+    const double rm = s_mean(s), rn = s_norm(s, rm);
+    if (s.empty() || rn <= kEps) return false;
+    const int search = std::max(0, c.is_search_radius);
+    const int cstep = c.pyramid_enabled ? std::max(1, std::max(1, c.pyramid_scale)) : 1;
+    const auto cs = circ_samples(ref, w, cx, cy, r, cstep);
+    const double crm = s_mean(cs), crn = s_norm(cs, crm);
+    Cand best;
+    if (!cs.empty() && crn > kEps) {  // search_ncorr_multigrid :208-265
+        const int minu = r - cx, maxu = w - 1 - r - cx, minv = r - cy, maxv = h - 1 - r - cy;
+        if (!(minu > maxu || minv > maxv)) {
+            const Cand coarse = search_disp(def, w, h, cs, crm, crn, cx, cy, r, minu, maxu, minv, maxv, cstep);
+            if (!std::isfinite(coarse.zncc)) {
+                best = coarse;
+            } else {
+                const int rr = std::max(std::max(std::max(1, c.pyramid_refinement_radius),
+                                                 static_cast<int>(std::ceil(1.5 * static_cast<double>(r)))), cstep);
+                best = search_disp(def, w, h, s, rm, rn, cx, cy, r,
+                                   std::max(minu, coarse.u - rr), std::min(maxu, coarse.u + rr),
+                                   std::max(minv, coarse.v - rr), std::min(maxv, coarse.v + rr), 1);
+            }
+        }
+    }
+    if (search > 0) {
+        const Cand local = search_disp(def, w, h, s, rm, rn, cx, cy, r, -search, search, -search, search, 1);
+        // prefer_local_when_ambiguous :267-280
+        if (!std::isfinite(local.zncc)) { /* keep global */ }
+        else if (!std::isfinite(best.zncc)) best = local;
+        else if (local.zncc + 0.02 >= best.zncc) best = local;
+    }
+    if (!std::isfinite(best.zncc)) return false;
+    ou = best.u; ov = best.v; oz = best.zncc;
+    return true;
+}
+
+double znssd_from_zncc(double z) {  // integer_search.cpp:25-31
+    if (!std::isfinite(z)) return kInf;
+    return std::max(0.0, 2.0 * (1.0 - std::max(-1.0, std::min(1.0, z))));
+}
+
+// ---------------------------------------------------------------------------------------
+// Seed selection (seed_selector.cpp:146-317, 388-539) with sift disabled and
+// truncate_roi_subsets false (pybind never sets it).
+// ---------------------------------------------------------------------------------------
+struct SeedEval { double x = 0, y = 0; double p[6] = {}; double corr = 0, quality = 0, norm = 0; bool valid = false; bool passed = false; };
+
+double texture_std(const float* ref, int w, int h, int r, int x, int y) {  // :424-452
+    if (x - r < 0 || y - r < 0 || x + r >= w || y + r >= h) return 0.0;
+    double sum = 0.0, sq = 0.0;
+    int cnt = 0;
+    for (int yy = y - r; yy <= y + r; ++yy)
+        for (int xx = x - r; xx <= x + r; ++xx) {
+            const double v = static_cast<double>(ref[static_cast<std::size_t>(yy) * w + xx]);
+            sum += v; sq += v * v; ++cnt;
+        }
+    if (cnt == 0) return 0.0;
+    const double m = sum / cnt;
+    return std::sqrt(std::max(0.0, sq / cnt - m * m));
+}
+
+struct Pt { int x, y; };
+
+std::vector<Pt> det_sample(const std::vector<Pt>& pts, int limit) {  // :33-47
+    if (limit <= 0 || static_cast<int>(pts.size()) <= limit) return pts;
+    std::vector<Pt> out;
+    const double st = static_cast<double>(pts.size() - 1U) / static_cast<double>(limit - 1);
+    for (int i = 0; i < limit; ++i) {
+        const auto idx = static_cast<std::size_t>(std::llround(static_cast<double>(i) * st));
+        out.push_back(pts[std::min(idx, pts.size() - 1U)]);
+    }
+    return out;
+}
+
+std::vector<std::pair<double, double>> gen_candidates(const float* ref, int w, int h, const uint8_t* roi, const orc_config& c) {  // :207-317
+    std::vector<std::pair<double, double>> cands;
+    const int rad = std::max(std::max(1, c.is_subset_radius), std::max(1, c.sp_subset_radius));
+    auto margin_ok = [&](int x, int y) { return !(x - rad < 0 || y - rad < 0 || x + rad >= w || y + rad >= h); };
+    std::vector<Pt> pts;
+    for (int y = 0; y < h; ++y) for (int x = 0; x < w; ++x) if (roi_valid(roi, w, h, x, y) && margin_ok(x, y)) pts.push_back({x, y});
+    if (pts.empty()) for (int y = 0; y < h; ++y) for (int x = 0; x < w; ++x) if (roi_valid(roi, w, h, x, y)) pts.push_back({x, y});
+    if (pts.empty()) return cands;
+    const int requested = std::max(1, c.seed_count);
+    const auto sp = det_sample(pts, std::max(1, c.kmeans_sample_limit));
+    const int tr = std::max(1, c.is_subset_radius);
+    if (requested == 1) {
+        double best = -1.0; Pt bp{}; bool found = false;
+        for (const auto& p : sp) {
+            if (!margin_ok(p.x, p.y)) continue;
+            const double t = texture_std(ref, w, h, tr, p.x, p.y);
+            if (!found || t > best) { best = t; bp = p; found = true; }
+        }
+        if (found) cands.emplace_back(bp.x, bp.y);
+        return cands;
+    }
+    // initialize_centers :49-67
+    const int count = std::min(requested, static_cast<int>(sp.size()));
+    std::vector<double> cxs, cys;
+    const double st = count == 1 ? 0.0 : static_cast<double>(sp.size() - 1U) / static_cast<double>(count - 1);
+    for (int i = 0; i < count; ++i) {
+        const auto idx = static_cast<std::size_t>(std::llround(static_cast<double>(i) * st));
+        const auto& p = sp[std::min(idx, sp.size() - 1U)];
+        cxs.push_back(p.x); cys.push_back(p.y);
+    }
+    // run_kmeans :69-108
+    const int iters = std::max(0, c.kmeans_iterations);
+    std::vector<double> sx(count), sy(count);
+    std::vector<int> cnt(count);
+    for (int it = 0; it < iters; ++it) {
+        std::fill(sx.begin(), sx.end(), 0.0); std::fill(sy.begin(), sy.end(), 0.0); std::fill(cnt.begin(), cnt.end(), 0);
+        for (const auto& p : sp) {
+            std::size_t best = 0; double bd = kInf;
+            for (int i = 0; i < count; ++i) {
+                const double dx = p.x - cxs[i], dy = p.y - cys[i];
+                const double d2 = dx * dx + dy * dy;
+                if (d2 < bd) { bd = d2; best = static_cast<std::size_t>(i); }
+            }
+            sx[best] += p.x; sy[best] += p.y; ++cnt[best];
+        }
+        for (int i = 0; i < count; ++i) if (cnt[i] > 0) { cxs[i] = sx[i] / cnt[i]; cys[i] = sy[i] / cnt[i]; }
+    }
+    for (int i = 0; i < count; ++i) {
+        const int rx = static_cast<int>(std::llround(cxs[i])), ry = static_cast<int>(std::llround(cys[i]));
+        if (roi_valid(roi, w, h, rx, ry) && margin_ok(rx, ry) && texture_std(ref, w, h, tr, rx, ry) >= c.min_texture_std) {
+            cands.emplace_back(rx, ry);
+            continue;
+        }
+        std::vector<std::size_t> order(sp.size());
+        std::iota(order.begin(), order.end(), 0U);
+        const double ccx = cxs[i], ccy = cys[i];
+        std::sort(order.begin(), order.end(), [&](std::size_t l, std::size_t r) {
+            const double lx = sp[l].x - ccx, ly = sp[l].y - ccy, qx = sp[r].x - ccx, qy = sp[r].y - ccy;
+            return lx * lx + ly * ly < qx * qx + qy * qy;
+        });
+        const std::size_t lim = std::min<std::size_t>(50U, order.size());
+        double best = -1.0; Pt bp = sp[order.front()];
+        for (std::size_t k = 0; k < lim; ++k) {
+            const auto& p = sp[order[k]];
+            const double t = texture_std(ref, w, h, tr, p.x, p.y);
+            if (t > best) { best = t; bp = p; }
+        }
+        cands.emplace_back(bp.x, bp.y);
+    }
+    return cands;
+}
+
+bool select_seed(const float* ref, const float* def, int w, int h, const uint8_t* roi, const orc_config& c,
+                 orc_seed& seed, std::vector<std::pair<double, double>>* cands_out) {
+    seed = orc_seed{};
+    seed.found = 0;
+    const auto cands = gen_candidates(ref, w, h, roi, c);
+    if (cands_out) *cands_out = cands;
+    if (c.sift_enabled) return false;  // sift_initializer.cpp:53-55 without OpenCV: no match, no seed
+    // Lazy, non-prefiltered deformed spline (seed_selector.cpp:166-173).
+    const int border = std::max(3, c.border);
+    std::vector<double> lazy;
+    Spline sp;
+    const bool refine = c.sp_enabled != 0;
+    if (refine) {
+        lazy.resize(static_cast<std::size_t>(w + 2 * border) * (h + 2 * border));
+        form_coefficients(def, w, h, c.degree, border, false, lazy.data());
+        sp.init(lazy.data(), w, h, c.degree, border);
+    }
+    GradSource gs{ref, w, h, nullptr, nullptr};  // reference interpolator is empty -> central differences
+    const SolverCfg scfg{std::max(1, c.sp_subset_radius), std::max(0, c.sp_max_iterations), c.sp_convergence_threshold, 0};
+    SeedEval best;
+    bool found = false;
+    for (const auto& cd : cands) {
+        SeedEval ev;
+        ev.x = cd.first; ev.y = cd.second;
+        double iu, iv, iz;
+        if (!integer_search(ref, def, w, h, c, cd.first, cd.second, iu, iv, iz)) continue;
+        double p[6] = {iu, iv, 0, 0, 0, 0};
+        double conf = znssd_from_zncc(iz), quality = conf;
+        if (refine) {  // subset_initializer.cpp:152-204
+            const orc_poi_result r = solve_icgn(ref, w, h, gs, sp, scfg, cd.first, cd.second, p, conf);
+            if (r.valid && r.status == kSuccess) {
+                for (int k = 0; k < 6; ++k) p[k] = r.p[k];
+                conf = r.correlation;
+                quality = r.correlation;
+            }
+        }
+        if (!std::isfinite(p[0]) || !std::isfinite(p[1]) || !std::isfinite(conf)) continue;  // :507-512
+        for (int k = 0; k < 6; ++k) ev.p[k] = p[k];
+        ev.corr = conf;
+        ev.quality = quality;
+        ev.norm = std::hypot(p[0], p[1]);
+        ev.passed = quality <= c.seed_max_znssd;
+        ev.valid = true;
+        if (ev.valid && ev.passed && ev.norm >= c.min_displacement_norm) {
+            bool better = !found;
+            if (found) {  // seed_is_better :110-133 (ZNSSD metric)
+                if (ev.quality < best.quality - 1e-9) better = true;
+                else if (ev.quality > best.quality + 1e-9) better = false;
+                else better = ev.norm > best.norm;
+            }
+            if (better) { best = ev; found = true; }
+        }
+    }
+    if (!found) return false;
+    seed.x = best.x; seed.y = best.y;
+    for (int k = 0; k < 6; ++k) seed.p[k] = best.p[k];
+    seed.correlation = best.corr;
+    seed.found = 1;
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+void orc_config_default(orc_config* c) {
+    std::memset(c, 0, sizeof(*c));
+    c->subset_radius = 15; c->max_iterations = 30; c->convergence_threshold = 1e-3;
+    c->optimizer = 0; c->shape_order = 1; c->criterion = 1; c->degree = 5; c->border = 3;
+    c->propagation_spacing = 5; c->propagation_max_znssd = 0.5;
+    c->is_subset_radius = 10; c->is_search_radius = 30; c->sift_enabled = 0; c->pyramid_enabled = 1;
+    c->pyramid_scale = 4; c->pyramid_refinement_radius = 4;
+    c->sp_enabled = 1; c->sp_subset_radius = 15; c->sp_max_iterations = 30; c->precision = 0;
+    c->sp_convergence_threshold = 1e-3;
+    c->seed_count = 256; c->kmeans_iterations = 20; c->seed_max_znssd = 0.2;
+    c->min_displacement_norm = 0.0; c->min_texture_std = 0.0; c->kmeans_sample_limit = 20000;
+    c->propagation_mode = 1;
+}
+
+double orc_bspline_basis(double x, int r, int d) { return valid_degree(d) ? basis(x, r, d) : kNaN; }
+
+int orc_bspline_qk(int d, double* qk) {
+    if (!valid_degree(d)) return -1;
+    build_qk(d, qk);
+    return 0;
+}
+
+int orc_prefilter(const float* image, int w, int h, int d, int border, int exact, double* coeffs) {
+    if (!valid_degree(d) || w <= 0 || h <= 0 || !image || !coeffs) return -1;
+    form_coefficients(image, w, h, d, border, exact != 0, coeffs);
+    return 0;
+}
+
+double orc_interp_value(const double* coeffs, int w, int h, int d, int border, double x, double y) {
+    Spline sp;
+    sp.init(coeffs, w, h, d, border);
+    return sp.value(x, y);
+}
+
+void orc_interp_gradient(const double* coeffs, int w, int h, int d, int border, double x, double y, double* gx, double* gy) {
+    Spline sp;
+    sp.init(coeffs, w, h, d, border);
+    sp.gradient(x, y, *gx, *gy);
+}
+
+void orc_reference_gradient(const float* img, int w, int h, double* gx, double* gy) {
+    GradSource gs{img, w, h, nullptr, nullptr};
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x) gs.at(x, y, gx[static_cast<std::size_t>(y) * w + x], gy[static_cast<std::size_t>(y) * w + x]);
+}
+
+int orc_solve_pois(const float* ref, int w, int h, const double* ref_gx, const double* ref_gy,
+                   const double* coeffs, int d, int border, const orc_config* cfg,
+                   int n, const double* xy, const double* p0, const double* conf0, orc_poi_result* out) {
+    if (cfg->shape_order != 1 || cfg->criterion != 1 || !valid_degree(d)) return -1;
+    Spline sp;
+    sp.init(coeffs, w, h, d, border);
+    GradSource gs{ref, w, h, ref_gx, ref_gy};
+    const SolverCfg scfg{cfg->subset_radius, cfg->max_iterations, cfg->convergence_threshold, cfg->optimizer};
+    for (int i = 0; i < n; ++i)
+        out[i] = solve_one(ref, w, h, gs, sp, scfg, xy[2 * i], xy[2 * i + 1], p0 + 6 * i, conf0 ? conf0[i] : 0.0);
+    return 0;
+}
+
+void orc_grid_dims(int w, int h, int spacing, int* gw, int* gh) {
+    const int step = std::max(0, spacing) + 1;
+    *gw = (w + step - 1) / step;
+    *gh = (h + step - 1) / step;
+}
+
+int orc_propagate(const float* ref, int w, int h, const uint8_t* roi, const double* ref_gx, const double* ref_gy,
+                  const double* coeffs, const orc_config* cfg, const orc_seed* seed, int max_solves,
+                  orc_grid_out* out, int* solves_done) {
+    Spline sp;
+    sp.init(coeffs, w, h, cfg->degree, cfg->border);
+    GradSource gs{ref, w, h, ref_gx, ref_gy};
+    return propagate(ref, w, h, roi, gs, sp, *cfg, *seed, max_solves, out, solves_done);
+}
+
+int orc_integer_search(const float* ref, const float* def, int w, int h, const orc_config* cfg,
+                       double px, double py, double* u, double* v, double* zncc) {
+    return integer_search(ref, def, w, h, *cfg, px, py, *u, *v, *zncc) ? 1 : 0;
+}
+
+int orc_select_seed(const float* ref, const float* def, int w, int h, const uint8_t* roi, const orc_config* cfg,
+                    orc_seed* seed, double* cand_xy, int cand_cap, int* n_candidates) {
+    std::vector<std::pair<double, double>> cands;
+    const bool ok = select_seed(ref, def, w, h, roi, *cfg, *seed, &cands);
+    if (n_candidates) *n_candidates = static_cast<int>(cands.size());
+    if (cand_xy)
+        for (int i = 0; i < static_cast<int>(cands.size()) && i < cand_cap; ++i) { cand_xy[2 * i] = cands[i].first; cand_xy[2 * i + 1] = cands[i].second; }
+    return ok ? 1 : 0;
+}
+
+int orc_subset_compute(const float* ref, const float* def, int w, int h, const uint8_t* roi,
+                       const orc_config* cfg, orc_grid_out* out, orc_seed* seed_out) {
+    if (w <= 0 || h <= 0 || !ref || !def) return 0;
+    orc_seed seed;
+    if (!select_seed(ref, def, w, h, roi, *cfg, seed, nullptr)) { if (seed_out) *seed_out = seed; return 0; }
+    if (seed_out) *seed_out = seed;
+    const int border = std::max(3, cfg->border);
+    std::vector<double> coeffs(static_cast<std::size_t>(w + 2 * border) * (h + 2 * border));
+    form_coefficients(def, w, h, cfg->degree, border, true, coeffs.data());
+    std::vector<double> gx(static_cast<std::size_t>(w) * h), gy(static_cast<std::size_t>(w) * h);
+    orc_reference_gradient(ref, w, h, gx.data(), gy.data());
+    Spline sp;
+    sp.init(coeffs.data(), w, h, cfg->degree, border);
+    GradSource gs{ref, w, h, gx.data(), gy.data()};
+    const int computed = propagate(ref, w, h, roi, gs, sp, *cfg, seed, -1, out, nullptr);
+    if (computed == 0) return 0;
+    int gw, gh;
+    orc_grid_dims(w, h, cfg->propagation_spacing, &gw, &gh);
+    return gw * gh;
+}
+
+}  // extern "C"

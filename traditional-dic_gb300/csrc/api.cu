@@ -1,0 +1,747 @@
+// C ABI of libtdic_gb300 (declared in include/tdic_gb300.h).  Host-side orchestration only:
+// argument checks, device memory from the context pool, the seed-alignment and grid geometry
+// of ReliabilityPropagation::propagate, k-means seed candidates of SeedSelector, and the
+// stream-ordered launches of the kernels in prefilter.cu, hotpath.cu and seed.cu.
+#include "tdic_internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <numeric>
+
+namespace tdic {
+
+void upload_qk_constants();
+
+// ---------------------------------------------------------------------------------------
+// DevicePool
+// ---------------------------------------------------------------------------------------
+size_t DevicePool::size_class(size_t bytes) {
+    if (bytes <= 4096) return 4096;
+    size_t c = 4096;
+    while (c < bytes && c < (size_t(1) << 26)) c <<= 1;         // powers of two up to 64 MiB
+    if (c >= bytes) return c;
+    const size_t chunk = size_t(1) << 24;                       // then 16 MiB granules
+    return (bytes + chunk - 1) / chunk * chunk;
+}
+
+void* DevicePool::acquire(size_t bytes) {
+    const size_t c = size_class(bytes);
+    auto it = free_.find(c);
+    void* p = nullptr;
+    if (it != free_.end()) {
+        p = it->second;
+        free_.erase(it);
+    } else {
+        cudaError_t e = cudaMalloc(&p, c);
+        if (e != cudaSuccess) {
+            trim();
+            e = cudaMalloc(&p, c);
+            if (e != cudaSuccess) {
+                (void)cudaGetLastError();
+                throw Error{TDIC_OOM, "device allocation of " + std::to_string(c) + " bytes failed"};
+            }
+        }
+        held_ += c;
+    }
+    live_[p] = c;
+    return p;
+}
+
+void DevicePool::release(void* p) {
+    auto it = live_.find(p);
+    if (it == live_.end()) return;
+    free_.emplace(it->second, p);
+    live_.erase(it);
+}
+
+void DevicePool::trim() {
+    for (auto& kv : free_) {
+        cudaFree(kv.second);
+        held_ -= kv.first;
+    }
+    free_.clear();
+}
+
+// ---------------------------------------------------------------------------------------
+// B-spline qk matrix (bspline.cpp:320-367), host side
+// ---------------------------------------------------------------------------------------
+namespace {
+int fact(int n) { int v = 1; for (int i = 2; i <= n; ++i) v *= i; return v; }
+int comb(int n, int k) { return (k < 0 || k > n) ? 0 : fact(n) / (fact(k) * fact(n - k)); }
+double basis(double x, int r, int d) {
+    if (r < 0 || r > d) return 0.0;
+    const int dfac = fact(d) / fact(d - r);
+    double sum = 0.0;
+    for (int k = 0; k <= d + 1; ++k) {
+        const double sign = k % 2 == 0 ? 1.0 : -1.0;
+        const double shift = static_cast<double>(d + 1) / 2.0 - static_cast<double>(k);
+        const double xx = x + shift;
+        sum += sign * comb(d + 1, k) * dfac * (xx > 0.0 ? std::pow(xx, d - r) : 0.0);
+    }
+    return sum / static_cast<double>(fact(d));
+}
+}  // namespace
+
+void build_qk(int d, double* qk) {
+    const int n = d + 1, off = d / 2;
+    for (int r = 0; r < n; ++r)
+        for (int c = 0; c < n; ++c) {
+            const double sign = r % 2 == 0 ? 1.0 : -1.0;
+            qk[r * n + c] = sign * basis(static_cast<double>(-off + c), r, d) / static_cast<double>(fact(r));
+        }
+}
+
+const SampleTable& sample_table(tdic_ctx* ctx, int radius) {
+    auto it = ctx->tables.find(radius);
+    if (it != ctx->tables.end()) return it->second;
+    std::vector<short2> off;
+    for (int dy = -radius; dy <= radius; ++dy)
+        for (int dx = -radius; dx <= radius; ++dx)
+            if (dx * dx + dy * dy <= radius * radius) off.push_back(make_short2(static_cast<short>(dx), static_cast<short>(dy)));
+    SampleTable t;
+    t.n = static_cast<int>(off.size());
+    t.offsets = Buffer(&ctx->pool, sizeof(short2) * std::max<size_t>(off.size(), 1));
+    TDIC_CUDA_TRY(cudaMemcpy(t.offsets.ptr, off.data(), sizeof(short2) * off.size(), cudaMemcpyHostToDevice));
+    auto res = ctx->tables.emplace(radius, std::move(t));
+    return res.first->second;
+}
+
+}  // namespace tdic
+
+using namespace tdic;
+
+namespace {
+
+template <typename F>
+tdic_status guarded(tdic_ctx* ctx, F&& f) {
+    if (!ctx) return TDIC_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+    try {
+        f();
+        return TDIC_OK;
+    } catch (const Error& e) {
+        ctx->last_error = e.msg;
+        return e.code;
+    } catch (const std::exception& e) {
+        ctx->last_error = e.what();
+        return TDIC_INVALID_ARG;
+    }
+}
+
+cudaStream_t pick(tdic_ctx* ctx, void* s) { return s ? static_cast<cudaStream_t>(s) : ctx->stream; }
+
+size_t dtype_size(tdic_dtype t) {
+    switch (t) {
+        case TDIC_U8: return 1;
+        case TDIC_U16: return 2;
+        case TDIC_F32: return 4;
+        case TDIC_F64: return 8;
+    }
+    return 0;
+}
+
+bool first_order_znssd(const tdic_config& c) { return c.shape_order == 1 && c.criterion == 1; }
+
+int normalized_degree(int d) { return (d == 1 || d == 3) ? d : 5; }
+
+void check_config(const tdic_config& c) {
+    TDIC_REQUIRE(first_order_znssd(c), TDIC_UNSUPPORTED,
+                 "only first-order ZNSSD routes are on the GPU path (second order / SSD: use the reference solver)");
+    TDIC_REQUIRE(c.optimizer == 0 || c.optimizer == 1, TDIC_INVALID_ARG, "optimizer must be 0 (icgn) or 1 (fgn)");
+    TDIC_REQUIRE(c.subset_radius >= 1 && c.subset_radius <= 100, TDIC_INVALID_ARG, "subset radius must be in [1, 100]");
+    TDIC_REQUIRE(c.max_iterations >= 0, TDIC_INVALID_ARG, "max_iterations must be >= 0");
+}
+
+// Upload (or alias) one image and convert it to float32 into dst.
+void upload_convert(tdic_pair* p, const void* src, int pitch, tdic_dtype dtype, tdic_memory mem, float* dst,
+                    cudaStream_t s) {
+    const size_t es = dtype_size(dtype);
+    TDIC_REQUIRE(es != 0, TDIC_INVALID_ARG, "unknown dtype");
+    const int pt = pitch > 0 ? pitch : p->w;
+    TDIC_REQUIRE(pt >= p->w, TDIC_INVALID_ARG, "pitch smaller than width");
+    const void* dsrc = src;
+    if (mem == TDIC_HOST) {
+        const size_t bytes = es * static_cast<size_t>(pt) * p->h;
+        if (p->staging.bytes < bytes) p->staging = Buffer(&p->ctx->pool, bytes);
+        TDIC_CUDA_TRY(cudaMemcpyAsync(p->staging.ptr, src, bytes, cudaMemcpyHostToDevice, s));
+        dsrc = p->staging.ptr;
+    }
+    launch_convert(dsrc, p->w, p->h, pt, dtype, dst, s);
+}
+
+void pair_compute(tdic_pair* p, const void* ref, const void* def, int pitch, tdic_dtype dtype, tdic_memory mem,
+                  cudaStream_t s) {
+    upload_convert(p, ref, pitch, dtype, mem, p->ref.as<float>(), s);
+    upload_convert(p, def, pitch, dtype, mem, p->def_f.as<float>(), s);
+    launch_prefilter(p, p->def_f.as<float>(), s);
+}
+
+int nearest_grid_index(int c, int step, int limit) {  // reliability_propagation.cpp:77-82
+    const int idx = static_cast<int>(std::llround(static_cast<double>(c) / static_cast<double>(step)));
+    return std::clamp(idx, 0, limit - 1);
+}
+
+bool roi_ok(const uint8_t* roi, int w, int h, int x, int y) {
+    if (x < 0 || y < 0 || x >= w || y >= h) return false;
+    return roi == nullptr || roi[static_cast<size_t>(y) * w + x] != 0;
+}
+
+// Device SoA output, either the caller's device arrays or pool buffers copied back.
+struct GridBuffers {
+    Buffer d[14];
+    tdic_grid_out dev{};
+};
+
+void alloc_grid(tdic_ctx* ctx, GridBuffers& g, int n, const tdic_grid_out* host_wanted) {
+    double** dptrs[10] = {&g.dev.x, &g.dev.y, &g.dev.u, &g.dev.v, &g.dev.du_dx, &g.dev.du_dy, &g.dev.dv_dx, &g.dev.dv_dy,
+                          &g.dev.correlation, &g.dev.zncc};
+    double* const* hptrs[10] = {&host_wanted->x, &host_wanted->y, &host_wanted->u, &host_wanted->v, &host_wanted->du_dx,
+                                &host_wanted->du_dy, &host_wanted->dv_dx, &host_wanted->dv_dy, &host_wanted->correlation,
+                                &host_wanted->zncc};
+    for (int i = 0; i < 10; ++i) {
+        if (*hptrs[i]) {
+            g.d[i] = Buffer(&ctx->pool, sizeof(double) * n);
+            *dptrs[i] = g.d[i].as<double>();
+        }
+    }
+    if (host_wanted->valid) { g.d[10] = Buffer(&ctx->pool, n); g.dev.valid = g.d[10].as<uint8_t>(); }
+    if (host_wanted->status) { g.d[11] = Buffer(&ctx->pool, n); g.dev.status = g.d[11].as<int8_t>(); }
+    if (host_wanted->iterations) { g.d[12] = Buffer(&ctx->pool, sizeof(int32_t) * n); g.dev.iterations = g.d[12].as<int32_t>(); }
+    if (host_wanted->converged) { g.d[13] = Buffer(&ctx->pool, n); g.dev.converged = g.d[13].as<uint8_t>(); }
+}
+
+void copy_grid_back(const GridBuffers& g, const tdic_grid_out* h, int n, cudaStream_t s) {
+    auto cp = [&](void* dst, const void* src, size_t bytes) {
+        if (dst && src) TDIC_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+    };
+    cp(h->x, g.dev.x, 8 * n); cp(h->y, g.dev.y, 8 * n); cp(h->u, g.dev.u, 8 * n); cp(h->v, g.dev.v, 8 * n);
+    cp(h->du_dx, g.dev.du_dx, 8 * n); cp(h->du_dy, g.dev.du_dy, 8 * n); cp(h->dv_dx, g.dev.dv_dx, 8 * n);
+    cp(h->dv_dy, g.dev.dv_dy, 8 * n); cp(h->correlation, g.dev.correlation, 8 * n); cp(h->zncc, g.dev.zncc, 8 * n);
+    cp(h->valid, g.dev.valid, n); cp(h->status, g.dev.status, n); cp(h->iterations, g.dev.iterations, 4 * n);
+    cp(h->converged, g.dev.converged, n);
+}
+
+void propagate_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const tdic_seed& seed, const uint8_t* roi,
+                    const tdic_grid_out* out, tdic_memory mem, int32_t* points_computed, cudaStream_t s) {
+    check_config(cfg);
+    TDIC_REQUIRE(pair->exact == 1, TDIC_INVALID_ARG, "propagation needs a pair with the exact prefilter");
+    const int w = pair->w, h = pair->h;
+    const int step = std::max(0, cfg.propagation_spacing) + 1;
+    int32_t gw, gh;
+    tdic_grid_dims(w, h, cfg.propagation_spacing, &gw, &gh);
+    const int n = gw * gh;
+    *points_computed = 0;
+    // Seed alignment on the host (reliability_propagation.cpp:201-216).
+    const int sxr = static_cast<int>(std::round(seed.x)), syr = static_cast<int>(std::round(seed.y));
+    bool seed_ok = seed.found != 0 && roi_ok(roi, w, h, sxr, syr);
+    int gxs = 0, gys = 0;
+    if (seed_ok) {
+        gxs = nearest_grid_index(sxr, step, gw);
+        gys = nearest_grid_index(syr, step, gh);
+        seed_ok = roi_ok(roi, w, h, gxs * step, gys * step);
+    }
+    // ROI at the grid points
+    std::vector<uint8_t> roi_grid(n, 1);
+    if (roi)
+        for (int i = 0; i < n; ++i) roi_grid[i] = roi[static_cast<size_t>((i / gw) * step) * w + (i % gw) * step] ? 1 : 0;
+    GridBuffers gb;
+    if (mem == TDIC_DEVICE) gb.dev = *out; else alloc_grid(ctx, gb, n, out);
+    Buffer d_roi(&ctx->pool, n);
+    Buffer claim(&ctx->pool, sizeof(int) * n);
+    Buffer keyparams(&ctx->pool, (sizeof(unsigned long long) + propagate_param_bytes(pair->precision)) * n);
+    Buffer order(&ctx->pool, sizeof(int) * n);
+    Buffer fetch(&ctx->pool, sizeof(int) * (n + 2));
+    Buffer misc(&ctx->pool, 64);
+    TDIC_CUDA_TRY(cudaMemcpyAsync(d_roi.ptr, roi_grid.data(), n, cudaMemcpyHostToDevice, s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(claim.ptr, 0, sizeof(int) * n, s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(keyparams.ptr, 0xff, sizeof(unsigned long long) * n, s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(fetch.ptr, 0, sizeof(int) * (n + 2), s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(misc.ptr, 0, 64, s));
+    PropagateLaunch L{};
+    L.gw = gw; L.gh = gh; L.step = step;
+    L.roi_grid = d_roi.as<uint8_t>();
+    L.seed_idx = gys * gw + gxs;
+    L.seed_solve = (gxs * step != sxr || gys * step != syr) ? 1 : 0;
+    for (int k = 0; k < 6; ++k) L.seed_p[k] = seed.p[k];
+    L.seed_corr = seed.correlation;
+    L.out = gb.dev;
+    L.claim = claim.as<int>();
+    L.key = keyparams.as<unsigned long long>();
+    L.params = nullptr;
+    L.order = order.as<int>();
+    int* m = misc.as<int>();
+    L.counters = m;                  // [0] tail
+    L.barrier = reinterpret_cast<unsigned int*>(m + 4);
+    L.flags = m + 8;                 // [0] error [1] no seed [2] accepted
+    L.fetch = fetch.as<int>();
+    if (!seed_ok) {
+        // Output every grid point with defaults; points_computed = 0.
+        L.seed_idx = 0;
+        L.seed_solve = 0;
+    }
+    if (seed_ok) launch_propagate(ctx, pair, cfg, L, s);
+    else launch_init_grid(L.out, gw, gh, step, s);  // every grid point with its defaults
+    int flags[3] = {0, 0, 0};
+    if (seed_ok) TDIC_CUDA_TRY(cudaMemcpyAsync(flags, L.flags, sizeof(flags), cudaMemcpyDeviceToHost, s));
+    if (mem == TDIC_HOST) copy_grid_back(gb, out, n, s);
+    TDIC_CUDA_TRY(cudaStreamSynchronize(s));
+    TDIC_REQUIRE(flags[0] == 0, TDIC_TIMEOUT, "propagation grid barrier timed out");
+    *points_computed = (seed_ok && !flags[1]) ? flags[2] : 0;
+}
+
+// ---------------------------------------------------------------------------------------
+// Seed candidates (seed_selector.cpp:33-108, 207-317, 388-452), truncate_roi_subsets false.
+// ---------------------------------------------------------------------------------------
+struct Pt { int x, y; };
+
+template <typename Acc>
+double texture_std(const Acc& ref, int w, int h, int r, int x, int y) {
+    if (x - r < 0 || y - r < 0 || x + r >= w || y + r >= h) return 0.0;
+    double sum = 0.0, sq = 0.0;
+    int cnt = 0;
+    for (int yy = y - r; yy <= y + r; ++yy)
+        for (int xx = x - r; xx <= x + r; ++xx) {
+            const double v = ref(static_cast<size_t>(yy) * w + xx);
+            sum += v; sq += v * v; ++cnt;
+        }
+    const double mn = sum / cnt;
+    return std::sqrt(std::max(0.0, sq / cnt - mn * mn));
+}
+
+template <typename Acc>
+std::vector<std::pair<int, int>> seed_candidates(const Acc& ref, int w, int h, const uint8_t* roi, const tdic_config& c) {
+    std::vector<std::pair<int, int>> out;
+    const int rad = std::max(std::max(1, c.is_subset_radius), std::max(1, c.sp_subset_radius));
+    auto margin_ok = [&](int x, int y) { return !(x - rad < 0 || y - rad < 0 || x + rad >= w || y + rad >= h); };
+    std::vector<Pt> pts;
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x)
+            if (roi_ok(roi, w, h, x, y) && margin_ok(x, y)) pts.push_back({x, y});
+    if (pts.empty())
+        for (int y = 0; y < h; ++y)
+            for (int x = 0; x < w; ++x)
+                if (roi_ok(roi, w, h, x, y)) pts.push_back({x, y});
+    if (pts.empty()) return out;
+    const int requested = std::max(1, c.seed_count);
+    const int limit = std::max(1, c.kmeans_sample_limit);
+    std::vector<Pt> sp;
+    if (static_cast<int>(pts.size()) <= limit) {
+        sp = pts;
+    } else {
+        const double st = static_cast<double>(pts.size() - 1U) / static_cast<double>(limit - 1);
+        for (int i = 0; i < limit; ++i) {
+            const auto idx = static_cast<size_t>(std::llround(static_cast<double>(i) * st));
+            sp.push_back(pts[std::min(idx, pts.size() - 1U)]);
+        }
+    }
+    const int tr = std::max(1, c.is_subset_radius);
+    if (requested == 1) {
+        double best = -1.0;
+        Pt bp{};
+        bool found = false;
+        for (const auto& p : sp) {
+            if (!margin_ok(p.x, p.y)) continue;
+            const double t = texture_std(ref, w, h, tr, p.x, p.y);
+            if (!found || t > best) { best = t; bp = p; found = true; }
+        }
+        if (found) out.emplace_back(bp.x, bp.y);
+        return out;
+    }
+    const int count = std::min(requested, static_cast<int>(sp.size()));
+    std::vector<double> cx(count), cy(count);
+    const double st = count == 1 ? 0.0 : static_cast<double>(sp.size() - 1U) / static_cast<double>(count - 1);
+    for (int i = 0; i < count; ++i) {
+        const auto idx = static_cast<size_t>(std::llround(static_cast<double>(i) * st));
+        const auto& p = sp[std::min(idx, sp.size() - 1U)];
+        cx[i] = p.x;
+        cy[i] = p.y;
+    }
+    std::vector<double> sx(count), sy(count);
+    std::vector<int> cnt(count);
+    for (int it = 0; it < std::max(0, c.kmeans_iterations); ++it) {
+        std::fill(sx.begin(), sx.end(), 0.0);
+        std::fill(sy.begin(), sy.end(), 0.0);
+        std::fill(cnt.begin(), cnt.end(), 0);
+        for (const auto& p : sp) {
+            int best = 0;
+            double bd = std::numeric_limits<double>::infinity();
+            for (int i = 0; i < count; ++i) {
+                const double dx = p.x - cx[i], dy = p.y - cy[i];
+                const double d2 = dx * dx + dy * dy;
+                if (d2 < bd) { bd = d2; best = i; }
+            }
+            sx[best] += p.x;
+            sy[best] += p.y;
+            ++cnt[best];
+        }
+        for (int i = 0; i < count; ++i)
+            if (cnt[i] > 0) { cx[i] = sx[i] / cnt[i]; cy[i] = sy[i] / cnt[i]; }
+    }
+    for (int i = 0; i < count; ++i) {
+        const int rx = static_cast<int>(std::llround(cx[i])), ry = static_cast<int>(std::llround(cy[i]));
+        if (roi_ok(roi, w, h, rx, ry) && margin_ok(rx, ry) && texture_std(ref, w, h, tr, rx, ry) >= c.min_texture_std) {
+            out.emplace_back(rx, ry);
+            continue;
+        }
+        std::vector<size_t> ord(sp.size());
+        std::iota(ord.begin(), ord.end(), 0U);
+        const double ccx = cx[i], ccy = cy[i];
+        std::sort(ord.begin(), ord.end(), [&](size_t l, size_t r) {
+            const double lx = sp[l].x - ccx, ly = sp[l].y - ccy, qx = sp[r].x - ccx, qy = sp[r].y - ccy;
+            return lx * lx + ly * ly < qx * qx + qy * qy;
+        });
+        const size_t lim = std::min<size_t>(50U, ord.size());
+        double best = -1.0;
+        Pt bp = sp[ord.front()];
+        for (size_t k = 0; k < lim; ++k) {
+            const auto& p = sp[ord[k]];
+            const double t = texture_std(ref, w, h, tr, p.x, p.y);
+            if (t > best) { best = t; bp = p; }
+        }
+        out.emplace_back(bp.x, bp.y);
+    }
+    return out;
+}
+
+double znssd_from_zncc(double z) {  // integer_search.cpp:25-31
+    if (!std::isfinite(z)) return std::numeric_limits<double>::infinity();
+    return std::max(0.0, 2.0 * (1.0 - std::max(-1.0, std::min(1.0, z))));
+}
+
+// Host view of the raw reference as dic::Image float values.
+struct HostImage {
+    const void* p;
+    tdic_dtype t;
+    float operator()(size_t i) const {
+        switch (t) {
+            case TDIC_U8: return static_cast<const uint8_t*>(p)[i];
+            case TDIC_U16: return static_cast<const uint16_t*>(p)[i];
+            case TDIC_F32: return static_cast<const float*>(p)[i];
+            case TDIC_F64: return static_cast<float>(static_cast<const double*>(p)[i]);
+        }
+        return 0.0f;
+    }
+};
+
+void select_seed_impl(tdic_ctx* ctx, tdic_pair* lazy, const HostImage& ref_host, const uint8_t* roi, const tdic_config& c,
+                      tdic_seed* seed, cudaStream_t s) {
+    std::memset(seed, 0, sizeof(*seed));
+    const int w = lazy->w, h = lazy->h;
+    const auto cands = seed_candidates(ref_host, w, h, roi, c);
+    if (c.sift_enabled) return;  // without OpenCV the SIFT prior finds no match: no seed
+    const int n = static_cast<int>(cands.size());
+    if (n == 0) return;
+    std::vector<int> cx(n), cy(n);
+    for (int i = 0; i < n; ++i) { cx[i] = cands[i].first; cy[i] = cands[i].second; }
+    std::vector<SearchResult> sr(n);
+    integer_search_batch(ctx, lazy, c, cx.data(), cy.data(), n, sr.data(), s);
+    // subpixel refinement: ICGN on the non-prefiltered spline (subset_initializer.cpp:152-204)
+    std::vector<tdic_poi_in> in;
+    std::vector<int> who;
+    for (int i = 0; i < n; ++i) {
+        if (!sr[i].ok) continue;
+        tdic_poi_in q{};
+        q.x = cx[i]; q.y = cy[i];
+        q.p0[0] = sr[i].u; q.p0[1] = sr[i].v;
+        q.confidence = znssd_from_zncc(sr[i].zncc);
+        in.push_back(q);
+        who.push_back(i);
+    }
+    std::vector<tdic_poi_out> ref_out(in.size());
+    const bool refine = c.sp_enabled != 0;
+    if (refine && !in.empty()) {
+        tdic_config sc = c;
+        sc.subset_radius = std::max(1, c.sp_subset_radius);
+        sc.max_iterations = std::max(0, c.sp_max_iterations);
+        sc.convergence_threshold = c.sp_convergence_threshold;
+        sc.optimizer = 0;
+        sc.shape_order = 1;
+        Buffer d_in(&ctx->pool, sizeof(tdic_poi_in) * in.size()), d_out(&ctx->pool, sizeof(tdic_poi_out) * in.size()),
+            d_fetch(&ctx->pool, sizeof(int));
+        TDIC_CUDA_TRY(cudaMemcpyAsync(d_in.ptr, in.data(), sizeof(tdic_poi_in) * in.size(), cudaMemcpyHostToDevice, s));
+        SolveLaunch L{d_in.as<tdic_poi_in>(), d_out.as<tdic_poi_out>(), static_cast<int>(in.size()), d_fetch.as<int>()};
+        launch_solve(ctx, lazy, sc, L, s);
+        TDIC_CUDA_TRY(cudaMemcpyAsync(ref_out.data(), d_out.ptr, sizeof(tdic_poi_out) * in.size(), cudaMemcpyDeviceToHost, s));
+        TDIC_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    bool found = false;
+    double bq = 0.0, bnorm = 0.0;
+    for (size_t k = 0; k < in.size(); ++k) {
+        double p[6] = {in[k].p0[0], in[k].p0[1], 0, 0, 0, 0};
+        double conf = in[k].confidence, quality = conf;
+        if (refine && ref_out[k].valid && ref_out[k].status == TDIC_SUCCESS) {
+            for (int j = 0; j < 6; ++j) p[j] = ref_out[k].p[j];
+            conf = ref_out[k].correlation;
+            quality = conf;
+        }
+        if (!std::isfinite(p[0]) || !std::isfinite(p[1]) || !std::isfinite(conf)) continue;
+        const double nrm = std::hypot(p[0], p[1]);
+        if (!(quality <= c.seed_max_znssd) || !(nrm >= c.min_displacement_norm)) continue;
+        bool better = !found;
+        if (found) {  // seed_is_better, seed_selector.cpp:110-133
+            if (quality < bq - 1e-9) better = true;
+            else if (quality > bq + 1e-9) better = false;
+            else better = nrm > bnorm;
+        }
+        if (better) {
+            found = true;
+            bq = quality;
+            bnorm = nrm;
+            seed->x = cx[who[k]];
+            seed->y = cy[who[k]];
+            for (int j = 0; j < 6; ++j) seed->p[j] = p[j];
+            seed->correlation = conf;
+            seed->found = 1;
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+void tdic_config_default(tdic_config* c) {
+    std::memset(c, 0, sizeof(*c));
+    c->subset_radius = 15; c->max_iterations = 30; c->convergence_threshold = 1e-3;
+    c->optimizer = 0; c->shape_order = 1; c->criterion = 1; c->degree = 5; c->border = 3;
+    c->propagation_spacing = 5; c->propagation_max_znssd = 0.5;
+    c->is_subset_radius = 10; c->is_search_radius = 30; c->sift_enabled = 0; c->pyramid_enabled = 1;
+    c->pyramid_scale = 4; c->pyramid_refinement_radius = 4;
+    c->sp_enabled = 1; c->sp_subset_radius = 15; c->sp_max_iterations = 30; c->precision = TDIC_FP32_MIXED;
+    c->sp_convergence_threshold = 1e-3;
+    c->seed_count = 256; c->kmeans_iterations = 20; c->seed_max_znssd = 0.2;
+    c->min_displacement_norm = 0.0; c->min_texture_std = 0.0; c->kmeans_sample_limit = 20000;
+    c->propagation_mode = 0;
+}
+
+void tdic_grid_dims(int32_t w, int32_t h, int32_t spacing, int32_t* gw, int32_t* gh) {
+    const int step = std::max(0, spacing) + 1;
+    *gw = (w + step - 1) / step;
+    *gh = (h + step - 1) / step;
+}
+
+tdic_status tdic_ctx_create(int32_t device, tdic_ctx** out) {
+    if (!out) return TDIC_INVALID_ARG;
+    *out = nullptr;
+    auto* ctx = new tdic_ctx();
+    ctx->device = device;
+    tdic_status st = guarded(ctx, [&] {
+        TDIC_CUDA_TRY(cudaSetDevice(device));
+        TDIC_CUDA_TRY(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
+        TDIC_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        upload_qk_constants();
+    });
+    if (st != TDIC_OK) {
+        static thread_local std::string msg;
+        msg = ctx->last_error;
+        delete ctx;
+        return st;
+    }
+    *out = ctx;
+    return TDIC_OK;
+}
+
+namespace {
+void ctx_free(tdic_ctx* ctx) {
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    ctx->tables.clear();
+    ctx->pool.trim();
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+}
+}  // namespace
+
+void tdic_ctx_destroy(tdic_ctx* ctx) {
+    if (!ctx) return;
+    {
+        std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+        if (ctx->live_pairs > 0) {  // freed by the last tdic_pair_destroy
+            ctx->destroy_requested = true;
+            return;
+        }
+        ctx_free(ctx);
+    }
+    delete ctx;
+}
+
+const char* tdic_last_error(const tdic_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+size_t tdic_ctx_device_bytes(const tdic_ctx* ctx) { return ctx ? ctx->pool.held_bytes() : 0; }
+
+tdic_status tdic_pair_create(tdic_ctx* ctx, const void* reference, const void* deformed, int32_t width, int32_t height,
+                             int32_t pitch, tdic_dtype dtype, tdic_memory memory, int32_t degree, int32_t border,
+                             int32_t exact_prefilter, int32_t precision, void* stream, tdic_pair** out) {
+    if (!out) return TDIC_INVALID_ARG;
+    *out = nullptr;
+    return guarded(ctx, [&] {
+        TDIC_REQUIRE(reference && deformed, TDIC_INVALID_ARG, "Cannot precompute B-spline data for an empty image.");
+        TDIC_REQUIRE(width > 0 && height > 0, TDIC_INVALID_ARG, "Cannot precompute B-spline data for an empty image.");
+        TDIC_REQUIRE(degree == 1 || degree == 3 || degree == 5, TDIC_INVALID_ARG,
+                     "Only B-spline degree 1, 3, and 5 are supported; got " + std::to_string(degree) + ".");
+        TDIC_REQUIRE(precision == TDIC_FP32_MIXED || precision == TDIC_FP64, TDIC_INVALID_ARG, "unknown precision");
+        TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
+        auto* p = new tdic_pair();
+        p->ctx = ctx;
+        p->w = width; p->h = height;
+        p->border = std::max(3, border);
+        p->degree = degree;
+        p->precision = precision;
+        p->exact = exact_prefilter ? 1 : 0;
+        p->cw = width + 2 * p->border;
+        p->ch = height + 2 * p->border;
+        try {
+            const size_t es = precision == TDIC_FP64 ? 8 : 4;
+            p->ref = Buffer(&ctx->pool, sizeof(float) * static_cast<size_t>(width) * height);
+            p->def_f = Buffer(&ctx->pool, sizeof(float) * static_cast<size_t>(width) * height);
+            p->coef = Buffer(&ctx->pool, es * static_cast<size_t>(p->cw) * p->ch);
+            pair_compute(p, reference, deformed, pitch, dtype, memory, pick(ctx, stream));
+        } catch (...) {
+            delete p;
+            throw;
+        }
+        ctx->live_pairs += 1;
+        *out = p;
+    });
+}
+
+tdic_status tdic_pair_update(tdic_pair* pair, const void* reference, const void* deformed, int32_t pitch,
+                             tdic_dtype dtype, tdic_memory memory, void* stream) {
+    if (!pair) return TDIC_INVALID_ARG;
+    return guarded(pair->ctx, [&] {
+        TDIC_REQUIRE(reference && deformed, TDIC_INVALID_ARG, "null image");
+        pair_compute(pair, reference, deformed, pitch, dtype, memory, pick(pair->ctx, stream));
+    });
+}
+
+void tdic_pair_destroy(tdic_pair* pair) {
+    if (!pair) return;
+    tdic_ctx* ctx = pair->ctx;
+    bool free_ctx = false;
+    {
+        std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+        cudaSetDevice(ctx->device);
+        cudaDeviceSynchronize();  // work on any stream may still read the pair's buffers
+        delete pair;
+        ctx->live_pairs -= 1;
+        if (ctx->destroy_requested && ctx->live_pairs == 0) {
+            ctx_free(ctx);
+            free_ctx = true;
+        }
+    }
+    if (free_ctx) delete ctx;
+}
+
+tdic_status tdic_pair_coefficients(tdic_pair* pair, void* host_out, size_t bytes) {
+    if (!pair) return TDIC_INVALID_ARG;
+    return guarded(pair->ctx, [&] {
+        TDIC_REQUIRE(host_out && bytes >= pair->coef.bytes, TDIC_INVALID_ARG, "output buffer too small");
+        TDIC_CUDA_TRY(cudaDeviceSynchronize());
+        TDIC_CUDA_TRY(cudaMemcpy(host_out, pair->coef.ptr, pair->coef.bytes, cudaMemcpyDeviceToHost));
+    });
+}
+
+tdic_status tdic_reference_gradient(tdic_pair* pair, double* gx, double* gy) {
+    if (!pair) return TDIC_INVALID_ARG;
+    return guarded(pair->ctx, [&] {
+        TDIC_REQUIRE(gx && gy, TDIC_INVALID_ARG, "null output");
+        tdic_ctx* ctx = pair->ctx;
+        const size_t n = static_cast<size_t>(pair->w) * pair->h;
+        Buffer dx(&ctx->pool, 8 * n), dy(&ctx->pool, 8 * n);
+        launch_reference_gradient(pair->ref.as<float>(), pair->w, pair->h, dx.as<double>(), dy.as<double>(), ctx->stream);
+        TDIC_CUDA_TRY(cudaMemcpyAsync(gx, dx.ptr, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
+        TDIC_CUDA_TRY(cudaMemcpyAsync(gy, dy.ptr, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
+        TDIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+tdic_status tdic_solve_pois(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cfg, const tdic_poi_in* in, int32_t n,
+                            tdic_poi_out* out, tdic_memory memory, void* stream) {
+    return guarded(ctx, [&] {
+        TDIC_REQUIRE(pair && cfg, TDIC_INVALID_ARG, "null pair or config");
+        TDIC_REQUIRE(n >= 0, TDIC_INVALID_ARG, "negative POI count");
+        check_config(*cfg);
+        if (n == 0) return;
+        TDIC_REQUIRE(in && out, TDIC_INVALID_ARG, "null POI arrays");
+        TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
+        cudaStream_t s = pick(ctx, stream);
+        Buffer fetch(&ctx->pool, sizeof(int));
+        if (memory == TDIC_DEVICE) {
+            launch_solve(ctx, pair, *cfg, SolveLaunch{in, out, n, fetch.as<int>()}, s);
+            TDIC_CUDA_TRY(cudaStreamSynchronize(s));  // keep `fetch` alive until the kernel is done
+            return;
+        }
+        Buffer d_in(&ctx->pool, sizeof(tdic_poi_in) * n), d_out(&ctx->pool, sizeof(tdic_poi_out) * n);
+        TDIC_CUDA_TRY(cudaMemcpyAsync(d_in.ptr, in, sizeof(tdic_poi_in) * n, cudaMemcpyHostToDevice, s));
+        launch_solve(ctx, pair, *cfg, SolveLaunch{d_in.as<tdic_poi_in>(), d_out.as<tdic_poi_out>(), n, fetch.as<int>()}, s);
+        TDIC_CUDA_TRY(cudaMemcpyAsync(out, d_out.ptr, sizeof(tdic_poi_out) * n, cudaMemcpyDeviceToHost, s));
+        TDIC_CUDA_TRY(cudaStreamSynchronize(s));
+    });
+}
+
+tdic_status tdic_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cfg, const tdic_seed* seed,
+                           const uint8_t* roi, tdic_grid_out* out, tdic_memory memory, int32_t* points_computed,
+                           void* stream) {
+    return guarded(ctx, [&] {
+        TDIC_REQUIRE(pair && cfg && seed && out && points_computed, TDIC_INVALID_ARG, "null argument");
+        TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
+        propagate_impl(ctx, pair, *cfg, *seed, roi, out, memory, points_computed, pick(ctx, stream));
+    });
+}
+
+tdic_status tdic_select_seed(tdic_ctx* ctx, tdic_pair* lazy, const float* reference_host, const uint8_t* roi,
+                             const tdic_config* cfg, tdic_seed* seed, void* stream) {
+    return guarded(ctx, [&] {
+        TDIC_REQUIRE(lazy && reference_host && cfg && seed, TDIC_INVALID_ARG, "null argument");
+        TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
+        select_seed_impl(ctx, lazy, HostImage{reference_host, TDIC_F32}, roi, *cfg, seed, pick(ctx, stream));
+    });
+}
+
+tdic_status tdic_subset_compute(tdic_ctx* ctx, const void* reference, const void* deformed, int32_t width,
+                                int32_t height, tdic_dtype dtype, const uint8_t* roi, const tdic_config* cfg,
+                                tdic_grid_out* out, int32_t* n_points, tdic_seed* seed_out, void* stream) {
+    return guarded(ctx, [&] {
+        TDIC_REQUIRE(cfg && out && n_points, TDIC_INVALID_ARG, "null argument");
+        *n_points = 0;
+        if (!reference || !deformed || width <= 0 || height <= 0) return;  // SubsetDIC::compute: empty result
+        check_config(*cfg);
+        TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
+        cudaStream_t s = pick(ctx, stream);
+        const int degree = normalized_degree(cfg->degree);
+        tdic_pair* pair = nullptr;
+        tdic_status st = tdic_pair_create(ctx, reference, deformed, width, height, 0, dtype, TDIC_HOST, degree,
+                                          cfg->border, 1, cfg->precision, s, &pair);
+        if (st != TDIC_OK) throw Error{st, ctx->last_error};
+        int32_t computed = 0;
+        try {
+            // Seed refinement runs on the clamp-padded, non-deconvolved coefficients of the same
+            // deformed image (seed_selector.cpp:166-173); the lazy pair reuses the uploaded images.
+            tdic_pair* lazy = nullptr;
+            st = tdic_pair_create(ctx, pair->ref.ptr, pair->def_f.ptr, width, height, 0, TDIC_F32, TDIC_DEVICE, degree,
+                                  cfg->border, 0, cfg->precision, s, &lazy);
+            if (st != TDIC_OK) throw Error{st, ctx->last_error};
+            tdic_seed seed{};
+            try {
+                select_seed_impl(ctx, lazy, HostImage{reference, dtype}, roi, *cfg, &seed, s);
+            } catch (...) {
+                tdic_pair_destroy(lazy);
+                throw;
+            }
+            tdic_pair_destroy(lazy);
+            if (seed_out) *seed_out = seed;
+            if (seed.found) propagate_impl(ctx, pair, *cfg, seed, roi, out, TDIC_HOST, &computed, s);
+        } catch (...) {
+            tdic_pair_destroy(pair);
+            throw;
+        }
+        tdic_pair_destroy(pair);
+        if (computed == 0) return;
+        int32_t gw, gh;
+        tdic_grid_dims(width, height, cfg->propagation_spacing, &gw, &gh);
+        *n_points = gw * gh;
+    });
+}
+
+}  // extern "C"

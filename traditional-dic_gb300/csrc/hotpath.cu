@@ -1,0 +1,953 @@
+// K3 / K4: first-order ZNSSD ICGN and FGN per POI, batched and inside the frontier-wave
+// propagation kernel.
+//
+// One cooperative group of G warps owns one POI at a time.  The reference subset (circular,
+// icgn.cpp:484-510) is staged in shared memory as {normalised reference value f^, gx, gy} per
+// sample; each iteration warps the samples, gathers the (d+1)^2 B-spline coefficient window of
+// every warped point from the L2-resident coefficient image, evaluates the spline with
+// separable weights w_m(t) = sum_r qk[r][m] t^r (qk of bspline.cpp:320-340, so the value equals
+// the reference's local polynomial block evaluation, bspline.cpp:96-113/153-175), and reduces
+// the ZNSSD residual and J^T r across the group with warp shuffles.  Precision of the FP32-mixed
+// build: interpolation and residual arithmetic in float with Kahan-compensated normalisation
+// sums; the 6x6 Hessian factorisation / inverse and the normalisation scalars in double.  The
+// FP64 build is the same code with every T = double.
+#include "tdic_internal.cuh"
+
+#include <cmath>
+
+namespace tdic {
+
+namespace {
+
+constexpr double kEps = 1e-12;   // icgn.cpp:13
+constexpr unsigned long long kSpinLimit = 1ull << 26;  // bounded waits (~2 s with backoff)
+
+__constant__ double c_qk_d[3][36];
+__constant__ float c_qk_f[3][36];
+
+template <typename T> __device__ __forceinline__ T qk_at(int deg_slot, int i);
+template <> __device__ __forceinline__ float qk_at<float>(int s, int i) { return c_qk_f[s][i]; }
+template <> __device__ __forceinline__ double qk_at<double>(int s, int i) { return c_qk_d[s][i]; }
+
+template <int DEG> struct Slot { static constexpr int value = DEG == 1 ? 0 : (DEG == 3 ? 1 : 2); };
+
+// ---------------------------------------------------------------------------------------
+// Small helpers
+// ---------------------------------------------------------------------------------------
+template <typename T> struct Kahan {
+    T s = T(0), c = T(0);
+    __device__ __forceinline__ void add(T x) {
+        const T y = x - c;
+        const T t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ T value() const { return s - c; }
+};
+
+template <typename T> __device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ void named_bar(int id, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// All-reduce K values over the group (every thread ends with the same sums, summed in the
+// same order, so redundant scalar math stays bit-identical across the group's warps).
+template <int G, int K, typename T>
+__device__ __forceinline__ void group_sum(T (&v)[K], T* red, int tid, int bar_id) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
+    if constexpr (G > 1) {
+        const int warp = tid >> 5, lane = tid & 31;
+        named_bar(bar_id, 32 * G);  // previous readers of red are done
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) red[warp * K + k] = v[k];
+        }
+        named_bar(bar_id, 32 * G);
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            T s = red[k];
+#pragma unroll
+            for (int w = 1; w < G; ++w) s += red[w * K + k];
+            v[k] = s;
+        }
+    }
+}
+
+template <int G>
+__device__ __forceinline__ void group_sync(int bar_id) {
+    if constexpr (G == 1) __syncwarp();
+    else named_bar(bar_id, 32 * G);
+}
+
+template <int G>
+__device__ __forceinline__ bool group_any(bool p, int* flag, int tid, int bar_id) {
+    const bool w = __any_sync(0xffffffffu, p);
+    if constexpr (G == 1) {
+        return w;
+    } else {
+        named_bar(bar_id, 32 * G);
+        if (tid == 0) *flag = 0;
+        named_bar(bar_id, 32 * G);
+        if (w && (tid & 31) == 0) *flag = 1;
+        named_bar(bar_id, 32 * G);
+        return *flag != 0;
+    }
+}
+
+template <typename T> __device__ __forceinline__ bool finite6(const T* p) {
+    bool ok = true;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) ok = ok && isfinite(p[i]);
+    return ok;
+}
+
+// ---------------------------------------------------------------------------------------
+// 6x6 LDLT with symmetric diagonal pivoting and sign tracking: success / positivity
+// semantics of Eigen::LDLT as used at icgn.cpp:538-542 and forward_gauss_newton.cpp:354-358;
+// solve applies the pseudo-inverse of D (zero where |D_ii| <= DBL_MIN).
+// ---------------------------------------------------------------------------------------
+template <typename M>
+struct Ldlt6 {
+    M m[6][6];
+    int t[6];
+    int sign;  // 0 zero, 1 positive semidefinite, 2 negative semidefinite, 3 indefinite
+    bool ok;
+
+    __device__ void factor(const M (&a)[6][6]) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+#pragma unroll
+            for (int j = 0; j < 6; ++j) m[i][j] = a[i][j];
+        sign = 0;
+        ok = true;
+        bool found_zero = false;
+        for (int k = 0; k < 6; ++k) {
+            int big = k;
+            M bigv = fabs(m[k][k]);
+            for (int i = k + 1; i < 6; ++i)
+                if (fabs(m[i][i]) > bigv) { bigv = fabs(m[i][i]); big = i; }
+            t[k] = big;
+            if (big != k) {
+                for (int j = 0; j < k; ++j) { const M x = m[k][j]; m[k][j] = m[big][j]; m[big][j] = x; }
+                for (int i = big + 1; i < 6; ++i) { const M x = m[i][k]; m[i][k] = m[i][big]; m[i][big] = x; }
+                { const M x = m[k][k]; m[k][k] = m[big][big]; m[big][big] = x; }
+                for (int i = k + 1; i < big; ++i) { const M x = m[i][k]; m[i][k] = m[big][i]; m[big][i] = x; }
+            }
+            if (k > 0) {
+                M temp[6];
+                for (int j = 0; j < k; ++j) temp[j] = m[j][j] * m[k][j];
+                M s = M(0);
+                for (int j = 0; j < k; ++j) s += m[k][j] * temp[j];
+                m[k][k] -= s;
+                for (int i = k + 1; i < 6; ++i) {
+                    M si = M(0);
+                    for (int j = 0; j < k; ++j) si += m[i][j] * temp[j];
+                    m[i][k] -= si;
+                }
+            }
+            const M akk = m[k][k];
+            const bool pivot_valid = fabs(akk) > M(0);
+            if (k == 0 && !pivot_valid) {
+                sign = 0;
+                for (int j = 0; j < 6; ++j) { t[j] = j; for (int i = 0; i < 6; ++i) m[i][j] = M(0); }
+                ok = true;
+                return;
+            }
+            if (pivot_valid) {
+                for (int i = k + 1; i < 6; ++i) m[i][k] /= akk;
+            } else {
+                for (int i = k + 1; i < 6; ++i) ok = ok && (m[i][k] == M(0));
+            }
+            if (found_zero && pivot_valid) ok = false;
+            else if (!pivot_valid) found_zero = true;
+            if (sign == 1) { if (akk < M(0)) sign = 3; }
+            else if (sign == 2) { if (akk > M(0)) sign = 3; }
+            else if (sign == 0) { if (akk > M(0)) sign = 1; else if (akk < M(0)) sign = 2; }
+        }
+    }
+    __device__ bool good() const { return ok && (sign == 1 || sign == 0); }
+    __device__ void solve(const M (&b)[6], M (&x)[6]) const {
+        for (int i = 0; i < 6; ++i) x[i] = b[i];
+        for (int k = 0; k < 6; ++k) { const M v = x[k]; x[k] = x[t[k]]; x[t[k]] = v; }
+        for (int i = 0; i < 6; ++i) { M s = x[i]; for (int j = 0; j < i; ++j) s -= m[i][j] * x[j]; x[i] = s; }
+        for (int i = 0; i < 6; ++i) {
+            const M d = m[i][i];
+            x[i] = fabs(d) > M(2.2250738585072014e-308) ? x[i] / d : M(0);
+        }
+        for (int i = 5; i >= 0; --i) { M s = x[i]; for (int j = i + 1; j < 6; ++j) s -= m[j][i] * x[j]; x[i] = s; }
+        for (int k = 5; k >= 0; --k) { const M v = x[k]; x[k] = x[t[k]]; x[t[k]] = v; }
+    }
+};
+
+// icgn.cpp:83-120
+template <typename M>
+__device__ __forceinline__ void ic_update(const M (&p)[6], const M (&dp)[6], M (&o)[6]) {
+    const M du = p[0], dv = p[1], dudx = p[2], dudy = p[3], dvdx = p[4], dvdy = p[5];
+    const M dp0 = dp[0], dp1 = dp[1], dp2 = dp[2], dp3 = dp[3], dp4 = dp[4], dp5 = dp[5];
+    const M den = dp2 + dp5 + dp2 * dp5 - dp3 * dp4 + M(1);
+    if (fabs(den) <= M(kEps)) {
+        for (int i = 0; i < 6; ++i) o[i] = M(NAN);
+        return;
+    }
+    o[0] = du - ((dudx + M(1)) * (dp0 + dp0 * dp5 - dp1 * dp3)) / den - (dudy * (dp1 - dp0 * dp4 + dp1 * dp2)) / den;
+    o[1] = dv - ((dvdy + M(1)) * (dp1 - dp0 * dp4 + dp1 * dp2)) / den - (dvdx * (dp0 + dp0 * dp5 - dp1 * dp3)) / den;
+    o[2] = ((dp5 + M(1)) * (dudx + M(1))) / den - (dp4 * dudy) / den - M(1);
+    o[3] = (dudy * (dp2 + M(1))) / den - (dp3 * (dudx + M(1))) / den;
+    o[4] = (dvdx * (dp5 + M(1))) / den - (dp4 * (dvdy + M(1))) / den;
+    o[5] = ((dp2 + M(1)) * (dvdy + M(1))) / den - (dp3 * dvdx) / den - M(1);
+}
+
+// forward_gauss_newton.cpp:64-76
+template <typename M>
+__device__ __forceinline__ void compose_warp(const M (&p)[6], const M (&dp)[6], M (&pn)[6]) {
+    pn[0] = dp[0] + p[0] + p[2] * dp[0] + p[3] * dp[1];
+    pn[1] = dp[1] + p[1] + p[4] * dp[0] + p[5] * dp[1];
+    pn[2] = dp[2] + p[2] * (M(1) + dp[2]) + p[3] * dp[4];
+    pn[3] = dp[3] + p[2] * dp[3] + p[3] * (M(1) + dp[5]);
+    pn[4] = dp[4] + p[4] * (M(1) + dp[2]) + p[5] * dp[4];
+    pn[5] = dp[5] + p[4] * dp[3] + p[5] * (M(1) + dp[5]);
+}
+
+// ---------------------------------------------------------------------------------------
+// B-spline evaluation from the coefficient image
+// ---------------------------------------------------------------------------------------
+template <int DEG, typename T>
+__device__ __forceinline__ void weights(T t, T (&w)[DEG + 1]) {
+    constexpr int NB = DEG + 1;
+#pragma unroll
+    for (int m = 0; m < NB; ++m) {
+        T acc = qk_at<T>(Slot<DEG>::value, DEG * NB + m);
+#pragma unroll
+        for (int r = DEG - 1; r >= 0; --r) acc = acc * t + qk_at<T>(Slot<DEG>::value, r * NB + m);
+        w[m] = acc;
+    }
+}
+
+template <int DEG, typename T>
+__device__ __forceinline__ void dweights(T t, T (&w)[DEG + 1]) {
+    constexpr int NB = DEG + 1;
+#pragma unroll
+    for (int m = 0; m < NB; ++m) {
+        T acc = T(DEG) * qk_at<T>(Slot<DEG>::value, DEG * NB + m);
+#pragma unroll
+        for (int r = DEG - 1; r >= 1; --r) acc = acc * t + T(r) * qk_at<T>(Slot<DEG>::value, r * NB + m);
+        w[m] = acc;
+    }
+}
+
+template <typename T>
+struct Env {
+    const float* ref;      // H x W float32 reference
+    const T* coef;         // (H + 2B) x (W + 2B) coefficients
+    int w, h, cw, border;
+    int radius, n, nmax;   // samples of this radius; nmax = smem capacity per group
+    const short2* off;     // sample offsets
+    int max_iter;
+    double thr;
+};
+
+struct Result {
+    double p[6];
+    double corr;
+    int iters;
+    int status;
+    bool valid;
+    bool conv;
+};
+
+__device__ __forceinline__ void result_init(Result& r, const double (&p0)[6], double conf) {
+    r.p[0] = p0[0];
+    r.p[1] = p0[1];
+    r.p[2] = r.p[3] = r.p[4] = r.p[5] = 0.0;
+    r.corr = conf;
+    r.iters = 0;
+    r.status = TDIC_INVALID_INPUT;
+    r.valid = false;
+    r.conv = false;
+}
+
+template <typename T> struct MixedOf { using type = double; };
+
+// Warp the samples of this thread, interpolate, store g (and for FGN its gradient) and
+// accumulate the shifted normalisation sums.  Returns false if a warped point left the image.
+template <int DEG, typename T, bool GRAD>
+__device__ __forceinline__ bool warp_interp(const Env<T>& e, int cx, int cy, const T (&p)[6], T fm, T* s_g,
+                                            T* s_gx, T* s_gy, int tid, int nt, Kahan<T>& sg, Kahan<T>& sg2) {
+    constexpr int NB = DEG + 1, OFF = DEG / 2;
+    bool ok = true;
+    const T xlo = T(-cx), ylo = T(-cy), xhi = T(e.w - 1 - cx), yhi = T(e.h - 1 - cy);
+    for (int i = tid; i < e.n; i += nt) {
+        const short2 o = __ldg(e.off + i);
+        const T lx = T(o.x), ly = T(o.y);
+        const T tx = ((lx + p[0]) + p[2] * lx) + p[3] * ly;
+        const T ty = ((ly + p[1]) + p[4] * lx) + p[5] * ly;
+        if (!(tx >= xlo && ty >= ylo && tx <= xhi && ty <= yhi)) { ok = false; continue; }
+        const T fx = floor(tx), fy = floor(ty);
+        const int ix = static_cast<int>(fx), iy = static_cast<int>(fy);
+        const T dx = tx - fx, dy = ty - fy;
+        T wx[NB], wy[NB];
+        weights<DEG, T>(dx, wx);
+        weights<DEG, T>(dy, wy);
+        const T* base = e.coef + static_cast<size_t>(cy + iy + e.border - OFF) * e.cw + (cx + ix + e.border - OFF);
+        T c[NB][NB];
+#pragma unroll
+        for (int m = 0; m < NB; ++m)
+#pragma unroll
+            for (int q = 0; q < NB; ++q) c[m][q] = __ldg(base + m * e.cw + q);
+        T g = T(0);
+#pragma unroll
+        for (int m = 0; m < NB; ++m) {
+            T rs = T(0);
+#pragma unroll
+            for (int q = 0; q < NB; ++q) rs += wx[q] * c[m][q];
+            g += wy[m] * rs;
+        }
+        s_g[i] = g;
+        if constexpr (GRAD) {
+            T dwx[NB], dwy[NB];
+            dweights<DEG, T>(dx, dwx);
+            dweights<DEG, T>(dy, dwy);
+            T gx = T(0), gy = T(0);
+#pragma unroll
+            for (int m = 0; m < NB; ++m) {
+                T rx = T(0), r0 = T(0);
+#pragma unroll
+                for (int q = 0; q < NB; ++q) { rx += dwx[q] * c[m][q]; r0 += wx[q] * c[m][q]; }
+                gx += wy[m] * rx;
+                gy += dwy[m] * r0;
+            }
+            s_gx[i] = gx;
+            s_gy[i] = gy;
+        }
+        const T gs = g - fm;
+        sg.add(gs);
+        sg2.add(gs * gs);
+    }
+    return ok;
+}
+
+// The per-POI solve.  OPT 0 = ICGN (icgn.cpp:446-627), 1 = FGN (forward_gauss_newton.cpp:188-399).
+// sm: 4 * nmax T values of this group; red: G * 32 T values; flag: one int.
+template <int OPT, int DEG, typename T, int G>
+__device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6], double conf, T* sm, T* red,
+                          int* flag, typename MixedOf<T>::type* s_hinv, int tid, int bar_id, Result& R) {
+    using M = typename MixedOf<T>::type;
+    constexpr int NT = 32 * G;
+    result_init(R, p0, conf);
+    const int r = e.radius;
+    if (e.w <= 0 || r < 1 || e.max_iter < 0) return;
+    if (cx - r < 0 || cy - r < 0 || cx + r >= e.w || cy + r >= e.h) return;
+    if (e.n < 6) return;
+    T* s_fn = sm;
+    T* s_a = sm + e.nmax;      // ICGN: reference gx; FGN: deformed gx
+    T* s_b = sm + 2 * e.nmax;  // ICGN: reference gy; FGN: deformed gy
+    T* s_g = sm + 3 * e.nmax;
+    const int W = e.w, H = e.h;
+
+    // --- setup: reference values (and ICGN gradients), mean -------------------------------
+    Kahan<T> ksum;
+    for (int i = tid; i < e.n; i += NT) {
+        const short2 o = __ldg(e.off + i);
+        const int x = cx + o.x, y = cy + o.y;
+        const float f = __ldg(e.ref + static_cast<size_t>(y) * W + x);
+        s_fn[i] = T(f);
+        if constexpr (OPT == 0) {
+            // reference gradient cache, reliability_propagation.cpp:84-112
+            const int xm = max(0, x - 1), xp = min(W - 1, x + 1), ym = max(0, y - 1), yp = min(H - 1, y + 1);
+            const T gx = (T(__ldg(e.ref + static_cast<size_t>(y) * W + xp)) - T(__ldg(e.ref + static_cast<size_t>(y) * W + xm))) /
+                         T(max(1, xp - xm));
+            const T gy = (T(__ldg(e.ref + static_cast<size_t>(yp) * W + x)) - T(__ldg(e.ref + static_cast<size_t>(ym) * W + x))) /
+                         T(max(1, yp - ym));
+            s_a[i] = gx;
+            s_b[i] = gy;
+        }
+        ksum.add(T(f));
+    }
+    T v1[1] = {ksum.value()};
+    group_sum<G, 1>(v1, red, tid, bar_id);
+    const double N = static_cast<double>(e.n);
+    const double mean = static_cast<double>(v1[0]) / N;
+    const T fm = T(mean);
+    Kahan<T> knorm;
+    for (int i = tid; i < e.n; i += NT) {
+        const T d = s_fn[i] - fm;
+        knorm.add(d * d);
+    }
+    v1[0] = knorm.value();
+    group_sum<G, 1>(v1, red, tid, bar_id);
+    const double norm = sqrt(static_cast<double>(v1[0]));
+    if (norm <= kEps) { R.status = TDIC_NUMERICAL_FAILURE; return; }
+    const T inv_norm = T(1.0 / norm);
+
+    if constexpr (OPT == 0) {
+        // normalised reference and Hessian sums: H = (2/|f|^2) sum SD SD^T with
+        // SD = [a, b, a lx, a ly, b lx, b ly]; 18 distinct sums {aa, ab, bb} x {1, lx, ly, lx^2, lx ly, ly^2}
+        T hs[18];
+#pragma unroll
+        for (int k = 0; k < 18; ++k) hs[k] = T(0);
+        for (int i = tid; i < e.n; i += NT) {
+            const short2 o = __ldg(e.off + i);
+            const T lx = T(o.x), ly = T(o.y);
+            s_fn[i] = (s_fn[i] - fm) * inv_norm;
+            const T a = s_a[i], b = s_b[i];
+            const T q[3] = {a * a, a * b, b * b};
+            const T m6[6] = {T(1), lx, ly, lx * lx, lx * ly, ly * ly};
+#pragma unroll
+            for (int u = 0; u < 3; ++u)
+#pragma unroll
+                for (int v = 0; v < 6; ++v) hs[u * 6 + v] += q[u] * m6[v];
+        }
+        group_sum<G, 18>(hs, red, tid, bar_id);
+        // index map: S(u, v) with u in {aa, ab, bb}, v in {1, lx, ly, lxlx, lxly, lyly}
+        auto S = [&](int u, int v) { return static_cast<M>(hs[u * 6 + v]); };
+        M Hm[6][6];
+        Hm[0][0] = S(0, 0); Hm[0][1] = S(1, 0); Hm[0][2] = S(0, 1); Hm[0][3] = S(0, 2); Hm[0][4] = S(1, 1); Hm[0][5] = S(1, 2);
+        Hm[1][1] = S(2, 0); Hm[1][2] = S(1, 1); Hm[1][3] = S(1, 2); Hm[1][4] = S(2, 1); Hm[1][5] = S(2, 2);
+        Hm[2][2] = S(0, 3); Hm[2][3] = S(0, 4); Hm[2][4] = S(1, 3); Hm[2][5] = S(1, 4);
+        Hm[3][3] = S(0, 5); Hm[3][4] = S(1, 4); Hm[3][5] = S(1, 5);
+        Hm[4][4] = S(2, 3); Hm[4][5] = S(2, 4);
+        Hm[5][5] = S(2, 5);
+        const M hsc = M(2.0 / (norm * norm));
+        for (int i = 0; i < 6; ++i)
+            for (int j = i; j < 6; ++j) { Hm[i][j] *= hsc; Hm[j][i] = Hm[i][j]; }
+        Ldlt6<M> f;
+        f.factor(Hm);
+        if (!f.good()) { R.status = TDIC_NUMERICAL_FAILURE; return; }
+        // explicit inverse, column by column (the reference's per-iteration solves applied to
+        // unit vectors); kept in the group's shared memory
+        group_sync<G>(bar_id);
+        if (tid < 6) {
+            M ej[6] = {0, 0, 0, 0, 0, 0}, col[6];
+            ej[tid] = M(1);
+            f.solve(ej, col);
+            for (int i = 0; i < 6; ++i) s_hinv[i * 6 + tid] = col[i];
+        }
+        group_sync<G>(bar_id);
+    } else {
+        for (int i = tid; i < e.n; i += NT) s_fn[i] = (s_fn[i] - fm) * inv_norm;
+    }
+
+    M p[6];
+    for (int k = 0; k < 6; ++k) p[k] = static_cast<M>(p0[k]);
+    double corr = INFINITY;
+    bool converged = false;
+    const M gscale = M(2.0 / norm);
+    for (int it = 0; it < e.max_iter; ++it) {
+        R.iters = it + 1;
+        T pt[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) pt[k] = static_cast<T>(p[k]);
+        Kahan<T> sg, sg2;
+        const bool ok = warp_interp<DEG, T, OPT == 1>(e, cx, cy, pt, fm, s_g, s_a, s_b, tid, NT, sg, sg2);
+        if (group_any<G>(!ok, flag, tid, bar_id)) { R.status = TDIC_INVALID_INPUT; return; }
+        T v2[2] = {sg.value(), sg2.value()};
+        group_sum<G, 2>(v2, red, tid, bar_id);
+        const double gmr = static_cast<double>(v2[0]) / N;                 // mean of g - fm
+        const double var = static_cast<double>(v2[1]) - static_cast<double>(v2[0]) * gmr;
+        const double gn = sqrt(var > 0.0 ? var : 0.0);
+        if (gn <= kEps) { R.status = TDIC_NUMERICAL_FAILURE; return; }
+        const T gsh = T(gmr), inv_gn = T(1.0 / gn);
+        M dp[6];
+        if constexpr (OPT == 0) {
+            T q[7];
+#pragma unroll
+            for (int k = 0; k < 7; ++k) q[k] = T(0);
+            for (int i = tid; i < e.n; i += NT) {
+                const short2 o = __ldg(e.off + i);
+                const T lx = T(o.x), ly = T(o.y);
+                const T diff = s_fn[i] - ((s_g[i] - fm) - gsh) * inv_gn;
+                const T da = diff * s_a[i], db = diff * s_b[i];
+                q[0] += da; q[1] += db; q[2] += da * lx; q[3] += da * ly; q[4] += db * lx; q[5] += db * ly;
+                q[6] += diff * diff;
+            }
+            group_sum<G, 7>(q, red, tid, bar_id);
+            corr = static_cast<double>(q[6]);
+            M grad[6];
+            for (int k = 0; k < 6; ++k) grad[k] = static_cast<M>(q[k]) * gscale;
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                M s = M(0);
+#pragma unroll
+                for (int j = 0; j < 6; ++j) s += s_hinv[i * 6 + j] * grad[j];
+                dp[i] = -s;
+            }
+        } else {
+            // FGN: SD from the deformed spline gradient through dW/dz (forward_gauss_newton.cpp:44-60)
+            const T p2 = pt[2], p3 = pt[3], p4 = pt[4], p5 = pt[5];
+            T q[25];
+#pragma unroll
+            for (int k = 0; k < 25; ++k) q[k] = T(0);
+            for (int i = tid; i < e.n; i += NT) {
+                const short2 o = __ldg(e.off + i);
+                const T lx = T(o.x), ly = T(o.y);
+                const T gx = s_a[i], gy = s_b[i];
+                const T ae = gx * (T(1) + p2) + gy * p4;
+                const T be = gx * p3 + gy * (T(1) + p5);
+                const T diff = s_fn[i] - ((s_g[i] - fm) - gsh) * inv_gn;
+                const T qq[3] = {ae * ae, ae * be, be * be};
+                const T m6[6] = {T(1), lx, ly, lx * lx, lx * ly, ly * ly};
+#pragma unroll
+                for (int u = 0; u < 3; ++u)
+#pragma unroll
+                    for (int v = 0; v < 6; ++v) q[u * 6 + v] += qq[u] * m6[v];
+                const T da = diff * ae, db = diff * be;
+                q[18] += da; q[19] += db; q[20] += da * lx; q[21] += da * ly; q[22] += db * lx; q[23] += db * ly;
+                q[24] += diff * diff;
+            }
+            group_sum<G, 25>(q, red, tid, bar_id);
+            corr = static_cast<double>(q[24]);
+            auto S = [&](int u, int v) { return static_cast<M>(q[u * 6 + v]); };
+            M Hm[6][6];
+            Hm[0][0] = S(0, 0); Hm[0][1] = S(1, 0); Hm[0][2] = S(0, 1); Hm[0][3] = S(0, 2); Hm[0][4] = S(1, 1); Hm[0][5] = S(1, 2);
+            Hm[1][1] = S(2, 0); Hm[1][2] = S(1, 1); Hm[1][3] = S(1, 2); Hm[1][4] = S(2, 1); Hm[1][5] = S(2, 2);
+            Hm[2][2] = S(0, 3); Hm[2][3] = S(0, 4); Hm[2][4] = S(1, 3); Hm[2][5] = S(1, 4);
+            Hm[3][3] = S(0, 5); Hm[3][4] = S(1, 4); Hm[3][5] = S(1, 5);
+            Hm[4][4] = S(2, 3); Hm[4][5] = S(2, 4);
+            Hm[5][5] = S(2, 5);
+            const M hsc = M(2.0 / (norm * norm));
+            for (int i = 0; i < 6; ++i)
+                for (int j = i; j < 6; ++j) { Hm[i][j] *= hsc; Hm[j][i] = Hm[i][j]; }
+            M grad[6];
+            for (int k = 0; k < 6; ++k) grad[k] = static_cast<M>(q[18 + k]) * gscale;
+            Ldlt6<M> f;
+            f.factor(Hm);
+            if (!f.good()) { R.status = TDIC_NUMERICAL_FAILURE; return; }
+            f.solve(grad, dp);
+        }
+        if (!finite6(dp)) { R.status = TDIC_NUMERICAL_FAILURE; return; }
+        M dn2 = M(0);
+        for (int k = 0; k < 6; ++k) dn2 += dp[k] * dp[k];
+        M dn = sqrt(dn2);
+        M pn[6];
+        if constexpr (OPT == 0) {
+            ic_update<M>(p, dp, pn);
+        } else {
+            if (dn > M(0.5)) {  // forward_gauss_newton.cpp:367-371
+                for (int k = 0; k < 6; ++k) dp[k] *= M(0.5) / dn;
+                dn = M(0.5);
+            }
+            compose_warp<M>(p, dp, pn);
+        }
+        for (int k = 0; k < 6; ++k) p[k] = pn[k];
+        if (!finite6(p)) { R.status = TDIC_NUMERICAL_FAILURE; return; }
+        if (dn < M(e.thr)) { converged = true; break; }
+    }
+    for (int k = 0; k < 6; ++k) R.p[k] = static_cast<double>(p[k]);
+    R.corr = corr;
+    R.conv = converged;
+    if (!converged && isfinite(corr)) converged = true;
+    R.status = converged ? TDIC_SUCCESS : TDIC_NOT_CONVERGED;
+    R.valid = converged;
+}
+
+// Per-group shared memory: [36 doubles: 6x6 inverse][16 bytes: ints][32*G T: reduction
+// scratch][4*nmax T: samples f^, a, b, g].
+template <typename T> __host__ __device__ __forceinline__ size_t group_smem_bytes(int nmax, int G) {
+    const size_t bytes = 36 * sizeof(double) + 16 + (static_cast<size_t>(4) * nmax + 32 * G) * sizeof(T);
+    return (bytes + 15) & ~size_t(15);
+}
+
+template <typename T>
+struct GroupSmem {
+    double* hinv;
+    int* ints;
+    T* red;
+    T* sm;
+    __device__ GroupSmem(unsigned char* base, int gi, int nmax, int G) {
+        unsigned char* g = base + gi * group_smem_bytes<T>(nmax, G);
+        hinv = reinterpret_cast<double*>(g);
+        ints = reinterpret_cast<int*>(g + 36 * sizeof(double));
+        red = reinterpret_cast<T*>(g + 36 * sizeof(double) + 16);
+        sm = red + 32 * G;
+    }
+};
+
+__device__ __forceinline__ void write_out(tdic_poi_out* o, const Result& R) {
+    for (int k = 0; k < 6; ++k) o->p[k] = R.p[k];
+    o->correlation = R.corr;
+    const double z = 1.0 - 0.5 * R.corr;
+    o->zncc = isfinite(R.corr) ? fmax(-1.0, fmin(1.0, z)) : -1.0;
+    o->iterations = R.iters;
+    o->status = static_cast<int8_t>(R.status);
+    o->valid = R.valid ? 1 : 0;
+    o->converged = R.conv ? 1 : 0;
+    o->pad_ = 0;
+}
+
+// Broadcast one int from group thread 0 to the group.
+template <int G>
+__device__ __forceinline__ int group_bcast(int v, int* slot, int tid, int bar_id) {
+    if constexpr (G == 1) {
+        return __shfl_sync(0xffffffffu, v, 0);
+    } else {
+        named_bar(bar_id, 32 * G);
+        if (tid == 0) *slot = v;
+        named_bar(bar_id, 32 * G);
+        return *slot;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Batched solve: persistent groups pull POIs from a work counter.
+// ---------------------------------------------------------------------------------------
+template <int OPT, int DEG, typename T, int G>
+__global__ void solve_batch_kernel(Env<T> e, const tdic_poi_in* __restrict__ in, tdic_poi_out* __restrict__ out, int n,
+                                   int* fetch) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int gi = threadIdx.x / (32 * G), tid = threadIdx.x % (32 * G);
+    GroupSmem<T> gs(smem_raw, gi, e.nmax, G);
+    T* sm = gs.sm;
+    T* red = gs.red;
+    int* ints = gs.ints;
+    const int bar_id = 1 + gi;
+    while (true) {
+        int job = 0;
+        if (tid == 0) job = atomicAdd(fetch, 1);
+        job = group_bcast<G>(job, ints + 1, tid, bar_id);
+        if (job >= n) break;
+        const tdic_poi_in pin = in[job];
+        double p0[6];
+        for (int k = 0; k < 6; ++k) p0[k] = pin.p0[k];
+        // icgn.cpp:472-473: std::round (halves away from zero), as CUDA's round()
+        const int rx = static_cast<int>(round(pin.x)), ry = static_cast<int>(round(pin.y));
+        Result R;
+        solve_poi<OPT, DEG, T, G>(e, rx, ry, p0, pin.confidence, sm, red, ints, gs.hinv, tid, bar_id, R);
+        if (tid == 0) write_out(out + job, R);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Frontier-wave propagation (persistent, cooperative launch, own bounded grid barrier).
+// ---------------------------------------------------------------------------------------
+struct PropEnv {
+    int gw, gh, step;
+    const uint8_t* roi_grid;
+    int seed_idx, seed_solve;
+    double seed_p[6];
+    double seed_corr;
+    double max_znssd;
+    tdic_grid_out out;
+    int* claim;
+    unsigned long long* key;
+    int* order;
+    int* counters;  // [0] = tail
+    int* fetch;     // per wave
+    unsigned int* barrier;
+    int* flags;     // [0] error, [1] no seed, [2] accepted count
+};
+
+__device__ __forceinline__ int ld_cg(const int* p) { return __ldcg(p); }
+
+__device__ bool grid_barrier(unsigned int* bar, int* err) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* vgen = bar + 1;
+        const unsigned int gen = *vgen;
+        __threadfence();
+        const unsigned int arrived = atomicAdd(bar, 1u);
+        if (arrived == gridDim.x - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            unsigned long long spins = 0;
+            while (*vgen == gen) {
+                if (++spins > kSpinLimit) { atomicExch(err, 1); break; }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *reinterpret_cast<volatile int*>(err) == 0;
+}
+
+template <typename P>
+__device__ void store_grid(const PropEnv& pe, P* params, int idx, const Result& R) {
+    const tdic_grid_out& o = pe.out;
+    if (o.u) o.u[idx] = R.p[0];
+    if (o.v) o.v[idx] = R.p[1];
+    if (o.du_dx) o.du_dx[idx] = R.p[2];
+    if (o.du_dy) o.du_dy[idx] = R.p[3];
+    if (o.dv_dx) o.dv_dx[idx] = R.p[4];
+    if (o.dv_dy) o.dv_dy[idx] = R.p[5];
+    if (o.correlation) o.correlation[idx] = R.corr;
+    if (o.zncc) o.zncc[idx] = fmax(-1.0, fmin(1.0, 1.0 - 0.5 * R.corr));
+    if (o.valid) o.valid[idx] = 1;
+    if (o.status) o.status[idx] = TDIC_SUCCESS;
+    if (o.iterations) o.iterations[idx] = R.iters;
+    if (o.converged) o.converged[idx] = R.conv ? 1 : 0;
+    for (int k = 0; k < 6; ++k) params[static_cast<size_t>(idx) * 6 + k] = static_cast<P>(R.p[k]);
+}
+
+// Claim the admissible 4-neighbours of accepted point n for wave `next` and offer n as their
+// parent (key = float ZNSSD bits : parent index, atomicMin).  reliability_propagation.cpp:290-323.
+__device__ void expand(const PropEnv& pe, int w, int h, int radius, int n, double corr, int next) {
+    const int step = pe.step;
+    const int nx = (n % pe.gw) * step, ny = (n / pe.gw) * step;
+    const unsigned long long k = (static_cast<unsigned long long>(__float_as_uint(static_cast<float>(corr))) << 32) |
+                                 static_cast<unsigned int>(n);
+    const int dxs[4] = {0, step, 0, -step}, dys[4] = {-step, 0, step, 0};  // up, right, down, left
+    for (int d = 0; d < 4; ++d) {
+        const int mx = nx + dxs[d], my = ny + dys[d];
+        if (mx < 0 || my < 0 || mx >= w || my >= h) continue;
+        const int m = (my / step) * pe.gw + mx / step;
+        int c = ld_cg(pe.claim + m);
+        if (c == 0) {
+            const bool admissible = pe.roi_grid[m] != 0 && mx - radius >= 0 && my - radius >= 0 && mx + radius < w &&
+                                    my + radius < h;
+            if (!admissible) { atomicCAS(pe.claim + m, 0, -1); continue; }
+            const int old = atomicCAS(pe.claim + m, 0, next + 1);
+            if (old == 0) {
+                const int pos = atomicAdd(pe.counters, 1);
+                pe.order[pos] = m;
+                c = next + 1;
+            } else {
+                c = old;
+            }
+        }
+        if (c == next + 1) atomicMin(pe.key + m, k);
+    }
+}
+
+template <int OPT, int DEG, typename T, int G>
+__global__ void propagate_kernel(Env<T> e, PropEnv pe) {
+    using P = typename MixedOf<T>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int gi = threadIdx.x / (32 * G), tid = threadIdx.x % (32 * G);
+    GroupSmem<T> gs(smem_raw, gi, e.nmax, G);
+    T* sm = gs.sm;
+    T* red = gs.red;
+    int* ints = gs.ints;
+    const int bar_id = 1 + gi;
+    P* params = reinterpret_cast<P*>(pe.key + static_cast<size_t>(pe.gw) * pe.gh);  // params follow the keys
+    const double cutoff = static_cast<double>(pe.step);
+
+    // Prologue: place the seed (reliability_propagation.cpp:201-278).
+    if (blockIdx.x == 0 && gi == 0) {
+        Result R;
+        bool ok = true;
+        if (pe.seed_solve) {
+            const int sx = (pe.seed_idx % pe.gw) * pe.step, sy = (pe.seed_idx / pe.gw) * pe.step;
+            solve_poi<OPT, DEG, T, G>(e, sx, sy, pe.seed_p, pe.seed_corr, sm, red, ints, gs.hinv, tid, bar_id, R);
+            ok = R.valid && R.status == TDIC_SUCCESS && finite6(R.p) && isfinite(R.corr);
+        } else {
+            for (int k = 0; k < 6; ++k) R.p[k] = pe.seed_p[k];
+            R.corr = pe.seed_corr;
+            R.iters = 0;
+            R.status = TDIC_SUCCESS;
+            R.valid = true;
+            R.conv = false;
+        }
+        if (tid == 0) {
+            if (!ok) {
+                pe.flags[1] = 1;
+            } else {
+                store_grid<P>(pe, params, pe.seed_idx, R);
+                pe.claim[pe.seed_idx] = 1;
+                pe.flags[2] = 1;
+                __threadfence();
+                expand(pe, e.w, e.h, e.radius, pe.seed_idx, fmax(0.0, R.corr), 1);
+            }
+        }
+    }
+    if (!grid_barrier(pe.barrier, pe.flags)) return;
+    if (*reinterpret_cast<volatile int*>(pe.flags + 1)) return;
+    int start = 0;
+    int end = ld_cg(pe.counters);
+    for (int wave = 1; start < end; ++wave) {
+        const int count = end - start;
+        while (true) {
+            int i = 0;
+            if (tid == 0) i = atomicAdd(pe.fetch + wave, 1);
+            i = group_bcast<G>(i, ints + 1, tid, bar_id);
+            if (i >= count) break;
+            const int n = ld_cg(pe.order + start + i);
+            const unsigned long long kk = __ldcg(pe.key + n);
+            const int parent = static_cast<int>(kk & 0xffffffffull);
+            double pp[6];
+            for (int k = 0; k < 6; ++k) pp[k] = static_cast<double>(__ldcg(params + static_cast<size_t>(parent) * 6 + k));
+            const int nx = (n % pe.gw) * pe.step, ny = (n / pe.gw) * pe.step;
+            const double ddx = static_cast<double>(nx - (parent % pe.gw) * pe.step);
+            const double ddy = static_cast<double>(ny - (parent / pe.gw) * pe.step);
+            double p0[6];
+            p0[0] = pp[0] + pp[2] * ddx + pp[3] * ddy;  // reliability_propagation.cpp:326-329
+            p0[1] = pp[1] + pp[4] * ddx + pp[5] * ddy;
+            p0[2] = pp[2]; p0[3] = pp[3]; p0[4] = pp[4]; p0[5] = pp[5];
+            Result R;
+            solve_poi<OPT, DEG, T, G>(e, nx, ny, p0, 0.0, sm, red, ints, gs.hinv, tid, bar_id, R);
+            const bool accepted = R.valid && R.status == TDIC_SUCCESS && R.corr < pe.max_znssd &&
+                                  fabs(p0[0] - R.p[0]) < cutoff && fabs(p0[1] - R.p[1]) < cutoff && finite6(R.p) &&
+                                  isfinite(R.corr);  // :359-368
+            if (accepted && tid == 0) {
+                store_grid<P>(pe, params, n, R);
+                atomicAdd(pe.flags + 2, 1);
+                __threadfence();
+                expand(pe, e.w, e.h, e.radius, n, R.corr, wave + 1);
+            }
+        }
+        if (!grid_barrier(pe.barrier, pe.flags)) return;
+        start = end;
+        end = ld_cg(pe.counters);
+    }
+}
+
+__global__ void init_grid_kernel(tdic_grid_out o, int gw, int gh, int step) {
+    const int n = gw * gh;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (o.x) o.x[i] = static_cast<double>((i % gw) * step);
+        if (o.y) o.y[i] = static_cast<double>((i / gw) * step);
+        if (o.u) o.u[i] = 0.0;
+        if (o.v) o.v[i] = 0.0;
+        if (o.du_dx) o.du_dx[i] = 0.0;
+        if (o.du_dy) o.du_dy[i] = 0.0;
+        if (o.dv_dx) o.dv_dx[i] = 0.0;
+        if (o.dv_dy) o.dv_dy[i] = 0.0;
+        if (o.correlation) o.correlation[i] = 0.0;
+        if (o.zncc) o.zncc[i] = 1.0;
+        if (o.valid) o.valid[i] = 0;
+        if (o.status) o.status[i] = TDIC_INVALID_INPUT;
+        if (o.iterations) o.iterations[i] = 0;
+        if (o.converged) o.converged[i] = 0;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Dispatch
+// ---------------------------------------------------------------------------------------
+template <typename T>
+Env<T> make_env(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, int radius, int max_iter, double thr) {
+    const SampleTable& tab = sample_table(ctx, radius);
+    Env<T> e;
+    e.ref = pair->ref.as<float>();
+    e.coef = pair->coef.as<T>();
+    e.w = pair->w; e.h = pair->h; e.cw = pair->cw; e.border = pair->border;
+    e.radius = radius; e.n = tab.n; e.nmax = tab.n;
+    e.off = tab.offsets.as<short2>();
+    e.max_iter = max_iter;
+    e.thr = thr;
+    (void)cfg;
+    return e;
+}
+
+constexpr int kGroupsPerBlockBatch = 4;  // 4 warps of 1-warp groups
+
+template <int OPT, int DEG, typename T>
+void solve_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const SolveLaunch& L, cudaStream_t s) {
+    constexpr int G = 1;
+    Env<T> e = make_env<T>(ctx, pair, cfg, cfg.subset_radius, cfg.max_iterations, cfg.convergence_threshold);
+    const int gpb = kGroupsPerBlockBatch;
+    const size_t smem = gpb * group_smem_bytes<T>(e.nmax, G);
+    auto kern = solve_batch_kernel<OPT, DEG, T, G>;
+    TDIC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    int per_sm = 0;
+    TDIC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * G * gpb, smem));
+    TDIC_REQUIRE(per_sm > 0, TDIC_UNSUPPORTED, "subset radius too large for shared memory");
+    int blocks = per_sm * ctx->num_sms;
+    const int need = (L.n + gpb - 1) / gpb;
+    if (blocks > need) blocks = need < 1 ? 1 : need;
+    TDIC_CUDA_TRY(cudaMemsetAsync(L.fetch, 0, sizeof(int), s));
+    kern<<<blocks, 32 * G * gpb, smem, s>>>(e, L.in, L.out, L.n, L.fetch);
+    TDIC_CUDA_TRY(cudaGetLastError());
+}
+
+template <int OPT, typename T>
+void solve_deg(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const SolveLaunch& L, cudaStream_t s) {
+    switch (pair->degree) {
+        case 1: solve_typed<OPT, 1, T>(ctx, pair, cfg, L, s); break;
+        case 3: solve_typed<OPT, 3, T>(ctx, pair, cfg, L, s); break;
+        default: solve_typed<OPT, 5, T>(ctx, pair, cfg, L, s); break;
+    }
+}
+
+template <int OPT, int DEG, typename T>
+void propagate_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const PropagateLaunch& L, cudaStream_t s) {
+    constexpr int G = 1;
+    constexpr int gpb = 4;
+    Env<T> e = make_env<T>(ctx, pair, cfg, cfg.subset_radius, cfg.max_iterations, cfg.convergence_threshold);
+    const size_t smem = gpb * group_smem_bytes<T>(e.nmax, G);
+    auto kern = propagate_kernel<OPT, DEG, T, G>;
+    TDIC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    int per_sm = 0;
+    TDIC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * G * gpb, smem));
+    TDIC_REQUIRE(per_sm > 0, TDIC_UNSUPPORTED, "subset radius too large for shared memory");
+    const int blocks = per_sm * ctx->num_sms;
+    PropEnv pe;
+    pe.gw = L.gw; pe.gh = L.gh; pe.step = L.step;
+    pe.roi_grid = L.roi_grid;
+    pe.seed_idx = L.seed_idx; pe.seed_solve = L.seed_solve;
+    for (int k = 0; k < 6; ++k) pe.seed_p[k] = L.seed_p[k];
+    pe.seed_corr = L.seed_corr;
+    pe.max_znssd = cfg.propagation_max_znssd;
+    pe.out = L.out;
+    pe.claim = L.claim; pe.key = L.key; pe.order = L.order; pe.counters = L.counters; pe.fetch = L.fetch;
+    pe.barrier = L.barrier; pe.flags = L.flags;
+    const int n = L.gw * L.gh;
+    init_grid_kernel<<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, s>>>(L.out, L.gw, L.gh, L.step);
+    TDIC_CUDA_TRY(cudaGetLastError());
+    void* args[] = {&e, &pe};
+    TDIC_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kern), dim3(blocks), dim3(32 * G * gpb), args,
+                                              smem, s));
+}
+
+template <int OPT, typename T>
+void propagate_deg(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const PropagateLaunch& L, cudaStream_t s) {
+    switch (pair->degree) {
+        case 1: propagate_typed<OPT, 1, T>(ctx, pair, cfg, L, s); break;
+        case 3: propagate_typed<OPT, 3, T>(ctx, pair, cfg, L, s); break;
+        default: propagate_typed<OPT, 5, T>(ctx, pair, cfg, L, s); break;
+    }
+}
+
+}  // namespace
+
+void upload_qk_constants() {
+    double qd[3][36] = {};
+    float qf[3][36] = {};
+    const int degs[3] = {1, 3, 5};
+    for (int s = 0; s < 3; ++s) {
+        build_qk(degs[s], qd[s]);
+        for (int i = 0; i < 36; ++i) qf[s][i] = static_cast<float>(qd[s][i]);
+    }
+    TDIC_CUDA_TRY(cudaMemcpyToSymbol(c_qk_d, qd, sizeof(qd)));
+    TDIC_CUDA_TRY(cudaMemcpyToSymbol(c_qk_f, qf, sizeof(qf)));
+}
+
+void launch_init_grid(const tdic_grid_out& out, int gw, int gh, int step, cudaStream_t s) {
+    const int n = gw * gh;
+    init_grid_kernel<<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, s>>>(out, gw, gh, step);
+    TDIC_CUDA_TRY(cudaGetLastError());
+}
+
+size_t propagate_param_bytes(int precision) {
+    (void)precision;
+    return 6 * sizeof(double);
+}
+
+void launch_solve(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const SolveLaunch& L, cudaStream_t s) {
+    if (L.n <= 0) return;
+    const bool fp64 = pair->precision == TDIC_FP64;
+    if (cfg.optimizer == 1) {
+        if (fp64) solve_deg<1, double>(ctx, pair, cfg, L, s); else solve_deg<1, float>(ctx, pair, cfg, L, s);
+    } else {
+        if (fp64) solve_deg<0, double>(ctx, pair, cfg, L, s); else solve_deg<0, float>(ctx, pair, cfg, L, s);
+    }
+}
+
+void launch_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const PropagateLaunch& L,
+                      cudaStream_t s) {
+    const bool fp64 = pair->precision == TDIC_FP64;
+    if (cfg.optimizer == 1) {
+        if (fp64) propagate_deg<1, double>(ctx, pair, cfg, L, s); else propagate_deg<1, float>(ctx, pair, cfg, L, s);
+    } else {
+        if (fp64) propagate_deg<0, double>(ctx, pair, cfg, L, s); else propagate_deg<0, float>(ctx, pair, cfg, L, s);
+    }
+}
+
+}  // namespace tdic

@@ -1,0 +1,301 @@
+// K5: integer-displacement ZNCC search for seed candidates
+// (IntegerSearchInitializer::estimate_with_interpolators, integer_search.cpp:333-432).
+//
+// Per candidate: a coarse search over every displacement that keeps the subset inside the
+// image, on a pyramid_scale-strided grid with the pyramid_scale-strided circular samples
+// (search_ncorr_multigrid :208-265); a full-sample refinement around the coarse optimum; a
+// full-sample local search over +-search_radius; the local-preference rule (:267-280).  Scores
+// are the circular-subset ZNCC of circular_subset_zncc (:129-166) accumulated in FP64 per
+// position; ties keep the first position in the reference's v-major scan order.
+#include "tdic_internal.cuh"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+
+namespace tdic {
+
+namespace {
+
+constexpr double kEps = 1e-12;
+
+struct CandGeom {
+    int cx, cy;
+    int min_u, max_u, min_v, max_v;  // coarse range
+    int inside;                      // the candidate's subset lies inside the image
+};
+
+struct Best {
+    double z;
+    int idx;
+};
+
+__device__ __forceinline__ bool better(double z, int idx, double bz, int bidx) {
+    // strict '>' in scan order: a larger score wins, equal scores keep the earlier position
+    if (z > bz) return true;
+    if (z == bz && idx < bidx) return true;
+    return false;
+}
+
+// ZNCC of the circular subset at displacement (u, v); -inf when the subset leaves the image or
+// the deformed subset is flat.  Samples: offsets off[0..n), reference values rv, mean rm, norm rn.
+__device__ double zncc_at(const float* __restrict__ def, int w, int h, const short2* off, const double* rv, int n,
+                          double rm, double rn, int cx, int cy, int u, int v) {
+    if (n == 0 || rn <= kEps) return -INFINITY;
+    double dm = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const int x = cx + u + off[i].x, y = cy + v + off[i].y;
+        if (x < 0 || y < 0 || x >= w || y >= h) return -INFINITY;
+        dm += static_cast<double>(__ldg(def + static_cast<size_t>(y) * w + x));
+    }
+    dm /= static_cast<double>(n);
+    double num = 0.0, dn = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double rd = rv[i] - rm;
+        const double dd = static_cast<double>(__ldg(def + static_cast<size_t>(cy + v + off[i].y) * w + cx + u + off[i].x)) - dm;
+        num += rd * dd;
+        dn += dd * dd;
+    }
+    if (dn <= kEps) return -INFINITY;
+    return num / sqrt(rn * dn);
+}
+
+// Reference samples of one candidate into shared memory: values, mean, norm (sum of squares).
+__device__ void load_ref(const float* __restrict__ ref, int w, const short2* off, int n, int cx, int cy, double* rv,
+                         double* stats) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        rv[i] = static_cast<double>(__ldg(ref + static_cast<size_t>(cy + off[i].y) * w + cx + off[i].x));
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int i = 0; i < n; ++i) m += rv[i];
+        m = n > 0 ? m / n : 0.0;
+        double s = 0.0;
+        for (int i = 0; i < n; ++i) { const double d = rv[i] - m; s += d * d; }
+        stats[0] = m;
+        stats[1] = s;
+    }
+    __syncthreads();
+}
+
+__device__ void block_argmax(double& z, int& idx, double* sz, int* si) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const double oz = __shfl_down_sync(0xffffffffu, z, o);
+        const int oi = __shfl_down_sync(0xffffffffu, idx, o);
+        if (better(oz, oi, z, idx)) { z = oz; idx = oi; }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { sz[warp] = z; si[warp] = idx; }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        z = lane < nw ? sz[lane] : -INFINITY;
+        idx = lane < nw ? si[lane] : 0x7fffffff;
+        for (int o = 16; o > 0; o >>= 1) {
+            const double oz = __shfl_down_sync(0xffffffffu, z, o);
+            const int oi = __shfl_down_sync(0xffffffffu, idx, o);
+            if (better(oz, oi, z, idx)) { z = oz; idx = oi; }
+        }
+    }
+    __syncthreads();
+}
+
+// Coarse search: grid.y = candidate, grid.x tiles the coarse positions.
+__global__ void coarse_kernel(const float* __restrict__ ref, const float* __restrict__ def, int w, int h,
+                              const CandGeom* __restrict__ geo, const short2* __restrict__ coff, int cn, int cstep,
+                              Best* __restrict__ partial, int tiles) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    double* rv = reinterpret_cast<double*>(smem);
+    double* stats = rv + cn;
+    double* sz = stats + 2;
+    int* si = reinterpret_cast<int*>(sz + 32);
+    short2* off = reinterpret_cast<short2*>(si + 32);
+    const CandGeom g = geo[blockIdx.y];
+    if (!g.inside) {  // uniform per block: no reference read outside the image
+        if (threadIdx.x == 0) partial[blockIdx.y * tiles + blockIdx.x] = Best{-INFINITY, 0x7fffffff};
+        return;
+    }
+    for (int i = threadIdx.x; i < cn; i += blockDim.x) off[i] = coff[i];
+    __syncthreads();
+    load_ref(ref, w, off, cn, g.cx, g.cy, rv, stats);
+    const int nu = g.max_u >= g.min_u ? (g.max_u - g.min_u) / cstep + 1 : 0;
+    const int nv = g.max_v >= g.min_v ? (g.max_v - g.min_v) / cstep + 1 : 0;
+    const int total = nu * nv;
+    double bz = -INFINITY;
+    int bi = 0x7fffffff;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += tiles * blockDim.x) {
+        const int vi = t / nu, ui = t - vi * nu;
+        const int u = g.min_u + ui * cstep, v = g.min_v + vi * cstep;
+        const double z = zncc_at(def, w, h, off, rv, cn, stats[0], stats[1], g.cx, g.cy, u, v);
+        if (better(z, t, bz, bi)) { bz = z; bi = t; }
+    }
+    block_argmax(bz, bi, sz, si);
+    if (threadIdx.x == 0) partial[blockIdx.y * tiles + blockIdx.x] = Best{bz, bi};
+}
+
+// Full-sample refinement around the coarse optimum and the local +-search window, then the
+// local-preference rule.  One block per candidate.
+__global__ void fine_kernel(const float* __restrict__ ref, const float* __restrict__ def, int w, int h, int r,
+                            const CandGeom* __restrict__ geo, const short2* __restrict__ foff, int fn,
+                            const Best* __restrict__ partial, int tiles, int cstep, int rr, int search, int coarse_ok_all,
+                            const int* __restrict__ coarse_ok, SearchResult* __restrict__ out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    double* rv = reinterpret_cast<double*>(smem);
+    double* stats = rv + fn;
+    double* sz = stats + 2;
+    int* si = reinterpret_cast<int*>(sz + 32);
+    short2* off = reinterpret_cast<short2*>(si + 32);
+    __shared__ double s_cz;
+    __shared__ int s_cu, s_cv;
+    const CandGeom g = geo[blockIdx.x];
+    if (!g.inside) {
+        if (threadIdx.x == 0) out[blockIdx.x] = SearchResult{0, 0, -INFINITY, 0};
+        return;
+    }
+    for (int i = threadIdx.x; i < fn; i += blockDim.x) off[i] = foff[i];
+    __syncthreads();
+    load_ref(ref, w, off, fn, g.cx, g.cy, rv, stats);
+    const bool full_ok = !(fn == 0 || stats[1] <= kEps);
+    // coarse winner
+    if (threadIdx.x == 0) {
+        double z = -INFINITY;
+        int idx = 0x7fffffff;
+        const bool have = coarse_ok_all && coarse_ok[blockIdx.x] && g.min_u <= g.max_u && g.min_v <= g.max_v;
+        if (have)
+            for (int b = 0; b < tiles; ++b) {
+                const Best c = partial[blockIdx.x * tiles + b];
+                if (better(c.z, c.idx, z, idx)) { z = c.z; idx = c.idx; }
+            }
+        const int nu = g.max_u >= g.min_u ? (g.max_u - g.min_u) / cstep + 1 : 1;
+        s_cz = have ? z : -INFINITY;
+        if (have && idx != 0x7fffffff) {
+            s_cu = g.min_u + (idx % nu) * cstep;
+            s_cv = g.min_v + (idx / nu) * cstep;
+        } else {
+            s_cu = 0;
+            s_cv = 0;
+        }
+    }
+    __syncthreads();
+    double best_z = s_cz;
+    int best_u = s_cu, best_v = s_cv;
+    bool have_global = coarse_ok_all && coarse_ok[blockIdx.x] && g.min_u <= g.max_u && g.min_v <= g.max_v;
+    if (have_global && isfinite(best_z) && full_ok) {
+        const int u0 = max(g.min_u, s_cu - rr), u1 = min(g.max_u, s_cu + rr);
+        const int v0 = max(g.min_v, s_cv - rr), v1 = min(g.max_v, s_cv + rr);
+        const int nu = u1 - u0 + 1, nv = v1 - v0 + 1;
+        double bz = -INFINITY;
+        int bi = 0x7fffffff;
+        for (int t = threadIdx.x; t < nu * nv; t += blockDim.x) {
+            const int u = u0 + t % nu, v = v0 + t / nu;
+            const int x = g.cx + u, y = g.cy + v;
+            if (!(x - r >= 0 && y - r >= 0 && x + r < w && y + r < h)) continue;
+            const double z = zncc_at(def, w, h, off, rv, fn, stats[0], stats[1], g.cx, g.cy, u, v);
+            if (better(z, t, bz, bi)) { bz = z; bi = t; }
+        }
+        block_argmax(bz, bi, sz, si);
+        if (threadIdx.x == 0) {
+            s_cz = bz;
+            if (bi != 0x7fffffff) { s_cu = u0 + bi % nu; s_cv = v0 + bi / nu; } else { s_cu = 0; s_cv = 0; }
+        }
+        __syncthreads();
+        best_z = s_cz;
+        best_u = s_cu;
+        best_v = s_cv;
+    } else if (!isfinite(best_z)) {
+        best_u = s_cu;
+        best_v = s_cv;
+    }
+    __syncthreads();
+    if (search > 0 && full_ok) {
+        const int n1 = 2 * search + 1;
+        double bz = -INFINITY;
+        int bi = 0x7fffffff;
+        for (int t = threadIdx.x; t < n1 * n1; t += blockDim.x) {
+            const int u = -search + t % n1, v = -search + t / n1;
+            const int x = g.cx + u, y = g.cy + v;
+            if (!(x - r >= 0 && y - r >= 0 && x + r < w && y + r < h)) continue;
+            const double z = zncc_at(def, w, h, off, rv, fn, stats[0], stats[1], g.cx, g.cy, u, v);
+            if (better(z, t, bz, bi)) { bz = z; bi = t; }
+        }
+        block_argmax(bz, bi, sz, si);
+        if (threadIdx.x == 0) {
+            const int lu = bi != 0x7fffffff ? -search + bi % n1 : 0;
+            const int lv = bi != 0x7fffffff ? -search + bi / n1 : 0;
+            // prefer_local_when_ambiguous
+            if (!isfinite(bz)) {
+            } else if (!isfinite(best_z)) { best_z = bz; best_u = lu; best_v = lv; }
+            else if (bz + 0.02 >= best_z) { best_z = bz; best_u = lu; best_v = lv; }
+            out[blockIdx.x] = SearchResult{best_u, best_v, best_z, (isfinite(best_z) && full_ok) ? 1 : 0};
+        }
+    } else if (threadIdx.x == 0) {
+        out[blockIdx.x] = SearchResult{best_u, best_v, best_z, (isfinite(best_z) && full_ok) ? 1 : 0};
+    }
+}
+
+std::vector<short2> circle_offsets(int r, int step) {
+    std::vector<short2> o;
+    step = step < 1 ? 1 : step;
+    for (int dy = -r; dy <= r; dy += step)
+        for (int dx = -r; dx <= r; dx += step)
+            if (dx * dx + dy * dy <= r * r) o.push_back(make_short2(static_cast<short>(dx), static_cast<short>(dy)));
+    return o;
+}
+
+}  // namespace
+
+void integer_search_batch(tdic_ctx* ctx, tdic_pair* lazy, const tdic_config& cfg, const int* cx, const int* cy, int n,
+                          SearchResult* out_host, cudaStream_t s) {
+    if (n <= 0) return;
+    const int w = lazy->w, h = lazy->h;
+    const int r = cfg.is_subset_radius < 1 ? 1 : cfg.is_subset_radius;
+    const int search = cfg.is_search_radius < 0 ? 0 : cfg.is_search_radius;
+    const int cstep = cfg.pyramid_enabled ? (cfg.pyramid_scale < 1 ? 1 : cfg.pyramid_scale) : 1;
+    int rr = cfg.pyramid_refinement_radius < 1 ? 1 : cfg.pyramid_refinement_radius;
+    rr = std::max(rr, static_cast<int>(std::ceil(1.5 * static_cast<double>(r))));
+    rr = std::max(rr, cstep);
+    const auto foff = circle_offsets(r, 1);
+    const auto coff = circle_offsets(r, cstep);
+    std::vector<CandGeom> geo(n);
+    std::vector<int> ok(n, 0);
+    for (int i = 0; i < n; ++i) {
+        geo[i].cx = cx[i];
+        geo[i].cy = cy[i];
+        geo[i].min_u = r - cx[i];
+        geo[i].max_u = w - 1 - r - cx[i];
+        geo[i].min_v = r - cy[i];
+        geo[i].max_v = h - 1 - r - cy[i];
+        ok[i] = (cx[i] - r >= 0 && cy[i] - r >= 0 && cx[i] + r < w && cy[i] + r < h) ? 1 : 0;
+        geo[i].inside = ok[i];
+    }
+    // A flat coarse subset (coarse_ref_norm <= eps) yields -inf in coarse_kernel, the reference's
+    // outcome of skipping the multigrid stage (integer_search.cpp:381-397).
+    const std::vector<int>& cok = ok;
+    Buffer d_geo(&ctx->pool, sizeof(CandGeom) * n), d_coff(&ctx->pool, sizeof(short2) * coff.size()),
+        d_foff(&ctx->pool, sizeof(short2) * foff.size()), d_cok(&ctx->pool, sizeof(int) * n),
+        d_out(&ctx->pool, sizeof(SearchResult) * n);
+    const int tiles = 64;
+    Buffer d_part(&ctx->pool, sizeof(Best) * static_cast<size_t>(tiles) * n);
+    TDIC_CUDA_TRY(cudaMemcpyAsync(d_geo.ptr, geo.data(), sizeof(CandGeom) * n, cudaMemcpyHostToDevice, s));
+    TDIC_CUDA_TRY(cudaMemcpyAsync(d_coff.ptr, coff.data(), sizeof(short2) * coff.size(), cudaMemcpyHostToDevice, s));
+    TDIC_CUDA_TRY(cudaMemcpyAsync(d_foff.ptr, foff.data(), sizeof(short2) * foff.size(), cudaMemcpyHostToDevice, s));
+    TDIC_CUDA_TRY(cudaMemcpyAsync(d_cok.ptr, cok.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    const size_t csm = sizeof(double) * (coff.size() + 2 + 32) + sizeof(int) * 32 + sizeof(short2) * coff.size() + 16;
+    const size_t fsm = sizeof(double) * (foff.size() + 2 + 32) + sizeof(int) * 32 + sizeof(short2) * foff.size() + 16;
+    TDIC_CUDA_TRY(cudaFuncSetAttribute(coarse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(csm)));
+    TDIC_CUDA_TRY(cudaFuncSetAttribute(fine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(fsm)));
+    coarse_kernel<<<dim3(tiles, n), 256, csm, s>>>(lazy->ref.as<float>(), lazy->def_f.as<float>(), w, h,
+                                                   d_geo.as<CandGeom>(), d_coff.as<short2>(), static_cast<int>(coff.size()),
+                                                   cstep, d_part.as<Best>(), tiles);
+    TDIC_CUDA_TRY(cudaGetLastError());
+    fine_kernel<<<n, 256, fsm, s>>>(lazy->ref.as<float>(), lazy->def_f.as<float>(), w, h, r, d_geo.as<CandGeom>(),
+                                    d_foff.as<short2>(), static_cast<int>(foff.size()), d_part.as<Best>(), tiles, cstep, rr,
+                                    search, 1, d_cok.as<int>(), d_out.as<SearchResult>());
+    TDIC_CUDA_TRY(cudaGetLastError());
+    TDIC_CUDA_TRY(cudaMemcpyAsync(out_host, d_out.ptr, sizeof(SearchResult) * n, cudaMemcpyDeviceToHost, s));
+    TDIC_CUDA_TRY(cudaStreamSynchronize(s));
+    for (int i = 0; i < n; ++i)
+        if (!ok[i]) out_host[i] = SearchResult{0, 0, -INFINITY, 0};
+}
+
+}  // namespace tdic

@@ -1,0 +1,162 @@
+// Internal declarations shared by the translation units of libtdic_gb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/tdic_gb300.h"
+
+namespace tdic {
+
+// ---------------------------------------------------------------------------------------
+// Errors: every CUDA call is checked; the first failure is recorded on the context and
+// turned into a tdic_status.  Nothing throws across the C ABI.
+// ---------------------------------------------------------------------------------------
+struct Error {
+    tdic_status code;
+    std::string msg;
+};
+
+#define TDIC_CUDA_TRY(expr)                                                                  \
+    do {                                                                                     \
+        cudaError_t e_ = (expr);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            throw ::tdic::Error{TDIC_CUDA_ERROR, std::string(#expr) + ": " + cudaGetErrorString(e_)}; \
+        }                                                                                    \
+    } while (0)
+
+#define TDIC_REQUIRE(cond, code, text)                                                       \
+    do {                                                                                     \
+        if (!(cond)) throw ::tdic::Error{(code), (text)};                                    \
+    } while (0)
+
+// ---------------------------------------------------------------------------------------
+// Caching device-memory pool: blocks are kept after release and reused by size class, so a
+// steady stream of pairs / propagations does no cudaMalloc after warm-up.
+// ---------------------------------------------------------------------------------------
+class DevicePool {
+public:
+    void* acquire(size_t bytes);
+    void release(void* p);
+    void trim();
+    size_t held_bytes() const { return held_; }
+    ~DevicePool() { trim(); }
+
+private:
+    static size_t size_class(size_t bytes);
+    std::multimap<size_t, void*> free_;
+    std::map<void*, size_t> live_;
+    size_t held_ = 0;
+};
+
+struct Buffer {
+    DevicePool* pool = nullptr;
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    Buffer() = default;
+    Buffer(DevicePool* p, size_t b) : pool(p), ptr(b ? p->acquire(b) : nullptr), bytes(b) {}
+    Buffer(const Buffer&) = delete;
+    Buffer& operator=(const Buffer&) = delete;
+    Buffer(Buffer&& o) noexcept { *this = std::move(o); }
+    Buffer& operator=(Buffer&& o) noexcept {
+        reset();
+        pool = o.pool; ptr = o.ptr; bytes = o.bytes;
+        o.ptr = nullptr; o.bytes = 0;
+        return *this;
+    }
+    ~Buffer() { reset(); }
+    void reset() {
+        if (ptr && pool) pool->release(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    template <typename T> T* as() const { return static_cast<T*>(ptr); }
+};
+
+// Circular-subset sample offsets (dx, dy) in the reference's row-major order
+// (icgn.cpp:484-510: dy outer, dx inner, dx^2 + dy^2 <= r^2), one table per radius.
+struct SampleTable {
+    Buffer offsets;  // short2[n]
+    int n = 0;
+};
+
+}  // namespace tdic
+
+struct tdic_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::recursive_mutex mu;
+    std::string last_error;
+    tdic::DevicePool pool;
+    std::map<int, tdic::SampleTable> tables;
+    // Pairs hold device memory of this context's pool: the context outlives its pairs.
+    // tdic_ctx_destroy with live pairs only marks the context; the last tdic_pair_destroy frees it.
+    int live_pairs = 0;
+    bool destroy_requested = false;
+};
+
+struct tdic_pair {
+    tdic_ctx* ctx = nullptr;
+    int w = 0, h = 0, border = 3, degree = 3, precision = 0, exact = 1;
+    int cw = 0, ch = 0;        // coefficient image size (w + 2B) x (h + 2B)
+    tdic::Buffer ref;          // float32 H x W reference (dic::Image stores float)
+    tdic::Buffer coef;         // T (cw x ch) coefficients of the deformed image
+    tdic::Buffer rowtmp;       // T (h x cw) row-pass intermediate
+    tdic::Buffer def_f;        // float32 H x W deformed (kept for seed search)
+    tdic::Buffer staging;      // raw input staging for host uploads
+};
+
+namespace tdic {
+
+// B-spline local polynomial matrix qk (bspline.cpp:320-340) for degree 1, 3, 5.
+void build_qk(int degree, double* qk);
+
+const SampleTable& sample_table(tdic_ctx* ctx, int radius);
+
+// Kernel launchers (prefilter.cu) --------------------------------------------------------
+void launch_convert(const void* src, int w, int h, int pitch, tdic_dtype dtype, float* dst, cudaStream_t s);
+void launch_prefilter(tdic_pair* pair, const float* image, cudaStream_t s);
+void launch_reference_gradient(const float* img, int w, int h, double* gx, double* gy, cudaStream_t s);
+
+// Hot path (hotpath.cu) -------------------------------------------------------------------
+struct SolveLaunch {
+    const tdic_poi_in* in;
+    tdic_poi_out* out;
+    int n;
+    int* fetch;  // work counter (zeroed by the launcher)
+};
+void launch_solve(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const SolveLaunch& L, cudaStream_t s);
+
+struct PropagateLaunch {
+    int gw, gh, step;
+    const uint8_t* roi_grid;   // gw*gh admission by ROI at grid points (1 = valid)
+    // seed
+    int seed_idx;              // grid index of the aligned seed
+    int seed_solve;            // 1 when the aligned point differs from the raw seed
+    double seed_p[6];
+    double seed_corr;
+    // outputs (device SoA; NULL entries skipped)
+    tdic_grid_out out;
+    // scratch
+    int* claim; unsigned long long* key; void* params; int* order; int* counters; int* fetch;
+    unsigned int* barrier;  // [count, generation]
+    int* flags;             // [error, no_seed, accepted]
+};
+void launch_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const PropagateLaunch& L,
+                      cudaStream_t s);
+size_t propagate_param_bytes(int precision);
+void launch_init_grid(const tdic_grid_out& out, int gw, int gh, int step, cudaStream_t s);
+
+// Seed search (seed.cu) -------------------------------------------------------------------
+struct SearchResult { int u, v; double zncc; int ok; };
+void integer_search_batch(tdic_ctx* ctx, tdic_pair* lazy, const tdic_config& cfg, const int* cx, const int* cy,
+                          int n, SearchResult* out, cudaStream_t s);
+
+}  // namespace tdic
