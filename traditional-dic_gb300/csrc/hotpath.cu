@@ -8,9 +8,11 @@
 // separable weights w_m(t) = sum_r qk[r][m] t^r (qk of bspline.cpp:320-340, so the value equals
 // the reference's local polynomial block evaluation, bspline.cpp:96-113/153-175), and reduces
 // the ZNSSD residual and J^T r across the group with warp shuffles.  Precision of the FP32-mixed
-// build: interpolation and residual arithmetic in float with Kahan-compensated normalisation
-// sums; the 6x6 Hessian factorisation / inverse and the normalisation scalars in double.  The
-// FP64 build is the same code with every T = double.
+// build: interpolation, residual and the 6x6 algebra in float with Kahan-compensated
+// normalisation sums whose totals are combined in double.  On GB300 an FP64 instruction holds
+// an SMSP's FP64 unit ~64 cycles and a double divide ~670 cycles, so FP64 is kept off the
+// per-iteration path; the Hessian is an FP32-accumulated sum, so factorising it in FP64 would
+// add cost but no accuracy.  The FP64 build is the same code with every T = double.
 #include "tdic_internal.cuh"
 
 #include <cmath>
@@ -115,6 +117,7 @@ template <typename T> __device__ __forceinline__ bool finite6(const T* p) {
 template <typename M>
 struct Ldlt6 {
     M m[6][6];
+    M dinv[6];  // reciprocal of each pivot (0 where |D_ii| is below DBL_MIN)
     int t[6];
     int sign;  // 0 zero, 1 positive semidefinite, 2 negative semidefinite, 3 indefinite
     bool ok;
@@ -155,12 +158,13 @@ struct Ldlt6 {
             const bool pivot_valid = fabs(akk) > M(0);
             if (k == 0 && !pivot_valid) {
                 sign = 0;
-                for (int j = 0; j < 6; ++j) { t[j] = j; for (int i = 0; i < 6; ++i) m[i][j] = M(0); }
+                for (int j = 0; j < 6; ++j) { t[j] = j; dinv[j] = M(0); for (int i = 0; i < 6; ++i) m[i][j] = M(0); }
                 ok = true;
                 return;
             }
             if (pivot_valid) {
-                for (int i = k + 1; i < 6; ++i) m[i][k] /= akk;
+                const M r = M(1) / akk;
+                for (int i = k + 1; i < 6; ++i) m[i][k] *= r;
             } else {
                 for (int i = k + 1; i < 6; ++i) ok = ok && (m[i][k] == M(0));
             }
@@ -170,16 +174,14 @@ struct Ldlt6 {
             else if (sign == 2) { if (akk > M(0)) sign = 3; }
             else if (sign == 0) { if (akk > M(0)) sign = 1; else if (akk < M(0)) sign = 2; }
         }
+        for (int i = 0; i < 6; ++i) dinv[i] = fabs(m[i][i]) > M(2.2250738585072014e-308) ? M(1) / m[i][i] : M(0);
     }
     __device__ bool good() const { return ok && (sign == 1 || sign == 0); }
     __device__ void solve(const M (&b)[6], M (&x)[6]) const {
         for (int i = 0; i < 6; ++i) x[i] = b[i];
         for (int k = 0; k < 6; ++k) { const M v = x[k]; x[k] = x[t[k]]; x[t[k]] = v; }
         for (int i = 0; i < 6; ++i) { M s = x[i]; for (int j = 0; j < i; ++j) s -= m[i][j] * x[j]; x[i] = s; }
-        for (int i = 0; i < 6; ++i) {
-            const M d = m[i][i];
-            x[i] = fabs(d) > M(2.2250738585072014e-308) ? x[i] / d : M(0);
-        }
+        for (int i = 0; i < 6; ++i) x[i] *= dinv[i];
         for (int i = 5; i >= 0; --i) { M s = x[i]; for (int j = i + 1; j < 6; ++j) s -= m[j][i] * x[j]; x[i] = s; }
         for (int k = 5; k >= 0; --k) { const M v = x[k]; x[k] = x[t[k]]; x[t[k]] = v; }
     }
@@ -195,12 +197,15 @@ __device__ __forceinline__ void ic_update(const M (&p)[6], const M (&dp)[6], M (
         for (int i = 0; i < 6; ++i) o[i] = M(NAN);
         return;
     }
-    o[0] = du - ((dudx + M(1)) * (dp0 + dp0 * dp5 - dp1 * dp3)) / den - (dudy * (dp1 - dp0 * dp4 + dp1 * dp2)) / den;
-    o[1] = dv - ((dvdy + M(1)) * (dp1 - dp0 * dp4 + dp1 * dp2)) / den - (dvdx * (dp0 + dp0 * dp5 - dp1 * dp3)) / den;
-    o[2] = ((dp5 + M(1)) * (dudx + M(1))) / den - (dp4 * dudy) / den - M(1);
-    o[3] = (dudy * (dp2 + M(1))) / den - (dp3 * (dudx + M(1))) / den;
-    o[4] = (dvdx * (dp5 + M(1))) / den - (dp4 * (dvdy + M(1))) / den;
-    o[5] = ((dp2 + M(1)) * (dvdy + M(1))) / den - (dp3 * dvdx) / den - M(1);
+    // one reciprocal instead of twelve divisions (same closed form, rounding differs by ~1 ulp)
+    const M r = M(1) / den;
+    const M a = dp0 + dp0 * dp5 - dp1 * dp3, b = dp1 - dp0 * dp4 + dp1 * dp2;
+    o[0] = du - ((dudx + M(1)) * a) * r - (dudy * b) * r;
+    o[1] = dv - ((dvdy + M(1)) * b) * r - (dvdx * a) * r;
+    o[2] = ((dp5 + M(1)) * (dudx + M(1))) * r - (dp4 * dudy) * r - M(1);
+    o[3] = (dudy * (dp2 + M(1))) * r - (dp3 * (dudx + M(1))) * r;
+    o[4] = (dvdx * (dp5 + M(1))) * r - (dp4 * (dvdy + M(1))) * r;
+    o[5] = ((dp2 + M(1)) * (dvdy + M(1))) * r - (dp3 * dvdx) * r - M(1);
 }
 
 // forward_gauss_newton.cpp:64-76
@@ -250,6 +255,7 @@ struct Env {
     const short2* off;     // sample offsets
     int max_iter;
     double thr;
+    double inv_n;          // 1 / n
 };
 
 struct Result {
@@ -272,7 +278,10 @@ __device__ __forceinline__ void result_init(Result& r, const double (&p0)[6], do
     r.conv = false;
 }
 
-template <typename T> struct MixedOf { using type = double; };
+// Per-iteration scalar type: the FP32-mixed build keeps the 6x6 inverse, the parameter
+// vector and its update in float (FP64 stays in the setup factorisation / inverse and in the
+// combine of the normalisation sums); the FP64 build is double throughout.
+template <typename T> struct MixedOf { using type = T; };
 
 // Warp the samples of this thread, interpolate, store g (and for FGN its gradient) and
 // accumulate the shifted normalisation sums.  Returns false if a warped point left the image.
@@ -336,8 +345,9 @@ __device__ __forceinline__ bool warp_interp(const Env<T>& e, int cx, int cy, con
 // sm: 4 * nmax T values of this group; red: G * 32 T values; flag: one int.
 template <int OPT, int DEG, typename T, int G>
 __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6], double conf, T* sm, T* red,
-                          int* flag, typename MixedOf<T>::type* s_hinv, int tid, int bar_id, Result& R) {
+                          int* flag, double* s_hinv_raw, int tid, int bar_id, Result& R) {
     using M = typename MixedOf<T>::type;
+    M* s_hinv = reinterpret_cast<M*>(s_hinv_raw);
     constexpr int NT = 32 * G;
     result_init(R, p0, conf);
     const int r = e.radius;
@@ -371,8 +381,8 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
     }
     T v1[1] = {ksum.value()};
     group_sum<G, 1>(v1, red, tid, bar_id);
-    const double N = static_cast<double>(e.n);
-    const double mean = static_cast<double>(v1[0]) / N;
+    const double inv_n = e.inv_n;  // 1 / N, from the host (no device-side FP64 divide)
+    const double mean = static_cast<double>(v1[0]) * inv_n;
     const T fm = T(mean);
     Kahan<T> knorm;
     for (int i = tid; i < e.n; i += NT) {
@@ -381,9 +391,9 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
     }
     v1[0] = knorm.value();
     group_sum<G, 1>(v1, red, tid, bar_id);
-    const double norm = sqrt(static_cast<double>(v1[0]));
-    if (norm <= kEps) { R.status = TDIC_NUMERICAL_FAILURE; return; }
-    const T inv_norm = T(1.0 / norm);
+    const double ss = static_cast<double>(v1[0]);  // sum (f - mean)^2
+    if (!(ss > kEps * kEps)) { R.status = TDIC_NUMERICAL_FAILURE; return; }  // |f - mean| <= 1e-12
+    const T inv_norm = T(1) / sqrt(T(ss));
 
     if constexpr (OPT == 0) {
         // normalised reference and Hessian sums: H = (2/|f|^2) sum SD SD^T with
@@ -413,10 +423,10 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
         Hm[3][3] = S(0, 5); Hm[3][4] = S(1, 4); Hm[3][5] = S(1, 5);
         Hm[4][4] = S(2, 3); Hm[4][5] = S(2, 4);
         Hm[5][5] = S(2, 5);
-        const M hsc = M(2.0 / (norm * norm));
+        const M hsc = M(2) * inv_norm * inv_norm;
         for (int i = 0; i < 6; ++i)
             for (int j = i; j < 6; ++j) { Hm[i][j] *= hsc; Hm[j][i] = Hm[i][j]; }
-        Ldlt6<M> f;
+        Ldlt6<M> f;  // once per POI
         f.factor(Hm);
         if (!f.good()) { R.status = TDIC_NUMERICAL_FAILURE; return; }
         // explicit inverse, column by column (the reference's per-iteration solves applied to
@@ -437,7 +447,7 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
     for (int k = 0; k < 6; ++k) p[k] = static_cast<M>(p0[k]);
     double corr = INFINITY;
     bool converged = false;
-    const M gscale = M(2.0 / norm);
+    const M gscale = M(2) * inv_norm;
     for (int it = 0; it < e.max_iter; ++it) {
         R.iters = it + 1;
         T pt[6];
@@ -448,11 +458,14 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
         if (group_any<G>(!ok, flag, tid, bar_id)) { R.status = TDIC_INVALID_INPUT; return; }
         T v2[2] = {sg.value(), sg2.value()};
         group_sum<G, 2>(v2, red, tid, bar_id);
-        const double gmr = static_cast<double>(v2[0]) / N;                 // mean of g - fm
-        const double var = static_cast<double>(v2[1]) - static_cast<double>(v2[0]) * gmr;
-        const double gn = sqrt(var > 0.0 ? var : 0.0);
-        if (gn <= kEps) { R.status = TDIC_NUMERICAL_FAILURE; return; }
-        const T gsh = T(gmr), inv_gn = T(1.0 / gn);
+        // normalisation sums combined in FP64: mean of (g - fm) and sum (g - mean)^2
+        const double gmr = static_cast<double>(v2[0]) * inv_n;
+        const double var = fma(-static_cast<double>(v2[0]), gmr, static_cast<double>(v2[1]));
+        if (!(var > kEps * kEps)) { R.status = TDIC_NUMERICAL_FAILURE; return; }  // |g - mean| <= 1e-12
+        const T gsh = T(gmr);
+        T inv_gn;
+        if constexpr (sizeof(T) == 4) inv_gn = 1.0f / sqrtf(static_cast<float>(var));
+        else inv_gn = T(1.0 / sqrt(var));
         M dp[6];
         if constexpr (OPT == 0) {
             T q[7];
@@ -510,12 +523,12 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
             Hm[3][3] = S(0, 5); Hm[3][4] = S(1, 4); Hm[3][5] = S(1, 5);
             Hm[4][4] = S(2, 3); Hm[4][5] = S(2, 4);
             Hm[5][5] = S(2, 5);
-            const M hsc = M(2.0 / (norm * norm));
+            const M hsc = M(2) * inv_norm * inv_norm;
             for (int i = 0; i < 6; ++i)
                 for (int j = i; j < 6; ++j) { Hm[i][j] *= hsc; Hm[j][i] = Hm[i][j]; }
             M grad[6];
             for (int k = 0; k < 6; ++k) grad[k] = static_cast<M>(q[18 + k]) * gscale;
-            Ldlt6<M> f;
+            Ldlt6<M> f;  // FGN refactorises every iteration
             f.factor(Hm);
             if (!f.good()) { R.status = TDIC_NUMERICAL_FAILURE; return; }
             f.solve(grad, dp);
@@ -717,7 +730,7 @@ __device__ void expand(const PropEnv& pe, int w, int h, int radius, int n, doubl
 }
 
 template <int OPT, int DEG, typename T, int G>
-__global__ void propagate_kernel(Env<T> e, PropEnv pe) {
+__global__ void __launch_bounds__(256, 2) propagate_kernel(Env<T> e, PropEnv pe) {
     using P = typename MixedOf<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int gi = threadIdx.x / (32 * G), tid = threadIdx.x % (32 * G);
@@ -832,6 +845,7 @@ Env<T> make_env(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, int radi
     e.off = tab.offsets.as<short2>();
     e.max_iter = max_iter;
     e.thr = thr;
+    e.inv_n = tab.n > 0 ? 1.0 / tab.n : 0.0;
     (void)cfg;
     return e;
 }
@@ -866,10 +880,15 @@ void solve_deg(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const Sol
     }
 }
 
+// Propagation groups: 4 warps per POI (the wave front is narrow, so per-POI latency, not
+// throughput, bounds a wave), 2 groups per CTA.
+constexpr int kPropG = 4;
+constexpr int kPropGroupsPerBlock = 2;
+
 template <int OPT, int DEG, typename T>
 void propagate_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const PropagateLaunch& L, cudaStream_t s) {
-    constexpr int G = 1;
-    constexpr int gpb = 4;
+    constexpr int G = kPropG;
+    constexpr int gpb = kPropGroupsPerBlock;
     Env<T> e = make_env<T>(ctx, pair, cfg, cfg.subset_radius, cfg.max_iterations, cfg.convergence_threshold);
     const size_t smem = gpb * group_smem_bytes<T>(e.nmax, G);
     auto kern = propagate_kernel<OPT, DEG, T, G>;
