@@ -41,7 +41,7 @@ WORKLOAD = {
     "workload": "synthetic speckle 2048x2048 uint8, sinusoidal u/v, radius 15, POI step 5 (BASELINE config 2)",
     "image": [2048, 2048], "dtype_in": "uint8", "subset_radius": 15, "poi_step": 5, "grid": [410, 410],
     "bspline_degree": 3, "threshold": 1e-3, "max_iterations": 20, "shape_function": "first_order",
-    "optimizer": "icgn", "propagation": "frontier waves", "l2": "flushed (256 MB write) between timed steps",
+    "optimizer": "icgn", "l2": "flushed (256 MB write) between timed steps",
 }
 CONFIG = {
     "subset": {"radius": 15},
@@ -231,6 +231,7 @@ def run_ours(args, world, rank, local, pg):
     h, w = pair_np.reference.shape
     cfg = S.config_from_dict(CONFIG)
     cfg.precision = L.FP64 if args.precision == "fp64" else L.FP32_MIXED
+    cfg.propagation_mode = S.PROPAGATION_MODES[args.mode]
     r = cfg.subset_radius
     stream = torch.cuda.Stream(device=dev)
     sptr = stream.cuda_stream
@@ -249,7 +250,8 @@ def run_ours(args, world, rank, local, pg):
 
     # Seed from the reference initializer (tdic_select_seed), once, untimed: it is an input of
     # the hot path.  The e2e leg below re-runs it every step.
-    _, seed = S.compute(pair_np.reference, pair_np.deformed, dict(CONFIG, gpu={"precision": args.precision}),
+    gpu_cfg = {"precision": args.precision, "propagation": args.mode}
+    _, seed = S.compute(pair_np.reference, pair_np.deformed, dict(CONFIG, gpu=gpu_cfg),
                         context=ctx, return_seed=True)
     assert seed.found, "no seed found"
     pair = S.Pair(ctx, ref_d, def_d, degree=3, precision=cfg.precision, stream=stream)
@@ -310,8 +312,7 @@ def run_ours(args, world, rank, local, pg):
     res32 = {k: outs[k].cpu().numpy().copy() for k in ("u", "v", "valid", "converged", "zncc")}
     fp64 = None
     if args.precision == "fp32" and not args.skip_fp64:
-        cfg64 = S.config_from_dict(CONFIG)
-        cfg64.precision = L.FP64
+        cfg64 = S.config_from_dict(dict(CONFIG, gpu={"precision": "fp64", "propagation": args.mode}))
         pair64 = S.Pair(ctx, ref_d, def_d, degree=3, precision=L.FP64, stream=stream)
         t64 = []
         for i in range(2):
@@ -344,7 +345,7 @@ def run_ours(args, world, rank, local, pg):
     ref_pin = torch.from_numpy(pair_np.reference).pin_memory()
     def_pin = torch.from_numpy(pair_np.deformed).pin_memory()
     ref_h, def_h = ref_pin.numpy(), def_pin.numpy()
-    e2e_cfg = dict(CONFIG, gpu={"precision": args.precision})
+    e2e_cfg = dict(CONFIG, gpu=gpu_cfg)
     S.compute(ref_h, def_h, e2e_cfg, context=ctx)
     barrier(pg)
     t0 = time.perf_counter()
@@ -377,7 +378,7 @@ def run_ours(args, world, rank, local, pg):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64 (mixed)" if args.precision == "fp32" else "f64",
-            "data": "synthetic", "config": dict(WORKLOAD, precision=args.precision,
+            "data": "synthetic", "config": dict(WORKLOAD, precision=args.precision, propagation=args.mode,
                                                   parallelism=f"replicas x{world}" if world > 1 else "1 GPU"),
             "converged_pois_per_step": conv,
             "roofline": roofline,
@@ -404,6 +405,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--mode", default="dataflow", choices=["dataflow", "waves"])
     ap.add_argument("--ref-solves", type=int, default=20000)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")

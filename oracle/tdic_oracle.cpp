@@ -582,7 +582,8 @@ int nearest_grid_index(int c, int step, int limit) {  // reliability_propagation
 
 float corr_key(double c) { return static_cast<float>(c); }
 
-// reliability_propagation.cpp:130-394 (mode 1, heap order) and the frontier-wave rule (mode 0).
+// reliability_propagation.cpp:130-394 (mode 1, heap order), the frontier-wave rule (mode 0) and
+// the dataflow order with frontier-wave cleanup (mode 2).
 int propagate(const float* ref, int w, int h, const uint8_t* roi, const GradSource& gs, const Spline& sp,
               const orc_config& c, const orc_seed& seed, int max_solves, orc_grid_out* out, int* solves_done) {
     int solves = 0;
@@ -673,64 +674,122 @@ int propagate(const float* ref, int w, int h, const uint8_t* roi, const GradSour
             }
         }
     } else {
-        // Frontier waves: every unclaimed, admissible 4-neighbour of the wave-w accepted set
-        // is solved in wave w+1 from the parent with the lowest (float) ZNSSD, ties to the
-        // lowest parent grid index.
-        std::vector<int> frontier{sidx};
-        std::vector<double> fcorr{std::max(0.0, aligned.correlation)};
         std::vector<int> best_parent(static_cast<std::size_t>(gw) * gh, -1);
         std::vector<float> best_key(static_cast<std::size_t>(gw) * gh, 0.0f);
         std::vector<double> pp(static_cast<std::size_t>(gw) * gh * 6, 0.0);
+        std::vector<double> pcorr(static_cast<std::size_t>(gw) * gh, 0.0);
         for (int k = 0; k < 6; ++k) pp[static_cast<std::size_t>(sidx) * 6 + k] = aligned.p[k];
-        while (!frontier.empty()) {
-            std::vector<int> next;
-            for (std::size_t fi = 0; fi < frontier.size(); ++fi) {
-                const int pidx = frontier[fi];
-                const int popx = (pidx % gw) * step, popy = (pidx / gw) * step;
-                const float key = corr_key(fcorr[fi]);
-                for (int n = 0; n < 4; ++n) {
-                    int nx, ny, nidx;
-                    const int offs[4][2] = {{0, -step}, {step, 0}, {0, step}, {-step, 0}};
-                    nx = popx + offs[n][0]; ny = popy + offs[n][1];
-                    if (nx < 0 || ny < 0 || nx >= w || ny >= h) continue;
-                    nidx = (ny / step) * gw + nx / step;
-                    if (best_parent[nidx] >= 0) {  // already a candidate of this wave
-                        if (key < best_key[nidx] || (key == best_key[nidx] && pidx < best_parent[nidx])) {
-                            best_key[nidx] = key; best_parent[nidx] = pidx;
+        pcorr[sidx] = std::max(0.0, aligned.correlation);
+        auto solve_from = [&](int nidx, int pidx, orc_poi_result& r, double* p0) {
+            const double* pp0 = &pp[static_cast<std::size_t>(pidx) * 6];
+            const int nx = (nidx % gw) * step, ny = (nidx / gw) * step;
+            const double ddx = nx - (pidx % gw) * step, ddy = ny - (pidx / gw) * step;
+            p0[0] = pp0[0] + pp0[2] * ddx + pp0[3] * ddy;
+            p0[1] = pp0[1] + pp0[4] * ddx + pp0[5] * ddy;
+            p0[2] = pp0[2]; p0[3] = pp0[3]; p0[4] = pp0[4]; p0[5] = pp0[5];
+            r = solve_one(ref, w, h, gs, sp, scfg, nx, ny, p0, 0.0);
+            ++solves;
+        };
+        auto keep = [&](int nidx, const orc_poi_result& r) {
+            store(out, nidx, r);
+            ++computed;
+            for (int k = 0; k < 6; ++k) pp[static_cast<std::size_t>(nidx) * 6 + k] = r.p[k];
+            pcorr[nidx] = r.correlation;
+        };
+        // Frontier waves: every unclaimed, admissible 4-neighbour of the wave-w accepted set
+        // is solved in wave w+1 from the parent with the lowest (float) ZNSSD, ties to the
+        // lowest parent grid index.
+        auto run_waves = [&](std::vector<int> frontier) {
+            while (!frontier.empty()) {
+                std::vector<int> next;
+                for (const int pidx : frontier) {
+                    const int popx = (pidx % gw) * step, popy = (pidx / gw) * step;
+                    const float key = corr_key(pcorr[pidx]);
+                    for (int n = 0; n < 4; ++n) {
+                        int nx, ny, nidx;
+                        const int offs[4][2] = {{0, -step}, {step, 0}, {0, step}, {-step, 0}};
+                        nx = popx + offs[n][0]; ny = popy + offs[n][1];
+                        if (nx < 0 || ny < 0 || nx >= w || ny >= h) continue;
+                        nidx = (ny / step) * gw + nx / step;
+                        if (best_parent[nidx] >= 0) {  // already a candidate of this wave
+                            if (key < best_key[nidx] || (key == best_key[nidx] && pidx < best_parent[nidx])) {
+                                best_key[nidx] = key; best_parent[nidx] = pidx;
+                            }
+                            continue;
                         }
-                        continue;
+                        if (!try_neighbor(popx, popy, n, nx, ny, nidx)) continue;
+                        best_parent[nidx] = pidx; best_key[nidx] = key;
+                        next.push_back(nidx);
                     }
-                    if (!try_neighbor(popx, popy, n, nx, ny, nidx)) continue;
-                    best_parent[nidx] = pidx; best_key[nidx] = key;
-                    next.push_back(nidx);
+                }
+                std::vector<int> acc;
+                for (int nidx : next) {
+                    calc[nidx] = 1;
+                    if (max_solves >= 0 && solves >= max_solves) continue;
+                    orc_poi_result r;
+                    double p0[6];
+                    solve_from(nidx, best_parent[nidx], r, p0);
+                    if (accept(r, p0[0], p0[1])) {
+                        keep(nidx, r);
+                        acc.push_back(nidx);
+                    }
+                }
+                for (int nidx : next) best_parent[nidx] = -2;  // resolved; never a candidate again
+                frontier.swap(acc);
+            }
+        };
+        if (c.propagation_mode == 2) {
+            // Dataflow order: every grid point's primary parent is one step toward the seed
+            // along its dominant axis (x on ties), its secondary parent one step along the
+            // other axis.  A point is solved from its primary parent if that one was accepted,
+            // else from its secondary parent if accepted; otherwise it is an orphan.  Orphans
+            // are then reached by frontier waves from every accepted point.
+            enum : int8_t { kPend = 0, kAcc = 2, kRej = 3, kOrphan = 4 };
+            std::vector<int8_t> st(static_cast<std::size_t>(gw) * gh, kPend);
+            st[sidx] = kAcc;
+            const int sgx = gxs, sgy = gys;
+            const int maxd = std::max(sgx, gw - 1 - sgx) + std::max(sgy, gh - 1 - sgy);
+            auto sgn = [](int v) { return v > 0 ? 1 : -1; };
+            for (int d = 1; d <= maxd; ++d) {
+                for (int gy = 0; gy < gh; ++gy) {
+                    const int rem = d - std::abs(gy - sgy);
+                    if (rem < 0) continue;
+                    const int xs[2] = {sgx - rem, sgx + rem};
+                    for (int t = 0; t < (rem == 0 ? 1 : 2); ++t) {
+                        const int gx = xs[t];
+                        if (gx < 0 || gx >= gw) continue;
+                        const int nidx = gy * gw + gx;
+                        const int dx = gx - sgx, dy = gy - sgy;
+                        int p1, p2 = -1;
+                        if (std::abs(dx) >= std::abs(dy)) {
+                            p1 = gy * gw + (gx - sgn(dx));
+                            if (dy != 0) p2 = (gy - sgn(dy)) * gw + gx;
+                        } else {
+                            p1 = (gy - sgn(dy)) * gw + gx;
+                            if (dx != 0) p2 = gy * gw + (gx - sgn(dx));
+                        }
+                        int parent = -1;
+                        if (st[p1] == kAcc) parent = p1;
+                        else if (p2 >= 0 && st[p2] == kAcc) parent = p2;
+                        if (parent < 0) { st[nidx] = kOrphan; continue; }
+                        const int nx = gx * step, ny = gy * step;
+                        const bool admissible = roi_valid(roi, w, h, nx, ny) && nx - radius >= 0 && ny - radius >= 0 &&
+                                                nx + radius < w && ny + radius < h;
+                        calc[nidx] = 1;
+                        if (!admissible || (max_solves >= 0 && solves >= max_solves)) { st[nidx] = kRej; continue; }
+                        orc_poi_result r;
+                        double p0[6];
+                        solve_from(nidx, parent, r, p0);
+                        if (accept(r, p0[0], p0[1])) { keep(nidx, r); st[nidx] = kAcc; }
+                        else st[nidx] = kRej;
+                    }
                 }
             }
-            std::vector<int> acc;
-            std::vector<double> acorr;
-            for (int nidx : next) {
-                calc[nidx] = 1;
-                if (max_solves >= 0 && solves >= max_solves) continue;
-                const int pidx = best_parent[nidx];
-                const double* pp0 = &pp[static_cast<std::size_t>(pidx) * 6];
-                const int nx = (nidx % gw) * step, ny = (nidx / gw) * step;
-                const double ddx = nx - (pidx % gw) * step, ddy = ny - (pidx / gw) * step;
-                double p0[6];
-                p0[0] = pp0[0] + pp0[2] * ddx + pp0[3] * ddy;
-                p0[1] = pp0[1] + pp0[4] * ddx + pp0[5] * ddy;
-                p0[2] = pp0[2]; p0[3] = pp0[3]; p0[4] = pp0[4]; p0[5] = pp0[5];
-                const orc_poi_result r = solve_one(ref, w, h, gs, sp, scfg, nx, ny, p0, 0.0);
-                ++solves;
-                if (accept(r, p0[0], p0[1])) {
-                    store(out, nidx, r);
-                    ++computed;
-                    for (int k = 0; k < 6; ++k) pp[static_cast<std::size_t>(nidx) * 6 + k] = r.p[k];
-                    acc.push_back(nidx);
-                    acorr.push_back(r.correlation);
-                }
-            }
-            for (int nidx : next) best_parent[nidx] = -2;  // resolved; never a candidate again
-            frontier.swap(acc);
-            fcorr.swap(acorr);
+            std::vector<int> all_acc;
+            for (int i = 0; i < gw * gh; ++i) if (st[i] == kAcc) all_acc.push_back(i);
+            run_waves(all_acc);
+        } else {
+            run_waves(std::vector<int>{sidx});
         }
     }
     if (solves_done) *solves_done = solves;

@@ -57,7 +57,8 @@ typedef struct orc_config {
     double min_displacement_norm;      /* 0 */
     double min_texture_std;            /* 0 */
     int32_t kmeans_sample_limit;       /* 20000 */
-    int32_t propagation_mode;          /* 1 = reliability-guided heap order (reference, default), 0 = frontier waves */
+    int32_t propagation_mode;          /* 1 = reliability-guided heap order (reference, default), 0 = frontier waves,
+                                          2 = dataflow (axis parents toward the seed) + frontier-wave cleanup */
 } orc_config;
 
 /* Per-POI solver result; mirrors dic::Displacement2D (result.hpp:32-51) plus the additive

@@ -132,19 +132,23 @@ def _seed_from_oracle(oracle, p, cfg):
     return seed
 
 
+@pytest.mark.parametrize("mode", [0, 2])
 @pytest.mark.parametrize("precision", [1, 0])
-def test_propagate_frontier_matches_oracle(oracle, gpu_ctx, workload0, precision):
+def test_propagate_matches_oracle_same_order(oracle, gpu_ctx, workload0, precision, mode):
+    """GPU propagation against the oracle run in the same visit order (0 frontier waves,
+    2 dataflow + wave clean-up)."""
     import __graft_entry__ as G
     from traditional_dic_gb300 import subset as S
     p = workload0
     cfg = S.config_from_dict(G.WORKLOAD0_CONFIG)
     cfg.precision = precision
+    cfg.propagation_mode = mode
     oseed = _seed_from_oracle(oracle, p, cfg)
     pair = S.Pair(gpu_ctx, p.reference, p.deformed, degree=3, precision=precision)
     seed = S.make_seed(oseed.x, oseed.y, list(oseed.p), oseed.correlation)
     got = S.propagate(gpu_ctx, pair, cfg, seed)
     ocfg = oracle.as_config(cfg)
-    ocfg.propagation_mode = 0
+    ocfg.propagation_mode = mode
     coef = oracle.prefilter(p.deformed.astype(np.float32), 3, 3, True)
     want = oracle.propagate(p.reference, coef, ocfg, oseed)
     assert got["points_computed"] == want["points_computed"] or precision == 0

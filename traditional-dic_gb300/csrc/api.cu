@@ -227,6 +227,8 @@ void propagate_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, cons
                     const tdic_grid_out* out, tdic_memory mem, int32_t* points_computed, cudaStream_t s) {
     check_config(cfg);
     TDIC_REQUIRE(pair->exact == 1, TDIC_INVALID_ARG, "propagation needs a pair with the exact prefilter");
+    TDIC_REQUIRE(cfg.propagation_mode == 0 || cfg.propagation_mode == 2, TDIC_UNSUPPORTED,
+                 "propagation_mode 1 (serial heap order) is not on the GPU path; use 0 (frontier waves) or 2 (dataflow)");
     const int w = pair->w, h = pair->h;
     const int step = std::max(0, cfg.propagation_spacing) + 1;
     int32_t gw, gh;
@@ -254,6 +256,16 @@ void propagate_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, cons
     Buffer order(&ctx->pool, sizeof(int) * n);
     Buffer fetch(&ctx->pool, sizeof(int) * (n + 2));
     Buffer misc(&ctx->pool, 64);
+    const bool dataflow = cfg.propagation_mode == 2;
+    Buffer dstate(&ctx->pool, dataflow ? sizeof(int) * n : 0), dcnt(&ctx->pool, dataflow ? sizeof(int) * n : 0),
+        dqs(&ctx->pool, dataflow ? sizeof(int) * n : 0), dq(&ctx->pool, dataflow ? sizeof(unsigned long long) * n : 0),
+        kcorr(&ctx->pool, dataflow ? sizeof(float) * n : 0);
+    if (dataflow) {
+        TDIC_CUDA_TRY(cudaMemsetAsync(dstate.ptr, 0, sizeof(int) * n, s));
+        TDIC_CUDA_TRY(cudaMemsetAsync(dcnt.ptr, 0, sizeof(int) * n, s));
+        TDIC_CUDA_TRY(cudaMemsetAsync(dqs.ptr, 0, sizeof(int) * n, s));
+        TDIC_CUDA_TRY(cudaMemsetAsync(dq.ptr, 0xff, sizeof(unsigned long long) * n, s));
+    }
     TDIC_CUDA_TRY(cudaMemcpyAsync(d_roi.ptr, roi_grid.data(), n, cudaMemcpyHostToDevice, s));
     TDIC_CUDA_TRY(cudaMemsetAsync(claim.ptr, 0, sizeof(int) * n, s));
     TDIC_CUDA_TRY(cudaMemsetAsync(keyparams.ptr, 0xff, sizeof(unsigned long long) * n, s));
@@ -276,6 +288,11 @@ void propagate_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, cons
     L.barrier = reinterpret_cast<unsigned int*>(m + 4);
     L.flags = m + 8;                 // [0] error [1] no seed [2] accepted
     L.fetch = fetch.as<int>();
+    L.mode = cfg.propagation_mode;
+    L.sgx = gxs;
+    L.sgy = gys;
+    L.dstate = dstate.as<int>(); L.dcnt = dcnt.as<int>(); L.dqs = dqs.as<int>();
+    L.dq = dq.as<unsigned long long>(); L.kcorr = kcorr.as<float>();
     if (!seed_ok) {
         // Output every grid point with defaults; points_computed = 0.
         L.seed_idx = 0;

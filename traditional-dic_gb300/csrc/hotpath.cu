@@ -59,13 +59,18 @@ __device__ __forceinline__ void named_bar(int id, int nthreads) {
 
 // All-reduce K values over the group (every thread ends with the same sums, summed in the
 // same order, so redundant scalar math stays bit-identical across the group's warps).
+// `red` holds two buffers of 32*G values used alternately (parity `rp`), so one named
+// barrier per reduction suffices: a buffer is rewritten only after every thread has passed the
+// barrier of the reduction in between, i.e. after all reads of its previous contents.
 template <int G, int K, typename T>
-__device__ __forceinline__ void group_sum(T (&v)[K], T* red, int tid, int bar_id) {
+__device__ __forceinline__ void group_sum(T (&v)[K], T* red_base, int& rp, int tid, int bar_id) {
+    static_assert(K <= 32, "reduction scratch holds 32 values per warp");
 #pragma unroll
     for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
     if constexpr (G > 1) {
+        T* red = red_base + rp * 32 * G;
+        rp ^= 1;
         const int warp = tid >> 5, lane = tid & 31;
-        named_bar(bar_id, 32 * G);  // previous readers of red are done
         if (lane == 0) {
 #pragma unroll
             for (int k = 0; k < K; ++k) red[warp * K + k] = v[k];
@@ -291,6 +296,7 @@ __device__ __forceinline__ bool warp_interp(const Env<T>& e, int cx, int cy, con
     constexpr int NB = DEG + 1, OFF = DEG / 2;
     bool ok = true;
     const T xlo = T(-cx), ylo = T(-cy), xhi = T(e.w - 1 - cx), yhi = T(e.h - 1 - cy);
+#pragma unroll 2
     for (int i = tid; i < e.n; i += nt) {
         const short2 o = __ldg(e.off + i);
         const T lx = T(o.x), ly = T(o.y);
@@ -342,7 +348,7 @@ __device__ __forceinline__ bool warp_interp(const Env<T>& e, int cx, int cy, con
 }
 
 // The per-POI solve.  OPT 0 = ICGN (icgn.cpp:446-627), 1 = FGN (forward_gauss_newton.cpp:188-399).
-// sm: 4 * nmax T values of this group; red: G * 32 T values; flag: one int.
+// sm: 4 * nmax T values of this group; red: 2 x 32 * G T values; flag: one int.
 template <int OPT, int DEG, typename T, int G>
 __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6], double conf, T* sm, T* red,
                           int* flag, double* s_hinv_raw, int tid, int bar_id, Result& R) {
@@ -350,6 +356,7 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
     M* s_hinv = reinterpret_cast<M*>(s_hinv_raw);
     constexpr int NT = 32 * G;
     result_init(R, p0, conf);
+    int rp = 0;  // reduction-buffer parity
     const int r = e.radius;
     if (e.w <= 0 || r < 1 || e.max_iter < 0) return;
     if (cx - r < 0 || cy - r < 0 || cx + r >= e.w || cy + r >= e.h) return;
@@ -380,7 +387,7 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
         ksum.add(T(f));
     }
     T v1[1] = {ksum.value()};
-    group_sum<G, 1>(v1, red, tid, bar_id);
+    group_sum<G, 1>(v1, red, rp, tid, bar_id);
     const double inv_n = e.inv_n;  // 1 / N, from the host (no device-side FP64 divide)
     const double mean = static_cast<double>(v1[0]) * inv_n;
     const T fm = T(mean);
@@ -390,7 +397,7 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
         knorm.add(d * d);
     }
     v1[0] = knorm.value();
-    group_sum<G, 1>(v1, red, tid, bar_id);
+    group_sum<G, 1>(v1, red, rp, tid, bar_id);
     const double ss = static_cast<double>(v1[0]);  // sum (f - mean)^2
     if (!(ss > kEps * kEps)) { R.status = TDIC_NUMERICAL_FAILURE; return; }  // |f - mean| <= 1e-12
     const T inv_norm = T(1) / sqrt(T(ss));
@@ -413,7 +420,7 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
 #pragma unroll
                 for (int v = 0; v < 6; ++v) hs[u * 6 + v] += q[u] * m6[v];
         }
-        group_sum<G, 18>(hs, red, tid, bar_id);
+        group_sum<G, 18>(hs, red, rp, tid, bar_id);
         // index map: S(u, v) with u in {aa, ab, bb}, v in {1, lx, ly, lxlx, lxly, lyly}
         auto S = [&](int u, int v) { return static_cast<M>(hs[u * 6 + v]); };
         M Hm[6][6];
@@ -455,9 +462,10 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
         for (int k = 0; k < 6; ++k) pt[k] = static_cast<T>(p[k]);
         Kahan<T> sg, sg2;
         const bool ok = warp_interp<DEG, T, OPT == 1>(e, cx, cy, pt, fm, s_g, s_a, s_b, tid, NT, sg, sg2);
-        if (group_any<G>(!ok, flag, tid, bar_id)) { R.status = TDIC_INVALID_INPUT; return; }
-        T v2[2] = {sg.value(), sg2.value()};
-        group_sum<G, 2>(v2, red, tid, bar_id);
+        // one reduction carries the two normalisation sums and the out-of-image count
+        T v2[3] = {sg.value(), sg2.value(), ok ? T(0) : T(1)};
+        group_sum<G, 3>(v2, red, rp, tid, bar_id);
+        if (v2[2] != T(0)) { R.status = TDIC_INVALID_INPUT; return; }
         // normalisation sums combined in FP64: mean of (g - fm) and sum (g - mean)^2
         const double gmr = static_cast<double>(v2[0]) * inv_n;
         const double var = fma(-static_cast<double>(v2[0]), gmr, static_cast<double>(v2[1]));
@@ -479,7 +487,7 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
                 q[0] += da; q[1] += db; q[2] += da * lx; q[3] += da * ly; q[4] += db * lx; q[5] += db * ly;
                 q[6] += diff * diff;
             }
-            group_sum<G, 7>(q, red, tid, bar_id);
+            group_sum<G, 7>(q, red, rp, tid, bar_id);
             corr = static_cast<double>(q[6]);
             M grad[6];
             for (int k = 0; k < 6; ++k) grad[k] = static_cast<M>(q[k]) * gscale;
@@ -513,7 +521,7 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
                 q[18] += da; q[19] += db; q[20] += da * lx; q[21] += da * ly; q[22] += db * lx; q[23] += db * ly;
                 q[24] += diff * diff;
             }
-            group_sum<G, 25>(q, red, tid, bar_id);
+            group_sum<G, 25>(q, red, rp, tid, bar_id);
             corr = static_cast<double>(q[24]);
             auto S = [&](int u, int v) { return static_cast<M>(q[u * 6 + v]); };
             M Hm[6][6];
@@ -562,7 +570,7 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
 // Per-group shared memory: [36 doubles: 6x6 inverse][16 bytes: ints][32*G T: reduction
 // scratch][4*nmax T: samples f^, a, b, g].
 template <typename T> __host__ __device__ __forceinline__ size_t group_smem_bytes(int nmax, int G) {
-    const size_t bytes = 36 * sizeof(double) + 16 + (static_cast<size_t>(4) * nmax + 32 * G) * sizeof(T);
+    const size_t bytes = 36 * sizeof(double) + 16 + (static_cast<size_t>(4) * nmax + 64 * G) * sizeof(T);
     return (bytes + 15) & ~size_t(15);
 }
 
@@ -577,7 +585,7 @@ struct GroupSmem {
         hinv = reinterpret_cast<double*>(g);
         ints = reinterpret_cast<int*>(g + 36 * sizeof(double));
         red = reinterpret_cast<T*>(g + 36 * sizeof(double) + 16);
-        sm = red + 32 * G;
+        sm = red + 64 * G;
     }
 };
 
@@ -649,11 +657,21 @@ struct PropEnv {
     int* claim;
     unsigned long long* key;
     int* order;
-    int* counters;  // [0] = tail
+    int* counters;  // [0] wave-list tail, [1] queue head, [2] queue tail, [3] items in flight
     int* fetch;     // per wave
     unsigned int* barrier;
     int* flags;     // [0] error, [1] no seed, [2] accepted count
+    // dataflow order (mode 2)
+    int mode;
+    int sgx, sgy;                 // seed grid coordinates
+    int* dstate;                  // 0 pending, 2 accepted, 3 rejected, 4 orphan
+    int* dcnt;                    // parents resolved so far
+    int* dqs;                     // 1 once queued
+    unsigned long long* dq;       // queue items: parent (high 32, -1 = orphan) : point (low 32)
+    float* kcorr;                 // ZNSSD of accepted points (wave keys of the clean-up)
 };
+
+enum { kDfPending = 0, kDfAccepted = 2, kDfRejected = 3, kDfOrphan = 4 };
 
 __device__ __forceinline__ int ld_cg(const int* p) { return __ldcg(p); }
 
@@ -729,6 +747,58 @@ __device__ void expand(const PropEnv& pe, int w, int h, int radius, int n, doubl
     }
 }
 
+// Dataflow order: primary parent = one step toward the seed along the dominant axis (x on
+// ties), secondary parent = one step along the other axis (absent on the seed's row/column).
+__device__ __forceinline__ void df_parents(const PropEnv& pe, int n, int& p1, int& p2) {
+    const int gx = n % pe.gw, gy = n / pe.gw;
+    const int dx = gx - pe.sgx, dy = gy - pe.sgy;
+    const int sx = dx > 0 ? 1 : -1, sy = dy > 0 ? 1 : -1;
+    p2 = -1;
+    if (abs(dx) >= abs(dy)) {
+        p1 = gy * pe.gw + gx - sx;
+        if (dy != 0) p2 = (gy - sy) * pe.gw + gx;
+    } else {
+        p1 = (gy - sy) * pe.gw + gx;
+        if (dx != 0) p2 = gy * pe.gw + gx - sx;
+    }
+}
+
+__device__ __forceinline__ void df_push(const PropEnv& pe, int c, int parent) {
+    atomicAdd(pe.counters + 3, 1);  // in flight before it is visible: termination stays exact
+    const int pos = atomicAdd(pe.counters + 2, 1);
+    const unsigned long long item = (static_cast<unsigned long long>(static_cast<unsigned int>(parent)) << 32) |
+                                    static_cast<unsigned int>(c);
+    atomicExch(pe.dq + pos, item);
+}
+
+// n has been resolved (state published and fenced).  Its children are the 4-neighbours one
+// step farther from the seed.  A child is queued from its primary parent as soon as that one
+// is accepted; otherwise the last of its parents to resolve decides: secondary parent if
+// accepted, else orphan.
+__device__ void df_notify(const PropEnv& pe, int n, bool accepted) {
+    const int gx = n % pe.gw, gy = n / pe.gw;
+    const int dn = abs(gx - pe.sgx) + abs(gy - pe.sgy);
+    const int cxs[4] = {gx, gx + 1, gx, gx - 1}, cys[4] = {gy - 1, gy, gy + 1, gy};
+    for (int d = 0; d < 4; ++d) {
+        const int cx = cxs[d], cy = cys[d];
+        if (cx < 0 || cy < 0 || cx >= pe.gw || cy >= pe.gh) continue;
+        if (abs(cx - pe.sgx) + abs(cy - pe.sgy) != dn + 1) continue;
+        const int c = cy * pe.gw + cx;
+        int p1, p2;
+        df_parents(pe, c, p1, p2);
+        if (accepted && p1 == n) {
+            if (atomicCAS(pe.dqs + c, 0, 1) == 0) df_push(pe, c, n);
+        }
+        const int total = p2 >= 0 ? 2 : 1;
+        if (atomicAdd(pe.dcnt + c, 1) + 1 == total) {
+            __threadfence();
+            if (ld_cg(pe.dstate + p1) == kDfAccepted) continue;  // queued by its primary parent
+            const int parent = (p2 >= 0 && ld_cg(pe.dstate + p2) == kDfAccepted) ? p2 : -1;
+            if (atomicCAS(pe.dqs + c, 0, 1) == 0) df_push(pe, c, parent);
+        }
+    }
+}
+
 template <int OPT, int DEG, typename T, int G>
 __global__ void __launch_bounds__(256, 2) propagate_kernel(Env<T> e, PropEnv pe) {
     using P = typename MixedOf<T>::type;
@@ -765,13 +835,100 @@ __global__ void __launch_bounds__(256, 2) propagate_kernel(Env<T> e, PropEnv pe)
                 store_grid<P>(pe, params, pe.seed_idx, R);
                 pe.claim[pe.seed_idx] = 1;
                 pe.flags[2] = 1;
-                __threadfence();
-                expand(pe, e.w, e.h, e.radius, pe.seed_idx, fmax(0.0, R.corr), 1);
+                if (pe.mode == 2) {
+                    pe.kcorr[pe.seed_idx] = static_cast<float>(fmax(0.0, R.corr));
+                    pe.dstate[pe.seed_idx] = kDfAccepted;
+                    pe.dqs[pe.seed_idx] = 1;
+                    __threadfence();
+                    df_notify(pe, pe.seed_idx, true);
+                } else {
+                    __threadfence();
+                    expand(pe, e.w, e.h, e.radius, pe.seed_idx, fmax(0.0, R.corr), 1);
+                }
             }
         }
     }
     if (!grid_barrier(pe.barrier, pe.flags)) return;
     if (*reinterpret_cast<volatile int*>(pe.flags + 1)) return;
+
+    if (pe.mode == 2) {
+        // ---- dataflow phase: ticketed work queue, no grid-wide synchronisation -------------
+        while (true) {
+            int item_c = -1, item_p = -1, state = 0;  // state: 0 item, 1 done, 2 error
+            if (tid == 0) {
+                const int t = atomicAdd(pe.counters + 1, 1);
+                // At most gw*gh - 1 points are ever queued (each once, never the seed), so a
+                // ticket beyond the array can only end by completion; it reads nothing.
+                const bool in_range = t < pe.gw * pe.gh;
+                unsigned long long spins = 0;
+                while (true) {
+                    const unsigned long long it = in_range ? __ldcg(pe.dq + t) : ~0ull;
+                    if (it != ~0ull) {
+                        item_c = static_cast<int>(it & 0xffffffffull);
+                        item_p = static_cast<int>(it >> 32);
+                        break;
+                    }
+                    if (ld_cg(pe.counters + 3) == 0) { state = 1; break; }  // nothing queued or running
+                    if (++spins > kSpinLimit) { atomicExch(pe.flags, 1); state = 2; break; }
+                    __nanosleep(spins < 64 ? 20 : 200);
+                }
+            }
+            state = group_bcast<G>(state, ints + 1, tid, bar_id);
+            if (state != 0) break;
+            item_c = group_bcast<G>(item_c, ints + 2, tid, bar_id);
+            item_p = group_bcast<G>(item_p, ints + 3, tid, bar_id);
+            const int n = item_c;
+            const int nx = (n % pe.gw) * pe.step, ny = (n / pe.gw) * pe.step;
+            bool accepted = false;
+            int new_state = kDfOrphan;
+            Result R;
+            if (item_p >= 0) {
+                const bool admissible = pe.roi_grid[n] != 0 && nx - e.radius >= 0 && ny - e.radius >= 0 &&
+                                        nx + e.radius < e.w && ny + e.radius < e.h;
+                new_state = kDfRejected;
+                if (admissible) {
+                    double pp[6];
+                    for (int k = 0; k < 6; ++k) pp[k] = static_cast<double>(__ldcg(params + static_cast<size_t>(item_p) * 6 + k));
+                    const double ddx = static_cast<double>(nx - (item_p % pe.gw) * pe.step);
+                    const double ddy = static_cast<double>(ny - (item_p / pe.gw) * pe.step);
+                    double p0[6];
+                    p0[0] = pp[0] + pp[2] * ddx + pp[3] * ddy;  // reliability_propagation.cpp:326-329
+                    p0[1] = pp[1] + pp[4] * ddx + pp[5] * ddy;
+                    p0[2] = pp[2]; p0[3] = pp[3]; p0[4] = pp[4]; p0[5] = pp[5];
+                    solve_poi<OPT, DEG, T, G>(e, nx, ny, p0, 0.0, sm, red, ints, gs.hinv, tid, bar_id, R);
+                    accepted = R.valid && R.status == TDIC_SUCCESS && R.corr < pe.max_znssd &&
+                               fabs(p0[0] - R.p[0]) < cutoff && fabs(p0[1] - R.p[1]) < cutoff && finite6(R.p) &&
+                               isfinite(R.corr);  // :359-368
+                    if (accepted) new_state = kDfAccepted;
+                }
+            }
+            if (tid == 0) {
+                if (accepted) {
+                    store_grid<P>(pe, params, n, R);
+                    pe.kcorr[n] = static_cast<float>(R.corr);
+                    atomicAdd(pe.flags + 2, 1);
+                }
+                pe.dstate[n] = new_state;
+                __threadfence();
+                df_notify(pe, n, accepted);
+                __threadfence();
+                atomicSub(pe.counters + 3, 1);
+            }
+        }
+        if (!grid_barrier(pe.barrier, pe.flags)) return;
+        // ---- clean-up: orphans are reached by frontier waves from every accepted point ------
+        const int ng = pe.gw * pe.gh;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ng; i += gridDim.x * blockDim.x) {
+            const int st = ld_cg(pe.dstate + i);
+            if (st == kDfAccepted || st == kDfRejected) pe.claim[i] = 1;
+        }
+        if (!grid_barrier(pe.barrier, pe.flags)) return;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ng; i += gridDim.x * blockDim.x)
+            if (ld_cg(pe.dstate + i) == kDfAccepted) expand(pe, e.w, e.h, e.radius, i, __ldcg(pe.kcorr + i), 1);
+        if (!grid_barrier(pe.barrier, pe.flags)) return;
+    }
+
+    // ---- frontier waves -----------------------------------------------------------------
     int start = 0;
     int end = ld_cg(pe.counters);
     for (int wave = 1; start < end; ++wave) {
@@ -907,6 +1064,8 @@ void propagate_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, con
     pe.out = L.out;
     pe.claim = L.claim; pe.key = L.key; pe.order = L.order; pe.counters = L.counters; pe.fetch = L.fetch;
     pe.barrier = L.barrier; pe.flags = L.flags;
+    pe.mode = L.mode; pe.sgx = L.sgx; pe.sgy = L.sgy;
+    pe.dstate = L.dstate; pe.dcnt = L.dcnt; pe.dqs = L.dqs; pe.dq = L.dq; pe.kcorr = L.kcorr;
     const int n = L.gw * L.gh;
     init_grid_kernel<<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, s>>>(L.out, L.gw, L.gh, L.step);
     TDIC_CUDA_TRY(cudaGetLastError());

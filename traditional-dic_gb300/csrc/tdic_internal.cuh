@@ -148,6 +148,10 @@ struct PropagateLaunch {
     int* claim; unsigned long long* key; void* params; int* order; int* counters; int* fetch;
     unsigned int* barrier;  // [count, generation]
     int* flags;             // [error, no_seed, accepted]
+    // dataflow order (propagation_mode 2)
+    int mode;
+    int sgx, sgy;
+    int* dstate; int* dcnt; int* dqs; unsigned long long* dq; float* kcorr;
 };
 void launch_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const PropagateLaunch& L,
                       cudaStream_t s);

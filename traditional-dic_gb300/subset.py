@@ -10,7 +10,7 @@ Both run on the GPU through libtdic_gb300.so; there is no CPU fallback.
 Additive result keys (not in the reference): ``zncc`` = clamp(1 - correlation / 2),
 ``iterations``, ``converged`` (strict |dp| < threshold) and ``status`` (dic::SolverStatus).
 GPU-only settings live under a separate ``"gpu"`` section of the config dict, which the
-reference parser ignores: ``{"gpu": {"precision": "fp32" | "fp64"}}``.
+reference parser ignores: ``{"gpu": {"precision": "fp32" | "fp64", "propagation": "dataflow" | "waves"}}``.
 """
 from __future__ import annotations
 
@@ -24,6 +24,8 @@ import numpy as np
 from . import _lib as L
 
 RESULT_KEYS = ("x", "y", "u", "v", "du_dx", "du_dy", "dv_dx", "dv_dy", "correlation", "valid")
+# GPU visit orders of the propagation (the reference's serial heap order is mode 1, CPU only)
+PROPAGATION_MODES = {"waves": 0, "dataflow": 2}
 EXTRA_KEYS = ("zncc", "iterations", "converged", "status")
 
 
@@ -266,6 +268,11 @@ def config_from_dict(d: dict | None) -> L.Config:
         if p not in ("fp32", "fp64"):
             raise RuntimeError("gpu.precision must be 'fp32' or 'fp64'.")
         cfg.precision = L.FP64 if p == "fp64" else L.FP32_MIXED
+    if "propagation" in gpu:
+        m = str(gpu["propagation"]).lower()
+        if m not in PROPAGATION_MODES:
+            raise RuntimeError("gpu.propagation must be 'waves' or 'dataflow'.")
+        cfg.propagation_mode = PROPAGATION_MODES[m]
     return cfg
 
 
