@@ -194,3 +194,20 @@ def test_compute_empty_results(gpu_ctx):
     assert all(len(r[k]) == 0 for k in S.RESULT_KEYS)
     r = S.compute(p.reference, p.deformed, {"initialization": {"integer_search": {"sift_enabled": True}}})
     assert len(r["x"]) == 0
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_solve_pois_large_radius(oracle, gpu_ctx, precision):
+    """r = 25 (1961 samples): shared-memory staging sized per radius, adaptive groups per CTA."""
+    from traditional_dic_gb300 import subset as S
+    p = small_speckle((128, 128), n=420)
+    cfg = _cfg(S, degree=5, subset_radius=25, max_iterations=20, convergence_threshold=1e-3, precision=precision)
+    pair = S.Pair(gpu_ctx, p.reference, p.deformed, degree=5, precision=precision)
+    xy, p0 = _poi_case(p, step=13, r=25)
+    got = S.solve_pois(gpu_ctx, pair, cfg, xy, p0)
+    coef = oracle.prefilter(p.deformed.astype(np.float32), 5, 3, True)
+    want = oracle.solve_pois(p.reference, coef, oracle.as_config(cfg), xy, p0)
+    assert np.mean(got["valid"] == want["valid"]) >= FLAG_AGREE
+    ok = got["valid"] & want["valid"]
+    tol = 1e-8 if precision == 1 else U_TOL
+    assert np.max(np.abs(got["p"][ok, :2] - want["p"][ok, :2])) <= tol

@@ -93,6 +93,16 @@ void build_qk(int d, double* qk) {
         }
 }
 
+void check_device_error(tdic_ctx* ctx, cudaStream_t s) {
+    int v = 0;
+    TDIC_CUDA_TRY(cudaMemcpyAsync(&v, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    TDIC_CUDA_TRY(cudaStreamSynchronize(s));
+    if (v != 0) {
+        TDIC_CUDA_TRY(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), s));
+        throw Error{TDIC_TIMEOUT, "a bounded in-kernel wait (TMA copy) timed out"};
+    }
+}
+
 const SampleTable& sample_table(tdic_ctx* ctx, int radius) {
     auto it = ctx->tables.find(radius);
     if (it != ctx->tables.end()) return it->second;
@@ -168,7 +178,7 @@ void upload_convert(tdic_pair* p, const void* src, int pitch, tdic_dtype dtype, 
         TDIC_CUDA_TRY(cudaMemcpyAsync(p->staging.ptr, src, bytes, cudaMemcpyHostToDevice, s));
         dsrc = p->staging.ptr;
     }
-    launch_convert(dsrc, p->w, p->h, pt, dtype, dst, s);
+    launch_convert(dsrc, p->w, p->h, pt, dtype, dst, p->rpitch, s);
 }
 
 void pair_compute(tdic_pair* p, const void* ref, const void* def, int pitch, tdic_dtype dtype, tdic_memory mem,
@@ -258,12 +268,10 @@ void propagate_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, cons
     Buffer misc(&ctx->pool, 64);
     const bool dataflow = cfg.propagation_mode == 2;
     Buffer dstate(&ctx->pool, dataflow ? sizeof(int) * n : 0), dcnt(&ctx->pool, dataflow ? sizeof(int) * n : 0),
-        dqs(&ctx->pool, dataflow ? sizeof(int) * n : 0), dq(&ctx->pool, dataflow ? sizeof(unsigned long long) * n : 0),
-        kcorr(&ctx->pool, dataflow ? sizeof(float) * n : 0);
+        dq(&ctx->pool, dataflow ? sizeof(unsigned long long) * n : 0), kcorr(&ctx->pool, dataflow ? sizeof(float) * n : 0);
     if (dataflow) {
         TDIC_CUDA_TRY(cudaMemsetAsync(dstate.ptr, 0, sizeof(int) * n, s));
         TDIC_CUDA_TRY(cudaMemsetAsync(dcnt.ptr, 0, sizeof(int) * n, s));
-        TDIC_CUDA_TRY(cudaMemsetAsync(dqs.ptr, 0, sizeof(int) * n, s));
         TDIC_CUDA_TRY(cudaMemsetAsync(dq.ptr, 0xff, sizeof(unsigned long long) * n, s));
     }
     TDIC_CUDA_TRY(cudaMemcpyAsync(d_roi.ptr, roi_grid.data(), n, cudaMemcpyHostToDevice, s));
@@ -271,6 +279,10 @@ void propagate_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, cons
     TDIC_CUDA_TRY(cudaMemsetAsync(keyparams.ptr, 0xff, sizeof(unsigned long long) * n, s));
     TDIC_CUDA_TRY(cudaMemsetAsync(fetch.ptr, 0, sizeof(int) * (n + 2), s));
     TDIC_CUDA_TRY(cudaMemsetAsync(misc.ptr, 0, 64, s));
+    {   // queue word: tail 0, in-flight bias 2^31 (low word)
+        const unsigned long long q0 = 0x80000000ull;
+        TDIC_CUDA_TRY(cudaMemcpyAsync(misc.as<int>() + 4, &q0, sizeof(q0), cudaMemcpyHostToDevice, s));
+    }
     PropagateLaunch L{};
     L.gw = gw; L.gh = gh; L.step = step;
     L.roi_grid = d_roi.as<uint8_t>();
@@ -284,14 +296,14 @@ void propagate_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, cons
     L.params = nullptr;
     L.order = order.as<int>();
     int* m = misc.as<int>();
-    L.counters = m;                  // [0] tail
-    L.barrier = reinterpret_cast<unsigned int*>(m + 4);
-    L.flags = m + 8;                 // [0] error [1] no seed [2] accepted
+    L.counters = m;                  // [0] wave-list tail, [1] queue head, [4..5] 64-bit queue word
+    L.barrier = reinterpret_cast<unsigned int*>(m + 8);
+    L.flags = m + 12;                // [0] error [1] no seed [2] accepted
     L.fetch = fetch.as<int>();
     L.mode = cfg.propagation_mode;
     L.sgx = gxs;
     L.sgy = gys;
-    L.dstate = dstate.as<int>(); L.dcnt = dcnt.as<int>(); L.dqs = dqs.as<int>();
+    L.dstate = dstate.as<int>(); L.dcnt = dcnt.as<int>();
     L.dq = dq.as<unsigned long long>(); L.kcorr = kcorr.as<float>();
     if (!seed_ok) {
         // Output every grid point with defaults; points_computed = 0.
@@ -303,8 +315,8 @@ void propagate_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, cons
     int flags[3] = {0, 0, 0};
     if (seed_ok) TDIC_CUDA_TRY(cudaMemcpyAsync(flags, L.flags, sizeof(flags), cudaMemcpyDeviceToHost, s));
     if (mem == TDIC_HOST) copy_grid_back(gb, out, n, s);
-    TDIC_CUDA_TRY(cudaStreamSynchronize(s));
-    TDIC_REQUIRE(flags[0] == 0, TDIC_TIMEOUT, "propagation grid barrier timed out");
+    check_device_error(ctx, s);
+    TDIC_REQUIRE(flags[0] == 0, TDIC_TIMEOUT, "propagation: a bounded in-kernel wait timed out");
     *points_computed = (seed_ok && !flags[1]) ? flags[2] : 0;
 }
 
@@ -481,7 +493,7 @@ void select_seed_impl(tdic_ctx* ctx, tdic_pair* lazy, const HostImage& ref_host,
         SolveLaunch L{d_in.as<tdic_poi_in>(), d_out.as<tdic_poi_out>(), static_cast<int>(in.size()), d_fetch.as<int>()};
         launch_solve(ctx, lazy, sc, L, s);
         TDIC_CUDA_TRY(cudaMemcpyAsync(ref_out.data(), d_out.ptr, sizeof(tdic_poi_out) * in.size(), cudaMemcpyDeviceToHost, s));
-        TDIC_CUDA_TRY(cudaStreamSynchronize(s));
+        check_device_error(ctx, s);
     }
     bool found = false;
     double bq = 0.0, bnorm = 0.0;
@@ -547,7 +559,10 @@ tdic_status tdic_ctx_create(int32_t device, tdic_ctx** out) {
     tdic_status st = guarded(ctx, [&] {
         TDIC_CUDA_TRY(cudaSetDevice(device));
         TDIC_CUDA_TRY(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
+        TDIC_CUDA_TRY(cudaDeviceGetAttribute(&ctx->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
         TDIC_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        TDIC_CUDA_TRY(cudaMalloc(&ctx->dev_err, sizeof(int)));
+        TDIC_CUDA_TRY(cudaMemset(ctx->dev_err, 0, sizeof(int)));
         upload_qk_constants();
     });
     if (st != TDIC_OK) {
@@ -566,6 +581,7 @@ void ctx_free(tdic_ctx* ctx) {
     cudaDeviceSynchronize();
     ctx->tables.clear();
     ctx->pool.trim();
+    if (ctx->dev_err) cudaFree(ctx->dev_err);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
 }
 }  // namespace
@@ -608,11 +624,14 @@ tdic_status tdic_pair_create(tdic_ctx* ctx, const void* reference, const void* d
         p->exact = exact_prefilter ? 1 : 0;
         p->cw = width + 2 * p->border;
         p->ch = height + 2 * p->border;
+        p->rpitch = (width + 31) / 32 * 32;
+        const int per128 = precision == TDIC_FP64 ? 16 : 32;
+        p->cpitch = (p->cw + per128 - 1) / per128 * per128;
         try {
             const size_t es = precision == TDIC_FP64 ? 8 : 4;
-            p->ref = Buffer(&ctx->pool, sizeof(float) * static_cast<size_t>(width) * height);
-            p->def_f = Buffer(&ctx->pool, sizeof(float) * static_cast<size_t>(width) * height);
-            p->coef = Buffer(&ctx->pool, es * static_cast<size_t>(p->cw) * p->ch);
+            p->ref = Buffer(&ctx->pool, sizeof(float) * static_cast<size_t>(p->rpitch) * height);
+            p->def_f = Buffer(&ctx->pool, sizeof(float) * static_cast<size_t>(p->rpitch) * height);
+            p->coef = Buffer(&ctx->pool, es * static_cast<size_t>(p->cpitch) * p->ch);
             pair_compute(p, reference, deformed, pitch, dtype, memory, pick(ctx, stream));
         } catch (...) {
             delete p;
@@ -653,9 +672,12 @@ void tdic_pair_destroy(tdic_pair* pair) {
 tdic_status tdic_pair_coefficients(tdic_pair* pair, void* host_out, size_t bytes) {
     if (!pair) return TDIC_INVALID_ARG;
     return guarded(pair->ctx, [&] {
-        TDIC_REQUIRE(host_out && bytes >= pair->coef.bytes, TDIC_INVALID_ARG, "output buffer too small");
+        const size_t es = pair->precision == TDIC_FP64 ? 8 : 4;
+        const size_t dense = es * static_cast<size_t>(pair->cw) * pair->ch;
+        TDIC_REQUIRE(host_out && bytes >= dense, TDIC_INVALID_ARG, "output buffer too small");
         TDIC_CUDA_TRY(cudaDeviceSynchronize());
-        TDIC_CUDA_TRY(cudaMemcpy(host_out, pair->coef.ptr, pair->coef.bytes, cudaMemcpyDeviceToHost));
+        TDIC_CUDA_TRY(cudaMemcpy2D(host_out, es * pair->cw, pair->coef.ptr, es * pair->cpitch, es * pair->cw, pair->ch,
+                                   cudaMemcpyDeviceToHost));
     });
 }
 
@@ -666,7 +688,8 @@ tdic_status tdic_reference_gradient(tdic_pair* pair, double* gx, double* gy) {
         tdic_ctx* ctx = pair->ctx;
         const size_t n = static_cast<size_t>(pair->w) * pair->h;
         Buffer dx(&ctx->pool, 8 * n), dy(&ctx->pool, 8 * n);
-        launch_reference_gradient(pair->ref.as<float>(), pair->w, pair->h, dx.as<double>(), dy.as<double>(), ctx->stream);
+        launch_reference_gradient(pair->ref.as<float>(), pair->w, pair->h, pair->rpitch, dx.as<double>(), dy.as<double>(),
+                                  ctx->stream);
         TDIC_CUDA_TRY(cudaMemcpyAsync(gx, dx.ptr, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
         TDIC_CUDA_TRY(cudaMemcpyAsync(gy, dy.ptr, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
         TDIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -686,14 +709,14 @@ tdic_status tdic_solve_pois(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* c
         Buffer fetch(&ctx->pool, sizeof(int));
         if (memory == TDIC_DEVICE) {
             launch_solve(ctx, pair, *cfg, SolveLaunch{in, out, n, fetch.as<int>()}, s);
-            TDIC_CUDA_TRY(cudaStreamSynchronize(s));  // keep `fetch` alive until the kernel is done
+            check_device_error(ctx, s);  // synchronises: keeps `fetch` alive until the kernel is done
             return;
         }
         Buffer d_in(&ctx->pool, sizeof(tdic_poi_in) * n), d_out(&ctx->pool, sizeof(tdic_poi_out) * n);
         TDIC_CUDA_TRY(cudaMemcpyAsync(d_in.ptr, in, sizeof(tdic_poi_in) * n, cudaMemcpyHostToDevice, s));
         launch_solve(ctx, pair, *cfg, SolveLaunch{d_in.as<tdic_poi_in>(), d_out.as<tdic_poi_out>(), n, fetch.as<int>()}, s);
         TDIC_CUDA_TRY(cudaMemcpyAsync(out, d_out.ptr, sizeof(tdic_poi_out) * n, cudaMemcpyDeviceToHost, s));
-        TDIC_CUDA_TRY(cudaStreamSynchronize(s));
+        check_device_error(ctx, s);
     });
 }
 
@@ -736,7 +759,7 @@ tdic_status tdic_subset_compute(tdic_ctx* ctx, const void* reference, const void
             // Seed refinement runs on the clamp-padded, non-deconvolved coefficients of the same
             // deformed image (seed_selector.cpp:166-173); the lazy pair reuses the uploaded images.
             tdic_pair* lazy = nullptr;
-            st = tdic_pair_create(ctx, pair->ref.ptr, pair->def_f.ptr, width, height, 0, TDIC_F32, TDIC_DEVICE, degree,
+            st = tdic_pair_create(ctx, pair->ref.ptr, pair->def_f.ptr, width, height, pair->rpitch, TDIC_F32, TDIC_DEVICE, degree,
                                   cfg->border, 0, cfg->precision, s, &lazy);
             if (st != TDIC_OK) throw Error{st, ctx->last_error};
             tdic_seed seed{};

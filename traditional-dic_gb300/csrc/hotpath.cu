@@ -15,6 +15,9 @@
 // add cost but no accuracy.  The FP64 build is the same code with every T = double.
 #include "tdic_internal.cuh"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <cmath>
 
 namespace tdic {
@@ -57,18 +60,19 @@ __device__ __forceinline__ void named_bar(int id, int nthreads) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
-// All-reduce K values over the group (every thread ends with the same sums, summed in the
-// same order, so redundant scalar math stays bit-identical across the group's warps).
-// `red` holds two buffers of 32*G values used alternately (parity `rp`), so one named
-// barrier per reduction suffices: a buffer is rewritten only after every thread has passed the
-// barrier of the reduction in between, i.e. after all reads of its previous contents.
+// All-reduce K values over the group: every thread ends with the same sums (summed in the same
+// order), so redundant scalar math stays bit-identical across the group's warps.  Warp shuffles,
+// then thread k < K adds the G warp partials of value k, then everyone reads the K totals.
+// `red` holds two buffers of 32*G values used alternately (parity `rp`): a buffer is rewritten
+// only after every thread has passed the barriers of the reduction in between.
 template <int G, int K, typename T>
 __device__ __forceinline__ void group_sum(T (&v)[K], T* red_base, int& rp, int tid, int bar_id) {
-    static_assert(K <= 32, "reduction scratch holds 32 values per warp");
+    static_assert(G == 1 || K * (G + 1) <= 32 * G, "reduction scratch: G*K partials + K totals per buffer");
 #pragma unroll
     for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
     if constexpr (G > 1) {
         T* red = red_base + rp * 32 * G;
+        T* tot = red + G * K;
         rp ^= 1;
         const int warp = tid >> 5, lane = tid & 31;
         if (lane == 0) {
@@ -76,13 +80,15 @@ __device__ __forceinline__ void group_sum(T (&v)[K], T* red_base, int& rp, int t
             for (int k = 0; k < K; ++k) red[warp * K + k] = v[k];
         }
         named_bar(bar_id, 32 * G);
+        if (tid < K) {
+            T acc = red[tid];
 #pragma unroll
-        for (int k = 0; k < K; ++k) {
-            T s = red[k];
-#pragma unroll
-            for (int w = 1; w < G; ++w) s += red[w * K + k];
-            v[k] = s;
+            for (int w = 1; w < G; ++w) acc += red[w * K + tid];
+            tot[tid] = acc;
         }
+        named_bar(bar_id, 32 * G);
+#pragma unroll
+        for (int k = 0; k < K; ++k) v[k] = tot[k];
     }
 }
 
@@ -107,6 +113,39 @@ __device__ __forceinline__ bool group_any(bool p, int* flag, int tid, int bar_id
     }
 }
 
+// ---------------------------------------------------------------------------------------
+// TMA (cp.async.bulk.tensor) and mbarrier helpers.  Every wait is bounded: on timeout the
+// caller records an error and leaves the kernel.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ int floor_to(int v, int a) {  // largest multiple of a not above v (a > 0)
+    const int r = v % a;
+    return v - (r < 0 ? r + a : r);
+}
+constexpr long long kTmaSpinLimit = 1ll << 22;  // try_wait suspends in hardware between polls
+
 template <typename T> __device__ __forceinline__ bool finite6(const T* p) {
     bool ok = true;
 #pragma unroll
@@ -117,8 +156,13 @@ template <typename T> __device__ __forceinline__ bool finite6(const T* p) {
 // ---------------------------------------------------------------------------------------
 // 6x6 LDLT with symmetric diagonal pivoting and sign tracking: success / positivity
 // semantics of Eigen::LDLT as used at icgn.cpp:538-542 and forward_gauss_newton.cpp:354-358;
-// solve applies the pseudo-inverse of D (zero where |D_ii| <= DBL_MIN).
+// solve applies the pseudo-inverse of D (zero where |D_ii| is not above the smallest normal).
 // ---------------------------------------------------------------------------------------
+// Smallest normal of M (the pseudo-inverse threshold of the LDLT solve).
+template <typename M> __device__ __forceinline__ M tiny_normal();
+template <> __device__ __forceinline__ float tiny_normal<float>() { return 1.17549435e-38f; }
+template <> __device__ __forceinline__ double tiny_normal<double>() { return 2.2250738585072014e-308; }
+
 template <typename M>
 struct Ldlt6 {
     M m[6][6];
@@ -179,7 +223,7 @@ struct Ldlt6 {
             else if (sign == 2) { if (akk > M(0)) sign = 3; }
             else if (sign == 0) { if (akk > M(0)) sign = 1; else if (akk < M(0)) sign = 2; }
         }
-        for (int i = 0; i < 6; ++i) dinv[i] = fabs(m[i][i]) > M(2.2250738585072014e-308) ? M(1) / m[i][i] : M(0);
+        for (int i = 0; i < 6; ++i) dinv[i] = fabs(m[i][i]) > tiny_normal<M>() ? M(1) / m[i][i] : M(0);
     }
     __device__ bool good() const { return ok && (sign == 1 || sign == 0); }
     __device__ void solve(const M (&b)[6], M (&x)[6]) const {
@@ -261,6 +305,10 @@ struct Env {
     int max_iter;
     double thr;
     double inv_n;          // 1 / n
+    int rpitch, cpitch;    // row pitches (elements) of ref and coef
+    int rbx, rby;          // TMA box of the reference window (floats)
+    int cbx, cby;          // TMA box of the coefficient window (T)
+    int* err;              // device error flag (TMA wait timeout)
 };
 
 struct Result {
@@ -283,22 +331,159 @@ __device__ __forceinline__ void result_init(Result& r, const double (&p0)[6], do
     r.conv = false;
 }
 
-// Per-iteration scalar type: the FP32-mixed build keeps the 6x6 inverse, the parameter
-// vector and its update in float (FP64 stays in the setup factorisation / inverse and in the
-// combine of the normalisation sums); the FP64 build is double throughout.
+// Per-iteration scalar type: the FP32-mixed build keeps the 6x6 algebra, the parameter vector
+// and its update in float (FP64 only combines the normalisation sums); the FP64 build is
+// double throughout.
 template <typename T> struct MixedOf { using type = T; };
 
-// Warp the samples of this thread, interpolate, store g (and for FGN its gradient) and
-// accumulate the shifted normalisation sums.  Returns false if a warped point left the image.
+
+// Unpivoted LDL^T of a 6x6 symmetric matrix, fully unrolled in registers.  Succeeds only when
+// every pivot is positive and finite; for such (numerically positive definite) matrices the
+// pivoted factorisation of icgn.cpp:538 reports success and isPositive() as well, so the
+// outcome is the same.  Anything else falls back to the pivoted Ldlt6.
+template <typename M>
+struct FastLdlt6 {
+    M L[6][6];
+    M D[6];
+    M dinv[6];
+    __device__ __forceinline__ bool factor(const M (&H)[6][6]) {
+        bool ok = true;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+            M LD[6];  // L[j][k] * D[k]
+#pragma unroll
+            for (int k = 0; k < j; ++k) LD[k] = L[j][k] * D[k];
+            M d = H[j][j];
+#pragma unroll
+            for (int k = 0; k < j; ++k) d -= L[j][k] * LD[k];
+            ok = ok && (d > M(0)) && isfinite(d);
+            D[j] = d;
+            dinv[j] = M(1) / d;
+#pragma unroll
+            for (int i = j + 1; i < 6; ++i) {
+                M v = H[i][j];
+#pragma unroll
+                for (int k = 0; k < j; ++k) v -= L[i][k] * LD[k];
+                L[i][j] = v * dinv[j];
+            }
+        }
+        return ok;
+    }
+    // x = H^-1 b
+    __device__ __forceinline__ void solve(const M (&b)[6], M (&x)[6]) const {
+        M y[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            M v = b[i];
+#pragma unroll
+            for (int k = 0; k < i; ++k) v -= L[i][k] * y[k];
+            y[i] = v;
+        }
+#pragma unroll
+        for (int i = 5; i >= 0; --i) {
+            M v = y[i] * dinv[i];
+#pragma unroll
+            for (int k = i + 1; k < 6; ++k) v -= L[k][i] * x[k];
+            x[i] = v;
+        }
+    }
+};
+
+// Factorise H and store H^-1 (row-major, 36 values) in shared memory; returns false when the
+// reference's LDLT would fail or report a matrix that is not positive semidefinite.
+template <int G, typename M>
+__device__ bool factor_inverse(const M (&H)[6][6], M* s_hinv, int tid, int bar_id) {
+    FastLdlt6<M> f;
+    bool good = f.factor(H);
+    if (good) {
+        if (tid < 6) {
+            M e6[6] = {M(0), M(0), M(0), M(0), M(0), M(0)}, col[6];
+            e6[tid] = M(1);
+            f.solve(e6, col);
+#pragma unroll
+            for (int i = 0; i < 6; ++i) s_hinv[i * 6 + tid] = col[i];
+        }
+    } else {
+        Ldlt6<M> g;
+        g.factor(H);
+        good = g.good();
+        if (good && tid < 6) {
+            M e6[6] = {M(0), M(0), M(0), M(0), M(0), M(0)}, col[6];
+            e6[tid] = M(1);
+            g.solve(e6, col);
+            for (int i = 0; i < 6; ++i) s_hinv[i * 6 + tid] = col[i];
+        }
+    }
+    return good;
+}
+
+template <int G, typename M>
+__device__ bool factor_solve(const M (&H)[6][6], const M (&b)[6], M (&x)[6]) {
+    FastLdlt6<M> f;
+    if (f.factor(H)) { f.solve(b, x); return true; }
+    Ldlt6<M> g;
+    g.factor(H);
+    if (!g.good()) return false;
+    g.solve(b, x);
+    return true;
+}
+
+__host__ __device__ __forceinline__ size_t round128(size_t b) { return (b + 127) & ~size_t(127); }
+
+// Per-group shared memory, each part 128-byte aligned (TMA destinations):
+// [coefficient window cbx*cby T][reference window rbx*rby float][mbarrier + 6x6 inverse (36
+// doubles) + ints][2 x 32*G T reduction scratch][4*nmax T samples f^, a, b, g].
+template <typename T>
+__host__ __device__ __forceinline__ size_t group_smem_bytes(int nmax, int G, int rbx, int rby, int cbx, int cby) {
+    size_t b = round128(static_cast<size_t>(cbx) * cby * sizeof(T));
+    b += round128(static_cast<size_t>(rbx) * rby * sizeof(float));
+    b += round128(16 + 36 * sizeof(double) + 16);
+    b += round128((static_cast<size_t>(64) * G + static_cast<size_t>(4) * nmax) * sizeof(T));
+    return b;
+}
+// CTA prefix: the sample-offset table shared by all groups.
+__host__ __device__ __forceinline__ size_t cta_prefix_bytes(int nmax) { return round128(sizeof(short2) * nmax); }
+
+template <typename T>
+struct GroupSmem {
+    T* cwin;
+    float* rwin;
+    uint64_t* bar;
+    double* hinv;
+    int* ints;
+    T* red;
+    T* sm;
+    __device__ GroupSmem(unsigned char* base, int gi, int nmax, int G, int rbx, int rby, int cbx, int cby) {
+        unsigned char* g = base + gi * group_smem_bytes<T>(nmax, G, rbx, rby, cbx, cby);
+        cwin = reinterpret_cast<T*>(g);
+        g += round128(static_cast<size_t>(cbx) * cby * sizeof(T));
+        rwin = reinterpret_cast<float*>(g);
+        g += round128(static_cast<size_t>(rbx) * rby * sizeof(float));
+        bar = reinterpret_cast<uint64_t*>(g);
+        hinv = reinterpret_cast<double*>(g + 16);
+        ints = reinterpret_cast<int*>(g + 16 + 36 * sizeof(double));
+        g += round128(16 + 36 * sizeof(double) + 16);
+        red = reinterpret_cast<T*>(g);
+        sm = red + 64 * G;
+    }
+};
+
+constexpr int kDriftMargin = 3;  // px of parameter drift covered by the staged coefficient window
+
+// Warp this thread's samples, interpolate from the staged coefficient window (global memory for
+// a stencil outside it), store g (and for FGN the spline gradient), accumulate the shifted
+// normalisation sums.  Returns false if a warped point left the image.
 template <int DEG, typename T, bool GRAD>
-__device__ __forceinline__ bool warp_interp(const Env<T>& e, int cx, int cy, const T (&p)[6], T fm, T* s_g,
-                                            T* s_gx, T* s_gy, int tid, int nt, Kahan<T>& sg, Kahan<T>& sg2) {
+__device__ __forceinline__ bool warp_interp(const Env<T>& e, int cx, int cy, const T (&p)[6], T fm, T* s_g, T* s_gx,
+                                            T* s_gy, const short2* off, const T* cwin, int wc0, int wr0, int tid,
+                                            int nt, Kahan<T>& sg, Kahan<T>& sg2) {
+    const int ww = e.cbx, wh = e.cby;
     constexpr int NB = DEG + 1, OFF = DEG / 2;
     bool ok = true;
     const T xlo = T(-cx), ylo = T(-cy), xhi = T(e.w - 1 - cx), yhi = T(e.h - 1 - cy);
 #pragma unroll 2
     for (int i = tid; i < e.n; i += nt) {
-        const short2 o = __ldg(e.off + i);
+        const short2 o = off[i];
         const T lx = T(o.x), ly = T(o.y);
         const T tx = ((lx + p[0]) + p[2] * lx) + p[3] * ly;
         const T ty = ((ly + p[1]) + p[4] * lx) + p[5] * ly;
@@ -309,12 +494,22 @@ __device__ __forceinline__ bool warp_interp(const Env<T>& e, int cx, int cy, con
         T wx[NB], wy[NB];
         weights<DEG, T>(dx, wx);
         weights<DEG, T>(dy, wy);
-        const T* base = e.coef + static_cast<size_t>(cy + iy + e.border - OFF) * e.cw + (cx + ix + e.border - OFF);
+        const int col = cx + ix + e.border - OFF, row = cy + iy + e.border - OFF;  // stencil corner
+        const int lc = col - wc0, lr = row - wr0;
         T c[NB][NB];
+        if (lc >= 0 && lr >= 0 && lc + NB <= ww && lr + NB <= wh) {
+            const T* b = cwin + lr * ww + lc;
 #pragma unroll
-        for (int m = 0; m < NB; ++m)
+            for (int m = 0; m < NB; ++m)
 #pragma unroll
-            for (int q = 0; q < NB; ++q) c[m][q] = __ldg(base + m * e.cw + q);
+                for (int q = 0; q < NB; ++q) c[m][q] = b[m * ww + q];
+        } else {
+            const T* b = e.coef + static_cast<size_t>(row) * e.cpitch + col;
+#pragma unroll
+            for (int m = 0; m < NB; ++m)
+#pragma unroll
+                for (int q = 0; q < NB; ++q) c[m][q] = __ldg(b + m * e.cpitch + q);
+        }
         T g = T(0);
 #pragma unroll
         for (int m = 0; m < NB; ++m) {
@@ -347,72 +542,112 @@ __device__ __forceinline__ bool warp_interp(const Env<T>& e, int cx, int cy, con
     return ok;
 }
 
+template <typename M>
+__device__ __forceinline__ void hessian_from_sums(const M (&S)[18], M scale, M (&Hm)[6][6]) {
+    // S(u, v) with u in {aa, ab, bb}, v in {1, lx, ly, lx^2, lx ly, ly^2}; SD = [a, b, a lx, a ly, b lx, b ly]
+    auto s = [&](int u, int v) { return S[u * 6 + v]; };
+    Hm[0][0] = s(0, 0); Hm[0][1] = s(1, 0); Hm[0][2] = s(0, 1); Hm[0][3] = s(0, 2); Hm[0][4] = s(1, 1); Hm[0][5] = s(1, 2);
+    Hm[1][1] = s(2, 0); Hm[1][2] = s(1, 1); Hm[1][3] = s(1, 2); Hm[1][4] = s(2, 1); Hm[1][5] = s(2, 2);
+    Hm[2][2] = s(0, 3); Hm[2][3] = s(0, 4); Hm[2][4] = s(1, 3); Hm[2][5] = s(1, 4);
+    Hm[3][3] = s(0, 5); Hm[3][4] = s(1, 4); Hm[3][5] = s(1, 5);
+    Hm[4][4] = s(2, 3); Hm[4][5] = s(2, 4);
+    Hm[5][5] = s(2, 5);
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = i; j < 6; ++j) { Hm[i][j] *= scale; Hm[j][i] = Hm[i][j]; }
+}
+
 // The per-POI solve.  OPT 0 = ICGN (icgn.cpp:446-627), 1 = FGN (forward_gauss_newton.cpp:188-399).
-// sm: 4 * nmax T values of this group; red: 2 x 32 * G T values; flag: one int.
+// `off` is the sample-offset table in shared memory; `phase` the parity of the group's
+// mbarrier (flips once per staged POI).  Returns false only when a TMA wait timed out (the
+// kernel must then leave: the copy may still land in shared memory).
 template <int OPT, int DEG, typename T, int G>
-__device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6], double conf, T* sm, T* red,
-                          int* flag, double* s_hinv_raw, int tid, int bar_id, Result& R) {
+__device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUtensorMap* tm_coef, const short2* off,
+                          int cx, int cy, const double (&p0)[6], double conf, const GroupSmem<T>& gs,
+                          uint32_t& phase, int tid, int bar_id, Result& R) {
     using M = typename MixedOf<T>::type;
-    M* s_hinv = reinterpret_cast<M*>(s_hinv_raw);
-    constexpr int NT = 32 * G;
+    constexpr int NT = 32 * G, OFF = DEG / 2;
+    M* s_hinv = reinterpret_cast<M*>(gs.hinv);
+    T* red = gs.red;
     result_init(R, p0, conf);
     int rp = 0;  // reduction-buffer parity
     const int r = e.radius;
-    if (e.w <= 0 || r < 1 || e.max_iter < 0) return;
-    if (cx - r < 0 || cy - r < 0 || cx + r >= e.w || cy + r >= e.h) return;
-    if (e.n < 6) return;
-    T* s_fn = sm;
-    T* s_a = sm + e.nmax;      // ICGN: reference gx; FGN: deformed gx
-    T* s_b = sm + 2 * e.nmax;  // ICGN: reference gy; FGN: deformed gy
-    T* s_g = sm + 3 * e.nmax;
+    if (e.w <= 0 || r < 1 || e.max_iter < 0) return true;
+    if (cx - r < 0 || cy - r < 0 || cx + r >= e.w || cy + r >= e.h) return true;
+    if (e.n < 6) return true;
+    T* s_fn = gs.sm;
+    T* s_a = gs.sm + e.nmax;      // ICGN: reference gx; FGN: deformed gx
+    T* s_b = gs.sm + 2 * e.nmax;  // ICGN: reference gy; FGN: deformed gy
+    T* s_g = gs.sm + 3 * e.nmax;
     const int W = e.w, H = e.h;
 
-    // --- setup: reference values (and ICGN gradients), mean -------------------------------
-    Kahan<T> ksum;
+    // --- TMA staging: the reference window (subset + one-pixel halo) and the coefficient
+    //     window under the subset warped by the initial guess (+ drift margin) ---------------
+    const int rx0 = floor_to(cx - r - 1, 4), ry0 = cy - r - 1;  // 16-byte aligned x (float)
+    constexpr int kAlign = 16 / static_cast<int>(sizeof(T));
+    int wc0 = 0, wr0 = 0;
+    {
+        // the box only needs the warped corners to a pixel (the drift margin is 3 px): float
+        // arithmetic keeps this off the GB300's narrow FP64 pipe
+        const float q0 = static_cast<float>(p0[0]), q1 = static_cast<float>(p0[1]), q2 = static_cast<float>(p0[2]),
+                    q3 = static_cast<float>(p0[3]), q4 = static_cast<float>(p0[4]), q5 = static_cast<float>(p0[5]);
+        const float rf = static_cast<float>(r);
+        const float ax = fabsf(q2) * rf + fabsf(q3) * rf, ay = fabsf(q4) * rf + fabsf(q5) * rf;
+        const float txmin = -rf + q0 - ax, tymin = -rf + q1 - ay;
+        const float txmax = rf + q0 + ax, tymax = rf + q1 + ay;
+        // a non-finite or absurd guess stages an arbitrary in-range box; samples outside it
+        // read global memory (and warps leaving the image end the solve anyway)
+        const bool sane = txmin > -1e6f && txmax < 1e6f && tymin > -1e6f && tymax < 1e6f;
+        const int c0 = sane ? cx + static_cast<int>(floorf(txmin)) - kDriftMargin + e.border - OFF : 0;
+        const int r0 = sane ? cy + static_cast<int>(floorf(tymin)) - kDriftMargin + e.border - OFF : 0;
+        wc0 = floor_to(min(max(c0, -e.cbx), e.cw), kAlign);
+        wr0 = min(max(r0, -e.cby), e.h + 2 * e.border);
+    }
+    group_sync<G>(bar_id);  // previous readers of the windows are done
+    if (tid == 0) {
+        fence_proxy_async();
+        mbar_expect_tx(gs.bar, static_cast<uint32_t>(e.rbx * e.rby * sizeof(float) + e.cbx * e.cby * sizeof(T)));
+        tma_load_2d(gs.rwin, tm_ref, rx0, ry0, gs.bar);
+        tma_load_2d(gs.cwin, tm_coef, wc0, wr0, gs.bar);
+    }
+    {
+        long long spins = 0;
+        while (!mbar_try_wait(gs.bar, phase)) {
+            if (++spins > kTmaSpinLimit) {
+                atomicExch(e.err, 3);
+                return false;
+            }
+        }
+        phase ^= 1u;
+    }
+
+    // --- one pass: reference values, gradients, shifted sums and Hessian sums ------------------
+    const int rww = e.rbx;
+    const float fshift = gs.rwin[(cy - ry0) * rww + (cx - rx0)];  // centre pixel: sums of f - fshift
+    Kahan<T> k1, k2;
+    T hs[18];
+#pragma unroll
+    for (int k = 0; k < 18; ++k) hs[k] = T(0);
     for (int i = tid; i < e.n; i += NT) {
-        const short2 o = __ldg(e.off + i);
+        const short2 o = off[i];
         const int x = cx + o.x, y = cy + o.y;
-        const float f = __ldg(e.ref + static_cast<size_t>(y) * W + x);
+        const float f = gs.rwin[(y - ry0) * rww + (x - rx0)];
         s_fn[i] = T(f);
+        const T fd = T(f) - T(fshift);
+        k1.add(fd);
+        k2.add(fd * fd);
         if constexpr (OPT == 0) {
             // reference gradient cache, reliability_propagation.cpp:84-112
             const int xm = max(0, x - 1), xp = min(W - 1, x + 1), ym = max(0, y - 1), yp = min(H - 1, y + 1);
-            const T gx = (T(__ldg(e.ref + static_cast<size_t>(y) * W + xp)) - T(__ldg(e.ref + static_cast<size_t>(y) * W + xm))) /
-                         T(max(1, xp - xm));
-            const T gy = (T(__ldg(e.ref + static_cast<size_t>(yp) * W + x)) - T(__ldg(e.ref + static_cast<size_t>(ym) * W + x))) /
-                         T(max(1, yp - ym));
-            s_a[i] = gx;
-            s_b[i] = gy;
-        }
-        ksum.add(T(f));
-    }
-    T v1[1] = {ksum.value()};
-    group_sum<G, 1>(v1, red, rp, tid, bar_id);
-    const double inv_n = e.inv_n;  // 1 / N, from the host (no device-side FP64 divide)
-    const double mean = static_cast<double>(v1[0]) * inv_n;
-    const T fm = T(mean);
-    Kahan<T> knorm;
-    for (int i = tid; i < e.n; i += NT) {
-        const T d = s_fn[i] - fm;
-        knorm.add(d * d);
-    }
-    v1[0] = knorm.value();
-    group_sum<G, 1>(v1, red, rp, tid, bar_id);
-    const double ss = static_cast<double>(v1[0]);  // sum (f - mean)^2
-    if (!(ss > kEps * kEps)) { R.status = TDIC_NUMERICAL_FAILURE; return; }  // |f - mean| <= 1e-12
-    const T inv_norm = T(1) / sqrt(T(ss));
-
-    if constexpr (OPT == 0) {
-        // normalised reference and Hessian sums: H = (2/|f|^2) sum SD SD^T with
-        // SD = [a, b, a lx, a ly, b lx, b ly]; 18 distinct sums {aa, ab, bb} x {1, lx, ly, lx^2, lx ly, ly^2}
-        T hs[18];
-#pragma unroll
-        for (int k = 0; k < 18; ++k) hs[k] = T(0);
-        for (int i = tid; i < e.n; i += NT) {
-            const short2 o = __ldg(e.off + i);
+            // the divisor is 1 (one-sided) or 2 (central): multiplying by 1 or 0.5 is exact
+            const T a = (T(gs.rwin[(y - ry0) * rww + (xp - rx0)]) - T(gs.rwin[(y - ry0) * rww + (xm - rx0)])) *
+                        (xp - xm == 2 ? T(0.5) : T(1));
+            const T b = (T(gs.rwin[(yp - ry0) * rww + (x - rx0)]) - T(gs.rwin[(ym - ry0) * rww + (x - rx0)])) *
+                        (yp - ym == 2 ? T(0.5) : T(1));
+            s_a[i] = a;
+            s_b[i] = b;
             const T lx = T(o.x), ly = T(o.y);
-            s_fn[i] = (s_fn[i] - fm) * inv_norm;
-            const T a = s_a[i], b = s_b[i];
             const T q[3] = {a * a, a * b, b * b};
             const T m6[6] = {T(1), lx, ly, lx * lx, lx * ly, ly * ly};
 #pragma unroll
@@ -420,35 +655,39 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
 #pragma unroll
                 for (int v = 0; v < 6; ++v) hs[u * 6 + v] += q[u] * m6[v];
         }
-        group_sum<G, 18>(hs, red, rp, tid, bar_id);
-        // index map: S(u, v) with u in {aa, ab, bb}, v in {1, lx, ly, lxlx, lxly, lyly}
-        auto S = [&](int u, int v) { return static_cast<M>(hs[u * 6 + v]); };
-        M Hm[6][6];
-        Hm[0][0] = S(0, 0); Hm[0][1] = S(1, 0); Hm[0][2] = S(0, 1); Hm[0][3] = S(0, 2); Hm[0][4] = S(1, 1); Hm[0][5] = S(1, 2);
-        Hm[1][1] = S(2, 0); Hm[1][2] = S(1, 1); Hm[1][3] = S(1, 2); Hm[1][4] = S(2, 1); Hm[1][5] = S(2, 2);
-        Hm[2][2] = S(0, 3); Hm[2][3] = S(0, 4); Hm[2][4] = S(1, 3); Hm[2][5] = S(1, 4);
-        Hm[3][3] = S(0, 5); Hm[3][4] = S(1, 4); Hm[3][5] = S(1, 5);
-        Hm[4][4] = S(2, 3); Hm[4][5] = S(2, 4);
-        Hm[5][5] = S(2, 5);
-        const M hsc = M(2) * inv_norm * inv_norm;
-        for (int i = 0; i < 6; ++i)
-            for (int j = i; j < 6; ++j) { Hm[i][j] *= hsc; Hm[j][i] = Hm[i][j]; }
-        Ldlt6<M> f;  // once per POI
-        f.factor(Hm);
-        if (!f.good()) { R.status = TDIC_NUMERICAL_FAILURE; return; }
-        // explicit inverse, column by column (the reference's per-iteration solves applied to
-        // unit vectors); kept in the group's shared memory
-        group_sync<G>(bar_id);
-        if (tid < 6) {
-            M ej[6] = {0, 0, 0, 0, 0, 0}, col[6];
-            ej[tid] = M(1);
-            f.solve(ej, col);
-            for (int i = 0; i < 6; ++i) s_hinv[i * 6 + tid] = col[i];
-        }
-        group_sync<G>(bar_id);
-    } else {
-        for (int i = tid; i < e.n; i += NT) s_fn[i] = (s_fn[i] - fm) * inv_norm;
     }
+    T v20[20];
+    v20[0] = k1.value();
+    v20[1] = k2.value();
+#pragma unroll
+    for (int k = 0; k < 18; ++k) v20[2 + k] = hs[k];
+    if constexpr (OPT == 0) {
+        group_sum<G, 20>(v20, red, rp, tid, bar_id);
+    } else {
+        T v2s[2] = {v20[0], v20[1]};
+        group_sum<G, 2>(v2s, red, rp, tid, bar_id);
+        v20[0] = v2s[0];
+        v20[1] = v2s[1];
+    }
+    // normalisation sums combined in FP64: mean = shift + S1/N, sum (f - mean)^2 = S2 - S1^2/N
+    const double inv_n = e.inv_n;
+    const double s1 = static_cast<double>(v20[0]), s2 = static_cast<double>(v20[1]);
+    const double mshift = s1 * inv_n;
+    const double ss = fma(-s1, mshift, s2);
+    if (!(ss > kEps * kEps)) { R.status = TDIC_NUMERICAL_FAILURE; return true; }  // |f - mean| <= 1e-12
+    const T fm = T(static_cast<double>(fshift) + mshift);
+    const T inv_norm = T(1) / sqrt(T(ss));
+    for (int i = tid; i < e.n; i += NT) s_fn[i] = (s_fn[i] - fm) * inv_norm;
+    if constexpr (OPT == 0) {
+        M S[18];
+#pragma unroll
+        for (int k = 0; k < 18; ++k) S[k] = static_cast<M>(v20[2 + k]);
+        M Hm[6][6];
+        hessian_from_sums<M>(S, M(2) * inv_norm * inv_norm, Hm);
+        const bool good = factor_inverse<G, M>(Hm, s_hinv, tid, bar_id);
+        if (!good) { R.status = TDIC_NUMERICAL_FAILURE; return true; }
+    }
+    group_sync<G>(bar_id);  // f^ (and the inverse) visible to the whole group
 
     M p[6];
     for (int k = 0; k < 6; ++k) p[k] = static_cast<M>(p0[k]);
@@ -461,26 +700,25 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
 #pragma unroll
         for (int k = 0; k < 6; ++k) pt[k] = static_cast<T>(p[k]);
         Kahan<T> sg, sg2;
-        const bool ok = warp_interp<DEG, T, OPT == 1>(e, cx, cy, pt, fm, s_g, s_a, s_b, tid, NT, sg, sg2);
+        const bool ok = warp_interp<DEG, T, OPT == 1>(e, cx, cy, pt, fm, s_g, s_a, s_b, off, gs.cwin, wc0, wr0, tid,
+                                                      NT, sg, sg2);
         // one reduction carries the two normalisation sums and the out-of-image count
-        T v2[3] = {sg.value(), sg2.value(), ok ? T(0) : T(1)};
-        group_sum<G, 3>(v2, red, rp, tid, bar_id);
-        if (v2[2] != T(0)) { R.status = TDIC_INVALID_INPUT; return; }
+        T v3[3] = {sg.value(), sg2.value(), ok ? T(0) : T(1)};
+        group_sum<G, 3>(v3, red, rp, tid, bar_id);
+        if (v3[2] != T(0)) { R.status = TDIC_INVALID_INPUT; return true; }
         // normalisation sums combined in FP64: mean of (g - fm) and sum (g - mean)^2
-        const double gmr = static_cast<double>(v2[0]) * inv_n;
-        const double var = fma(-static_cast<double>(v2[0]), gmr, static_cast<double>(v2[1]));
-        if (!(var > kEps * kEps)) { R.status = TDIC_NUMERICAL_FAILURE; return; }  // |g - mean| <= 1e-12
+        const double gmr = static_cast<double>(v3[0]) * inv_n;
+        const double var = fma(-static_cast<double>(v3[0]), gmr, static_cast<double>(v3[1]));
+        if (!(var > kEps * kEps)) { R.status = TDIC_NUMERICAL_FAILURE; return true; }  // |g - mean| <= 1e-12
         const T gsh = T(gmr);
-        T inv_gn;
-        if constexpr (sizeof(T) == 4) inv_gn = 1.0f / sqrtf(static_cast<float>(var));
-        else inv_gn = T(1.0 / sqrt(var));
+        const T inv_gn = T(1) / sqrt(T(var));
         M dp[6];
         if constexpr (OPT == 0) {
             T q[7];
 #pragma unroll
             for (int k = 0; k < 7; ++k) q[k] = T(0);
             for (int i = tid; i < e.n; i += NT) {
-                const short2 o = __ldg(e.off + i);
+                const short2 o = off[i];
                 const T lx = T(o.x), ly = T(o.y);
                 const T diff = s_fn[i] - ((s_g[i] - fm) - gsh) * inv_gn;
                 const T da = diff * s_a[i], db = diff * s_b[i];
@@ -490,13 +728,14 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
             group_sum<G, 7>(q, red, rp, tid, bar_id);
             corr = static_cast<double>(q[6]);
             M grad[6];
+#pragma unroll
             for (int k = 0; k < 6; ++k) grad[k] = static_cast<M>(q[k]) * gscale;
 #pragma unroll
             for (int i = 0; i < 6; ++i) {
-                M s = M(0);
+                M sacc = M(0);
 #pragma unroll
-                for (int j = 0; j < 6; ++j) s += s_hinv[i * 6 + j] * grad[j];
-                dp[i] = -s;
+                for (int j = 0; j < 6; ++j) sacc += s_hinv[i * 6 + j] * grad[j];
+                dp[i] = -sacc;
             }
         } else {
             // FGN: SD from the deformed spline gradient through dW/dz (forward_gauss_newton.cpp:44-60)
@@ -505,7 +744,7 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
 #pragma unroll
             for (int k = 0; k < 25; ++k) q[k] = T(0);
             for (int i = tid; i < e.n; i += NT) {
-                const short2 o = __ldg(e.off + i);
+                const short2 o = off[i];
                 const T lx = T(o.x), ly = T(o.y);
                 const T gx = s_a[i], gy = s_b[i];
                 const T ae = gx * (T(1) + p2) + gy * p4;
@@ -523,26 +762,19 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
             }
             group_sum<G, 25>(q, red, rp, tid, bar_id);
             corr = static_cast<double>(q[24]);
-            auto S = [&](int u, int v) { return static_cast<M>(q[u * 6 + v]); };
+            M S[18];
+#pragma unroll
+            for (int k = 0; k < 18; ++k) S[k] = static_cast<M>(q[k]);
             M Hm[6][6];
-            Hm[0][0] = S(0, 0); Hm[0][1] = S(1, 0); Hm[0][2] = S(0, 1); Hm[0][3] = S(0, 2); Hm[0][4] = S(1, 1); Hm[0][5] = S(1, 2);
-            Hm[1][1] = S(2, 0); Hm[1][2] = S(1, 1); Hm[1][3] = S(1, 2); Hm[1][4] = S(2, 1); Hm[1][5] = S(2, 2);
-            Hm[2][2] = S(0, 3); Hm[2][3] = S(0, 4); Hm[2][4] = S(1, 3); Hm[2][5] = S(1, 4);
-            Hm[3][3] = S(0, 5); Hm[3][4] = S(1, 4); Hm[3][5] = S(1, 5);
-            Hm[4][4] = S(2, 3); Hm[4][5] = S(2, 4);
-            Hm[5][5] = S(2, 5);
-            const M hsc = M(2) * inv_norm * inv_norm;
-            for (int i = 0; i < 6; ++i)
-                for (int j = i; j < 6; ++j) { Hm[i][j] *= hsc; Hm[j][i] = Hm[i][j]; }
+            hessian_from_sums<M>(S, M(2) * inv_norm * inv_norm, Hm);
             M grad[6];
+#pragma unroll
             for (int k = 0; k < 6; ++k) grad[k] = static_cast<M>(q[18 + k]) * gscale;
-            Ldlt6<M> f;  // FGN refactorises every iteration
-            f.factor(Hm);
-            if (!f.good()) { R.status = TDIC_NUMERICAL_FAILURE; return; }
-            f.solve(grad, dp);
+            if (!factor_solve<G, M>(Hm, grad, dp)) { R.status = TDIC_NUMERICAL_FAILURE; return true; }
         }
-        if (!finite6(dp)) { R.status = TDIC_NUMERICAL_FAILURE; return; }
+        if (!finite6(dp)) { R.status = TDIC_NUMERICAL_FAILURE; return true; }
         M dn2 = M(0);
+#pragma unroll
         for (int k = 0; k < 6; ++k) dn2 += dp[k] * dp[k];
         M dn = sqrt(dn2);
         M pn[6];
@@ -550,13 +782,16 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
             ic_update<M>(p, dp, pn);
         } else {
             if (dn > M(0.5)) {  // forward_gauss_newton.cpp:367-371
-                for (int k = 0; k < 6; ++k) dp[k] *= M(0.5) / dn;
+                const M sc = M(0.5) / dn;
+#pragma unroll
+                for (int k = 0; k < 6; ++k) dp[k] *= sc;
                 dn = M(0.5);
             }
             compose_warp<M>(p, dp, pn);
         }
+#pragma unroll
         for (int k = 0; k < 6; ++k) p[k] = pn[k];
-        if (!finite6(p)) { R.status = TDIC_NUMERICAL_FAILURE; return; }
+        if (!finite6(p)) { R.status = TDIC_NUMERICAL_FAILURE; return true; }
         if (dn < M(e.thr)) { converged = true; break; }
     }
     for (int k = 0; k < 6; ++k) R.p[k] = static_cast<double>(p[k]);
@@ -565,29 +800,8 @@ __device__ void solve_poi(const Env<T>& e, int cx, int cy, const double (&p0)[6]
     if (!converged && isfinite(corr)) converged = true;
     R.status = converged ? TDIC_SUCCESS : TDIC_NOT_CONVERGED;
     R.valid = converged;
+    return true;
 }
-
-// Per-group shared memory: [36 doubles: 6x6 inverse][16 bytes: ints][32*G T: reduction
-// scratch][4*nmax T: samples f^, a, b, g].
-template <typename T> __host__ __device__ __forceinline__ size_t group_smem_bytes(int nmax, int G) {
-    const size_t bytes = 36 * sizeof(double) + 16 + (static_cast<size_t>(4) * nmax + 64 * G) * sizeof(T);
-    return (bytes + 15) & ~size_t(15);
-}
-
-template <typename T>
-struct GroupSmem {
-    double* hinv;
-    int* ints;
-    T* red;
-    T* sm;
-    __device__ GroupSmem(unsigned char* base, int gi, int nmax, int G) {
-        unsigned char* g = base + gi * group_smem_bytes<T>(nmax, G);
-        hinv = reinterpret_cast<double*>(g);
-        ints = reinterpret_cast<int*>(g + 36 * sizeof(double));
-        red = reinterpret_cast<T*>(g + 36 * sizeof(double) + 16);
-        sm = red + 64 * G;
-    }
-};
 
 __device__ __forceinline__ void write_out(tdic_poi_out* o, const Result& R) {
     for (int k = 0; k < 6; ++k) o->p[k] = R.p[k];
@@ -614,19 +828,63 @@ __device__ __forceinline__ int group_bcast(int v, int* slot, int tid, int bar_id
     }
 }
 
+// Broadcast three ints from group thread 0 (slots[0..2]) with one pair of barriers.
+template <int G>
+__device__ __forceinline__ void group_bcast3(int& a, int& b, int& c, int* slots, int tid, int bar_id) {
+    if constexpr (G == 1) {
+        a = __shfl_sync(0xffffffffu, a, 0);
+        b = __shfl_sync(0xffffffffu, b, 0);
+        c = __shfl_sync(0xffffffffu, c, 0);
+    } else {
+        named_bar(bar_id, 32 * G);
+        if (tid == 0) { slots[0] = a; slots[1] = b; slots[2] = c; }
+        named_bar(bar_id, 32 * G);
+        a = slots[0];
+        b = slots[1];
+        c = slots[2];
+    }
+}
+
+// Kernel preamble: copy the sample-offset table into shared memory (CTA-wide) and initialise
+// each group's mbarrier.  Returns the shared offset table.
+template <typename T, int G>
+__device__ short2* kernel_preamble(const Env<T>& e, const CUtensorMap* tm_ref, const CUtensorMap* tm_coef,
+                                   unsigned char* smem_raw, int gi, int tid) {
+    // TMA destinations need 128-byte alignment; the layout assumes an aligned dynamic base.
+    if ((smem_u32(smem_raw) & 127u) != 0u) {
+        if (threadIdx.x == 0) atomicExch(e.err, 4);
+        return nullptr;
+    }
+    short2* s_off = reinterpret_cast<short2*>(smem_raw);
+    for (int i = threadIdx.x; i < e.n; i += blockDim.x) s_off[i] = e.off[i];
+    if (tid == 0) {
+        GroupSmem<T> gs(smem_raw + cta_prefix_bytes(e.nmax), gi, e.nmax, G, e.rbx, e.rby, e.cbx, e.cby);
+        mbar_init(gs.bar, 1);
+        fence_proxy_async();
+    }
+    if (threadIdx.x == 0) {
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tm_ref)) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tm_coef)) : "memory");
+    }
+    __syncthreads();
+    return s_off;
+}
+
 // ---------------------------------------------------------------------------------------
 // Batched solve: persistent groups pull POIs from a work counter.
 // ---------------------------------------------------------------------------------------
 template <int OPT, int DEG, typename T, int G>
-__global__ void solve_batch_kernel(Env<T> e, const tdic_poi_in* __restrict__ in, tdic_poi_out* __restrict__ out, int n,
-                                   int* fetch) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+__global__ void solve_batch_kernel(Env<T> e, const __grid_constant__ CUtensorMap tm_ref,
+                                   const __grid_constant__ CUtensorMap tm_coef, const tdic_poi_in* __restrict__ in,
+                                   tdic_poi_out* __restrict__ out, int n, int* fetch) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     const int gi = threadIdx.x / (32 * G), tid = threadIdx.x % (32 * G);
-    GroupSmem<T> gs(smem_raw, gi, e.nmax, G);
-    T* sm = gs.sm;
-    T* red = gs.red;
+    short2* s_off = kernel_preamble<T, G>(e, &tm_ref, &tm_coef, smem_raw, gi, tid);
+    if (s_off == nullptr) return;
+    GroupSmem<T> gs(smem_raw + cta_prefix_bytes(e.nmax), gi, e.nmax, G, e.rbx, e.rby, e.cbx, e.cby);
     int* ints = gs.ints;
     const int bar_id = 1 + gi;
+    uint32_t phase = 0;
     while (true) {
         int job = 0;
         if (tid == 0) job = atomicAdd(fetch, 1);
@@ -638,7 +896,8 @@ __global__ void solve_batch_kernel(Env<T> e, const tdic_poi_in* __restrict__ in,
         // icgn.cpp:472-473: std::round (halves away from zero), as CUDA's round()
         const int rx = static_cast<int>(round(pin.x)), ry = static_cast<int>(round(pin.y));
         Result R;
-        solve_poi<OPT, DEG, T, G>(e, rx, ry, p0, pin.confidence, sm, red, ints, gs.hinv, tid, bar_id, R);
+        if (!solve_poi<OPT, DEG, T, G>(e, &tm_ref, &tm_coef, s_off, rx, ry, p0, pin.confidence, gs, phase, tid, bar_id, R))
+            return;  // a TMA wait timed out: e.err is set
         if (tid == 0) write_out(out + job, R);
     }
 }
@@ -657,7 +916,8 @@ struct PropEnv {
     int* claim;
     unsigned long long* key;
     int* order;
-    int* counters;  // [0] wave-list tail, [1] queue head, [2] queue tail, [3] items in flight
+    int* counters;  // [0] wave-list tail, [1] queue head
+    unsigned long long* qword;  // queue tail (high 32) : items in flight + 2^31 (low 32)
     int* fetch;     // per wave
     unsigned int* barrier;
     int* flags;     // [0] error, [1] no seed, [2] accepted count
@@ -666,7 +926,6 @@ struct PropEnv {
     int sgx, sgy;                 // seed grid coordinates
     int* dstate;                  // 0 pending, 2 accepted, 3 rejected, 4 orphan
     int* dcnt;                    // parents resolved so far
-    int* dqs;                     // 1 once queued
     unsigned long long* dq;       // queue items: parent (high 32, -1 = orphan) : point (low 32)
     float* kcorr;                 // ZNSSD of accepted points (wave keys of the clean-up)
 };
@@ -697,6 +956,27 @@ __device__ bool grid_barrier(unsigned int* bar, int* err) {
     }
     __syncthreads();
     return *reinterpret_cast<volatile int*>(err) == 0;
+}
+
+template <typename P>
+__device__ __forceinline__ void store_params(P* params, int idx, const Result& R) {
+    for (int k = 0; k < 6; ++k) params[static_cast<size_t>(idx) * 6 + k] = static_cast<P>(R.p[k]);
+}
+
+__device__ void store_outputs(const PropEnv& pe, int idx, const Result& R) {
+    const tdic_grid_out& o = pe.out;
+    if (o.u) o.u[idx] = R.p[0];
+    if (o.v) o.v[idx] = R.p[1];
+    if (o.du_dx) o.du_dx[idx] = R.p[2];
+    if (o.du_dy) o.du_dy[idx] = R.p[3];
+    if (o.dv_dx) o.dv_dx[idx] = R.p[4];
+    if (o.dv_dy) o.dv_dy[idx] = R.p[5];
+    if (o.correlation) o.correlation[idx] = R.corr;
+    if (o.zncc) o.zncc[idx] = fmax(-1.0, fmin(1.0, 1.0 - 0.5 * R.corr));
+    if (o.valid) o.valid[idx] = 1;
+    if (o.status) o.status[idx] = TDIC_SUCCESS;
+    if (o.iterations) o.iterations[idx] = R.iters;
+    if (o.converged) o.converged[idx] = R.conv ? 1 : 0;
 }
 
 template <typename P>
@@ -763,22 +1043,33 @@ __device__ __forceinline__ void df_parents(const PropEnv& pe, int n, int& p1, in
     }
 }
 
-__device__ __forceinline__ void df_push(const PropEnv& pe, int c, int parent) {
-    atomicAdd(pe.counters + 3, 1);  // in flight before it is visible: termination stays exact
-    const int pos = atomicAdd(pe.counters + 2, 1);
-    const unsigned long long item = (static_cast<unsigned long long>(static_cast<unsigned int>(parent)) << 32) |
-                                    static_cast<unsigned int>(c);
-    atomicExch(pe.dq + pos, item);
+// Release / acquire fences at GPU scope (cheaper than the sequentially consistent
+// __threadfence); they order the message-passing patterns below.
+__device__ __forceinline__ void fence_acq_rel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+constexpr unsigned int kInFlightBias = 0x80000000u;  // in-flight count = low word - bias
 
-// n has been resolved (state published and fenced).  Its children are the 4-neighbours one
-// step farther from the seed.  A child is queued from its primary parent as soon as that one
-// is accepted; otherwise the last of its parents to resolve decides: secondary parent if
-// accepted, else orphan.
-__device__ void df_notify(const PropEnv& pe, int n, bool accepted) {
+// n has been resolved: its state (and, if accepted, its parameters) are written.  Its children
+// are the 4-neighbours one step farther from the seed.  A child is queued from its primary
+// parent as soon as that one is accepted; otherwise the last of its parents to resolve
+// decides: secondary parent if accepted, else orphan.  Exactly one thread decides each child
+// (the accepted primary, or the unique last parent when the primary failed), so no further
+// claim is needed.  `self_in_flight` is 1 when n itself was a queued item: the in-flight count
+// then trades n for its queued children in one atomic, before the children become visible.
+__device__ void df_resolve(const PropEnv& pe, int n, bool accepted, int self_in_flight) {
     const int gx = n % pe.gw, gy = n / pe.gw;
     const int dn = abs(gx - pe.sgx) + abs(gy - pe.sgy);
     const int cxs[4] = {gx, gx + 1, gx, gx - 1}, cys[4] = {gy - 1, gy, gy + 1, gy};
+    unsigned long long push[4];
+    int k = 0;
+    fence_acq_rel();  // publish n's state and parameters before any child counter update
     for (int d = 0; d < 4; ++d) {
         const int cx = cxs[d], cy = cys[d];
         if (cx < 0 || cy < 0 || cx >= pe.gw || cy >= pe.gh) continue;
@@ -786,29 +1077,46 @@ __device__ void df_notify(const PropEnv& pe, int n, bool accepted) {
         const int c = cy * pe.gw + cx;
         int p1, p2;
         df_parents(pe, c, p1, p2);
-        if (accepted && p1 == n) {
-            if (atomicCAS(pe.dqs + c, 0, 1) == 0) df_push(pe, c, n);
+        int parent = -2;  // -2: not decided here
+        if (p1 == n && accepted) {
+            parent = n;
+        } else if (p2 < 0) {
+            parent = -1;  // single parent, failed: orphan
+        } else if (atomicAdd(pe.dcnt + c, 1) == 1) {  // the second of two parents to resolve
+            fence_acq_rel();
+            const int s1 = ld_cg(pe.dstate + p1);
+            if (s1 != kDfAccepted) parent = (ld_cg(pe.dstate + p2) == kDfAccepted) ? p2 : -1;
         }
-        const int total = p2 >= 0 ? 2 : 1;
-        if (atomicAdd(pe.dcnt + c, 1) + 1 == total) {
-            __threadfence();
-            if (ld_cg(pe.dstate + p1) == kDfAccepted) continue;  // queued by its primary parent
-            const int parent = (p2 >= 0 && ld_cg(pe.dstate + p2) == kDfAccepted) ? p2 : -1;
-            if (atomicCAS(pe.dqs + c, 0, 1) == 0) df_push(pe, c, parent);
-        }
+        if (p1 == n && accepted && p2 >= 0) atomicAdd(pe.dcnt + c, 1);  // keep the count for the other parent
+        if (parent != -2)
+            push[k++] = (static_cast<unsigned long long>(static_cast<unsigned int>(parent)) << 32) |
+                        static_cast<unsigned int>(c);
     }
+    // One 64-bit atomic updates both the queue tail (high word, +k) and the in-flight count
+    // (low word, + k - self).  The low word carries an offset of 2^31 so it never borrows.
+    if (k == 0 && self_in_flight == 0) return;
+    const unsigned long long add = (static_cast<unsigned long long>(k) << 32) +
+                                   static_cast<unsigned long long>(static_cast<long long>(k - self_in_flight));
+    const unsigned long long old = atomicAdd(pe.qword, add);
+    const int pos = static_cast<int>(old >> 32);
+    for (int i = 0; i < k; ++i) st_release_u64(pe.dq + pos + i, push[i]);
 }
 
 template <int OPT, int DEG, typename T, int G>
-__global__ void __launch_bounds__(256, 2) propagate_kernel(Env<T> e, PropEnv pe) {
+__global__ void __launch_bounds__(256, 2) propagate_kernel(Env<T> e, const __grid_constant__ CUtensorMap tm_ref,
+                                                           const __grid_constant__ CUtensorMap tm_coef, PropEnv pe) {
     using P = typename MixedOf<T>::type;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     const int gi = threadIdx.x / (32 * G), tid = threadIdx.x % (32 * G);
-    GroupSmem<T> gs(smem_raw, gi, e.nmax, G);
-    T* sm = gs.sm;
-    T* red = gs.red;
+    short2* s_off = kernel_preamble<T, G>(e, &tm_ref, &tm_coef, smem_raw, gi, tid);
+    if (s_off == nullptr) {  // every block takes this path together: nothing waits on a barrier yet
+        if (threadIdx.x == 0) atomicExch(pe.flags, 1);
+        return;
+    }
+    GroupSmem<T> gs(smem_raw + cta_prefix_bytes(e.nmax), gi, e.nmax, G, e.rbx, e.rby, e.cbx, e.cby);
     int* ints = gs.ints;
     const int bar_id = 1 + gi;
+    uint32_t phase = 0;
     P* params = reinterpret_cast<P*>(pe.key + static_cast<size_t>(pe.gw) * pe.gh);  // params follow the keys
     const double cutoff = static_cast<double>(pe.step);
 
@@ -818,8 +1126,12 @@ __global__ void __launch_bounds__(256, 2) propagate_kernel(Env<T> e, PropEnv pe)
         bool ok = true;
         if (pe.seed_solve) {
             const int sx = (pe.seed_idx % pe.gw) * pe.step, sy = (pe.seed_idx / pe.gw) * pe.step;
-            solve_poi<OPT, DEG, T, G>(e, sx, sy, pe.seed_p, pe.seed_corr, sm, red, ints, gs.hinv, tid, bar_id, R);
-            ok = R.valid && R.status == TDIC_SUCCESS && finite6(R.p) && isfinite(R.corr);
+            if (!solve_poi<OPT, DEG, T, G>(e, &tm_ref, &tm_coef, s_off, sx, sy, pe.seed_p, pe.seed_corr, gs, phase, tid,
+                                           bar_id, R)) {
+                if (tid == 0) { pe.flags[1] = 1; atomicExch(pe.flags, 1); }
+                ok = false;
+            }
+            ok = ok && R.valid && R.status == TDIC_SUCCESS && finite6(R.p) && isfinite(R.corr);
         } else {
             for (int k = 0; k < 6; ++k) R.p[k] = pe.seed_p[k];
             R.corr = pe.seed_corr;
@@ -838,9 +1150,7 @@ __global__ void __launch_bounds__(256, 2) propagate_kernel(Env<T> e, PropEnv pe)
                 if (pe.mode == 2) {
                     pe.kcorr[pe.seed_idx] = static_cast<float>(fmax(0.0, R.corr));
                     pe.dstate[pe.seed_idx] = kDfAccepted;
-                    pe.dqs[pe.seed_idx] = 1;
-                    __threadfence();
-                    df_notify(pe, pe.seed_idx, true);
+                    df_resolve(pe, pe.seed_idx, true, 0);
                 } else {
                     __threadfence();
                     expand(pe, e.w, e.h, e.radius, pe.seed_idx, fmax(0.0, R.corr), 1);
@@ -862,21 +1172,20 @@ __global__ void __launch_bounds__(256, 2) propagate_kernel(Env<T> e, PropEnv pe)
                 const bool in_range = t < pe.gw * pe.gh;
                 unsigned long long spins = 0;
                 while (true) {
-                    const unsigned long long it = in_range ? __ldcg(pe.dq + t) : ~0ull;
-                    if (it != ~0ull) {
+                    const unsigned long long it = in_range ? ld_acquire_u64(pe.dq + t) : ~0ull;
+                    if (it != ~0ull) {  // acquire: the parent's parameters were released before it
                         item_c = static_cast<int>(it & 0xffffffffull);
                         item_p = static_cast<int>(it >> 32);
                         break;
                     }
-                    if (ld_cg(pe.counters + 3) == 0) { state = 1; break; }  // nothing queued or running
+                    const unsigned int inflight = static_cast<unsigned int>(__ldcg(pe.qword) & 0xffffffffull);
+                    if (inflight == kInFlightBias) { state = 1; break; }  // nothing queued or running
                     if (++spins > kSpinLimit) { atomicExch(pe.flags, 1); state = 2; break; }
                     __nanosleep(spins < 64 ? 20 : 200);
                 }
             }
-            state = group_bcast<G>(state, ints + 1, tid, bar_id);
+            group_bcast3<G>(state, item_c, item_p, ints + 1, tid, bar_id);
             if (state != 0) break;
-            item_c = group_bcast<G>(item_c, ints + 2, tid, bar_id);
-            item_p = group_bcast<G>(item_p, ints + 3, tid, bar_id);
             const int n = item_c;
             const int nx = (n % pe.gw) * pe.step, ny = (n / pe.gw) * pe.step;
             bool accepted = false;
@@ -895,7 +1204,11 @@ __global__ void __launch_bounds__(256, 2) propagate_kernel(Env<T> e, PropEnv pe)
                     p0[0] = pp[0] + pp[2] * ddx + pp[3] * ddy;  // reliability_propagation.cpp:326-329
                     p0[1] = pp[1] + pp[4] * ddx + pp[5] * ddy;
                     p0[2] = pp[2]; p0[3] = pp[3]; p0[4] = pp[4]; p0[5] = pp[5];
-                    solve_poi<OPT, DEG, T, G>(e, nx, ny, p0, 0.0, sm, red, ints, gs.hinv, tid, bar_id, R);
+                    if (!solve_poi<OPT, DEG, T, G>(e, &tm_ref, &tm_coef, s_off, nx, ny, p0, 0.0, gs, phase, tid, bar_id,
+                                                   R)) {
+                        if (tid == 0) atomicExch(pe.flags, 1);
+                        return;  // TMA wait timed out
+                    }
                     accepted = R.valid && R.status == TDIC_SUCCESS && R.corr < pe.max_znssd &&
                                fabs(p0[0] - R.p[0]) < cutoff && fabs(p0[1] - R.p[1]) < cutoff && finite6(R.p) &&
                                isfinite(R.corr);  // :359-368
@@ -903,16 +1216,17 @@ __global__ void __launch_bounds__(256, 2) propagate_kernel(Env<T> e, PropEnv pe)
                 }
             }
             if (tid == 0) {
+                // children first: the parameters and state they need, then the output arrays
                 if (accepted) {
-                    store_grid<P>(pe, params, n, R);
+                    store_params<P>(params, n, R);
                     pe.kcorr[n] = static_cast<float>(R.corr);
-                    atomicAdd(pe.flags + 2, 1);
                 }
                 pe.dstate[n] = new_state;
-                __threadfence();
-                df_notify(pe, n, accepted);
-                __threadfence();
-                atomicSub(pe.counters + 3, 1);
+                df_resolve(pe, n, accepted, 1);
+                if (accepted) {
+                    store_outputs(pe, n, R);
+                    atomicAdd(pe.flags + 2, 1);
+                }
             }
         }
         if (!grid_barrier(pe.barrier, pe.flags)) return;
@@ -951,7 +1265,10 @@ __global__ void __launch_bounds__(256, 2) propagate_kernel(Env<T> e, PropEnv pe)
             p0[1] = pp[1] + pp[4] * ddx + pp[5] * ddy;
             p0[2] = pp[2]; p0[3] = pp[3]; p0[4] = pp[4]; p0[5] = pp[5];
             Result R;
-            solve_poi<OPT, DEG, T, G>(e, nx, ny, p0, 0.0, sm, red, ints, gs.hinv, tid, bar_id, R);
+            if (!solve_poi<OPT, DEG, T, G>(e, &tm_ref, &tm_coef, s_off, nx, ny, p0, 0.0, gs, phase, tid, bar_id, R)) {
+                if (tid == 0) atomicExch(pe.flags, 1);
+                return;  // TMA wait timed out
+            }
             const bool accepted = R.valid && R.status == TDIC_SUCCESS && R.corr < pe.max_znssd &&
                                   fabs(p0[0] - R.p[0]) < cutoff && fabs(p0[1] - R.p[1]) < cutoff && finite6(R.p) &&
                                   isfinite(R.corr);  // :359-368
@@ -1003,8 +1320,62 @@ Env<T> make_env(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, int radi
     e.max_iter = max_iter;
     e.thr = thr;
     e.inv_n = tab.n > 0 ? 1.0 / tab.n : 0.0;
+    e.rpitch = pair->rpitch;
+    e.cpitch = pair->cpitch;
+    // Reference window: the subset with a one-pixel halo, x rounded down to 4 floats (16 B).
+    e.rby = 2 * radius + 3;
+    e.rbx = (2 * radius + 3 + 3 + 3) / 4 * 4;
+    // Coefficient window: the subset warped by the initial guess (a few px of growth for the
+    // gradient terms), a drift margin on both sides and the spline stencil, x rounded down to
+    // 16 bytes.  Stencils that fall outside it read global memory.
+    const int nb = pair->degree + 1;
+    const int align = 16 / static_cast<int>(sizeof(T));
+    const int cside = 2 * radius + 1 + 4 + 2 * kDriftMargin + nb;
+    e.cby = cside;
+    e.cbx = (cside + align - 1 + align - 1) / align * align;
+    TDIC_REQUIRE(e.rbx <= 256 && e.rby <= 256 && e.cbx <= 256 && e.cby <= 256, TDIC_UNSUPPORTED,
+                 "subset radius too large for a TMA box");
+    e.err = ctx->dev_err;
     (void)cfg;
     return e;
+}
+
+struct TensorMaps {
+    CUtensorMap ref;
+    CUtensorMap coef;
+};
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        TDIC_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+        TDIC_REQUIRE(q == cudaDriverEntryPointSuccess && p, TDIC_CUDA_ERROR, "cuTensorMapEncodeTiled unavailable");
+        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+void encode_2d(CUtensorMap* m, CUtensorMapDataType dt, size_t es, const void* base, int w, int h, int pitch, int bx,
+               int by) {
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(w), static_cast<cuuint64_t>(h)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(pitch) * es};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(bx), static_cast<cuuint32_t>(by)};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = encode_fn()(m, dt, 2, const_cast<void*>(base), dims, strides, box, estr,
+                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    TDIC_REQUIRE(r == CUDA_SUCCESS, TDIC_CUDA_ERROR, "cuTensorMapEncodeTiled failed (" + std::to_string(int(r)) + ")");
+}
+
+template <typename T>
+TensorMaps make_tensor_maps(const tdic_pair* pair, const Env<T>& e) {
+    TensorMaps t;
+    encode_2d(&t.ref, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pair->ref.ptr, pair->w, pair->h, pair->rpitch, e.rbx, e.rby);
+    encode_2d(&t.coef, sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, sizeof(T),
+              pair->coef.ptr, pair->cw, pair->ch, pair->cpitch, e.cbx, e.cby);
+    return t;
 }
 
 constexpr int kGroupsPerBlockBatch = 4;  // 4 warps of 1-warp groups
@@ -1013,8 +1384,14 @@ template <int OPT, int DEG, typename T>
 void solve_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const SolveLaunch& L, cudaStream_t s) {
     constexpr int G = 1;
     Env<T> e = make_env<T>(ctx, pair, cfg, cfg.subset_radius, cfg.max_iterations, cfg.convergence_threshold);
-    const int gpb = kGroupsPerBlockBatch;
-    const size_t smem = gpb * group_smem_bytes<T>(e.nmax, G);
+    const TensorMaps tm = make_tensor_maps<T>(pair, e);
+    const size_t per_group = group_smem_bytes<T>(e.nmax, G, e.rbx, e.rby, e.cbx, e.cby);
+    const size_t prefix = cta_prefix_bytes(e.nmax);
+    int gpb = kGroupsPerBlockBatch;
+    while (gpb > 1 && prefix + gpb * per_group > static_cast<size_t>(ctx->max_smem_optin)) --gpb;
+    TDIC_REQUIRE(prefix + per_group <= static_cast<size_t>(ctx->max_smem_optin), TDIC_UNSUPPORTED,
+                 "subset radius too large for shared memory");
+    const size_t smem = prefix + gpb * per_group;
     auto kern = solve_batch_kernel<OPT, DEG, T, G>;
     TDIC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     int per_sm = 0;
@@ -1024,7 +1401,7 @@ void solve_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const S
     const int need = (L.n + gpb - 1) / gpb;
     if (blocks > need) blocks = need < 1 ? 1 : need;
     TDIC_CUDA_TRY(cudaMemsetAsync(L.fetch, 0, sizeof(int), s));
-    kern<<<blocks, 32 * G * gpb, smem, s>>>(e, L.in, L.out, L.n, L.fetch);
+    kern<<<blocks, 32 * G * gpb, smem, s>>>(e, tm.ref, tm.coef, L.in, L.out, L.n, L.fetch);
     TDIC_CUDA_TRY(cudaGetLastError());
 }
 
@@ -1037,17 +1414,25 @@ void solve_deg(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const Sol
     }
 }
 
-// Propagation groups: 4 warps per POI (the wave front is narrow, so per-POI latency, not
-// throughput, bounds a wave), 2 groups per CTA.
+// Propagation groups: 4 warps per POI, two groups per CTA, two CTAs per SM.  Per-POI latency
+// on the dataflow critical path bounds the propagation; measured on 2048^2, r = 15, 8 warps
+// per POI were 14% slower (the two-stage group reductions and barriers grow with the group)
+// and one or two groups per CTA timed the same.
 constexpr int kPropG = 4;
 constexpr int kPropGroupsPerBlock = 2;
 
 template <int OPT, int DEG, typename T>
 void propagate_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const PropagateLaunch& L, cudaStream_t s) {
     constexpr int G = kPropG;
-    constexpr int gpb = kPropGroupsPerBlock;
     Env<T> e = make_env<T>(ctx, pair, cfg, cfg.subset_radius, cfg.max_iterations, cfg.convergence_threshold);
-    const size_t smem = gpb * group_smem_bytes<T>(e.nmax, G);
+    TensorMaps tm = make_tensor_maps<T>(pair, e);
+    const size_t per_group = group_smem_bytes<T>(e.nmax, G, e.rbx, e.rby, e.cbx, e.cby);
+    const size_t prefix = cta_prefix_bytes(e.nmax);
+    int gpb = kPropGroupsPerBlock;
+    while (gpb > 1 && prefix + gpb * per_group > static_cast<size_t>(ctx->max_smem_optin)) --gpb;
+    TDIC_REQUIRE(prefix + per_group <= static_cast<size_t>(ctx->max_smem_optin), TDIC_UNSUPPORTED,
+                 "subset radius too large for shared memory");
+    const size_t smem = prefix + gpb * per_group;
     auto kern = propagate_kernel<OPT, DEG, T, G>;
     TDIC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     int per_sm = 0;
@@ -1065,11 +1450,12 @@ void propagate_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, con
     pe.claim = L.claim; pe.key = L.key; pe.order = L.order; pe.counters = L.counters; pe.fetch = L.fetch;
     pe.barrier = L.barrier; pe.flags = L.flags;
     pe.mode = L.mode; pe.sgx = L.sgx; pe.sgy = L.sgy;
-    pe.dstate = L.dstate; pe.dcnt = L.dcnt; pe.dqs = L.dqs; pe.dq = L.dq; pe.kcorr = L.kcorr;
+    pe.dstate = L.dstate; pe.dcnt = L.dcnt; pe.dq = L.dq; pe.kcorr = L.kcorr;
+    pe.qword = reinterpret_cast<unsigned long long*>(L.counters + 4);
     const int n = L.gw * L.gh;
     init_grid_kernel<<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, s>>>(L.out, L.gw, L.gh, L.step);
     TDIC_CUDA_TRY(cudaGetLastError());
-    void* args[] = {&e, &pe};
+    void* args[] = {&e, &tm.ref, &tm.coef, &pe};
     TDIC_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kern), dim3(blocks), dim3(32 * G * gpb), args,
                                               smem, s));
 }

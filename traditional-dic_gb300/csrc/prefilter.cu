@@ -78,8 +78,8 @@ __device__ inline void pole_pass(T* x, int n, int st, T z) {
 
 template <typename In, typename T, int DEG>
 __global__ void __launch_bounds__(128) prefilter_tile_kernel(const In* __restrict__ img, int w, int h, int pitch,
-                                                             int border, int cw, int ch, T z0, T z1, T gain,
-                                                             T* __restrict__ out) {
+                                                             int border, int cw, int ch, int opitch, T z0, T z1,
+                                                             T gain, T* __restrict__ out) {
     constexpr int M = Margin<T, DEG>::M;
     constexpr int TW = TileW<T>::value;
     constexpr int L = TW + 2 * M;  // tile side with margins
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(128) prefilter_tile_kernel(const In* __restric
     for (int i = threadIdx.x; i < TW * TW; i += blockDim.x) {
         const int r = i / TW, c = i - r * TW;
         const int oy = ty0 + r, ox = tx0 + c;
-        if (oy < ch && ox < cw) out[static_cast<size_t>(oy) * cw + ox] = s[(M + r) * P + M + c];
+        if (oy < ch && ox < cw) out[static_cast<size_t>(oy) * opitch + ox] = s[(M + r) * P + M + c];
     }
 }
 
@@ -118,39 +118,40 @@ __global__ void __launch_bounds__(128) prefilter_tile_kernel(const In* __restric
 // (clamp padding, no deconvolution: form_coefficients with use_exact_prefilter = false).
 template <typename In, typename T>
 __global__ void pad_copy_kernel(const In* __restrict__ img, int w, int h, int pitch, int border, int cw, int ch,
-                                int symmetric, T* __restrict__ out) {
+                                int opitch, int symmetric, T* __restrict__ out) {
     const size_t n = static_cast<size_t>(cw) * ch;
     for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<size_t>(gridDim.x) * blockDim.x) {
         const int py = static_cast<int>(i / cw), px = static_cast<int>(i - static_cast<size_t>(py) * cw);
         const int sy = symmetric ? sym_index(py - border, h) : clampi(py - border, 0, h - 1);
         const int sx = symmetric ? sym_index(px - border, w) : clampi(px - border, 0, w - 1);
-        out[i] = static_cast<T>(load_px(img + static_cast<size_t>(sy) * pitch + sx));
+        out[static_cast<size_t>(py) * opitch + px] = static_cast<T>(load_px(img + static_cast<size_t>(sy) * pitch + sx));
     }
 }
 
 template <typename In>
-__global__ void convert_kernel(const In* __restrict__ src, int w, int h, int pitch, float* __restrict__ dst) {
+__global__ void convert_kernel(const In* __restrict__ src, int w, int h, int pitch, float* __restrict__ dst,
+                               int dpitch) {
     const size_t n = static_cast<size_t>(w) * h;
     for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<size_t>(gridDim.x) * blockDim.x) {
         const int y = static_cast<int>(i / w), x = static_cast<int>(i - static_cast<size_t>(y) * w);
-        dst[i] = static_cast<float>(src[static_cast<size_t>(y) * pitch + x]);
+        dst[static_cast<size_t>(y) * dpitch + x] = static_cast<float>(src[static_cast<size_t>(y) * pitch + x]);
     }
 }
 
 // K2 (reliability_propagation.cpp:84-112): central differences on raw pixels, one-sided (/1)
 // at the border.
-__global__ void gradient_kernel(const float* __restrict__ img, int w, int h, double* __restrict__ gx,
+__global__ void gradient_kernel(const float* __restrict__ img, int w, int h, int pitch, double* __restrict__ gx,
                                 double* __restrict__ gy) {
     const size_t n = static_cast<size_t>(w) * h;
     for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<size_t>(gridDim.x) * blockDim.x) {
         const int y = static_cast<int>(i / w), x = static_cast<int>(i - static_cast<size_t>(y) * w);
         const int xm = max(0, x - 1), xp = min(w - 1, x + 1), ym = max(0, y - 1), yp = min(h - 1, y + 1);
-        gx[i] = (static_cast<double>(img[static_cast<size_t>(y) * w + xp]) - static_cast<double>(img[static_cast<size_t>(y) * w + xm])) /
+        gx[i] = (static_cast<double>(img[static_cast<size_t>(y) * pitch + xp]) - static_cast<double>(img[static_cast<size_t>(y) * pitch + xm])) /
                 static_cast<double>(max(1, xp - xm));
-        gy[i] = (static_cast<double>(img[static_cast<size_t>(yp) * w + x]) - static_cast<double>(img[static_cast<size_t>(ym) * w + x])) /
+        gy[i] = (static_cast<double>(img[static_cast<size_t>(yp) * pitch + x]) - static_cast<double>(img[static_cast<size_t>(ym) * pitch + x])) /
                 static_cast<double>(max(1, yp - ym));
     }
 }
@@ -161,11 +162,11 @@ int grid_for(size_t n, int threads) {
 }
 
 template <typename In, typename T>
-void prefilter_typed(const In* img, int w, int h, int pitch, int border, int cw, int ch, int degree, int exact,
-                     T* out, cudaStream_t s) {
+void prefilter_typed(const In* img, int w, int h, int pitch, int border, int cw, int ch, int opitch, int degree,
+                     int exact, T* out, cudaStream_t s) {
     if (!exact || degree == 1) {
         pad_copy_kernel<In, T><<<grid_for(static_cast<size_t>(cw) * ch, 256), 256, 0, s>>>(img, w, h, pitch, border, cw,
-                                                                                         ch, exact, out);
+                                                                                         ch, opitch, exact, out);
         return;
     }
     const Poles p = poles_for(degree);
@@ -176,14 +177,14 @@ void prefilter_typed(const In* img, int w, int h, int pitch, int border, int cw,
         const size_t smem = static_cast<size_t>(L) * (L + 1) * sizeof(T);
         TDIC_CUDA_TRY(cudaFuncSetAttribute(prefilter_tile_kernel<In, T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(smem)));
-        prefilter_tile_kernel<In, T, 3><<<grid, 128, smem, s>>>(img, w, h, pitch, border, cw, ch, T(p.z[0]), T(0),
+        prefilter_tile_kernel<In, T, 3><<<grid, 128, smem, s>>>(img, w, h, pitch, border, cw, ch, opitch, T(p.z[0]), T(0),
                                                                 T(p.gain * p.gain), out);  // one gain per 1-D pass
     } else {
         constexpr int M = Margin<T, 5>::M, L = TW + 2 * M;
         const size_t smem = static_cast<size_t>(L) * (L + 1) * sizeof(T);
         TDIC_CUDA_TRY(cudaFuncSetAttribute(prefilter_tile_kernel<In, T, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(smem)));
-        prefilter_tile_kernel<In, T, 5><<<grid, 128, smem, s>>>(img, w, h, pitch, border, cw, ch, T(p.z[0]), T(p.z[1]),
+        prefilter_tile_kernel<In, T, 5><<<grid, 128, smem, s>>>(img, w, h, pitch, border, cw, ch, opitch, T(p.z[0]), T(p.z[1]),
                                                                 T(p.gain * p.gain), out);  // one gain per 1-D pass
     }
     TDIC_CUDA_TRY(cudaGetLastError());
@@ -191,13 +192,14 @@ void prefilter_typed(const In* img, int w, int h, int pitch, int border, int cw,
 
 }  // namespace
 
-void launch_convert(const void* src, int w, int h, int pitch, tdic_dtype dtype, float* dst, cudaStream_t s) {
+void launch_convert(const void* src, int w, int h, int pitch, tdic_dtype dtype, float* dst, int dst_pitch,
+                    cudaStream_t s) {
     const int g = grid_for(static_cast<size_t>(w) * h, 256);
     switch (dtype) {
-        case TDIC_U8: convert_kernel<uint8_t><<<g, 256, 0, s>>>(static_cast<const uint8_t*>(src), w, h, pitch, dst); break;
-        case TDIC_U16: convert_kernel<uint16_t><<<g, 256, 0, s>>>(static_cast<const uint16_t*>(src), w, h, pitch, dst); break;
-        case TDIC_F32: convert_kernel<float><<<g, 256, 0, s>>>(static_cast<const float*>(src), w, h, pitch, dst); break;
-        case TDIC_F64: convert_kernel<double><<<g, 256, 0, s>>>(static_cast<const double*>(src), w, h, pitch, dst); break;
+        case TDIC_U8: convert_kernel<uint8_t><<<g, 256, 0, s>>>(static_cast<const uint8_t*>(src), w, h, pitch, dst, dst_pitch); break;
+        case TDIC_U16: convert_kernel<uint16_t><<<g, 256, 0, s>>>(static_cast<const uint16_t*>(src), w, h, pitch, dst, dst_pitch); break;
+        case TDIC_F32: convert_kernel<float><<<g, 256, 0, s>>>(static_cast<const float*>(src), w, h, pitch, dst, dst_pitch); break;
+        case TDIC_F64: convert_kernel<double><<<g, 256, 0, s>>>(static_cast<const double*>(src), w, h, pitch, dst, dst_pitch); break;
     }
     TDIC_CUDA_TRY(cudaGetLastError());
 }
@@ -206,15 +208,15 @@ void launch_convert(const void* src, int w, int h, int pitch, tdic_dtype dtype, 
 // numpy input is rounded to float by the reference binding, bind_subset.cpp:50-64).
 void launch_prefilter(tdic_pair* pair, const float* image, cudaStream_t s) {
     if (pair->precision == TDIC_FP64)
-        prefilter_typed<float, double>(image, pair->w, pair->h, pair->w, pair->border, pair->cw, pair->ch, pair->degree,
-                                       pair->exact, pair->coef.as<double>(), s);
+        prefilter_typed<float, double>(image, pair->w, pair->h, pair->rpitch, pair->border, pair->cw, pair->ch,
+                                       pair->cpitch, pair->degree, pair->exact, pair->coef.as<double>(), s);
     else
-        prefilter_typed<float, float>(image, pair->w, pair->h, pair->w, pair->border, pair->cw, pair->ch, pair->degree,
-                                      pair->exact, pair->coef.as<float>(), s);
+        prefilter_typed<float, float>(image, pair->w, pair->h, pair->rpitch, pair->border, pair->cw, pair->ch,
+                                      pair->cpitch, pair->degree, pair->exact, pair->coef.as<float>(), s);
 }
 
-void launch_reference_gradient(const float* img, int w, int h, double* gx, double* gy, cudaStream_t s) {
-    gradient_kernel<<<grid_for(static_cast<size_t>(w) * h, 256), 256, 0, s>>>(img, w, h, gx, gy);
+void launch_reference_gradient(const float* img, int w, int h, int pitch, double* gx, double* gy, cudaStream_t s) {
+    gradient_kernel<<<grid_for(static_cast<size_t>(w) * h, 256), 256, 0, s>>>(img, w, h, pitch, gx, gy);
     TDIC_CUDA_TRY(cudaGetLastError());
 }
 

@@ -39,20 +39,20 @@ __device__ __forceinline__ bool better(double z, int idx, double bz, int bidx) {
 
 // ZNCC of the circular subset at displacement (u, v); -inf when the subset leaves the image or
 // the deformed subset is flat.  Samples: offsets off[0..n), reference values rv, mean rm, norm rn.
-__device__ double zncc_at(const float* __restrict__ def, int w, int h, const short2* off, const double* rv, int n,
-                          double rm, double rn, int cx, int cy, int u, int v) {
+__device__ double zncc_at(const float* __restrict__ def, int w, int h, int pitch, const short2* off, const double* rv,
+                          int n, double rm, double rn, int cx, int cy, int u, int v) {
     if (n == 0 || rn <= kEps) return -INFINITY;
     double dm = 0.0;
     for (int i = 0; i < n; ++i) {
         const int x = cx + u + off[i].x, y = cy + v + off[i].y;
         if (x < 0 || y < 0 || x >= w || y >= h) return -INFINITY;
-        dm += static_cast<double>(__ldg(def + static_cast<size_t>(y) * w + x));
+        dm += static_cast<double>(__ldg(def + static_cast<size_t>(y) * pitch + x));
     }
     dm /= static_cast<double>(n);
     double num = 0.0, dn = 0.0;
     for (int i = 0; i < n; ++i) {
         const double rd = rv[i] - rm;
-        const double dd = static_cast<double>(__ldg(def + static_cast<size_t>(cy + v + off[i].y) * w + cx + u + off[i].x)) - dm;
+        const double dd = static_cast<double>(__ldg(def + static_cast<size_t>(cy + v + off[i].y) * pitch + cx + u + off[i].x)) - dm;
         num += rd * dd;
         dn += dd * dd;
     }
@@ -61,10 +61,10 @@ __device__ double zncc_at(const float* __restrict__ def, int w, int h, const sho
 }
 
 // Reference samples of one candidate into shared memory: values, mean, norm (sum of squares).
-__device__ void load_ref(const float* __restrict__ ref, int w, const short2* off, int n, int cx, int cy, double* rv,
+__device__ void load_ref(const float* __restrict__ ref, int pitch, const short2* off, int n, int cx, int cy, double* rv,
                          double* stats) {
     for (int i = threadIdx.x; i < n; i += blockDim.x)
-        rv[i] = static_cast<double>(__ldg(ref + static_cast<size_t>(cy + off[i].y) * w + cx + off[i].x));
+        rv[i] = static_cast<double>(__ldg(ref + static_cast<size_t>(cy + off[i].y) * pitch + cx + off[i].x));
     __syncthreads();
     if (threadIdx.x == 0) {
         double m = 0.0;
@@ -101,7 +101,7 @@ __device__ void block_argmax(double& z, int& idx, double* sz, int* si) {
 }
 
 // Coarse search: grid.y = candidate, grid.x tiles the coarse positions.
-__global__ void coarse_kernel(const float* __restrict__ ref, const float* __restrict__ def, int w, int h,
+__global__ void coarse_kernel(const float* __restrict__ ref, const float* __restrict__ def, int w, int h, int pitch,
                               const CandGeom* __restrict__ geo, const short2* __restrict__ coff, int cn, int cstep,
                               Best* __restrict__ partial, int tiles) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -117,7 +117,7 @@ __global__ void coarse_kernel(const float* __restrict__ ref, const float* __rest
     }
     for (int i = threadIdx.x; i < cn; i += blockDim.x) off[i] = coff[i];
     __syncthreads();
-    load_ref(ref, w, off, cn, g.cx, g.cy, rv, stats);
+    load_ref(ref, pitch, off, cn, g.cx, g.cy, rv, stats);
     const int nu = g.max_u >= g.min_u ? (g.max_u - g.min_u) / cstep + 1 : 0;
     const int nv = g.max_v >= g.min_v ? (g.max_v - g.min_v) / cstep + 1 : 0;
     const int total = nu * nv;
@@ -126,7 +126,7 @@ __global__ void coarse_kernel(const float* __restrict__ ref, const float* __rest
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += tiles * blockDim.x) {
         const int vi = t / nu, ui = t - vi * nu;
         const int u = g.min_u + ui * cstep, v = g.min_v + vi * cstep;
-        const double z = zncc_at(def, w, h, off, rv, cn, stats[0], stats[1], g.cx, g.cy, u, v);
+        const double z = zncc_at(def, w, h, pitch, off, rv, cn, stats[0], stats[1], g.cx, g.cy, u, v);
         if (better(z, t, bz, bi)) { bz = z; bi = t; }
     }
     block_argmax(bz, bi, sz, si);
@@ -135,7 +135,7 @@ __global__ void coarse_kernel(const float* __restrict__ ref, const float* __rest
 
 // Full-sample refinement around the coarse optimum and the local +-search window, then the
 // local-preference rule.  One block per candidate.
-__global__ void fine_kernel(const float* __restrict__ ref, const float* __restrict__ def, int w, int h, int r,
+__global__ void fine_kernel(const float* __restrict__ ref, const float* __restrict__ def, int w, int h, int pitch, int r,
                             const CandGeom* __restrict__ geo, const short2* __restrict__ foff, int fn,
                             const Best* __restrict__ partial, int tiles, int cstep, int rr, int search, int coarse_ok_all,
                             const int* __restrict__ coarse_ok, SearchResult* __restrict__ out) {
@@ -154,7 +154,7 @@ __global__ void fine_kernel(const float* __restrict__ ref, const float* __restri
     }
     for (int i = threadIdx.x; i < fn; i += blockDim.x) off[i] = foff[i];
     __syncthreads();
-    load_ref(ref, w, off, fn, g.cx, g.cy, rv, stats);
+    load_ref(ref, pitch, off, fn, g.cx, g.cy, rv, stats);
     const bool full_ok = !(fn == 0 || stats[1] <= kEps);
     // coarse winner
     if (threadIdx.x == 0) {
@@ -190,7 +190,7 @@ __global__ void fine_kernel(const float* __restrict__ ref, const float* __restri
             const int u = u0 + t % nu, v = v0 + t / nu;
             const int x = g.cx + u, y = g.cy + v;
             if (!(x - r >= 0 && y - r >= 0 && x + r < w && y + r < h)) continue;
-            const double z = zncc_at(def, w, h, off, rv, fn, stats[0], stats[1], g.cx, g.cy, u, v);
+            const double z = zncc_at(def, w, h, pitch, off, rv, fn, stats[0], stats[1], g.cx, g.cy, u, v);
             if (better(z, t, bz, bi)) { bz = z; bi = t; }
         }
         block_argmax(bz, bi, sz, si);
@@ -215,7 +215,7 @@ __global__ void fine_kernel(const float* __restrict__ ref, const float* __restri
             const int u = -search + t % n1, v = -search + t / n1;
             const int x = g.cx + u, y = g.cy + v;
             if (!(x - r >= 0 && y - r >= 0 && x + r < w && y + r < h)) continue;
-            const double z = zncc_at(def, w, h, off, rv, fn, stats[0], stats[1], g.cx, g.cy, u, v);
+            const double z = zncc_at(def, w, h, pitch, off, rv, fn, stats[0], stats[1], g.cx, g.cy, u, v);
             if (better(z, t, bz, bi)) { bz = z; bi = t; }
         }
         block_argmax(bz, bi, sz, si);
@@ -284,11 +284,11 @@ void integer_search_batch(tdic_ctx* ctx, tdic_pair* lazy, const tdic_config& cfg
     const size_t fsm = sizeof(double) * (foff.size() + 2 + 32) + sizeof(int) * 32 + sizeof(short2) * foff.size() + 16;
     TDIC_CUDA_TRY(cudaFuncSetAttribute(coarse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(csm)));
     TDIC_CUDA_TRY(cudaFuncSetAttribute(fine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(fsm)));
-    coarse_kernel<<<dim3(tiles, n), 256, csm, s>>>(lazy->ref.as<float>(), lazy->def_f.as<float>(), w, h,
+    coarse_kernel<<<dim3(tiles, n), 256, csm, s>>>(lazy->ref.as<float>(), lazy->def_f.as<float>(), w, h, lazy->rpitch,
                                                    d_geo.as<CandGeom>(), d_coff.as<short2>(), static_cast<int>(coff.size()),
                                                    cstep, d_part.as<Best>(), tiles);
     TDIC_CUDA_TRY(cudaGetLastError());
-    fine_kernel<<<n, 256, fsm, s>>>(lazy->ref.as<float>(), lazy->def_f.as<float>(), w, h, r, d_geo.as<CandGeom>(),
+    fine_kernel<<<n, 256, fsm, s>>>(lazy->ref.as<float>(), lazy->def_f.as<float>(), w, h, lazy->rpitch, r, d_geo.as<CandGeom>(),
                                     d_foff.as<short2>(), static_cast<int>(foff.size()), d_part.as<Best>(), tiles, cstep, rr,
                                     search, 1, d_cok.as<int>(), d_out.as<SearchResult>());
     TDIC_CUDA_TRY(cudaGetLastError());

@@ -91,6 +91,8 @@ struct SampleTable {
 struct tdic_ctx {
     int device = 0;
     int num_sms = 0;
+    int max_smem_optin = 0;  // dynamic shared memory a CTA may opt in to
+    int* dev_err = nullptr;  // device error flag of bounded in-kernel waits (0 = none)
     cudaStream_t stream = nullptr;
     std::recursive_mutex mu;
     std::string last_error;
@@ -106,10 +108,11 @@ struct tdic_pair {
     tdic_ctx* ctx = nullptr;
     int w = 0, h = 0, border = 3, degree = 3, precision = 0, exact = 1;
     int cw = 0, ch = 0;        // coefficient image size (w + 2B) x (h + 2B)
-    tdic::Buffer ref;          // float32 H x W reference (dic::Image stores float)
-    tdic::Buffer coef;         // T (cw x ch) coefficients of the deformed image
-    tdic::Buffer rowtmp;       // T (h x cw) row-pass intermediate
-    tdic::Buffer def_f;        // float32 H x W deformed (kept for seed search)
+    int rpitch = 0;            // floats per row of ref / def_f (128-byte multiple: TMA row stride)
+    int cpitch = 0;            // elements per row of coef (128-byte multiple)
+    tdic::Buffer ref;          // float32 H x W reference, row pitch rpitch (dic::Image stores float)
+    tdic::Buffer coef;         // T coefficients of the deformed image, ch rows of cpitch
+    tdic::Buffer def_f;        // float32 H x W deformed, row pitch rpitch (prefilter input, seed search)
     tdic::Buffer staging;      // raw input staging for host uploads
 };
 
@@ -121,9 +124,10 @@ void build_qk(int degree, double* qk);
 const SampleTable& sample_table(tdic_ctx* ctx, int radius);
 
 // Kernel launchers (prefilter.cu) --------------------------------------------------------
-void launch_convert(const void* src, int w, int h, int pitch, tdic_dtype dtype, float* dst, cudaStream_t s);
+void launch_convert(const void* src, int w, int h, int pitch, tdic_dtype dtype, float* dst, int dst_pitch,
+                    cudaStream_t s);
 void launch_prefilter(tdic_pair* pair, const float* image, cudaStream_t s);
-void launch_reference_gradient(const float* img, int w, int h, double* gx, double* gy, cudaStream_t s);
+void launch_reference_gradient(const float* img, int w, int h, int pitch, double* gx, double* gy, cudaStream_t s);
 
 // Hot path (hotpath.cu) -------------------------------------------------------------------
 struct SolveLaunch {
@@ -133,6 +137,8 @@ struct SolveLaunch {
     int* fetch;  // work counter (zeroed by the launcher)
 };
 void launch_solve(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const SolveLaunch& L, cudaStream_t s);
+// Throws TDIC_TIMEOUT when a bounded in-kernel wait gave up; clears the flag.  Synchronises s.
+void check_device_error(tdic_ctx* ctx, cudaStream_t s);
 
 struct PropagateLaunch {
     int gw, gh, step;
@@ -151,7 +157,7 @@ struct PropagateLaunch {
     // dataflow order (propagation_mode 2)
     int mode;
     int sgx, sgy;
-    int* dstate; int* dcnt; int* dqs; unsigned long long* dq; float* kcorr;
+    int* dstate; int* dcnt; unsigned long long* dq; float* kcorr;
 };
 void launch_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const PropagateLaunch& L,
                       cudaStream_t s);
