@@ -47,7 +47,10 @@ enum { TDIC_SUCCESS = 0, TDIC_NOT_CONVERGED = 1, TDIC_INVALID_INPUT = 2, TDIC_NU
 /* The knobs of dic::SubsetConfig reachable from the pybind config dict
  * (include/dic/subset/subset_config.hpp:33-50, include/dic/initialization/seed_config.hpp:32-68,
  * include/dic/interpolation/bspline.hpp:42-67), C++ defaults from tdic_config_default().
- * propagation_mode and precision are GPU-only knobs (the reference has neither). */
+ * propagation_mode and precision are GPU-only knobs (the reference has neither).  The visit
+ * order of the propagation: 2 = dataflow (a grid point is solved as soon as its parent one step
+ * toward the seed is accepted), 0 = frontier waves; 1 = the reference's serial heap order
+ * exists in the CPU oracle only (TDIC_UNSUPPORTED here). */
 typedef struct tdic_config {
     int32_t subset_radius;             /* subset.radius                               15 */
     int32_t max_iterations;            /* optimization.max_iterations                 30 */
@@ -76,7 +79,7 @@ typedef struct tdic_config {
     double min_displacement_norm;      /* seed_selection.min_displacement_norm          0 */
     double min_texture_std;            /* seed_selection.min_texture_std                0 */
     int32_t kmeans_sample_limit;       /* seed_selection.kmeans_sample_limit        20000 */
-    int32_t propagation_mode;          /* 0 = frontier waves (GPU only)                 0 */
+    int32_t propagation_mode;          /* 2 dataflow, 0 frontier waves (GPU orders)     2 */
 } tdic_config;
 
 /* One POI for a batched solve: centre (rounded to the nearest pixel as icgn.cpp:472-473),
@@ -175,9 +178,11 @@ tdic_status tdic_solve_pois(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* c
 /* Propagation over the POI grid from one seed: replaces the heap loop of
  * ReliabilityPropagation::propagate (reliability_propagation.cpp:130-394).  The grid
  * geometry, seed alignment (:201-264), neighbour admission (:303-323), guess extrapolation
- * (:326-329) and acceptance rule (:359-368) are the reference's; the visit order is the
- * frontier-wave rule (every admissible neighbour of wave w's accepted set is solved in wave
- * w+1 from the parent with the lowest ZNSSD, ties to the lowest parent index).
+ * (:326-329) and acceptance rule (:359-368) are the reference's; the visit order is
+ * cfg->propagation_mode: dataflow (each point solved from its parent one step toward the seed
+ * as soon as that parent is accepted, the other axis's parent if it failed; unreached points
+ * swept by waves) or frontier waves (every admissible neighbour of wave w's accepted set is
+ * solved in wave w+1 from the parent with the lowest ZNSSD, ties to the lowest parent index).
  * roi: host uint8 H x W mask (NULL = all valid).  out: host or device arrays per `memory`
  * of grid_w*grid_h entries.  *points_computed = accepted points including the seed (0 means
  * the seed could not be placed: SubsetDIC::compute then returns the empty result). */

@@ -542,7 +542,7 @@ void tdic_config_default(tdic_config* c) {
     c->sp_convergence_threshold = 1e-3;
     c->seed_count = 256; c->kmeans_iterations = 20; c->seed_max_znssd = 0.2;
     c->min_displacement_norm = 0.0; c->min_texture_std = 0.0; c->kmeans_sample_limit = 20000;
-    c->propagation_mode = 0;
+    c->propagation_mode = 2;
 }
 
 void tdic_grid_dims(int32_t w, int32_t h, int32_t spacing, int32_t* gw, int32_t* gh) {

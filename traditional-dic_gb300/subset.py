@@ -435,8 +435,8 @@ def make_seed(x, y, p, correlation) -> L.Seed:
 
 
 def propagate(ctx: Context, pair: Pair, config: L.Config, seed: L.Seed, roi=None) -> dict:
-    """Frontier-wave propagation (tdic_propagate) with host outputs; returns the grid dict plus
-    ``points_computed``."""
+    """Propagation over the POI grid (tdic_propagate) in the config's visit order, with host
+    outputs; returns the grid dict plus ``points_computed``."""
     gw, gh = L.grid_dims(pair.width, pair.height, config.propagation_spacing)
     arrs, g = _alloc_grid(gw * gh)
     rptr, rkeep = _roi_arg(roi, pair.width, pair.height)
