@@ -190,6 +190,24 @@ tdic_status tdic_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cf
                            const tdic_seed* seed, const uint8_t* roi, tdic_grid_out* out,
                            tdic_memory memory, int32_t* points_computed, void* stream);
 
+/* tdic_propagate without device allocation (no counterpart in the reference, whose CPU
+ * propagation has nothing to allocate on a device).  For callers that cannot allocate device
+ * memory at propagation time: a real-time loop that must not stall on cudaMalloc's device
+ * synchronisation, or a process whose device memory belongs to another allocator.  The same
+ * kernel runs with its scratch in one static device array of about 11.8 MiB per device,
+ * which caps the call at 131072 grid points and 32768 subset samples (radius <= 100);
+ * larger calls fail with TDIC_INVALID_ARG.  out_device: device arrays of grid_w*grid_h
+ * entries (NULL entries skipped); roi: host mask as for tdic_propagate.  The pair and the
+ * context are made beforehand with the calls above, which do allocate.  The first call on a
+ * device looks up the array's device address (set-up, once per device); make that first
+ * call before any stream capture.  Every call on a device shares the array and finds the
+ * previous call's contents, which it re-initialises; calls that overlapped would race, so
+ * this entry point holds a process-wide lock and waits for its kernel before returning. */
+tdic_status tdic_propagate_noalloc(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cfg,
+                                   const tdic_seed* seed, const uint8_t* roi,
+                                   const tdic_grid_out* out_device, int32_t* points_computed,
+                                   void* stream);
+
 /* Seed selection: SeedSelector::select_best_seed (seed_selector.cpp:146-205) with k-means
  * candidates (:207-317), integer search (integer_search.cpp:333-432, kernel K5) and subpixel
  * ICGN refinement on the non-prefiltered spline (subset_initializer.cpp:152-204).  `lazy` is

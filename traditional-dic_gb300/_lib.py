@@ -79,6 +79,8 @@ SIGNATURES = {
                                   C.c_int, C.c_void_p]),
     "tdic_propagate": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Config), C.POINTER(Seed), C.c_void_p,
                                  C.POINTER(GridOut), C.c_int, C.POINTER(C.c_int32), C.c_void_p]),
+    "tdic_propagate_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Config), C.POINTER(Seed), C.c_void_p,
+                                         C.POINTER(GridOut), C.POINTER(C.c_int32), C.c_void_p]),
     "tdic_select_seed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Config),
                                    C.POINTER(Seed), C.c_void_p]),
     "tdic_subset_compute": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int, C.c_void_p,

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <mutex>
 #include <numeric>
 
 namespace tdic {
@@ -781,6 +782,184 @@ tdic_status tdic_subset_compute(tdic_ctx* ctx, const void* reference, const void
         int32_t gw, gh;
         tdic_grid_dims(width, height, cfg->propagation_spacing, &gw, &gh);
         *n_points = gw * gh;
+    });
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Propagation without allocation.  Some callers cannot allocate device memory at the time
+// they propagate: a real-time loop that must not stall on cudaMalloc's device
+// synchronisation, or a host process whose device memory is handed out by another allocator
+// that it may not bypass.  tdic_propagate_noalloc runs the same propagation kernel with its
+// scratch (work queue, claims, keys, parameters, sample offsets, ROI at the grid points) in
+// one file-scope device array instead of the context pool.
+// ---------------------------------------------------------------------------------------
+namespace {
+
+constexpr int kNoAllocMaxPoints = 131072;   // grid points per call (e.g. a 362 x 362 grid)
+constexpr int kNoAllocMaxOffsets = 32768;   // subset samples (a circle of radius 100 has 31417)
+
+struct NoAllocLayout {
+    size_t roi, claim, key, order, fetch, misc, dstate, dcnt, dq, kcorr, offsets, total;
+};
+
+constexpr size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+
+constexpr NoAllocLayout noalloc_layout(size_t n, size_t n_off) {
+    NoAllocLayout l{};
+    size_t o = 0;
+    l.roi = o;     o = align256(o + n);
+    l.claim = o;   o = align256(o + 4 * n);
+    l.key = o;     o = align256(o + (8 + 6 * 8) * n);   // keys then six float64 parameters
+    l.order = o;   o = align256(o + 4 * n);
+    l.fetch = o;   o = align256(o + 4 * (n + 2));
+    l.misc = o;    o = align256(o + 64);
+    l.dstate = o;  o = align256(o + 4 * n);
+    l.dcnt = o;    o = align256(o + 4 * n);
+    l.dq = o;      o = align256(o + 8 * n);
+    l.kcorr = o;   o = align256(o + 4 * n);
+    l.offsets = o; o = align256(o + 4 * n_off);
+    l.total = o;
+    return l;
+}
+
+constexpr size_t kNoAllocBytes = noalloc_layout(kNoAllocMaxPoints, kNoAllocMaxOffsets).total;  // about 11.8 MiB
+
+// One instance per device, created when the module is loaded on that device.
+static __device__ __align__(256) unsigned char noalloc_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex noalloc_mu;                                    // held for a whole call
+unsigned char* noalloc_ptr[kNoAllocMaxDevices] = {};      // address of the array, per device
+
+// Set-up, once per device, with that device current: the array's device address.
+unsigned char* noalloc_scratch_ptr(int device) {
+    TDIC_REQUIRE(device >= 0 && device < kNoAllocMaxDevices, TDIC_UNSUPPORTED, "device ordinal out of range");
+    if (!noalloc_ptr[device]) {
+        unsigned char* ptr = nullptr;
+        TDIC_CUDA_TRY(cudaGetSymbolAddress((void**)&ptr, noalloc_scratch));
+        noalloc_ptr[device] = ptr;
+    }
+    return noalloc_ptr[device];
+}
+
+// Host data reach the array through a small stack buffer: a pageable host-to-device copy
+// returns once its source has been staged, so the buffer can be refilled at once.
+template <typename Fill>
+void upload_chunked(unsigned char* dst, size_t bytes, Fill&& fill, cudaStream_t s) {
+    unsigned char chunk[4096];
+    for (size_t done = 0; done < bytes; done += sizeof(chunk)) {
+        const size_t k = std::min(sizeof(chunk), bytes - done);
+        fill(chunk, done, k);
+        TDIC_CUDA_TRY(cudaMemcpyAsync(dst + done, chunk, k, cudaMemcpyHostToDevice, s));
+    }
+}
+
+void propagate_noalloc_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const tdic_seed& seed,
+                            const uint8_t* roi, const tdic_grid_out* out, int32_t* points_computed, cudaStream_t s) {
+    check_config(cfg);
+    TDIC_REQUIRE(pair->exact == 1, TDIC_INVALID_ARG, "propagation needs a pair with the exact prefilter");
+    TDIC_REQUIRE(cfg.propagation_mode == 0 || cfg.propagation_mode == 2, TDIC_UNSUPPORTED,
+                 "propagation_mode 1 (serial heap order) is not on the GPU path; use 0 (frontier waves) or 2 (dataflow)");
+    const int w = pair->w, h = pair->h;
+    const int step = std::max(0, cfg.propagation_spacing) + 1;
+    int32_t gw, gh;
+    tdic_grid_dims(w, h, cfg.propagation_spacing, &gw, &gh);
+    const int n = gw * gh;
+    const int r = cfg.subset_radius;
+    int n_off = 0;
+    for (int dy = -r; dy <= r; ++dy)
+        for (int dx = -r; dx <= r; ++dx) n_off += dx * dx + dy * dy <= r * r;
+    TDIC_REQUIRE(n <= kNoAllocMaxPoints, TDIC_INVALID_ARG,
+                 "tdic_propagate_noalloc: the grid has " + std::to_string(n) + " points; its static scratch holds at most " +
+                     std::to_string(kNoAllocMaxPoints) + " (use tdic_propagate)");
+    TDIC_REQUIRE(n_off <= kNoAllocMaxOffsets, TDIC_INVALID_ARG,
+                 "tdic_propagate_noalloc: the subset has more samples than its static scratch holds");
+    *points_computed = 0;
+    const int sxr = static_cast<int>(std::round(seed.x)), syr = static_cast<int>(std::round(seed.y));
+    bool seed_ok = seed.found != 0 && roi_ok(roi, w, h, sxr, syr);
+    int gxs = 0, gys = 0;
+    if (seed_ok) {
+        gxs = nearest_grid_index(sxr, step, gw);
+        gys = nearest_grid_index(syr, step, gh);
+        seed_ok = roi_ok(roi, w, h, gxs * step, gys * step);
+    }
+    unsigned char* base = noalloc_scratch_ptr(ctx->device);
+    constexpr NoAllocLayout lay = noalloc_layout(kNoAllocMaxPoints, kNoAllocMaxOffsets);
+    // The array keeps the previous call's contents: everything the kernel reads before it
+    // writes is set here.
+    upload_chunked(base + lay.roi, n, [&](unsigned char* c, size_t at, size_t k) {
+        for (size_t j = 0; j < k; ++j) {
+            const size_t i = at + j;
+            c[j] = roi ? (roi[((i / gw) * step) * static_cast<size_t>(w) + (i % gw) * step] ? 1 : 0) : 1;
+        }
+    }, s);
+    // the row-major order of the context's table, so the sums run in the same order
+    int ody = -r, odx = -r - 1;
+    upload_chunked(base + lay.offsets, 4 * static_cast<size_t>(n_off), [&](unsigned char* c, size_t, size_t k) {
+        for (size_t j = 0; j < k; j += 4) {
+            do {
+                if (++odx > r) { odx = -r; ++ody; }
+            } while (odx * odx + ody * ody > r * r);
+            const short2 o = make_short2(static_cast<short>(odx), static_cast<short>(ody));
+            std::memcpy(c + j, &o, 4);
+        }
+    }, s);
+    TDIC_CUDA_TRY(cudaMemsetAsync(base + lay.claim, 0, sizeof(int) * n, s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(base + lay.key, 0xff, sizeof(unsigned long long) * n, s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(base + lay.fetch, 0, sizeof(int) * (n + 2), s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(base + lay.misc, 0, 64, s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(base + lay.misc + 19, 0x80, 1, s));  // queue word: tail 0, in-flight bias 2^31
+    TDIC_CUDA_TRY(cudaMemsetAsync(base + lay.dstate, 0, sizeof(int) * n, s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(base + lay.dcnt, 0, sizeof(int) * n, s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(base + lay.dq, 0xff, sizeof(unsigned long long) * n, s));
+    PropagateLaunch L{};
+    L.gw = gw; L.gh = gh; L.step = step;
+    L.roi_grid = base + lay.roi;
+    L.seed_idx = seed_ok ? gys * gw + gxs : 0;
+    L.seed_solve = seed_ok && (gxs * step != sxr || gys * step != syr) ? 1 : 0;
+    for (int k = 0; k < 6; ++k) L.seed_p[k] = seed.p[k];
+    L.seed_corr = seed.correlation;
+    L.out = *out;
+    L.claim = reinterpret_cast<int*>(base + lay.claim);
+    L.key = reinterpret_cast<unsigned long long*>(base + lay.key);
+    L.params = nullptr;
+    L.order = reinterpret_cast<int*>(base + lay.order);
+    int* m = reinterpret_cast<int*>(base + lay.misc);
+    L.counters = m;
+    L.barrier = reinterpret_cast<unsigned int*>(m + 8);
+    L.flags = m + 12;
+    L.fetch = reinterpret_cast<int*>(base + lay.fetch);
+    L.mode = cfg.propagation_mode;
+    L.sgx = gxs; L.sgy = gys;
+    L.dstate = reinterpret_cast<int*>(base + lay.dstate);
+    L.dcnt = reinterpret_cast<int*>(base + lay.dcnt);
+    L.dq = reinterpret_cast<unsigned long long*>(base + lay.dq);
+    L.kcorr = reinterpret_cast<float*>(base + lay.kcorr);
+    L.offsets = reinterpret_cast<const short2*>(base + lay.offsets);
+    L.n_offsets = n_off;
+    if (seed_ok) launch_propagate(ctx, pair, cfg, L, s);
+    else launch_init_grid(L.out, gw, gh, step, s);
+    int flags[3] = {0, 0, 0};
+    if (seed_ok) TDIC_CUDA_TRY(cudaMemcpyAsync(flags, L.flags, sizeof(flags), cudaMemcpyDeviceToHost, s));
+    check_device_error(ctx, s);
+    TDIC_REQUIRE(flags[0] == 0, TDIC_TIMEOUT, "propagation: a bounded in-kernel wait timed out");
+    *points_computed = (seed_ok && !flags[1]) ? flags[2] : 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+tdic_status tdic_propagate_noalloc(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cfg, const tdic_seed* seed,
+                                   const uint8_t* roi, const tdic_grid_out* out_device, int32_t* points_computed,
+                                   void* stream) {
+    return guarded(ctx, [&] {
+        TDIC_REQUIRE(pair && cfg && seed && out_device && points_computed, TDIC_INVALID_ARG, "null argument");
+        TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
+        std::lock_guard<std::mutex> lock(noalloc_mu);
+        propagate_noalloc_impl(ctx, pair, *cfg, *seed, roi, out_device, points_computed, pick(ctx, stream));
     });
 }
 

@@ -1309,17 +1309,22 @@ __global__ void init_grid_kernel(tdic_grid_out o, int gw, int gh, int step) {
 // Dispatch
 // ---------------------------------------------------------------------------------------
 template <typename T>
-Env<T> make_env(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, int radius, int max_iter, double thr) {
-    const SampleTable& tab = sample_table(ctx, radius);
+Env<T> make_env(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, int radius, int max_iter, double thr,
+                const short2* off = nullptr, int n_off = 0) {
+    if (!off) {
+        const SampleTable& tab = sample_table(ctx, radius);
+        off = tab.offsets.as<short2>();
+        n_off = tab.n;
+    }
     Env<T> e;
     e.ref = pair->ref.as<float>();
     e.coef = pair->coef.as<T>();
     e.w = pair->w; e.h = pair->h; e.cw = pair->cw; e.border = pair->border;
-    e.radius = radius; e.n = tab.n; e.nmax = tab.n;
-    e.off = tab.offsets.as<short2>();
+    e.radius = radius; e.n = n_off; e.nmax = n_off;
+    e.off = off;
     e.max_iter = max_iter;
     e.thr = thr;
-    e.inv_n = tab.n > 0 ? 1.0 / tab.n : 0.0;
+    e.inv_n = n_off > 0 ? 1.0 / n_off : 0.0;
     e.rpitch = pair->rpitch;
     e.cpitch = pair->cpitch;
     // Reference window: the subset with a one-pixel halo, x rounded down to 4 floats (16 B).
@@ -1424,7 +1429,8 @@ constexpr int kPropGroupsPerBlock = 2;
 template <int OPT, int DEG, typename T>
 void propagate_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const PropagateLaunch& L, cudaStream_t s) {
     constexpr int G = kPropG;
-    Env<T> e = make_env<T>(ctx, pair, cfg, cfg.subset_radius, cfg.max_iterations, cfg.convergence_threshold);
+    Env<T> e = make_env<T>(ctx, pair, cfg, cfg.subset_radius, cfg.max_iterations, cfg.convergence_threshold,
+                           L.offsets, L.n_offsets);
     TensorMaps tm = make_tensor_maps<T>(pair, e);
     const size_t per_group = group_smem_bytes<T>(e.nmax, G, e.rbx, e.rby, e.cbx, e.cby);
     const size_t prefix = cta_prefix_bytes(e.nmax);

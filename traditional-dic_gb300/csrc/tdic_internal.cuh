@@ -158,6 +158,8 @@ struct PropagateLaunch {
     int mode;
     int sgx, sgy;
     int* dstate; int* dcnt; unsigned long long* dq; float* kcorr;
+    // subset sample offsets; NULL = the context's table for the radius
+    const short2* offsets; int n_offsets;
 };
 void launch_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const PropagateLaunch& L,
                       cudaStream_t s);
