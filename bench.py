@@ -1,13 +1,13 @@
 """Benchmark: converged POIs/s of the 2D subset-DIC hot path on one GB300 (per rank).
 
-Workload (BASELINE configuration 2): a 2048 x 2048 uint8 synthetic speckle pair (24000 blobs,
+Workload: a 2048 x 2048 uint8 synthetic speckle pair (24000 blobs,
 u = 0.5 sin(2 pi x / 256), v = 0.3 cos(2 pi y / 192), noise 1), first-order ZNSSD ICGN, bicubic
 B-spline, subset radius 15, POI step 5 (410 x 410 grid, 163,216 interior POIs), threshold 1e-3,
 20 iterations, seed from the reference initializer.
 
 One step = the hot path over one image pair with the inputs resident in HBM: image conversion
-and B-spline prefilter (K1), then the frontier-wave propagation over every grid POI (K3), with
-device outputs.  ``value`` = converged POIs (valid, strictly converged, accepted) / step time.
+and B-spline prefilter (K1), then the propagation over every grid POI (K3, dataflow order by
+default), with device outputs.  ``value`` = converged POIs (valid, strictly converged, accepted) / step time.
 ``e2e`` = the same through the public API ``subset.compute`` with pinned host images: upload,
 seed selection, prefilter, propagation and the device->host result dict, every step.
 L2 (129 MB) is flushed with a 256 MB write between timed steps.
@@ -19,6 +19,7 @@ workload: reliability-guided heap propagation, single thread as the reference ru
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import statistics
@@ -38,11 +39,22 @@ __graft_entry__.load_package()
 METRIC = "converged POIs/s, 2048^2 r=15 (FP32 vs FP64, <=1e-3 px)"
 UNIT = "POI/s"
 WORKLOAD = {
-    "workload": "synthetic speckle 2048x2048 uint8, sinusoidal u/v, radius 15, POI step 5 (BASELINE config 2)",
+    "workload": "synthetic speckle 2048x2048 uint8, sinusoidal u/v, radius 15, POI step 5",
     "image": [2048, 2048], "dtype_in": "uint8", "subset_radius": 15, "poi_step": 5, "grid": [410, 410],
     "bspline_degree": 3, "threshold": 1e-3, "max_iterations": 20, "shape_function": "first_order",
     "optimizer": "icgn", "l2": "flushed (256 MB write) between timed steps",
 }
+
+
+def workload_desc(side: int) -> dict:
+    """WORKLOAD for a side x side case of the same generator (2048 = the benchmark itself)."""
+    if side == 2048:
+        return dict(WORKLOAD)
+    g = (side + 4) // 5
+    return dict(WORKLOAD, workload=f"synthetic speckle {side}x{side} uint8 (profiling case), sinusoidal u/v, "
+                                   f"radius 15, POI step 5", image=[side, side], grid=[g, g])
+
+
 CONFIG = {
     "subset": {"radius": 15},
     "optimization": {"max_iterations": 20, "convergence_threshold": 1e-3},
@@ -227,7 +239,7 @@ def run_ours(args, world, rank, local, pg):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     ctx = S.Context(local)
-    pair_np = synthetic.workload(1)
+    pair_np = synthetic.workload(1, side=args.side)
     h, w = pair_np.reference.shape
     cfg = S.config_from_dict(CONFIG)
     cfg.precision = L.FP64 if args.precision == "fp64" else L.FP32_MIXED
@@ -255,13 +267,13 @@ def run_ours(args, world, rank, local, pg):
                         context=ctx, return_seed=True)
     assert seed.found, "no seed found"
     pair = S.Pair(ctx, ref_d, def_d, degree=3, precision=cfg.precision, stream=stream)
-    pc = __import__("ctypes").c_int32()
+    pc = C.c_int32()
 
     def step():
         pair.update(ref_d, def_d, stream=stream)
-        ctx.check(ctx.lib.tdic_propagate(ctx.handle, pair.handle, __import__("ctypes").byref(cfg),
-                                         __import__("ctypes").byref(seed), None, __import__("ctypes").byref(grid),
-                                         L.DEVICE, __import__("ctypes").byref(pc), sptr))
+        ctx.check(ctx.lib.tdic_propagate(ctx.handle, pair.handle, C.byref(cfg),
+                                         C.byref(seed), None, C.byref(grid),
+                                         L.DEVICE, C.byref(pc), sptr))
 
     for _ in range(args.warmup):
         step()
@@ -279,9 +291,9 @@ def run_ours(args, world, rank, local, pg):
             e0.record(stream)
             pair.update(ref_d, def_d, stream=stream)
             e1.record(stream)
-            ctx.check(ctx.lib.tdic_propagate(ctx.handle, pair.handle, __import__("ctypes").byref(cfg),
-                                             __import__("ctypes").byref(seed), None, __import__("ctypes").byref(grid),
-                                             L.DEVICE, __import__("ctypes").byref(pc), sptr))
+            ctx.check(ctx.lib.tdic_propagate(ctx.handle, pair.handle, C.byref(cfg),
+                                             C.byref(seed), None, C.byref(grid),
+                                             L.DEVICE, C.byref(pc), sptr))
             e2.record(stream)
         e2.synchronize()
         times.append(e0.elapsed_time(e2) / 1e3)
@@ -320,9 +332,9 @@ def run_ours(args, world, rank, local, pg):
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
             pair64.update(ref_d, def_d, stream=stream)
-            ctx.check(ctx.lib.tdic_propagate(ctx.handle, pair64.handle, __import__("ctypes").byref(cfg64),
-                                             __import__("ctypes").byref(seed), None, __import__("ctypes").byref(grid),
-                                             L.DEVICE, __import__("ctypes").byref(pc), sptr))
+            ctx.check(ctx.lib.tdic_propagate(ctx.handle, pair64.handle, C.byref(cfg64),
+                                             C.byref(seed), None, C.byref(grid),
+                                             L.DEVICE, C.byref(pc), sptr))
             b.record(stream)
             b.synchronize()
             if i:
@@ -378,7 +390,7 @@ def run_ours(args, world, rank, local, pg):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64 (mixed)" if args.precision == "fp32" else "f64",
-            "data": "synthetic", "config": dict(WORKLOAD, precision=args.precision, propagation=args.mode,
+            "data": "synthetic", "config": dict(workload_desc(args.side), precision=args.precision, propagation=args.mode,
                                                   parallelism=f"replicas x{world}" if world > 1 else "1 GPU"),
             "converged_pois_per_step": conv,
             "roofline": roofline,
@@ -409,6 +421,8 @@ def main():
     ap.add_argument("--ref-solves", type=int, default=20000)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--side", type=int, default=2048,
+                    help="image side; 2048 is the benchmark workload, smaller sides are profiling cases")
     args = ap.parse_args()
     world, rank, local, pg = dist_setup(args)
     if args.impl == "reference":

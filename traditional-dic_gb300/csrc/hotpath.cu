@@ -311,19 +311,23 @@ struct Env {
     int* err;              // device error flag (TMA wait timeout)
 };
 
+// Per-POI result in the solve's own precision (float on the FP32-mixed path); outputs are
+// widened to double when they are written.
+template <typename M>
 struct Result {
-    double p[6];
-    double corr;
+    M p[6];
+    M corr;
     int iters;
     int status;
     bool valid;
     bool conv;
 };
 
-__device__ __forceinline__ void result_init(Result& r, const double (&p0)[6], double conf) {
+template <typename M>
+__device__ __forceinline__ void result_init(Result<M>& r, const M (&p0)[6], M conf) {
     r.p[0] = p0[0];
     r.p[1] = p0[1];
-    r.p[2] = r.p[3] = r.p[4] = r.p[5] = 0.0;
+    r.p[2] = r.p[3] = r.p[4] = r.p[5] = M(0);
     r.corr = conf;
     r.iters = 0;
     r.status = TDIC_INVALID_INPUT;
@@ -331,9 +335,8 @@ __device__ __forceinline__ void result_init(Result& r, const double (&p0)[6], do
     r.conv = false;
 }
 
-// Per-iteration scalar type: the FP32-mixed build keeps the 6x6 algebra, the parameter vector
-// and its update in float (FP64 only combines the normalisation sums); the FP64 build is
-// double throughout.
+// Per-iteration scalar type: the FP32-mixed build keeps the 6x6 algebra, the parameter vector,
+// its update and the normalisation algebra in float; the FP64 build is double throughout.
 template <typename T> struct MixedOf { using type = T; };
 
 
@@ -564,8 +567,9 @@ __device__ __forceinline__ void hessian_from_sums(const M (&S)[18], M scale, M (
 // kernel must then leave: the copy may still land in shared memory).
 template <int OPT, int DEG, typename T, int G>
 __device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUtensorMap* tm_coef, const short2* off,
-                          int cx, int cy, const double (&p0)[6], double conf, const GroupSmem<T>& gs,
-                          uint32_t& phase, int tid, int bar_id, Result& R) {
+                          int cx, int cy, const typename MixedOf<T>::type (&p0)[6],
+                          typename MixedOf<T>::type conf, const GroupSmem<T>& gs, uint32_t& phase, int tid,
+                          int bar_id, Result<typename MixedOf<T>::type>& R) {
     using M = typename MixedOf<T>::type;
     constexpr int NT = 32 * G, OFF = DEG / 2;
     M* s_hinv = reinterpret_cast<M*>(gs.hinv);
@@ -591,7 +595,7 @@ __device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUte
         // the box only needs the warped corners to a pixel (the drift margin is 3 px): float
         // arithmetic keeps this off the GB300's narrow FP64 pipe
         const float q0 = static_cast<float>(p0[0]), q1 = static_cast<float>(p0[1]), q2 = static_cast<float>(p0[2]),
-                    q3 = static_cast<float>(p0[3]), q4 = static_cast<float>(p0[4]), q5 = static_cast<float>(p0[5]);
+                    q3 = static_cast<float>(p0[3]), q4 = static_cast<float>(p0[4]), q5 = static_cast<float>(p0[5]);  // no-ops on the FP32 path
         const float rf = static_cast<float>(r);
         const float ax = fabsf(q2) * rf + fabsf(q3) * rf, ay = fabsf(q4) * rf + fabsf(q5) * rf;
         const float txmin = -rf + q0 - ax, tymin = -rf + q1 - ay;
@@ -669,13 +673,15 @@ __device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUte
         v20[0] = v2s[0];
         v20[1] = v2s[1];
     }
-    // normalisation sums combined in FP64: mean = shift + S1/N, sum (f - mean)^2 = S2 - S1^2/N
-    const double inv_n = e.inv_n;
-    const double s1 = static_cast<double>(v20[0]), s2 = static_cast<double>(v20[1]);
-    const double mshift = s1 * inv_n;
-    const double ss = fma(-s1, mshift, s2);
-    if (!(ss > kEps * kEps)) { R.status = TDIC_NUMERICAL_FAILURE; return true; }  // |f - mean| <= 1e-12
-    const T fm = T(static_cast<double>(fshift) + mshift);
+    // normalisation: mean = shift + S1/N, sum (f - mean)^2 = S2 - S1 * (S1/N), the latter as one
+    // fused multiply-add (a single rounding of the exact difference); the compensated sums
+    // S1, S2 carry the accuracy.
+    const M inv_n = M(e.inv_n), thr = M(e.thr);
+    const M s1 = static_cast<M>(v20[0]), s2 = static_cast<M>(v20[1]);
+    const M mshift = s1 * inv_n;
+    const M ss = fma(-s1, mshift, s2);
+    if (!(ss > M(kEps * kEps))) { R.status = TDIC_NUMERICAL_FAILURE; return true; }  // |f - mean| <= 1e-12
+    const T fm = T(M(fshift) + mshift);
     const T inv_norm = T(1) / sqrt(T(ss));
     for (int i = tid; i < e.n; i += NT) s_fn[i] = (s_fn[i] - fm) * inv_norm;
     if constexpr (OPT == 0) {
@@ -690,8 +696,8 @@ __device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUte
     group_sync<G>(bar_id);  // f^ (and the inverse) visible to the whole group
 
     M p[6];
-    for (int k = 0; k < 6; ++k) p[k] = static_cast<M>(p0[k]);
-    double corr = INFINITY;
+    for (int k = 0; k < 6; ++k) p[k] = p0[k];
+    M corr = M(INFINITY);
     bool converged = false;
     const M gscale = M(2) * inv_norm;
     for (int it = 0; it < e.max_iter; ++it) {
@@ -706,10 +712,10 @@ __device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUte
         T v3[3] = {sg.value(), sg2.value(), ok ? T(0) : T(1)};
         group_sum<G, 3>(v3, red, rp, tid, bar_id);
         if (v3[2] != T(0)) { R.status = TDIC_INVALID_INPUT; return true; }
-        // normalisation sums combined in FP64: mean of (g - fm) and sum (g - mean)^2
-        const double gmr = static_cast<double>(v3[0]) * inv_n;
-        const double var = fma(-static_cast<double>(v3[0]), gmr, static_cast<double>(v3[1]));
-        if (!(var > kEps * kEps)) { R.status = TDIC_NUMERICAL_FAILURE; return true; }  // |g - mean| <= 1e-12
+        // mean of (g - fm) and sum (g - mean)^2, as in the set-up
+        const M gmr = static_cast<M>(v3[0]) * inv_n;
+        const M var = fma(-static_cast<M>(v3[0]), gmr, static_cast<M>(v3[1]));
+        if (!(var > M(kEps * kEps))) { R.status = TDIC_NUMERICAL_FAILURE; return true; }  // |g - mean| <= 1e-12
         const T gsh = T(gmr);
         const T inv_gn = T(1) / sqrt(T(var));
         M dp[6];
@@ -726,7 +732,7 @@ __device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUte
                 q[6] += diff * diff;
             }
             group_sum<G, 7>(q, red, rp, tid, bar_id);
-            corr = static_cast<double>(q[6]);
+            corr = static_cast<M>(q[6]);
             M grad[6];
 #pragma unroll
             for (int k = 0; k < 6; ++k) grad[k] = static_cast<M>(q[k]) * gscale;
@@ -761,7 +767,7 @@ __device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUte
                 q[24] += diff * diff;
             }
             group_sum<G, 25>(q, red, rp, tid, bar_id);
-            corr = static_cast<double>(q[24]);
+            corr = static_cast<M>(q[24]);
             M S[18];
 #pragma unroll
             for (int k = 0; k < 18; ++k) S[k] = static_cast<M>(q[k]);
@@ -792,9 +798,9 @@ __device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUte
 #pragma unroll
         for (int k = 0; k < 6; ++k) p[k] = pn[k];
         if (!finite6(p)) { R.status = TDIC_NUMERICAL_FAILURE; return true; }
-        if (dn < M(e.thr)) { converged = true; break; }
+        if (dn < thr) { converged = true; break; }
     }
-    for (int k = 0; k < 6; ++k) R.p[k] = static_cast<double>(p[k]);
+    for (int k = 0; k < 6; ++k) R.p[k] = p[k];
     R.corr = corr;
     R.conv = converged;
     if (!converged && isfinite(corr)) converged = true;
@@ -803,11 +809,13 @@ __device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUte
     return true;
 }
 
-__device__ __forceinline__ void write_out(tdic_poi_out* o, const Result& R) {
-    for (int k = 0; k < 6; ++k) o->p[k] = R.p[k];
-    o->correlation = R.corr;
-    const double z = 1.0 - 0.5 * R.corr;
-    o->zncc = isfinite(R.corr) ? fmax(-1.0, fmin(1.0, z)) : -1.0;
+template <typename M>
+__device__ __forceinline__ void write_out(tdic_poi_out* o, const Result<M>& R) {
+    for (int k = 0; k < 6; ++k) o->p[k] = static_cast<double>(R.p[k]);
+    const double corr = static_cast<double>(R.corr);
+    o->correlation = corr;
+    const double z = 1.0 - 0.5 * corr;
+    o->zncc = isfinite(corr) ? fmax(-1.0, fmin(1.0, z)) : -1.0;
     o->iterations = R.iters;
     o->status = static_cast<int8_t>(R.status);
     o->valid = R.valid ? 1 : 0;
@@ -849,7 +857,7 @@ __device__ __forceinline__ void group_bcast3(int& a, int& b, int& c, int* slots,
 // each group's mbarrier.  Returns the shared offset table.
 template <typename T, int G>
 __device__ short2* kernel_preamble(const Env<T>& e, const CUtensorMap* tm_ref, const CUtensorMap* tm_coef,
-                                   unsigned char* smem_raw, int gi, int tid) {
+                                   unsigned char* smem_raw, int gi, int tid, bool group_member = true) {
     // TMA destinations need 128-byte alignment; the layout assumes an aligned dynamic base.
     if ((smem_u32(smem_raw) & 127u) != 0u) {
         if (threadIdx.x == 0) atomicExch(e.err, 4);
@@ -857,7 +865,7 @@ __device__ short2* kernel_preamble(const Env<T>& e, const CUtensorMap* tm_ref, c
     }
     short2* s_off = reinterpret_cast<short2*>(smem_raw);
     for (int i = threadIdx.x; i < e.n; i += blockDim.x) s_off[i] = e.off[i];
-    if (tid == 0) {
+    if (tid == 0 && group_member) {
         GroupSmem<T> gs(smem_raw + cta_prefix_bytes(e.nmax), gi, e.nmax, G, e.rbx, e.rby, e.cbx, e.cby);
         mbar_init(gs.bar, 1);
         fence_proxy_async();
@@ -877,6 +885,7 @@ template <int OPT, int DEG, typename T, int G>
 __global__ void solve_batch_kernel(Env<T> e, const __grid_constant__ CUtensorMap tm_ref,
                                    const __grid_constant__ CUtensorMap tm_coef, const tdic_poi_in* __restrict__ in,
                                    tdic_poi_out* __restrict__ out, int n, int* fetch) {
+    using M = typename MixedOf<T>::type;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int gi = threadIdx.x / (32 * G), tid = threadIdx.x % (32 * G);
     short2* s_off = kernel_preamble<T, G>(e, &tm_ref, &tm_coef, smem_raw, gi, tid);
@@ -891,12 +900,13 @@ __global__ void solve_batch_kernel(Env<T> e, const __grid_constant__ CUtensorMap
         job = group_bcast<G>(job, ints + 1, tid, bar_id);
         if (job >= n) break;
         const tdic_poi_in pin = in[job];
-        double p0[6];
-        for (int k = 0; k < 6; ++k) p0[k] = pin.p0[k];
+        M p0[6];
+        for (int k = 0; k < 6; ++k) p0[k] = static_cast<M>(pin.p0[k]);
         // icgn.cpp:472-473: std::round (halves away from zero), as CUDA's round()
         const int rx = static_cast<int>(round(pin.x)), ry = static_cast<int>(round(pin.y));
-        Result R;
-        if (!solve_poi<OPT, DEG, T, G>(e, &tm_ref, &tm_coef, s_off, rx, ry, p0, pin.confidence, gs, phase, tid, bar_id, R))
+        Result<M> R;
+        if (!solve_poi<OPT, DEG, T, G>(e, &tm_ref, &tm_coef, s_off, rx, ry, p0, static_cast<M>(pin.confidence), gs,
+                                       phase, tid, bar_id, R))
             return;  // a TMA wait timed out: e.err is set
         if (tid == 0) write_out(out + job, R);
     }
@@ -934,7 +944,11 @@ enum { kDfPending = 0, kDfAccepted = 2, kDfRejected = 3, kDfOrphan = 4 };
 
 __device__ __forceinline__ int ld_cg(const int* p) { return __ldcg(p); }
 
-__device__ bool grid_barrier(unsigned int* bar, int* err) {
+// Grid-wide barrier over the co-resident blocks (bar: count, generation, snapshot).  With
+// `snap`, the last block to arrive copies *snap into bar[2] while every other block waits, so
+// all blocks read the same value after the barrier (the wave-list tail: appends of the next
+// wave may start as soon as the barrier opens).
+__device__ bool grid_barrier(unsigned int* bar, int* err, const int* snap = nullptr) {
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned int* vgen = bar + 1;
@@ -942,6 +956,7 @@ __device__ bool grid_barrier(unsigned int* bar, int* err) {
         __threadfence();
         const unsigned int arrived = atomicAdd(bar, 1u);
         if (arrived == gridDim.x - 1) {
+            if (snap) bar[2] = static_cast<unsigned int>(*reinterpret_cast<const volatile int*>(snap));
             atomicExch(bar, 0u);
             __threadfence();
             atomicAdd(bar + 1, 1u);
@@ -958,51 +973,41 @@ __device__ bool grid_barrier(unsigned int* bar, int* err) {
     return *reinterpret_cast<volatile int*>(err) == 0;
 }
 
-template <typename P>
-__device__ __forceinline__ void store_params(P* params, int idx, const Result& R) {
-    for (int k = 0; k < 6; ++k) params[static_cast<size_t>(idx) * 6 + k] = static_cast<P>(R.p[k]);
+template <typename M>
+__device__ __forceinline__ void store_params(M* params, int idx, const Result<M>& R) {
+    for (int k = 0; k < 6; ++k) params[static_cast<size_t>(idx) * 6 + k] = R.p[k];
 }
 
-__device__ void store_outputs(const PropEnv& pe, int idx, const Result& R) {
+template <typename M>
+__device__ void store_outputs(const PropEnv& pe, int idx, const Result<M>& R) {
     const tdic_grid_out& o = pe.out;
-    if (o.u) o.u[idx] = R.p[0];
-    if (o.v) o.v[idx] = R.p[1];
-    if (o.du_dx) o.du_dx[idx] = R.p[2];
-    if (o.du_dy) o.du_dy[idx] = R.p[3];
-    if (o.dv_dx) o.dv_dx[idx] = R.p[4];
-    if (o.dv_dy) o.dv_dy[idx] = R.p[5];
-    if (o.correlation) o.correlation[idx] = R.corr;
-    if (o.zncc) o.zncc[idx] = fmax(-1.0, fmin(1.0, 1.0 - 0.5 * R.corr));
+    if (o.u) o.u[idx] = static_cast<double>(R.p[0]);
+    if (o.v) o.v[idx] = static_cast<double>(R.p[1]);
+    if (o.du_dx) o.du_dx[idx] = static_cast<double>(R.p[2]);
+    if (o.du_dy) o.du_dy[idx] = static_cast<double>(R.p[3]);
+    if (o.dv_dx) o.dv_dx[idx] = static_cast<double>(R.p[4]);
+    if (o.dv_dy) o.dv_dy[idx] = static_cast<double>(R.p[5]);
+    const double corr = static_cast<double>(R.corr);
+    if (o.correlation) o.correlation[idx] = corr;
+    if (o.zncc) o.zncc[idx] = fmax(-1.0, fmin(1.0, 1.0 - 0.5 * corr));
     if (o.valid) o.valid[idx] = 1;
     if (o.status) o.status[idx] = TDIC_SUCCESS;
     if (o.iterations) o.iterations[idx] = R.iters;
     if (o.converged) o.converged[idx] = R.conv ? 1 : 0;
 }
 
-template <typename P>
-__device__ void store_grid(const PropEnv& pe, P* params, int idx, const Result& R) {
-    const tdic_grid_out& o = pe.out;
-    if (o.u) o.u[idx] = R.p[0];
-    if (o.v) o.v[idx] = R.p[1];
-    if (o.du_dx) o.du_dx[idx] = R.p[2];
-    if (o.du_dy) o.du_dy[idx] = R.p[3];
-    if (o.dv_dx) o.dv_dx[idx] = R.p[4];
-    if (o.dv_dy) o.dv_dy[idx] = R.p[5];
-    if (o.correlation) o.correlation[idx] = R.corr;
-    if (o.zncc) o.zncc[idx] = fmax(-1.0, fmin(1.0, 1.0 - 0.5 * R.corr));
-    if (o.valid) o.valid[idx] = 1;
-    if (o.status) o.status[idx] = TDIC_SUCCESS;
-    if (o.iterations) o.iterations[idx] = R.iters;
-    if (o.converged) o.converged[idx] = R.conv ? 1 : 0;
-    for (int k = 0; k < 6; ++k) params[static_cast<size_t>(idx) * 6 + k] = static_cast<P>(R.p[k]);
+template <typename M>
+__device__ void store_grid(const PropEnv& pe, M* params, int idx, const Result<M>& R) {
+    store_params(params, idx, R);
+    store_outputs(pe, idx, R);
 }
 
 // Claim the admissible 4-neighbours of accepted point n for wave `next` and offer n as their
 // parent (key = float ZNSSD bits : parent index, atomicMin).  reliability_propagation.cpp:290-323.
-__device__ void expand(const PropEnv& pe, int w, int h, int radius, int n, double corr, int next) {
+__device__ void expand(const PropEnv& pe, int w, int h, int radius, int n, float corr, int next) {
     const int step = pe.step;
     const int nx = (n % pe.gw) * step, ny = (n / pe.gw) * step;
-    const unsigned long long k = (static_cast<unsigned long long>(__float_as_uint(static_cast<float>(corr))) << 32) |
+    const unsigned long long k = (static_cast<unsigned long long>(__float_as_uint(corr)) << 32) |
                                  static_cast<unsigned int>(n);
     const int dxs[4] = {0, step, 0, -step}, dys[4] = {-step, 0, step, 0};  // up, right, down, left
     for (int d = 0; d < 4; ++d) {
@@ -1056,85 +1061,264 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
 }
 constexpr unsigned int kInFlightBias = 0x80000000u;  // in-flight count = low word - bias
 
+// Queue item: parent (high 32, -1 = orphan) : point (low 32).
+__device__ __forceinline__ unsigned long long df_item(int parent, int c) {
+    return (static_cast<unsigned long long>(static_cast<unsigned int>(parent)) << 32) | static_cast<unsigned int>(c);
+}
+
+// Add (k to the queue tail, dflight to the in-flight count) in one 64-bit atomic and publish k
+// items.  The in-flight count sits in the low word with an offset of 2^31, so it never borrows.
+__device__ __forceinline__ void df_publish(const PropEnv& pe, const unsigned long long* items, int k, int dflight) {
+    const unsigned long long add = (static_cast<unsigned long long>(k) << 32) +
+                                   static_cast<unsigned long long>(static_cast<long long>(dflight));
+    if (k == 0) {
+        if (dflight != 0) atomicAdd(pe.qword, add);  // result unused: a reduction, no round trip
+        return;
+    }
+    const int pos = static_cast<int>(atomicAdd(pe.qword, add) >> 32);
+    for (int i = 0; i < k; ++i) st_release_u64(pe.dq + pos + i, items[i]);  // release: n's state first
+}
+
 // n has been resolved: its state (and, if accepted, its parameters) are written.  Its children
 // are the 4-neighbours one step farther from the seed.  A child is queued from its primary
 // parent as soon as that one is accepted; otherwise the last of its parents to resolve
 // decides: secondary parent if accepted, else orphan.  Exactly one thread decides each child
 // (the accepted primary, or the unique last parent when the primary failed), so no further
-// claim is needed.  `self_in_flight` is 1 when n itself was a queued item: the in-flight count
-// then trades n for its queued children in one atomic, before the children become visible.
-__device__ void df_resolve(const PropEnv& pe, int n, bool accepted, int self_in_flight) {
+// claim is needed.
+//
+// Children that n decides alone are published first, with one atomic, so they wait on no
+// other memory round trip; the parent counters follow.  `cont` (from df_pick_cont, or -1) is
+// a child whose primary parent is n (accepted) that the caller solves itself instead of
+// queueing it, which takes the queue off the critical path of a chain of primary parents.
+// `self_in_flight` is 1 when n itself was counted in flight (a queued or continued item); the
+// continued child inherits that count, otherwise the last atomic gives it up.
+__device__ int df_children(const PropEnv& pe, int n, int (&kid)[4], int (&kp1)[4], int (&kp2)[4]) {
     const int gx = n % pe.gw, gy = n / pe.gw;
     const int dn = abs(gx - pe.sgx) + abs(gy - pe.sgy);
     const int cxs[4] = {gx, gx + 1, gx, gx - 1}, cys[4] = {gy - 1, gy, gy + 1, gy};
-    unsigned long long push[4];
-    int k = 0;
-    fence_acq_rel();  // publish n's state and parameters before any child counter update
+    int nk = 0;
     for (int d = 0; d < 4; ++d) {
         const int cx = cxs[d], cy = cys[d];
         if (cx < 0 || cy < 0 || cx >= pe.gw || cy >= pe.gh) continue;
         if (abs(cx - pe.sgx) + abs(cy - pe.sgy) != dn + 1) continue;
-        const int c = cy * pe.gw + cx;
-        int p1, p2;
-        df_parents(pe, c, p1, p2);
-        int parent = -2;  // -2: not decided here
-        if (p1 == n && accepted) {
-            parent = n;
-        } else if (p2 < 0) {
-            parent = -1;  // single parent, failed: orphan
-        } else if (atomicAdd(pe.dcnt + c, 1) == 1) {  // the second of two parents to resolve
-            fence_acq_rel();
-            const int s1 = ld_cg(pe.dstate + p1);
-            if (s1 != kDfAccepted) parent = (ld_cg(pe.dstate + p2) == kDfAccepted) ? p2 : -1;
-        }
-        if (p1 == n && accepted && p2 >= 0) atomicAdd(pe.dcnt + c, 1);  // keep the count for the other parent
-        if (parent != -2)
-            push[k++] = (static_cast<unsigned long long>(static_cast<unsigned int>(parent)) << 32) |
-                        static_cast<unsigned int>(c);
+        kid[nk] = cy * pe.gw + cx;
+        df_parents(pe, kid[nk], kp1[nk], kp2[nk]);
+        ++nk;
     }
-    // One 64-bit atomic updates both the queue tail (high word, +k) and the in-flight count
-    // (low word, + k - self).  The low word carries an offset of 2^31 so it never borrows.
-    if (k == 0 && self_in_flight == 0) return;
-    const unsigned long long add = (static_cast<unsigned long long>(k) << 32) +
-                                   static_cast<unsigned long long>(static_cast<long long>(k - self_in_flight));
-    const unsigned long long old = atomicAdd(pe.qword, add);
-    const int pos = static_cast<int>(old >> 32);
-    for (int i = 0; i < k; ++i) st_release_u64(pe.dq + pos + i, push[i]);
+    return nk;
 }
 
+// Length of the longest primary-parent chain below grid point c (the depth of its subtree).
+// With the primary parent one step toward the seed along the dominant axis (x on ties), a
+// point off the diagonal band owns only the rest of its row (|dx| > |dy|) or column
+// (|dx| < |dy| - 1); a diagonal point, and the point just before it on the y side that is the
+// diagonal point's primary parent, reach the far corner of their quadrant.
+__device__ __forceinline__ int df_depth(const PropEnv& pe, int c) {
+    const int dx = c % pe.gw - pe.sgx, dy = c / pe.gw - pe.sgy;
+    const int ax = abs(dx), ay = abs(dy);
+    const int ex = dx > 0 ? pe.gw - 1 - pe.sgx : (dx < 0 ? pe.sgx : max(pe.sgx, pe.gw - 1 - pe.sgx));
+    const int ey = dy > 0 ? pe.gh - 1 - pe.sgy : (dy < 0 ? pe.sgy : max(pe.sgy, pe.gh - 1 - pe.sgy));
+    if (ax > ay) return ex - ax;
+    if (ax < ay - 1) return ey - ay;
+    return (ex - ax) + (ey - ay);
+}
+
+// The child an accepted n continues with: of the children whose primary parent is n, the one
+// with the deepest subtree (the first in up, right, down, left order on ties), so that the
+// longest chains run without a queue hand-off; -1 if none.  Only scheduling depends on it.
+__device__ int df_pick_cont(const PropEnv& pe, int n, bool accepted) {
+    if (!accepted) return -1;
+    int kid[4], kp1[4], kp2[4];
+    const int nk = df_children(pe, n, kid, kp1, kp2);
+    int best = -1, best_depth = -1;
+    for (int i = 0; i < nk; ++i) {
+        if (kp1[i] != n) continue;
+        const int dep = df_depth(pe, kid[i]);
+        if (dep > best_depth) { best = kid[i]; best_depth = dep; }
+    }
+    return best;
+}
+
+__device__ void df_resolve(const PropEnv& pe, int n, bool accepted, int self_in_flight, int cont) {
+    int kid[4], kp1[4], kp2[4];
+    const int nk = df_children(pe, n, kid, kp1, kp2);
+    // children decided by n alone: accepted primary (queued, or continued), failed single parent
+    unsigned long long push[4];
+    int k = 0;
+    for (int i = 0; i < nk; ++i) {
+        if (kp1[i] == n && accepted) {
+            if (kid[i] != cont) push[k++] = df_item(n, kid[i]);
+        } else if (kp2[i] < 0) {
+            push[k++] = df_item(-1, kid[i]);  // its only parent failed: orphan
+        }
+    }
+    const int handed = cont >= 0 ? self_in_flight : 0;  // n's in-flight count passes to the continued child
+    df_publish(pe, push, k, k + (cont >= 0 ? 1 : 0) - handed);
+    // children with two parents: count the parents, the second one decides
+    bool counted = false;
+    for (int i = 0; i < nk; ++i) counted |= kp2[i] >= 0;
+    if (counted) fence_acq_rel();  // publish n's state before any child counter update
+    int k2 = 0;
+    for (int i = 0; i < nk; ++i) {
+        if (kp2[i] < 0) continue;
+        if (kp1[i] == n && accepted) {
+            atomicAdd(pe.dcnt + kid[i], 1);  // keep the count for the other parent (no round trip)
+        } else if (atomicAdd(pe.dcnt + kid[i], 1) == 1) {  // the second of two parents to resolve
+            fence_acq_rel();
+            if (ld_cg(pe.dstate + kp1[i]) != kDfAccepted)
+                push[k2++] = df_item(ld_cg(pe.dstate + kp2[i]) == kDfAccepted ? kp2[i] : -1, kid[i]);
+        }
+    }
+    df_publish(pe, push, k2, k2 - (self_in_flight - handed));
+}
+
+// Propagation groups: 4 warps per POI, two groups and one resolver warp per CTA, two CTAs per
+// SM.  Per-POI latency on the dataflow critical path bounds the propagation; measured on
+// 2048^2, r = 15: 8 warps per POI were 14% slower (the two-stage group reductions and barriers
+// grow with the group), four groups sharing one resolver warp 5% slower.
+constexpr int kPropG = 4;
+constexpr int kPropGroupsPerBlock = 2;
+constexpr int kPropMinBlocks = 2;  // resident CTAs per SM the register budget is sized for
+
+// Dataflow hand-over between a solver group and the resolver warp of its block (shared memory).
+template <typename P>
+struct DfSlot {
+    int post;    // 1: a solved point waits for the resolver
+    int want;    // 1: the group waits for a queued item
+    int ready;   // 1: item in (c, par); 2: propagation finished; 3: error
+    int n, state, cont, iters, conv;
+    int c, par;
+    P p[6];
+    P corr;
+};
+
+__device__ __forceinline__ int vld(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+__device__ __forceinline__ void vst(int* p, int v) { *reinterpret_cast<volatile int*>(p) = v; }
+
+// One lane of the resolver warp serves one solver group: it settles the points the group posts
+// (parameters, state, children, outputs) and fetches queue items when the group asks for one.
+// The group never waits on these global-memory round trips unless its queue runs dry.
+template <typename P>
+__device__ void df_resolver_lane(const PropEnv& pe, DfSlot<P>* slot, P* params, int* s_done) {
+    const int ng = pe.gw * pe.gh;
+    int ticket = -1;
+    unsigned long long idle = 0;
+    while (true) {
+        bool progress = false;
+        if (vld(&slot->post) == 1) {
+            __threadfence_block();
+            const int n = slot->n, st = slot->state, cont = slot->cont;
+            Result<P> R;
+            for (int k = 0; k < 6; ++k) R.p[k] = slot->p[k];
+            R.corr = slot->corr;
+            R.iters = slot->iters;
+            R.conv = slot->conv != 0;
+            const bool acc = st == kDfAccepted;
+            if (acc) {
+                store_params(params, n, R);
+                pe.kcorr[n] = static_cast<float>(R.corr);
+            }
+            pe.dstate[n] = st;
+            df_resolve(pe, n, acc, 1, cont);
+            if (acc) {
+                store_outputs(pe, n, R);
+                atomicAdd(pe.flags + 2, 1);
+            }
+            __threadfence_block();
+            vst(&slot->post, 0);
+            progress = true;
+        }
+        if (vld(&slot->want) == 1) {
+            int deliver = 0;
+            if (vld(s_done)) {
+                deliver = 2;
+            } else if (*reinterpret_cast<volatile int*>(pe.flags) != 0) {
+                deliver = 3;
+            } else {
+                // At most gw*gh - 1 points are ever queued (each once, never the seed), so a
+                // ticket beyond the array can only end by completion; it reads nothing.
+                if (ticket < 0) ticket = atomicAdd(pe.counters + 1, 1);
+                const unsigned long long it = ticket < ng ? ld_acquire_u64(pe.dq + ticket) : ~0ull;
+                if (it != ~0ull) {  // acquire: the parent's parameters were released before it
+                    slot->c = static_cast<int>(it & 0xffffffffull);
+                    slot->par = static_cast<int>(it >> 32);
+                    ticket = -1;
+                    deliver = 1;
+                } else if (static_cast<unsigned int>(__ldcg(pe.qword) & 0xffffffffull) == kInFlightBias) {
+                    vst(s_done, 1);  // nothing queued or running anywhere
+                    deliver = 2;
+                }
+            }
+            if (deliver != 0) {
+                vst(&slot->want, 0);
+                __threadfence_block();
+                vst(&slot->ready, deliver);
+                if (deliver != 1) return;
+                progress = true;
+            }
+        }
+        if (progress) {
+            idle = 0;
+        } else {
+            if (++idle > kSpinLimit) {
+                atomicExch(pe.flags, 1);
+                vst(&slot->ready, 3);
+                return;
+            }
+            __nanosleep(idle < 64 ? 20 : 100);
+        }
+    }
+}
+
+// The propagation.  Blocks hold `gpb` solver groups of G warps; in the dataflow order one more
+// warp per block is the resolver.  Launched cooperatively (co-resident blocks, own grid barrier).
 template <int OPT, int DEG, typename T, int G>
-__global__ void __launch_bounds__(256, 2) propagate_kernel(Env<T> e, const __grid_constant__ CUtensorMap tm_ref,
-                                                           const __grid_constant__ CUtensorMap tm_coef, PropEnv pe) {
+__global__ void __launch_bounds__(32 * G * kPropGroupsPerBlock + 32, sizeof(T) == 4 ? kPropMinBlocks : 1)
+    propagate_kernel(Env<T> e, const __grid_constant__ CUtensorMap tm_ref, const __grid_constant__ CUtensorMap tm_coef,
+                     PropEnv pe) {
     using P = typename MixedOf<T>::type;
     extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int gpb = static_cast<int>(blockDim.x - 32) / (32 * G);
     const int gi = threadIdx.x / (32 * G), tid = threadIdx.x % (32 * G);
-    short2* s_off = kernel_preamble<T, G>(e, &tm_ref, &tm_coef, smem_raw, gi, tid);
+    const bool solver = gi < gpb;
+    short2* s_off = kernel_preamble<T, G>(e, &tm_ref, &tm_coef, smem_raw, gi, tid, solver);
     if (s_off == nullptr) {  // every block takes this path together: nothing waits on a barrier yet
         if (threadIdx.x == 0) atomicExch(pe.flags, 1);
         return;
     }
-    GroupSmem<T> gs(smem_raw + cta_prefix_bytes(e.nmax), gi, e.nmax, G, e.rbx, e.rby, e.cbx, e.cby);
+    GroupSmem<T> gs(smem_raw + cta_prefix_bytes(e.nmax), solver ? gi : 0, e.nmax, G, e.rbx, e.rby, e.cbx, e.cby);
     int* ints = gs.ints;
     const int bar_id = 1 + gi;
     uint32_t phase = 0;
     P* params = reinterpret_cast<P*>(pe.key + static_cast<size_t>(pe.gw) * pe.gh);  // params follow the keys
-    const double cutoff = static_cast<double>(pe.step);
+    const P cutoff = static_cast<P>(pe.step), max_znssd = static_cast<P>(pe.max_znssd);
+    unsigned char* ctl = smem_raw + cta_prefix_bytes(e.nmax) +
+                         gpb * group_smem_bytes<T>(e.nmax, G, e.rbx, e.rby, e.cbx, e.cby);
+    DfSlot<P>* slots = reinterpret_cast<DfSlot<P>*>(ctl);
+    int* s_done = reinterpret_cast<int*>(ctl + round128(gpb * sizeof(DfSlot<P>)));
+    if (threadIdx.x < gpb) {
+        DfSlot<P>* sl = slots + threadIdx.x;
+        sl->post = 0; sl->want = 0; sl->ready = 0;
+    }
+    if (threadIdx.x == 0) *s_done = 0;
 
     // Prologue: place the seed (reliability_propagation.cpp:201-278).
     if (blockIdx.x == 0 && gi == 0) {
-        Result R;
+        Result<P> R;
         bool ok = true;
         if (pe.seed_solve) {
             const int sx = (pe.seed_idx % pe.gw) * pe.step, sy = (pe.seed_idx / pe.gw) * pe.step;
-            if (!solve_poi<OPT, DEG, T, G>(e, &tm_ref, &tm_coef, s_off, sx, sy, pe.seed_p, pe.seed_corr, gs, phase, tid,
-                                           bar_id, R)) {
+            P sp[6];
+            for (int k = 0; k < 6; ++k) sp[k] = static_cast<P>(pe.seed_p[k]);
+            if (!solve_poi<OPT, DEG, T, G>(e, &tm_ref, &tm_coef, s_off, sx, sy, sp, static_cast<P>(pe.seed_corr), gs,
+                                           phase, tid, bar_id, R)) {
                 if (tid == 0) { pe.flags[1] = 1; atomicExch(pe.flags, 1); }
                 ok = false;
             }
             ok = ok && R.valid && R.status == TDIC_SUCCESS && finite6(R.p) && isfinite(R.corr);
         } else {
-            for (int k = 0; k < 6; ++k) R.p[k] = pe.seed_p[k];
-            R.corr = pe.seed_corr;
+            for (int k = 0; k < 6; ++k) R.p[k] = static_cast<P>(pe.seed_p[k]);
+            R.corr = static_cast<P>(pe.seed_corr);
             R.iters = 0;
             R.status = TDIC_SUCCESS;
             R.valid = true;
@@ -1148,86 +1332,110 @@ __global__ void __launch_bounds__(256, 2) propagate_kernel(Env<T> e, const __gri
                 pe.claim[pe.seed_idx] = 1;
                 pe.flags[2] = 1;
                 if (pe.mode == 2) {
-                    pe.kcorr[pe.seed_idx] = static_cast<float>(fmax(0.0, R.corr));
+                    pe.kcorr[pe.seed_idx] = static_cast<float>(fmax(P(0), R.corr));
                     pe.dstate[pe.seed_idx] = kDfAccepted;
-                    df_resolve(pe, pe.seed_idx, true, 0);
+                    df_resolve(pe, pe.seed_idx, true, 0, -1);
                 } else {
                     __threadfence();
-                    expand(pe, e.w, e.h, e.radius, pe.seed_idx, fmax(0.0, R.corr), 1);
+                    expand(pe, e.w, e.h, e.radius, pe.seed_idx, static_cast<float>(fmax(P(0), R.corr)), 1);
                 }
             }
         }
     }
-    if (!grid_barrier(pe.barrier, pe.flags)) return;
+    if (!grid_barrier(pe.barrier, pe.flags, pe.counters)) return;
     if (*reinterpret_cast<volatile int*>(pe.flags + 1)) return;
 
     if (pe.mode == 2) {
-        // ---- dataflow phase: ticketed work queue, no grid-wide synchronisation -------------
-        while (true) {
-            int item_c = -1, item_p = -1, state = 0;  // state: 0 item, 1 done, 2 error
-            if (tid == 0) {
-                const int t = atomicAdd(pe.counters + 1, 1);
-                // At most gw*gh - 1 points are ever queued (each once, never the seed), so a
-                // ticket beyond the array can only end by completion; it reads nothing.
-                const bool in_range = t < pe.gw * pe.gh;
-                unsigned long long spins = 0;
-                while (true) {
-                    const unsigned long long it = in_range ? ld_acquire_u64(pe.dq + t) : ~0ull;
-                    if (it != ~0ull) {  // acquire: the parent's parameters were released before it
-                        item_c = static_cast<int>(it & 0xffffffffull);
-                        item_p = static_cast<int>(it >> 32);
-                        break;
+        // ---- dataflow phase: no grid-wide synchronisation ------------------------------------
+        if (solver) {
+            DfSlot<P>* slot = slots + gi;
+            // A group continues with a child whose primary parent it just accepted (every
+            // thread derives the same child); otherwise it asks its resolver lane for an item.
+            int cont_c = -1, cont_p = -1;
+            P cp[6];
+            while (true) {
+                int item_c = cont_c, item_p = cont_p, state = 0;  // state: 0 item, 1 done, 2 error
+                if (cont_c < 0) {
+                    if (tid == 0) {
+                        vst(&slot->ready, 0);
+                        __threadfence_block();
+                        vst(&slot->want, 1);
+                        unsigned long long spins = 0;
+                        while (true) {
+                            const int r = vld(&slot->ready);
+                            if (r != 0) {
+                                __threadfence_block();
+                                state = r == 1 ? 0 : (r == 2 ? 1 : 2);
+                                item_c = slot->c;
+                                item_p = slot->par;
+                                break;
+                            }
+                            if (++spins > kSpinLimit) { atomicExch(pe.flags, 1); state = 2; break; }
+                            __nanosleep(spins < 64 ? 20 : 200);
+                        }
                     }
-                    const unsigned int inflight = static_cast<unsigned int>(__ldcg(pe.qword) & 0xffffffffull);
-                    if (inflight == kInFlightBias) { state = 1; break; }  // nothing queued or running
-                    if (++spins > kSpinLimit) { atomicExch(pe.flags, 1); state = 2; break; }
-                    __nanosleep(spins < 64 ? 20 : 200);
+                    group_bcast3<G>(state, item_c, item_p, ints + 1, tid, bar_id);
+                    if (state != 0) break;
                 }
-            }
-            group_bcast3<G>(state, item_c, item_p, ints + 1, tid, bar_id);
-            if (state != 0) break;
-            const int n = item_c;
-            const int nx = (n % pe.gw) * pe.step, ny = (n / pe.gw) * pe.step;
-            bool accepted = false;
-            int new_state = kDfOrphan;
-            Result R;
-            if (item_p >= 0) {
-                const bool admissible = pe.roi_grid[n] != 0 && nx - e.radius >= 0 && ny - e.radius >= 0 &&
-                                        nx + e.radius < e.w && ny + e.radius < e.h;
-                new_state = kDfRejected;
-                if (admissible) {
-                    double pp[6];
-                    for (int k = 0; k < 6; ++k) pp[k] = static_cast<double>(__ldcg(params + static_cast<size_t>(item_p) * 6 + k));
-                    const double ddx = static_cast<double>(nx - (item_p % pe.gw) * pe.step);
-                    const double ddy = static_cast<double>(ny - (item_p / pe.gw) * pe.step);
-                    double p0[6];
-                    p0[0] = pp[0] + pp[2] * ddx + pp[3] * ddy;  // reliability_propagation.cpp:326-329
-                    p0[1] = pp[1] + pp[4] * ddx + pp[5] * ddy;
-                    p0[2] = pp[2]; p0[3] = pp[3]; p0[4] = pp[4]; p0[5] = pp[5];
-                    if (!solve_poi<OPT, DEG, T, G>(e, &tm_ref, &tm_coef, s_off, nx, ny, p0, 0.0, gs, phase, tid, bar_id,
-                                                   R)) {
-                        if (tid == 0) atomicExch(pe.flags, 1);
-                        return;  // TMA wait timed out
+                const int n = item_c;
+                const int nx = (n % pe.gw) * pe.step, ny = (n / pe.gw) * pe.step;
+                bool accepted = false;
+                int new_state = kDfOrphan;
+                Result<P> R;
+                R.iters = 0;
+                R.conv = false;
+                if (item_p >= 0) {
+                    const bool admissible = pe.roi_grid[n] != 0 && nx - e.radius >= 0 && ny - e.radius >= 0 &&
+                                            nx + e.radius < e.w && ny + e.radius < e.h;
+                    new_state = kDfRejected;
+                    if (admissible) {
+                        P pp[6];
+                        if (cont_c >= 0) {
+                            for (int k = 0; k < 6; ++k) pp[k] = cp[k];
+                        } else {
+                            for (int k = 0; k < 6; ++k) pp[k] = __ldcg(params + static_cast<size_t>(item_p) * 6 + k);
+                        }
+                        const P ddx = static_cast<P>(nx - (item_p % pe.gw) * pe.step);
+                        const P ddy = static_cast<P>(ny - (item_p / pe.gw) * pe.step);
+                        P p0[6];
+                        p0[0] = pp[0] + pp[2] * ddx + pp[3] * ddy;  // reliability_propagation.cpp:326-329
+                        p0[1] = pp[1] + pp[4] * ddx + pp[5] * ddy;
+                        p0[2] = pp[2]; p0[3] = pp[3]; p0[4] = pp[4]; p0[5] = pp[5];
+                        if (!solve_poi<OPT, DEG, T, G>(e, &tm_ref, &tm_coef, s_off, nx, ny, p0, P(0), gs, phase, tid,
+                                                       bar_id, R)) {
+                            if (tid == 0) atomicExch(pe.flags, 1);
+                            return;  // TMA wait timed out
+                        }
+                        accepted = R.valid && R.status == TDIC_SUCCESS && R.corr < max_znssd &&
+                                   fabs(p0[0] - R.p[0]) < cutoff && fabs(p0[1] - R.p[1]) < cutoff && finite6(R.p) &&
+                                   isfinite(R.corr);  // :359-368
+                        if (accepted) new_state = kDfAccepted;
                     }
-                    accepted = R.valid && R.status == TDIC_SUCCESS && R.corr < pe.max_znssd &&
-                               fabs(p0[0] - R.p[0]) < cutoff && fabs(p0[1] - R.p[1]) < cutoff && finite6(R.p) &&
-                               isfinite(R.corr);  // :359-368
-                    if (accepted) new_state = kDfAccepted;
                 }
+                const int next = df_pick_cont(pe, n, accepted);
+                if (tid == 0) {
+                    // hand n to the resolver lane (its slot holds one point; normally long free)
+                    unsigned long long spins = 0;
+                    while (vld(&slot->post) != 0) {
+                        if (++spins > kSpinLimit) { atomicExch(pe.flags, 1); break; }
+                        __nanosleep(20);
+                    }
+                    slot->n = n; slot->state = new_state; slot->cont = next;
+                    slot->iters = R.iters; slot->conv = R.conv ? 1 : 0;
+                    for (int k = 0; k < 6; ++k) slot->p[k] = R.p[k];
+                    slot->corr = R.corr;
+                    __threadfence_block();
+                    vst(&slot->post, 1);
+                }
+                if (next >= 0)
+                    for (int k = 0; k < 6; ++k) cp[k] = R.p[k];
+                cont_c = next;
+                cont_p = n;
             }
-            if (tid == 0) {
-                // children first: the parameters and state they need, then the output arrays
-                if (accepted) {
-                    store_params<P>(params, n, R);
-                    pe.kcorr[n] = static_cast<float>(R.corr);
-                }
-                pe.dstate[n] = new_state;
-                df_resolve(pe, n, accepted, 1);
-                if (accepted) {
-                    store_outputs(pe, n, R);
-                    atomicAdd(pe.flags + 2, 1);
-                }
-            }
+        } else {
+            const int lane = threadIdx.x & 31;
+            if (lane < gpb) df_resolver_lane<P>(pe, slots + lane, params, s_done);
+            __syncwarp();
         }
         if (!grid_barrier(pe.barrier, pe.flags)) return;
         // ---- clean-up: orphans are reached by frontier waves from every accepted point ------
@@ -1239,15 +1447,15 @@ __global__ void __launch_bounds__(256, 2) propagate_kernel(Env<T> e, const __gri
         if (!grid_barrier(pe.barrier, pe.flags)) return;
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ng; i += gridDim.x * blockDim.x)
             if (ld_cg(pe.dstate + i) == kDfAccepted) expand(pe, e.w, e.h, e.radius, i, __ldcg(pe.kcorr + i), 1);
-        if (!grid_barrier(pe.barrier, pe.flags)) return;
+        if (!grid_barrier(pe.barrier, pe.flags, pe.counters)) return;
     }
 
     // ---- frontier waves -----------------------------------------------------------------
     int start = 0;
-    int end = ld_cg(pe.counters);
+    int end = static_cast<int>(__ldcg(pe.barrier + 2));  // the wave-list tail at the last barrier
     for (int wave = 1; start < end; ++wave) {
         const int count = end - start;
-        while (true) {
+        while (solver) {
             int i = 0;
             if (tid == 0) i = atomicAdd(pe.fetch + wave, 1);
             i = group_bcast<G>(i, ints + 1, tid, bar_id);
@@ -1255,33 +1463,33 @@ __global__ void __launch_bounds__(256, 2) propagate_kernel(Env<T> e, const __gri
             const int n = ld_cg(pe.order + start + i);
             const unsigned long long kk = __ldcg(pe.key + n);
             const int parent = static_cast<int>(kk & 0xffffffffull);
-            double pp[6];
-            for (int k = 0; k < 6; ++k) pp[k] = static_cast<double>(__ldcg(params + static_cast<size_t>(parent) * 6 + k));
+            P pp[6];
+            for (int k = 0; k < 6; ++k) pp[k] = __ldcg(params + static_cast<size_t>(parent) * 6 + k);
             const int nx = (n % pe.gw) * pe.step, ny = (n / pe.gw) * pe.step;
-            const double ddx = static_cast<double>(nx - (parent % pe.gw) * pe.step);
-            const double ddy = static_cast<double>(ny - (parent / pe.gw) * pe.step);
-            double p0[6];
+            const P ddx = static_cast<P>(nx - (parent % pe.gw) * pe.step);
+            const P ddy = static_cast<P>(ny - (parent / pe.gw) * pe.step);
+            P p0[6];
             p0[0] = pp[0] + pp[2] * ddx + pp[3] * ddy;  // reliability_propagation.cpp:326-329
             p0[1] = pp[1] + pp[4] * ddx + pp[5] * ddy;
             p0[2] = pp[2]; p0[3] = pp[3]; p0[4] = pp[4]; p0[5] = pp[5];
-            Result R;
-            if (!solve_poi<OPT, DEG, T, G>(e, &tm_ref, &tm_coef, s_off, nx, ny, p0, 0.0, gs, phase, tid, bar_id, R)) {
+            Result<P> R;
+            if (!solve_poi<OPT, DEG, T, G>(e, &tm_ref, &tm_coef, s_off, nx, ny, p0, P(0), gs, phase, tid, bar_id, R)) {
                 if (tid == 0) atomicExch(pe.flags, 1);
                 return;  // TMA wait timed out
             }
-            const bool accepted = R.valid && R.status == TDIC_SUCCESS && R.corr < pe.max_znssd &&
+            const bool accepted = R.valid && R.status == TDIC_SUCCESS && R.corr < max_znssd &&
                                   fabs(p0[0] - R.p[0]) < cutoff && fabs(p0[1] - R.p[1]) < cutoff && finite6(R.p) &&
                                   isfinite(R.corr);  // :359-368
             if (accepted && tid == 0) {
                 store_grid<P>(pe, params, n, R);
                 atomicAdd(pe.flags + 2, 1);
                 __threadfence();
-                expand(pe, e.w, e.h, e.radius, n, R.corr, wave + 1);
+                expand(pe, e.w, e.h, e.radius, n, static_cast<float>(R.corr), wave + 1);
             }
         }
-        if (!grid_barrier(pe.barrier, pe.flags)) return;
+        if (!grid_barrier(pe.barrier, pe.flags, pe.counters)) return;
         start = end;
-        end = ld_cg(pe.counters);
+        end = static_cast<int>(__ldcg(pe.barrier + 2));
     }
 }
 
@@ -1419,13 +1627,6 @@ void solve_deg(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const Sol
     }
 }
 
-// Propagation groups: 4 warps per POI, two groups per CTA, two CTAs per SM.  Per-POI latency
-// on the dataflow critical path bounds the propagation; measured on 2048^2, r = 15, 8 warps
-// per POI were 14% slower (the two-stage group reductions and barriers grow with the group)
-// and one or two groups per CTA timed the same.
-constexpr int kPropG = 4;
-constexpr int kPropGroupsPerBlock = 2;
-
 template <int OPT, int DEG, typename T>
 void propagate_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const PropagateLaunch& L, cudaStream_t s) {
     constexpr int G = kPropG;
@@ -1435,14 +1636,17 @@ void propagate_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, con
     const size_t per_group = group_smem_bytes<T>(e.nmax, G, e.rbx, e.rby, e.cbx, e.cby);
     const size_t prefix = cta_prefix_bytes(e.nmax);
     int gpb = kPropGroupsPerBlock;
-    while (gpb > 1 && prefix + gpb * per_group > static_cast<size_t>(ctx->max_smem_optin)) --gpb;
-    TDIC_REQUIRE(prefix + per_group <= static_cast<size_t>(ctx->max_smem_optin), TDIC_UNSUPPORTED,
+    using P = typename MixedOf<T>::type;
+    const size_t ctl = round128(kPropGroupsPerBlock * sizeof(DfSlot<P>)) + 128;  // resolver hand-over
+    while (gpb > 1 && prefix + gpb * per_group + ctl > static_cast<size_t>(ctx->max_smem_optin)) --gpb;
+    TDIC_REQUIRE(prefix + per_group + ctl <= static_cast<size_t>(ctx->max_smem_optin), TDIC_UNSUPPORTED,
                  "subset radius too large for shared memory");
-    const size_t smem = prefix + gpb * per_group;
+    const size_t smem = prefix + gpb * per_group + ctl;
+    const int threads = 32 * G * gpb + 32;  // solver groups + the resolver warp
     auto kern = propagate_kernel<OPT, DEG, T, G>;
     TDIC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     int per_sm = 0;
-    TDIC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * G * gpb, smem));
+    TDIC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
     TDIC_REQUIRE(per_sm > 0, TDIC_UNSUPPORTED, "subset radius too large for shared memory");
     const int blocks = per_sm * ctx->num_sms;
     PropEnv pe;
@@ -1462,7 +1666,7 @@ void propagate_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, con
     init_grid_kernel<<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, s>>>(L.out, L.gw, L.gh, L.step);
     TDIC_CUDA_TRY(cudaGetLastError());
     void* args[] = {&e, &tm.ref, &tm.coef, &pe};
-    TDIC_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kern), dim3(blocks), dim3(32 * G * gpb), args,
+    TDIC_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kern), dim3(blocks), dim3(threads), args,
                                               smem, s));
 }
 

@@ -147,14 +147,17 @@ def speckle_pair(shape, n_blobs, fld: Field, noise: float, seed: int, dtype=np.u
 
 
 def workload(index: int, side: int | None = None) -> Pair:
-    """The seeded pair of workload ``index`` (0: 256^2, 1: 2048^2, 4: 5120^2; 2/3 need ``side``)."""
+    """The seeded pair of workload ``index`` (0: 256^2, 1: 2048^2, 4: 5120^2).  For workload 1,
+    ``side`` renders the same field and speckle density on a side x side image (the blob count
+    scales with the area), a smaller case of the same work for profiling."""
     seed = BASE_SEED + index
     if index == 0:
         f = Field("linear", dict(u0=2.3, ux=0.001, uy=0.0, v0=-1.7, vx=0.0, vy=-0.0005))
         return speckle_pair((256, 256), 1500, f, 0.5, seed)
     if index == 1:
+        side = side or 2048
         f = Field("sine", dict(au=0.5, lu=256.0, av=0.3, lv=192.0))
-        return speckle_pair((2048, 2048), 24000, f, 1.0, seed)
+        return speckle_pair((side, side), int(round(24000 * (side / 2048.0) ** 2)), f, 1.0, seed)
     if index == 4:
         f = Field("bump", dict(cx=2560.0, cy=2560.0, s=600.0, a=4.0, shear=0.02, sa=0.2, sl=64.0))
         return speckle_pair((5120, 5120), 150000, f, 2.0, seed, dtype=np.uint16, sigma=(1.5, 5.0))
