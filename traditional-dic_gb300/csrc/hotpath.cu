@@ -50,35 +50,67 @@ template <typename T> struct Kahan {
     __device__ __forceinline__ T value() const { return s - c; }
 };
 
-template <typename T> __device__ __forceinline__ T warp_sum(T v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
 __device__ __forceinline__ void named_bar(int id, int nthreads) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
+// Reduce-scatter of K values over a warp by recursive halving: at each of log2(KP) levels a
+// lane keeps one half of its values and trades the other half with its partner, so the K
+// sums take KP - 1 shuffles (KP = K rounded up to a power of two) instead of 5K; the levels
+// left over for KP < 32 finish the sum of one value.  Lane l ends with the warp total of value
+// (l >> (5 - log2 KP)) & (KP - 1).
+template <int K> struct Pow2Ceil {
+    static constexpr int value = K <= 1 ? 1 : K <= 2 ? 2 : K <= 4 ? 4 : K <= 8 ? 8 : K <= 16 ? 16 : 32;
+    static constexpr int log2 = K <= 1 ? 0 : K <= 2 ? 1 : K <= 4 ? 2 : K <= 8 ? 3 : K <= 16 ? 4 : 5;
+};
+
+template <int K, typename T>
+__device__ __forceinline__ T warp_scatter_sum(const T (&v)[K], int lane) {
+    static_assert(K >= 1 && K <= 32, "at most one value per lane");
+    constexpr int KP = Pow2Ceil<K>::value, LG = Pow2Ceil<K>::log2;
+    T w[KP];
+#pragma unroll
+    for (int j = 0; j < KP; ++j) w[j] = j < K ? v[j] : T(0);
+#pragma unroll
+    for (int lev = 0; lev < LG; ++lev) {
+        const int o = 16 >> lev;
+        const int half = KP >> (lev + 1);
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int j = 0; j < half; ++j) {
+            const T send = upper ? w[j] : w[j + half];
+            const T keep = upper ? w[j + half] : w[j];
+            w[j] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    T r = w[0];
+#pragma unroll
+    for (int lev = LG; lev < 5; ++lev) r += __shfl_xor_sync(0xffffffffu, r, 16 >> lev);
+    return r;
+}
+
 // All-reduce K values over the group: every thread ends with the same sums (summed in the same
-// order), so redundant scalar math stays bit-identical across the group's warps.  Warp shuffles,
-// then thread k < K adds the G warp partials of value k, then everyone reads the K totals.
-// `red` holds two buffers of 32*G values used alternately (parity `rp`): a buffer is rewritten
-// only after every thread has passed the barriers of the reduction in between.
+// order), so redundant scalar math stays bit-identical across the group's warps.  A warp
+// reduce-scatter, then thread k < K adds the G warp partials of value k, then everyone reads
+// the K totals.  `red` holds two buffers of 32*G values used alternately (parity `rp`): a
+// buffer is rewritten only after every thread has passed the barriers of the reduction in
+// between.
 template <int G, int K, typename T>
 __device__ __forceinline__ void group_sum(T (&v)[K], T* red_base, int& rp, int tid, int bar_id) {
     static_assert(G == 1 || K * (G + 1) <= 32 * G, "reduction scratch: G*K partials + K totals per buffer");
+    constexpr int LG = Pow2Ceil<K>::log2;
+    const int lane = tid & 31;
+    const T r = warp_scatter_sum<K, T>(v, lane);
+    const int idx = (lane >> (5 - LG)) & ((1 << LG) - 1);
+    if constexpr (G == 1) {
 #pragma unroll
-    for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
-    if constexpr (G > 1) {
+        for (int k = 0; k < K; ++k) v[k] = __shfl_sync(0xffffffffu, r, k << (5 - LG));
+    } else {
         T* red = red_base + rp * 32 * G;
         T* tot = red + G * K;
         rp ^= 1;
-        const int warp = tid >> 5, lane = tid & 31;
-        if (lane == 0) {
-#pragma unroll
-            for (int k = 0; k < K; ++k) red[warp * K + k] = v[k];
-        }
+        const int warp = tid >> 5;
+        if ((lane & ((1 << (5 - LG)) - 1)) == 0 && idx < K) red[warp * K + idx] = r;
         named_bar(bar_id, 32 * G);
         if (tid < K) {
             T acc = red[tid];
