@@ -181,6 +181,28 @@ def test_compute_matches_oracle_pipeline(oracle, gpu_ctx, workload0):
     assert d.max() <= 10 * U_TOL
 
 
+@pytest.mark.parametrize("with_roi", [False, True])
+def test_select_seed_matches_oracle(oracle, gpu_ctx, workload0, with_roi):
+    """Seed selection (sampled candidate points, k-means, integer search, subpixel refinement)
+    against the oracle; 256^2 has more candidate points than the k-means sample limit."""
+    import __graft_entry__ as G
+    from traditional_dic_gb300 import subset as S
+    p = workload0
+    roi = None
+    if with_roi:
+        yy, xx = np.mgrid[:256, :256]
+        roi = (((xx - 150) ** 2 + (yy - 120) ** 2) < 90 ** 2) | ((xx < 60) & (yy > 100))
+    cfg = S.config_from_dict(G.WORKLOAD0_CONFIG)
+    lazy = S.Pair(gpu_ctx, p.reference, p.deformed, degree=3, exact=False)
+    got = S.select_seed(gpu_ctx, lazy, p.reference.astype(np.float32), cfg, roi=roi)
+    want, _ = oracle.select_seed(p.reference, p.deformed, oracle.as_config(cfg), roi=roi)
+    assert got.found and want.found
+    assert (got.x, got.y) == (want.x, want.y)
+    assert abs(got.p[0] - want.p[0]) <= U_TOL and abs(got.p[1] - want.p[1]) <= U_TOL
+    if roi is not None:
+        assert roi[int(got.y), int(got.x)]
+
+
 def _heap(oracle, cfg):
     c = oracle.as_config(cfg)
     c.propagation_mode = 1

@@ -340,32 +340,90 @@ double texture_std(const Acc& ref, int w, int h, int r, int x, int y) {
     return std::sqrt(std::max(0.0, sq / cnt - mn * mn));
 }
 
+// The candidate points of SeedSelector (ROI and the subset margin), in row-major order,
+// addressed by rank without materialising them (a 2048^2 image has four million).
+class ValidPoints {
+public:
+    ValidPoints(int w, int h, const uint8_t* roi, int rad, bool margin)
+        : w_(w), h_(h), roi_(roi), x0_(margin ? rad : 0), x1_(margin ? w - 1 - rad : w - 1),
+          y0_(margin ? rad : 0), y1_(margin ? h - 1 - rad : h - 1), rows_(std::max(0, h)) {
+        total_ = 0;
+        for (int y = 0; y < h_; ++y) {
+            long long c = 0;
+            if (y >= y0_ && y <= y1_ && x1_ >= x0_) {
+                if (!roi_) {
+                    c = x1_ - x0_ + 1;
+                } else {
+                    const uint8_t* r = roi_ + static_cast<size_t>(y) * w_;
+                    for (int x = x0_; x <= x1_; ++x) c += r[x] != 0;
+                }
+            }
+            rows_[y] = c;
+            total_ += c;
+        }
+    }
+    long long size() const { return total_; }
+    // The points of the given ranks (ascending, repeats allowed).
+    std::vector<Pt> select(const std::vector<long long>& ranks) const {
+        std::vector<Pt> out;
+        out.reserve(ranks.size());
+        long long base = 0;
+        int y = 0;
+        std::vector<int> xs;  // valid x of row y (with a ROI)
+        int xs_row = -1;
+        for (const long long rk : ranks) {
+            while (y < h_ && base + rows_[y] <= rk) base += rows_[y++];
+            if (y >= h_) break;
+            const long long k = rk - base;
+            if (!roi_) {
+                out.push_back({x0_ + static_cast<int>(k), y});
+            } else {
+                if (xs_row != y) {
+                    xs.clear();
+                    const uint8_t* r = roi_ + static_cast<size_t>(y) * w_;
+                    for (int x = x0_; x <= x1_; ++x)
+                        if (r[x]) xs.push_back(x);
+                    xs_row = y;
+                }
+                out.push_back({xs[static_cast<size_t>(k)], y});
+            }
+        }
+        return out;
+    }
+private:
+    int w_, h_;
+    const uint8_t* roi_;
+    int x0_, x1_, y0_, y1_;
+    std::vector<long long> rows_;
+    long long total_;
+};
+
+// SeedSelector's candidate points (seed_selector.cpp:207-317): a deterministic sample of the
+// ROI points, k-means centres, and the texture check with its nearest-50 fallback.  The
+// nearest-centre assignment of each k-means iteration runs on the device; the centre sums
+// are accumulated here in point order, as in run_kmeans.
 template <typename Acc>
-std::vector<std::pair<int, int>> seed_candidates(const Acc& ref, int w, int h, const uint8_t* roi, const tdic_config& c) {
+std::vector<std::pair<int, int>> seed_candidates(tdic_ctx* ctx, const Acc& ref, int w, int h, const uint8_t* roi,
+                                                 const tdic_config& c, cudaStream_t s) {
     std::vector<std::pair<int, int>> out;
     const int rad = std::max(std::max(1, c.is_subset_radius), std::max(1, c.sp_subset_radius));
     auto margin_ok = [&](int x, int y) { return !(x - rad < 0 || y - rad < 0 || x + rad >= w || y + rad >= h); };
-    std::vector<Pt> pts;
-    for (int y = 0; y < h; ++y)
-        for (int x = 0; x < w; ++x)
-            if (roi_ok(roi, w, h, x, y) && margin_ok(x, y)) pts.push_back({x, y});
-    if (pts.empty())
-        for (int y = 0; y < h; ++y)
-            for (int x = 0; x < w; ++x)
-                if (roi_ok(roi, w, h, x, y)) pts.push_back({x, y});
-    if (pts.empty()) return out;
+    ValidPoints vp(w, h, roi, rad, true);
+    if (vp.size() == 0) vp = ValidPoints(w, h, roi, rad, false);
+    const long long npts = vp.size();
+    if (npts == 0) return out;
     const int requested = std::max(1, c.seed_count);
     const int limit = std::max(1, c.kmeans_sample_limit);
-    std::vector<Pt> sp;
-    if (static_cast<int>(pts.size()) <= limit) {
-        sp = pts;
+    std::vector<long long> ranks;
+    if (npts <= limit) {
+        ranks.resize(static_cast<size_t>(npts));
+        std::iota(ranks.begin(), ranks.end(), 0LL);
     } else {
-        const double st = static_cast<double>(pts.size() - 1U) / static_cast<double>(limit - 1);
-        for (int i = 0; i < limit; ++i) {
-            const auto idx = static_cast<size_t>(std::llround(static_cast<double>(i) * st));
-            sp.push_back(pts[std::min(idx, pts.size() - 1U)]);
-        }
+        const double st = static_cast<double>(npts - 1) / static_cast<double>(limit - 1);
+        for (int i = 0; i < limit; ++i)
+            ranks.push_back(std::min<long long>(std::llround(static_cast<double>(i) * st), npts - 1));
     }
+    const std::vector<Pt> sp = vp.select(ranks);
     const int tr = std::max(1, c.is_subset_radius);
     if (requested == 1) {
         double best = -1.0;
@@ -388,26 +446,27 @@ std::vector<std::pair<int, int>> seed_candidates(const Acc& ref, int w, int h, c
         cx[i] = p.x;
         cy[i] = p.y;
     }
-    std::vector<double> sx(count), sy(count);
-    std::vector<int> cnt(count);
-    for (int it = 0; it < std::max(0, c.kmeans_iterations); ++it) {
-        std::fill(sx.begin(), sx.end(), 0.0);
-        std::fill(sy.begin(), sy.end(), 0.0);
-        std::fill(cnt.begin(), cnt.end(), 0);
-        for (const auto& p : sp) {
-            int best = 0;
-            double bd = std::numeric_limits<double>::infinity();
-            for (int i = 0; i < count; ++i) {
-                const double dx = p.x - cx[i], dy = p.y - cy[i];
-                const double d2 = dx * dx + dy * dy;
-                if (d2 < bd) { bd = d2; best = i; }
+    const int iters = std::max(0, c.kmeans_iterations);
+    if (iters > 0) {
+        const int m = static_cast<int>(sp.size());
+        std::vector<int> px(m), py(m), asg(m);
+        for (int j = 0; j < m; ++j) { px[j] = sp[j].x; py[j] = sp[j].y; }
+        KmeansAssigner ka(ctx, px.data(), py.data(), m, count, s);
+        std::vector<double> sx(count), sy(count);
+        std::vector<int> cnt(count);
+        for (int it = 0; it < iters; ++it) {
+            ka.assign(cx.data(), cy.data(), asg.data());
+            std::fill(sx.begin(), sx.end(), 0.0);
+            std::fill(sy.begin(), sy.end(), 0.0);
+            std::fill(cnt.begin(), cnt.end(), 0);
+            for (int j = 0; j < m; ++j) {
+                sx[asg[j]] += px[j];
+                sy[asg[j]] += py[j];
+                ++cnt[asg[j]];
             }
-            sx[best] += p.x;
-            sy[best] += p.y;
-            ++cnt[best];
+            for (int i = 0; i < count; ++i)
+                if (cnt[i] > 0) { cx[i] = sx[i] / cnt[i]; cy[i] = sy[i] / cnt[i]; }
         }
-        for (int i = 0; i < count; ++i)
-            if (cnt[i] > 0) { cx[i] = sx[i] / cnt[i]; cy[i] = sy[i] / cnt[i]; }
     }
     for (int i = 0; i < count; ++i) {
         const int rx = static_cast<int>(std::llround(cx[i])), ry = static_cast<int>(std::llround(cy[i]));
@@ -459,7 +518,7 @@ void select_seed_impl(tdic_ctx* ctx, tdic_pair* lazy, const HostImage& ref_host,
                       tdic_seed* seed, cudaStream_t s) {
     std::memset(seed, 0, sizeof(*seed));
     const int w = lazy->w, h = lazy->h;
-    const auto cands = seed_candidates(ref_host, w, h, roi, c);
+    const auto cands = seed_candidates(ctx, ref_host, w, h, roi, c, s);
     if (c.sift_enabled) return;  // without OpenCV the SIFT prior finds no match: no seed
     const int n = static_cast<int>(cands.size());
     if (n == 0) return;

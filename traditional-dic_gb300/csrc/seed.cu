@@ -233,6 +233,25 @@ __global__ void fine_kernel(const float* __restrict__ ref, const float* __restri
     }
 }
 
+// One thread per point.  Each squared distance is rounded as the reference's
+// dx * dx + dy * dy on a host without fused multiply-add (product, product, sum), so the
+// nearest centre and its ties resolve as there.
+__global__ void kmeans_assign_kernel(const int2* __restrict__ pts, int m, const double2* __restrict__ ctr, int k,
+                                     int* __restrict__ assign) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    const double x = static_cast<double>(pts[j].x), y = static_cast<double>(pts[j].y);
+    int best = 0;
+    double bd = INFINITY;
+    for (int i = 0; i < k; ++i) {
+        const double2 c = __ldg(ctr + i);  // same address across the warp: one broadcast load
+        const double dx = __dsub_rn(x, c.x), dy = __dsub_rn(y, c.y);
+        const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+        if (d2 < bd) { bd = d2; best = i; }
+    }
+    assign[j] = best;
+}
+
 std::vector<short2> circle_offsets(int r, int step) {
     std::vector<short2> o;
     step = step < 1 ? 1 : step;
@@ -243,6 +262,25 @@ std::vector<short2> circle_offsets(int r, int step) {
 }
 
 }  // namespace
+
+KmeansAssigner::KmeansAssigner(tdic_ctx* ctx, const int* px, const int* py, int m, int k, cudaStream_t s)
+    : ctx_(ctx), s_(s), m_(m), k_(k), pts_(&ctx->pool, sizeof(int2) * std::max(m, 1)),
+      ctr_(&ctx->pool, sizeof(double2) * std::max(k, 1)), out_(&ctx->pool, sizeof(int) * std::max(m, 1)) {
+    std::vector<int2> p(m);
+    for (int i = 0; i < m; ++i) p[i] = make_int2(px[i], py[i]);
+    TDIC_CUDA_TRY(cudaMemcpyAsync(pts_.ptr, p.data(), sizeof(int2) * m, cudaMemcpyHostToDevice, s_));
+    TDIC_CUDA_TRY(cudaStreamSynchronize(s_));  // p is a local
+}
+
+void KmeansAssigner::assign(const double* cx, const double* cy, int* assign_host) {
+    std::vector<double2> c(k_);
+    for (int i = 0; i < k_; ++i) c[i] = make_double2(cx[i], cy[i]);
+    TDIC_CUDA_TRY(cudaMemcpyAsync(ctr_.ptr, c.data(), sizeof(double2) * k_, cudaMemcpyHostToDevice, s_));
+    kmeans_assign_kernel<<<(m_ + 255) / 256, 256, 0, s_>>>(pts_.as<int2>(), m_, ctr_.as<double2>(), k_, out_.as<int>());
+    TDIC_CUDA_TRY(cudaGetLastError());
+    TDIC_CUDA_TRY(cudaMemcpyAsync(assign_host, out_.ptr, sizeof(int) * m_, cudaMemcpyDeviceToHost, s_));
+    TDIC_CUDA_TRY(cudaStreamSynchronize(s_));
+}
 
 void integer_search_batch(tdic_ctx* ctx, tdic_pair* lazy, const tdic_config& cfg, const int* cx, const int* cy, int n,
                           SearchResult* out_host, cudaStream_t s) {

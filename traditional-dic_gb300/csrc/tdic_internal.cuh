@@ -168,6 +168,18 @@ void launch_init_grid(const tdic_grid_out& out, int gw, int gh, int step, cudaSt
 
 // Seed search (seed.cu) -------------------------------------------------------------------
 struct SearchResult { int u, v; double zncc; int ok; };
+// Nearest-centre assignment of k-means (run_kmeans, seed_selector.cpp:69-104) on the device:
+// assign[i] = the lowest-index centre at the smallest squared distance from point i.
+class KmeansAssigner {
+public:
+    KmeansAssigner(tdic_ctx* ctx, const int* px, const int* py, int m, int k, cudaStream_t s);
+    void assign(const double* cx, const double* cy, int* assign_host);
+private:
+    tdic_ctx* ctx_;
+    cudaStream_t s_;
+    int m_, k_;
+    Buffer pts_, ctr_, out_;
+};
 void integer_search_batch(tdic_ctx* ctx, tdic_pair* lazy, const tdic_config& cfg, const int* cx, const int* cy,
                           int n, SearchResult* out, cudaStream_t s);
 
