@@ -4,9 +4,10 @@
 // Per candidate: a coarse search over every displacement that keeps the subset inside the
 // image, on a pyramid_scale-strided grid with the pyramid_scale-strided circular samples
 // (search_ncorr_multigrid :208-265); a full-sample refinement around the coarse optimum; a
-// full-sample local search over +-search_radius; the local-preference rule (:267-280).  Scores
-// are the circular-subset ZNCC of circular_subset_zncc (:129-166) accumulated in FP64 per
-// position; ties keep the first position in the reference's v-major scan order.
+// full-sample local search over +-search_radius; the local-preference rule (:267-280).  The
+// winner of each search is the reference's: the circular-subset ZNCC of circular_subset_zncc
+// (:129-166) in FP64 decides, ties keep the first position in the reference's v-major scan
+// order; FP32 scores only select the positions that are rescored in FP64.
 #include "tdic_internal.cuh"
 
 #include <algorithm>
@@ -37,45 +38,112 @@ __device__ __forceinline__ bool better(double z, int idx, double bz, int bidx) {
     return false;
 }
 
-// ZNCC of the circular subset at displacement (u, v); -inf when the subset leaves the image or
-// the deformed subset is flat.  Samples: offsets off[0..n), reference values rv, mean rm, norm rn.
-__device__ double zncc_at(const float* __restrict__ def, int w, int h, int pitch, const short2* off, const double* rv,
-                          int n, double rm, double rn, int cx, int cy, int u, int v) {
-    if (n == 0 || rn <= kEps) return -INFINITY;
-    double dm = 0.0;
-    for (int i = 0; i < n; ++i) {
-        const int x = cx + u + off[i].x, y = cy + v + off[i].y;
-        if (x < 0 || y < 0 || x >= w || y >= h) return -INFINITY;
-        dm += static_cast<double>(__ldg(def + static_cast<size_t>(y) * pitch + x));
+// The search scores every position in FP32 and rescores in FP64, exactly as
+// circular_subset_zncc (integer_search.cpp:129-166: sums in sample order, each operation
+// rounded once, no fused multiply-add), only the positions whose FP32 score is within
+// kScoreMargin of the FP32 maximum, or whose deformed subset is nearly flat.  The FP32 score
+// of a textured subset is within n * 2^-23 (~4e-5 for 317 samples) of the FP64 one, well
+// inside kScoreMargin / 2, so the FP64 maximum is always among the rescored positions and the
+// winner (with the reference's scan-order tie rule) is the reference's.
+constexpr float kScoreMargin = 1e-3f;
+
+// Reference samples of one candidate (shared memory): FP64 values and their mean and norm in
+// the reference's order, plus FP32 copies for the scoring pass.
+struct RefSet {
+    double* r64;
+    float* r32;
+    double* stats;  // mean, norm
+    float* fstats;  // mean, norm, sum of centred FP32 values
+};
+
+__device__ void load_ref(const float* __restrict__ ref, int pitch, const short2* off, int n, int cx, int cy,
+                         const RefSet& rs) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float v = __ldg(ref + static_cast<size_t>(cy + off[i].y) * pitch + cx + off[i].x);
+        rs.r64[i] = static_cast<double>(v);
+        rs.r32[i] = v;
     }
-    dm /= static_cast<double>(n);
-    double num = 0.0, dn = 0.0;
-    for (int i = 0; i < n; ++i) {
-        const double rd = rv[i] - rm;
-        const double dd = static_cast<double>(__ldg(def + static_cast<size_t>(cy + v + off[i].y) * pitch + cx + u + off[i].x)) - dm;
-        num += rd * dd;
-        dn += dd * dd;
+    __syncthreads();
+    if (threadIdx.x == 0) {  // sample_mean, sample_norm (integer_search.cpp:111-127)
+        double m = 0.0;
+        for (int i = 0; i < n; ++i) m = __dadd_rn(m, rs.r64[i]);
+        m = n > 0 ? __ddiv_rn(m, static_cast<double>(n)) : 0.0;
+        double q = 0.0;
+        for (int i = 0; i < n; ++i) {
+            const double d = __dsub_rn(rs.r64[i], m);
+            q = __dadd_rn(q, __dmul_rn(d, d));
+        }
+        rs.stats[0] = m;
+        rs.stats[1] = q;
+        const float mf = static_cast<float>(m);
+        float sr = 0.0f;
+        for (int i = 0; i < n; ++i) sr += rs.r32[i] - mf;
+        rs.fstats[0] = mf;
+        rs.fstats[1] = static_cast<float>(q);
+        rs.fstats[2] = sr;
     }
-    if (dn <= kEps) return -INFINITY;
-    return num / sqrt(rn * dn);
+    __syncthreads();
 }
 
-// Reference samples of one candidate into shared memory: values, mean, norm (sum of squares).
-__device__ void load_ref(const float* __restrict__ ref, int pitch, const short2* off, int n, int cx, int cy, double* rv,
-                         double* stats) {
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-        rv[i] = static_cast<double>(__ldg(ref + static_cast<size_t>(cy + off[i].y) * pitch + cx + off[i].x));
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double m = 0.0;
-        for (int i = 0; i < n; ++i) m += rv[i];
-        m = n > 0 ? m / n : 0.0;
-        double s = 0.0;
-        for (int i = 0; i < n; ++i) { const double d = rv[i] - m; s += d * d; }
-        stats[0] = m;
-        stats[1] = s;
+// circular_subset_zncc in FP64, rounded as on the reference's host.  The caller guarantees
+// that the subset lies inside the image.
+__device__ double zncc64(const float* __restrict__ def, int pitch, const short2* off, const double* r64, int n,
+                         double rm, double rn, int cx, int cy, int u, int v) {
+    if (n == 0 || rn <= kEps) return -INFINITY;
+    double dm = 0.0;
+    for (int i = 0; i < n; ++i)
+        dm = __dadd_rn(dm, static_cast<double>(__ldg(def + static_cast<size_t>(cy + v + off[i].y) * pitch + cx + u + off[i].x)));
+    dm = __ddiv_rn(dm, static_cast<double>(n));
+    double num = 0.0, dn = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double rd = __dsub_rn(r64[i], rm);
+        const double dd = __dsub_rn(
+            static_cast<double>(__ldg(def + static_cast<size_t>(cy + v + off[i].y) * pitch + cx + u + off[i].x)), dm);
+        num = __dadd_rn(num, __dmul_rn(rd, dd));
+        dn = __dadd_rn(dn, __dmul_rn(dd, dd));
     }
+    if (dn <= kEps) return -INFINITY;
+    return __ddiv_rn(num, __dsqrt_rn(__dmul_rn(rn, dn)));
+}
+
+// FP32 score of the same position.  The mean is refined by the sum of the centred values
+// (first-order correction of its rounding); `rescore` marks a nearly flat deformed subset
+// (norm below 1e-3 of the mean square), where the FP32 score is not trusted.
+__device__ float zncc32(const float* __restrict__ def, int pitch, const short2* off, const float* r32, int n, float rm,
+                        float rn, float sr, int cx, int cy, int u, int v, bool& rescore) {
+    rescore = false;
+    if (n == 0) return -INFINITY;
+    const float* base = def + static_cast<size_t>(cy + v) * pitch + cx + u;
+    float dm = 0.0f;
+    for (int i = 0; i < n; ++i) dm += __ldg(base + off[i].y * pitch + off[i].x);
+    const float inv_n = 1.0f / static_cast<float>(n);
+    dm *= inv_n;
+    float num = 0.0f, dn = 0.0f, s1 = 0.0f, q2 = 0.0f;
+    for (int i = 0; i < n; ++i) {
+        const float d = __ldg(base + off[i].y * pitch + off[i].x);
+        const float dd = d - dm;
+        num = fmaf(r32[i] - rm, dd, num);
+        dn = fmaf(dd, dd, dn);
+        s1 += dd;
+        q2 = fmaf(d, d, q2);
+    }
+    const float c = s1 * inv_n;
+    num = fmaf(-c, sr, num);
+    dn = fmaf(-c, s1, dn);
+    if (!(dn > 1e-3f * q2 * inv_n)) { rescore = true; return -INFINITY; }
+    return num * rsqrtf(rn * dn);
+}
+
+__device__ float block_max(float z, float* sf) {
+    for (int o = 16; o > 0; o >>= 1) z = fmaxf(z, __shfl_xor_sync(0xffffffffu, z, o));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __syncthreads();
+    if (lane == 0) sf[warp] = z;
+    __syncthreads();
+    const int nw = blockDim.x >> 5;
+    float m = -INFINITY;
+    for (int i = 0; i < nw; ++i) m = fmaxf(m, sf[i]);
+    return m;
 }
 
 __device__ void block_argmax(double& z, int& idx, double* sz, int* si) {
@@ -100,37 +168,123 @@ __device__ void block_argmax(double& z, int& idx, double* sz, int* si) {
     __syncthreads();
 }
 
-// Coarse search: grid.y = candidate, grid.x tiles the coarse positions.
-__global__ void coarse_kernel(const float* __restrict__ ref, const float* __restrict__ def, int w, int h, int pitch,
-                              const CandGeom* __restrict__ geo, const short2* __restrict__ coff, int cn, int cstep,
-                              Best* __restrict__ partial, int tiles) {
+// Shared memory of the search kernels: FP64 samples, FP32 samples, statistics, reduction
+// scratch, offsets.
+struct SearchSmem {
+    RefSet rs;
+    double* sz;
+    int* si;
+    float* sf;
+    short2* off;
+    __device__ SearchSmem(unsigned char* smem, int n) {
+        rs.r64 = reinterpret_cast<double*>(smem);
+        rs.stats = rs.r64 + n;
+        sz = rs.stats + 2;
+        rs.r32 = reinterpret_cast<float*>(sz + 32);
+        rs.fstats = rs.r32 + n;
+        sf = rs.fstats + 4;
+        si = reinterpret_cast<int*>(sf + 32);
+        off = reinterpret_cast<short2*>(si + 32);
+    }
+};
+
+size_t search_smem_bytes(size_t n) {
+    return sizeof(double) * (n + 2 + 32) + sizeof(float) * (n + 4 + 32) + sizeof(int) * 32 + sizeof(short2) * n + 16;
+}
+
+// Coarse search (search_ncorr_multigrid's first stage, :208-247): grid.y = candidate, grid.x
+// tiles the positions.  Pass 1: the FP32 maximum of each tile.
+__global__ void coarse_max_kernel(const float* __restrict__ ref, const float* __restrict__ def, int pitch,
+                                  const CandGeom* __restrict__ geo, const short2* __restrict__ coff, int cn, int cstep,
+                                  float* __restrict__ tile_max, int tiles) {
     extern __shared__ __align__(16) unsigned char smem[];
-    double* rv = reinterpret_cast<double*>(smem);
-    double* stats = rv + cn;
-    double* sz = stats + 2;
-    int* si = reinterpret_cast<int*>(sz + 32);
-    short2* off = reinterpret_cast<short2*>(si + 32);
+    SearchSmem sm(smem, cn);
     const CandGeom g = geo[blockIdx.y];
     if (!g.inside) {  // uniform per block: no reference read outside the image
+        if (threadIdx.x == 0) tile_max[blockIdx.y * tiles + blockIdx.x] = -INFINITY;
+        return;
+    }
+    for (int i = threadIdx.x; i < cn; i += blockDim.x) sm.off[i] = coff[i];
+    __syncthreads();
+    load_ref(ref, pitch, sm.off, cn, g.cx, g.cy, sm.rs);
+    const int nu = g.max_u >= g.min_u ? (g.max_u - g.min_u) / cstep + 1 : 0;
+    const int nv = g.max_v >= g.min_v ? (g.max_v - g.min_v) / cstep + 1 : 0;
+    const float rm = sm.rs.fstats[0], rn = sm.rs.fstats[1], sr = sm.rs.fstats[2];
+    float best = -INFINITY;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nu * nv; t += tiles * blockDim.x) {
+        const int vi = t / nu, ui = t - vi * nu;
+        bool flat;
+        const float z = zncc32(def, pitch, sm.off, sm.rs.r32, cn, rm, rn, sr, g.cx, g.cy, g.min_u + ui * cstep,
+                               g.min_v + vi * cstep, flat);
+        best = fmaxf(best, z);
+    }
+    best = block_max(best, sm.sf);
+    if (threadIdx.x == 0) tile_max[blockIdx.y * tiles + blockIdx.x] = best;
+}
+
+// Pass 2: rescore the positions near the candidate's FP32 maximum in FP64; the first of the
+// best in scan order per tile.
+__global__ void coarse_pick_kernel(const float* __restrict__ ref, const float* __restrict__ def, int pitch,
+                                   const CandGeom* __restrict__ geo, const short2* __restrict__ coff, int cn, int cstep,
+                                   const float* __restrict__ tile_max, Best* __restrict__ partial, int tiles) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    SearchSmem sm(smem, cn);
+    const CandGeom g = geo[blockIdx.y];
+    if (!g.inside) {
         if (threadIdx.x == 0) partial[blockIdx.y * tiles + blockIdx.x] = Best{-INFINITY, 0x7fffffff};
         return;
     }
-    for (int i = threadIdx.x; i < cn; i += blockDim.x) off[i] = coff[i];
+    for (int i = threadIdx.x; i < cn; i += blockDim.x) sm.off[i] = coff[i];
     __syncthreads();
-    load_ref(ref, pitch, off, cn, g.cx, g.cy, rv, stats);
+    load_ref(ref, pitch, sm.off, cn, g.cx, g.cy, sm.rs);
+    float m32 = -INFINITY;
+    for (int b = 0; b < tiles; ++b) m32 = fmaxf(m32, __ldg(tile_max + blockIdx.y * tiles + b));
+    const float thr = m32 - kScoreMargin;
     const int nu = g.max_u >= g.min_u ? (g.max_u - g.min_u) / cstep + 1 : 0;
     const int nv = g.max_v >= g.min_v ? (g.max_v - g.min_v) / cstep + 1 : 0;
-    const int total = nu * nv;
+    const float rm = sm.rs.fstats[0], rn = sm.rs.fstats[1], sr = sm.rs.fstats[2];
     double bz = -INFINITY;
     int bi = 0x7fffffff;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += tiles * blockDim.x) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nu * nv; t += tiles * blockDim.x) {
         const int vi = t / nu, ui = t - vi * nu;
         const int u = g.min_u + ui * cstep, v = g.min_v + vi * cstep;
-        const double z = zncc_at(def, w, h, pitch, off, rv, cn, stats[0], stats[1], g.cx, g.cy, u, v);
+        bool flat;
+        const float z32 = zncc32(def, pitch, sm.off, sm.rs.r32, cn, rm, rn, sr, g.cx, g.cy, u, v, flat);
+        if (!(flat || z32 >= thr)) continue;
+        const double z = zncc64(def, pitch, sm.off, sm.rs.r64, cn, sm.rs.stats[0], sm.rs.stats[1], g.cx, g.cy, u, v);
         if (better(z, t, bz, bi)) { bz = z; bi = t; }
     }
-    block_argmax(bz, bi, sz, si);
+    block_argmax(bz, bi, sm.sz, sm.si);
     if (threadIdx.x == 0) partial[blockIdx.y * tiles + blockIdx.x] = Best{bz, bi};
+}
+
+// Exact block-wide argmax of circular_subset_zncc over the positions (u0 + t % nu, v0 + t / nu)
+// whose subset lies inside the image, t in scan order: FP32 maximum, then FP64 rescoring near it.
+__device__ void window_argmax(const float* __restrict__ def, int w, int h, int pitch, int r, const CandGeom& g,
+                              const SearchSmem& sm, int n, int u0, int v0, int nu, int nv, double& bz, int& bi) {
+    const float rm = sm.rs.fstats[0], rn = sm.rs.fstats[1], sr = sm.rs.fstats[2];
+    float best = -INFINITY;
+    for (int t = threadIdx.x; t < nu * nv; t += blockDim.x) {
+        const int u = u0 + t % nu, v = v0 + t / nu;
+        const int x = g.cx + u, y = g.cy + v;
+        if (!(x - r >= 0 && y - r >= 0 && x + r < w && y + r < h)) continue;
+        bool flat;
+        best = fmaxf(best, zncc32(def, pitch, sm.off, sm.rs.r32, n, rm, rn, sr, g.cx, g.cy, u, v, flat));
+    }
+    const float thr = block_max(best, sm.sf) - kScoreMargin;
+    bz = -INFINITY;
+    bi = 0x7fffffff;
+    for (int t = threadIdx.x; t < nu * nv; t += blockDim.x) {
+        const int u = u0 + t % nu, v = v0 + t / nu;
+        const int x = g.cx + u, y = g.cy + v;
+        if (!(x - r >= 0 && y - r >= 0 && x + r < w && y + r < h)) continue;
+        bool flat;
+        const float z32 = zncc32(def, pitch, sm.off, sm.rs.r32, n, rm, rn, sr, g.cx, g.cy, u, v, flat);
+        if (!(flat || z32 >= thr)) continue;
+        const double z = zncc64(def, pitch, sm.off, sm.rs.r64, n, sm.rs.stats[0], sm.rs.stats[1], g.cx, g.cy, u, v);
+        if (better(z, t, bz, bi)) { bz = z; bi = t; }
+    }
+    block_argmax(bz, bi, sm.sz, sm.si);
 }
 
 // Full-sample refinement around the coarse optimum and the local +-search window, then the
@@ -140,11 +294,7 @@ __global__ void fine_kernel(const float* __restrict__ ref, const float* __restri
                             const Best* __restrict__ partial, int tiles, int cstep, int rr, int search, int coarse_ok_all,
                             const int* __restrict__ coarse_ok, SearchResult* __restrict__ out) {
     extern __shared__ __align__(16) unsigned char smem[];
-    double* rv = reinterpret_cast<double*>(smem);
-    double* stats = rv + fn;
-    double* sz = stats + 2;
-    int* si = reinterpret_cast<int*>(sz + 32);
-    short2* off = reinterpret_cast<short2*>(si + 32);
+    SearchSmem sm(smem, fn);
     __shared__ double s_cz;
     __shared__ int s_cu, s_cv;
     const CandGeom g = geo[blockIdx.x];
@@ -152,10 +302,10 @@ __global__ void fine_kernel(const float* __restrict__ ref, const float* __restri
         if (threadIdx.x == 0) out[blockIdx.x] = SearchResult{0, 0, -INFINITY, 0};
         return;
     }
-    for (int i = threadIdx.x; i < fn; i += blockDim.x) off[i] = foff[i];
+    for (int i = threadIdx.x; i < fn; i += blockDim.x) sm.off[i] = foff[i];
     __syncthreads();
-    load_ref(ref, pitch, off, fn, g.cx, g.cy, rv, stats);
-    const bool full_ok = !(fn == 0 || stats[1] <= kEps);
+    load_ref(ref, pitch, sm.off, fn, g.cx, g.cy, sm.rs);
+    const bool full_ok = !(fn == 0 || sm.rs.stats[1] <= kEps);
     // coarse winner
     if (threadIdx.x == 0) {
         double z = -INFINITY;
@@ -184,16 +334,9 @@ __global__ void fine_kernel(const float* __restrict__ ref, const float* __restri
         const int u0 = max(g.min_u, s_cu - rr), u1 = min(g.max_u, s_cu + rr);
         const int v0 = max(g.min_v, s_cv - rr), v1 = min(g.max_v, s_cv + rr);
         const int nu = u1 - u0 + 1, nv = v1 - v0 + 1;
-        double bz = -INFINITY;
-        int bi = 0x7fffffff;
-        for (int t = threadIdx.x; t < nu * nv; t += blockDim.x) {
-            const int u = u0 + t % nu, v = v0 + t / nu;
-            const int x = g.cx + u, y = g.cy + v;
-            if (!(x - r >= 0 && y - r >= 0 && x + r < w && y + r < h)) continue;
-            const double z = zncc_at(def, w, h, pitch, off, rv, fn, stats[0], stats[1], g.cx, g.cy, u, v);
-            if (better(z, t, bz, bi)) { bz = z; bi = t; }
-        }
-        block_argmax(bz, bi, sz, si);
+        double bz;
+        int bi;
+        window_argmax(def, w, h, pitch, r, g, sm, fn, u0, v0, nu, nv, bz, bi);
         if (threadIdx.x == 0) {
             s_cz = bz;
             if (bi != 0x7fffffff) { s_cu = u0 + bi % nu; s_cv = v0 + bi / nu; } else { s_cu = 0; s_cv = 0; }
@@ -209,16 +352,9 @@ __global__ void fine_kernel(const float* __restrict__ ref, const float* __restri
     __syncthreads();
     if (search > 0 && full_ok) {
         const int n1 = 2 * search + 1;
-        double bz = -INFINITY;
-        int bi = 0x7fffffff;
-        for (int t = threadIdx.x; t < n1 * n1; t += blockDim.x) {
-            const int u = -search + t % n1, v = -search + t / n1;
-            const int x = g.cx + u, y = g.cy + v;
-            if (!(x - r >= 0 && y - r >= 0 && x + r < w && y + r < h)) continue;
-            const double z = zncc_at(def, w, h, pitch, off, rv, fn, stats[0], stats[1], g.cx, g.cy, u, v);
-            if (better(z, t, bz, bi)) { bz = z; bi = t; }
-        }
-        block_argmax(bz, bi, sz, si);
+        double bz;
+        int bi;
+        window_argmax(def, w, h, pitch, r, g, sm, fn, -search, -search, n1, n1, bz, bi);
         if (threadIdx.x == 0) {
             const int lu = bi != 0x7fffffff ? -search + bi % n1 : 0;
             const int lv = bi != 0x7fffffff ? -search + bi / n1 : 0;
@@ -306,29 +442,35 @@ void integer_search_batch(tdic_ctx* ctx, tdic_pair* lazy, const tdic_config& cfg
         ok[i] = (cx[i] - r >= 0 && cy[i] - r >= 0 && cx[i] + r < w && cy[i] + r < h) ? 1 : 0;
         geo[i].inside = ok[i];
     }
-    // A flat coarse subset (coarse_ref_norm <= eps) yields -inf in coarse_kernel, the reference's
-    // outcome of skipping the multigrid stage (integer_search.cpp:381-397).
+    // A flat coarse subset (coarse_ref_norm <= eps) scores -inf everywhere in the coarse search,
+    // the reference's outcome of skipping the multigrid stage (integer_search.cpp:381-397).
     const std::vector<int>& cok = ok;
     Buffer d_geo(&ctx->pool, sizeof(CandGeom) * n), d_coff(&ctx->pool, sizeof(short2) * coff.size()),
         d_foff(&ctx->pool, sizeof(short2) * foff.size()), d_cok(&ctx->pool, sizeof(int) * n),
         d_out(&ctx->pool, sizeof(SearchResult) * n);
     const int tiles = 64;
     Buffer d_part(&ctx->pool, sizeof(Best) * static_cast<size_t>(tiles) * n);
+    Buffer d_tmax(&ctx->pool, sizeof(float) * static_cast<size_t>(tiles) * n);
     TDIC_CUDA_TRY(cudaMemcpyAsync(d_geo.ptr, geo.data(), sizeof(CandGeom) * n, cudaMemcpyHostToDevice, s));
     TDIC_CUDA_TRY(cudaMemcpyAsync(d_coff.ptr, coff.data(), sizeof(short2) * coff.size(), cudaMemcpyHostToDevice, s));
     TDIC_CUDA_TRY(cudaMemcpyAsync(d_foff.ptr, foff.data(), sizeof(short2) * foff.size(), cudaMemcpyHostToDevice, s));
     TDIC_CUDA_TRY(cudaMemcpyAsync(d_cok.ptr, cok.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
-    const size_t csm = sizeof(double) * (coff.size() + 2 + 32) + sizeof(int) * 32 + sizeof(short2) * coff.size() + 16;
-    const size_t fsm = sizeof(double) * (foff.size() + 2 + 32) + sizeof(int) * 32 + sizeof(short2) * foff.size() + 16;
-    TDIC_CUDA_TRY(cudaFuncSetAttribute(coarse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(csm)));
+    const size_t csm = search_smem_bytes(coff.size()), fsm = search_smem_bytes(foff.size());
+    TDIC_CUDA_TRY(cudaFuncSetAttribute(coarse_max_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(csm)));
+    TDIC_CUDA_TRY(cudaFuncSetAttribute(coarse_pick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(csm)));
     TDIC_CUDA_TRY(cudaFuncSetAttribute(fine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(fsm)));
-    coarse_kernel<<<dim3(tiles, n), 256, csm, s>>>(lazy->ref.as<float>(), lazy->def_f.as<float>(), w, h, lazy->rpitch,
-                                                   d_geo.as<CandGeom>(), d_coff.as<short2>(), static_cast<int>(coff.size()),
-                                                   cstep, d_part.as<Best>(), tiles);
+    const float* dref = lazy->ref.as<float>();
+    const float* ddef = lazy->def_f.as<float>();
+    coarse_max_kernel<<<dim3(tiles, n), 256, csm, s>>>(dref, ddef, lazy->rpitch, d_geo.as<CandGeom>(), d_coff.as<short2>(),
+                                                       static_cast<int>(coff.size()), cstep, d_tmax.as<float>(), tiles);
     TDIC_CUDA_TRY(cudaGetLastError());
-    fine_kernel<<<n, 256, fsm, s>>>(lazy->ref.as<float>(), lazy->def_f.as<float>(), w, h, lazy->rpitch, r, d_geo.as<CandGeom>(),
-                                    d_foff.as<short2>(), static_cast<int>(foff.size()), d_part.as<Best>(), tiles, cstep, rr,
-                                    search, 1, d_cok.as<int>(), d_out.as<SearchResult>());
+    coarse_pick_kernel<<<dim3(tiles, n), 256, csm, s>>>(dref, ddef, lazy->rpitch, d_geo.as<CandGeom>(), d_coff.as<short2>(),
+                                                        static_cast<int>(coff.size()), cstep, d_tmax.as<float>(),
+                                                        d_part.as<Best>(), tiles);
+    TDIC_CUDA_TRY(cudaGetLastError());
+    fine_kernel<<<n, 256, fsm, s>>>(dref, ddef, w, h, lazy->rpitch, r, d_geo.as<CandGeom>(), d_foff.as<short2>(),
+                                    static_cast<int>(foff.size()), d_part.as<Best>(), tiles, cstep, rr, search, 1,
+                                    d_cok.as<int>(), d_out.as<SearchResult>());
     TDIC_CUDA_TRY(cudaGetLastError());
     TDIC_CUDA_TRY(cudaMemcpyAsync(out_host, d_out.ptr, sizeof(SearchResult) * n, cudaMemcpyDeviceToHost, s));
     TDIC_CUDA_TRY(cudaStreamSynchronize(s));
