@@ -46,6 +46,9 @@ WORKLOAD = {
 }
 
 
+PROPAGATE_DRAM_BYTES = 36_848_896 + 500_992  # ncu, propagate_kernel, 2048^2 r=15, one launch
+
+
 def workload_desc(side: int) -> dict:
     """WORKLOAD for a side x side case of the same generator (2048 = the benchmark itself)."""
     if side == 2048:
@@ -317,7 +320,11 @@ def run_ours(args, world, rank, local, pg):
                 "frac": flops / t_prop / 1e12 / fp32_peak,
                 "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, TF32 off (MEASURED_PEAKS.json holds "
                                "HBM and bf16 only)",
-                "algorithmic_flops_per_launch": flops, "traffic": None,
+                "algorithmic_flops_per_launch": flops,
+                # DRAM bytes (read + write) of one launch on this workload, from one ncu capture
+                # (dram__bytes_read.sum + dram__bytes_write.sum after the L2 flush); recorded for
+                # the benchmark workload only
+                "traffic": PROPAGATE_DRAM_BYTES if args.side == 2048 else None,
                 "hbm_peak_gbs": peaks.get("hbm_gbs")}
 
     # FP64 GPU path on the same configuration, for the precision comparison.
