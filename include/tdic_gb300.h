@@ -208,6 +208,37 @@ tdic_status tdic_propagate_noalloc(tdic_ctx* ctx, tdic_pair* pair, const tdic_co
                                    const tdic_grid_out* out_device, int32_t* points_computed,
                                    void* stream);
 
+/* Batched propagation: several image pairs in one persistent launch over a shared work queue
+ * (no counterpart in the reference, which propagates one pair per SubsetDIC::compute call).
+ * Job j propagates pairs[j] from seeds[j] with cfgs[j] exactly as tdic_propagate does in the
+ * dataflow order (same results); subset radius, spacing, iterations, thresholds and ROI
+ * (rois[j]: host H x W mask or NULL; rois may be NULL) may differ between jobs, the spline
+ * degree, precision and optimizer may not; propagation_mode must be 2.  At most 512 jobs and
+ * 2^22 grid points per job.  The batch owns device outputs (tdic_batch_outputs) and scratch;
+ * its pairs must outlive it.
+ *   tdic_batch_tune    times each launch configuration (warps per POI, groups per block) on
+ *                      this batch and keeps the fastest; optional.
+ *   tdic_batch_launch  enqueues one propagation of every job on `stream` and returns without
+ *                      waiting: device memsets and kernel launches only, so it can be captured
+ *                      in a CUDA graph and replayed.
+ *   tdic_batch_finish  waits for `stream` and reports points_computed[j] (0: the seed of job j
+ *                      could not be placed, its grid holds the defaults). */
+typedef struct tdic_batch tdic_batch;
+tdic_status tdic_batch_create(tdic_ctx* ctx, int32_t n, tdic_pair* const* pairs,
+                              const tdic_config* cfgs, const tdic_seed* seeds,
+                              const uint8_t* const* rois, void* stream, tdic_batch** out);
+tdic_status tdic_batch_tune(tdic_batch* batch, void* stream);
+tdic_status tdic_batch_launch(tdic_batch* batch, void* stream);
+tdic_status tdic_batch_finish(tdic_batch* batch, void* stream, int32_t* points_computed);
+/* Device arrays (grid_w*grid_h entries each) of job j's results; valid until the batch is
+ * destroyed, rewritten by every launch. */
+tdic_status tdic_batch_outputs(tdic_batch* batch, int32_t job, tdic_grid_out* device_arrays);
+/* Copy job j's grid into host arrays (NULL entries skipped); waits for `stream`. */
+tdic_status tdic_batch_results(tdic_batch* batch, int32_t job, const tdic_grid_out* host_arrays, void* stream);
+/* The launch configuration in use: warps per POI and solver groups per thread block. */
+tdic_status tdic_batch_config(tdic_batch* batch, int32_t* warps_per_poi, int32_t* groups_per_block);
+void tdic_batch_destroy(tdic_batch* batch);
+
 /* Seed selection: SeedSelector::select_best_seed (seed_selector.cpp:146-205) with k-means
  * candidates (:207-317), integer search (integer_search.cpp:333-432, kernel K5) and subpixel
  * ICGN refinement on the non-prefiltered spline (subset_initializer.cpp:152-204).  `lazy` is

@@ -81,6 +81,15 @@ SIGNATURES = {
                                  C.POINTER(GridOut), C.c_int, C.POINTER(C.c_int32), C.c_void_p]),
     "tdic_propagate_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Config), C.POINTER(Seed), C.c_void_p,
                                          C.POINTER(GridOut), C.POINTER(C.c_int32), C.c_void_p]),
+    "tdic_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.POINTER(C.c_void_p)]),
+    "tdic_batch_tune": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "tdic_batch_launch": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "tdic_batch_finish": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "tdic_batch_outputs": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(GridOut)]),
+    "tdic_batch_results": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(GridOut), C.c_void_p]),
+    "tdic_batch_config": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "tdic_batch_destroy": (None, [C.c_void_p]),
     "tdic_select_seed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Config),
                                    C.POINTER(Seed), C.c_void_p]),
     "tdic_subset_compute": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int, C.c_void_p,

@@ -1023,3 +1023,184 @@ tdic_status tdic_propagate_noalloc(tdic_ctx* ctx, tdic_pair* pair, const tdic_co
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Batched propagation: several image pairs (each with its own radius, spacing, threshold, ROI
+// and seed) in one persistent launch over a shared work queue.
+// ---------------------------------------------------------------------------------------
+struct tdic_batch {
+    tdic_ctx* ctx = nullptr;
+    int n = 0;
+    std::unique_ptr<tdic::BatchPlanBase> plan;
+    int config = 0;
+};
+
+namespace {
+
+void batch_create_impl(tdic_ctx* ctx, int n, tdic_pair* const* pairs, const tdic_config* cfgs, const tdic_seed* seeds,
+                       const uint8_t* const* rois, cudaStream_t s, tdic_batch** out) {
+    TDIC_REQUIRE(n >= 1 && n <= kMaxBatchJobs, TDIC_INVALID_ARG, "batch: 1 to 512 image pairs");
+    const tdic_pair* p0 = pairs[0];
+    TDIC_REQUIRE(p0 != nullptr, TDIC_INVALID_ARG, "batch: null pair");
+    std::vector<BatchSeed> bs(n);
+    std::vector<std::vector<uint8_t>> roi_copy(n);
+    for (int j = 0; j < n; ++j) {
+        const tdic_pair* p = pairs[j];
+        const tdic_config& c = cfgs[j];
+        TDIC_REQUIRE(p != nullptr, TDIC_INVALID_ARG, "batch: null pair");
+        check_config(c);
+        TDIC_REQUIRE(p->ctx == ctx, TDIC_INVALID_ARG, "batch: every pair must belong to the context");
+        TDIC_REQUIRE(p->exact == 1, TDIC_INVALID_ARG, "batch: propagation needs pairs with the exact prefilter");
+        TDIC_REQUIRE(p->degree == p0->degree && p->precision == p0->precision, TDIC_INVALID_ARG,
+                     "batch: every pair must have the same spline degree and precision");
+        TDIC_REQUIRE(c.optimizer == cfgs[0].optimizer, TDIC_INVALID_ARG, "batch: every job must use the same optimizer");
+        TDIC_REQUIRE(c.propagation_mode == 2, TDIC_UNSUPPORTED, "batch: only the dataflow order (propagation_mode 2)");
+        // seed alignment (reliability_propagation.cpp:201-216), as tdic_propagate
+        const uint8_t* roi = rois ? rois[j] : nullptr;
+        const int w = p->w, h = p->h, step = std::max(0, c.propagation_spacing) + 1;
+        int32_t gw, gh;
+        tdic_grid_dims(w, h, c.propagation_spacing, &gw, &gh);
+        const tdic_seed& sd = seeds[j];
+        const int sxr = static_cast<int>(std::round(sd.x)), syr = static_cast<int>(std::round(sd.y));
+        BatchSeed& b = bs[j];
+        b.ok = sd.found != 0 && roi_ok(roi, w, h, sxr, syr);
+        if (b.ok) {
+            b.gx = nearest_grid_index(sxr, step, gw);
+            b.gy = nearest_grid_index(syr, step, gh);
+            b.ok = roi_ok(roi, w, h, b.gx * step, b.gy * step);
+        }
+        if (b.ok) {
+            b.idx = b.gy * gw + b.gx;
+            b.solve = (b.gx * step != sxr || b.gy * step != syr) ? 1 : 0;
+        } else {
+            b.idx = -1; b.gx = 0; b.gy = 0; b.solve = 0;
+        }
+        for (int k = 0; k < 6; ++k) b.p[k] = sd.p[k];
+        b.corr = sd.correlation;
+        if (roi) roi_copy[j].assign(roi, roi + static_cast<size_t>(w) * h);
+    }
+    auto b = std::make_unique<tdic_batch>();
+    b->ctx = ctx;
+    b->n = n;
+    b->plan = batch_build(ctx, n, pairs, cfgs, bs.data(), roi_copy, s);
+    ++ctx->live_pairs;  // the batch holds buffers of the context's pool
+    *out = b.release();
+}
+
+}  // namespace
+
+extern "C" {
+
+tdic_status tdic_batch_create(tdic_ctx* ctx, int32_t n, tdic_pair* const* pairs, const tdic_config* cfgs,
+                              const tdic_seed* seeds, const uint8_t* const* rois, void* stream, tdic_batch** out) {
+    return guarded(ctx, [&] {
+        TDIC_REQUIRE(pairs && cfgs && seeds && out, TDIC_INVALID_ARG, "null argument");
+        *out = nullptr;
+        TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
+        batch_create_impl(ctx, n, pairs, cfgs, seeds, rois, pick(ctx, stream), out);
+    });
+}
+
+tdic_status tdic_batch_tune(tdic_batch* b, void* stream) {
+    if (!b) return TDIC_INVALID_ARG;
+    return guarded(b->ctx, [&] {
+        TDIC_CUDA_TRY(cudaSetDevice(b->ctx->device));
+        cudaStream_t s = pick(b->ctx, stream);
+        const int nc = batch_config_count(b->plan.get());
+        cudaEvent_t e0, e1;
+        TDIC_CUDA_TRY(cudaEventCreate(&e0));
+        TDIC_CUDA_TRY(cudaEventCreate(&e1));
+        float best = 0.0f;
+        int best_c = 0;
+        try {
+            for (int c = 0; c < nc; ++c) {
+                batch_launch(b->plan.get(), c, s);  // warm-up of this configuration
+                TDIC_CUDA_TRY(cudaEventRecord(e0, s));
+                batch_launch(b->plan.get(), c, s);
+                TDIC_CUDA_TRY(cudaEventRecord(e1, s));
+                TDIC_CUDA_TRY(cudaEventSynchronize(e1));
+                float ms = 0.0f;
+                TDIC_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+                if (c == 0 || ms < best) { best = ms; best_c = c; }
+            }
+        } catch (...) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            throw;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        check_device_error(b->ctx, s);
+        b->config = best_c;
+    });
+}
+
+tdic_status tdic_batch_launch(tdic_batch* b, void* stream) {
+    if (!b) return TDIC_INVALID_ARG;
+    return guarded(b->ctx, [&] { batch_launch(b->plan.get(), b->config, pick(b->ctx, stream)); });
+}
+
+tdic_status tdic_batch_finish(tdic_batch* b, void* stream, int32_t* points_computed) {
+    if (!b) return TDIC_INVALID_ARG;
+    return guarded(b->ctx, [&] {
+        TDIC_REQUIRE(points_computed, TDIC_INVALID_ARG, "null argument");
+        cudaStream_t s = pick(b->ctx, stream);
+        int err = 0;
+        batch_finish(b->plan.get(), points_computed, &err, s);
+        check_device_error(b->ctx, s);
+        TDIC_REQUIRE(err == 0, TDIC_TIMEOUT, "batch propagation: a bounded in-kernel wait timed out");
+    });
+}
+
+tdic_status tdic_batch_outputs(tdic_batch* b, int32_t job, tdic_grid_out* device_arrays) {
+    if (!b) return TDIC_INVALID_ARG;
+    return guarded(b->ctx, [&] {
+        TDIC_REQUIRE(device_arrays && job >= 0 && job < b->n, TDIC_INVALID_ARG, "batch: job out of range");
+        *device_arrays = batch_outputs(b->plan.get(), job);
+    });
+}
+
+tdic_status tdic_batch_results(tdic_batch* b, int32_t job, const tdic_grid_out* host_arrays, void* stream) {
+    if (!b) return TDIC_INVALID_ARG;
+    return guarded(b->ctx, [&] {
+        TDIC_REQUIRE(host_arrays && job >= 0 && job < b->n, TDIC_INVALID_ARG, "batch: job out of range");
+        cudaStream_t s = pick(b->ctx, stream);
+        GridBuffers g;
+        g.dev = batch_outputs(b->plan.get(), job);
+        int32_t gw = 0, gh = 0;
+        batch_grid(b->plan.get(), job, &gw, &gh);
+        copy_grid_back(g, host_arrays, gw * gh, s);
+        TDIC_CUDA_TRY(cudaStreamSynchronize(s));
+    });
+}
+
+tdic_status tdic_batch_config(tdic_batch* b, int32_t* warps_per_poi, int32_t* groups_per_block) {
+    if (!b) return TDIC_INVALID_ARG;
+    return guarded(b->ctx, [&] {
+        TDIC_REQUIRE(warps_per_poi && groups_per_block, TDIC_INVALID_ARG, "null argument");
+        int g = 0, k = 0;
+        batch_config_info(b->plan.get(), b->config, &g, &k);
+        *warps_per_poi = g;
+        *groups_per_block = k;
+    });
+}
+
+void tdic_batch_destroy(tdic_batch* b) {
+    if (!b) return;
+    tdic_ctx* ctx = b->ctx;
+    bool free_ctx = false;
+    {
+        std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+        cudaSetDevice(ctx->device);
+        cudaDeviceSynchronize();  // a launch on any stream may still use the batch's buffers
+        delete b;
+        ctx->live_pairs -= 1;
+        if (ctx->destroy_requested && ctx->live_pairs == 0) {
+            ctx_free(ctx);
+            free_ctx = true;
+        }
+    }
+    if (free_ctx) delete ctx;
+}
+
+}  // extern "C"

@@ -15,6 +15,9 @@
 // add cost but no accuracy.  The FP64 build is the same code with every T = double.
 #include "tdic_internal.cuh"
 
+#include <algorithm>
+#include <type_traits>
+
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -885,24 +888,44 @@ __device__ __forceinline__ void group_bcast3(int& a, int& b, int& c, int* slots,
     }
 }
 
-// Kernel preamble: copy the sample-offset table into shared memory (CTA-wide) and initialise
-// each group's mbarrier.  Returns the shared offset table.
+// Shared-memory shape of a launch: the sample-offset tables it stages (one per subset radius)
+// and the per-group capacities (samples, reference and coefficient windows).  `total` is the
+// number of grid points of all its jobs (the work-queue capacity).
+struct Shape {
+    const short2* tab;
+    int ntab;
+    int nmax, rbx, rby, cbx, cby;
+    int total;
+};
+
+template <typename T>
+__host__ __device__ inline Shape shape_of(const Env<T>& e, int total) {
+    return Shape{e.off, e.n, e.nmax, e.rbx, e.rby, e.cbx, e.cby, total};
+}
+
 template <typename T, int G>
-__device__ short2* kernel_preamble(const Env<T>& e, const CUtensorMap* tm_ref, const CUtensorMap* tm_coef,
+__device__ __forceinline__ GroupSmem<T> group_smem(unsigned char* smem_raw, const Shape& sh, int gi) {
+    return GroupSmem<T>(smem_raw + cta_prefix_bytes(sh.ntab), gi, sh.nmax, G, sh.rbx, sh.rby, sh.cbx, sh.cby);
+}
+
+// Kernel preamble: copy the sample-offset tables into shared memory (CTA-wide) and initialise
+// each group's mbarrier.  Returns the shared tables.
+template <typename T, int G>
+__device__ short2* kernel_preamble(const Shape& sh, int* err, const CUtensorMap* tm_ref, const CUtensorMap* tm_coef,
                                    unsigned char* smem_raw, int gi, int tid, bool group_member = true) {
     // TMA destinations need 128-byte alignment; the layout assumes an aligned dynamic base.
     if ((smem_u32(smem_raw) & 127u) != 0u) {
-        if (threadIdx.x == 0) atomicExch(e.err, 4);
+        if (threadIdx.x == 0) atomicExch(err, 4);
         return nullptr;
     }
     short2* s_off = reinterpret_cast<short2*>(smem_raw);
-    for (int i = threadIdx.x; i < e.n; i += blockDim.x) s_off[i] = e.off[i];
+    for (int i = threadIdx.x; i < sh.ntab; i += blockDim.x) s_off[i] = sh.tab[i];
     if (tid == 0 && group_member) {
-        GroupSmem<T> gs(smem_raw + cta_prefix_bytes(e.nmax), gi, e.nmax, G, e.rbx, e.rby, e.cbx, e.cby);
+        GroupSmem<T> gs = group_smem<T, G>(smem_raw, sh, gi);
         mbar_init(gs.bar, 1);
         fence_proxy_async();
     }
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && tm_ref != nullptr) {
         asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tm_ref)) : "memory");
         asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tm_coef)) : "memory");
     }
@@ -914,15 +937,16 @@ __device__ short2* kernel_preamble(const Env<T>& e, const CUtensorMap* tm_ref, c
 // Batched solve: persistent groups pull POIs from a work counter.
 // ---------------------------------------------------------------------------------------
 template <int OPT, int DEG, typename T, int G>
-__global__ void solve_batch_kernel(Env<T> e, const __grid_constant__ CUtensorMap tm_ref,
+__global__ void solve_batch_kernel(const __grid_constant__ Env<T> e, const __grid_constant__ CUtensorMap tm_ref,
                                    const __grid_constant__ CUtensorMap tm_coef, const tdic_poi_in* __restrict__ in,
                                    tdic_poi_out* __restrict__ out, int n, int* fetch) {
     using M = typename MixedOf<T>::type;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int gi = threadIdx.x / (32 * G), tid = threadIdx.x % (32 * G);
-    short2* s_off = kernel_preamble<T, G>(e, &tm_ref, &tm_coef, smem_raw, gi, tid);
+    const Shape sh = shape_of(e, 0);
+    short2* s_off = kernel_preamble<T, G>(sh, e.err, &tm_ref, &tm_coef, smem_raw, gi, tid);
     if (s_off == nullptr) return;
-    GroupSmem<T> gs(smem_raw + cta_prefix_bytes(e.nmax), gi, e.nmax, G, e.rbx, e.rby, e.cbx, e.cby);
+    GroupSmem<T> gs = group_smem<T, G>(smem_raw, sh, gi);
     int* ints = gs.ints;
     const int bar_id = 1 + gi;
     uint32_t phase = 0;
@@ -957,12 +981,15 @@ struct PropEnv {
     tdic_grid_out out;
     int* claim;
     unsigned long long* key;
+    void* params;   // six parameters per grid point, in the solve's precision
     int* order;
     int* counters;  // [0] wave-list tail, [1] queue head
     unsigned long long* qword;  // queue tail (high 32) : items in flight + 2^31 (low 32)
     int* fetch;     // per wave
     unsigned int* barrier;
-    int* flags;     // [0] error, [1] no seed, [2] accepted count
+    int* flags;     // [1] no seed, [2] accepted count of this job
+    int* err;       // error word of the launch (a bounded wait ran out)
+    int jtag;       // job index << kJobShift in queue items and wave lists (0 for one job)
     // dataflow order (mode 2)
     int mode;
     int sgx, sgy;                 // seed grid coordinates
@@ -973,6 +1000,12 @@ struct PropEnv {
 };
 
 enum { kDfPending = 0, kDfAccepted = 2, kDfRejected = 3, kDfOrphan = 4 };
+
+// A launch over several jobs (image pairs) tags the grid points of its queue items and wave
+// lists with the job: point index in the low kJobShift bits, job above.
+constexpr int kJobShift = 22;
+constexpr int kPointMask = (1 << kJobShift) - 1;
+static_assert(kMaxBatchJobs <= (1 << (31 - kJobShift)), "job index must fit above the point bits");
 
 __device__ __forceinline__ int ld_cg(const int* p) { return __ldcg(p); }
 
@@ -1054,7 +1087,7 @@ __device__ void expand(const PropEnv& pe, int w, int h, int radius, int n, float
             const int old = atomicCAS(pe.claim + m, 0, next + 1);
             if (old == 0) {
                 const int pos = atomicAdd(pe.counters, 1);
-                pe.order[pos] = m;
+                pe.order[pos] = m | pe.jtag;
                 c = next + 1;
             } else {
                 c = old;
@@ -1093,7 +1126,7 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
 }
 constexpr unsigned int kInFlightBias = 0x80000000u;  // in-flight count = low word - bias
 
-// Queue item: parent (high 32, -1 = orphan) : point (low 32).
+// Queue item: parent point (high 32, -1 = orphan) : tagged point (low 32).
 __device__ __forceinline__ unsigned long long df_item(int parent, int c) {
     return (static_cast<unsigned long long>(static_cast<unsigned int>(parent)) << 32) | static_cast<unsigned int>(c);
 }
@@ -1179,9 +1212,9 @@ __device__ void df_resolve(const PropEnv& pe, int n, bool accepted, int self_in_
     int k = 0;
     for (int i = 0; i < nk; ++i) {
         if (kp1[i] == n && accepted) {
-            if (kid[i] != cont) push[k++] = df_item(n, kid[i]);
+            if (kid[i] != cont) push[k++] = df_item(n, kid[i] | pe.jtag);
         } else if (kp2[i] < 0) {
-            push[k++] = df_item(-1, kid[i]);  // its only parent failed: orphan
+            push[k++] = df_item(-1, kid[i] | pe.jtag);  // its only parent failed: orphan
         }
     }
     const int handed = cont >= 0 ? self_in_flight : 0;  // n's in-flight count passes to the continued child
@@ -1198,7 +1231,7 @@ __device__ void df_resolve(const PropEnv& pe, int n, bool accepted, int self_in_
         } else if (atomicAdd(pe.dcnt + kid[i], 1) == 1) {  // the second of two parents to resolve
             fence_acq_rel();
             if (ld_cg(pe.dstate + kp1[i]) != kDfAccepted)
-                push[k2++] = df_item(ld_cg(pe.dstate + kp2[i]) == kDfAccepted ? kp2[i] : -1, kid[i]);
+                push[k2++] = df_item(ld_cg(pe.dstate + kp2[i]) == kDfAccepted ? kp2[i] : -1, kid[i] | pe.jtag);
         }
     }
     df_publish(pe, push, k2, k2 - (self_in_flight - handed));
@@ -1211,6 +1244,7 @@ __device__ void df_resolve(const PropEnv& pe, int n, bool accepted, int self_in_
 constexpr int kPropG = 4;
 constexpr int kPropGroupsPerBlock = 2;
 constexpr int kPropMinBlocks = 2;  // resident CTAs per SM the register budget is sized for
+constexpr int kPropMaxThreads = 32 * kPropG * kPropGroupsPerBlock + 32;  // also 8-warp groups, one per CTA
 
 // Dataflow hand-over between a solver group and the resolver warp of its block (shared memory).
 template <typename P>
@@ -1227,19 +1261,63 @@ struct DfSlot {
 __device__ __forceinline__ int vld(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
 __device__ __forceinline__ void vst(int* p, int v) { *reinterpret_cast<volatile int*>(p) = v; }
 
+// Where a propagation launch finds its jobs.  OneJob: one image pair, everything in kernel
+// parameters.  JobTable: several pairs, per-job environments and tensor maps in device memory,
+// grid points tagged with the job in queue items and wave lists.
+template <typename T>
+struct OneJob {
+    const Env<T>& e;
+    const PropEnv& pe;
+    const CUtensorMap* tr;
+    const CUtensorMap* tc;
+    __device__ int count() const { return 1; }
+    __device__ int job_of(int) const { return 0; }
+    __device__ int point_of(int c) const { return c; }
+    __device__ const Env<T>& env(int) const { return e; }
+    __device__ const PropEnv& prop(int) const { return pe; }
+    __device__ const CUtensorMap* tm_ref(int) const { return tr; }
+    __device__ const CUtensorMap* tm_coef(int) const { return tc; }
+    __device__ int table(int) const { return 0; }
+};
+
+template <typename T>
+struct BatchJob {
+    Env<T> e;
+    PropEnv pe;
+    int table;  // first entry of the job's sample-offset table in the staged tables
+};
+
+template <typename T>
+struct JobTable {
+    const BatchJob<T>* jobs;
+    int n;
+    const CUtensorMap* maps;  // reference and coefficient map of each job
+    __device__ int count() const { return n; }
+    __device__ int job_of(int c) const { return c >> kJobShift; }
+    __device__ int point_of(int c) const { return c & kPointMask; }
+    __device__ Env<T> env(int j) const { return jobs[j].e; }
+    __device__ const PropEnv& prop(int j) const { return jobs[j].pe; }
+    __device__ const CUtensorMap* tm_ref(int j) const { return maps + 2 * j; }
+    __device__ const CUtensorMap* tm_coef(int j) const { return maps + 2 * j + 1; }
+    __device__ int table(int j) const { return jobs[j].table; }
+};
+
 // One lane of the resolver warp serves one solver group: it settles the points the group posts
 // (parameters, state, children, outputs) and fetches queue items when the group asks for one.
 // The group never waits on these global-memory round trips unless its queue runs dry.
-template <typename P>
-__device__ void df_resolver_lane(const PropEnv& pe, DfSlot<P>* slot, P* params, int* s_done) {
-    const int ng = pe.gw * pe.gh;
+template <typename P, typename Src>
+__device__ void df_resolver_lane(const Src& src, DfSlot<P>* slot, int* s_done, int total) {
+    const PropEnv& g = src.prop(0);  // queue, counters and error word are shared by all jobs
     int ticket = -1;
     unsigned long long idle = 0;
     while (true) {
         bool progress = false;
         if (vld(&slot->post) == 1) {
             __threadfence_block();
-            const int n = slot->n, st = slot->state, cont = slot->cont;
+            const int tagged = slot->n, st = slot->state, cont = slot->cont;
+            const PropEnv& pe = src.prop(src.job_of(tagged));
+            const int n = src.point_of(tagged);
+            P* params = reinterpret_cast<P*>(pe.params);
             Result<P> R;
             for (int k = 0; k < 6; ++k) R.p[k] = slot->p[k];
             R.corr = slot->corr;
@@ -1264,19 +1342,19 @@ __device__ void df_resolver_lane(const PropEnv& pe, DfSlot<P>* slot, P* params, 
             int deliver = 0;
             if (vld(s_done)) {
                 deliver = 2;
-            } else if (*reinterpret_cast<volatile int*>(pe.flags) != 0) {
+            } else if (*reinterpret_cast<volatile int*>(g.err) != 0) {
                 deliver = 3;
             } else {
-                // At most gw*gh - 1 points are ever queued (each once, never the seed), so a
+                // At most `total` - 1 points are ever queued (each once, never a seed), so a
                 // ticket beyond the array can only end by completion; it reads nothing.
-                if (ticket < 0) ticket = atomicAdd(pe.counters + 1, 1);
-                const unsigned long long it = ticket < ng ? ld_acquire_u64(pe.dq + ticket) : ~0ull;
+                if (ticket < 0) ticket = atomicAdd(g.counters + 1, 1);
+                const unsigned long long it = ticket < total ? ld_acquire_u64(g.dq + ticket) : ~0ull;
                 if (it != ~0ull) {  // acquire: the parent's parameters were released before it
                     slot->c = static_cast<int>(it & 0xffffffffull);
                     slot->par = static_cast<int>(it >> 32);
                     ticket = -1;
                     deliver = 1;
-                } else if (static_cast<unsigned int>(__ldcg(pe.qword) & 0xffffffffull) == kInFlightBias) {
+                } else if (static_cast<unsigned int>(__ldcg(g.qword) & 0xffffffffull) == kInFlightBias) {
                     vst(s_done, 1);  // nothing queued or running anywhere
                     deliver = 2;
                 }
@@ -1293,7 +1371,7 @@ __device__ void df_resolver_lane(const PropEnv& pe, DfSlot<P>* slot, P* params, 
             idle = 0;
         } else {
             if (++idle > kSpinLimit) {
-                atomicExch(pe.flags, 1);
+                atomicExch(g.err, 1);
                 vst(&slot->ready, 3);
                 return;
             }
@@ -1302,30 +1380,44 @@ __device__ void df_resolver_lane(const PropEnv& pe, DfSlot<P>* slot, P* params, 
     }
 }
 
-// The propagation.  Blocks hold `gpb` solver groups of G warps; in the dataflow order one more
-// warp per block is the resolver.  Launched cooperatively (co-resident blocks, own grid barrier).
-template <int OPT, int DEG, typename T, int G>
-__global__ void __launch_bounds__(32 * G * kPropGroupsPerBlock + 32, sizeof(T) == 4 ? kPropMinBlocks : 1)
-    propagate_kernel(Env<T> e, const __grid_constant__ CUtensorMap tm_ref, const __grid_constant__ CUtensorMap tm_coef,
-                     PropEnv pe) {
+// Guess extrapolation from an accepted neighbour (reliability_propagation.cpp:326-329).
+template <typename P>
+__device__ __forceinline__ void extrapolate(const P (&pp)[6], P ddx, P ddy, P (&p0)[6]) {
+    p0[0] = pp[0] + pp[2] * ddx + pp[3] * ddy;
+    p0[1] = pp[1] + pp[4] * ddx + pp[5] * ddy;
+    p0[2] = pp[2]; p0[3] = pp[3]; p0[4] = pp[4]; p0[5] = pp[5];
+}
+
+// The acceptance rule of reliability_propagation.cpp:359-368.
+template <typename P>
+__device__ __forceinline__ bool acceptable(const Result<P>& R, const P (&p0)[6], P cutoff, P max_znssd) {
+    return R.valid && R.status == TDIC_SUCCESS && R.corr < max_znssd && fabs(p0[0] - R.p[0]) < cutoff &&
+           fabs(p0[1] - R.p[1]) < cutoff && finite6(R.p) && isfinite(R.corr);
+}
+
+// The propagation.  Blocks hold `gpb` solver groups of G warps and one resolver warp.
+// Launched cooperatively (co-resident blocks, own grid barrier).
+template <int OPT, int DEG, typename T, int G, typename Src>
+__device__ __forceinline__ void propagate_body(const Src& src, const Shape& sh) {
     using P = typename MixedOf<T>::type;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int gpb = static_cast<int>(blockDim.x - 32) / (32 * G);
     const int gi = threadIdx.x / (32 * G), tid = threadIdx.x % (32 * G);
     const bool solver = gi < gpb;
-    short2* s_off = kernel_preamble<T, G>(e, &tm_ref, &tm_coef, smem_raw, gi, tid, solver);
-    if (s_off == nullptr) {  // every block takes this path together: nothing waits on a barrier yet
-        if (threadIdx.x == 0) atomicExch(pe.flags, 1);
+    const PropEnv& g = src.prop(0);  // shared queue, wave lists, barrier and error word
+    const bool one = src.count() == 1;
+    short2* s_tab = kernel_preamble<T, G>(sh, g.err, one ? src.tm_ref(0) : nullptr, one ? src.tm_coef(0) : nullptr,
+                                          smem_raw, gi, tid, solver);
+    if (s_tab == nullptr) {  // every block takes this path together: nothing waits on a barrier yet
+        if (threadIdx.x == 0) atomicExch(g.err, 1);
         return;
     }
-    GroupSmem<T> gs(smem_raw + cta_prefix_bytes(e.nmax), solver ? gi : 0, e.nmax, G, e.rbx, e.rby, e.cbx, e.cby);
+    GroupSmem<T> gs = group_smem<T, G>(smem_raw, sh, solver ? gi : 0);
     int* ints = gs.ints;
     const int bar_id = 1 + gi;
     uint32_t phase = 0;
-    P* params = reinterpret_cast<P*>(pe.key + static_cast<size_t>(pe.gw) * pe.gh);  // params follow the keys
-    const P cutoff = static_cast<P>(pe.step), max_znssd = static_cast<P>(pe.max_znssd);
-    unsigned char* ctl = smem_raw + cta_prefix_bytes(e.nmax) +
-                         gpb * group_smem_bytes<T>(e.nmax, G, e.rbx, e.rby, e.cbx, e.cby);
+    unsigned char* ctl = smem_raw + cta_prefix_bytes(sh.ntab) +
+                         gpb * group_smem_bytes<T>(sh.nmax, G, sh.rbx, sh.rby, sh.cbx, sh.cby);
     DfSlot<P>* slots = reinterpret_cast<DfSlot<P>*>(ctl);
     int* s_done = reinterpret_cast<int*>(ctl + round128(gpb * sizeof(DfSlot<P>)));
     if (threadIdx.x < gpb) {
@@ -1334,17 +1426,22 @@ __global__ void __launch_bounds__(32 * G * kPropGroupsPerBlock + 32, sizeof(T) =
     }
     if (threadIdx.x == 0) *s_done = 0;
 
-    // Prologue: place the seed (reliability_propagation.cpp:201-278).
-    if (blockIdx.x == 0 && gi == 0) {
+    // Prologue: place each job's seed (reliability_propagation.cpp:201-278), one group per job.
+    for (int j = blockIdx.x; j < src.count(); j += gridDim.x) {
+        if (gi != 0) continue;
+        const PropEnv& pe = src.prop(j);
+        auto&& e = src.env(j);
+        if (pe.seed_idx < 0) continue;  // no seed placed for this job
+        P* params = reinterpret_cast<P*>(pe.params);
         Result<P> R;
         bool ok = true;
         if (pe.seed_solve) {
             const int sx = (pe.seed_idx % pe.gw) * pe.step, sy = (pe.seed_idx / pe.gw) * pe.step;
             P sp[6];
             for (int k = 0; k < 6; ++k) sp[k] = static_cast<P>(pe.seed_p[k]);
-            if (!solve_poi<OPT, DEG, T, G>(e, &tm_ref, &tm_coef, s_off, sx, sy, sp, static_cast<P>(pe.seed_corr), gs,
-                                           phase, tid, bar_id, R)) {
-                if (tid == 0) { pe.flags[1] = 1; atomicExch(pe.flags, 1); }
+            if (!solve_poi<OPT, DEG, T, G>(e, src.tm_ref(j), src.tm_coef(j), s_tab + src.table(j), sx, sy, sp,
+                                           static_cast<P>(pe.seed_corr), gs, phase, tid, bar_id, R)) {
+                if (tid == 0) { pe.flags[1] = 1; atomicExch(g.err, 1); }
                 ok = false;
             }
             ok = ok && R.valid && R.status == TDIC_SUCCESS && finite6(R.p) && isfinite(R.corr);
@@ -1374,10 +1471,10 @@ __global__ void __launch_bounds__(32 * G * kPropGroupsPerBlock + 32, sizeof(T) =
             }
         }
     }
-    if (!grid_barrier(pe.barrier, pe.flags, pe.counters)) return;
-    if (*reinterpret_cast<volatile int*>(pe.flags + 1)) return;
+    if (!grid_barrier(g.barrier, g.err, g.counters)) return;
+    if (one && *reinterpret_cast<volatile int*>(g.flags + 1)) return;
 
-    if (pe.mode == 2) {
+    if (g.mode == 2) {
         // ---- dataflow phase: no grid-wide synchronisation ------------------------------------
         if (solver) {
             DfSlot<P>* slot = slots + gi;
@@ -1402,14 +1499,17 @@ __global__ void __launch_bounds__(32 * G * kPropGroupsPerBlock + 32, sizeof(T) =
                                 item_p = slot->par;
                                 break;
                             }
-                            if (++spins > kSpinLimit) { atomicExch(pe.flags, 1); state = 2; break; }
+                            if (++spins > kSpinLimit) { atomicExch(g.err, 1); state = 2; break; }
                             __nanosleep(spins < 64 ? 20 : 200);
                         }
                     }
                     group_bcast3<G>(state, item_c, item_p, ints + 1, tid, bar_id);
                     if (state != 0) break;
                 }
-                const int n = item_c;
+                const int j = src.job_of(item_c), n = src.point_of(item_c);
+                const PropEnv& pe = src.prop(j);
+                auto&& e = src.env(j);
+                const P cutoff = static_cast<P>(pe.step), max_znssd = static_cast<P>(pe.max_znssd);
                 const int nx = (n % pe.gw) * pe.step, ny = (n / pe.gw) * pe.step;
                 bool accepted = false;
                 int new_state = kDfOrphan;
@@ -1425,22 +1525,18 @@ __global__ void __launch_bounds__(32 * G * kPropGroupsPerBlock + 32, sizeof(T) =
                         if (cont_c >= 0) {
                             for (int k = 0; k < 6; ++k) pp[k] = cp[k];
                         } else {
+                            const P* params = reinterpret_cast<const P*>(pe.params);
                             for (int k = 0; k < 6; ++k) pp[k] = __ldcg(params + static_cast<size_t>(item_p) * 6 + k);
                         }
-                        const P ddx = static_cast<P>(nx - (item_p % pe.gw) * pe.step);
-                        const P ddy = static_cast<P>(ny - (item_p / pe.gw) * pe.step);
                         P p0[6];
-                        p0[0] = pp[0] + pp[2] * ddx + pp[3] * ddy;  // reliability_propagation.cpp:326-329
-                        p0[1] = pp[1] + pp[4] * ddx + pp[5] * ddy;
-                        p0[2] = pp[2]; p0[3] = pp[3]; p0[4] = pp[4]; p0[5] = pp[5];
-                        if (!solve_poi<OPT, DEG, T, G>(e, &tm_ref, &tm_coef, s_off, nx, ny, p0, P(0), gs, phase, tid,
-                                                       bar_id, R)) {
-                            if (tid == 0) atomicExch(pe.flags, 1);
+                        extrapolate(pp, static_cast<P>(nx - (item_p % pe.gw) * pe.step),
+                                    static_cast<P>(ny - (item_p / pe.gw) * pe.step), p0);
+                        if (!solve_poi<OPT, DEG, T, G>(e, src.tm_ref(j), src.tm_coef(j), s_tab + src.table(j), nx, ny,
+                                                       p0, P(0), gs, phase, tid, bar_id, R)) {
+                            if (tid == 0) atomicExch(g.err, 1);
                             return;  // TMA wait timed out
                         }
-                        accepted = R.valid && R.status == TDIC_SUCCESS && R.corr < max_znssd &&
-                                   fabs(p0[0] - R.p[0]) < cutoff && fabs(p0[1] - R.p[1]) < cutoff && finite6(R.p) &&
-                                   isfinite(R.corr);  // :359-368
+                        accepted = acceptable(R, p0, cutoff, max_znssd);
                         if (accepted) new_state = kDfAccepted;
                     }
                 }
@@ -1449,10 +1545,10 @@ __global__ void __launch_bounds__(32 * G * kPropGroupsPerBlock + 32, sizeof(T) =
                     // hand n to the resolver lane (its slot holds one point; normally long free)
                     unsigned long long spins = 0;
                     while (vld(&slot->post) != 0) {
-                        if (++spins > kSpinLimit) { atomicExch(pe.flags, 1); break; }
+                        if (++spins > kSpinLimit) { atomicExch(g.err, 1); break; }
                         __nanosleep(20);
                     }
-                    slot->n = n; slot->state = new_state; slot->cont = next;
+                    slot->n = item_c; slot->state = new_state; slot->cont = next;
                     slot->iters = R.iters; slot->conv = R.conv ? 1 : 0;
                     for (int k = 0; k < 6; ++k) slot->p[k] = R.p[k];
                     slot->corr = R.corr;
@@ -1461,68 +1557,90 @@ __global__ void __launch_bounds__(32 * G * kPropGroupsPerBlock + 32, sizeof(T) =
                 }
                 if (next >= 0)
                     for (int k = 0; k < 6; ++k) cp[k] = R.p[k];
-                cont_c = next;
+                cont_c = next >= 0 ? (next | pe.jtag) : -1;
                 cont_p = n;
             }
         } else {
             const int lane = threadIdx.x & 31;
-            if (lane < gpb) df_resolver_lane<P>(pe, slots + lane, params, s_done);
+            if (lane < gpb) df_resolver_lane<P>(src, slots + lane, s_done, sh.total);
             __syncwarp();
         }
-        if (!grid_barrier(pe.barrier, pe.flags)) return;
+        if (!grid_barrier(g.barrier, g.err)) return;
         // ---- clean-up: orphans are reached by frontier waves from every accepted point ------
-        const int ng = pe.gw * pe.gh;
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ng; i += gridDim.x * blockDim.x) {
-            const int st = ld_cg(pe.dstate + i);
-            if (st == kDfAccepted || st == kDfRejected) pe.claim[i] = 1;
+        for (int j = 0; j < src.count(); ++j) {
+            const PropEnv& pe = src.prop(j);
+            const int ng = pe.gw * pe.gh;
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ng; i += gridDim.x * blockDim.x) {
+                const int st = ld_cg(pe.dstate + i);
+                if (st == kDfAccepted || st == kDfRejected) pe.claim[i] = 1;
+            }
         }
-        if (!grid_barrier(pe.barrier, pe.flags)) return;
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ng; i += gridDim.x * blockDim.x)
-            if (ld_cg(pe.dstate + i) == kDfAccepted) expand(pe, e.w, e.h, e.radius, i, __ldcg(pe.kcorr + i), 1);
-        if (!grid_barrier(pe.barrier, pe.flags, pe.counters)) return;
+        if (!grid_barrier(g.barrier, g.err)) return;
+        for (int j = 0; j < src.count(); ++j) {
+            const PropEnv& pe = src.prop(j);
+            const Env<T>& e = src.env(j);
+            const int ng = pe.gw * pe.gh;
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ng; i += gridDim.x * blockDim.x)
+                if (ld_cg(pe.dstate + i) == kDfAccepted) expand(pe, e.w, e.h, e.radius, i, __ldcg(pe.kcorr + i), 1);
+        }
+        if (!grid_barrier(g.barrier, g.err, g.counters)) return;
     }
 
     // ---- frontier waves -----------------------------------------------------------------
     int start = 0;
-    int end = static_cast<int>(__ldcg(pe.barrier + 2));  // the wave-list tail at the last barrier
+    int end = static_cast<int>(__ldcg(g.barrier + 2));  // the wave-list tail at the last barrier
     for (int wave = 1; start < end; ++wave) {
         const int count = end - start;
         while (solver) {
             int i = 0;
-            if (tid == 0) i = atomicAdd(pe.fetch + wave, 1);
+            if (tid == 0) i = atomicAdd(g.fetch + wave, 1);
             i = group_bcast<G>(i, ints + 1, tid, bar_id);
             if (i >= count) break;
-            const int n = ld_cg(pe.order + start + i);
+            const int tagged = ld_cg(g.order + start + i);
+            const int j = src.job_of(tagged), n = src.point_of(tagged);
+            const PropEnv& pe = src.prop(j);
+            auto&& e = src.env(j);
+            const P cutoff = static_cast<P>(pe.step), max_znssd = static_cast<P>(pe.max_znssd);
+            P* params = reinterpret_cast<P*>(pe.params);
             const unsigned long long kk = __ldcg(pe.key + n);
             const int parent = static_cast<int>(kk & 0xffffffffull);
             P pp[6];
             for (int k = 0; k < 6; ++k) pp[k] = __ldcg(params + static_cast<size_t>(parent) * 6 + k);
             const int nx = (n % pe.gw) * pe.step, ny = (n / pe.gw) * pe.step;
-            const P ddx = static_cast<P>(nx - (parent % pe.gw) * pe.step);
-            const P ddy = static_cast<P>(ny - (parent / pe.gw) * pe.step);
             P p0[6];
-            p0[0] = pp[0] + pp[2] * ddx + pp[3] * ddy;  // reliability_propagation.cpp:326-329
-            p0[1] = pp[1] + pp[4] * ddx + pp[5] * ddy;
-            p0[2] = pp[2]; p0[3] = pp[3]; p0[4] = pp[4]; p0[5] = pp[5];
+            extrapolate(pp, static_cast<P>(nx - (parent % pe.gw) * pe.step),
+                        static_cast<P>(ny - (parent / pe.gw) * pe.step), p0);
             Result<P> R;
-            if (!solve_poi<OPT, DEG, T, G>(e, &tm_ref, &tm_coef, s_off, nx, ny, p0, P(0), gs, phase, tid, bar_id, R)) {
-                if (tid == 0) atomicExch(pe.flags, 1);
+            if (!solve_poi<OPT, DEG, T, G>(e, src.tm_ref(j), src.tm_coef(j), s_tab + src.table(j), nx, ny, p0, P(0), gs,
+                                           phase, tid, bar_id, R)) {
+                if (tid == 0) atomicExch(g.err, 1);
                 return;  // TMA wait timed out
             }
-            const bool accepted = R.valid && R.status == TDIC_SUCCESS && R.corr < max_znssd &&
-                                  fabs(p0[0] - R.p[0]) < cutoff && fabs(p0[1] - R.p[1]) < cutoff && finite6(R.p) &&
-                                  isfinite(R.corr);  // :359-368
-            if (accepted && tid == 0) {
+            if (acceptable(R, p0, cutoff, max_znssd) && tid == 0) {
                 store_grid<P>(pe, params, n, R);
                 atomicAdd(pe.flags + 2, 1);
                 __threadfence();
                 expand(pe, e.w, e.h, e.radius, n, static_cast<float>(R.corr), wave + 1);
             }
         }
-        if (!grid_barrier(pe.barrier, pe.flags, pe.counters)) return;
+        if (!grid_barrier(g.barrier, g.err, g.counters)) return;
         start = end;
-        end = static_cast<int>(__ldcg(pe.barrier + 2));
+        end = static_cast<int>(__ldcg(g.barrier + 2));
     }
+}
+
+template <int OPT, int DEG, typename T, int G>
+__global__ void __launch_bounds__(kPropMaxThreads, sizeof(T) == 4 ? kPropMinBlocks : 1)
+    propagate_kernel(const __grid_constant__ Env<T> e, const __grid_constant__ CUtensorMap tm_ref,
+                     const __grid_constant__ CUtensorMap tm_coef, const __grid_constant__ PropEnv pe) {
+    propagate_body<OPT, DEG, T, G>(OneJob<T>{e, pe, &tm_ref, &tm_coef}, shape_of(e, pe.gw * pe.gh));
+}
+
+template <int OPT, int DEG, typename T, int G>
+__global__ void __launch_bounds__(kPropMaxThreads, sizeof(T) == 4 ? kPropMinBlocks : 1)
+    propagate_batch_kernel(const BatchJob<T>* __restrict__ jobs, int njobs, const CUtensorMap* __restrict__ maps,
+                           const __grid_constant__ Shape sh) {
+    propagate_body<OPT, DEG, T, G>(JobTable<T>{jobs, njobs, maps}, sh);
 }
 
 __global__ void init_grid_kernel(tdic_grid_out o, int gw, int gh, int step) {
@@ -1690,7 +1808,8 @@ void propagate_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, con
     pe.max_znssd = cfg.propagation_max_znssd;
     pe.out = L.out;
     pe.claim = L.claim; pe.key = L.key; pe.order = L.order; pe.counters = L.counters; pe.fetch = L.fetch;
-    pe.barrier = L.barrier; pe.flags = L.flags;
+    pe.params = L.key + static_cast<size_t>(L.gw) * L.gh;  // the parameters follow the keys
+    pe.barrier = L.barrier; pe.flags = L.flags; pe.err = L.flags; pe.jtag = 0;
     pe.mode = L.mode; pe.sgx = L.sgx; pe.sgy = L.sgy;
     pe.dstate = L.dstate; pe.dcnt = L.dcnt; pe.dq = L.dq; pe.kcorr = L.kcorr;
     pe.qword = reinterpret_cast<unsigned long long*>(L.counters + 4);
@@ -1700,6 +1819,254 @@ void propagate_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, con
     void* args[] = {&e, &tm.ref, &tm.coef, &pe};
     TDIC_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kern), dim3(blocks), dim3(threads), args,
                                               smem, s));
+}
+
+// ---------------------------------------------------------------------------------------
+// Batched propagation: several image pairs in one persistent launch.
+// ---------------------------------------------------------------------------------------
+template <typename T>
+struct BatchPlan final : BatchPlanBase {
+    using P = typename MixedOf<T>::type;
+    int n = 0, opt = 0, deg = 3;
+    size_t total = 0;
+    std::vector<size_t> off;            // first grid point of each job
+    std::vector<int> gw, gh, step, seed_ok;
+    std::vector<BatchJob<T>> jobs;      // host copy of the job table
+    std::vector<tdic_grid_out> outs;    // device outputs of each job
+    Shape sh{};
+    Buffer d_jobs, d_maps, d_tab, d_roi, d_claim, d_key, d_params, d_dstate, d_dcnt, d_kcorr, d_dq, d_order, d_fetch,
+        d_misc, d_flags, d_out;
+    // launch configurations: (warps per POI, groups per CTA) -> grid size and shared memory
+    struct Config { int G, gpb, blocks, threads; size_t smem; };
+    std::vector<Config> configs;
+    int chosen = 0;
+};
+
+template <int OPT, int DEG, typename T, int G>
+void batch_kernel_setup(BatchPlan<T>& b, tdic_ctx* ctx, int gpb) {
+    const size_t per_group = group_smem_bytes<T>(b.sh.nmax, G, b.sh.rbx, b.sh.rby, b.sh.cbx, b.sh.cby);
+    const size_t prefix = cta_prefix_bytes(b.sh.ntab);
+    const size_t ctl = round128(kPropGroupsPerBlock * sizeof(DfSlot<typename MixedOf<T>::type>)) + 128;
+    const size_t smem = prefix + gpb * per_group + ctl;
+    if (smem > static_cast<size_t>(ctx->max_smem_optin)) return;
+    const int threads = 32 * G * gpb + 32;
+    auto kern = propagate_batch_kernel<OPT, DEG, T, G>;
+    // the attribute is an upper bound shared by every configuration of this kernel: only raise it
+    cudaFuncAttributes fa{};
+    TDIC_CUDA_TRY(cudaFuncGetAttributes(&fa, kern));
+    if (static_cast<int>(smem) > fa.maxDynamicSharedSizeBytes)
+        TDIC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    int per_sm = 0;
+    TDIC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+    if (per_sm <= 0) return;
+    b.configs.push_back({G, gpb, per_sm * ctx->num_sms, threads, smem});
+}
+
+template <int OPT, int DEG, typename T, int G>
+void batch_kernel_launch(BatchPlan<T>& b, const typename BatchPlan<T>::Config& c, cudaStream_t s) {
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3(c.blocks);
+    lc.blockDim = dim3(c.threads);
+    lc.dynamicSmemBytes = c.smem;
+    lc.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;  // co-resident blocks: the kernel has a grid barrier
+    attr[0].val.cooperative = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    TDIC_CUDA_TRY(cudaLaunchKernelEx(&lc, propagate_batch_kernel<OPT, DEG, T, G>, b.d_jobs.template as<BatchJob<T>>(),
+                                     b.n, b.d_maps.template as<CUtensorMap>(), b.sh));
+}
+
+template <int OPT, int DEG, typename T>
+void batch_configs(BatchPlan<T>& b, tdic_ctx* ctx) {
+    b.configs.clear();
+    batch_kernel_setup<OPT, DEG, T, 4>(b, ctx, 2);
+    batch_kernel_setup<OPT, DEG, T, 4>(b, ctx, 1);
+    batch_kernel_setup<OPT, DEG, T, 8>(b, ctx, 1);
+    TDIC_REQUIRE(!b.configs.empty(), TDIC_UNSUPPORTED, "batch: subset radius too large for shared memory");
+}
+
+template <int OPT, int DEG, typename T>
+void batch_dispatch(BatchPlan<T>& b, const typename BatchPlan<T>::Config& c, cudaStream_t s) {
+    if (c.G == 8) batch_kernel_launch<OPT, DEG, T, 8>(b, c, s);
+    else batch_kernel_launch<OPT, DEG, T, 4>(b, c, s);
+}
+
+template <typename T, typename F>
+void with_opt_deg(int opt, int deg, F&& f) {
+    if (opt == 1) {
+        if (deg == 1) f(std::integral_constant<int, 1>{}, std::integral_constant<int, 1>{});
+        else if (deg == 3) f(std::integral_constant<int, 1>{}, std::integral_constant<int, 3>{});
+        else f(std::integral_constant<int, 1>{}, std::integral_constant<int, 5>{});
+    } else {
+        if (deg == 1) f(std::integral_constant<int, 0>{}, std::integral_constant<int, 1>{});
+        else if (deg == 3) f(std::integral_constant<int, 0>{}, std::integral_constant<int, 3>{});
+        else f(std::integral_constant<int, 0>{}, std::integral_constant<int, 5>{});
+    }
+}
+
+template <typename T>
+std::unique_ptr<BatchPlanBase> batch_plan_build(tdic_ctx* ctx, int n, tdic_pair* const* pairs, const tdic_config* cfgs,
+                                                const BatchSeed* seeds, const std::vector<std::vector<uint8_t>>& rois,
+                                                cudaStream_t s) {
+    using P = typename MixedOf<T>::type;
+    auto b = std::make_unique<BatchPlan<T>>();
+    b->n = n;
+    b->opt = cfgs[0].optimizer;
+    b->deg = pairs[0]->degree;
+    // sample-offset tables, one per radius, concatenated
+    std::vector<int> radii;
+    for (int j = 0; j < n; ++j) radii.push_back(cfgs[j].subset_radius);
+    std::sort(radii.begin(), radii.end());
+    radii.erase(std::unique(radii.begin(), radii.end()), radii.end());
+    std::vector<short2> tab;
+    std::vector<int> tab_off(radii.size()), tab_n(radii.size());
+    for (size_t k = 0; k < radii.size(); ++k) {
+        const int r = radii[k];
+        tab_off[k] = static_cast<int>(tab.size());
+        for (int dy = -r; dy <= r; ++dy)
+            for (int dx = -r; dx <= r; ++dx)
+                if (dx * dx + dy * dy <= r * r) tab.push_back(make_short2(static_cast<short>(dx), static_cast<short>(dy)));
+        tab_n[k] = static_cast<int>(tab.size()) - tab_off[k];
+    }
+    b->d_tab = Buffer(&ctx->pool, sizeof(short2) * tab.size());
+    TDIC_CUDA_TRY(cudaMemcpyAsync(b->d_tab.ptr, tab.data(), sizeof(short2) * tab.size(), cudaMemcpyHostToDevice, s));
+    // grid geometry and point offsets
+    b->off.resize(n + 1);
+    b->gw.resize(n); b->gh.resize(n); b->step.resize(n); b->seed_ok.resize(n);
+    size_t total = 0;
+    for (int j = 0; j < n; ++j) {
+        int32_t gw, gh;
+        tdic_grid_dims(pairs[j]->w, pairs[j]->h, cfgs[j].propagation_spacing, &gw, &gh);
+        TDIC_REQUIRE(static_cast<long long>(gw) * gh <= kPointMask + 1LL, TDIC_INVALID_ARG,
+                     "batch: a job has more than 2^22 grid points");
+        b->gw[j] = gw; b->gh[j] = gh; b->step[j] = std::max(0, cfgs[j].propagation_spacing) + 1;
+        b->off[j] = total;
+        total += static_cast<size_t>(gw) * gh;
+    }
+    b->off[n] = total;
+    b->total = total;
+    TDIC_REQUIRE(total < (1ull << 31), TDIC_INVALID_ARG, "batch: more than 2^31 grid points in total");
+    // device buffers: per-point scratch of all jobs, shared queue state, outputs
+    b->d_roi = Buffer(&ctx->pool, total);
+    b->d_claim = Buffer(&ctx->pool, sizeof(int) * total);
+    b->d_key = Buffer(&ctx->pool, sizeof(unsigned long long) * total);
+    b->d_params = Buffer(&ctx->pool, sizeof(P) * 6 * total);
+    b->d_dstate = Buffer(&ctx->pool, sizeof(int) * total);
+    b->d_dcnt = Buffer(&ctx->pool, sizeof(int) * total);
+    b->d_kcorr = Buffer(&ctx->pool, sizeof(float) * total);
+    b->d_dq = Buffer(&ctx->pool, sizeof(unsigned long long) * total);
+    b->d_order = Buffer(&ctx->pool, sizeof(int) * total);
+    b->d_fetch = Buffer(&ctx->pool, sizeof(int) * (total + 2));
+    b->d_misc = Buffer(&ctx->pool, 64);
+    b->d_flags = Buffer(&ctx->pool, sizeof(int) * 4 * n);
+    b->d_out = Buffer(&ctx->pool, (10 * sizeof(double) + sizeof(int32_t) + 3) * total);
+    double* dbl = b->d_out.template as<double>();
+    int32_t* it = reinterpret_cast<int32_t*>(dbl + 10 * total);
+    uint8_t* bytes = reinterpret_cast<uint8_t*>(it + total);
+    // ROI at the grid points, per job (host masks of W x H, or all valid)
+    std::vector<uint8_t> roi_grid(total, 1);
+    for (int j = 0; j < n; ++j)
+        if (!rois[j].empty())
+            for (int i = 0; i < b->gw[j] * b->gh[j]; ++i)
+                roi_grid[b->off[j] + i] =
+                    rois[j][static_cast<size_t>((i / b->gw[j]) * b->step[j]) * pairs[j]->w + (i % b->gw[j]) * b->step[j]];
+    TDIC_CUDA_TRY(cudaMemcpyAsync(b->d_roi.ptr, roi_grid.data(), total, cudaMemcpyHostToDevice, s));
+    // environments, capacities and tensor maps
+    Shape sh{b->d_tab.template as<short2>(), static_cast<int>(tab.size()), 0, 0, 0, 0, 0, static_cast<int>(total)};
+    std::vector<Env<T>> envs(n);
+    for (int j = 0; j < n; ++j) {
+        const int k = static_cast<int>(std::lower_bound(radii.begin(), radii.end(), cfgs[j].subset_radius) - radii.begin());
+        envs[j] = make_env<T>(ctx, pairs[j], cfgs[j], cfgs[j].subset_radius, cfgs[j].max_iterations,
+                              cfgs[j].convergence_threshold, b->d_tab.template as<short2>() + tab_off[k], tab_n[k]);
+        sh.nmax = std::max(sh.nmax, envs[j].n);
+        sh.rbx = std::max(sh.rbx, envs[j].rbx); sh.rby = std::max(sh.rby, envs[j].rby);
+        sh.cbx = std::max(sh.cbx, envs[j].cbx); sh.cby = std::max(sh.cby, envs[j].cby);
+    }
+    b->sh = sh;
+    std::vector<CUtensorMap> maps(2 * static_cast<size_t>(n));
+    b->jobs.resize(n);
+    b->outs.resize(n);
+    unsigned char* misc = b->d_misc.template as<unsigned char>();
+    int* m = reinterpret_cast<int*>(misc);
+    for (int j = 0; j < n; ++j) {
+        const int k = static_cast<int>(std::lower_bound(radii.begin(), radii.end(), cfgs[j].subset_radius) - radii.begin());
+        Env<T> e = envs[j];
+        e.nmax = sh.nmax;  // the per-group arrays are laid out for the largest subset
+        const TensorMaps tm = make_tensor_maps<T>(pairs[j], e);
+        maps[2 * j] = tm.ref;
+        maps[2 * j + 1] = tm.coef;
+        const size_t o = b->off[j];
+        tdic_grid_out go{};
+        go.x = dbl + 0 * total + o; go.y = dbl + 1 * total + o; go.u = dbl + 2 * total + o; go.v = dbl + 3 * total + o;
+        go.du_dx = dbl + 4 * total + o; go.du_dy = dbl + 5 * total + o; go.dv_dx = dbl + 6 * total + o;
+        go.dv_dy = dbl + 7 * total + o; go.correlation = dbl + 8 * total + o; go.zncc = dbl + 9 * total + o;
+        go.iterations = it + o;
+        go.valid = bytes + o;
+        go.status = reinterpret_cast<int8_t*>(bytes + total + o);
+        go.converged = bytes + 2 * total + o;
+        b->outs[j] = go;
+        PropEnv pe{};
+        pe.gw = b->gw[j]; pe.gh = b->gh[j]; pe.step = b->step[j];
+        pe.roi_grid = b->d_roi.template as<uint8_t>() + o;
+        pe.seed_idx = seeds[j].ok ? seeds[j].idx : -1;
+        pe.seed_solve = seeds[j].solve;
+        for (int q = 0; q < 6; ++q) pe.seed_p[q] = seeds[j].p[q];
+        pe.seed_corr = seeds[j].corr;
+        pe.max_znssd = cfgs[j].propagation_max_znssd;
+        pe.out = go;
+        pe.claim = b->d_claim.template as<int>() + o;
+        pe.key = b->d_key.template as<unsigned long long>() + o;
+        pe.params = b->d_params.template as<P>() + 6 * o;
+        pe.order = b->d_order.template as<int>();
+        pe.counters = m;                                            // [0] wave-list tail, [1] queue head
+        pe.qword = reinterpret_cast<unsigned long long*>(m + 4);    // queue tail : in flight + 2^31
+        pe.barrier = reinterpret_cast<unsigned int*>(m + 8);
+        pe.err = m + 12;
+        pe.fetch = b->d_fetch.template as<int>();
+        pe.flags = b->d_flags.template as<int>() + 4 * j;
+        pe.jtag = j << kJobShift;
+        pe.mode = 2;
+        pe.sgx = seeds[j].gx; pe.sgy = seeds[j].gy;
+        pe.dstate = b->d_dstate.template as<int>() + o;
+        pe.dcnt = b->d_dcnt.template as<int>() + o;
+        pe.dq = b->d_dq.template as<unsigned long long>();
+        pe.kcorr = b->d_kcorr.template as<float>() + o;
+        b->jobs[j].e = e;
+        b->jobs[j].pe = pe;
+        b->jobs[j].table = tab_off[k];
+        b->seed_ok[j] = seeds[j].ok;
+    }
+    b->d_jobs = Buffer(&ctx->pool, sizeof(BatchJob<T>) * n);
+    b->d_maps = Buffer(&ctx->pool, sizeof(CUtensorMap) * maps.size());
+    TDIC_CUDA_TRY(cudaMemcpyAsync(b->d_jobs.ptr, b->jobs.data(), sizeof(BatchJob<T>) * n, cudaMemcpyHostToDevice, s));
+    TDIC_CUDA_TRY(cudaMemcpyAsync(b->d_maps.ptr, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice, s));
+    TDIC_CUDA_TRY(cudaStreamSynchronize(s));  // host staging vectors go out of scope
+    with_opt_deg<T>(b->opt, b->deg, [&](auto O, auto D) { batch_configs<decltype(O)::value, decltype(D)::value, T>(*b, ctx); });
+    return b;
+}
+
+// Everything one propagation of the batch needs, enqueued on `s` without a host wait.
+template <typename T>
+void batch_plan_launch(BatchPlan<T>& b, int config, cudaStream_t s) {
+    const size_t total = b.total;
+    TDIC_CUDA_TRY(cudaMemsetAsync(b.d_claim.ptr, 0, sizeof(int) * total, s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(b.d_key.ptr, 0xff, sizeof(unsigned long long) * total, s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(b.d_dstate.ptr, 0, sizeof(int) * total, s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(b.d_dcnt.ptr, 0, sizeof(int) * total, s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(b.d_dq.ptr, 0xff, sizeof(unsigned long long) * total, s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(b.d_fetch.ptr, 0, sizeof(int) * (total + 2), s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(b.d_flags.ptr, 0, sizeof(int) * 4 * b.n, s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(b.d_misc.ptr, 0, 64, s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(b.d_misc.template as<unsigned char>() + 19, 0x80, 1, s));  // in-flight bias 2^31
+    for (int j = 0; j < b.n; ++j) {
+        const int np = b.gw[j] * b.gh[j];
+        init_grid_kernel<<<std::min((np + 255) / 256, 4096), 256, 0, s>>>(b.outs[j], b.gw[j], b.gh[j], b.step[j]);
+    }
+    TDIC_CUDA_TRY(cudaGetLastError());
+    const auto& c = b.configs[config];
+    with_opt_deg<T>(b.opt, b.deg, [&](auto O, auto D) { batch_dispatch<decltype(O)::value, decltype(D)::value, T>(b, c, s); });
 }
 
 template <int OPT, typename T>
@@ -1753,6 +2120,61 @@ void launch_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, co
         if (fp64) propagate_deg<1, double>(ctx, pair, cfg, L, s); else propagate_deg<1, float>(ctx, pair, cfg, L, s);
     } else {
         if (fp64) propagate_deg<0, double>(ctx, pair, cfg, L, s); else propagate_deg<0, float>(ctx, pair, cfg, L, s);
+    }
+}
+
+std::unique_ptr<BatchPlanBase> batch_build(tdic_ctx* ctx, int n, tdic_pair* const* pairs, const tdic_config* cfgs,
+                                           const BatchSeed* seeds, const std::vector<std::vector<uint8_t>>& rois,
+                                           cudaStream_t s) {
+    if (pairs[0]->precision == TDIC_FP64) return batch_plan_build<double>(ctx, n, pairs, cfgs, seeds, rois, s);
+    return batch_plan_build<float>(ctx, n, pairs, cfgs, seeds, rois, s);
+}
+
+int batch_config_count(BatchPlanBase* p) {
+    if (auto* b = dynamic_cast<BatchPlan<double>*>(p)) return static_cast<int>(b->configs.size());
+    return static_cast<int>(static_cast<BatchPlan<float>*>(p)->configs.size());
+}
+
+void batch_launch(BatchPlanBase* p, int config, cudaStream_t s) {
+    if (auto* b = dynamic_cast<BatchPlan<double>*>(p)) batch_plan_launch(*b, config, s);
+    else batch_plan_launch(*static_cast<BatchPlan<float>*>(p), config, s);
+}
+
+template <typename T>
+void batch_read(BatchPlan<T>& b, int32_t* computed, int* err, cudaStream_t s) {
+    std::vector<int> flags(4 * static_cast<size_t>(b.n));
+    int e = 0;
+    TDIC_CUDA_TRY(cudaMemcpyAsync(flags.data(), b.d_flags.ptr, sizeof(int) * flags.size(), cudaMemcpyDeviceToHost, s));
+    TDIC_CUDA_TRY(cudaMemcpyAsync(&e, b.d_misc.template as<int>() + 12, sizeof(int), cudaMemcpyDeviceToHost, s));
+    TDIC_CUDA_TRY(cudaStreamSynchronize(s));
+    *err = e;
+    for (int j = 0; j < b.n; ++j)
+        computed[j] = (b.seed_ok[j] && !flags[4 * j + 1]) ? flags[4 * j + 2] : 0;
+}
+
+void batch_finish(BatchPlanBase* p, int32_t* computed, int* err, cudaStream_t s) {
+    if (auto* b = dynamic_cast<BatchPlan<double>*>(p)) batch_read(*b, computed, err, s);
+    else batch_read(*static_cast<BatchPlan<float>*>(p), computed, err, s);
+}
+
+tdic_grid_out batch_outputs(BatchPlanBase* p, int job) {
+    if (auto* b = dynamic_cast<BatchPlan<double>*>(p)) return b->outs[job];
+    return static_cast<BatchPlan<float>*>(p)->outs[job];
+}
+
+void batch_grid(BatchPlanBase* p, int job, int32_t* gw, int32_t* gh) {
+    if (auto* b = dynamic_cast<BatchPlan<double>*>(p)) { *gw = b->gw[job]; *gh = b->gh[job]; return; }
+    auto* f = static_cast<BatchPlan<float>*>(p);
+    *gw = f->gw[job];
+    *gh = f->gh[job];
+}
+
+void batch_config_info(BatchPlanBase* p, int config, int* warps_per_poi, int* groups_per_block) {
+    if (auto* b = dynamic_cast<BatchPlan<double>*>(p)) {
+        *warps_per_poi = b->configs[config].G; *groups_per_block = b->configs[config].gpb;
+    } else {
+        auto* f = static_cast<BatchPlan<float>*>(p);
+        *warps_per_poi = f->configs[config].G; *groups_per_block = f->configs[config].gpb;
     }
 }
 

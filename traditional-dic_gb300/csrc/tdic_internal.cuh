@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -27,6 +28,7 @@ struct Error {
     do {                                                                                     \
         cudaError_t e_ = (expr);                                                             \
         if (e_ != cudaSuccess) {                                                             \
+            (void)cudaGetLastError(); /* a non-sticky error must not surface in a later call */ \
             throw ::tdic::Error{TDIC_CUDA_ERROR, std::string(#expr) + ": " + cudaGetErrorString(e_)}; \
         }                                                                                    \
     } while (0)
@@ -182,5 +184,28 @@ private:
 };
 void integer_search_batch(tdic_ctx* ctx, tdic_pair* lazy, const tdic_config& cfg, const int* cx, const int* cy,
                           int n, SearchResult* out, cudaStream_t s);
+
+// Batched propagation (several image pairs in one persistent launch).  Grid points of a batch
+// are tagged with their job in queue items: 22 bits of point, the job above.
+constexpr int kMaxBatchJobs = 512;
+struct BatchSeed {
+    int ok;            // the seed is placed (reliability_propagation.cpp:201-216)
+    int idx, gx, gy;   // aligned grid point
+    int solve;         // 1 when the aligned point differs from the raw seed
+    double p[6];
+    double corr;
+};
+struct BatchPlanBase {
+    virtual ~BatchPlanBase() = default;
+};
+std::unique_ptr<BatchPlanBase> batch_build(tdic_ctx* ctx, int n, tdic_pair* const* pairs, const tdic_config* cfgs,
+                                           const BatchSeed* seeds, const std::vector<std::vector<uint8_t>>& rois,
+                                           cudaStream_t s);
+int batch_config_count(BatchPlanBase* p);
+void batch_config_info(BatchPlanBase* p, int config, int* warps_per_poi, int* groups_per_block);
+void batch_launch(BatchPlanBase* p, int config, cudaStream_t s);
+void batch_finish(BatchPlanBase* p, int32_t* computed, int* err, cudaStream_t s);
+tdic_grid_out batch_outputs(BatchPlanBase* p, int job);
+void batch_grid(BatchPlanBase* p, int job, int32_t* gw, int32_t* gh);
 
 }  // namespace tdic

@@ -451,6 +451,82 @@ def propagate(ctx: Context, pair: Pair, config: L.Config, seed: L.Seed, roi=None
     return out
 
 
+class Batch:
+    """Several image pairs propagated in one persistent launch (tdic_batch_*): job j is
+    ``propagate(ctx, pairs[j], configs[j], seeds[j], rois[j])`` in the dataflow order.
+    ``launch`` only enqueues work on the stream (it can be captured in a CUDA graph);
+    ``finish`` waits and returns the points computed per job; ``outputs(j)`` copies job j's grid
+    to host arrays (``device_outputs(j)`` gives the device pointers)."""
+
+    def __init__(self, ctx: Context, pairs, configs, seeds, rois=None, stream=None):
+        n = len(pairs)
+        if not (len(configs) == len(seeds) == n) or (rois is not None and len(rois) != n):
+            raise ValueError("pairs, configs, seeds (and rois) must have the same length")
+        self.ctx, self.n, self.pairs = ctx, n, list(pairs)
+        self._cfgs = (L.Config * n)(*configs)
+        self._seeds = (L.Seed * n)(*seeds)
+        self._pairs = (C.c_void_p * n)(*[p.handle.value for p in pairs])
+        self._rois_keep, roi_ptrs = [], (C.c_void_p * n)()
+        for j in range(n):
+            r = None if rois is None else rois[j]
+            ptr, keep = _roi_arg(r, pairs[j].width, pairs[j].height)
+            if ptr == "mismatch":
+                raise ValueError("roi shape differs from the images")
+            roi_ptrs[j] = ptr
+            self._rois_keep.append(keep)
+        self._roi_ptrs = roi_ptrs
+        self.grid_shapes = []
+        for j in range(n):
+            gw, gh = L.grid_dims(pairs[j].width, pairs[j].height, configs[j].propagation_spacing)
+            self.grid_shapes.append((gh, gw))
+        h = C.c_void_p()
+        ctx.check(ctx.lib.tdic_batch_create(ctx.handle, n, self._pairs, self._cfgs, self._seeds,
+                                            roi_ptrs if rois is not None else None, _stream_ptr(stream), C.byref(h)))
+        self.handle = h
+
+    def tune(self, stream=None) -> tuple:
+        self.ctx.check(self.ctx.lib.tdic_batch_tune(self.handle, _stream_ptr(stream)))
+        return self.config()
+
+    def config(self) -> tuple:
+        g, k = C.c_int32(), C.c_int32()
+        self.ctx.check(self.ctx.lib.tdic_batch_config(self.handle, C.byref(g), C.byref(k)))
+        return g.value, k.value
+
+    def launch(self, stream=None) -> None:
+        self.ctx.check(self.ctx.lib.tdic_batch_launch(self.handle, _stream_ptr(stream)))
+
+    def finish(self, stream=None) -> np.ndarray:
+        pc = np.zeros(self.n, np.int32)
+        self.ctx.check(self.ctx.lib.tdic_batch_finish(self.handle, _stream_ptr(stream), pc.ctypes.data))
+        return pc
+
+    def device_outputs(self, j: int) -> L.GridOut:
+        g = L.GridOut()
+        self.ctx.check(self.ctx.lib.tdic_batch_outputs(self.handle, int(j), C.byref(g)))
+        return g
+
+    def outputs(self, j: int, stream=None) -> dict:
+        """Job j's grid as host arrays (the keys of ``propagate``'s result)."""
+        gh, gw = self.grid_shapes[j]
+        arrs, host = _alloc_grid(gw * gh)
+        self.ctx.check(self.ctx.lib.tdic_batch_results(self.handle, int(j), C.byref(host), _stream_ptr(stream)))
+        out = _finish(arrs)
+        out["grid_shape"] = (gh, gw)
+        return out
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.ctx.lib.tdic_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def select_seed(ctx: Context, lazy_pair: Pair, reference: np.ndarray, config: L.Config, roi=None) -> L.Seed:
     ref = np.ascontiguousarray(reference, np.float32)
     rptr, rkeep = _roi_arg(roi, lazy_pair.width, lazy_pair.height)
