@@ -1,0 +1,253 @@
+"""Serving loop for streams of image pairs (continuous batching on one GPU).
+
+Requests (``Server.submit``) arrive at any time.  A host thread admits them while their device
+footprint fits the memory budget, prepares each on a preparation stream (upload, B-spline
+prefilter, seed selection: ``SubsetDIC::compute``'s steps before the propagation), and
+propagates all prepared requests in one batched persistent launch (``subset.Batch``) on the
+propagation stream.  Requests that arrive while a batch is on the GPU are prepared meanwhile
+and go into the next batch, so preparation kernels overlap the running propagation.  Each
+request's result equals ``subset.compute`` of the same pair and configuration alone (the batch
+gives every job the single-pair result).
+
+Image pairs are kept in a cache per shape and refreshed in place for later requests, so the loop
+allocates no device memory once warm.
+"""
+from __future__ import annotations
+
+import collections
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+from . import subset as S
+
+
+@dataclass
+class Request:
+    """One submitted pair.  ``wait()`` returns the result dict of ``subset.compute``."""
+    id: int
+    reference: np.ndarray
+    deformed: np.ndarray
+    config: dict | None
+    roi: np.ndarray | None
+    arrival: float
+    started: float = 0.0
+    finished: float = 0.0
+    batch_size: int = 0
+    result: dict | None = None
+    error: BaseException | None = None
+    _done: threading.Event = field(default_factory=threading.Event, repr=False)
+
+    def wait(self, timeout: float | None = None) -> dict:
+        if not self._done.wait(timeout):
+            raise TimeoutError(f"request {self.id} not finished")
+        if self.error is not None:
+            raise self.error
+        return self.result
+
+    @property
+    def latency(self) -> float:
+        """Seconds from submission to result."""
+        return self.finished - self.arrival
+
+
+@dataclass
+class _Prepared:
+    req: Request
+    pair: S.Pair
+    lazy: S.Pair
+    cfg: L.Config
+    seed: L.Seed
+    key: tuple
+    bytes: int
+
+
+def _footprint(w: int, h: int, cfg: L.Config) -> int:
+    """Device bytes of one request: the images of its two pairs (float32 images, coefficients,
+    upload staging) and the propagation scratch and outputs of its grid points."""
+    gw, gh = L.grid_dims(w, h, cfg.propagation_spacing)
+    coef = 8 if cfg.precision == L.FP64 else 4
+    return 2 * (2 * 4 * w * h + coef * (w + 8) * (h + 8) + 8 * w * h) + 260 * gw * gh
+
+
+class Server:
+    """Continuous-batching request loop on one device (see the module docstring).
+
+    memory_budget: device bytes the admitted (prepared or running) requests may hold.
+    max_batch: requests per batched launch (at most 512)."""
+
+    def __init__(self, context: S.Context | None = None, memory_budget: int = 48 << 30, max_batch: int = 64):
+        import torch
+        self.ctx = context or S.default_context()
+        self.memory_budget = int(memory_budget)
+        self.max_batch = max(1, min(512, int(max_batch)))
+        self._torch = torch
+        self._prep = torch.cuda.Stream()
+        self._main = torch.cuda.Stream()
+        self._queue: collections.deque[Request] = collections.deque()
+        self._cv = threading.Condition()
+        self._stop = False
+        self._next_id = 0
+        self._cache: dict[tuple, list] = collections.defaultdict(list)  # shape key -> [(pair, lazy)]
+        self._held = 0
+        self.batches: list[int] = []  # size of every batch launched
+        self._thread = threading.Thread(target=self._loop, name="tdic-serve", daemon=True)
+        self._thread.start()
+
+    # ---- client side -------------------------------------------------------------------------
+    def submit(self, reference: np.ndarray, deformed: np.ndarray, config: dict | None = None, roi=None) -> Request:
+        ref = S._check_image(reference, "reference")
+        de = S._check_image(deformed, "deformed")
+        with self._cv:
+            req = Request(self._next_id, ref, de, config, roi, time.perf_counter())
+            self._next_id += 1
+            self._queue.append(req)
+            self._cv.notify()
+        return req
+
+    def close(self) -> None:
+        with self._cv:
+            self._stop = True
+            self._cv.notify()
+        self._thread.join()
+        for entries in self._cache.values():
+            for pair, lazy in entries:
+                pair.close()
+                lazy.close()
+        self._cache.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- server side -------------------------------------------------------------------------
+    def _pairs_for(self, req: Request, cfg: L.Config):
+        h, w = req.reference.shape
+        degree = cfg.degree if cfg.degree in (1, 3) else 5
+        key = (w, h, req.reference.dtype.str, degree, cfg.precision)
+        if self._cache[key]:
+            pair, lazy = self._cache[key].pop()
+            pair.update(req.reference, req.deformed, stream=self._prep)
+            lazy.update(req.reference, req.deformed, stream=self._prep)
+        else:
+            pair = S.Pair(self.ctx, req.reference, req.deformed, degree=degree, border=cfg.border,
+                          precision=cfg.precision, stream=self._prep)
+            lazy = S.Pair(self.ctx, req.reference, req.deformed, degree=degree, border=cfg.border, exact=False,
+                          precision=cfg.precision, stream=self._prep)
+        return key, pair, lazy
+
+    def _prepare(self, req: Request) -> _Prepared | None:
+        """Upload, prefilter and seed selection on the preparation stream.  None when the
+        request finished here (no seed: the reference's empty result)."""
+        req.started = time.perf_counter()
+        cfg = S.config_from_dict(req.config)
+        cfg.propagation_mode = S.PROPAGATION_MODES["dataflow"]
+        h, w = req.reference.shape
+        if req.roi is not None and np.asarray(req.roi).shape != (h, w):
+            self._complete(req, S._empty_result())
+            return None
+        key, pair, lazy = self._pairs_for(req, cfg)
+        seed = S.select_seed(self.ctx, lazy, req.reference.astype(np.float32, copy=False), cfg, roi=req.roi,
+                             stream=self._prep)
+        nbytes = _footprint(w, h, cfg)
+        if not seed.found:
+            self._cache[key].append((pair, lazy))
+            self._complete(req, S._empty_result())
+            return None
+        return _Prepared(req, pair, lazy, cfg, seed, key, nbytes)
+
+    def _complete(self, req: Request, result=None, error=None) -> None:
+        req.result, req.error = result, error
+        req.finished = time.perf_counter()
+        req._done.set()
+
+    def _launch(self, ready: list[_Prepared]):
+        first = ready[0]
+        sig = (first.pair.degree, first.pair.precision, first.cfg.optimizer)
+        group = [p for p in ready if (p.pair.degree, p.pair.precision, p.cfg.optimizer) == sig][:self.max_batch]
+        rest = [p for p in ready if p not in group]
+        self._prep.synchronize()  # the group's pairs and seeds are ready
+        batch = S.Batch(self.ctx, [p.pair for p in group], [p.cfg for p in group], [p.seed for p in group],
+                        [p.req.roi for p in group], stream=self._main)
+        batch.launch(stream=self._main)
+        done = self._torch.cuda.Event()
+        done.record(self._main)
+        self.batches.append(len(group))
+        return (batch, group, done), rest
+
+    def _collect(self, inflight) -> None:
+        batch, group, _ = inflight
+        try:
+            pc = batch.finish(stream=self._main)
+            for j, p in enumerate(group):
+                p.req.batch_size = len(group)
+                if pc[j] == 0:
+                    self._complete(p.req, S._empty_result())
+                else:
+                    out = batch.outputs(j, stream=self._main)
+                    self._complete(p.req, {k: out[k] for k in S.RESULT_KEYS + S.EXTRA_KEYS})
+        except BaseException as exc:  # every request of the batch learns of the failure
+            for p in group:
+                if not p.req._done.is_set():
+                    self._complete(p.req, error=exc)
+        finally:
+            batch.close()
+            for p in group:
+                self._cache[p.key].append((p.pair, p.lazy))
+                self._held -= p.bytes
+
+    def _loop(self) -> None:
+        inflight = None
+        ready: list[_Prepared] = []
+        while True:
+            with self._cv:
+                if self._stop and not self._queue and not ready and inflight is None:
+                    break
+                if not self._queue and not ready and inflight is None:
+                    self._cv.wait(0.05)
+                    continue
+            progressed = False
+            # the running batch first: its results free memory and the GPU for the next one
+            if inflight is not None and inflight[2].query():
+                self._collect(inflight)
+                inflight = None
+                progressed = True
+            if inflight is None and ready:
+                try:
+                    inflight, ready = self._launch(ready)
+                except BaseException as exc:
+                    for p in ready:
+                        self._complete(p.req, error=exc)
+                        self._cache[p.key].append((p.pair, p.lazy))
+                        self._held -= p.bytes
+                    ready = []
+                progressed = True
+            # admit and prepare queued requests while the budget allows (overlaps the batch)
+            while len(ready) < self.max_batch:
+                with self._cv:
+                    if not self._queue:
+                        break
+                    req = self._queue[0]
+                    h, w = req.reference.shape
+                    est = _footprint(w, h, S.config_from_dict(req.config))
+                    if self._held + est > self.memory_budget and (ready or inflight is not None):
+                        break  # wait for memory to free up
+                    self._queue.popleft()
+                try:
+                    prepared = self._prepare(req)
+                except BaseException as exc:
+                    self._complete(req, error=exc)
+                    prepared = None
+                progressed = True
+                if prepared is not None:
+                    self._held += prepared.bytes
+                    ready.append(prepared)
+                if inflight is not None and inflight[2].query():
+                    break  # launch the next batch without delay
+            if not progressed:
+                time.sleep(0.0002)

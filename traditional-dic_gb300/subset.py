@@ -527,10 +527,11 @@ class Batch:
             pass
 
 
-def select_seed(ctx: Context, lazy_pair: Pair, reference: np.ndarray, config: L.Config, roi=None) -> L.Seed:
+def select_seed(ctx: Context, lazy_pair: Pair, reference: np.ndarray, config: L.Config, roi=None,
+                stream=None) -> L.Seed:
     ref = np.ascontiguousarray(reference, np.float32)
     rptr, rkeep = _roi_arg(roi, lazy_pair.width, lazy_pair.height)
     seed = L.Seed()
     ctx.check(ctx.lib.tdic_select_seed(ctx.handle, lazy_pair.handle, ref.ctypes.data, rptr, C.byref(config),
-                                       C.byref(seed), None))
+                                       C.byref(seed), _stream_ptr(stream)))
     return seed

@@ -164,22 +164,73 @@ def workload(index: int, side: int | None = None) -> Pair:
     raise ValueError("use batch_workload() for the uneven batch")
 
 
-def batch_workload(n_pairs: int = 48, seed: int = BASE_SEED + 2, max_side: int = 4096):
+def _batch_pair(args):
+    side, dtype_name, params, seed = args
+    return speckle_pair((side, side), int(round(24000 * (side / 2048.0) ** 2)), Field("linear", params), 1.0, seed,
+                        dtype=np.dtype(dtype_name).type)
+
+
+def batch_workload(n_pairs: int = 48, seed: int = BASE_SEED + 2, max_side: int = 4096, pool=None):
     """Uneven batch: sides log-U[512, max_side], half uint8 / half uint16, affine fields,
-    per-pair radius in {7, 11, 15, 21, 25} and POI step in {3, 5, 8}."""
+    per-pair radius in {7, 11, 15, 21, 25} and POI step in {3, 5, 8}.  All parameters are drawn
+    first from one generator; the pairs (each from its own seed) render in ``pool`` (an
+    executor whose workers can import this package) when one is given."""
     rng = np.random.default_rng(seed)
-    pairs = []
+    specs, extra = [], []
     for i in range(n_pairs):
         side = int(round(math.exp(rng.uniform(math.log(512), math.log(max_side)))))
         dtype = np.uint8 if i % 2 == 0 else np.uint16
-        f = Field("linear", dict(u0=rng.uniform(-5, 5), ux=rng.uniform(-0.01, 0.01), uy=rng.uniform(-0.01, 0.01),
-                                 v0=rng.uniform(-5, 5), vx=rng.uniform(-0.01, 0.01), vy=rng.uniform(-0.01, 0.01)))
+        params = dict(u0=rng.uniform(-5, 5), ux=rng.uniform(-0.01, 0.01), uy=rng.uniform(-0.01, 0.01),
+                      v0=rng.uniform(-5, 5), vx=rng.uniform(-0.01, 0.01), vy=rng.uniform(-0.01, 0.01))
         # centre the affine field so the translation stays within U(-5, 5) over the image
-        f.params["u0"] -= f.params["ux"] * side / 2 + f.params["uy"] * side / 2
-        f.params["v0"] -= f.params["vx"] * side / 2 + f.params["vy"] * side / 2
-        blobs = int(round(24000 * (side / 2048.0) ** 2))
-        p = speckle_pair((side, side), blobs, f, 1.0, seed * 1000 + i, dtype=dtype)
-        p.meta["radius"] = int(rng.choice([7, 11, 15, 21, 25]))
-        p.meta["step"] = int(rng.choice([3, 5, 8]))
-        pairs.append(p)
+        params["u0"] -= params["ux"] * side / 2 + params["uy"] * side / 2
+        params["v0"] -= params["vx"] * side / 2 + params["vy"] * side / 2
+        radius = int(rng.choice([7, 11, 15, 21, 25]))
+        step = int(rng.choice([3, 5, 8]))
+        specs.append((side, np.dtype(dtype).name, params, seed * 1000 + i))
+        extra.append((radius, step))
+    pairs = list(pool.map(_batch_pair, specs)) if pool is not None else [_batch_pair(a) for a in specs]
+    for p, (radius, step) in zip(pairs, extra):
+        p.meta["radius"] = radius
+        p.meta["step"] = step
     return pairs
+
+
+def _serve_pair(args):
+    side, dtype_name, kind, params, seed = args
+    return speckle_pair((side, side), int(round(24000 * (side / 2048.0) ** 2)), Field(kind, params), 1.0, seed,
+                        dtype=np.dtype(dtype_name).type)
+
+
+def serve_workload(n_requests: int = 40, rate: float = 40.0, seed: int = BASE_SEED + 3,
+                   sides=(1024, 2048, 3072, 4096), pool=None):
+    """Served request stream: Poisson arrivals at ``rate`` per second, sides uniform over
+    ``sides``, uint8 or uint16, a Gaussian bump (3 px, sigma = side / 6) or an affine field
+    (translation U(-5, 5), gradients U(-0.01, 0.01)), radius in {7, 11, 15, 21, 25} and POI step
+    in {3, 5, 8}.  Returns [(arrival seconds from the start, Pair)]; pairs render in ``pool``
+    when one is given."""
+    rng = np.random.default_rng(seed)
+    specs, extra, t = [], [], 0.0
+    for i in range(n_requests):
+        t += rng.exponential(1.0 / rate)
+        side = int(rng.choice(sides))
+        dtype = np.uint8 if rng.uniform() < 0.5 else np.uint16
+        if rng.uniform() < 0.5:
+            kind = "bump"
+            params = dict(cx=side / 2.0, cy=side / 2.0, s=side / 6.0, a=3.0, shear=0.0, sa=0.0, sl=64.0)
+        else:
+            kind = "linear"
+            params = dict(u0=rng.uniform(-5, 5), ux=rng.uniform(-0.01, 0.01), uy=rng.uniform(-0.01, 0.01),
+                          v0=rng.uniform(-5, 5), vx=rng.uniform(-0.01, 0.01), vy=rng.uniform(-0.01, 0.01))
+            params["u0"] -= params["ux"] * side / 2 + params["uy"] * side / 2
+            params["v0"] -= params["vx"] * side / 2 + params["vy"] * side / 2
+        radius = int(rng.choice([7, 11, 15, 21, 25]))
+        step = int(rng.choice([3, 5, 8]))
+        specs.append((side, np.dtype(dtype).name, kind, params, seed * 1000 + i))
+        extra.append((t, radius, step, kind))
+    pairs = list(pool.map(_serve_pair, specs)) if pool is not None else [_serve_pair(a) for a in specs]
+    out = []
+    for p, (arrival, radius, step, kind) in zip(pairs, extra):
+        p.meta.update(radius=radius, step=step, kind=kind)
+        out.append((arrival, p))
+    return out
