@@ -542,12 +542,17 @@ def run_serve(args, ctx) -> dict:
         return [r.latency for r in reqs], conv, span
 
     with serve.Server(ctx) as server:
-        served_run(server)                    # warm: device buffers and pair cache for every shape
+        served_run(server)                    # warm: the device pool holds buffers for every shape
+        nb = len(server.batches)
+        marks = {k: len(v) for k, v in server.stats.items()}
         lat, conv, span = served_run(server)
-        sizes = server.batches[-len(stream):]
+        sizes = server.batches[nb:]
+        stage = {k: 1e3 * float(np.mean(v[marks[k]:])) for k, v in server.stats.items() if len(v) > marks[k]}
     out = _latency_stats(lat, conv, span)
     out.update(requests=len(stream), rate_per_s=40.0, batches=len(sizes),
-               mean_batch=float(np.mean(sizes)) if sizes else 0.0)
+               mean_batch=float(np.mean(sizes)) if sizes else 0.0,
+               mean_ms={"prepare_per_request": stage.get("prepare"), "propagate_per_batch": stage.get("propagate"),
+                        "collect_per_batch": stage.get("collect")})
 
     def plain(precision):
         for arrival, p in stream[:2]:         # warm

@@ -157,6 +157,8 @@ tdic_status tdic_pair_create(tdic_ctx* ctx, const void* reference, const void* d
 /* Recompute an existing pair from new images of the same shape (no allocation). */
 tdic_status tdic_pair_update(tdic_pair* pair, const void* reference, const void* deformed,
                              int32_t pitch, tdic_dtype dtype, tdic_memory memory, void* stream);
+/* Waits for the work enqueued on the pair through this library (on any stream), then frees it.
+ * Work captured in a CUDA graph is not tracked: synchronise its stream after replaying first. */
 void tdic_pair_destroy(tdic_pair* pair);
 /* Copy the coefficient image ((H+2B) x (W+2B), float32 or float64 per the pair's precision)
  * into a host buffer of `bytes` bytes; for tests. */
@@ -220,7 +222,8 @@ tdic_status tdic_propagate_noalloc(tdic_ctx* ctx, tdic_pair* pair, const tdic_co
  *                      this batch and keeps the fastest; optional.
  *   tdic_batch_launch  enqueues one propagation of every job on `stream` and returns without
  *                      waiting: device memsets and kernel launches only, so it can be captured
- *                      in a CUDA graph and replayed.
+ *                      in a CUDA graph and replayed (synchronise the replay stream before
+ *                      destroying the batch or its pairs: replays are not tracked).
  *   tdic_batch_finish  waits for `stream` and reports points_computed[j] (0: the seed of job j
  *                      could not be placed, its grid holds the defaults). */
 typedef struct tdic_batch tdic_batch;
@@ -247,6 +250,16 @@ void tdic_batch_destroy(tdic_batch* batch);
 tdic_status tdic_select_seed(tdic_ctx* ctx, tdic_pair* lazy, const float* reference_host,
                              const uint8_t* roi, const tdic_config* cfg, tdic_seed* seed,
                              void* stream);
+
+/* SubsetDIC::compute up to the propagation (subset_dic.cpp:39-64): creates the pair from host
+ * images (as tdic_pair_create with the exact prefilter) and selects its seed (as
+ * tdic_select_seed, on a seed spline built from the uploaded images; texture statistics on the
+ * raw host images).  The caller propagates (tdic_propagate, or one job of a tdic_batch) and
+ * destroys *pair_out.  seed_out->found = 0 means SubsetDIC::compute's empty result. */
+tdic_status tdic_subset_prepare(tdic_ctx* ctx, const void* reference, const void* deformed,
+                                int32_t width, int32_t height, tdic_dtype dtype,
+                                const uint8_t* roi, const tdic_config* cfg, void* stream,
+                                tdic_pair** pair_out, tdic_seed* seed_out);
 
 /* Whole pybind path: _traditional_dic.subset.compute (bind_subset.cpp:253-315) ->
  * SubsetDIC::compute (subset_dic.cpp:39-105).  Host images of `dtype`, host roi (NULL = full

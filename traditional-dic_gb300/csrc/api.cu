@@ -692,7 +692,9 @@ tdic_status tdic_pair_create(tdic_ctx* ctx, const void* reference, const void* d
             p->ref = Buffer(&ctx->pool, sizeof(float) * static_cast<size_t>(p->rpitch) * height);
             p->def_f = Buffer(&ctx->pool, sizeof(float) * static_cast<size_t>(p->rpitch) * height);
             p->coef = Buffer(&ctx->pool, es * static_cast<size_t>(p->cpitch) * p->ch);
+            TDIC_CUDA_TRY(cudaEventCreateWithFlags(&p->last_use, cudaEventDisableTiming));
             pair_compute(p, reference, deformed, pitch, dtype, memory, pick(ctx, stream));
+            mark_use(p, pick(ctx, stream));
         } catch (...) {
             delete p;
             throw;
@@ -708,6 +710,7 @@ tdic_status tdic_pair_update(tdic_pair* pair, const void* reference, const void*
     return guarded(pair->ctx, [&] {
         TDIC_REQUIRE(reference && deformed, TDIC_INVALID_ARG, "null image");
         pair_compute(pair, reference, deformed, pitch, dtype, memory, pick(pair->ctx, stream));
+        mark_use(pair, pick(pair->ctx, stream));
     });
 }
 
@@ -718,7 +721,9 @@ void tdic_pair_destroy(tdic_pair* pair) {
     {
         std::lock_guard<std::recursive_mutex> lock(ctx->mu);
         cudaSetDevice(ctx->device);
-        cudaDeviceSynchronize();  // work on any stream may still read the pair's buffers
+        // work enqueued on any stream may still read the pair's buffers: wait for the last of it
+        if (pair->last_use) cudaEventSynchronize(pair->last_use);
+        (void)cudaGetLastError();  // nothing to report from a destructor
         delete pair;
         ctx->live_pairs -= 1;
         if (ctx->destroy_requested && ctx->live_pairs == 0) {
@@ -752,6 +757,7 @@ tdic_status tdic_reference_gradient(tdic_pair* pair, double* gx, double* gy) {
                                   ctx->stream);
         TDIC_CUDA_TRY(cudaMemcpyAsync(gx, dx.ptr, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
         TDIC_CUDA_TRY(cudaMemcpyAsync(gy, dy.ptr, 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
+        mark_use(pair, ctx->stream);
         TDIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     });
 }
@@ -769,12 +775,14 @@ tdic_status tdic_solve_pois(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* c
         Buffer fetch(&ctx->pool, sizeof(int));
         if (memory == TDIC_DEVICE) {
             launch_solve(ctx, pair, *cfg, SolveLaunch{in, out, n, fetch.as<int>()}, s);
+            mark_use(pair, s);
             check_device_error(ctx, s);  // synchronises: keeps `fetch` alive until the kernel is done
             return;
         }
         Buffer d_in(&ctx->pool, sizeof(tdic_poi_in) * n), d_out(&ctx->pool, sizeof(tdic_poi_out) * n);
         TDIC_CUDA_TRY(cudaMemcpyAsync(d_in.ptr, in, sizeof(tdic_poi_in) * n, cudaMemcpyHostToDevice, s));
         launch_solve(ctx, pair, *cfg, SolveLaunch{d_in.as<tdic_poi_in>(), d_out.as<tdic_poi_out>(), n, fetch.as<int>()}, s);
+        mark_use(pair, s);
         TDIC_CUDA_TRY(cudaMemcpyAsync(out, d_out.ptr, sizeof(tdic_poi_out) * n, cudaMemcpyDeviceToHost, s));
         check_device_error(ctx, s);
     });
@@ -787,6 +795,7 @@ tdic_status tdic_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cf
         TDIC_REQUIRE(pair && cfg && seed && out && points_computed, TDIC_INVALID_ARG, "null argument");
         TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
         propagate_impl(ctx, pair, *cfg, *seed, roi, out, memory, points_computed, pick(ctx, stream));
+        mark_use(pair, pick(ctx, stream));
     });
 }
 
@@ -796,6 +805,55 @@ tdic_status tdic_select_seed(tdic_ctx* ctx, tdic_pair* lazy, const float* refere
         TDIC_REQUIRE(lazy && reference_host && cfg && seed, TDIC_INVALID_ARG, "null argument");
         TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
         select_seed_impl(ctx, lazy, HostImage{reference_host, TDIC_F32}, roi, *cfg, seed, pick(ctx, stream));
+        mark_use(lazy, pick(ctx, stream));
+    });
+}
+
+// SubsetDIC::compute up to the propagation (subset_dic.cpp:39-64): the pair from the host
+// images, the seed on the clamp-padded non-deconvolved spline of the same images
+// (seed_selector.cpp:166-173; the seed pair reuses the uploaded images), host texture statistics
+// on the raw images.
+static void prepare_impl(tdic_ctx* ctx, const void* reference, const void* deformed, int32_t width, int32_t height,
+                  tdic_dtype dtype, const uint8_t* roi, const tdic_config& cfg, cudaStream_t s, tdic_pair** pair_out,
+                  tdic_seed* seed_out) {
+    const int degree = normalized_degree(cfg.degree);
+    tdic_pair* pair = nullptr;
+    tdic_status st = tdic_pair_create(ctx, reference, deformed, width, height, 0, dtype, TDIC_HOST, degree, cfg.border, 1,
+                                      cfg.precision, s, &pair);
+    if (st != TDIC_OK) throw Error{st, ctx->last_error};
+    try {
+        tdic_pair* lazy = nullptr;
+        st = tdic_pair_create(ctx, pair->ref.ptr, pair->def_f.ptr, width, height, pair->rpitch, TDIC_F32, TDIC_DEVICE,
+                              degree, cfg.border, 0, cfg.precision, s, &lazy);
+        if (st != TDIC_OK) throw Error{st, ctx->last_error};
+        tdic_seed seed{};
+        try {
+            select_seed_impl(ctx, lazy, HostImage{reference, dtype}, roi, cfg, &seed, s);
+            mark_use(lazy, s);
+        } catch (...) {
+            tdic_pair_destroy(lazy);
+            throw;
+        }
+        tdic_pair_destroy(lazy);
+        *seed_out = seed;
+    } catch (...) {
+        tdic_pair_destroy(pair);
+        throw;
+    }
+    *pair_out = pair;
+}
+
+tdic_status tdic_subset_prepare(tdic_ctx* ctx, const void* reference, const void* deformed, int32_t width,
+                                int32_t height, tdic_dtype dtype, const uint8_t* roi, const tdic_config* cfg,
+                                void* stream, tdic_pair** pair_out, tdic_seed* seed_out) {
+    return guarded(ctx, [&] {
+        TDIC_REQUIRE(cfg && pair_out && seed_out && reference && deformed, TDIC_INVALID_ARG, "null argument");
+        TDIC_REQUIRE(width > 0 && height > 0, TDIC_INVALID_ARG, "empty image");
+        *pair_out = nullptr;
+        std::memset(seed_out, 0, sizeof(*seed_out));
+        check_config(*cfg);
+        TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
+        prepare_impl(ctx, reference, deformed, width, height, dtype, roi, *cfg, pick(ctx, stream), pair_out, seed_out);
     });
 }
 
@@ -809,29 +867,16 @@ tdic_status tdic_subset_compute(tdic_ctx* ctx, const void* reference, const void
         check_config(*cfg);
         TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
         cudaStream_t s = pick(ctx, stream);
-        const int degree = normalized_degree(cfg->degree);
         tdic_pair* pair = nullptr;
-        tdic_status st = tdic_pair_create(ctx, reference, deformed, width, height, 0, dtype, TDIC_HOST, degree,
-                                          cfg->border, 1, cfg->precision, s, &pair);
-        if (st != TDIC_OK) throw Error{st, ctx->last_error};
+        tdic_seed seed{};
+        prepare_impl(ctx, reference, deformed, width, height, dtype, roi, *cfg, s, &pair, &seed);
+        if (seed_out) *seed_out = seed;
         int32_t computed = 0;
         try {
-            // Seed refinement runs on the clamp-padded, non-deconvolved coefficients of the same
-            // deformed image (seed_selector.cpp:166-173); the lazy pair reuses the uploaded images.
-            tdic_pair* lazy = nullptr;
-            st = tdic_pair_create(ctx, pair->ref.ptr, pair->def_f.ptr, width, height, pair->rpitch, TDIC_F32, TDIC_DEVICE, degree,
-                                  cfg->border, 0, cfg->precision, s, &lazy);
-            if (st != TDIC_OK) throw Error{st, ctx->last_error};
-            tdic_seed seed{};
-            try {
-                select_seed_impl(ctx, lazy, HostImage{reference, dtype}, roi, *cfg, &seed, s);
-            } catch (...) {
-                tdic_pair_destroy(lazy);
-                throw;
+            if (seed.found) {
+                propagate_impl(ctx, pair, *cfg, seed, roi, out, TDIC_HOST, &computed, s);
+                mark_use(pair, s);
             }
-            tdic_pair_destroy(lazy);
-            if (seed_out) *seed_out = seed;
-            if (seed.found) propagate_impl(ctx, pair, *cfg, seed, roi, out, TDIC_HOST, &computed, s);
         } catch (...) {
             tdic_pair_destroy(pair);
             throw;
@@ -1019,6 +1064,7 @@ tdic_status tdic_propagate_noalloc(tdic_ctx* ctx, tdic_pair* pair, const tdic_co
         TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
         std::lock_guard<std::mutex> lock(noalloc_mu);
         propagate_noalloc_impl(ctx, pair, *cfg, *seed, roi, out_device, points_computed, pick(ctx, stream));
+        mark_use(pair, pick(ctx, stream));
     });
 }
 
@@ -1031,11 +1077,23 @@ tdic_status tdic_propagate_noalloc(tdic_ctx* ctx, tdic_pair* pair, const tdic_co
 struct tdic_batch {
     tdic_ctx* ctx = nullptr;
     int n = 0;
+    std::vector<tdic_pair*> pairs;
     std::unique_ptr<tdic::BatchPlanBase> plan;
     int config = 0;
+    cudaEvent_t last_use = nullptr;  // recorded after the last launch
+    ~tdic_batch() {
+        if (last_use) cudaEventDestroy(last_use);
+    }
 };
 
 namespace {
+
+// Every launch of the batch reads its pairs and writes its own buffers.
+void batch_mark(tdic_batch* b, cudaStream_t s) {
+    if (capturing(s)) return;
+    for (tdic_pair* p : b->pairs) mark_use(p, s);
+    TDIC_CUDA_TRY(cudaEventRecord(b->last_use, s));
+}
 
 void batch_create_impl(tdic_ctx* ctx, int n, tdic_pair* const* pairs, const tdic_config* cfgs, const tdic_seed* seeds,
                        const uint8_t* const* rois, cudaStream_t s, tdic_batch** out) {
@@ -1082,6 +1140,8 @@ void batch_create_impl(tdic_ctx* ctx, int n, tdic_pair* const* pairs, const tdic
     auto b = std::make_unique<tdic_batch>();
     b->ctx = ctx;
     b->n = n;
+    b->pairs.assign(pairs, pairs + n);
+    TDIC_CUDA_TRY(cudaEventCreateWithFlags(&b->last_use, cudaEventDisableTiming));
     b->plan = batch_build(ctx, n, pairs, cfgs, bs.data(), roi_copy, s);
     ++ctx->live_pairs;  // the batch holds buffers of the context's pool
     *out = b.release();
@@ -1118,6 +1178,7 @@ tdic_status tdic_batch_tune(tdic_batch* b, void* stream) {
                 TDIC_CUDA_TRY(cudaEventRecord(e0, s));
                 batch_launch(b->plan.get(), c, s);
                 TDIC_CUDA_TRY(cudaEventRecord(e1, s));
+                batch_mark(b, s);
                 TDIC_CUDA_TRY(cudaEventSynchronize(e1));
                 float ms = 0.0f;
                 TDIC_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
@@ -1137,7 +1198,11 @@ tdic_status tdic_batch_tune(tdic_batch* b, void* stream) {
 
 tdic_status tdic_batch_launch(tdic_batch* b, void* stream) {
     if (!b) return TDIC_INVALID_ARG;
-    return guarded(b->ctx, [&] { batch_launch(b->plan.get(), b->config, pick(b->ctx, stream)); });
+    return guarded(b->ctx, [&] {
+        cudaStream_t s = pick(b->ctx, stream);
+        batch_launch(b->plan.get(), b->config, s);
+        batch_mark(b, s);
+    });
 }
 
 tdic_status tdic_batch_finish(tdic_batch* b, void* stream, int32_t* points_computed) {
@@ -1192,7 +1257,8 @@ void tdic_batch_destroy(tdic_batch* b) {
     {
         std::lock_guard<std::recursive_mutex> lock(ctx->mu);
         cudaSetDevice(ctx->device);
-        cudaDeviceSynchronize();  // a launch on any stream may still use the batch's buffers
+        if (b->last_use) cudaEventSynchronize(b->last_use);  // the last launch may still run
+        (void)cudaGetLastError();  // nothing to report from a destructor
         delete b;
         ctx->live_pairs -= 1;
         if (ctx->destroy_requested && ctx->live_pairs == 0) {

@@ -116,6 +116,10 @@ struct tdic_pair {
     tdic::Buffer coef;         // T coefficients of the deformed image, ch rows of cpitch
     tdic::Buffer def_f;        // float32 H x W deformed, row pitch rpitch (prefilter input, seed search)
     tdic::Buffer staging;      // raw input staging for host uploads
+    cudaEvent_t last_use = nullptr;  // recorded after the last work enqueued on the pair
+    ~tdic_pair() {
+        if (last_use) cudaEventDestroy(last_use);
+    }
 };
 
 namespace tdic {
@@ -124,6 +128,19 @@ namespace tdic {
 void build_qk(int degree, double* qk);
 
 const SampleTable& sample_table(tdic_ctx* ctx, int radius);
+
+// True while `s` is being captured into a CUDA graph: captured work runs only when the graph
+// is replayed, so it is not tracked by the last-use events.
+inline bool capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    TDIC_CUDA_TRY(cudaStreamIsCapturing(s, &st));
+    return st != cudaStreamCaptureStatusNone;
+}
+
+// Mark the pair as used by the work enqueued so far on `s` (its destruction waits for it).
+inline void mark_use(tdic_pair* p, cudaStream_t s) {
+    if (p && p->last_use && !capturing(s)) TDIC_CUDA_TRY(cudaEventRecord(p->last_use, s));
+}
 
 // Kernel launchers (prefilter.cu) --------------------------------------------------------
 void launch_convert(const void* src, int w, int h, int pitch, tdic_dtype dtype, float* dst, int dst_pitch,

@@ -9,8 +9,7 @@ and go into the next batch, so preparation kernels overlap the running propagati
 request's result equals ``subset.compute`` of the same pair and configuration alone (the batch
 gives every job the single-pair result).
 
-Image pairs are kept in a cache per shape and refreshed in place for later requests, so the loop
-allocates no device memory once warm.
+Device memory comes from the context's caching pool, so the loop allocates none once warm.
 """
 from __future__ import annotations
 
@@ -58,19 +57,17 @@ class Request:
 class _Prepared:
     req: Request
     pair: S.Pair
-    lazy: S.Pair
     cfg: L.Config
     seed: L.Seed
-    key: tuple
     bytes: int
 
 
 def _footprint(w: int, h: int, cfg: L.Config) -> int:
-    """Device bytes of one request: the images of its two pairs (float32 images, coefficients,
-    upload staging) and the propagation scratch and outputs of its grid points."""
+    """Device bytes of one request: its pair (float32 images, coefficients, upload staging) and
+    the propagation scratch and outputs of its grid points."""
     gw, gh = L.grid_dims(w, h, cfg.propagation_spacing)
     coef = 8 if cfg.precision == L.FP64 else 4
-    return 2 * (2 * 4 * w * h + coef * (w + 8) * (h + 8) + 8 * w * h) + 260 * gw * gh
+    return 2 * 4 * w * h + coef * (w + 8) * (h + 8) + 8 * w * h + 260 * gw * gh
 
 
 class Server:
@@ -91,9 +88,11 @@ class Server:
         self._cv = threading.Condition()
         self._stop = False
         self._next_id = 0
-        self._cache: dict[tuple, list] = collections.defaultdict(list)  # shape key -> [(pair, lazy)]
         self._held = 0
         self.batches: list[int] = []  # size of every batch launched
+        # seconds per request (preparation) and per batch (device propagation, collection of
+        # the results to host arrays)
+        self.stats: dict[str, list[float]] = {"prepare": [], "propagate": [], "collect": []}
         self._thread = threading.Thread(target=self._loop, name="tdic-serve", daemon=True)
         self._thread.start()
 
@@ -113,11 +112,6 @@ class Server:
             self._stop = True
             self._cv.notify()
         self._thread.join()
-        for entries in self._cache.values():
-            for pair, lazy in entries:
-                pair.close()
-                lazy.close()
-        self._cache.clear()
 
     def __enter__(self):
         return self
@@ -126,21 +120,6 @@ class Server:
         self.close()
 
     # ---- server side -------------------------------------------------------------------------
-    def _pairs_for(self, req: Request, cfg: L.Config):
-        h, w = req.reference.shape
-        degree = cfg.degree if cfg.degree in (1, 3) else 5
-        key = (w, h, req.reference.dtype.str, degree, cfg.precision)
-        if self._cache[key]:
-            pair, lazy = self._cache[key].pop()
-            pair.update(req.reference, req.deformed, stream=self._prep)
-            lazy.update(req.reference, req.deformed, stream=self._prep)
-        else:
-            pair = S.Pair(self.ctx, req.reference, req.deformed, degree=degree, border=cfg.border,
-                          precision=cfg.precision, stream=self._prep)
-            lazy = S.Pair(self.ctx, req.reference, req.deformed, degree=degree, border=cfg.border, exact=False,
-                          precision=cfg.precision, stream=self._prep)
-        return key, pair, lazy
-
     def _prepare(self, req: Request) -> _Prepared | None:
         """Upload, prefilter and seed selection on the preparation stream.  None when the
         request finished here (no seed: the reference's empty result)."""
@@ -151,15 +130,13 @@ class Server:
         if req.roi is not None and np.asarray(req.roi).shape != (h, w):
             self._complete(req, S._empty_result())
             return None
-        key, pair, lazy = self._pairs_for(req, cfg)
-        seed = S.select_seed(self.ctx, lazy, req.reference.astype(np.float32, copy=False), cfg, roi=req.roi,
-                             stream=self._prep)
-        nbytes = _footprint(w, h, cfg)
+        pair, seed = S.prepare(self.ctx, req.reference, req.deformed, cfg, roi=req.roi, stream=self._prep)
+        self.stats["prepare"].append(time.perf_counter() - req.started)
         if not seed.found:
-            self._cache[key].append((pair, lazy))
+            pair.close()
             self._complete(req, S._empty_result())
             return None
-        return _Prepared(req, pair, lazy, cfg, seed, key, nbytes)
+        return _Prepared(req, pair, cfg, seed, _footprint(w, h, cfg))
 
     def _complete(self, req: Request, result=None, error=None) -> None:
         req.result, req.error = result, error
@@ -174,14 +151,18 @@ class Server:
         self._prep.synchronize()  # the group's pairs and seeds are ready
         batch = S.Batch(self.ctx, [p.pair for p in group], [p.cfg for p in group], [p.seed for p in group],
                         [p.req.roi for p in group], stream=self._main)
+        start = self._torch.cuda.Event(enable_timing=True)
+        done = self._torch.cuda.Event(enable_timing=True)
+        start.record(self._main)
         batch.launch(stream=self._main)
-        done = self._torch.cuda.Event()
         done.record(self._main)
         self.batches.append(len(group))
-        return (batch, group, done), rest
+        return (batch, group, done, start), rest
 
     def _collect(self, inflight) -> None:
-        batch, group, _ = inflight
+        batch, group, done, start = inflight
+        t0 = time.perf_counter()
+        self.stats["propagate"].append(start.elapsed_time(done) / 1e3)
         try:
             pc = batch.finish(stream=self._main)
             for j, p in enumerate(group):
@@ -198,8 +179,9 @@ class Server:
         finally:
             batch.close()
             for p in group:
-                self._cache[p.key].append((p.pair, p.lazy))
+                p.pair.close()
                 self._held -= p.bytes
+            self.stats["collect"].append(time.perf_counter() - t0)
 
     def _loop(self) -> None:
         inflight = None
@@ -223,7 +205,7 @@ class Server:
                 except BaseException as exc:
                     for p in ready:
                         self._complete(p.req, error=exc)
-                        self._cache[p.key].append((p.pair, p.lazy))
+                        p.pair.close()
                         self._held -= p.bytes
                     ready = []
                 progressed = True

@@ -115,6 +115,16 @@ class Pair:
                                            _stream_ptr(stream), C.byref(hnd)))
         self.handle = hnd
 
+    @classmethod
+    def _adopt(cls, ctx: Context, handle: C.c_void_p, width: int, height: int, degree: int, precision: int,
+               border: int) -> "Pair":
+        """Wrap a pair the library created (tdic_subset_prepare)."""
+        self = cls.__new__(cls)
+        self.ctx, self.handle = ctx, handle
+        self.width, self.height, self.degree, self.precision = width, height, degree, precision
+        self.border = max(3, border)
+        return self
+
     def update(self, reference, deformed, stream=None) -> None:
         rp, w, h, dt, mem, self._keep_r = _image_arg(reference)
         dp, _, _, _, _, self._keep_d = _image_arg(deformed)
@@ -525,6 +535,24 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def prepare(ctx: Context, reference: np.ndarray, deformed: np.ndarray, config: L.Config, roi=None, stream=None):
+    """SubsetDIC::compute up to the propagation (tdic_subset_prepare): the pair on the device and
+    its seed.  Returns (Pair, Seed); seed.found == 0 is the reference's empty result."""
+    ref = _check_image(reference, "reference")
+    de = _check_image(deformed, "deformed")
+    if ref.shape != de.shape or ref.dtype != de.dtype:
+        raise ValueError("reference and deformed must have the same shape and dtype")
+    h, w = ref.shape
+    rptr, rkeep = _roi_arg(roi, w, h)
+    if rptr == "mismatch":
+        raise ValueError("roi shape differs from the images")
+    hnd, seed = C.c_void_p(), L.Seed()
+    ctx.check(ctx.lib.tdic_subset_prepare(ctx.handle, ref.ctypes.data, de.ctypes.data, w, h, L.DTYPES[ref.dtype.name],
+                                          rptr, C.byref(config), _stream_ptr(stream), C.byref(hnd), C.byref(seed)))
+    degree = config.degree if config.degree in (1, 3) else 5
+    return Pair._adopt(ctx, hnd, w, h, degree, config.precision, config.border), seed
 
 
 def select_seed(ctx: Context, lazy_pair: Pair, reference: np.ndarray, config: L.Config, roi=None,
