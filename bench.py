@@ -541,7 +541,7 @@ def run_serve(args, ctx) -> dict:
         span = max(r.finished for r in reqs) - min(r.arrival for r in reqs)
         return [r.latency for r in reqs], conv, span
 
-    with serve.Server(ctx) as server:
+    with serve.Server(ctx, reserve_sms=args.serve_reserve_sms) as server:
         served_run(server)                    # warm: the device pool holds buffers for every shape
         nb = len(server.batches)
         marks = {k: len(v) for k, v in server.stats.items()}
@@ -549,7 +549,7 @@ def run_serve(args, ctx) -> dict:
         sizes = server.batches[nb:]
         stage = {k: 1e3 * float(np.mean(v[marks[k]:])) for k, v in server.stats.items() if len(v) > marks[k]}
     out = _latency_stats(lat, conv, span)
-    out.update(requests=len(stream), rate_per_s=40.0, batches=len(sizes),
+    out.update(requests=len(stream), rate_per_s=40.0, batches=len(sizes), propagation_sms=server._sms,
                mean_batch=float(np.mean(sizes)) if sizes else 0.0,
                mean_ms={"prepare_per_request": stage.get("prepare"), "propagate_per_batch": stage.get("propagate"),
                         "collect_per_batch": stage.get("collect")})
@@ -591,6 +591,8 @@ def main():
     ap.add_argument("--serve", action="store_true",
                     help="also serve the Poisson request stream (continuous batching) against per-request solves")
     ap.add_argument("--serve-requests", type=int, default=40)
+    ap.add_argument("--serve-reserve-sms", type=int, default=None,
+                    help="SMs the served propagation leaves to request preparation (default: a tenth)")
     ap.add_argument("--side", type=int, default=2048,
                     help="image side; 2048 is the benchmark workload, smaller sides are profiling cases")
     args = ap.parse_args()

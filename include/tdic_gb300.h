@@ -238,6 +238,10 @@ tdic_status tdic_batch_finish(tdic_batch* batch, void* stream, int32_t* points_c
 tdic_status tdic_batch_outputs(tdic_batch* batch, int32_t job, tdic_grid_out* device_arrays);
 /* Copy job j's grid into host arrays (NULL entries skipped); waits for `stream`. */
 tdic_status tdic_batch_results(tdic_batch* batch, int32_t job, const tdic_grid_out* host_arrays, void* stream);
+/* Launch the batch on `sms` SMs' worth of thread blocks (0 = the whole device; default).  The
+ * propagation holds its SMs for its whole duration, so leaving some free lets kernels on other
+ * streams (the preparation of the next requests in a serving loop) run alongside it. */
+tdic_status tdic_batch_set_sms(tdic_batch* batch, int32_t sms);
 /* The launch configuration in use: warps per POI and solver groups per thread block. */
 tdic_status tdic_batch_config(tdic_batch* batch, int32_t* warps_per_poi, int32_t* groups_per_block);
 void tdic_batch_destroy(tdic_batch* batch);

@@ -1239,6 +1239,11 @@ tdic_status tdic_batch_results(tdic_batch* b, int32_t job, const tdic_grid_out* 
     });
 }
 
+tdic_status tdic_batch_set_sms(tdic_batch* b, int32_t sms) {
+    if (!b) return TDIC_INVALID_ARG;
+    return guarded(b->ctx, [&] { batch_set_sms(b->plan.get(), sms); });
+}
+
 tdic_status tdic_batch_config(tdic_batch* b, int32_t* warps_per_poi, int32_t* groups_per_block) {
     if (!b) return TDIC_INVALID_ARG;
     return guarded(b->ctx, [&] {

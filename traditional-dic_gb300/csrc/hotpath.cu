@@ -1837,9 +1837,11 @@ struct BatchPlan final : BatchPlanBase {
     Buffer d_jobs, d_maps, d_tab, d_roi, d_claim, d_key, d_params, d_dstate, d_dcnt, d_kcorr, d_dq, d_order, d_fetch,
         d_misc, d_flags, d_out;
     // launch configurations: (warps per POI, groups per CTA) -> grid size and shared memory
-    struct Config { int G, gpb, blocks, threads; size_t smem; };
+    struct Config { int G, gpb, blocks, threads; size_t smem; int per_sm; };
     std::vector<Config> configs;
     int chosen = 0;
+    int sms = 0;      // SMs' worth of blocks a launch uses (fewer than the device leaves room for other work)
+    int num_sms = 0;
 };
 
 template <int OPT, int DEG, typename T, int G>
@@ -1859,13 +1861,13 @@ void batch_kernel_setup(BatchPlan<T>& b, tdic_ctx* ctx, int gpb) {
     int per_sm = 0;
     TDIC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
     if (per_sm <= 0) return;
-    b.configs.push_back({G, gpb, per_sm * ctx->num_sms, threads, smem});
+    b.configs.push_back({G, gpb, per_sm * ctx->num_sms, threads, smem, per_sm});
 }
 
 template <int OPT, int DEG, typename T, int G>
 void batch_kernel_launch(BatchPlan<T>& b, const typename BatchPlan<T>::Config& c, cudaStream_t s) {
     cudaLaunchConfig_t lc = {};
-    lc.gridDim = dim3(c.blocks);
+    lc.gridDim = dim3(std::min(c.blocks, c.per_sm * std::max(1, b.sms)));
     lc.blockDim = dim3(c.threads);
     lc.dynamicSmemBytes = c.smem;
     lc.stream = s;
@@ -2044,6 +2046,8 @@ std::unique_ptr<BatchPlanBase> batch_plan_build(tdic_ctx* ctx, int n, tdic_pair*
     TDIC_CUDA_TRY(cudaMemcpyAsync(b->d_maps.ptr, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice, s));
     TDIC_CUDA_TRY(cudaStreamSynchronize(s));  // host staging vectors go out of scope
     with_opt_deg<T>(b->opt, b->deg, [&](auto O, auto D) { batch_configs<decltype(O)::value, decltype(D)::value, T>(*b, ctx); });
+    b->num_sms = ctx->num_sms;
+    b->sms = ctx->num_sms;
     return b;
 }
 
@@ -2160,6 +2164,12 @@ void batch_finish(BatchPlanBase* p, int32_t* computed, int* err, cudaStream_t s)
 tdic_grid_out batch_outputs(BatchPlanBase* p, int job) {
     if (auto* b = dynamic_cast<BatchPlan<double>*>(p)) return b->outs[job];
     return static_cast<BatchPlan<float>*>(p)->outs[job];
+}
+
+void batch_set_sms(BatchPlanBase* p, int sms) {
+    if (auto* b = dynamic_cast<BatchPlan<double>*>(p)) { b->sms = sms <= 0 ? b->num_sms : std::min(sms, b->num_sms); return; }
+    auto* f = static_cast<BatchPlan<float>*>(p);
+    f->sms = sms <= 0 ? f->num_sms : std::min(sms, f->num_sms);
 }
 
 void batch_grid(BatchPlanBase* p, int job, int32_t* gw, int32_t* gh) {

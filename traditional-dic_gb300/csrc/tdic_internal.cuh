@@ -224,5 +224,6 @@ void batch_launch(BatchPlanBase* p, int config, cudaStream_t s);
 void batch_finish(BatchPlanBase* p, int32_t* computed, int* err, cudaStream_t s);
 tdic_grid_out batch_outputs(BatchPlanBase* p, int job);
 void batch_grid(BatchPlanBase* p, int job, int32_t* gw, int32_t* gh);
+void batch_set_sms(BatchPlanBase* p, int sms);
 
 }  // namespace tdic

@@ -74,16 +74,23 @@ class Server:
     """Continuous-batching request loop on one device (see the module docstring).
 
     memory_budget: device bytes the admitted (prepared or running) requests may hold.
-    max_batch: requests per batched launch (at most 512)."""
+    max_batch: requests per batched launch (at most 512).
+    reserve_sms: SMs the propagation leaves to the preparation of the next requests (the
+    propagation holds its SMs until it ends; default a tenth of the device)."""
 
-    def __init__(self, context: S.Context | None = None, memory_budget: int = 48 << 30, max_batch: int = 64):
+    def __init__(self, context: S.Context | None = None, memory_budget: int = 48 << 30, max_batch: int = 64,
+                 reserve_sms: int | None = None):
         import torch
         self.ctx = context or S.default_context()
         self.memory_budget = int(memory_budget)
         self.max_batch = max(1, min(512, int(max_batch)))
+        n_sms = torch.cuda.get_device_properties(self.ctx.device).multi_processor_count
+        reserve = max(1, n_sms // 10) if reserve_sms is None else max(0, int(reserve_sms))
+        self._sms = max(1, n_sms - reserve)
         self._torch = torch
-        self._prep = torch.cuda.Stream()
-        self._main = torch.cuda.Stream()
+        self._prep = torch.cuda.Stream()   # uploads, prefilter, seed selection
+        self._main = torch.cuda.Stream()   # batched propagation
+        self._copy = torch.cuda.Stream()   # results of finished batches to host
         self._queue: collections.deque[Request] = collections.deque()
         self._cv = threading.Condition()
         self._stop = False
@@ -151,6 +158,7 @@ class Server:
         self._prep.synchronize()  # the group's pairs and seeds are ready
         batch = S.Batch(self.ctx, [p.pair for p in group], [p.cfg for p in group], [p.seed for p in group],
                         [p.req.roi for p in group], stream=self._main)
+        batch.set_sms(self._sms)
         start = self._torch.cuda.Event(enable_timing=True)
         done = self._torch.cuda.Event(enable_timing=True)
         start.record(self._main)
@@ -164,13 +172,13 @@ class Server:
         t0 = time.perf_counter()
         self.stats["propagate"].append(start.elapsed_time(done) / 1e3)
         try:
-            pc = batch.finish(stream=self._main)
+            pc = batch.finish(stream=self._copy)
             for j, p in enumerate(group):
                 p.req.batch_size = len(group)
                 if pc[j] == 0:
                     self._complete(p.req, S._empty_result())
                 else:
-                    out = batch.outputs(j, stream=self._main)
+                    out = batch.outputs(j, stream=self._copy)
                     self._complete(p.req, {k: out[k] for k in S.RESULT_KEYS + S.EXTRA_KEYS})
         except BaseException as exc:  # every request of the batch learns of the failure
             for p in group:
@@ -194,11 +202,12 @@ class Server:
                     self._cv.wait(0.05)
                     continue
             progressed = False
-            # the running batch first: its results free memory and the GPU for the next one
+            finished = None
             if inflight is not None and inflight[2].query():
-                self._collect(inflight)
-                inflight = None
+                finished, inflight = inflight, None
                 progressed = True
+            # the next batch goes to the GPU first; the finished one's results are copied out
+            # (on the copy stream) while it runs
             if inflight is None and ready:
                 try:
                     inflight, ready = self._launch(ready)
@@ -209,6 +218,8 @@ class Server:
                         self._held -= p.bytes
                     ready = []
                 progressed = True
+            if finished is not None:
+                self._collect(finished)
             # admit and prepare queued requests while the budget allows (overlaps the batch)
             while len(ready) < self.max_batch:
                 with self._cv:

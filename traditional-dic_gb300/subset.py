@@ -498,6 +498,11 @@ class Batch:
         self.ctx.check(self.ctx.lib.tdic_batch_tune(self.handle, _stream_ptr(stream)))
         return self.config()
 
+    def set_sms(self, sms: int) -> None:
+        """Launch on ``sms`` SMs' worth of blocks (0: the whole device), leaving the rest to
+        other streams."""
+        self.ctx.check(self.ctx.lib.tdic_batch_set_sms(self.handle, int(sms)))
+
     def config(self) -> tuple:
         g, k = C.c_int32(), C.c_int32()
         self.ctx.check(self.ctx.lib.tdic_batch_config(self.handle, C.byref(g), C.byref(k)))
