@@ -265,6 +265,24 @@ tdic_status tdic_subset_prepare(tdic_ctx* ctx, const void* reference, const void
                                 const uint8_t* roi, const tdic_config* cfg, void* stream,
                                 tdic_pair** pair_out, tdic_seed* seed_out);
 
+/* Least-squares strain of 2D point displacements: dic::compute_least_squares_strain_2d
+ * (src/postprocess/least_squares_strain.cpp:11-78), as bound by
+ * _traditional_dic.postprocess.compute_least_squares_strain_2d.  points, displacement: host
+ * arrays of n (x, y) / (u, v) pairs; neighbours within `radius` (the point included) give a plane
+ * fit of u and v; green_lagrange != 0 gives E = (H + H^T + H^T H) / 2, else the small strain.
+ * Points or displacements that are not finite are left out (valid = 0, sample_count = 0).
+ * TDIC_INVALID_ARG unless radius > 0 and min_samples >= 3 (the reference's check). */
+typedef struct tdic_ls_strain {
+    double du_dx, du_dy, dv_dx, dv_dy;
+    double exx, eyy, exy;
+    int32_t sample_count;
+    uint8_t valid;
+    uint8_t pad_[3];
+} tdic_ls_strain;
+tdic_status tdic_ls_strain_2d(tdic_ctx* ctx, const double* points, const double* displacement,
+                              int32_t n, double radius, int32_t min_samples, int32_t green_lagrange,
+                              tdic_ls_strain* out, void* stream);
+
 /* Whole pybind path: _traditional_dic.subset.compute (bind_subset.cpp:253-315) ->
  * SubsetDIC::compute (subset_dic.cpp:39-105).  Host images of `dtype`, host roi (NULL = full
  * image), host outputs of grid_w*grid_h entries.  *n_points = grid_w*grid_h, or 0 for the

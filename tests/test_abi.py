@@ -14,7 +14,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def header_functions():
     text = open(os.path.join(ROOT, "include", "tdic_gb300.h")).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(tdic_[a-z_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(tdic_[a-z_0-9]+)\s*\(", text)))
 
 
 def test_library_exports_every_declared_symbol(pkg):

@@ -1,0 +1,109 @@
+"""Least-squares strain and result files.  CPU: the numpy oracle of
+compute_least_squares_strain_2d on exact fields and degenerate neighbourhoods, and the result
+writers.  GPU: the device strain against the oracle."""
+import csv
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+import strain_oracle as SO  # noqa: E402
+
+
+def _grid(nx=12, ny=9, step=5.0):
+    ys, xs = np.mgrid[0:ny, 0:nx].astype(np.float64) * step
+    return np.column_stack([xs.ravel() + 3.0, ys.ravel() + 7.0])
+
+
+def test_oracle_recovers_an_affine_field():
+    pts = _grid()
+    h = np.array([[0.01, -0.004], [0.003, 0.02]])
+    disp = 0.7 + pts @ h.T
+    r = SO.least_squares_strain_2d(pts, disp, radius=12.0, min_samples=6, green_lagrange=True)
+    assert r["valid"].all()
+    for k, want in (("du_dx", h[0, 0]), ("du_dy", h[0, 1]), ("dv_dx", h[1, 0]), ("dv_dy", h[1, 1])):
+        assert np.allclose(r[k], want, atol=1e-12), k
+    e = 0.5 * (h + h.T + h.T @ h)
+    assert np.allclose(r["exx"], e[0, 0]) and np.allclose(r["eyy"], e[1, 1]) and np.allclose(r["exy"], e[0, 1])
+    small = SO.least_squares_strain_2d(pts, disp, radius=12.0, green_lagrange=False)
+    assert np.allclose(small["exy"], 0.5 * (h[0, 1] + h[1, 0]))
+    # a centre point has the 5-px neighbours within 12 px: (2*2+1)^2 - 4 corners
+    assert r["sample_count"][5 * 12 + 5] == 21
+
+
+def test_oracle_degenerate_neighbourhoods():
+    line = np.column_stack([np.arange(10.0) * 4.0, np.full(10, 2.0)])
+    disp = np.column_stack([0.1 + 0.02 * line[:, 0], -0.3 + 0.0 * line[:, 0]])
+    r = SO.least_squares_strain_2d(line, disp, radius=9.0, min_samples=3)
+    inner = r["valid"]
+    assert inner.any()
+    assert np.allclose(r["du_dx"][inner], 0.02) and np.all(r["du_dy"][inner] == 0.0)  # basic solution
+    few = SO.least_squares_strain_2d(line, disp, radius=3.0, min_samples=3)
+    assert not few["valid"].any() and np.all(few["sample_count"] == 1)
+    bad = disp.copy()
+    bad[4, 0] = np.nan
+    r = SO.least_squares_strain_2d(line, bad, radius=9.0, min_samples=3)
+    assert not r["valid"][4] and r["sample_count"][4] == 0 and r["sample_count"][3] == 4
+
+
+def test_result_writers(tmp_path, pkg):
+    from traditional_dic_gb300 import results
+    n = 7
+    res = {k: np.linspace(-1, 1, n) for k in results.SUBSET_COLUMNS[:-1]}
+    res["valid"] = np.array([1, 0, 1, 1, 0, 1, 1], bool)
+    results.save_subset_csv(res, tmp_path / "d.csv")
+    rows = list(csv.reader(open(tmp_path / "d.csv")))
+    assert rows[0] == results.SUBSET_COLUMNS and len(rows) == n + 1
+    assert float(rows[3][2]) == res["u"][2] and rows[2][-1] == "0"
+    results.write_stats(res, tmp_path / "s.json")
+    st = json.loads(open(tmp_path / "s.json").read())
+    assert st["total_points"] == 7 and st["valid_points"] == 5 and "znssd_mean" in st
+    assert st["u_mean"] == pytest.approx(res["u"][res["valid"]].mean())
+
+
+def _compare(got, want, tol=1e-9):
+    assert np.array_equal(got.valid, want["valid"])
+    assert np.array_equal(got.sample_count, want["sample_count"])
+    v = want["valid"]
+    for k in ("du_dx", "du_dy", "dv_dx", "dv_dy", "exx", "eyy", "exy"):
+        assert np.allclose(got[k][v], want[k][v], rtol=0, atol=tol), k
+
+
+@pytest.mark.gpu
+def test_gpu_strain_matches_oracle_on_points(gpu_ctx):
+    from traditional_dic_gb300 import postprocess as P
+    rng = np.random.default_rng(5)
+    pts = rng.uniform(0, 300, (4000, 2))
+    disp = np.column_stack([0.5 + 0.003 * pts[:, 0] - 0.001 * pts[:, 1], -0.2 + 0.002 * pts[:, 1]])
+    disp += rng.normal(0, 0.01, disp.shape)
+    disp[::97] = np.nan
+    for green in (True, False):
+        got = P.compute_least_squares_strain_2d(pts, disp, 15.0, 6, green, context=gpu_ctx)
+        _compare(got, SO.least_squares_strain_2d(pts, disp, 15.0, 6, green))
+    line = np.column_stack([np.arange(20.0) * 3.0, np.full(20, 5.0)])
+    ld = np.column_stack([0.02 * line[:, 0], 0.01 * line[:, 0]])
+    _compare(P.compute_least_squares_strain_2d(line, ld, 7.0, 3, True, context=gpu_ctx),
+             SO.least_squares_strain_2d(line, ld, 7.0, 3, True))
+    with pytest.raises(Exception, match="radius must be positive"):
+        P.compute_least_squares_strain_2d(pts, disp, 0.0, 6, context=gpu_ctx)
+
+
+@pytest.mark.gpu
+def test_gpu_strain_of_a_subset_result(gpu_ctx, workload0, tmp_path):
+    import __graft_entry__ as G
+    from traditional_dic_gb300 import postprocess as P, subset as S
+    res = S.compute(workload0.reference, workload0.deformed, G.WORKLOAD0_CONFIG, context=gpu_ctx)
+    v = res["valid"]
+    pts = np.column_stack([res["x"][v], res["y"][v]])
+    disp = np.column_stack([res["u"][v], res["v"][v]])
+    got = P.compute_least_squares_strain_2d(pts, disp, 25.0, 6, True, context=gpu_ctx)
+    _compare(got, SO.least_squares_strain_2d(pts, disp, 25.0, 6, True))
+    # the imposed field: du/dx = 0.001, dv/dy = -0.0005
+    assert abs(np.median(got.du_dx[got.valid]) - 0.001) < 2e-4
+    assert abs(np.median(got.dv_dy[got.valid]) + 0.0005) < 2e-4
+    P.save_least_squares_strain_csv(tmp_path / "strain.csv", pts, disp, radius=25.0, context=gpu_ctx)
+    rows = list(csv.reader(open(tmp_path / "strain.csv")))
+    assert rows[0][:3] == ["x", "y", "du_dx"] and len(rows) == len(pts) + 1

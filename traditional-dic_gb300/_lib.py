@@ -56,6 +56,12 @@ GRID_FIELDS = ("x", "y", "u", "v", "du_dx", "du_dy", "dv_dx", "dv_dy", "correlat
                "iterations", "converged")
 
 
+class LsStrain(C.Structure):
+    _fields_ = [("du_dx", C.c_double), ("du_dy", C.c_double), ("dv_dx", C.c_double), ("dv_dy", C.c_double),
+                ("exx", C.c_double), ("eyy", C.c_double), ("exy", C.c_double), ("sample_count", C.c_int32),
+                ("valid", C.c_uint8), ("pad_", C.c_uint8 * 3)]
+
+
 class GridOut(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in GRID_FIELDS]
 
@@ -93,6 +99,8 @@ SIGNATURES = {
     "tdic_batch_destroy": (None, [C.c_void_p]),
     "tdic_subset_prepare": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int, C.c_void_p,
                                       C.POINTER(Config), C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(Seed)]),
+    "tdic_ls_strain_2d": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.c_int32,
+                                    C.c_void_p, C.c_void_p]),
     "tdic_select_seed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Config),
                                    C.POINTER(Seed), C.c_void_p]),
     "tdic_subset_compute": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int, C.c_void_p,

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libtdic_gb300.so")
-SOURCES = ["api.cu", "prefilter.cu", "hotpath.cu", "seed.cu"]
+SOURCES = ["api.cu", "prefilter.cu", "hotpath.cu", "seed.cu", "strain.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xcompiler", "-Wall", "-I", os.path.join(HERE, "..", "include")]

@@ -843,6 +843,20 @@ static void prepare_impl(tdic_ctx* ctx, const void* reference, const void* defor
     *pair_out = pair;
 }
 
+tdic_status tdic_ls_strain_2d(tdic_ctx* ctx, const double* points, const double* displacement, int32_t n,
+                              double radius, int32_t min_samples, int32_t green_lagrange, tdic_ls_strain* out,
+                              void* stream) {
+    return guarded(ctx, [&] {
+        TDIC_REQUIRE(n >= 0, TDIC_INVALID_ARG, "points and displacement must both be Nx2 matrices");
+        TDIC_REQUIRE(radius > 0.0 && min_samples >= 3, TDIC_INVALID_ARG,
+                     "radius must be positive and min_samples at least 3");
+        if (n == 0) return;
+        TDIC_REQUIRE(points && displacement && out, TDIC_INVALID_ARG, "null argument");
+        TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
+        ls_strain_2d(ctx, points, displacement, n, radius, min_samples, green_lagrange ? 1 : 0, out, pick(ctx, stream));
+    });
+}
+
 tdic_status tdic_subset_prepare(tdic_ctx* ctx, const void* reference, const void* deformed, int32_t width,
                                 int32_t height, tdic_dtype dtype, const uint8_t* roi, const tdic_config* cfg,
                                 void* stream, tdic_pair** pair_out, tdic_seed* seed_out) {

@@ -202,6 +202,10 @@ private:
 void integer_search_batch(tdic_ctx* ctx, tdic_pair* lazy, const tdic_config& cfg, const int* cx, const int* cy,
                           int n, SearchResult* out, cudaStream_t s);
 
+// Least-squares strain (strain.cu).
+void ls_strain_2d(tdic_ctx* ctx, const double* points, const double* disp, int n, double radius, int min_samples,
+                  int green, tdic_ls_strain* out, cudaStream_t s);
+
 // Batched propagation (several image pairs in one persistent launch).  Grid points of a batch
 // are tagged with their job in queue items: 22 bits of point, the job above.
 constexpr int kMaxBatchJobs = 512;
