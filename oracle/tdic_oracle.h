@@ -12,10 +12,14 @@
  * network) is absent.  Parity of this restatement is pinned by (a) a numpy transcription of
  * the reference's FFT deconvolution (bspline.cpp:191-244), (b) a numpy transcription of the
  * reference's local polynomial block evaluation (bspline.cpp:96-175, 320-340), (c) analytic
- * known-answer tests (linear-image reproduction, pure translation / affine recovery) and
- * (d) numpy.linalg for the 6x6 solves.  No reference-produced golden vectors exist for this
- * path (tests/data/f0/subset_ring/baseline.npz is missing from the reference checkout), so
- * parity at the level of Eigen's LDLT / kissfft rounding (~1e-15 relative) is unpinned.
+ * known-answer tests (linear-image reproduction, pure translation / affine recovery),
+ * (d) numpy.linalg for the 6x6 solves and (e) golden vectors (tests/golden/subset_icgn_256.npz)
+ * from an independent numpy transcription of the prefilter and of solve_first_order_znssd
+ * (tests/golden/make_golden.py), which this library reproduces to 1e-10 (coefficients) and
+ * 1e-8 px (per-POI parameters, identical iteration counts and statuses).  No reference-produced
+ * golden vectors exist for this path (tests/data/f0/subset_ring/baseline.npz is missing from
+ * the reference checkout) and the reference cannot be run here, so parity at the level of
+ * Eigen's LDLT / kissfft rounding (~1e-15 relative) is unpinned.
  */
 #ifndef TDIC_ORACLE_H
 #define TDIC_ORACLE_H

@@ -1,0 +1,82 @@
+"""Golden vectors (tests/golden/subset_icgn_256.npz, made by tests/golden/make_golden.py from an
+independent numpy transcription of the reference): the C++ oracle (CPU) and the GPU path (GPU)
+must reproduce the B-spline coefficients and the per-POI ICGN results."""
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "subset_icgn_256.npz")
+P_TOL = 1e-8       # px and displacement gradients between two FP64 transcriptions
+U_TOL = 1e-3       # px, FP32-mixed path
+
+
+@pytest.fixture(scope="module")
+def golden():
+    d = np.load(GOLDEN)
+    return {k: d[k] for k in d.files}
+
+
+def _inputs(g):
+    pois = g["pois"]
+    xy = pois[:, :2]
+    p0 = np.zeros((len(pois), 6))
+    p0[:, :2] = pois[:, 2:4]
+    return xy, p0
+
+
+def _config(g, make_default):
+    degree, border, radius, max_iter, thr = g["settings"]
+    cfg = make_default()
+    cfg.subset_radius, cfg.max_iterations, cfg.convergence_threshold = int(radius), int(max_iter), float(thr)
+    cfg.degree, cfg.border, cfg.optimizer = int(degree), int(border), 0
+    return cfg
+
+
+def _check(got_p, got_iters, got_status, got_corr, g, tol):
+    res = g["results"]
+    want_p, want_corr = res[:, :6], res[:, 6]
+    want_iters, want_status = res[:, 7].astype(int), res[:, 8].astype(int)
+    assert np.array_equal(np.asarray(got_status, int), want_status)
+    ok = want_status == 0
+    assert np.array_equal(np.asarray(got_iters, int)[ok], want_iters[ok])
+    assert np.max(np.abs(got_p[ok] - want_p[ok])) <= tol
+    assert np.max(np.abs(np.asarray(got_corr)[ok] - want_corr[ok])) <= max(tol, 1e-9)
+
+
+def test_oracle_coefficients_match_golden(oracle, golden):
+    degree, border = int(golden["settings"][0]), int(golden["settings"][1])
+    coef = oracle.prefilter(golden["deformed"].astype(np.float32), degree, border, True)
+    assert np.max(np.abs(coef[:40, :40] - golden["coef_crop"])) <= 1e-10
+
+
+def test_oracle_icgn_matches_golden(oracle, golden):
+    cfg = _config(golden, oracle.default_config)
+    coef = oracle.prefilter(golden["deformed"].astype(np.float32), cfg.degree, cfg.border, True)
+    xy, p0 = _inputs(golden)
+    ref = golden["reference"].astype(np.float32)
+    r = oracle.solve_pois(ref, coef, cfg, xy, p0, gradients=oracle.reference_gradient(ref))
+    _check(r["p"], r["iterations"], r["status"], r["correlation"], golden, P_TOL)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [1, 0])
+def test_gpu_icgn_matches_golden(gpu_ctx, golden, precision):
+    from traditional_dic_gb300 import subset as S, _lib as L
+    cfg = _config(golden, L.default_config)
+    cfg.precision = precision
+    pair = S.Pair(gpu_ctx, golden["reference"], golden["deformed"], degree=cfg.degree, border=cfg.border,
+                  precision=precision)
+    coef = pair.coefficients()
+    if precision == 1:
+        assert np.max(np.abs(coef[:40, :40] - golden["coef_crop"])) <= 1e-10
+    xy, p0 = _inputs(golden)
+    r = S.solve_pois(gpu_ctx, pair, cfg, xy, p0)
+    if precision == 1:
+        _check(r["p"], r["iterations"], r["status"], r["correlation"], golden, P_TOL)
+    else:
+        res = golden["results"]
+        ok = res[:, 8] == 0
+        assert np.array_equal(r["status"], res[:, 8].astype(int))
+        assert np.max(np.abs(r["p"][ok, :2] - res[ok, :2])) <= U_TOL
+    pair.close()
