@@ -1,0 +1,60 @@
+"""The multi-GPU mode of bench.py runs independent replicas (the propagation does not shard:
+each image pair's grid depends on its own seed chain).  Its host-side harness - process group,
+barrier, max / sum over ranks - is checked here with two gloo ranks on the CPU, each solving
+its own small job with the oracle."""
+import os
+import socket
+import sys
+
+import numpy as np
+import torch.multiprocessing as mp
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, world, port, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import bench
+    import oracle as O
+    w, r, local, pg = bench.dist_setup(None)
+    assert (w, r, local) == (world, rank, rank) and pg is not None
+    # a rank-local job: one translated image pair, solved by the oracle
+    rng = np.random.default_rng(100 + rank)
+    img = rng.uniform(0, 255, (48, 48))
+    from scipy.ndimage import gaussian_filter, shift
+    ref = gaussian_filter(img, 1.5).astype(np.float32)
+    de = shift(ref.astype(np.float64), (0.0, 0.3 + 0.1 * rank), order=3, mode="nearest").astype(np.float32)
+    cfg = O.default_config()
+    cfg.subset_radius, cfg.degree = 8, 3
+    coef = O.prefilter(de, 3, 3, True)
+    res = O.solve_pois(ref, coef, cfg, [[24.0, 24.0]], [[0.0] * 6], gradients=O.reference_gradient(ref))
+    bench.barrier(pg)
+    u_max = bench.max_over_ranks(pg, float(res["p"][0, 0]))
+    n_sum = bench.sum_over_ranks(pg, float(res["converged"].sum()))
+    out[rank] = (float(res["p"][0, 0]), u_max, n_sum)
+    pg.destroy_process_group()
+
+
+def test_two_replicas_on_gloo(oracle):
+    world, port = 2, _free_port()
+    ctx = mp.get_context("spawn")
+    out = ctx.Manager().dict()
+    procs = [ctx.Process(target=_rank, args=(r, world, port, out)) for r in range(world)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+    assert all(p.exitcode == 0 for p in procs), [p.exitcode for p in procs]
+    u = [out[r][0] for r in range(world)]
+    assert abs(u[0] - 0.3) < 0.02 and abs(u[1] - 0.4) < 0.02       # each rank solved its own job
+    assert all(out[r][1] == max(u) for r in range(world))           # max over ranks
+    assert all(out[r][2] == 2.0 for r in range(world))              # sum over ranks
