@@ -32,7 +32,7 @@ typedef enum tdic_status {
     TDIC_OOM = 2,           /* device allocation or admission refused */
     TDIC_CUDA_ERROR = 3,    /* a CUDA runtime error (message in tdic_last_error) */
     TDIC_TIMEOUT = 4,       /* a bounded device-side wait ran out */
-    TDIC_UNSUPPORTED = 5    /* second-order / SSD / masked routes: not on this path */
+    TDIC_UNSUPPORTED = 5    /* a route or size this path does not cover (masked subsets, ...) */
 } tdic_status;
 
 typedef enum tdic_dtype { TDIC_U8 = 0, TDIC_U16 = 1, TDIC_F32 = 2, TDIC_F64 = 3 } tdic_dtype;
@@ -90,10 +90,12 @@ typedef struct tdic_poi_in {
     double confidence;
 } tdic_poi_in;
 
-/* dic::Displacement2D (include/dic/core/result.hpp:32-51, first-order part) plus additive
- * fields: zncc = clamp(1 - correlation / 2, -1, 1), iterations (loop bodies entered),
- * converged (strict |dp| < threshold; the reference's `valid` is also true when the loop ran
- * out with a finite correlation, icgn.cpp:620-625). */
+/* dic::Displacement2D (include/dic/core/result.hpp:32-51) plus additive fields: zncc =
+ * clamp(1 - correlation / 2, -1, 1), iterations (loop bodies entered), converged (strict
+ * |dp| < threshold; the reference's `valid` is also true when the loop ran out with a finite
+ * correlation, icgn.cpp:620-625).  correlation is the ZNSSD, or the SSD when criterion = 0.
+ * q: the second-order terms d2u_dx2, d2u_dxdy, d2u_dy2, d2v_dx2, d2v_dxdy, d2v_dy2 (zero for
+ * the first-order shape function). */
 typedef struct tdic_poi_out {
     double p[6];
     double correlation;
@@ -103,6 +105,7 @@ typedef struct tdic_poi_out {
     int8_t valid;
     int8_t converged;
     int8_t pad_;
+    double q[6];
 } tdic_poi_out;
 
 /* The propagation seed (PropagationSeed, reliability_propagation.hpp:35-39). */
@@ -116,12 +119,15 @@ typedef struct tdic_seed {
 
 /* Structure-of-arrays grid result, one entry per grid point i = gy * grid_w + gx
  * (reliability_propagation.cpp:159-176); keys of results_to_dict (bind_subset.cpp:102-153)
- * plus zncc / iterations / converged / status.  Any pointer may be NULL (not written). */
+ * plus zncc / iterations / converged / status and the second-order terms of
+ * dic::Displacement2D (result.hpp:42-47; zero for the first-order shape function).  Any
+ * pointer may be NULL (not written). */
 typedef struct tdic_grid_out {
     double* x; double* y; double* u; double* v;
     double* du_dx; double* du_dy; double* dv_dx; double* dv_dy;
     double* correlation; double* zncc;
     uint8_t* valid; int8_t* status; int32_t* iterations; uint8_t* converged;
+    double* d2u_dx2; double* d2u_dxdy; double* d2u_dy2; double* d2v_dx2; double* d2v_dxdy; double* d2v_dy2;
 } tdic_grid_out;
 
 typedef struct tdic_ctx tdic_ctx;
@@ -170,9 +176,10 @@ tdic_status tdic_pair_coefficients(tdic_pair* pair, void* host_out, size_t bytes
 tdic_status tdic_reference_gradient(tdic_pair* pair, double* gx, double* gy);
 
 /* Batched per-POI solve: replaces SubsetSolver::solve_with_interpolators (subset_solver.hpp:
- * 39-65 -> icgn.cpp:384-405 -> icgn.cpp:446-627, or forward_gauss_newton.cpp:188-399 when
- * cfg->optimizer == 1) for n POIs at once.  in/out are host or device pointers per `memory`.
- * Only first-order ZNSSD routes are on this path (others: TDIC_UNSUPPORTED). */
+ * 39-65 -> icgn.cpp:384-405, forward_gauss_newton.cpp:117-142) for n POIs at once, on the
+ * route of cfg: optimizer (0 ICGN, 1 FGN) x shape_order (1, 2) x criterion (1 ZNSSD, 0 SSD),
+ * i.e. icgn.cpp:446-627, 832-988, 1168-1362, 1576-1739 and forward_gauss_newton.cpp:188-399,
+ * 622-794, 1069-1297, 1540-1739.  in/out are host or device pointers per `memory`. */
 tdic_status tdic_solve_pois(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cfg,
                             const tdic_poi_in* in, int32_t n, tdic_poi_out* out,
                             tdic_memory memory, void* stream);

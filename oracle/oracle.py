@@ -7,7 +7,9 @@ The C library restates the reference's hot path (lbd-hfut/Traditional-DIC): B-sp
 prefilter (src/interpolation/bspline.cpp:369-392), reference gradient cache
 (src/subset/seed/reliability_propagation.cpp:84-112), first-order ZNSSD ICGN
 (src/subset/solver/icgn.cpp:446-627), first-order FGN
-(src/subset/solver/forward_gauss_newton.cpp:188-399), reliability-guided propagation
+(src/subset/solver/forward_gauss_newton.cpp:188-399), their SSD and second-order variants
+(icgn.cpp:832-988, 1168-1362, 1576-1739; forward_gauss_newton.cpp:622-794, 1069-1297, 1540-1739),
+reliability-guided propagation
 (reliability_propagation.cpp:130-394), integer search (src/initialization/integer_search.cpp:333-432)
 and seed selection (src/subset/seed/seed_selector.cpp:146-317).
 """
@@ -44,12 +46,17 @@ class Config(C.Structure):
 
 class PoiResult(C.Structure):
     _fields_ = [("p", C.c_double * 6), ("correlation", C.c_double), ("iterations", C.c_int32),
-                ("status", C.c_int8), ("valid", C.c_int8), ("converged", C.c_int8), ("pad_", C.c_int8)]
+                ("status", C.c_int8), ("valid", C.c_int8), ("converged", C.c_int8), ("pad_", C.c_int8),
+                ("q", C.c_double * 6)]
+
+
+SECOND_ORDER_KEYS = ("d2u_dx2", "d2u_dxdy", "d2u_dy2", "d2v_dx2", "d2v_dxdy", "d2v_dy2")
 
 
 class GridOut(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in ("x", "y", "u", "v", "du_dx", "du_dy", "dv_dx", "dv_dy",
-                                           "correlation", "valid", "status", "iterations", "converged")]
+                                           "correlation", "valid", "status", "iterations", "converged")
+                + SECOND_ORDER_KEYS]
 
 
 class Seed(C.Structure):
@@ -171,7 +178,8 @@ def reference_gradient(image):
 
 
 def solve_pois(reference, coeffs, cfg, xy, p0, confidence0=None, gradients=None, degree=None, border=None):
-    """Per-POI first-order ZNSSD solve (ICGN or FGN per cfg.optimizer). Returns a dict of arrays."""
+    """Per-POI solve: ICGN or FGN (cfg.optimizer), first or second order (cfg.shape_order), ZNSSD or
+    SSD (cfg.criterion 1 / 0).  Returns a dict of arrays; "q" holds the six second-order terms."""
     cfg = as_config(cfg)
     ref = _img(reference)
     h, w = ref.shape
@@ -190,12 +198,13 @@ def solve_pois(reference, coeffs, cfg, xy, p0, confidence0=None, gradients=None,
     rc = lib().orc_solve_pois(_ptr(ref), w, h, _ptr(gx), _ptr(gy), _ptr(c), d, b, C.byref(cfg), n,
                               _ptr(xy), _ptr(p0), _ptr(conf), C.addressof(out))
     if rc != 0:
-        raise NotImplementedError("only first-order ZNSSD routes are restated")
+        raise ValueError("degree must be 1, 3 or 5")
     arr = np.frombuffer(out, dtype=np.dtype([("p", "<f8", 6), ("correlation", "<f8"), ("iterations", "<i4"),
                                               ("status", "i1"), ("valid", "i1"), ("converged", "i1"),
-                                              ("pad", "i1")]), count=n)
-    return {"p": arr["p"].copy(), "correlation": arr["correlation"].copy(), "iterations": arr["iterations"].copy(),
-            "status": arr["status"].copy(), "valid": arr["valid"].astype(bool), "converged": arr["converged"].astype(bool)}
+                                              ("pad", "i1"), ("q", "<f8", 6)]), count=n)
+    return {"p": arr["p"].copy(), "q": arr["q"].copy(), "correlation": arr["correlation"].copy(),
+            "iterations": arr["iterations"].copy(), "status": arr["status"].copy(),
+            "valid": arr["valid"].astype(bool), "converged": arr["converged"].astype(bool)}
 
 
 def grid_dims(w, h, spacing):
@@ -205,7 +214,7 @@ def grid_dims(w, h, spacing):
 
 
 def _alloc_grid(n):
-    arrs = {k: np.zeros(n, np.float64) for k in GRID_KEYS}
+    arrs = {k: np.zeros(n, np.float64) for k in GRID_KEYS + SECOND_ORDER_KEYS}
     arrs["valid"] = np.zeros(n, np.uint8)
     arrs["status"] = np.zeros(n, np.int8)
     arrs["iterations"] = np.zeros(n, np.int32)
@@ -215,7 +224,7 @@ def _alloc_grid(n):
 
 
 def _finish_grid(arrs, n):
-    out = {k: arrs[k][:n] for k in GRID_KEYS}
+    out = {k: arrs[k][:n] for k in GRID_KEYS + SECOND_ORDER_KEYS}
     out["valid"] = arrs["valid"][:n].astype(bool)
     out["zncc"] = np.clip(1.0 - 0.5 * out["correlation"], -1.0, 1.0)
     out["iterations"] = arrs["iterations"][:n]

@@ -219,30 +219,32 @@ void form_coefficients(const float* img, int w, int h, int d, int border, bool e
 }
 
 // ---------------------------------------------------------------------------------------
-// 6x6 LDLT with symmetric diagonal pivoting and sign tracking: restates the factorisation
-// semantics relied on by icgn.cpp:538-542 / forward_gauss_newton.cpp:354-358
-// (info() == Success, isPositive()) and the pseudo-inverse solve of D.
+// N x N LDLT (N = 6 first order, 12 second order) with symmetric diagonal pivoting and sign
+// tracking: restates the factorisation semantics relied on by icgn.cpp:538-542, 1262-1266 /
+// forward_gauss_newton.cpp:354-358, 1249-1253 (info() == Success, isPositive()) and the
+// pseudo-inverse solve of D.
 // ---------------------------------------------------------------------------------------
-struct Ldlt6 {
-    double m[6][6];
-    int t[6];
+template <int N>
+struct LdltN {
+    double m[N][N];
+    int t[N];
     enum { kZero, kPosSemi, kNegSemi, kIndef } sign = kZero;
     bool ok = true;
 
-    void factor(const double a[6][6]) {
-        for (int i = 0; i < 6; ++i) for (int j = 0; j < 6; ++j) m[i][j] = a[i][j];
+    void factor(const double a[N][N]) {
+        for (int i = 0; i < N; ++i) for (int j = 0; j < N; ++j) m[i][j] = a[i][j];
         sign = kZero;
         ok = true;
         bool found_zero = false;
-        double temp[6];
-        for (int k = 0; k < 6; ++k) {
+        double temp[N];
+        for (int k = 0; k < N; ++k) {
             int big = k;
             double bigv = std::fabs(m[k][k]);
-            for (int i = k + 1; i < 6; ++i) if (std::fabs(m[i][i]) > bigv) { bigv = std::fabs(m[i][i]); big = i; }
+            for (int i = k + 1; i < N; ++i) if (std::fabs(m[i][i]) > bigv) { bigv = std::fabs(m[i][i]); big = i; }
             t[k] = big;
             if (big != k) {
                 for (int j = 0; j < k; ++j) std::swap(m[k][j], m[big][j]);
-                for (int i = big + 1; i < 6; ++i) std::swap(m[i][k], m[i][big]);
+                for (int i = big + 1; i < N; ++i) std::swap(m[i][k], m[i][big]);
                 std::swap(m[k][k], m[big][big]);
                 for (int i = k + 1; i < big; ++i) { const double tmp = m[i][k]; m[i][k] = m[big][i]; m[big][i] = tmp; }
             }
@@ -251,7 +253,7 @@ struct Ldlt6 {
                 double s = 0.0;
                 for (int j = 0; j < k; ++j) s += m[k][j] * temp[j];
                 m[k][k] -= s;
-                for (int i = k + 1; i < 6; ++i) {
+                for (int i = k + 1; i < N; ++i) {
                     double si = 0.0;
                     for (int j = 0; j < k; ++j) si += m[i][j] * temp[j];
                     m[i][k] -= si;
@@ -261,14 +263,14 @@ struct Ldlt6 {
             const bool pivot_valid = std::fabs(akk) > 0.0;
             if (k == 0 && !pivot_valid) {
                 sign = kZero;
-                for (int j = 0; j < 6; ++j) { t[j] = j; for (int i = 0; i < 6; ++i) m[i][j] = 0.0; }
+                for (int j = 0; j < N; ++j) { t[j] = j; for (int i = 0; i < N; ++i) m[i][j] = 0.0; }
                 ok = true;
                 return;
             }
             if (pivot_valid) {
-                for (int i = k + 1; i < 6; ++i) m[i][k] /= akk;
+                for (int i = k + 1; i < N; ++i) m[i][k] /= akk;
             } else {
-                for (int i = k + 1; i < 6; ++i) ok = ok && (m[i][k] == 0.0);
+                for (int i = k + 1; i < N; ++i) ok = ok && (m[i][k] == 0.0);
             }
             if (found_zero && pivot_valid) ok = false;
             else if (!pivot_valid) found_zero = true;
@@ -279,15 +281,68 @@ struct Ldlt6 {
     }
     bool success() const { return ok; }
     bool positive() const { return sign == kPosSemi || sign == kZero; }
-    void solve(const double b[6], double x[6]) const {
-        for (int i = 0; i < 6; ++i) x[i] = b[i];
-        for (int k = 0; k < 6; ++k) std::swap(x[k], x[t[k]]);
-        for (int i = 0; i < 6; ++i) { double s = x[i]; for (int j = 0; j < i; ++j) s -= m[i][j] * x[j]; x[i] = s; }
-        for (int i = 0; i < 6; ++i) { const double dd = m[i][i]; x[i] = std::fabs(dd) > DBL_MIN ? x[i] / dd : 0.0; }
-        for (int i = 5; i >= 0; --i) { double s = x[i]; for (int j = i + 1; j < 6; ++j) s -= m[j][i] * x[j]; x[i] = s; }
-        for (int k = 5; k >= 0; --k) std::swap(x[k], x[t[k]]);
+    void solve(const double b[N], double x[N]) const {
+        for (int i = 0; i < N; ++i) x[i] = b[i];
+        for (int k = 0; k < N; ++k) std::swap(x[k], x[t[k]]);
+        for (int i = 0; i < N; ++i) { double s = x[i]; for (int j = 0; j < i; ++j) s -= m[i][j] * x[j]; x[i] = s; }
+        for (int i = 0; i < N; ++i) { const double dd = m[i][i]; x[i] = std::fabs(dd) > DBL_MIN ? x[i] / dd : 0.0; }
+        for (int i = N - 1; i >= 0; --i) { double s = x[i]; for (int j = i + 1; j < N; ++j) s -= m[j][i] * x[j]; x[i] = s; }
+        for (int k = N - 1; k >= 0; --k) std::swap(x[k], x[t[k]]);
     }
 };
+using Ldlt6 = LdltN<6>;
+
+// ---------------------------------------------------------------------------------------
+// 6x6 LU with full pivoting: the Eigen::FullPivLU semantics used by the second-order
+// inverse-compositional update (icgn.cpp:325-329): pivot = first largest |entry| of the
+// remaining corner in column-major order, rank counted against 6 * DBL_EPSILON * |largest
+// pivot|, inverse = the solve of the identity (row permutation, unit-lower and upper
+// substitution, column permutation).
+// ---------------------------------------------------------------------------------------
+bool fullpiv_inverse6(const double a[6][6], double inv[6][6]) {
+    double lu[6][6];
+    for (int i = 0; i < 6; ++i) for (int j = 0; j < 6; ++j) lu[i][j] = a[i][j];
+    int rt[6], ct[6];
+    int nonzero = 6;
+    double maxpivot = 0.0;
+    for (int k = 0; k < 6; ++k) {
+        int br = k, bc = k;
+        double big = -1.0;
+        for (int c = k; c < 6; ++c)
+            for (int r = k; r < 6; ++r)
+                if (std::fabs(lu[r][c]) > big) { big = std::fabs(lu[r][c]); br = r; bc = c; }
+        if (big == 0.0) {
+            nonzero = k;
+            for (int i = k; i < 6; ++i) { rt[i] = i; ct[i] = i; }
+            break;
+        }
+        if (big > maxpivot) maxpivot = big;
+        rt[k] = br; ct[k] = bc;
+        if (br != k) for (int j = 0; j < 6; ++j) std::swap(lu[k][j], lu[br][j]);
+        if (bc != k) for (int i = 0; i < 6; ++i) std::swap(lu[i][k], lu[i][bc]);
+        for (int r = k + 1; r < 6; ++r) lu[r][k] /= lu[k][k];
+        for (int c = k + 1; c < 6; ++c)
+            for (int r = k + 1; r < 6; ++r) lu[r][c] -= lu[r][k] * lu[k][c];
+    }
+    int rank = 0;
+    const double thr = maxpivot * (6.0 * DBL_EPSILON);
+    for (int i = 0; i < nonzero; ++i) rank += std::fabs(lu[i][i]) > thr ? 1 : 0;
+    if (rank != 6) return false;
+    int q[6] = {0, 1, 2, 3, 4, 5};
+    for (int k = 0; k < 6; ++k) std::swap(q[k], q[ct[k]]);
+    for (int col = 0; col < 6; ++col) {
+        double c[6] = {0, 0, 0, 0, 0, 0};
+        c[col] = 1.0;
+        for (int k = 0; k < 6; ++k) std::swap(c[k], c[rt[k]]);
+        for (int i = 0; i < 6; ++i) for (int j = 0; j < i; ++j) c[i] -= lu[i][j] * c[j];
+        for (int i = 5; i >= 0; --i) {
+            for (int j = i + 1; j < 6; ++j) c[i] -= lu[i][j] * c[j];
+            c[i] /= lu[i][i];
+        }
+        for (int i = 0; i < 6; ++i) inv[q[i]][col] = c[i];
+    }
+    return true;
+}
 
 bool finite6(const double* p) { for (int i = 0; i < 6; ++i) if (!std::isfinite(p[i])) return false; return true; }
 
@@ -315,6 +370,60 @@ void compose_warp(const double* p, const double* dp, double* pn) {
     pn[5] = dp[5] + p[4] * dp[3] + p[5] * (1.0 + dp[5]);
 }
 
+// Second-order shape function: parameters [u, v, ux, uy, vx, vy, uxx, uxy, uyy, vxx, vxy, vyy].
+
+// The 6x6 warp matrix G'(p) (icgn.cpp:196-261): maps [1, x, y, x^2, xy, y^2] to
+// [x', y', 1, x'^2, x'y', y'^2] up to second order.
+void warp_matrix2(const double* p, double G[6][6]) {
+    const double u = p[0], v = p[1], ux = p[2], uy = p[3], vx = p[4], vy = p[5];
+    const double uxx = p[6], uxy = p[7], uyy = p[8], vxx = p[9], vxy = p[10], vyy = p[11];
+    for (int i = 0; i < 6; ++i) for (int j = 0; j < 6; ++j) G[i][j] = 0.0;
+    G[0][0] = u; G[0][1] = 1.0 + ux; G[0][2] = uy; G[0][3] = 0.5 * uxx; G[0][4] = uxy; G[0][5] = 0.5 * uyy;
+    G[1][0] = v; G[1][1] = vx; G[1][2] = 1.0 + vy; G[1][3] = 0.5 * vxx; G[1][4] = vxy; G[1][5] = 0.5 * vyy;
+    G[2][0] = 1.0;
+    G[3][0] = u * u; G[3][1] = 2.0 * u * (1.0 + ux); G[3][2] = 2.0 * u * uy;
+    G[3][3] = 1.0 + 2.0 * ux + ux * ux + u * uxx; G[3][4] = 2.0 * (uy + ux * uy + u * uxy); G[3][5] = uy * uy + u * uyy;
+    G[4][0] = u * v; G[4][1] = v + u * vx + v * ux; G[4][2] = u + u * vy + v * uy;
+    G[4][3] = vx + ux * vx + 0.5 * (u * vxx + v * uxx);
+    G[4][4] = 1.0 + vy + ux + ux * vy + uy * vx + u * vxy + v * uxy;
+    G[4][5] = uy + uy * vy + 0.5 * (u * vyy + v * uyy);
+    G[5][0] = v * v; G[5][1] = 2.0 * v * vx; G[5][2] = 2.0 * v * (1.0 + vy);
+    G[5][3] = vx * vx + v * vxx; G[5][4] = 2.0 * (vx + vx * vy + v * vxy); G[5][5] = 1.0 + 2.0 * vy + vy * vy + v * vyy;
+}
+
+// icgn.cpp:308-357: G'(p_new) = G'(p) * G'(dp)^-1 * P^-1, parameters read back from rows 0 and 1
+// (extract_from_warp_matrix, icgn.cpp:265-287); additive p - dp when G'(dp) is not invertible.
+void ic_update2(const double* p, const double* dp, double* out) {
+    double Gp[6][6], Gd[6][6], Gi[6][6];
+    warp_matrix2(p, Gp);
+    warp_matrix2(dp, Gd);
+    if (!fullpiv_inverse6(Gd, Gi)) { for (int i = 0; i < 12; ++i) out[i] = p[i] - dp[i]; return; }
+    double X[2][6];
+    for (int r = 0; r < 2; ++r)
+        for (int c = 0; c < 6; ++c) { double s = 0.0; for (int k = 0; k < 6; ++k) s += Gp[r][k] * Gi[k][c]; X[r][c] = s; }
+    // P^-1 moves columns (0, 1, 2) to (1, 2, 0): new column 0 = old 2, 1 = old 0, 2 = old 1.
+    double N[2][6];
+    for (int r = 0; r < 2; ++r) { N[r][0] = X[r][2]; N[r][1] = X[r][0]; N[r][2] = X[r][1]; for (int c = 3; c < 6; ++c) N[r][c] = X[r][c]; }
+    out[0] = N[0][0]; out[2] = N[0][1] - 1.0; out[3] = N[0][2]; out[6] = 2.0 * N[0][3]; out[7] = N[0][4]; out[8] = 2.0 * N[0][5];
+    out[1] = N[1][0]; out[4] = N[1][1]; out[5] = N[1][2] - 1.0; out[9] = 2.0 * N[1][3]; out[10] = N[1][4]; out[11] = 2.0 * N[1][5];
+}
+
+// forward_gauss_newton.cpp:1025-1053: W(p) o W(dp) to second order in (lx, ly), first in dp.
+void compose_warp2(const double* p, const double* dp, double* pn) {
+    pn[0] = dp[0] + p[0] + p[2] * dp[0] + p[3] * dp[1];
+    pn[1] = dp[1] + p[1] + p[4] * dp[0] + p[5] * dp[1];
+    pn[2] = dp[2] + p[2] * (1.0 + dp[2]) + p[3] * dp[4] + p[6] * dp[0] + p[7] * dp[1];
+    pn[3] = dp[3] + p[2] * dp[3] + p[3] * (1.0 + dp[5]) + p[7] * dp[0] + p[8] * dp[1];
+    pn[4] = dp[4] + p[4] * (1.0 + dp[2]) + p[5] * dp[4] + p[9] * dp[0] + p[10] * dp[1];
+    pn[5] = dp[5] + p[4] * dp[3] + p[5] * (1.0 + dp[5]) + p[10] * dp[0] + p[11] * dp[1];
+    pn[6] = dp[6] + p[2] * dp[6] + p[3] * dp[9] + p[6] * (1.0 + 2.0 * dp[2]) + 2.0 * p[7] * dp[4];
+    pn[7] = dp[7] + p[2] * dp[7] + p[3] * dp[10] + p[6] * dp[3] + p[7] * (1.0 + dp[2] + dp[5]) + p[8] * dp[4];
+    pn[8] = dp[8] + p[2] * dp[8] + p[3] * dp[11] + p[7] * dp[3] + p[8] * (1.0 + 2.0 * dp[5]);
+    pn[9] = dp[9] + p[4] * dp[6] + p[5] * dp[9] + p[9] * (1.0 + 2.0 * dp[2]) + 2.0 * p[10] * dp[4];
+    pn[10] = dp[10] + p[4] * dp[7] + p[5] * dp[10] + p[9] * dp[3] + p[10] * (1.0 + dp[2] + dp[5]) + p[11] * dp[4];
+    pn[11] = dp[11] + p[4] * dp[8] + p[5] * dp[11] + p[10] * dp[3] + p[11] * (1.0 + 2.0 * dp[5]);
+}
+
 struct GradSource {  // reference_gradient_at, icgn.cpp:55-71 / central difference icgn.cpp:42-53
     const float* img; int w, h;
     const double* gx; const double* gy;
@@ -327,19 +436,58 @@ struct GradSource {  // reference_gradient_at, icgn.cpp:55-71 / central differen
     }
 };
 
-struct SolverCfg { int radius; int max_iter; double thr; int optimizer; };
+struct SolverCfg {
+    int radius; int max_iter; double thr; int optimizer;
+    int order = 1;      // shape function: 1 first order (6 parameters), 2 second order (12)
+    bool ssd = false;   // objective: SSD instead of ZNSSD
+};
 
 void init_result(orc_poi_result& r, const double* p0, double conf) {
     // icgn.cpp:454-462: u, v from the initial guess, gradients default to zero.
-    for (int i = 0; i < 6; ++i) r.p[i] = 0.0;
+    for (int i = 0; i < 6; ++i) { r.p[i] = 0.0; r.q[i] = 0.0; }
     r.p[0] = p0[0]; r.p[1] = p0[1];
     r.correlation = conf;
     r.iterations = 0; r.status = kInvalidInput; r.valid = 0; r.converged = 0; r.pad_ = 0;
 }
 
-struct Sample { double lx, ly, ref, refn, sd[6]; };
+// Shape-function terms of one sample: m = [1, lx, ly, lx^2/2, lx ly, ly^2/2]; the steepest
+// descent row for gradient (a, b) is [a m0, b m0, a m1, a m2, b m1, b m2, a m3, a m4, a m5,
+// b m3, b m4, b m5] (icgn.cpp:142-165 second order; the first six for first order).
+template <int NP>
+void sd_row(double a, double b, double lx, double ly, double* sd) {
+    sd[0] = a; sd[1] = b; sd[2] = a * lx; sd[3] = a * ly; sd[4] = b * lx; sd[5] = b * ly;
+    if constexpr (NP == 12) {
+        const double x2 = lx * lx * 0.5, y2 = ly * ly * 0.5, xy = lx * ly;
+        sd[6] = a * x2; sd[7] = a * xy; sd[8] = a * y2; sd[9] = b * x2; sd[10] = b * xy; sd[11] = b * y2;
+    }
+}
 
-// icgn.cpp:446-627
+// Warped sample position (icgn.cpp:555-558 first order; warp_second_order icgn.cpp:167-182).
+template <int NP>
+void warp_pt(int cx, int cy, double lx, double ly, const double* p, double& wx, double& wy) {
+    if constexpr (NP == 6) {
+        wx = static_cast<double>(cx) + lx + p[0] + p[2] * lx + p[3] * ly;
+        wy = static_cast<double>(cy) + ly + p[1] + p[4] * lx + p[5] * ly;
+    } else {
+        const double x2 = lx * lx * 0.5, y2 = ly * ly * 0.5, xy = lx * ly;
+        wx = static_cast<double>(cx) + lx + p[0] + p[2] * lx + p[3] * ly + p[6] * x2 + p[7] * xy + p[8] * y2;
+        wy = static_cast<double>(cy) + ly + p[1] + p[4] * lx + p[5] * ly + p[9] * x2 + p[10] * xy + p[11] * y2;
+    }
+}
+
+void store_params(orc_poi_result& res, const double* p, int np) {
+    for (int k = 0; k < 6; ++k) res.p[k] = p[k];
+    for (int k = 0; k < 6; ++k) res.q[k] = np == 12 ? p[6 + k] : 0.0;
+}
+
+struct Sample { double lx, ly, ref, refn, sd[12]; };
+
+// ICGN, first order (NP = 6) or second order (NP = 12), ZNSSD or SSD:
+//   icgn.cpp:446-627   first-order ZNSSD      icgn.cpp:832-988    first-order SSD
+//   icgn.cpp:1168-1362 second-order ZNSSD     icgn.cpp:1576-1739  second-order SSD
+// SSD drops the normalisation (raw residual f - g, Hessian and gradient without the 2/|f|
+// factors); second order needs 12 samples and updates through the warp matrix (ic_update2).
+template <int NP>
 orc_poi_result solve_icgn(const float* ref, int w, int h, const GradSource& gs, const Spline& sp,
                           const SolverCfg& cfg, double px, double py, const double* p0, double conf) {
     orc_poi_result res;
@@ -359,37 +507,41 @@ orc_poi_result solve_icgn(const float* ref, int w, int h, const GradSource& gs, 
             q.ref = static_cast<double>(ref[static_cast<std::size_t>(cy + dy) * w + cx + dx]);
             double gx, gy;
             gs.at(cx + dx, cy + dy, gx, gy);
-            q.sd[0] = gx; q.sd[1] = gy; q.sd[2] = gx * q.lx; q.sd[3] = gx * q.ly; q.sd[4] = gy * q.lx; q.sd[5] = gy * q.ly;
+            sd_row<NP>(gx, gy, q.lx, q.ly, q.sd);
             mean += q.ref;
             s.push_back(q);
         }
-    if (s.size() < 6) return res;
+    if (s.size() < static_cast<std::size_t>(NP)) return res;
     const double N = static_cast<double>(s.size());
-    mean /= N;
-    double norm = 0.0;
-    for (const auto& q : s) { const double df = q.ref - mean; norm += df * df; }
-    norm = std::sqrt(norm);
-    if (norm <= kEps) { res.status = kNumericalFailure; return res; }
-    for (auto& q : s) q.refn = (q.ref - mean) / norm;
-    double H[6][6] = {};
-    for (const auto& q : s) for (int i = 0; i < 6; ++i) for (int j = 0; j < 6; ++j) H[i][j] += q.sd[i] * q.sd[j];
-    const double hs = 2.0 / (norm * norm);
-    for (int i = 0; i < 6; ++i) for (int j = 0; j < 6; ++j) H[i][j] *= hs;
-    Ldlt6 f;
+    double norm = 1.0;
+    if (!cfg.ssd) {
+        mean /= N;
+        norm = 0.0;
+        for (const auto& q : s) { const double df = q.ref - mean; norm += df * df; }
+        norm = std::sqrt(norm);
+        if (norm <= kEps) { res.status = kNumericalFailure; return res; }
+        for (auto& q : s) q.refn = (q.ref - mean) / norm;
+    }
+    double H[NP][NP] = {};
+    for (const auto& q : s) for (int i = 0; i < NP; ++i) for (int j = 0; j < NP; ++j) H[i][j] += q.sd[i] * q.sd[j];
+    if (!cfg.ssd) {
+        const double hs = 2.0 / (norm * norm);
+        for (int i = 0; i < NP; ++i) for (int j = 0; j < NP; ++j) H[i][j] *= hs;
+    }
+    LdltN<NP> f;
     f.factor(H);
     if (!f.success() || !f.positive()) { res.status = kNumericalFailure; return res; }
-    double p[6];
-    for (int i = 0; i < 6; ++i) p[i] = p0[i];
+    double p[NP];
+    for (int i = 0; i < NP; ++i) p[i] = i < 6 ? p0[i] : 0.0;
     double corr = kInf;
     bool converged = false;
     std::vector<double> g(s.size());
-    int it = 0;
-    for (; it < cfg.max_iter; ++it) {
+    for (int it = 0; it < cfg.max_iter; ++it) {
         res.iterations = it + 1;
         double gm = 0.0;
         for (std::size_t i = 0; i < s.size(); ++i) {
-            const double wx = static_cast<double>(cx) + s[i].lx + p[0] + p[2] * s[i].lx + p[3] * s[i].ly;
-            const double wy = static_cast<double>(cy) + s[i].ly + p[1] + p[4] * s[i].lx + p[5] * s[i].ly;
+            double wx, wy;
+            warp_pt<NP>(cx, cy, s[i].lx, s[i].ly, p, wx, wy);
             if (!(wx >= 0.0 && wy >= 0.0 && wx <= static_cast<double>(w - 1) && wy <= static_cast<double>(h - 1))) {
                 res.status = kInvalidInput;
                 return res;
@@ -397,33 +549,46 @@ orc_poi_result solve_icgn(const float* ref, int w, int h, const GradSource& gs, 
             g[i] = sp.value(wx, wy);
             gm += g[i];
         }
-        gm /= N;
-        double gn = 0.0;
-        for (double v : g) { const double df = v - gm; gn += df * df; }
-        gn = std::sqrt(gn);
-        if (gn <= kEps) { res.status = kNumericalFailure; return res; }
-        double grad[6] = {0, 0, 0, 0, 0, 0};
+        double grad[NP] = {};
         corr = 0.0;
-        for (std::size_t i = 0; i < s.size(); ++i) {
-            const double nd = s[i].refn - (g[i] - gm) / gn;
-            for (int k = 0; k < 6; ++k) grad[k] += nd * s[i].sd[k];
-            corr += nd * nd;
+        if (!cfg.ssd) {
+            gm /= N;
+            double gn = 0.0;
+            for (double v : g) { const double df = v - gm; gn += df * df; }
+            gn = std::sqrt(gn);
+            if (gn <= kEps) { res.status = kNumericalFailure; return res; }
+            for (std::size_t i = 0; i < s.size(); ++i) {
+                const double nd = s[i].refn - (g[i] - gm) / gn;
+                for (int k = 0; k < NP; ++k) grad[k] += nd * s[i].sd[k];
+                corr += nd * nd;
+            }
+            for (int k = 0; k < NP; ++k) grad[k] *= 2.0 / norm;
+        } else {
+            for (std::size_t i = 0; i < s.size(); ++i) {
+                const double rd = s[i].ref - g[i];
+                for (int k = 0; k < NP; ++k) grad[k] += rd * s[i].sd[k];
+                corr += rd * rd;
+            }
         }
-        for (int k = 0; k < 6; ++k) grad[k] *= 2.0 / norm;
-        double dp[6];
+        double dp[NP];
         f.solve(grad, dp);
-        for (int k = 0; k < 6; ++k) dp[k] = -dp[k];
-        if (!finite6(dp)) { res.status = kNumericalFailure; return res; }
+        for (int k = 0; k < NP; ++k) dp[k] = -dp[k];
+        bool fin = true;
+        for (int k = 0; k < NP; ++k) fin = fin && std::isfinite(dp[k]);
+        if (!fin) { res.status = kNumericalFailure; return res; }
         double dn = 0.0;
-        for (int k = 0; k < 6; ++k) dn += dp[k] * dp[k];
+        for (int k = 0; k < NP; ++k) dn += dp[k] * dp[k];
         dn = std::sqrt(dn);
-        double pn[6];
-        ic_update(p, dp, pn);
-        for (int k = 0; k < 6; ++k) p[k] = pn[k];
-        if (!finite6(p)) { res.status = kNumericalFailure; return res; }
+        double pn[NP];
+        if constexpr (NP == 6) ic_update(p, dp, pn);
+        else ic_update2(p, dp, pn);
+        for (int k = 0; k < NP; ++k) p[k] = pn[k];
+        fin = true;
+        for (int k = 0; k < NP; ++k) fin = fin && std::isfinite(p[k]);
+        if (!fin) { res.status = kNumericalFailure; return res; }
         if (dn < cfg.thr) { converged = true; break; }
     }
-    for (int k = 0; k < 6; ++k) res.p[k] = p[k];
+    store_params(res, p, NP);
     res.correlation = corr;
     res.converged = converged ? 1 : 0;
     if (!converged && std::isfinite(corr)) converged = true;
@@ -432,7 +597,13 @@ orc_poi_result solve_icgn(const float* ref, int w, int h, const GradSource& gs, 
     return res;
 }
 
-// forward_gauss_newton.cpp:188-399 (sd: 44-60, compose: 64-76)
+// Forward Gauss-Newton, first or second order, ZNSSD or SSD:
+//   forward_gauss_newton.cpp:188-399   first-order ZNSSD (step cap 0.5)
+//   forward_gauss_newton.cpp:622-794   first-order SSD (cap 0.35; converges on the uncapped norm)
+//   forward_gauss_newton.cpp:1069-1297 second-order ZNSSD (LM term 1e-4 max diag, cap 0.5)
+//   forward_gauss_newton.cpp:1540-1739 second-order SSD (LM term, cap 0.35)
+// SD from the deformed spline gradient through dW/dz at the sample (:44-60, :986-1019).
+template <int NP>
 orc_poi_result solve_fgn(const float* ref, int w, int h, const Spline& sp, const SolverCfg& cfg,
                          double px, double py, const double* p0, double conf) {
     orc_poi_result res;
@@ -452,16 +623,20 @@ orc_poi_result solve_fgn(const float* ref, int w, int h, const Spline& sp, const
             mean += q.ref;
             s.push_back(q);
         }
-    if (s.size() < 6) return res;
+    if (s.size() < static_cast<std::size_t>(NP)) return res;
     const double N = static_cast<double>(s.size());
-    mean /= N;
-    double norm = 0.0;
-    for (const auto& q : s) { const double df = q.ref - mean; norm += df * df; }
-    norm = std::sqrt(norm);
-    if (norm <= kEps) { res.status = kNumericalFailure; return res; }
-    for (auto& q : s) q.refn = (q.ref - mean) / norm;
-    double p[6];
-    for (int i = 0; i < 6; ++i) p[i] = p0[i];
+    double norm = 1.0;
+    if (!cfg.ssd) {
+        mean /= N;
+        norm = 0.0;
+        for (const auto& q : s) { const double df = q.ref - mean; norm += df * df; }
+        norm = std::sqrt(norm);
+        if (norm <= kEps) { res.status = kNumericalFailure; return res; }
+        for (auto& q : s) q.refn = (q.ref - mean) / norm;
+    }
+    const double cap = cfg.ssd ? 0.35 : 0.5;
+    double p[NP];
+    for (int i = 0; i < NP; ++i) p[i] = i < 6 ? p0[i] : 0.0;
     double corr = kInf;
     bool converged = false;
     std::vector<double> g(s.size());
@@ -469,8 +644,8 @@ orc_poi_result solve_fgn(const float* ref, int w, int h, const Spline& sp, const
         res.iterations = it + 1;
         double gm = 0.0;
         for (std::size_t i = 0; i < s.size(); ++i) {
-            const double wx = static_cast<double>(cx) + s[i].lx + p[0] + p[2] * s[i].lx + p[3] * s[i].ly;
-            const double wy = static_cast<double>(cy) + s[i].ly + p[1] + p[4] * s[i].lx + p[5] * s[i].ly;
+            double wx, wy;
+            warp_pt<NP>(cx, cy, s[i].lx, s[i].ly, p, wx, wy);
             if (!(wx >= 0.0 && wy >= 0.0 && wx <= static_cast<double>(w - 1) && wy <= static_cast<double>(h - 1))) {
                 res.status = kInvalidInput;
                 return res;
@@ -478,49 +653,80 @@ orc_poi_result solve_fgn(const float* ref, int w, int h, const Spline& sp, const
             g[i] = sp.value(wx, wy);
             gm += g[i];
         }
-        gm /= N;
-        double gn = 0.0;
-        for (double v : g) { const double df = v - gm; gn += df * df; }
-        gn = std::sqrt(gn);
-        if (gn <= kEps) { res.status = kNumericalFailure; return res; }
-        double H[6][6] = {};
-        double grad[6] = {0, 0, 0, 0, 0, 0};
+        double gn = 1.0;
+        if (!cfg.ssd) {
+            gm /= N;
+            gn = 0.0;
+            for (double v : g) { const double df = v - gm; gn += df * df; }
+            gn = std::sqrt(gn);
+            if (gn <= kEps) { res.status = kNumericalFailure; return res; }
+        }
+        double H[NP][NP] = {};
+        double grad[NP] = {};
         corr = 0.0;
         for (std::size_t i = 0; i < s.size(); ++i) {
-            const double wx = static_cast<double>(cx) + s[i].lx + p[0] + p[2] * s[i].lx + p[3] * s[i].ly;
-            const double wy = static_cast<double>(cy) + s[i].ly + p[1] + p[4] * s[i].lx + p[5] * s[i].ly;
+            const double lx = s[i].lx, ly = s[i].ly;
+            double wx, wy;
+            warp_pt<NP>(cx, cy, lx, ly, p, wx, wy);
             double gx, gy;
             sp.gradient(wx, wy, gx, gy);
-            const double gxe = gx * (1.0 + p[2]) + gy * p[4];
-            const double gye = gx * p[3] + gy * (1.0 + p[5]);
-            const double sd[6] = {gxe, gye, gxe * s[i].lx, gxe * s[i].ly, gye * s[i].lx, gye * s[i].ly};
-            const double nd = s[i].refn - (g[i] - gm) / gn;
-            for (int a = 0; a < 6; ++a) { for (int b = 0; b < 6; ++b) H[a][b] += sd[a] * sd[b]; grad[a] += nd * sd[a]; }
+            double gxe, gye;
+            if constexpr (NP == 6) {
+                gxe = gx * (1.0 + p[2]) + gy * p[4];
+                gye = gx * p[3] + gy * (1.0 + p[5]);
+            } else {
+                const double a00 = 1.0 + p[2] + p[6] * lx + p[7] * ly;
+                const double a01 = p[3] + p[7] * lx + p[8] * ly;
+                const double a10 = p[4] + p[9] * lx + p[10] * ly;
+                const double a11 = 1.0 + p[5] + p[10] * lx + p[11] * ly;
+                gxe = gx * a00 + gy * a10;
+                gye = gx * a01 + gy * a11;
+            }
+            double sd[NP];
+            sd_row<NP>(gxe, gye, lx, ly, sd);
+            const double nd = cfg.ssd ? s[i].ref - g[i] : s[i].refn - (g[i] - gm) / gn;
+            for (int a = 0; a < NP; ++a) { for (int b = 0; b < NP; ++b) H[a][b] += sd[a] * sd[b]; grad[a] += nd * sd[a]; }
             corr += nd * nd;
         }
-        const double hs = 2.0 / (norm * norm);
-        for (int a = 0; a < 6; ++a) for (int b = 0; b < 6; ++b) H[a][b] *= hs;
-        for (int a = 0; a < 6; ++a) grad[a] *= 2.0 / norm;
-        Ldlt6 f;
+        if (!cfg.ssd) {
+            const double hs = 2.0 / (norm * norm);
+            for (int a = 0; a < NP; ++a) for (int b = 0; b < NP; ++b) H[a][b] *= hs;
+            for (int a = 0; a < NP; ++a) grad[a] *= 2.0 / norm;
+        }
+        if constexpr (NP == 12) {  // forward_gauss_newton.cpp:1242-1245, 1682-1685
+            double dmax = H[0][0];
+            for (int a = 1; a < NP; ++a) dmax = std::max(dmax, H[a][a]);
+            const double lambda = 1e-4 * dmax;
+            for (int a = 0; a < NP; ++a) H[a][a] += lambda;
+        }
+        LdltN<NP> f;
         f.factor(H);
         if (!f.success() || !f.positive()) { res.status = kNumericalFailure; return res; }
-        double dp[6];
+        double dp[NP];
         f.solve(grad, dp);
-        if (!finite6(dp)) { res.status = kNumericalFailure; return res; }
+        bool fin = true;
+        for (int k = 0; k < NP; ++k) fin = fin && std::isfinite(dp[k]);
+        if (!fin) { res.status = kNumericalFailure; return res; }
         double dn = 0.0;
-        for (int k = 0; k < 6; ++k) dn += dp[k] * dp[k];
+        for (int k = 0; k < NP; ++k) dn += dp[k] * dp[k];
         dn = std::sqrt(dn);
-        if (dn > 0.5) {  // forward_gauss_newton.cpp:367-371
-            for (int k = 0; k < 6; ++k) dp[k] *= 0.5 / dn;
-            dn = 0.5;
+        const double dn_raw = dn;
+        if (dn > cap) {  // forward_gauss_newton.cpp:367-371, 763-767, 1260-1264, 1700-1705
+            for (int k = 0; k < NP; ++k) dp[k] *= cap / dn;
+            dn = cap;
         }
-        double pn[6];
-        compose_warp(p, dp, pn);
-        for (int k = 0; k < 6; ++k) p[k] = pn[k];
-        if (!finite6(p)) { res.status = kNumericalFailure; return res; }
-        if (dn < cfg.thr) { converged = true; break; }
+        // first-order SSD tests convergence on the norm before the cap (:764, :774)
+        const double dn_test = (NP == 6 && cfg.ssd) ? dn_raw : dn;
+        double pn[NP];
+        if constexpr (NP == 6) compose_warp(p, dp, pn);
+        else compose_warp2(p, dp, pn);
+        for (int k = 0; k < NP; ++k) p[k] = pn[k];
+        fin = true;
+        for (int k = 0; k < NP; ++k) fin = fin && std::isfinite(p[k]);
+        if (!fin) { res.status = kNumericalFailure; return res; }
+        if (dn_test < cfg.thr) { converged = true; break; }
     }
-    for (int k = 0; k < 6; ++k) res.p[k] = p[k];
+    store_params(res, p, NP);
     res.correlation = corr;
     res.converged = converged ? 1 : 0;
     if (!converged && std::isfinite(corr)) converged = true;
@@ -529,10 +735,22 @@ orc_poi_result solve_fgn(const float* ref, int w, int h, const Spline& sp, const
     return res;
 }
 
+// ICGNSolver / ForwardGaussNewtonSolver::solve_with_interpolators dispatch (icgn.cpp:384-405,
+// forward_gauss_newton.cpp:117-142).
 orc_poi_result solve_one(const float* ref, int w, int h, const GradSource& gs, const Spline& sp,
                          const SolverCfg& cfg, double px, double py, const double* p0, double conf) {
-    if (cfg.optimizer == 1) return solve_fgn(ref, w, h, sp, cfg, px, py, p0, conf);
-    return solve_icgn(ref, w, h, gs, sp, cfg, px, py, p0, conf);
+    if (cfg.optimizer == 1)
+        return cfg.order == 2 ? solve_fgn<12>(ref, w, h, sp, cfg, px, py, p0, conf)
+                              : solve_fgn<6>(ref, w, h, sp, cfg, px, py, p0, conf);
+    return cfg.order == 2 ? solve_icgn<12>(ref, w, h, gs, sp, cfg, px, py, p0, conf)
+                          : solve_icgn<6>(ref, w, h, gs, sp, cfg, px, py, p0, conf);
+}
+
+SolverCfg solver_cfg(const orc_config& c) {
+    SolverCfg s{c.subset_radius, c.max_iterations, c.convergence_threshold, c.optimizer};
+    s.order = c.shape_order == 2 ? 2 : 1;
+    s.ssd = c.criterion == 0;
+    return s;
 }
 
 bool all_finite7(const orc_poi_result& r) {  // reliability_propagation.cpp:67-75
@@ -557,6 +775,8 @@ void clear_grid(orc_grid_out* out, int gw, int gh, int step) {
         out->status[i] = kInvalidInput;
         out->iterations[i] = 0;
         out->converged[i] = 0;
+        double* d2[6] = {out->d2u_dx2, out->d2u_dxdy, out->d2u_dy2, out->d2v_dx2, out->d2v_dxdy, out->d2v_dy2};
+        for (double* a : d2) if (a) a[i] = 0.0;
     }
 }
 
@@ -568,6 +788,8 @@ void store(orc_grid_out* out, int idx, const orc_poi_result& r) {
     out->status[idx] = r.status;
     out->iterations[idx] = r.iterations;
     out->converged[idx] = r.converged;
+    double* d2[6] = {out->d2u_dx2, out->d2u_dxdy, out->d2u_dy2, out->d2v_dx2, out->d2v_dxdy, out->d2v_dy2};
+    for (int k = 0; k < 6; ++k) if (d2[k]) d2[k][idx] = r.q[k];
 }
 
 bool roi_valid(const uint8_t* roi, int w, int h, int x, int y) {
@@ -594,7 +816,7 @@ int propagate(const float* ref, int w, int h, const uint8_t* roi, const GradSour
     const int gw = (w + step - 1) / step, gh = (h + step - 1) / step;
     clear_grid(out, gw, gh, step);
     const int radius = c.subset_radius;
-    const SolverCfg scfg{c.subset_radius, c.max_iterations, c.convergence_threshold, c.optimizer};
+    const SolverCfg scfg = solver_cfg(c);
     std::vector<uint8_t> calc(static_cast<std::size_t>(gw) * gh, 0);
     const double cutoff_corr = c.propagation_max_znssd, cutoff_disp = static_cast<double>(step);
     int computed = 0;
@@ -608,7 +830,7 @@ int propagate(const float* ref, int w, int h, const uint8_t* roi, const GradSour
     if (!roi_valid(roi, w, h, sx, sy)) return 0;
     const int sidx = gys * gw + gxs;
     orc_poi_result aligned;
-    for (int k = 0; k < 6; ++k) aligned.p[k] = seed.p[k];
+    for (int k = 0; k < 6; ++k) { aligned.p[k] = seed.p[k]; aligned.q[k] = 0.0; }
     aligned.correlation = seed.correlation;
     aligned.iterations = 0; aligned.status = kSuccess; aligned.valid = 1; aligned.converged = 0;
     if (sx != sxr || sy != syr) {
@@ -1017,7 +1239,9 @@ bool select_seed(const float* ref, const float* def, int w, int h, const uint8_t
         sp.init(lazy.data(), w, h, c.degree, border);
     }
     GradSource gs{ref, w, h, nullptr, nullptr};  // reference interpolator is empty -> central differences
-    const SolverCfg scfg{std::max(1, c.sp_subset_radius), std::max(0, c.sp_max_iterations), c.sp_convergence_threshold, 0};
+    // subset_initializer.cpp:165-177: the subpixel solver is first-order ICGN with the configured objective
+    SolverCfg scfg{std::max(1, c.sp_subset_radius), std::max(0, c.sp_max_iterations), c.sp_convergence_threshold, 0};
+    scfg.ssd = c.criterion == 0;
     SeedEval best;
     bool found = false;
     for (const auto& cd : cands) {
@@ -1028,7 +1252,7 @@ bool select_seed(const float* ref, const float* def, int w, int h, const uint8_t
         double p[6] = {iu, iv, 0, 0, 0, 0};
         double conf = znssd_from_zncc(iz), quality = conf;
         if (refine) {  // subset_initializer.cpp:152-204
-            const orc_poi_result r = solve_icgn(ref, w, h, gs, sp, scfg, cd.first, cd.second, p, conf);
+            const orc_poi_result r = solve_icgn<6>(ref, w, h, gs, sp, scfg, cd.first, cd.second, p, conf);
             if (r.valid && r.status == kSuccess) {
                 for (int k = 0; k < 6; ++k) p[k] = r.p[k];
                 conf = r.correlation;
@@ -1113,11 +1337,11 @@ void orc_reference_gradient(const float* img, int w, int h, double* gx, double* 
 int orc_solve_pois(const float* ref, int w, int h, const double* ref_gx, const double* ref_gy,
                    const double* coeffs, int d, int border, const orc_config* cfg,
                    int n, const double* xy, const double* p0, const double* conf0, orc_poi_result* out) {
-    if (cfg->shape_order != 1 || cfg->criterion != 1 || !valid_degree(d)) return -1;
+    if (!valid_degree(d)) return -1;
     Spline sp;
     sp.init(coeffs, w, h, d, border);
     GradSource gs{ref, w, h, ref_gx, ref_gy};
-    const SolverCfg scfg{cfg->subset_radius, cfg->max_iterations, cfg->convergence_threshold, cfg->optimizer};
+    const SolverCfg scfg = solver_cfg(*cfg);
     for (int i = 0; i < n; ++i)
         out[i] = solve_one(ref, w, h, gs, sp, scfg, xy[2 * i], xy[2 * i + 1], p0 + 6 * i, conf0 ? conf0[i] : 0.0);
     return 0;

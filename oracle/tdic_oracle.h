@@ -70,12 +70,13 @@ typedef struct orc_config {
  * 0 Success, 1 NotConverged, 2 InvalidInput, 3 NumericalFailure. */
 typedef struct orc_poi_result {
     double p[6];          /* u, v, du_dx, du_dy, dv_dx, dv_dy */
-    double correlation;   /* ZNSSD at the pre-update parameters of the last iteration */
+    double correlation;   /* ZNSSD (SSD) at the pre-update parameters of the last iteration */
     int32_t iterations;   /* loop bodies entered */
     int8_t status;
     int8_t valid;
     int8_t converged;     /* strict: |dp| < threshold was reached */
     int8_t pad_;
+    double q[6];          /* second order: d2u_dx2, d2u_dxdy, d2u_dy2, d2v_dx2, d2v_dxdy, d2v_dy2 (else 0) */
 } orc_poi_result;
 
 /* Structure-of-arrays grid output (bind_subset.cpp:102-153 plus additive keys). */
@@ -84,6 +85,8 @@ typedef struct orc_grid_out {
     double* du_dx; double* du_dy; double* dv_dx; double* dv_dy;
     double* correlation;
     uint8_t* valid; int8_t* status; int32_t* iterations; uint8_t* converged;
+    /* second-order terms (Displacement2D d2u_dx2 ... d2v_dy2); NULL = not written */
+    double* d2u_dx2; double* d2u_dxdy; double* d2u_dy2; double* d2v_dx2; double* d2v_dxdy; double* d2v_dy2;
 } orc_grid_out;
 
 /* Seed placed by the seed selector (seed_selector.cpp:146-205). */
@@ -112,10 +115,11 @@ void orc_interp_gradient(const double* coeffs, int w, int h, int degree, int bor
 /* reliability_propagation.cpp:84-112 */
 void orc_reference_gradient(const float* image, int w, int h, double* gx, double* gy);
 
-/* icgn.cpp:446-627 (optimizer 0) / forward_gauss_newton.cpp:188-399 (optimizer 1) for each
- * POI.  ref_gx/ref_gy may be NULL (central differences on the fly, icgn.cpp:42-53).
- * confidence0 may be NULL (initial.confidence = 0).  Returns 0, or -1 if the route is not a
- * first-order ZNSSD route. */
+/* ICGNSolver (optimizer 0) / ForwardGaussNewtonSolver (optimizer 1) ::solve_with_interpolators
+ * for each POI, routed on shape_order (1, 2) and criterion (1 ZNSSD, 0 SSD): icgn.cpp:446-627,
+ * 832-988, 1168-1362, 1576-1739; forward_gauss_newton.cpp:188-399, 622-794, 1069-1297,
+ * 1540-1739.  ref_gx/ref_gy may be NULL (central differences on the fly, icgn.cpp:42-53).
+ * confidence0 may be NULL (initial.confidence = 0).  Returns 0, or -1 for a bad degree. */
 int orc_solve_pois(const float* ref, int w, int h, const double* ref_gx, const double* ref_gy,
                    const double* coeffs, int degree, int border, const orc_config* cfg,
                    int n, const double* xy, const double* p0, const double* confidence0,

@@ -18,6 +18,17 @@ Input: the seeded 256 x 256 uint8 speckle pair of the small workload (stored in 
 a grid of subset centres (and one too close to the border) with initial guesses from the imposed
 field rounded to 0.5 px and zero gradients.
 
+tests/golden/subset_variants_256.npz holds the other solver routes on the same POIs, for the
+small workload's pair (affine field) and for a 256 x 256 pair with a Gaussian bump (curvature):
+  * first-order SSD ICGN (icgn.cpp:832-988): raw residual f - g, Hessian and gradient unscaled;
+  * second-order ZNSSD / SSD ICGN (icgn.cpp:142-357, 1168-1362, 1576-1739): 12 parameters, update
+    through the 6 x 6 warp matrix G'(p) G'(dp)^-1 P^-1 (numpy.linalg.inv; additive update when
+    G'(dp) is rank deficient);
+  * FGN (forward_gauss_newton.cpp:622-794, 986-1053, 1069-1297, 1540-1739): SD from the spline
+    gradient (bspline.cpp:115-151, 476-500) through dW/dz, step caps 0.5 (ZNSSD) / 0.35 (SSD),
+    the first-order SSD route converging on the norm before the cap, and the second-order routes
+    with the 1e-4 * max(diag H) damping term.
+
 Run from the repository root:  python tests/golden/make_golden.py
 """
 import math
@@ -159,6 +170,218 @@ def icgn(ref, coef, qk, px, py, p0):
     return p, corr, it, 0 if converged else 1, converged
 
 
+def spline_gradients(coef, qk, xs, ys, w, h, d, border):
+    """d/dx and d/dy of the spline at (xs, ys): bspline.cpp:115-151 through the local block."""
+    off = d // 2
+    ix = np.clip(np.floor(xs).astype(int), 0, w - 1)
+    iy = np.clip(np.floor(ys).astype(int), 0, h - 1)
+    dx, dy = xs - ix, ys - iy
+    n = d + 1
+    rr = np.clip(iy[:, None] + border - off + np.arange(n)[None, :], 0, coef.shape[0] - 1)
+    cc = np.clip(ix[:, None] + border - off + np.arange(n)[None, :], 0, coef.shape[1] - 1)
+    blocks = coef[rr[:, :, None], cc[:, None, :]]
+    poly = np.einsum("ra,mab,cb->mrc", qk, blocks, qk)
+    k = np.arange(n)
+    ypow = dy[:, None] ** k[None, :]
+    xpow = dx[:, None] ** k[None, :]
+    dxpow = np.where(k[None, :] >= 1, k[None, :] * dx[:, None] ** np.maximum(k - 1, 0)[None, :], 0.0)
+    dypow = np.where(k[None, :] >= 1, k[None, :] * dy[:, None] ** np.maximum(k - 1, 0)[None, :], 0.0)
+    return (np.einsum("mrc,mr,mc->m", poly, ypow, dxpow), np.einsum("mrc,mr,mc->m", poly, dypow, xpow))
+
+
+def warp_matrix(p):
+    u, v, ux, uy, vx, vy, uxx, uxy, uyy, vxx, vxy, vyy = p
+    return np.array([
+        [u, 1 + ux, uy, 0.5 * uxx, uxy, 0.5 * uyy],
+        [v, vx, 1 + vy, 0.5 * vxx, vxy, 0.5 * vyy],
+        [1, 0, 0, 0, 0, 0],
+        [u * u, 2 * u * (1 + ux), 2 * u * uy, 1 + 2 * ux + ux * ux + u * uxx, 2 * (uy + ux * uy + u * uxy),
+         uy * uy + u * uyy],
+        [u * v, v + u * vx + v * ux, u + u * vy + v * uy, vx + ux * vx + 0.5 * (u * vxx + v * uxx),
+         1 + vy + ux + ux * vy + uy * vx + u * vxy + v * uxy, uy + uy * vy + 0.5 * (u * vyy + v * uyy)],
+        [v * v, 2 * v * vx, 2 * v * (1 + vy), vx * vx + v * vxx, 2 * (vx + vx * vy + v * vxy),
+         1 + 2 * vy + vy * vy + v * vyy]])
+
+
+def ic_update2(p, dp):
+    gd = warp_matrix(dp)
+    sv = np.linalg.svd(gd, compute_uv=False)
+    if np.sum(sv > sv[0] * 6 * np.finfo(float).eps) < 6:
+        return p - dp
+    x = warp_matrix(p) @ np.linalg.inv(gd)
+    n = x[:, [2, 0, 1, 3, 4, 5]]
+    return np.array([n[0, 0], n[1, 0], n[0, 1] - 1, n[0, 2], n[1, 1], n[1, 2] - 1,
+                     2 * n[0, 3], n[0, 4], 2 * n[0, 5], 2 * n[1, 3], n[1, 4], 2 * n[1, 5]])
+
+
+def compose1(p, dp):
+    return np.array([dp[0] + p[0] + p[2] * dp[0] + p[3] * dp[1], dp[1] + p[1] + p[4] * dp[0] + p[5] * dp[1],
+                     dp[2] + p[2] * (1 + dp[2]) + p[3] * dp[4], dp[3] + p[2] * dp[3] + p[3] * (1 + dp[5]),
+                     dp[4] + p[4] * (1 + dp[2]) + p[5] * dp[4], dp[5] + p[4] * dp[3] + p[5] * (1 + dp[5])])
+
+
+def compose2(p, dp):
+    q = np.empty(12)
+    q[:6] = compose1(p[:6], dp[:6])
+    q[2] += p[6] * dp[0] + p[7] * dp[1]
+    q[3] += p[7] * dp[0] + p[8] * dp[1]
+    q[4] += p[9] * dp[0] + p[10] * dp[1]
+    q[5] += p[10] * dp[0] + p[11] * dp[1]
+    q[6] = dp[6] + p[2] * dp[6] + p[3] * dp[9] + p[6] * (1 + 2 * dp[2]) + 2 * p[7] * dp[4]
+    q[7] = dp[7] + p[2] * dp[7] + p[3] * dp[10] + p[6] * dp[3] + p[7] * (1 + dp[2] + dp[5]) + p[8] * dp[4]
+    q[8] = dp[8] + p[2] * dp[8] + p[3] * dp[11] + p[7] * dp[3] + p[8] * (1 + 2 * dp[5])
+    q[9] = dp[9] + p[4] * dp[6] + p[5] * dp[9] + p[9] * (1 + 2 * dp[2]) + 2 * p[10] * dp[4]
+    q[10] = dp[10] + p[4] * dp[7] + p[5] * dp[10] + p[9] * dp[3] + p[10] * (1 + dp[2] + dp[5]) + p[11] * dp[4]
+    q[11] = dp[11] + p[4] * dp[8] + p[5] * dp[11] + p[10] * dp[3] + p[11] * (1 + 2 * dp[5])
+    return q
+
+
+def shape_terms(lx, ly, order):
+    m = [np.ones_like(lx), lx, ly]
+    if order == 2:
+        m += [lx * lx * 0.5, lx * ly, ly * ly * 0.5]
+    return m
+
+
+def sd_rows(a, b, lx, ly, order):
+    m = shape_terms(lx, ly, order)
+    cols = [a * m[0], b * m[0], a * m[1], a * m[2], b * m[1], b * m[2]]
+    if order == 2:
+        cols += [a * m[3], a * m[4], a * m[5], b * m[3], b * m[4], b * m[5]]
+    return np.column_stack(cols)
+
+
+def solve_variant(ref, coef, qk, px, py, p0, optimizer, order, ssd):
+    """(p[12], correlation, iterations, status, converged) of one POI on one solver route."""
+    h, w = ref.shape
+    npar = 6 * order
+    cx, cy = int(np.round(px)), int(np.round(py))
+    r = RADIUS
+    p = np.zeros(npar)
+    p[:2] = p0
+    out = lambda st, corr, it, conv: (np.concatenate([p[:6], p[6:], np.zeros(12 - npar)]), corr, it, st, conv)
+    if cx - r < 0 or cy - r < 0 or cx + r >= w or cy + r >= h:
+        return out(2, np.nan, 0, False)
+    off = np.array([(dx, dy) for dy in range(-r, r + 1) for dx in range(-r, r + 1) if dx * dx + dy * dy <= r * r],
+                   dtype=np.float64)
+    lx, ly = off[:, 0], off[:, 1]
+    xs, ys = cx + off[:, 0].astype(int), cy + off[:, 1].astype(int)
+    f = ref[ys, xs].astype(np.float64)
+    fn = 1.0
+    if not ssd:
+        fm = f.mean()
+        fn = math.sqrt(np.sum((f - fm) ** 2))
+        if fn <= EPS:
+            return out(3, np.inf, 0, False)
+        fhat = (f - fm) / fn
+    if optimizer == 0:
+        xm, xp = np.maximum(0, xs - 1), np.minimum(w - 1, xs + 1)
+        ym, yp = np.maximum(0, ys - 1), np.minimum(h - 1, ys + 1)
+        gx = (ref[ys, xp].astype(np.float64) - ref[ys, xm]) / np.maximum(1, xp - xm)
+        gy = (ref[yp, xs].astype(np.float64) - ref[ym, xs]) / np.maximum(1, yp - ym)
+        sd = sd_rows(gx, gy, lx, ly, order)
+        hess = sd.T @ sd * (1.0 if ssd else 2.0 / (fn * fn))
+    cap = 0.35 if ssd else 0.5
+    corr, converged, it = np.inf, False, 0
+    for it in range(1, MAX_ITER + 1):
+        m = shape_terms(lx, ly, order)
+        wx = cx + lx + p[0] + p[2] * lx + p[3] * ly
+        wy = cy + ly + p[1] + p[4] * lx + p[5] * ly
+        if order == 2:
+            wx = wx + p[6] * m[3] + p[7] * m[4] + p[8] * m[5]
+            wy = wy + p[9] * m[3] + p[10] * m[4] + p[11] * m[5]
+        if np.any((wx < 0) | (wy < 0) | (wx > w - 1) | (wy > h - 1)):
+            return out(2, corr, it, False)
+        g = spline_values(coef, qk, wx, wy, w, h, DEGREE, BORDER)
+        if ssd:
+            diff = f - g
+        else:
+            gm = g.mean()
+            gn = math.sqrt(np.sum((g - gm) ** 2))
+            if gn <= EPS:
+                return out(3, corr, it, False)
+            diff = fhat - (g - gm) / gn
+        corr = float(diff @ diff)
+        if optimizer == 0:
+            grad = (diff @ sd) * (1.0 if ssd else 2.0 / fn)
+            dp = -np.linalg.solve(hess, grad)
+        else:
+            dgx, dgy = spline_gradients(coef, qk, wx, wy, w, h, DEGREE, BORDER)
+            if order == 1:
+                a00, a01, a10, a11 = 1 + p[2], p[3], p[4], 1 + p[5]
+            else:
+                a00 = 1 + p[2] + p[6] * lx + p[7] * ly
+                a01 = p[3] + p[7] * lx + p[8] * ly
+                a10 = p[4] + p[9] * lx + p[10] * ly
+                a11 = 1 + p[5] + p[10] * lx + p[11] * ly
+            sd = sd_rows(dgx * a00 + dgy * a10, dgx * a01 + dgy * a11, lx, ly, order)
+            hess = sd.T @ sd * (1.0 if ssd else 2.0 / (fn * fn))
+            grad = (diff @ sd) * (1.0 if ssd else 2.0 / fn)
+            if order == 2:
+                hess = hess + 1e-4 * np.max(np.diag(hess)) * np.eye(npar)
+            dp = np.linalg.solve(hess, grad)
+        if not np.all(np.isfinite(dp)):
+            return out(3, corr, it, False)
+        dn = float(np.linalg.norm(dp))
+        dn_test = dn
+        if optimizer == 1 and dn > cap:
+            dp = dp * (cap / dn)
+            if not (ssd and order == 1):
+                dn_test = cap
+        if optimizer == 0:
+            p = ic_update(p, dp) if order == 1 else ic_update2(p, dp)
+        else:
+            p = compose1(p, dp) if order == 1 else compose2(p, dp)
+        if not np.all(np.isfinite(p)):
+            return out(3, corr, it, False)
+        if dn_test < THRESHOLD:
+            converged = True
+            break
+    if not converged and math.isfinite(corr):
+        converged = True
+    return out(0 if converged else 1, corr, it, converged)
+
+
+# (name, optimizer 0 icgn / 1 fgn, shape order, ssd)
+VARIANTS = [("icgn1_ssd", 0, 1, True), ("icgn2_znssd", 0, 2, False), ("icgn2_ssd", 0, 2, True),
+            ("fgn1_ssd", 1, 1, True), ("fgn2_znssd", 1, 2, False), ("fgn2_ssd", 1, 2, True)]
+VARIANTS_OUT = os.path.join(HERE, "subset_variants_256.npz")
+
+
+def bump_pair():
+    from traditional_dic_gb300 import synthetic
+    f = synthetic.Field("bump", dict(cx=128.0, cy=128.0, s=60.0, a=3.0))
+    return synthetic.speckle_pair((256, 256), 1500, f, 0.5, synthetic.BASE_SEED + 17)
+
+
+def main_variants():
+    from traditional_dic_gb300 import synthetic
+    qk = qk_matrix(DEGREE)
+    pts = [(x, y) for y in range(20, 240, 22) for x in range(20, 240, 22)] + [(5.0, 128.0)]
+    arrays = {}
+    for tag, pair in (("a", synthetic.workload(0)), ("b", bump_pair())):
+        ref, de = pair.reference, pair.deformed
+        coef = coefficients(de, DEGREE, BORDER)
+        pois = []
+        for x, y in pts:
+            u, v = pair.field.uv(np.float64(x), np.float64(y))
+            pois.append((x, y, round(2 * float(u)) / 2.0, round(2 * float(v)) / 2.0))
+        pois = np.array(pois, np.float64)
+        arrays[f"reference_{tag}"] = ref
+        arrays[f"deformed_{tag}"] = de
+        arrays[f"pois_{tag}"] = pois
+        for name, opt, order, ssd in VARIANTS:
+            res = []
+            for x, y, u0, v0 in pois:
+                p, corr, iters, status, conv = solve_variant(ref, coef, qk, x, y, (u0, v0), opt, order, ssd)
+                res.append(np.concatenate([p, [corr, iters, status, float(conv)]]))
+            arrays[f"{name}_{tag}"] = np.array(res, np.float64)
+            print(f"{name} {tag}: {int(sum(r[15] for r in res))} converged")
+    arrays["settings"] = np.array([DEGREE, BORDER, RADIUS, MAX_ITER, THRESHOLD])
+    np.savez_compressed(VARIANTS_OUT, **arrays)
+    print(f"wrote {VARIANTS_OUT}")
+
+
 def main():
     sys.path.insert(0, ROOT)
     import __graft_entry__ as G
@@ -181,6 +404,7 @@ def main():
                         pois=np.array(pois, np.float64), results=np.array(res, np.float64),
                         settings=np.array([DEGREE, BORDER, RADIUS, MAX_ITER, THRESHOLD]))
     print(f"wrote {OUT}: {len(pois)} POIs, {int(sum(r[9] for r in res))} converged")
+    main_variants()
 
 
 if __name__ == "__main__":

@@ -32,8 +32,9 @@ def test_struct_layouts_match_header(pkg, oracle):
     assert C.sizeof(L.Config) == 136
     assert C.sizeof(L.Config) == C.sizeof(oracle.Config)
     assert [f for f, _ in L.Config._fields_] == [f for f, _ in oracle.Config._fields_]
-    assert C.sizeof(L.PoiIn) == 72 and C.sizeof(L.PoiOut) == 72 and C.sizeof(L.Seed) == 80
-    assert C.sizeof(L.GridOut) == 14 * C.sizeof(C.c_void_p)
+    assert C.sizeof(L.PoiIn) == 72 and C.sizeof(L.PoiOut) == 120 and C.sizeof(L.Seed) == 80
+    assert C.sizeof(L.GridOut) == 20 * C.sizeof(C.c_void_p)
+    assert C.sizeof(oracle.PoiResult) == 112 and C.sizeof(oracle.GridOut) == 19 * C.sizeof(C.c_void_p)
 
 
 def test_defaults_match_reference_cpp_defaults(pkg, oracle):

@@ -80,3 +80,55 @@ def test_gpu_icgn_matches_golden(gpu_ctx, golden, precision):
         assert np.array_equal(r["status"], res[:, 8].astype(int))
         assert np.max(np.abs(r["p"][ok, :2] - res[ok, :2])) <= U_TOL
     pair.close()
+
+
+# ---- the other solver routes (tests/golden/subset_variants_256.npz) --------------------------
+VARIANTS_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "subset_variants_256.npz")
+VARIANTS = [("icgn1_ssd", 0, 1, 0), ("icgn2_znssd", 0, 2, 1), ("icgn2_ssd", 0, 2, 0),
+            ("fgn1_ssd", 1, 1, 0), ("fgn2_znssd", 1, 2, 1), ("fgn2_ssd", 1, 2, 0)]
+Q_TOL = 1e-9       # second-order terms (px / px^2) between two FP64 transcriptions
+
+
+@pytest.fixture(scope="module")
+def variants():
+    d = np.load(VARIANTS_FILE)
+    return {k: d[k] for k in d.files}
+
+
+def _variant_config(g, make_default, opt, order, crit):
+    degree, border, radius, max_iter, thr = g["settings"]
+    cfg = make_default()
+    cfg.subset_radius, cfg.max_iterations, cfg.convergence_threshold = int(radius), int(max_iter), float(thr)
+    cfg.degree, cfg.border = int(degree), int(border)
+    cfg.optimizer, cfg.shape_order, cfg.criterion = opt, order, crit
+    return cfg
+
+
+def _variant_inputs(g, tag):
+    pois = g[f"pois_{tag}"]
+    p0 = np.zeros((len(pois), 6))
+    p0[:, :2] = pois[:, 2:4]
+    return pois[:, :2], p0
+
+
+def _check_variant(r, want, p_tol, q_tol, corr_rtol):
+    want_p, want_q, want_corr = want[:, :6], want[:, 6:12], want[:, 12]
+    want_iters, want_status = want[:, 13].astype(int), want[:, 14].astype(int)
+    assert np.array_equal(np.asarray(r["status"], int), want_status)
+    ok = want_status == 0
+    assert np.array_equal(np.asarray(r["iterations"], int)[ok], want_iters[ok])
+    assert np.max(np.abs(r["p"][ok] - want_p[ok])) <= p_tol
+    assert np.max(np.abs(r["q"][ok] - want_q[ok])) <= q_tol
+    c = np.asarray(r["correlation"])[ok]
+    assert np.max(np.abs(c - want_corr[ok]) / np.maximum(1.0, np.abs(want_corr[ok]))) <= corr_rtol
+
+
+@pytest.mark.parametrize("tag", ["a", "b"])
+@pytest.mark.parametrize("name,opt,order,crit", VARIANTS)
+def test_oracle_variants_match_golden(oracle, variants, name, opt, order, crit, tag):
+    cfg = _variant_config(variants, oracle.default_config, opt, order, crit)
+    ref = variants[f"reference_{tag}"].astype(np.float32)
+    coef = oracle.prefilter(variants[f"deformed_{tag}"].astype(np.float32), cfg.degree, cfg.border, True)
+    xy, p0 = _variant_inputs(variants, tag)
+    r = oracle.solve_pois(ref, coef, cfg, xy, p0, gradients=oracle.reference_gradient(ref))
+    _check_variant(r, variants[f"{name}_{tag}"], P_TOL, Q_TOL, 1e-9)

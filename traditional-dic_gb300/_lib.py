@@ -44,7 +44,8 @@ class PoiIn(C.Structure):
 
 class PoiOut(C.Structure):
     _fields_ = [("p", C.c_double * 6), ("correlation", C.c_double), ("zncc", C.c_double), ("iterations", C.c_int32),
-                ("status", C.c_int8), ("valid", C.c_int8), ("converged", C.c_int8), ("pad_", C.c_int8)]
+                ("status", C.c_int8), ("valid", C.c_int8), ("converged", C.c_int8), ("pad_", C.c_int8),
+                ("q", C.c_double * 6)]
 
 
 class Seed(C.Structure):
@@ -54,6 +55,8 @@ class Seed(C.Structure):
 
 GRID_FIELDS = ("x", "y", "u", "v", "du_dx", "du_dy", "dv_dx", "dv_dy", "correlation", "zncc", "valid", "status",
                "iterations", "converged")
+# second-order terms of dic::Displacement2D (written for shape_order 2, zero otherwise)
+SECOND_ORDER_FIELDS = ("d2u_dx2", "d2u_dxdy", "d2u_dy2", "d2v_dx2", "d2v_dxdy", "d2v_dy2")
 
 
 class LsStrain(C.Structure):
@@ -63,7 +66,7 @@ class LsStrain(C.Structure):
 
 
 class GridOut(C.Structure):
-    _fields_ = [(n, C.c_void_p) for n in GRID_FIELDS]
+    _fields_ = [(n, C.c_void_p) for n in GRID_FIELDS + SECOND_ORDER_FIELDS]
 
 
 # Every exported symbol of include/tdic_gb300.h with its ctypes signature.

@@ -158,9 +158,9 @@ bool first_order_znssd(const tdic_config& c) { return c.shape_order == 1 && c.cr
 int normalized_degree(int d) { return (d == 1 || d == 3) ? d : 5; }
 
 void check_config(const tdic_config& c) {
-    TDIC_REQUIRE(first_order_znssd(c), TDIC_UNSUPPORTED,
-                 "only first-order ZNSSD routes are on the GPU path (second order / SSD: use the reference solver)");
     TDIC_REQUIRE(c.optimizer == 0 || c.optimizer == 1, TDIC_INVALID_ARG, "optimizer must be 0 (icgn) or 1 (fgn)");
+    TDIC_REQUIRE(c.shape_order == 1 || c.shape_order == 2, TDIC_INVALID_ARG, "shape_order must be 1 or 2");
+    TDIC_REQUIRE(c.criterion == 0 || c.criterion == 1, TDIC_INVALID_ARG, "criterion must be 1 (znssd) or 0 (ssd)");
     TDIC_REQUIRE(c.subset_radius >= 1 && c.subset_radius <= 100, TDIC_INVALID_ARG, "subset radius must be in [1, 100]");
     TDIC_REQUIRE(c.max_iterations >= 0, TDIC_INVALID_ARG, "max_iterations must be >= 0");
 }
@@ -201,20 +201,23 @@ bool roi_ok(const uint8_t* roi, int w, int h, int x, int y) {
 
 // Device SoA output, either the caller's device arrays or pool buffers copied back.
 struct GridBuffers {
-    Buffer d[14];
+    Buffer d[20];
     tdic_grid_out dev{};
 };
 
 void alloc_grid(tdic_ctx* ctx, GridBuffers& g, int n, const tdic_grid_out* host_wanted) {
-    double** dptrs[10] = {&g.dev.x, &g.dev.y, &g.dev.u, &g.dev.v, &g.dev.du_dx, &g.dev.du_dy, &g.dev.dv_dx, &g.dev.dv_dy,
-                          &g.dev.correlation, &g.dev.zncc};
-    double* const* hptrs[10] = {&host_wanted->x, &host_wanted->y, &host_wanted->u, &host_wanted->v, &host_wanted->du_dx,
+    double** dptrs[16] = {&g.dev.x, &g.dev.y, &g.dev.u, &g.dev.v, &g.dev.du_dx, &g.dev.du_dy, &g.dev.dv_dx, &g.dev.dv_dy,
+                          &g.dev.correlation, &g.dev.zncc, &g.dev.d2u_dx2, &g.dev.d2u_dxdy, &g.dev.d2u_dy2,
+                          &g.dev.d2v_dx2, &g.dev.d2v_dxdy, &g.dev.d2v_dy2};
+    double* const* hptrs[16] = {&host_wanted->x, &host_wanted->y, &host_wanted->u, &host_wanted->v, &host_wanted->du_dx,
                                 &host_wanted->du_dy, &host_wanted->dv_dx, &host_wanted->dv_dy, &host_wanted->correlation,
-                                &host_wanted->zncc};
-    for (int i = 0; i < 10; ++i) {
+                                &host_wanted->zncc, &host_wanted->d2u_dx2, &host_wanted->d2u_dxdy, &host_wanted->d2u_dy2,
+                                &host_wanted->d2v_dx2, &host_wanted->d2v_dxdy, &host_wanted->d2v_dy2};
+    for (int i = 0; i < 16; ++i) {
+        const int slot = i < 10 ? i : i + 4;
         if (*hptrs[i]) {
-            g.d[i] = Buffer(&ctx->pool, sizeof(double) * n);
-            *dptrs[i] = g.d[i].as<double>();
+            g.d[slot] = Buffer(&ctx->pool, sizeof(double) * n);
+            *dptrs[i] = g.d[slot].as<double>();
         }
     }
     if (host_wanted->valid) { g.d[10] = Buffer(&ctx->pool, n); g.dev.valid = g.d[10].as<uint8_t>(); }
@@ -232,6 +235,8 @@ void copy_grid_back(const GridBuffers& g, const tdic_grid_out* h, int n, cudaStr
     cp(h->dv_dy, g.dev.dv_dy, 8 * n); cp(h->correlation, g.dev.correlation, 8 * n); cp(h->zncc, g.dev.zncc, 8 * n);
     cp(h->valid, g.dev.valid, n); cp(h->status, g.dev.status, n); cp(h->iterations, g.dev.iterations, 4 * n);
     cp(h->converged, g.dev.converged, n);
+    cp(h->d2u_dx2, g.dev.d2u_dx2, 8 * n); cp(h->d2u_dxdy, g.dev.d2u_dxdy, 8 * n); cp(h->d2u_dy2, g.dev.d2u_dy2, 8 * n);
+    cp(h->d2v_dx2, g.dev.d2v_dx2, 8 * n); cp(h->d2v_dxdy, g.dev.d2v_dxdy, 8 * n); cp(h->d2v_dy2, g.dev.d2v_dy2, 8 * n);
 }
 
 void propagate_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const tdic_seed& seed, const uint8_t* roi,
@@ -1126,6 +1131,8 @@ void batch_create_impl(tdic_ctx* ctx, int n, tdic_pair* const* pairs, const tdic
         TDIC_REQUIRE(p->degree == p0->degree && p->precision == p0->precision, TDIC_INVALID_ARG,
                      "batch: every pair must have the same spline degree and precision");
         TDIC_REQUIRE(c.optimizer == cfgs[0].optimizer, TDIC_INVALID_ARG, "batch: every job must use the same optimizer");
+        TDIC_REQUIRE(first_order_znssd(c), TDIC_UNSUPPORTED,
+                     "batch: only the first-order ZNSSD route (propagate other routes one pair at a time)");
         TDIC_REQUIRE(c.propagation_mode == 2, TDIC_UNSUPPORTED, "batch: only the dataflow order (propagation_mode 2)");
         // seed alignment (reliability_propagation.cpp:201-216), as tdic_propagate
         const uint8_t* roi = rois ? rois[j] : nullptr;

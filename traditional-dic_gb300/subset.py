@@ -299,25 +299,36 @@ def _empty_result() -> dict:
     return out
 
 
-def _alloc_grid(n: int):
+def _alloc_grid(n: int, second_order: bool = False):
     arrs = {k: np.zeros(n, np.float64) for k in ("x", "y", "u", "v", "du_dx", "du_dy", "dv_dx", "dv_dy", "correlation",
                                                   "zncc")}
     arrs["valid"] = np.zeros(n, np.uint8)
     arrs["status"] = np.zeros(n, np.int8)
     arrs["iterations"] = np.zeros(n, np.int32)
     arrs["converged"] = np.zeros(n, np.uint8)
-    g = L.GridOut(**{k: arrs[k].ctypes.data for k in L.GRID_FIELDS})
+    keys = L.GRID_FIELDS
+    if second_order:
+        for k in L.SECOND_ORDER_FIELDS:
+            arrs[k] = np.zeros(n, np.float64)
+        keys = keys + L.SECOND_ORDER_FIELDS
+    g = L.GridOut(**{k: arrs[k].ctypes.data for k in keys})
     return arrs, g
 
 
 def _finish(arrs: dict) -> dict:
+    """The reference's result dict (results_to_dict, bind_subset.cpp:102-153) plus the additive
+    keys; for the second-order shape function also the six second-order terms."""
     out = {k: arrs[k] for k in RESULT_KEYS if k != "valid"}
     out["valid"] = arrs["valid"].astype(bool)
     out["zncc"] = arrs["zncc"]
     out["iterations"] = arrs["iterations"]
     out["converged"] = arrs["converged"].astype(bool)
     out["status"] = arrs["status"]
-    return {k: out[k] for k in RESULT_KEYS + EXTRA_KEYS}
+    res = {k: out[k] for k in RESULT_KEYS + EXTRA_KEYS}
+    for k in L.SECOND_ORDER_FIELDS:
+        if k in arrs:
+            res[k] = arrs[k]
+    return res
 
 
 def _roi_arg(roi, w: int, h: int):
@@ -356,7 +367,7 @@ def compute(reference, deformed, config: dict | None = None, roi=None, *, contex
     if de.dtype != ref.dtype:
         de = de.astype(ref.dtype)
     gw, gh = L.grid_dims(w, h, cfg.propagation_spacing)
-    arrs, g = _alloc_grid(gw * gh)
+    arrs, g = _alloc_grid(gw * gh, cfg.shape_order == 2)
     n = C.c_int32()
     ctx.check(ctx.lib.tdic_subset_compute(ctx.handle, ref.ctypes.data, de.ctypes.data, w, h, L.DTYPES[ref.dtype.name],
                                           rptr, C.byref(cfg), C.byref(g), C.byref(n), C.byref(seed), None))
@@ -417,7 +428,8 @@ def subset(reference: np.ndarray, deformed: np.ndarray, config: str | Path | dic
 
 
 def solve_pois(ctx: Context, pair: Pair, config: L.Config, xy, p0, confidence=None) -> dict:
-    """Batched per-POI solve (tdic_solve_pois) on host arrays."""
+    """Batched per-POI solve (tdic_solve_pois) on host arrays, on the config's route (optimizer,
+    shape_order, criterion); "q" holds the six second-order terms (zero for first order)."""
     xy = np.ascontiguousarray(xy, np.float64).reshape(-1, 2)
     p0 = np.ascontiguousarray(p0, np.float64).reshape(-1, 6)
     n = xy.shape[0]
@@ -426,10 +438,11 @@ def solve_pois(ctx: Context, pair: Pair, config: L.Config, xy, p0, confidence=No
     if confidence is not None:
         inp["confidence"] = confidence
     out = np.zeros(n, dtype=np.dtype([("p", "<f8", 6), ("correlation", "<f8"), ("zncc", "<f8"), ("iterations", "<i4"),
-                                      ("status", "i1"), ("valid", "i1"), ("converged", "i1"), ("pad", "i1")]))
+                                      ("status", "i1"), ("valid", "i1"), ("converged", "i1"), ("pad", "i1"),
+                                      ("q", "<f8", 6)]))
     ctx.check(ctx.lib.tdic_solve_pois(ctx.handle, pair.handle, C.byref(config), inp.ctypes.data, n, out.ctypes.data,
                                       L.HOST, None))
-    return {"p": out["p"].copy(), "correlation": out["correlation"].copy(), "zncc": out["zncc"].copy(),
+    return {"p": out["p"].copy(), "q": out["q"].copy(), "correlation": out["correlation"].copy(), "zncc": out["zncc"].copy(),
             "iterations": out["iterations"].copy(), "status": out["status"].copy(),
             "valid": out["valid"].astype(bool), "converged": out["converged"].astype(bool)}
 
@@ -448,7 +461,7 @@ def propagate(ctx: Context, pair: Pair, config: L.Config, seed: L.Seed, roi=None
     """Propagation over the POI grid (tdic_propagate) in the config's visit order, with host
     outputs; returns the grid dict plus ``points_computed``."""
     gw, gh = L.grid_dims(pair.width, pair.height, config.propagation_spacing)
-    arrs, g = _alloc_grid(gw * gh)
+    arrs, g = _alloc_grid(gw * gh, config.shape_order == 2)
     rptr, rkeep = _roi_arg(roi, pair.width, pair.height)
     if rptr == "mismatch":
         raise ValueError("roi shape differs from the images")
