@@ -80,6 +80,12 @@ typedef struct tdic_config {
     double min_texture_std;            /* seed_selection.min_texture_std                0 */
     int32_t kmeans_sample_limit;       /* seed_selection.kmeans_sample_limit        20000 */
     int32_t propagation_mode;          /* 2 dataflow, 0 frontier waves (GPU orders)     2 */
+    /* Masked subsets (SubsetConfig, subset_config.hpp:40-42; set from the YAML subset section,
+     * yaml_parser.cpp:103-111, not from the pybind dict): samples outside the ROI are left out of
+     * each subset, and SubsetDIC::compute pads the images (subset_dic.cpp:53-56). */
+    int32_t truncate_roi_subsets;      /* subset.truncate_roi_subsets                    0 */
+    int32_t min_valid_samples;         /* subset.min_valid_samples                       12 */
+    double min_valid_sample_ratio;     /* subset.min_valid_sample_ratio                 0.5 */
 } tdic_config;
 
 /* One POI for a batched solve: centre (rounded to the nearest pixel as icgn.cpp:472-473),
@@ -184,8 +190,28 @@ tdic_status tdic_solve_pois(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* c
                             const tdic_poi_in* in, int32_t n, tdic_poi_out* out,
                             tdic_memory memory, void* stream);
 
+/* Masked per-POI solve: replaces SubsetSolver::solve_with_mask (icgn.cpp:407-432,
+ * forward_gauss_newton.cpp:144-170; the routes at icgn.cpp:629-818, 990-1154, 1364-1562,
+ * 1741-1912 and forward_gauss_newton.cpp:401-604, 796-968, 1299-1522, 1741-1941).  roi: host
+ * H x W mask of the pair's image (NULL = every pixel valid).  The centre must be a ROI pixel (no
+ * margin check); samples outside the image or the ROI are left out, and at least
+ * max(6 or 12, cfg->min_valid_samples, ceil(cfg->min_valid_sample_ratio * full circle)) must
+ * remain (else status InvalidInput).  in/out as tdic_solve_pois. */
+tdic_status tdic_solve_pois_masked(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cfg,
+                                   const uint8_t* roi, const tdic_poi_in* in, int32_t n,
+                                   tdic_poi_out* out, tdic_memory memory, void* stream);
+
+/* recommended_subset_padding (src/subset/padding.cpp:28-36) when cfg->truncate_roi_subsets, else 0. */
+int32_t tdic_subset_padding(const tdic_config* cfg);
+/* Output grid of tdic_subset_compute: tdic_grid_dims, or with truncate_roi_subsets the grid of the
+ * padded image restricted to points inside the image (subset_dic.cpp:92-104). */
+void tdic_subset_grid_dims(int32_t width, int32_t height, const tdic_config* cfg, int32_t* grid_w,
+                           int32_t* grid_h);
+
 /* Propagation over the POI grid from one seed: replaces the heap loop of
- * ReliabilityPropagation::propagate (reliability_propagation.cpp:130-394).  The grid
+ * ReliabilityPropagation::propagate (reliability_propagation.cpp:130-394).  With
+ * cfg->truncate_roi_subsets every solve is masked by roi (NULL = all pixels); the images are
+ * used as given (SubsetDIC::compute pads them first: tdic_subset_compute does).  The grid
  * geometry, seed alignment (:201-264), neighbour admission (:303-323), guess extrapolation
  * (:326-329) and acceptance rule (:359-368) are the reference's; the visit order is
  * cfg->propagation_mode: dataflow (each point solved from its parent one step toward the seed
@@ -262,7 +288,8 @@ tdic_status tdic_select_seed(tdic_ctx* ctx, tdic_pair* lazy, const float* refere
                              const uint8_t* roi, const tdic_config* cfg, tdic_seed* seed,
                              void* stream);
 
-/* SubsetDIC::compute up to the propagation (subset_dic.cpp:39-64): creates the pair from host
+/* SubsetDIC::compute up to the propagation (subset_dic.cpp:39-64), without truncate_roi_subsets
+ * (TDIC_UNSUPPORTED): creates the pair from host
  * images (as tdic_pair_create with the exact prefilter) and selects its seed (as
  * tdic_select_seed, on a seed spline built from the uploaded images; texture statistics on the
  * raw host images).  The caller propagates (tdic_propagate, or one job of a tdic_batch) and
@@ -292,8 +319,11 @@ tdic_status tdic_ls_strain_2d(tdic_ctx* ctx, const double* points, const double*
 
 /* Whole pybind path: _traditional_dic.subset.compute (bind_subset.cpp:253-315) ->
  * SubsetDIC::compute (subset_dic.cpp:39-105).  Host images of `dtype`, host roi (NULL = full
- * image), host outputs of grid_w*grid_h entries.  *n_points = grid_w*grid_h, or 0 for the
- * reference's empty result (no seed found, or nothing computed). */
+ * image), host outputs of grid_w*grid_h entries (tdic_subset_grid_dims).  *n_points =
+ * grid_w*grid_h, or 0 for the reference's empty result (no seed found, or nothing computed).
+ * With cfg->truncate_roi_subsets (masked subsets; x and y outputs required) the images are padded
+ * as SubsetDIC::compute pads them, the grid points are gx * step - pad, and seed_out is in image
+ * coordinates. */
 tdic_status tdic_subset_compute(tdic_ctx* ctx, const void* reference, const void* deformed,
                                 int32_t width, int32_t height, tdic_dtype dtype,
                                 const uint8_t* roi, const tdic_config* cfg, tdic_grid_out* out,

@@ -37,6 +37,7 @@ CONFIG_FIELDS = [
     ("precision", C.c_int32), ("sp_convergence_threshold", C.c_double), ("seed_count", C.c_int32),
     ("kmeans_iterations", C.c_int32), ("seed_max_znssd", C.c_double), ("min_displacement_norm", C.c_double),
     ("min_texture_std", C.c_double), ("kmeans_sample_limit", C.c_int32), ("propagation_mode", C.c_int32),
+    ("truncate_roi_subsets", C.c_int32), ("min_valid_samples", C.c_int32), ("min_valid_sample_ratio", C.c_double),
 ]
 
 
@@ -93,7 +94,12 @@ def lib():
             L.orc_reference_gradient.argtypes = [P, C.c_int, C.c_int, P, P]
             L.orc_solve_pois.argtypes = [P, C.c_int, C.c_int, P, P, P, C.c_int, C.c_int, C.POINTER(Config),
                                          C.c_int, P, P, P, P]
+            L.orc_solve_pois_masked.argtypes = [P, C.c_int, C.c_int, P, P, P, P, C.c_int, C.c_int, C.POINTER(Config),
+                                                C.c_int, P, P, P, P]
             L.orc_grid_dims.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+            L.orc_subset_padding.argtypes = [C.POINTER(Config)]
+            L.orc_truncated_grid_dims.argtypes = [C.c_int, C.c_int, C.POINTER(Config), C.POINTER(C.c_int),
+                                                  C.POINTER(C.c_int)]
             L.orc_propagate.argtypes = [P, C.c_int, C.c_int, P, P, P, P, C.POINTER(Config), C.POINTER(Seed),
                                         C.c_int, C.POINTER(GridOut), C.POINTER(C.c_int)]
             L.orc_integer_search.argtypes = [P, P, C.c_int, C.c_int, C.POINTER(Config), C.c_double, C.c_double,
@@ -177,7 +183,8 @@ def reference_gradient(image):
     return gx, gy
 
 
-def solve_pois(reference, coeffs, cfg, xy, p0, confidence0=None, gradients=None, degree=None, border=None):
+def solve_pois(reference, coeffs, cfg, xy, p0, confidence0=None, gradients=None, degree=None, border=None,
+               roi=None, masked=False):
     """Per-POI solve: ICGN or FGN (cfg.optimizer), first or second order (cfg.shape_order), ZNSSD or
     SSD (cfg.criterion 1 / 0).  Returns a dict of arrays; "q" holds the six second-order terms."""
     cfg = as_config(cfg)
@@ -195,8 +202,13 @@ def solve_pois(reference, coeffs, cfg, xy, p0, confidence0=None, gradients=None,
     out = (PoiResult * max(n, 1))()
     d = cfg.degree if degree is None else degree
     b = cfg.border if border is None else border
-    rc = lib().orc_solve_pois(_ptr(ref), w, h, _ptr(gx), _ptr(gy), _ptr(c), d, b, C.byref(cfg), n,
-                              _ptr(xy), _ptr(p0), _ptr(conf), C.addressof(out))
+    if masked:  # solve_with_mask over roi (None: every pixel valid)
+        m = None if roi is None else np.ascontiguousarray(roi != 0, np.uint8)
+        rc = lib().orc_solve_pois_masked(_ptr(ref), w, h, _ptr(m), _ptr(gx), _ptr(gy), _ptr(c), d, b, C.byref(cfg),
+                                         n, _ptr(xy), _ptr(p0), _ptr(conf), C.addressof(out))
+    else:
+        rc = lib().orc_solve_pois(_ptr(ref), w, h, _ptr(gx), _ptr(gy), _ptr(c), d, b, C.byref(cfg), n,
+                                  _ptr(xy), _ptr(p0), _ptr(conf), C.addressof(out))
     if rc != 0:
         raise ValueError("degree must be 1, 3 or 5")
     arr = np.frombuffer(out, dtype=np.dtype([("p", "<f8", 6), ("correlation", "<f8"), ("iterations", "<i4"),
@@ -205,6 +217,18 @@ def solve_pois(reference, coeffs, cfg, xy, p0, confidence0=None, gradients=None,
     return {"p": arr["p"].copy(), "q": arr["q"].copy(), "correlation": arr["correlation"].copy(),
             "iterations": arr["iterations"].copy(), "status": arr["status"].copy(),
             "valid": arr["valid"].astype(bool), "converged": arr["converged"].astype(bool)}
+
+
+def subset_padding(cfg) -> int:
+    """recommended_subset_padding (src/subset/padding.cpp:28-36)."""
+    return lib().orc_subset_padding(C.byref(as_config(cfg)))
+
+
+def truncated_grid_dims(w, h, cfg):
+    """Grid of subset_compute's output when truncating (the padded grid cropped to the image)."""
+    gw, gh = C.c_int(), C.c_int()
+    lib().orc_truncated_grid_dims(w, h, C.byref(as_config(cfg)), C.byref(gw), C.byref(gh))
+    return gw.value, gh.value
 
 
 def grid_dims(w, h, spacing):
@@ -295,7 +319,8 @@ def subset_compute(reference, deformed, cfg=None, roi=None):
     ref, de = _img(reference), _img(deformed)
     h, w = ref.shape
     r = None if roi is None else np.ascontiguousarray(roi != 0, np.uint8)
-    gw, gh = grid_dims(w, h, cfg.propagation_spacing)
+    pad = subset_padding(cfg) if cfg.truncate_roi_subsets else 0
+    gw, gh = grid_dims(w + 2 * pad, h + 2 * pad, cfg.propagation_spacing)
     arrs, g = _alloc_grid(gw * gh)
     seed = Seed()
     n = lib().orc_subset_compute(_ptr(ref), _ptr(de), w, h, _ptr(r), C.byref(cfg), C.byref(g), C.byref(seed))

@@ -440,7 +440,25 @@ struct SolverCfg {
     int radius; int max_iter; double thr; int optimizer;
     int order = 1;      // shape function: 1 first order (6 parameters), 2 second order (12)
     bool ssd = false;   // objective: SSD instead of ZNSSD
+    // masked subsets (solve_with_mask, truncate_roi_subsets): samples outside the image or the
+    // ROI are left out; NULL = the full circular subset of solve_with_interpolators
+    const uint8_t* roi = nullptr;
+    int min_valid = 12;
+    double ratio = 0.5;
 };
+
+// Subset samples of the masked routes (icgn.cpp:629-704 and its siblings): the centre must be a
+// ROI pixel (no margin check); a circle sample counts towards the full count, and is kept only
+// inside the image and the ROI; at least max(NP, min_valid_samples, ceil(ratio * full)) kept.
+inline bool masked_centre_ok(const SolverCfg& c, int w, int h, int cx, int cy) {
+    return cx >= 0 && cy >= 0 && cx < w && cy < h && c.roi[static_cast<std::size_t>(cy) * w + cx] != 0;
+}
+inline bool masked_keep(const SolverCfg& c, int w, int h, int x, int y) {
+    return x >= 0 && y >= 0 && x < w && y < h && c.roi[static_cast<std::size_t>(y) * w + x] != 0;
+}
+inline int masked_min_samples(const SolverCfg& c, int np, int full) {
+    return std::max(np, std::max(c.min_valid, static_cast<int>(std::ceil(c.ratio * static_cast<double>(full)))));
+}
 
 void init_result(orc_poi_result& r, const double* p0, double conf) {
     // icgn.cpp:454-462: u, v from the initial guess, gradients default to zero.
@@ -495,13 +513,18 @@ orc_poi_result solve_icgn(const float* ref, int w, int h, const GradSource& gs, 
     if (w <= 0 || h <= 0 || cfg.radius < 1 || cfg.max_iter < 0) return res;
     const int cx = static_cast<int>(std::round(px)), cy = static_cast<int>(std::round(py));
     const int r = cfg.radius;
-    if (cx - r < 0 || cy - r < 0 || cx + r >= w || cy + r >= h) return res;
+    const bool masked = cfg.roi != nullptr;
+    if (masked ? !masked_centre_ok(cfg, w, h, cx, cy) : (cx - r < 0 || cy - r < 0 || cx + r >= w || cy + r >= h))
+        return res;
     std::vector<Sample> s;
     s.reserve(static_cast<std::size_t>((2 * r + 1) * (2 * r + 1)));
     double mean = 0.0;
+    int full = 0;
     for (int dy = -r; dy <= r; ++dy)
         for (int dx = -r; dx <= r; ++dx) {
             if (dx * dx + dy * dy > r * r) continue;
+            ++full;
+            if (masked && !masked_keep(cfg, w, h, cx + dx, cy + dy)) continue;
             Sample q;
             q.lx = dx; q.ly = dy;
             q.ref = static_cast<double>(ref[static_cast<std::size_t>(cy + dy) * w + cx + dx]);
@@ -511,7 +534,7 @@ orc_poi_result solve_icgn(const float* ref, int w, int h, const GradSource& gs, 
             mean += q.ref;
             s.push_back(q);
         }
-    if (s.size() < static_cast<std::size_t>(NP)) return res;
+    if (static_cast<int>(s.size()) < (masked ? masked_min_samples(cfg, NP, full) : NP)) return res;
     const double N = static_cast<double>(s.size());
     double norm = 1.0;
     if (!cfg.ssd) {
@@ -611,19 +634,24 @@ orc_poi_result solve_fgn(const float* ref, int w, int h, const Spline& sp, const
     if (w <= 0 || h <= 0 || cfg.radius < 1 || cfg.max_iter < 0) return res;
     const int cx = static_cast<int>(std::round(px)), cy = static_cast<int>(std::round(py));
     const int r = cfg.radius;
-    if (cx - r < 0 || cy - r < 0 || cx + r >= w || cy + r >= h) return res;
+    const bool masked = cfg.roi != nullptr;
+    if (masked ? !masked_centre_ok(cfg, w, h, cx, cy) : (cx - r < 0 || cy - r < 0 || cx + r >= w || cy + r >= h))
+        return res;
     std::vector<Sample> s;
     double mean = 0.0;
+    int full = 0;
     for (int dy = -r; dy <= r; ++dy)
         for (int dx = -r; dx <= r; ++dx) {
             if (dx * dx + dy * dy > r * r) continue;
+            ++full;
+            if (masked && !masked_keep(cfg, w, h, cx + dx, cy + dy)) continue;
             Sample q;
             q.lx = dx; q.ly = dy;
             q.ref = static_cast<double>(ref[static_cast<std::size_t>(cy + dy) * w + cx + dx]);
             mean += q.ref;
             s.push_back(q);
         }
-    if (s.size() < static_cast<std::size_t>(NP)) return res;
+    if (static_cast<int>(s.size()) < (masked ? masked_min_samples(cfg, NP, full) : NP)) return res;
     const double N = static_cast<double>(s.size());
     double norm = 1.0;
     if (!cfg.ssd) {
@@ -634,7 +662,13 @@ orc_poi_result solve_fgn(const float* ref, int w, int h, const Spline& sp, const
         if (norm <= kEps) { res.status = kNumericalFailure; return res; }
         for (auto& q : s) q.refn = (q.ref - mean) / norm;
     }
-    const double cap = cfg.ssd ? 0.35 : 0.5;
+    // Step cap, whether convergence is tested on the capped norm, and the damping term per route
+    // (forward_gauss_newton.cpp: unmasked 367-379, 763-774, 1242-1271, 1682-1713; masked 572-584,
+    // 936-948, 1485-1496, 1886-1915): the masked second-order ZNSSD route has no damping term,
+    // caps at 0.3 and tests the norm before the cap; the masked first-order SSD route tests the capped one.
+    const double cap = cfg.ssd ? 0.35 : (masked && NP == 12 ? 0.3 : 0.5);
+    const bool test_capped = masked ? !(NP == 12 && !cfg.ssd) : !(NP == 6 && cfg.ssd);
+    const bool damping = NP == 12 && (!masked || cfg.ssd);
     double p[NP];
     for (int i = 0; i < NP; ++i) p[i] = i < 6 ? p0[i] : 0.0;
     double corr = kInf;
@@ -693,7 +727,7 @@ orc_poi_result solve_fgn(const float* ref, int w, int h, const Spline& sp, const
             for (int a = 0; a < NP; ++a) for (int b = 0; b < NP; ++b) H[a][b] *= hs;
             for (int a = 0; a < NP; ++a) grad[a] *= 2.0 / norm;
         }
-        if constexpr (NP == 12) {  // forward_gauss_newton.cpp:1242-1245, 1682-1685
+        if (damping) {  // forward_gauss_newton.cpp:1242-1245, 1682-1685, 1886-1889
             double dmax = H[0][0];
             for (int a = 1; a < NP; ++a) dmax = std::max(dmax, H[a][a]);
             const double lambda = 1e-4 * dmax;
@@ -715,8 +749,7 @@ orc_poi_result solve_fgn(const float* ref, int w, int h, const Spline& sp, const
             for (int k = 0; k < NP; ++k) dp[k] *= cap / dn;
             dn = cap;
         }
-        // first-order SSD tests convergence on the norm before the cap (:764, :774)
-        const double dn_test = (NP == 6 && cfg.ssd) ? dn_raw : dn;
+        const double dn_test = test_capped ? dn : dn_raw;
         double pn[NP];
         if constexpr (NP == 6) compose_warp(p, dp, pn);
         else compose_warp2(p, dp, pn);
@@ -816,7 +849,14 @@ int propagate(const float* ref, int w, int h, const uint8_t* roi, const GradSour
     const int gw = (w + step - 1) / step, gh = (h + step - 1) / step;
     clear_grid(out, gw, gh, step);
     const int radius = c.subset_radius;
-    const SolverCfg scfg = solver_cfg(c);
+    SolverCfg scfg = solver_cfg(c);
+    std::vector<uint8_t> ones;
+    if (c.truncate_roi_subsets) {  // solve_with_mask (reliability_propagation.cpp:233-238, 341-347)
+        if (roi == nullptr) ones.assign(static_cast<std::size_t>(w) * h, 1);
+        scfg.roi = roi ? roi : ones.data();
+        scfg.min_valid = c.min_valid_samples;
+        scfg.ratio = c.min_valid_sample_ratio;
+    }
     std::vector<uint8_t> calc(static_cast<std::size_t>(gw) * gh, 0);
     const double cutoff_corr = c.propagation_max_znssd, cutoff_disp = static_cast<double>(step);
     int computed = 0;
@@ -1034,6 +1074,30 @@ std::vector<ISample> circ_samples(const float* ref, int w, int cx, int cy, int r
         }
     return s;
 }
+// collect_masked_reference_samples (integer_search.cpp:82-108): samples inside the image and the ROI.
+std::vector<ISample> circ_samples_masked(const float* ref, int w, int h, const uint8_t* roi, int cx, int cy, int r,
+                                         int step) {
+    step = std::max(1, step);
+    std::vector<ISample> s;
+    for (int dy = -r; dy <= r; dy += step)
+        for (int dx = -r; dx <= r; dx += step) {
+            if (dx * dx + dy * dy > r * r) continue;
+            const int x = cx + dx, y = cy + dy;
+            if (x < 0 || y < 0 || x >= w || y >= h || !roi[static_cast<std::size_t>(y) * w + x]) continue;
+            s.push_back({dx, dy, static_cast<double>(ref[static_cast<std::size_t>(y) * w + x])});
+        }
+    return s;
+}
+int full_circle_count(int r, int step) {  // integer_search.cpp:33-45
+    step = std::max(1, step);
+    int n = 0;
+    for (int dy = -r; dy <= r; dy += step)
+        for (int dx = -r; dx <= r; dx += step) n += dx * dx + dy * dy <= r * r ? 1 : 0;
+    return n;
+}
+int min_required_samples(int r, int step) {  // integer_search.cpp:47-50
+    return std::max(12, static_cast<int>(std::ceil(0.5 * full_circle_count(r, step))));
+}
 double s_mean(const std::vector<ISample>& s) { double m = 0; for (auto& q : s) m += q.v; return s.empty() ? 0.0 : m / static_cast<double>(s.size()); }
 double s_norm(const std::vector<ISample>& s, double m) { double n = 0; for (auto& q : s) { const double d = q.v - m; n += d * d; } return n; }
 
@@ -1071,20 +1135,28 @@ Cand search_disp(const float* def, int w, int h, const std::vector<ISample>& s, 
     return best;
 }
 
+// roi != NULL: estimate_with_mask_interpolators (integer_search.cpp:447-545): the centre must be a
+// ROI pixel, the samples are the ROI ones and at least min_required_samples of them.
 bool integer_search(const float* ref, const float* def, int w, int h, const orc_config& c,
-                    double px, double py, double& ou, double& ov, double& oz) {
+                    double px, double py, double& ou, double& ov, double& oz, const uint8_t* roi = nullptr) {
     const int cx = static_cast<int>(std::round(px)), cy = static_cast<int>(std::round(py));
     const int r = std::max(1, c.is_subset_radius);
-    if (!(cx - r >= 0 && cy - r >= 0 && cx + r < w && cy + r < h)) return false;
-    const auto s = circ_samples(ref, w, cx, cy, r, 1);
+    if (roi) {
+        if (!(cx >= 0 && cy >= 0 && cx < w && cy < h) || !roi[static_cast<std::size_t>(cy) * w + cx]) return false;
+    } else if (!(cx - r >= 0 && cy - r >= 0 && cx + r < w && cy + r < h)) {
+        return false;
+    }
+    const auto s = roi ? circ_samples_masked(ref, w, h, roi, cx, cy, r, 1) : circ_samples(ref, w, cx, cy, r, 1);
+    if (roi && static_cast<int>(s.size()) < min_required_samples(r, 1)) return false;
     const double rm = s_mean(s), rn = s_norm(s, rm);
     if (s.empty() || rn <= kEps) return false;
     const int search = std::max(0, c.is_search_radius);
     const int cstep = c.pyramid_enabled ? std::max(1, std::max(1, c.pyramid_scale)) : 1;
-    const auto cs = circ_samples(ref, w, cx, cy, r, cstep);
+    const auto cs = roi ? circ_samples_masked(ref, w, h, roi, cx, cy, r, cstep) : circ_samples(ref, w, cx, cy, r, cstep);
     const double crm = s_mean(cs), crn = s_norm(cs, crm);
     Cand best;
-    if (!cs.empty() && crn > kEps) {  // search_ncorr_multigrid :208-265
+    const bool coarse_ok = roi ? static_cast<int>(cs.size()) >= min_required_samples(r, cstep) : !cs.empty();
+    if (coarse_ok && crn > kEps) {  // search_ncorr_multigrid :208-265
         const int minu = r - cx, maxu = w - 1 - r - cx, minv = r - cy, maxv = h - 1 - r - cy;
         if (!(minu > maxu || minv > maxv)) {
             const Cand coarse = search_disp(def, w, h, cs, crm, crn, cx, cy, r, minu, maxu, minv, maxv, cstep);
@@ -1152,9 +1224,31 @@ std::vector<Pt> det_sample(const std::vector<Pt>& pts, int limit) {  // :33-47
 std::vector<std::pair<double, double>> gen_candidates(const float* ref, int w, int h, const uint8_t* roi, const orc_config& c) {  // :207-317
     std::vector<std::pair<double, double>> cands;
     const int rad = std::max(std::max(1, c.is_subset_radius), std::max(1, c.sp_subset_radius));
-    auto margin_ok = [&](int x, int y) { return !(x - rad < 0 || y - rad < 0 || x + rad >= w || y + rad >= h); };
+    const bool trunc = c.truncate_roi_subsets != 0;
+    // is_candidate_margin_valid (:388-422): the search radius widens the margin when truncating,
+    // and the circle of radius `rad` must then hold enough ROI pixels
+    const int margin = rad + (trunc ? std::max(0, c.is_search_radius) : 0);
+    auto margin_ok = [&](int x, int y) {
+        if (x - margin < 0 || y - margin < 0 || x + margin >= w || y + margin >= h) return false;
+        if (!trunc) return true;
+        int valid = 0, full = 0;
+        for (int yy = y - rad; yy <= y + rad; ++yy)
+            for (int xx = x - rad; xx <= x + rad; ++xx) {
+                const int dx = xx - x, dy = yy - y;
+                if (dx * dx + dy * dy > rad * rad) continue;
+                ++full;
+                valid += roi_valid(roi, w, h, xx, yy) ? 1 : 0;
+            }
+        const int need = std::max(c.min_valid_samples,
+                                  static_cast<int>(std::ceil(c.min_valid_sample_ratio * static_cast<double>(full))));
+        return valid >= std::max(6, need);
+    };
     std::vector<Pt> pts;
-    for (int y = 0; y < h; ++y) for (int x = 0; x < w; ++x) if (roi_valid(roi, w, h, x, y) && margin_ok(x, y)) pts.push_back({x, y});
+    if (trunc) {  // :219-229: ROI points inside the search margin (no sample count)
+        for (int y = margin; y < h - margin; ++y) for (int x = margin; x < w - margin; ++x) if (roi_valid(roi, w, h, x, y)) pts.push_back({x, y});
+    } else {
+        for (int y = 0; y < h; ++y) for (int x = 0; x < w; ++x) if (roi_valid(roi, w, h, x, y) && margin_ok(x, y)) pts.push_back({x, y});
+    }
     if (pts.empty()) for (int y = 0; y < h; ++y) for (int x = 0; x < w; ++x) if (roi_valid(roi, w, h, x, y)) pts.push_back({x, y});
     if (pts.empty()) return cands;
     const int requested = std::max(1, c.seed_count);
@@ -1242,13 +1336,23 @@ bool select_seed(const float* ref, const float* def, int w, int h, const uint8_t
     // subset_initializer.cpp:165-177: the subpixel solver is first-order ICGN with the configured objective
     SolverCfg scfg{std::max(1, c.sp_subset_radius), std::max(0, c.sp_max_iterations), c.sp_convergence_threshold, 0};
     scfg.ssd = c.criterion == 0;
+    // truncate_roi_subsets: masked integer search and masked refinement (subset_initializer.cpp:140-149, 206-245)
+    std::vector<uint8_t> ones;
+    const uint8_t* mask = nullptr;
+    if (c.truncate_roi_subsets) {
+        if (roi == nullptr) ones.assign(static_cast<std::size_t>(w) * h, 1);
+        mask = roi ? roi : ones.data();
+        scfg.roi = mask;
+        scfg.min_valid = c.min_valid_samples;
+        scfg.ratio = c.min_valid_sample_ratio;
+    }
     SeedEval best;
     bool found = false;
     for (const auto& cd : cands) {
         SeedEval ev;
         ev.x = cd.first; ev.y = cd.second;
         double iu, iv, iz;
-        if (!integer_search(ref, def, w, h, c, cd.first, cd.second, iu, iv, iz)) continue;
+        if (!integer_search(ref, def, w, h, c, cd.first, cd.second, iu, iv, iz, mask)) continue;
         double p[6] = {iu, iv, 0, 0, 0, 0};
         double conf = znssd_from_zncc(iz), quality = conf;
         if (refine) {  // subset_initializer.cpp:152-204
@@ -1300,6 +1404,7 @@ void orc_config_default(orc_config* c) {
     c->seed_count = 256; c->kmeans_iterations = 20; c->seed_max_znssd = 0.2;
     c->min_displacement_norm = 0.0; c->min_texture_std = 0.0; c->kmeans_sample_limit = 20000;
     c->propagation_mode = 1;
+    c->truncate_roi_subsets = 0; c->min_valid_samples = 12; c->min_valid_sample_ratio = 0.5;
 }
 
 double orc_bspline_basis(double x, int r, int d) { return valid_degree(d) ? basis(x, r, d) : kNaN; }
@@ -1347,6 +1452,24 @@ int orc_solve_pois(const float* ref, int w, int h, const double* ref_gx, const d
     return 0;
 }
 
+int orc_solve_pois_masked(const float* ref, int w, int h, const uint8_t* roi, const double* ref_gx,
+                          const double* ref_gy, const double* coeffs, int d, int border, const orc_config* cfg,
+                          int n, const double* xy, const double* p0, const double* conf0, orc_poi_result* out) {
+    if (!valid_degree(d)) return -1;
+    Spline sp;
+    sp.init(coeffs, w, h, d, border);
+    GradSource gs{ref, w, h, ref_gx, ref_gy};
+    std::vector<uint8_t> ones;
+    if (!roi) ones.assign(static_cast<std::size_t>(w) * h, 1);
+    SolverCfg scfg = solver_cfg(*cfg);
+    scfg.roi = roi ? roi : ones.data();
+    scfg.min_valid = cfg->min_valid_samples;
+    scfg.ratio = cfg->min_valid_sample_ratio;
+    for (int i = 0; i < n; ++i)
+        out[i] = solve_one(ref, w, h, gs, sp, scfg, xy[2 * i], xy[2 * i + 1], p0 + 6 * i, conf0 ? conf0[i] : 0.0);
+    return 0;
+}
+
 void orc_grid_dims(int w, int h, int spacing, int* gw, int* gh) {
     const int step = std::max(0, spacing) + 1;
     *gw = (w + step - 1) / step;
@@ -1377,9 +1500,93 @@ int orc_select_seed(const float* ref, const float* def, int w, int h, const uint
     return ok ? 1 : 0;
 }
 
+int orc_subset_padding(const orc_config* c) {  // padding.cpp:28-36
+    const int ir = std::max(1, c->is_subset_radius), sr = std::max(1, c->sp_subset_radius);
+    return std::max(0, c->is_search_radius) + std::max(c->subset_radius, std::max(ir, sr)) + std::max(0, c->border);
+}
+
+void orc_truncated_grid_dims(int w, int h, const orc_config* c, int* gw, int* gh) {
+    const int pad = c->truncate_roi_subsets ? orc_subset_padding(c) : 0;
+    const int step = std::max(0, c->propagation_spacing) + 1;
+    auto count = [&](int n) {  // grid points gx * step - pad inside [0, n)
+        const int lo = (pad + step - 1) / step, hi = (n - 1 + pad) / step;
+        return std::max(0, hi - lo + 1);
+    };
+    *gw = count(w);
+    *gh = count(h);
+}
+
+namespace {
+int mirror_index(int i, int n) {  // padding.cpp:11-24
+    if (n <= 1) return 0;
+    while (i < 0 || i >= n) i = i < 0 ? -i - 1 : 2 * n - i - 1;
+    return i;
+}
+}  // namespace
+
 int orc_subset_compute(const float* ref, const float* def, int w, int h, const uint8_t* roi,
                        const orc_config* cfg, orc_grid_out* out, orc_seed* seed_out) {
     if (w <= 0 || h <= 0 || !ref || !def) return 0;
+    if (cfg->truncate_roi_subsets) {
+        // subset_dic.cpp:53-104: mirror-padded images, zero-padded ROI, the padded result cropped
+        const int pad = orc_subset_padding(cfg);
+        const int pw = w + 2 * pad, ph = h + 2 * pad;
+        std::vector<float> pr(static_cast<std::size_t>(pw) * ph), pd(pr.size());
+        std::vector<uint8_t> pm(pr.size(), 0);
+        for (int y = 0; y < ph; ++y)
+            for (int x = 0; x < pw; ++x) {
+                const std::size_t s = static_cast<std::size_t>(mirror_index(y - pad, h)) * w + mirror_index(x - pad, w);
+                pr[static_cast<std::size_t>(y) * pw + x] = ref[s];
+                pd[static_cast<std::size_t>(y) * pw + x] = def[s];
+            }
+        for (int y = 0; y < h; ++y)
+            for (int x = 0; x < w; ++x)
+                pm[static_cast<std::size_t>(y + pad) * pw + x + pad] = roi ? (roi[static_cast<std::size_t>(y) * w + x] != 0) : 1;
+        orc_config c = *cfg;
+        c.truncate_roi_subsets = 1;
+        int gw, gh;
+        orc_grid_dims(pw, ph, c.propagation_spacing, &gw, &gh);
+        const std::size_t n = static_cast<std::size_t>(gw) * gh;
+        std::vector<double> d[16];
+        for (auto& a : d) a.assign(n, 0.0);
+        std::vector<uint8_t> valid(n), conv(n);
+        std::vector<int8_t> status(n);
+        std::vector<int32_t> iters(n);
+        orc_grid_out t{d[0].data(), d[1].data(), d[2].data(), d[3].data(), d[4].data(), d[5].data(), d[6].data(),
+                       d[7].data(), d[8].data(), valid.data(), status.data(), iters.data(), conv.data(),
+                       d[9].data(), d[10].data(), d[11].data(), d[12].data(), d[13].data(), d[14].data()};
+        orc_seed seed;
+        const bool found = select_seed(pr.data(), pd.data(), pw, ph, pm.data(), c, seed, nullptr);
+        if (found) { seed.x -= pad; seed.y -= pad; }
+        if (seed_out) *seed_out = seed;
+        if (!found) return 0;
+        seed.x += pad; seed.y += pad;
+        const int border = std::max(3, c.border);
+        std::vector<double> coeffs(static_cast<std::size_t>(pw + 2 * border) * (ph + 2 * border));
+        form_coefficients(pd.data(), pw, ph, c.degree, border, true, coeffs.data());
+        std::vector<double> gx(pr.size()), gy(pr.size());
+        orc_reference_gradient(pr.data(), pw, ph, gx.data(), gy.data());
+        Spline sp;
+        sp.init(coeffs.data(), pw, ph, c.degree, border);
+        GradSource gs{pr.data(), pw, ph, gx.data(), gy.data()};
+        if (propagate(pr.data(), pw, ph, pm.data(), gs, sp, c, seed, -1, &t, nullptr) == 0) return 0;
+        int k = 0;
+        for (std::size_t i = 0; i < n; ++i) {
+            const double x = t.x[i] - pad, y = t.y[i] - pad;
+            if (x < 0.0 || y < 0.0 || x >= w || y >= h) continue;
+            out->x[k] = x; out->y[k] = y;
+            out->u[k] = t.u[i]; out->v[k] = t.v[i];
+            out->du_dx[k] = t.du_dx[i]; out->du_dy[k] = t.du_dy[i]; out->dv_dx[k] = t.dv_dx[i]; out->dv_dy[k] = t.dv_dy[i];
+            out->correlation[k] = t.correlation[i];
+            out->valid[k] = t.valid[i]; out->status[k] = t.status[i]; out->iterations[k] = t.iterations[i];
+            out->converged[k] = t.converged[i];
+            double* src2[6] = {t.d2u_dx2, t.d2u_dxdy, t.d2u_dy2, t.d2v_dx2, t.d2v_dxdy, t.d2v_dy2};
+            double* dst2[6] = {out->d2u_dx2, out->d2u_dxdy, out->d2u_dy2, out->d2v_dx2, out->d2v_dxdy, out->d2v_dy2};
+            for (int j = 0; j < 6; ++j) if (dst2[j]) dst2[j][k] = src2[j][i];
+            ++k;
+        }
+        return k;
+    }
     orc_seed seed;
     if (!select_seed(ref, def, w, h, roi, *cfg, seed, nullptr)) { if (seed_out) *seed_out = seed; return 0; }
     if (seed_out) *seed_out = seed;

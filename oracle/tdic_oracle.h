@@ -63,6 +63,9 @@ typedef struct orc_config {
     int32_t kmeans_sample_limit;       /* 20000 */
     int32_t propagation_mode;          /* 1 = reliability-guided heap order (reference, default), 0 = frontier waves,
                                           2 = dataflow (axis parents toward the seed) + frontier-wave cleanup */
+    int32_t truncate_roi_subsets;      /* subset.truncate_roi_subsets (YAML only)        0 */
+    int32_t min_valid_samples;         /* subset.min_valid_samples                       12 */
+    double min_valid_sample_ratio;     /* subset.min_valid_sample_ratio                 0.5 */
 } orc_config;
 
 /* Per-POI solver result; mirrors dic::Displacement2D (result.hpp:32-51) plus the additive
@@ -124,6 +127,13 @@ int orc_solve_pois(const float* ref, int w, int h, const double* ref_gx, const d
                    const double* coeffs, int degree, int border, const orc_config* cfg,
                    int n, const double* xy, const double* p0, const double* confidence0,
                    orc_poi_result* out);
+/* solve_with_mask (icgn.cpp:407-432, forward_gauss_newton.cpp:144-170): the masked routes
+ * (icgn.cpp:629-818, 990-1154, 1364-1562, 1741-1912; forward_gauss_newton.cpp:401-604, 796-968,
+ * 1299-1522, 1741-1941) over the ROI mask `roi` (h x w, NULL = every pixel valid). */
+int orc_solve_pois_masked(const float* ref, int w, int h, const uint8_t* roi, const double* ref_gx,
+                          const double* ref_gy, const double* coeffs, int degree, int border,
+                          const orc_config* cfg, int n, const double* xy, const double* p0,
+                          const double* confidence0, orc_poi_result* out);
 
 void orc_grid_dims(int w, int h, int spacing, int* grid_w, int* grid_h);
 
@@ -144,9 +154,15 @@ int orc_select_seed(const float* ref, const float* def, int w, int h, const uint
                     const orc_config* cfg, orc_seed* seed, double* cand_xy, int cand_cap,
                     int* n_candidates);
 /* subset_dic.cpp:39-105 + bind_subset.cpp:253-315: returns the number of output points
- * (grid_w*grid_h) or 0 for the empty result. */
+ * (grid_w*grid_h) or 0 for the empty result.  With truncate_roi_subsets the images are
+ * mirror-padded and the ROI zero-padded by recommended_subset_padding (src/subset/padding.cpp:28-36),
+ * the grid is laid over the padded image and only its points inside the original image are
+ * written, shifted back (subset_dic.cpp:53-104): size `out` for orc_truncated_grid_dims. */
 int orc_subset_compute(const float* ref, const float* def, int w, int h, const uint8_t* roi,
                        const orc_config* cfg, orc_grid_out* out, orc_seed* seed_out);
+/* recommended_subset_padding (padding.cpp:28-36) and the grid of the padded image. */
+int orc_subset_padding(const orc_config* cfg);
+void orc_truncated_grid_dims(int w, int h, const orc_config* cfg, int* grid_w, int* grid_h);
 
 #ifdef __cplusplus
 }

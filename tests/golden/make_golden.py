@@ -29,6 +29,14 @@ small workload's pair (affine field) and for a 256 x 256 pair with a Gaussian bu
     the first-order SSD route converging on the norm before the cap, and the second-order routes
     with the 1e-4 * max(diag H) damping term.
 
+tests/golden/subset_masked_256.npz holds masked subsets (solve_with_mask, icgn.cpp:629-818 and
+siblings; forward_gauss_newton.cpp:401-604, 796-968, 1299-1522, 1741-1941) over a disc ROI, with
+POIs inside, on and outside its edge and at the image border: samples outside the image or the
+ROI are dropped, the centre must be a ROI pixel (no margin check), at least max(6 or 12,
+min_valid_samples = 12, ceil(0.5 * full circle)) samples are needed; the masked FGN routes cap the
+step at 0.5 (first-order ZNSSD), 0.35 (SSD) and 0.3 (second-order ZNSSD, no damping term,
+convergence on the norm before the cap).
+
 Run from the repository root:  python tests/golden/make_golden.py
 """
 import math
@@ -251,8 +259,9 @@ def sd_rows(a, b, lx, ly, order):
     return np.column_stack(cols)
 
 
-def solve_variant(ref, coef, qk, px, py, p0, optimizer, order, ssd):
-    """(p[12], correlation, iterations, status, converged) of one POI on one solver route."""
+def solve_variant(ref, coef, qk, px, py, p0, optimizer, order, ssd, roi=None):
+    """(p[12], correlation, iterations, status, converged) of one POI on one solver route;
+    roi: the masked route over that mask."""
     h, w = ref.shape
     npar = 6 * order
     cx, cy = int(np.round(px)), int(np.round(py))
@@ -260,10 +269,23 @@ def solve_variant(ref, coef, qk, px, py, p0, optimizer, order, ssd):
     p = np.zeros(npar)
     p[:2] = p0
     out = lambda st, corr, it, conv: (np.concatenate([p[:6], p[6:], np.zeros(12 - npar)]), corr, it, st, conv)
-    if cx - r < 0 or cy - r < 0 or cx + r >= w or cy + r >= h:
+    masked = roi is not None
+    if masked:
+        if not (0 <= cx < w and 0 <= cy < h) or not roi[cy, cx]:
+            return out(2, np.nan, 0, False)
+    elif cx - r < 0 or cy - r < 0 or cx + r >= w or cy + r >= h:
         return out(2, np.nan, 0, False)
     off = np.array([(dx, dy) for dy in range(-r, r + 1) for dx in range(-r, r + 1) if dx * dx + dy * dy <= r * r],
                    dtype=np.float64)
+    full = len(off)
+    if masked:
+        xx, yy = cx + off[:, 0].astype(int), cy + off[:, 1].astype(int)
+        inside = (xx >= 0) & (yy >= 0) & (xx < w) & (yy < h)
+        keep = inside.copy()
+        keep[inside] = roi[yy[inside], xx[inside]]
+        off = off[keep]
+        if len(off) < max(npar, 12, int(math.ceil(0.5 * full))):
+            return out(2, np.nan, 0, False)
     lx, ly = off[:, 0], off[:, 1]
     xs, ys = cx + off[:, 0].astype(int), cy + off[:, 1].astype(int)
     f = ref[ys, xs].astype(np.float64)
@@ -281,7 +303,9 @@ def solve_variant(ref, coef, qk, px, py, p0, optimizer, order, ssd):
         gy = (ref[yp, xs].astype(np.float64) - ref[ym, xs]) / np.maximum(1, yp - ym)
         sd = sd_rows(gx, gy, lx, ly, order)
         hess = sd.T @ sd * (1.0 if ssd else 2.0 / (fn * fn))
-    cap = 0.35 if ssd else 0.5
+    cap = 0.35 if ssd else (0.3 if masked and order == 2 else 0.5)
+    test_capped = (not (order == 2 and not ssd)) if masked else (not (order == 1 and ssd))
+    damping = order == 2 and (not masked or ssd)
     corr, converged, it = np.inf, False, 0
     for it in range(1, MAX_ITER + 1):
         m = shape_terms(lx, ly, order)
@@ -317,7 +341,7 @@ def solve_variant(ref, coef, qk, px, py, p0, optimizer, order, ssd):
             sd = sd_rows(dgx * a00 + dgy * a10, dgx * a01 + dgy * a11, lx, ly, order)
             hess = sd.T @ sd * (1.0 if ssd else 2.0 / (fn * fn))
             grad = (diff @ sd) * (1.0 if ssd else 2.0 / fn)
-            if order == 2:
+            if damping:
                 hess = hess + 1e-4 * np.max(np.diag(hess)) * np.eye(npar)
             dp = np.linalg.solve(hess, grad)
         if not np.all(np.isfinite(dp)):
@@ -326,7 +350,7 @@ def solve_variant(ref, coef, qk, px, py, p0, optimizer, order, ssd):
         dn_test = dn
         if optimizer == 1 and dn > cap:
             dp = dp * (cap / dn)
-            if not (ssd and order == 1):
+            if test_capped:
                 dn_test = cap
         if optimizer == 0:
             p = ic_update(p, dp) if order == 1 else ic_update2(p, dp)
@@ -382,6 +406,42 @@ def main_variants():
     print(f"wrote {VARIANTS_OUT}")
 
 
+MASKED_OUT = os.path.join(HERE, "subset_masked_256.npz")
+MASKED = [("icgn1_znssd", 0, 1, False), ("icgn2_ssd", 0, 2, True), ("fgn1_ssd", 1, 1, True),
+          ("fgn2_znssd", 1, 2, False)]
+
+
+def disc_roi(h, w):
+    yy, xx = np.mgrid[:h, :w]
+    return ((xx - 140) ** 2 + (yy - 120) ** 2) < 95 ** 2
+
+
+def main_masked():
+    from traditional_dic_gb300 import synthetic
+    qk = qk_matrix(DEGREE)
+    pair = synthetic.workload(0)
+    ref, de = pair.reference, pair.deformed
+    h, w = ref.shape
+    roi = disc_roi(h, w)
+    coef = coefficients(de, DEGREE, BORDER)
+    pts = [(x, y) for y in range(3, 256, 19) for x in range(3, 256, 19)]
+    pois = []
+    for x, y in pts:
+        u, v = pair.field.uv(np.float64(x), np.float64(y))
+        pois.append((x, y, round(2 * float(u)) / 2.0, round(2 * float(v)) / 2.0))
+    pois = np.array(pois, np.float64)
+    arrays = {"roi": roi, "pois": pois, "settings": np.array([DEGREE, BORDER, RADIUS, MAX_ITER, THRESHOLD])}
+    for name, opt, order, ssd in MASKED:
+        res = []
+        for x, y, u0, v0 in pois:
+            p, corr, iters, status, conv = solve_variant(ref, coef, qk, x, y, (u0, v0), opt, order, ssd, roi=roi)
+            res.append(np.concatenate([p, [corr, iters, status, float(conv)]]))
+        arrays[name] = np.array(res, np.float64)
+        print(f"masked {name}: {int(sum(r[15] for r in res))} converged of {len(res)}")
+    np.savez_compressed(MASKED_OUT, **arrays)
+    print(f"wrote {MASKED_OUT}")
+
+
 def main():
     sys.path.insert(0, ROOT)
     import __graft_entry__ as G
@@ -405,6 +465,7 @@ def main():
                         settings=np.array([DEGREE, BORDER, RADIUS, MAX_ITER, THRESHOLD]))
     print(f"wrote {OUT}: {len(pois)} POIs, {int(sum(r[9] for r in res))} converged")
     main_variants()
+    main_masked()
 
 
 if __name__ == "__main__":

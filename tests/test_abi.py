@@ -29,7 +29,7 @@ def test_library_exports_every_declared_symbol(pkg):
 
 def test_struct_layouts_match_header(pkg, oracle):
     from traditional_dic_gb300 import _lib as L
-    assert C.sizeof(L.Config) == 136
+    assert C.sizeof(L.Config) == 152
     assert C.sizeof(L.Config) == C.sizeof(oracle.Config)
     assert [f for f, _ in L.Config._fields_] == [f for f, _ in oracle.Config._fields_]
     assert C.sizeof(L.PoiIn) == 72 and C.sizeof(L.PoiOut) == 120 and C.sizeof(L.Seed) == 80

@@ -132,3 +132,30 @@ def test_oracle_variants_match_golden(oracle, variants, name, opt, order, crit, 
     xy, p0 = _variant_inputs(variants, tag)
     r = oracle.solve_pois(ref, coef, cfg, xy, p0, gradients=oracle.reference_gradient(ref))
     _check_variant(r, variants[f"{name}_{tag}"], P_TOL, Q_TOL, 1e-9)
+
+
+# ---- masked subsets (tests/golden/subset_masked_256.npz) ------------------------------------
+MASKED_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "subset_masked_256.npz")
+MASKED = [("icgn1_znssd", 0, 1, 1), ("icgn2_ssd", 0, 2, 0), ("fgn1_ssd", 1, 1, 0), ("fgn2_znssd", 1, 2, 1)]
+
+
+@pytest.fixture(scope="module")
+def masked():
+    d = np.load(MASKED_FILE)
+    return {k: d[k] for k in d.files}
+
+
+@pytest.mark.parametrize("name,opt,order,crit", MASKED)
+def test_oracle_masked_match_golden(oracle, masked, golden, name, opt, order, crit):
+    cfg = _variant_config(masked, oracle.default_config, opt, order, crit)
+    cfg.truncate_roi_subsets = 1
+    ref = golden["reference"].astype(np.float32)
+    coef = oracle.prefilter(golden["deformed"].astype(np.float32), cfg.degree, cfg.border, True)
+    pois = masked["pois"]
+    p0 = np.zeros((len(pois), 6))
+    p0[:, :2] = pois[:, 2:4]
+    r = oracle.solve_pois(ref, coef, cfg, pois[:, :2], p0, gradients=oracle.reference_gradient(ref),
+                          roi=masked["roi"], masked=True)
+    want = masked[name]
+    assert (want[:, 14] == 0).sum() > 60 and (want[:, 14] == 2).sum() > 60   # both kinds of points present
+    _check_variant(r, want, P_TOL, Q_TOL, 1e-9)

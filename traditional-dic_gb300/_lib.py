@@ -28,6 +28,7 @@ CONFIG_FIELDS = [
     ("precision", C.c_int32), ("sp_convergence_threshold", C.c_double), ("seed_count", C.c_int32),
     ("kmeans_iterations", C.c_int32), ("seed_max_znssd", C.c_double), ("min_displacement_norm", C.c_double),
     ("min_texture_std", C.c_double), ("kmeans_sample_limit", C.c_int32), ("propagation_mode", C.c_int32),
+    ("truncate_roi_subsets", C.c_int32), ("min_valid_samples", C.c_int32), ("min_valid_sample_ratio", C.c_double),
 ]
 
 
@@ -73,6 +74,11 @@ class GridOut(C.Structure):
 SIGNATURES = {
     "tdic_config_default": (None, [C.POINTER(Config)]),
     "tdic_grid_dims": (None, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "tdic_subset_padding": (C.c_int32, [C.POINTER(Config)]),
+    "tdic_subset_grid_dims": (None, [C.c_int32, C.c_int32, C.POINTER(Config), C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_int32)]),
+    "tdic_solve_pois_masked": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Config), C.c_void_p, C.c_void_p,
+                                         C.c_int32, C.c_void_p, C.c_int, C.c_void_p]),
     "tdic_ctx_create": (C.c_int, [C.c_int32, C.POINTER(C.c_void_p)]),
     "tdic_ctx_destroy": (None, [C.c_void_p]),
     "tdic_last_error": (C.c_char_p, [C.c_void_p]),
@@ -149,6 +155,13 @@ def default_config() -> Config:
 def grid_dims(w: int, h: int, spacing: int):
     gw, gh = C.c_int32(), C.c_int32()
     load().tdic_grid_dims(w, h, spacing, C.byref(gw), C.byref(gh))
+    return gw.value, gh.value
+
+
+def subset_grid_dims(w: int, h: int, cfg: Config):
+    """Output grid of tdic_subset_compute (with truncate_roi_subsets: the padded grid cropped to the image)."""
+    gw, gh = C.c_int32(), C.c_int32()
+    load().tdic_subset_grid_dims(w, h, C.byref(cfg), C.byref(gw), C.byref(gh))
     return gw.value, gh.value
 
 

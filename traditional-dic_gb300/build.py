@@ -2,8 +2,8 @@
 
 nvcc compiles each translation unit in parallel (one -gencode, sm_103a) and links a shared
 library into _build/ next to this file.  variants.cu is compiled once per solver route other than
-first-order ZNSSD (-DTDIC_ROUTE=1 SSD, 2 second order, 3 second-order SSD), so the routes' kernels
-build side by side.  No torch types cross the ABI, so the library is built with plain nvcc, not
+first-order ZNSSD (-DTDIC_ROUTE=1 SSD, 2 second order, 3 second-order SSD, 4 masked first-order
+ZNSSD), so the routes' kernels build side by side.  No torch types cross the ABI, so the library is built with plain nvcc, not
 torch.utils.cpp_extension.
 """
 from __future__ import annotations
@@ -20,7 +20,7 @@ LIB = os.path.join(BUILD, "libtdic_gb300.so")
 UNITS = [("api.cu", "api.o", []), ("prefilter.cu", "prefilter.o", []), ("hotpath.cu", "hotpath.o", []),
          ("seed.cu", "seed.o", []), ("strain.cu", "strain.o", []),
          ("variants.cu", "route1.o", ["-DTDIC_ROUTE=1"]), ("variants.cu", "route2.o", ["-DTDIC_ROUTE=2"]),
-         ("variants.cu", "route3.o", ["-DTDIC_ROUTE=3"])]
+         ("variants.cu", "route3.o", ["-DTDIC_ROUTE=3"]), ("variants.cu", "route4.o", ["-DTDIC_ROUTE=4"])]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xcompiler", "-Wall", "-I", os.path.join(HERE, "..", "include")]

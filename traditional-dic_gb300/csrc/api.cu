@@ -289,9 +289,17 @@ void propagate_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, cons
         const unsigned long long q0 = 0x80000000ull;
         TDIC_CUDA_TRY(cudaMemcpyAsync(misc.as<int>() + 4, &q0, sizeof(q0), cudaMemcpyHostToDevice, s));
     }
+    // truncate_roi_subsets: the solves take the masked routes over the pixel ROI
+    // (reliability_propagation.cpp:233-238, 341-347)
+    Buffer d_roi_px(&ctx->pool, cfg.truncate_roi_subsets ? static_cast<size_t>(w) * h : 0);
+    if (cfg.truncate_roi_subsets) {
+        if (roi) TDIC_CUDA_TRY(cudaMemcpyAsync(d_roi_px.ptr, roi, static_cast<size_t>(w) * h, cudaMemcpyHostToDevice, s));
+        else TDIC_CUDA_TRY(cudaMemsetAsync(d_roi_px.ptr, 1, static_cast<size_t>(w) * h, s));
+    }
     PropagateLaunch L{};
     L.gw = gw; L.gh = gh; L.step = step;
     L.roi_grid = d_roi.as<uint8_t>();
+    L.roi_px = cfg.truncate_roi_subsets ? d_roi_px.as<uint8_t>() : nullptr;
     L.seed_idx = gys * gw + gxs;
     L.seed_solve = (gxs * step != sxr || gys * step != syr) ? 1 : 0;
     for (int k = 0; k < 6; ++k) L.seed_p[k] = seed.p[k];
@@ -412,9 +420,27 @@ std::vector<std::pair<int, int>> seed_candidates(tdic_ctx* ctx, const Acc& ref, 
                                                  const tdic_config& c, cudaStream_t s) {
     std::vector<std::pair<int, int>> out;
     const int rad = std::max(std::max(1, c.is_subset_radius), std::max(1, c.sp_subset_radius));
-    auto margin_ok = [&](int x, int y) { return !(x - rad < 0 || y - rad < 0 || x + rad >= w || y + rad >= h); };
-    ValidPoints vp(w, h, roi, rad, true);
-    if (vp.size() == 0) vp = ValidPoints(w, h, roi, rad, false);
+    // is_candidate_margin_valid (seed_selector.cpp:388-422): truncating widens the margin by the
+    // search radius and asks for enough ROI pixels in the circle of radius `rad`; the first pool
+    // of points is then every ROI point inside that margin (:219-229)
+    const bool trunc = c.truncate_roi_subsets != 0;
+    const int margin = rad + (trunc ? std::max(0, c.is_search_radius) : 0);
+    auto margin_ok = [&](int x, int y) {
+        if (x - margin < 0 || y - margin < 0 || x + margin >= w || y + margin >= h) return false;
+        if (!trunc) return true;
+        int valid = 0, full = 0;
+        for (int yy = y - rad; yy <= y + rad; ++yy)
+            for (int xx = x - rad; xx <= x + rad; ++xx) {
+                if ((xx - x) * (xx - x) + (yy - y) * (yy - y) > rad * rad) continue;
+                ++full;
+                valid += roi_ok(roi, w, h, xx, yy) ? 1 : 0;
+            }
+        const int need = std::max(c.min_valid_samples,
+                                  static_cast<int>(std::ceil(c.min_valid_sample_ratio * static_cast<double>(full))));
+        return valid >= std::max(6, need);
+    };
+    ValidPoints vp(w, h, roi, margin, true);
+    if (vp.size() == 0) vp = ValidPoints(w, h, roi, margin, false);
     const long long npts = vp.size();
     if (npts == 0) return out;
     const int requested = std::max(1, c.seed_count);
@@ -529,8 +555,16 @@ void select_seed_impl(tdic_ctx* ctx, tdic_pair* lazy, const HostImage& ref_host,
     if (n == 0) return;
     std::vector<int> cx(n), cy(n);
     for (int i = 0; i < n; ++i) { cx[i] = cands[i].first; cy[i] = cands[i].second; }
+    // truncate_roi_subsets: masked integer search and masked refinement (subset_initializer.cpp:
+    // 140-149, 206-245) over the ROI (every pixel when none is given)
+    std::vector<uint8_t> ones;
+    const uint8_t* mroi = nullptr;
+    if (c.truncate_roi_subsets) {
+        if (!roi) ones.assign(static_cast<size_t>(w) * h, 1);
+        mroi = roi ? roi : ones.data();
+    }
     std::vector<SearchResult> sr(n);
-    integer_search_batch(ctx, lazy, c, cx.data(), cy.data(), n, sr.data(), s);
+    integer_search_batch(ctx, lazy, c, cx.data(), cy.data(), n, sr.data(), s, mroi);
     // subpixel refinement: ICGN on the non-prefiltered spline (subset_initializer.cpp:152-204)
     std::vector<tdic_poi_in> in;
     std::vector<int> who;
@@ -556,6 +590,11 @@ void select_seed_impl(tdic_ctx* ctx, tdic_pair* lazy, const HostImage& ref_host,
             d_fetch(&ctx->pool, sizeof(int));
         TDIC_CUDA_TRY(cudaMemcpyAsync(d_in.ptr, in.data(), sizeof(tdic_poi_in) * in.size(), cudaMemcpyHostToDevice, s));
         SolveLaunch L{d_in.as<tdic_poi_in>(), d_out.as<tdic_poi_out>(), static_cast<int>(in.size()), d_fetch.as<int>()};
+        Buffer d_mroi(&ctx->pool, mroi ? static_cast<size_t>(w) * h : 0);
+        if (mroi) {
+            TDIC_CUDA_TRY(cudaMemcpyAsync(d_mroi.ptr, mroi, static_cast<size_t>(w) * h, cudaMemcpyHostToDevice, s));
+            L.roi = d_mroi.as<uint8_t>();
+        }
         launch_solve(ctx, lazy, sc, L, s);
         TDIC_CUDA_TRY(cudaMemcpyAsync(ref_out.data(), d_out.ptr, sizeof(tdic_poi_out) * in.size(), cudaMemcpyDeviceToHost, s));
         check_device_error(ctx, s);
@@ -608,6 +647,7 @@ void tdic_config_default(tdic_config* c) {
     c->seed_count = 256; c->kmeans_iterations = 20; c->seed_max_znssd = 0.2;
     c->min_displacement_norm = 0.0; c->min_texture_std = 0.0; c->kmeans_sample_limit = 20000;
     c->propagation_mode = 2;
+    c->truncate_roi_subsets = 0; c->min_valid_samples = 12; c->min_valid_sample_ratio = 0.5;
 }
 
 void tdic_grid_dims(int32_t w, int32_t h, int32_t spacing, int32_t* gw, int32_t* gh) {
@@ -793,6 +833,58 @@ tdic_status tdic_solve_pois(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* c
     });
 }
 
+tdic_status tdic_solve_pois_masked(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cfg, const uint8_t* roi,
+                                   const tdic_poi_in* in, int32_t n, tdic_poi_out* out, tdic_memory memory,
+                                   void* stream) {
+    return guarded(ctx, [&] {
+        TDIC_REQUIRE(pair && cfg, TDIC_INVALID_ARG, "null pair or config");
+        TDIC_REQUIRE(n >= 0, TDIC_INVALID_ARG, "negative POI count");
+        check_config(*cfg);
+        if (n == 0) return;
+        TDIC_REQUIRE(in && out, TDIC_INVALID_ARG, "null POI arrays");
+        TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
+        cudaStream_t s = pick(ctx, stream);
+        const size_t px = static_cast<size_t>(pair->w) * pair->h;
+        Buffer fetch(&ctx->pool, sizeof(int)), d_roi(&ctx->pool, px);
+        if (roi) TDIC_CUDA_TRY(cudaMemcpyAsync(d_roi.ptr, roi, px, cudaMemcpyHostToDevice, s));
+        else TDIC_CUDA_TRY(cudaMemsetAsync(d_roi.ptr, 1, px, s));
+        SolveLaunch L{in, out, n, fetch.as<int>()};
+        L.roi = d_roi.as<uint8_t>();
+        if (memory == TDIC_DEVICE) {
+            launch_solve(ctx, pair, *cfg, L, s);
+            mark_use(pair, s);
+            check_device_error(ctx, s);
+            return;
+        }
+        Buffer d_in(&ctx->pool, sizeof(tdic_poi_in) * n), d_out(&ctx->pool, sizeof(tdic_poi_out) * n);
+        TDIC_CUDA_TRY(cudaMemcpyAsync(d_in.ptr, in, sizeof(tdic_poi_in) * n, cudaMemcpyHostToDevice, s));
+        L.in = d_in.as<tdic_poi_in>();
+        L.out = d_out.as<tdic_poi_out>();
+        launch_solve(ctx, pair, *cfg, L, s);
+        mark_use(pair, s);
+        TDIC_CUDA_TRY(cudaMemcpyAsync(out, d_out.ptr, sizeof(tdic_poi_out) * n, cudaMemcpyDeviceToHost, s));
+        check_device_error(ctx, s);
+    });
+}
+
+int32_t tdic_subset_padding(const tdic_config* c) {  // recommended_subset_padding, padding.cpp:28-36
+    if (!c || !c->truncate_roi_subsets) return 0;
+    const int ir = std::max(1, c->is_subset_radius), sr = std::max(1, c->sp_subset_radius);
+    return std::max(0, c->is_search_radius) + std::max(c->subset_radius, std::max(ir, sr)) + std::max(0, c->border);
+}
+
+void tdic_subset_grid_dims(int32_t w, int32_t h, const tdic_config* c, int32_t* gw, int32_t* gh) {
+    const int pad = tdic_subset_padding(c);
+    const int step = std::max(0, c ? c->propagation_spacing : 5) + 1;
+    auto count = [&](int n) {  // padded grid points gx * step - pad inside [0, n)
+        if (n <= 0) return 0;
+        const int lo = (pad + step - 1) / step, hi = (n - 1 + pad) / step;
+        return std::max(0, hi - lo + 1);
+    };
+    *gw = count(w);
+    *gh = count(h);
+}
+
 tdic_status tdic_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cfg, const tdic_seed* seed,
                            const uint8_t* roi, tdic_grid_out* out, tdic_memory memory, int32_t* points_computed,
                            void* stream) {
@@ -848,6 +940,91 @@ static void prepare_impl(tdic_ctx* ctx, const void* reference, const void* defor
     *pair_out = pair;
 }
 
+// SubsetDIC::compute with truncate_roi_subsets (subset_dic.cpp:53-104): the images mirror-padded
+// and the ROI zero-padded by recommended_subset_padding (padding.cpp:11-24, 28-36, 55-85), seed
+// and propagation over the padded pair, then the grid points inside the original image, shifted
+// back (a padded grid point gx * step is the image point gx * step - pad).
+static void truncated_compute(tdic_ctx* ctx, const void* reference, const void* deformed, int w, int h,
+                              tdic_dtype dtype, const uint8_t* roi, const tdic_config& cfg, tdic_grid_out* out,
+                              int32_t* n_points, tdic_seed* seed_out, cudaStream_t s) {
+    const int pad = tdic_subset_padding(&cfg);
+    const int pw = w + 2 * pad, ph = h + 2 * pad;
+    const HostImage ri{reference, dtype}, di{deformed, dtype};
+    auto mirror = [](int i, int n) {
+        if (n <= 1) return 0;
+        while (i < 0 || i >= n) i = i < 0 ? -i - 1 : 2 * n - i - 1;
+        return i;
+    };
+    std::vector<float> pr(static_cast<size_t>(pw) * ph), pd(pr.size());
+    std::vector<uint8_t> pm(pr.size(), 0);
+    std::vector<int> mx(pw);
+    for (int x = 0; x < pw; ++x) mx[x] = mirror(x - pad, w);
+    for (int y = 0; y < ph; ++y) {
+        const size_t row = static_cast<size_t>(mirror(y - pad, h)) * w;
+        for (int x = 0; x < pw; ++x) {
+            pr[static_cast<size_t>(y) * pw + x] = ri(row + mx[x]);
+            pd[static_cast<size_t>(y) * pw + x] = di(row + mx[x]);
+        }
+    }
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x)
+            pm[static_cast<size_t>(y + pad) * pw + x + pad] = roi ? (roi[static_cast<size_t>(y) * w + x] != 0) : 1;
+    tdic_pair* pair = nullptr;
+    tdic_seed seed{};
+    prepare_impl(ctx, pr.data(), pd.data(), pw, ph, TDIC_F32, pm.data(), cfg, s, &pair, &seed);
+    int32_t gw, gh;
+    tdic_grid_dims(pw, ph, cfg.propagation_spacing, &gw, &gh);
+    const size_t n = static_cast<size_t>(gw) * gh;
+    // padded-grid host outputs for the arrays the caller asked for (x, y always: the crop needs them)
+    std::vector<double> dbl[16];
+    std::vector<uint8_t> u8[2];
+    std::vector<int8_t> st;
+    std::vector<int32_t> it;
+    tdic_grid_out t{};
+    double** tdp[16] = {&t.x, &t.y, &t.u, &t.v, &t.du_dx, &t.du_dy, &t.dv_dx, &t.dv_dy, &t.correlation, &t.zncc,
+                        &t.d2u_dx2, &t.d2u_dxdy, &t.d2u_dy2, &t.d2v_dx2, &t.d2v_dxdy, &t.d2v_dy2};
+    double* const odp[16] = {out->x, out->y, out->u, out->v, out->du_dx, out->du_dy, out->dv_dx, out->dv_dy,
+                             out->correlation, out->zncc, out->d2u_dx2, out->d2u_dxdy, out->d2u_dy2, out->d2v_dx2,
+                             out->d2v_dxdy, out->d2v_dy2};
+    for (int k = 0; k < 16; ++k)
+        if (odp[k] || k < 2) { dbl[k].assign(n, 0.0); *tdp[k] = dbl[k].data(); }
+    if (out->valid) { u8[0].assign(n, 0); t.valid = u8[0].data(); }
+    if (out->converged) { u8[1].assign(n, 0); t.converged = u8[1].data(); }
+    if (out->status) { st.assign(n, 0); t.status = st.data(); }
+    if (out->iterations) { it.assign(n, 0); t.iterations = it.data(); }
+    int32_t computed = 0;
+    try {
+        if (seed.found) {
+            propagate_impl(ctx, pair, cfg, seed, pm.data(), &t, TDIC_HOST, &computed, s);
+            mark_use(pair, s);
+        }
+    } catch (...) {
+        tdic_pair_destroy(pair);
+        throw;
+    }
+    tdic_pair_destroy(pair);
+    if (seed_out) {
+        *seed_out = seed;
+        if (seed.found) { seed_out->x -= pad; seed_out->y -= pad; }
+    }
+    if (computed == 0) return;
+    int32_t k = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const double x = t.x[i] - pad, y = t.y[i] - pad;
+        if (x < 0.0 || y < 0.0 || x >= w || y >= h) continue;
+        for (int f = 0; f < 16; ++f)
+            if (odp[f]) odp[f][k] = (*tdp[f])[i];
+        out->x[k] = x;
+        out->y[k] = y;
+        if (out->valid) out->valid[k] = t.valid[i];
+        if (out->converged) out->converged[k] = t.converged[i];
+        if (out->status) out->status[k] = t.status[i];
+        if (out->iterations) out->iterations[k] = t.iterations[i];
+        ++k;
+    }
+    *n_points = k;
+}
+
 tdic_status tdic_ls_strain_2d(tdic_ctx* ctx, const double* points, const double* displacement, int32_t n,
                               double radius, int32_t min_samples, int32_t green_lagrange, tdic_ls_strain* out,
                               void* stream) {
@@ -871,6 +1048,8 @@ tdic_status tdic_subset_prepare(tdic_ctx* ctx, const void* reference, const void
         *pair_out = nullptr;
         std::memset(seed_out, 0, sizeof(*seed_out));
         check_config(*cfg);
+        TDIC_REQUIRE(!cfg->truncate_roi_subsets, TDIC_UNSUPPORTED,
+                     "prepare: masked subsets pad the images; use tdic_subset_compute");
         TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
         prepare_impl(ctx, reference, deformed, width, height, dtype, roi, *cfg, pick(ctx, stream), pair_out, seed_out);
     });
@@ -886,6 +1065,11 @@ tdic_status tdic_subset_compute(tdic_ctx* ctx, const void* reference, const void
         check_config(*cfg);
         TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
         cudaStream_t s = pick(ctx, stream);
+        if (cfg->truncate_roi_subsets) {
+            TDIC_REQUIRE(out->x && out->y, TDIC_INVALID_ARG, "masked subsets: x and y outputs are required");
+            truncated_compute(ctx, reference, deformed, width, height, dtype, roi, *cfg, out, n_points, seed_out, s);
+            return;
+        }
         tdic_pair* pair = nullptr;
         tdic_seed seed{};
         prepare_impl(ctx, reference, deformed, width, height, dtype, roi, *cfg, s, &pair, &seed);
@@ -982,6 +1166,7 @@ void upload_chunked(unsigned char* dst, size_t bytes, Fill&& fill, cudaStream_t 
 void propagate_noalloc_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const tdic_seed& seed,
                             const uint8_t* roi, const tdic_grid_out* out, int32_t* points_computed, cudaStream_t s) {
     check_config(cfg);
+    TDIC_REQUIRE(!cfg.truncate_roi_subsets, TDIC_UNSUPPORTED, "no-allocation propagation: masked subsets not covered");
     TDIC_REQUIRE(pair->exact == 1, TDIC_INVALID_ARG, "propagation needs a pair with the exact prefilter");
     TDIC_REQUIRE(cfg.propagation_mode == 0 || cfg.propagation_mode == 2, TDIC_UNSUPPORTED,
                  "propagation_mode 1 (serial heap order) is not on the GPU path; use 0 (frontier waves) or 2 (dataflow)");
@@ -1131,8 +1316,8 @@ void batch_create_impl(tdic_ctx* ctx, int n, tdic_pair* const* pairs, const tdic
         TDIC_REQUIRE(p->degree == p0->degree && p->precision == p0->precision, TDIC_INVALID_ARG,
                      "batch: every pair must have the same spline degree and precision");
         TDIC_REQUIRE(c.optimizer == cfgs[0].optimizer, TDIC_INVALID_ARG, "batch: every job must use the same optimizer");
-        TDIC_REQUIRE(first_order_znssd(c), TDIC_UNSUPPORTED,
-                     "batch: only the first-order ZNSSD route (propagate other routes one pair at a time)");
+        TDIC_REQUIRE(first_order_znssd(c) && !c.truncate_roi_subsets, TDIC_UNSUPPORTED,
+                     "batch: only the first-order ZNSSD route without masked subsets (propagate others one pair at a time)");
         TDIC_REQUIRE(c.propagation_mode == 2, TDIC_UNSUPPORTED, "batch: only the dataflow order (propagation_mode 2)");
         // seed alignment (reliability_propagation.cpp:201-216), as tdic_propagate
         const uint8_t* roi = rois ? rois[j] : nullptr;

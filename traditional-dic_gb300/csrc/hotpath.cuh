@@ -346,6 +346,10 @@ struct Env {
     int rbx, rby;          // TMA box of the reference window (floats)
     int cbx, cby;          // TMA box of the coefficient window (T)
     int* err;              // device error flag (TMA wait timeout)
+    // masked subsets (solve_with_mask): ROI of the image (w x h bytes, row pitch w) or NULL;
+    // min_keep = max(NP, min_valid_samples, ceil(min_valid_sample_ratio * n))
+    const uint8_t* roi;
+    int min_keep;
 };
 
 // Per-POI result in the solve's own precision (float on the FP32-mixed path); outputs are
@@ -881,17 +885,19 @@ constexpr int kDriftMargin = 3;  // px of parameter drift covered by the staged 
 // Warp this thread's samples, interpolate from the staged coefficient window (global memory for
 // a stencil outside it), store g (and for FGN the spline gradient), accumulate the shifted
 // normalisation sums.  Returns false if a warped point left the image.
-// NP = 12: the second-order warp (icgn.cpp:167-182); SUMS = false (SSD): no normalisation sums.
+// NP = 12: the second-order warp (icgn.cpp:167-182); SUMS = false (SSD): no normalisation sums;
+// s_chk (masked subsets): samples whose entry is NaN lie outside the ROI and are skipped.
 template <int DEG, typename T, bool GRAD, int NP = 6, bool SUMS = true>
 __device__ __forceinline__ bool warp_interp(const Env<T>& e, int cx, int cy, const T (&p)[NP], T fm, T* s_g, T* s_gx,
                                             T* s_gy, const short2* off, const T* cwin, int wc0, int wr0, int tid,
-                                            int nt, Kahan<T>& sg, Kahan<T>& sg2) {
+                                            int nt, Kahan<T>& sg, Kahan<T>& sg2, const T* s_chk = nullptr) {
     const int ww = e.cbx, wh = e.cby;
     constexpr int NB = DEG + 1, OFF = DEG / 2;
     bool ok = true;
     const T xlo = T(-cx), ylo = T(-cy), xhi = T(e.w - 1 - cx), yhi = T(e.h - 1 - cy);
 #pragma unroll 2
     for (int i = tid; i < e.n; i += nt) {
+        if (s_chk != nullptr && isnan(s_chk[i])) continue;
         const short2 o = off[i];
         const T lx = T(o.x), ly = T(o.y);
         T tx = ((lx + p[0]) + p[2] * lx) + p[3] * ly;
@@ -1268,9 +1274,17 @@ __device__ bool solve_poi_var(const Env<T>& e, const CUtensorMap* tm_ref, const 
     result_init(R, p0, conf);
     int rp = 0;
     const int r = e.radius;
+    // masked subsets (solve_with_mask, icgn.cpp:629-704 and siblings): the centre must be a ROI
+    // pixel (no margin check); samples outside the image or the ROI are left out (marked NaN in
+    // s_fn) and at least e.min_keep must remain
+    const bool masked = e.roi != nullptr;
     if (e.w <= 0 || r < 1 || e.max_iter < 0) return true;
-    if (cx - r < 0 || cy - r < 0 || cx + r >= e.w || cy + r >= e.h) return true;
-    if (e.n < NP) return true;
+    if (masked) {
+        if (cx < 0 || cy < 0 || cx >= e.w || cy >= e.h || e.roi[static_cast<size_t>(cy) * e.w + cx] == 0) return true;
+    } else {
+        if (cx - r < 0 || cy - r < 0 || cx + r >= e.w || cy + r >= e.h) return true;
+        if (e.n < NP) return true;
+    }
     T* s_fn = gs.sm;              // ZNSSD: normalised reference f^; SSD: raw f
     T* s_a = gs.sm + e.nmax;      // ICGN: reference gx; FGN: deformed gx
     T* s_b = gs.sm + 2 * e.nmax;  // ICGN: reference gy; FGN: deformed gy
@@ -1288,9 +1302,15 @@ __device__ bool solve_poi_var(const Env<T>& e, const CUtensorMap* tm_ref, const 
     T hs[NH];
 #pragma unroll
     for (int k = 0; k < NH; ++k) hs[k] = T(0);
+    T kept = T(0);
     for (int i = tid; i < e.n; i += NT) {
         const short2 o = off[i];
         const int x = cx + o.x, y = cy + o.y;
+        if (masked && (x < 0 || y < 0 || x >= W || y >= H || e.roi[static_cast<size_t>(y) * W + x] == 0)) {
+            s_fn[i] = T(NAN);
+            continue;
+        }
+        kept += T(1);
         const float f = gs.rwin[(y - ry0) * rww + (x - rx0)];
         s_fn[i] = T(f);
         if constexpr (!SSD) {
@@ -1321,8 +1341,9 @@ __device__ bool solve_poi_var(const Env<T>& e, const CUtensorMap* tm_ref, const 
                 for (int v = 0; v < NM; ++v) hs[u * NM + v] += q[u] * m[v];
         }
     }
-    constexpr int KS = SSD ? 0 : 2, KH = OPT == 0 ? NH : 0, K0 = KS + KH;
-    T v0[K0 > 0 ? K0 : 1];
+    // one reduction: (ZNSSD) the two shifted sums, (ICGN) the Hessian sums, the kept count
+    constexpr int KS = SSD ? 0 : 2, KH = OPT == 0 ? NH : 0, K0 = KS + KH + 1;
+    T v0[K0];
     if constexpr (KS > 0) {
         v0[0] = k1.value();
         v0[1] = k2.value();
@@ -1331,8 +1352,12 @@ __device__ bool solve_poi_var(const Env<T>& e, const CUtensorMap* tm_ref, const 
 #pragma unroll
         for (int k = 0; k < NH; ++k) v0[KS + k] = hs[k];
     }
-    if constexpr (K0 > 0) group_sum_n<G, K0, T>(v0, red, rp, tid, bar_id);
-    const M inv_n = M(e.inv_n), thr = M(e.thr);
+    v0[K0 - 1] = kept;
+    group_sum_n<G, K0, T>(v0, red, rp, tid, bar_id);
+    const int nkept = static_cast<int>(v0[K0 - 1]);
+    if (masked && nkept < e.min_keep) return true;  // too few ROI samples: InvalidInput
+    // the reference divides by the kept count: 1 / n rounded as the host's double reciprocal
+    const M inv_n = masked ? M(1.0 / static_cast<double>(nkept)) : M(e.inv_n), thr = M(e.thr);
     T fm = T(0), inv_norm = T(1);
     if constexpr (!SSD) {
         const M s1 = static_cast<M>(v0[0]), s2 = static_cast<M>(v0[1]);
@@ -1407,7 +1432,7 @@ __device__ bool solve_poi_var(const Env<T>& e, const CUtensorMap* tm_ref, const 
         for (int k = 0; k < NP; ++k) pt[k] = static_cast<T>(p[k]);
         Kahan<T> sg, sg2;
         const bool ok = warp_interp<DEG, T, OPT == 1, NP, !SSD>(e, cx, cy, pt, fm, s_g, s_a, s_b, off, gs.cwin, wc0,
-                                                                wr0, tid, NT, sg, sg2);
+                                                                wr0, tid, NT, sg, sg2, masked ? s_fn : nullptr);
         T gsh = T(0), inv_gn = T(1);
         if constexpr (!SSD) {
             T v3[3] = {sg.value(), sg2.value(), ok ? T(0) : T(1)};
@@ -1429,6 +1454,7 @@ __device__ bool solve_poi_var(const Env<T>& e, const CUtensorMap* tm_ref, const 
 #pragma unroll
             for (int k = 0; k <= NP; ++k) q[k] = T(0);
             for (int i = tid; i < e.n; i += NT) {
+                if (masked && isnan(s_fn[i])) continue;
                 const short2 o = off[i];
                 const T lx = T(o.x), ly = T(o.y);
                 const T diff = SSD ? s_fn[i] - s_g[i] : s_fn[i] - ((s_g[i] - fm) - gsh) * inv_gn;
@@ -1459,6 +1485,7 @@ __device__ bool solve_poi_var(const Env<T>& e, const CUtensorMap* tm_ref, const 
 #pragma unroll
             for (int k = 0; k < KQ; ++k) q[k] = T(0);
             for (int i = tid; i < e.n; i += NT) {
+                if (masked && isnan(s_fn[i])) continue;
                 const short2 o = off[i];
                 const T lx = T(o.x), ly = T(o.y);
                 const T gx = s_a[i], gy = s_b[i];
@@ -1522,7 +1549,8 @@ __device__ bool solve_poi_var(const Env<T>& e, const CUtensorMap* tm_ref, const 
                     const M dk = hess12_entry<M>(mS, k, k) * hscale;
                     dmax = k == 0 ? dk : fmax(dmax, dk);
                 }
-                const M lambda = M(1e-4) * dmax;  // forward_gauss_newton.cpp:1242-1245, 1682-1685
+                // forward_gauss_newton.cpp:1242-1245, 1682-1685, 1886-1889 (not the masked ZNSSD route)
+                const M lambda = (!masked || SSD) ? M(1e-4) * dmax : M(0);
                 for (int t = tid; t < 144; t += NT) {
                     const int i = t / 12, j = t % 12;
                     M h = hess12_entry<M>(mS, i, j) * hscale;
@@ -1550,12 +1578,16 @@ __device__ bool solve_poi_var(const Env<T>& e, const CUtensorMap* tm_ref, const 
             if constexpr (NP == 6) ic_update<M>(p, dp, pn);
             else ic_update2<M>(p, dp, pn);
         } else {
-            const M cap = SSD ? M(0.35) : M(0.5);
-            if (dn > cap) {  // forward_gauss_newton.cpp:367-371, 763-767, 1260-1264, 1700-1705
+            // step cap and whether convergence sees the capped norm, per route (unmasked
+            // forward_gauss_newton.cpp:367-371, 763-767, 1260-1264, 1700-1705; masked 572-576,
+            // 936-940, 1485-1489, 1902-1906)
+            const M cap = SSD ? M(0.35) : ((masked && NP == 12) ? M(0.3) : M(0.5));
+            const bool test_capped = masked ? !(NP == 12 && !SSD) : !(NP == 6 && SSD);
+            if (dn > cap) {
                 const M sc = cap / dn;
 #pragma unroll
                 for (int k = 0; k < NP; ++k) dp[k] *= sc;
-                if (!(NP == 6 && SSD)) dn = cap;  // first-order SSD keeps the norm before the cap (:764)
+                if (test_capped) dn = cap;
             }
             if constexpr (NP == 6) compose_warp<M>(p, dp, pn);
             else compose_warp2<M>(p, dp, pn);
@@ -2438,7 +2470,7 @@ __global__ void init_grid_kernel(tdic_grid_out o, int gw, int gh, int step) {
 // ---------------------------------------------------------------------------------------
 template <typename T>
 Env<T> make_env(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, int radius, int max_iter, double thr,
-                const short2* off = nullptr, int n_off = 0) {
+                const short2* off = nullptr, int n_off = 0, const uint8_t* roi = nullptr) {
     if (!off) {
         const SampleTable& tab = sample_table(ctx, radius);
         off = tab.offsets.as<short2>();
@@ -2469,7 +2501,13 @@ Env<T> make_env(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, int radi
     TDIC_REQUIRE(e.rbx <= 256 && e.rby <= 256 && e.cbx <= 256 && e.cby <= 256, TDIC_UNSUPPORTED,
                  "subset radius too large for a TMA box");
     e.err = ctx->dev_err;
-    (void)cfg;
+    // masked subsets keep at least max(NP, min_valid_samples, ceil(ratio * full circle)) samples
+    // (icgn.cpp:702-706, 1434-1438 and siblings)
+    e.roi = roi;
+    const int np = cfg.shape_order == 2 ? 12 : 6;
+    e.min_keep = roi ? std::max(np, std::max(cfg.min_valid_samples,
+                                             static_cast<int>(std::ceil(cfg.min_valid_sample_ratio * n_off))))
+                     : 0;
     return e;
 }
 
@@ -2516,7 +2554,8 @@ constexpr int kGroupsPerBlockBatch = 4;  // 4 warps of 1-warp groups
 template <int OPT, int DEG, typename T, int VAR = 0>
 void solve_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const SolveLaunch& L, cudaStream_t s) {
     constexpr int G = 1;
-    Env<T> e = make_env<T>(ctx, pair, cfg, cfg.subset_radius, cfg.max_iterations, cfg.convergence_threshold);
+    Env<T> e = make_env<T>(ctx, pair, cfg, cfg.subset_radius, cfg.max_iterations, cfg.convergence_threshold,
+                           nullptr, 0, L.roi);
     const TensorMaps tm = make_tensor_maps<T>(pair, e);
     const size_t per_group = group_smem_bytes<T>(e.nmax, G, e.rbx, e.rby, e.cbx, e.cby, (VAR & 2) ? kMat12 : kMat6);
     const size_t prefix = cta_prefix_bytes(e.nmax);
@@ -2551,7 +2590,7 @@ template <int OPT, int DEG, typename T, int VAR = 0>
 void propagate_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const PropagateLaunch& L, cudaStream_t s) {
     constexpr int G = kPropG;
     Env<T> e = make_env<T>(ctx, pair, cfg, cfg.subset_radius, cfg.max_iterations, cfg.convergence_threshold,
-                           L.offsets, L.n_offsets);
+                           L.offsets, L.n_offsets, L.roi_px);
     TensorMaps tm = make_tensor_maps<T>(pair, e);
     const size_t per_group =
         group_smem_bytes<T>(e.nmax, G, e.rbx, e.rby, e.cbx, e.cby, (VAR & 2) ? kMat12 : kMat6);

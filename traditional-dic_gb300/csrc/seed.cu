@@ -23,7 +23,10 @@ constexpr double kEps = 1e-12;
 struct CandGeom {
     int cx, cy;
     int min_u, max_u, min_v, max_v;  // coarse range
-    int inside;                      // the candidate's subset lies inside the image
+    int inside;                      // the candidate's subset lies inside the image (masked: enough ROI samples)
+    // the candidate's sample tables: coarse (pyramid-strided) and full, as (first entry, count)
+    // in the concatenated offset arrays; one shared table each unless the subsets are masked
+    int c_start, c_n, f_start, f_n;
 };
 
 struct Best {
@@ -198,8 +201,10 @@ __global__ void coarse_max_kernel(const float* __restrict__ ref, const float* __
                                   const CandGeom* __restrict__ geo, const short2* __restrict__ coff, int cn, int cstep,
                                   float* __restrict__ tile_max, int tiles) {
     extern __shared__ __align__(16) unsigned char smem[];
-    SearchSmem sm(smem, cn);
     const CandGeom g = geo[blockIdx.y];
+    cn = g.c_n;
+    coff += g.c_start;
+    SearchSmem sm(smem, cn);
     if (!g.inside) {  // uniform per block: no reference read outside the image
         if (threadIdx.x == 0) tile_max[blockIdx.y * tiles + blockIdx.x] = -INFINITY;
         return;
@@ -228,8 +233,10 @@ __global__ void coarse_pick_kernel(const float* __restrict__ ref, const float* _
                                    const CandGeom* __restrict__ geo, const short2* __restrict__ coff, int cn, int cstep,
                                    const float* __restrict__ tile_max, Best* __restrict__ partial, int tiles) {
     extern __shared__ __align__(16) unsigned char smem[];
-    SearchSmem sm(smem, cn);
     const CandGeom g = geo[blockIdx.y];
+    cn = g.c_n;
+    coff += g.c_start;
+    SearchSmem sm(smem, cn);
     if (!g.inside) {
         if (threadIdx.x == 0) partial[blockIdx.y * tiles + blockIdx.x] = Best{-INFINITY, 0x7fffffff};
         return;
@@ -294,10 +301,12 @@ __global__ void fine_kernel(const float* __restrict__ ref, const float* __restri
                             const Best* __restrict__ partial, int tiles, int cstep, int rr, int search, int coarse_ok_all,
                             const int* __restrict__ coarse_ok, SearchResult* __restrict__ out) {
     extern __shared__ __align__(16) unsigned char smem[];
+    const CandGeom g = geo[blockIdx.x];
+    fn = g.f_n;
+    foff += g.f_start;
     SearchSmem sm(smem, fn);
     __shared__ double s_cz;
     __shared__ int s_cu, s_cv;
-    const CandGeom g = geo[blockIdx.x];
     if (!g.inside) {
         if (threadIdx.x == 0) out[blockIdx.x] = SearchResult{0, 0, -INFINITY, 0};
         return;
@@ -418,8 +427,12 @@ void KmeansAssigner::assign(const double* cx, const double* cy, int* assign_host
     TDIC_CUDA_TRY(cudaStreamSynchronize(s_));
 }
 
+// roi (host, w x h, or NULL): estimate_with_mask_interpolators (integer_search.cpp:447-545) - the
+// centre must be a ROI pixel, each candidate's samples are its ROI samples (in the reference's
+// order), at least min_required_samples of them (max(12, ceil(0.5 * full circle))) for the full
+// set, and for the coarse set before the multigrid stage runs.
 void integer_search_batch(tdic_ctx* ctx, tdic_pair* lazy, const tdic_config& cfg, const int* cx, const int* cy, int n,
-                          SearchResult* out_host, cudaStream_t s) {
+                          SearchResult* out_host, cudaStream_t s, const uint8_t* roi) {
     if (n <= 0) return;
     const int w = lazy->w, h = lazy->h;
     const int r = cfg.is_subset_radius < 1 ? 1 : cfg.is_subset_radius;
@@ -428,23 +441,56 @@ void integer_search_batch(tdic_ctx* ctx, tdic_pair* lazy, const tdic_config& cfg
     int rr = cfg.pyramid_refinement_radius < 1 ? 1 : cfg.pyramid_refinement_radius;
     rr = std::max(rr, static_cast<int>(std::ceil(1.5 * static_cast<double>(r))));
     rr = std::max(rr, cstep);
-    const auto foff = circle_offsets(r, 1);
-    const auto coff = circle_offsets(r, cstep);
+    const auto foff_full = circle_offsets(r, 1);
+    const auto coff_full = circle_offsets(r, cstep);
     std::vector<CandGeom> geo(n);
-    std::vector<int> ok(n, 0);
-    for (int i = 0; i < n; ++i) {
-        geo[i].cx = cx[i];
-        geo[i].cy = cy[i];
-        geo[i].min_u = r - cx[i];
-        geo[i].max_u = w - 1 - r - cx[i];
-        geo[i].min_v = r - cy[i];
-        geo[i].max_v = h - 1 - r - cy[i];
-        ok[i] = (cx[i] - r >= 0 && cy[i] - r >= 0 && cx[i] + r < w && cy[i] + r < h) ? 1 : 0;
-        geo[i].inside = ok[i];
+    std::vector<int> ok(n, 0), cok(n, 0);
+    std::vector<short2> foff, coff;
+    auto need = [&](int step) {  // min_required_samples (integer_search.cpp:47-50)
+        return std::max(12, static_cast<int>(std::ceil(0.5 * static_cast<double>(circle_offsets(r, step).size()))));
+    };
+    if (!roi) {
+        foff = foff_full;
+        coff = coff_full;
     }
+    for (int i = 0; i < n; ++i) {
+        CandGeom& g = geo[i];
+        g.cx = cx[i];
+        g.cy = cy[i];
+        g.min_u = r - cx[i];
+        g.max_u = w - 1 - r - cx[i];
+        g.min_v = r - cy[i];
+        g.max_v = h - 1 - r - cy[i];
+        if (!roi) {
+            ok[i] = (cx[i] - r >= 0 && cy[i] - r >= 0 && cx[i] + r < w && cy[i] + r < h) ? 1 : 0;
+            cok[i] = ok[i];
+            g.c_start = 0; g.c_n = static_cast<int>(coff.size());
+            g.f_start = 0; g.f_n = static_cast<int>(foff.size());
+        } else {
+            auto keep = [&](const short2& o) {
+                const int x = cx[i] + o.x, y = cy[i] + o.y;
+                return x >= 0 && y >= 0 && x < w && y < h && roi[static_cast<size_t>(y) * w + x] != 0;
+            };
+            const bool centre = cx[i] >= 0 && cy[i] >= 0 && cx[i] < w && cy[i] < h &&
+                                roi[static_cast<size_t>(cy[i]) * w + cx[i]] != 0;
+            g.f_start = static_cast<int>(foff.size());
+            for (const short2& o : foff_full) if (centre && keep(o)) foff.push_back(o);
+            g.f_n = static_cast<int>(foff.size()) - g.f_start;
+            g.c_start = static_cast<int>(coff.size());
+            for (const short2& o : coff_full) if (centre && keep(o)) coff.push_back(o);
+            g.c_n = static_cast<int>(coff.size()) - g.c_start;
+            ok[i] = centre && g.f_n >= need(1) ? 1 : 0;
+            cok[i] = ok[i] && g.c_n >= need(cstep) ? 1 : 0;
+            if (!cok[i]) g.c_n = 0;  // no multigrid stage: every coarse score is -inf
+        }
+        g.inside = ok[i];
+    }
+    if (foff.empty()) foff.push_back(make_short2(0, 0));  // keep the device tables non-empty
+    if (coff.empty()) coff.push_back(make_short2(0, 0));
+    int cmax = 1, fmax = 1;
+    for (const CandGeom& g : geo) { cmax = std::max(cmax, g.c_n); fmax = std::max(fmax, g.f_n); }
     // A flat coarse subset (coarse_ref_norm <= eps) scores -inf everywhere in the coarse search,
     // the reference's outcome of skipping the multigrid stage (integer_search.cpp:381-397).
-    const std::vector<int>& cok = ok;
     Buffer d_geo(&ctx->pool, sizeof(CandGeom) * n), d_coff(&ctx->pool, sizeof(short2) * coff.size()),
         d_foff(&ctx->pool, sizeof(short2) * foff.size()), d_cok(&ctx->pool, sizeof(int) * n),
         d_out(&ctx->pool, sizeof(SearchResult) * n);
@@ -455,7 +501,7 @@ void integer_search_batch(tdic_ctx* ctx, tdic_pair* lazy, const tdic_config& cfg
     TDIC_CUDA_TRY(cudaMemcpyAsync(d_coff.ptr, coff.data(), sizeof(short2) * coff.size(), cudaMemcpyHostToDevice, s));
     TDIC_CUDA_TRY(cudaMemcpyAsync(d_foff.ptr, foff.data(), sizeof(short2) * foff.size(), cudaMemcpyHostToDevice, s));
     TDIC_CUDA_TRY(cudaMemcpyAsync(d_cok.ptr, cok.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
-    const size_t csm = search_smem_bytes(coff.size()), fsm = search_smem_bytes(foff.size());
+    const size_t csm = search_smem_bytes(static_cast<size_t>(cmax)), fsm = search_smem_bytes(static_cast<size_t>(fmax));
     TDIC_CUDA_TRY(cudaFuncSetAttribute(coarse_max_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(csm)));
     TDIC_CUDA_TRY(cudaFuncSetAttribute(coarse_pick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(csm)));
     TDIC_CUDA_TRY(cudaFuncSetAttribute(fine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(fsm)));

@@ -154,6 +154,8 @@ struct SolveLaunch {
     tdic_poi_out* out;
     int n;
     int* fetch;  // work counter (zeroed by the launcher)
+    // masked subsets (solve_with_mask): device ROI of the pair's image (w x h bytes), or NULL
+    const uint8_t* roi = nullptr;
 };
 void launch_solve(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const SolveLaunch& L, cudaStream_t s);
 // Throws TDIC_TIMEOUT when a bounded in-kernel wait gave up; clears the flag.  Synchronises s.
@@ -179,6 +181,8 @@ struct PropagateLaunch {
     int* dstate; int* dcnt; unsigned long long* dq; float* kcorr;
     // subset sample offsets; NULL = the context's table for the radius
     const short2* offsets; int n_offsets;
+    // masked subsets (truncate_roi_subsets): device ROI of the pair's image (w x h bytes), or NULL
+    const uint8_t* roi_px = nullptr;
 };
 void launch_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const PropagateLaunch& L,
                       cudaStream_t s);
@@ -199,8 +203,9 @@ private:
     int m_, k_;
     Buffer pts_, ctr_, out_;
 };
+// roi (host mask of the pair's image, or NULL): the masked search of truncate_roi_subsets.
 void integer_search_batch(tdic_ctx* ctx, tdic_pair* lazy, const tdic_config& cfg, const int* cx, const int* cy,
-                          int n, SearchResult* out, cudaStream_t s);
+                          int n, SearchResult* out, cudaStream_t s, const uint8_t* roi = nullptr);
 
 // Least-squares strain (strain.cu).
 void ls_strain_2d(tdic_ctx* ctx, const double* points, const double* disp, int n, double radius, int min_samples,

@@ -355,7 +355,17 @@ def compute(reference, deformed, config: dict | None = None, roi=None, *, contex
     de = _check_image(deformed, "deformed")
     if config is not None and not isinstance(config, dict):
         raise RuntimeError("config must be a dict (from YAML) or None.")
-    cfg = config_from_dict(config)
+    return compute_config(ref, de, config_from_dict(config), roi, context=context, return_seed=return_seed)
+
+
+def compute_config(reference, deformed, cfg: L.Config, roi=None, *, context: Context | None = None,
+                   return_seed: bool = False):
+    """``SubsetDIC::compute`` (subset_dic.cpp:39-105) with a full configuration structure: the
+    C++ ``SubsetConfig`` knobs the pybind dict does not reach, e.g. ``truncate_roi_subsets`` with
+    ``min_valid_samples`` / ``min_valid_sample_ratio`` (masked subsets over padded images; the
+    grid points are then gx * step - pad, see ``tdic_subset_grid_dims``)."""
+    ref = _check_image(reference, "reference")
+    de = _check_image(deformed, "deformed")
     ctx = context or default_context()
     seed = L.Seed()
     if ref.shape != de.shape or ref.size == 0:
@@ -366,12 +376,12 @@ def compute(reference, deformed, config: dict | None = None, roi=None, *, contex
         return (_empty_result(), seed) if return_seed else _empty_result()
     if de.dtype != ref.dtype:
         de = de.astype(ref.dtype)
-    gw, gh = L.grid_dims(w, h, cfg.propagation_spacing)
+    gw, gh = L.subset_grid_dims(w, h, cfg)
     arrs, g = _alloc_grid(gw * gh, cfg.shape_order == 2)
     n = C.c_int32()
     ctx.check(ctx.lib.tdic_subset_compute(ctx.handle, ref.ctypes.data, de.ctypes.data, w, h, L.DTYPES[ref.dtype.name],
                                           rptr, C.byref(cfg), C.byref(g), C.byref(n), C.byref(seed), None))
-    res = _empty_result() if n.value == 0 else _finish(arrs)
+    res = _empty_result() if n.value == 0 else {k: v[:n.value] for k, v in _finish(arrs).items()}
     return (res, seed) if return_seed else res
 
 
@@ -427,9 +437,11 @@ def subset(reference: np.ndarray, deformed: np.ndarray, config: str | Path | dic
     return compute(reference, deformed, config_dict, roi)
 
 
-def solve_pois(ctx: Context, pair: Pair, config: L.Config, xy, p0, confidence=None) -> dict:
+def solve_pois(ctx: Context, pair: Pair, config: L.Config, xy, p0, confidence=None, roi=None,
+               masked: bool = False) -> dict:
     """Batched per-POI solve (tdic_solve_pois) on host arrays, on the config's route (optimizer,
-    shape_order, criterion); "q" holds the six second-order terms (zero for first order)."""
+    shape_order, criterion); "q" holds the six second-order terms (zero for first order).
+    ``masked``: solve_with_mask over ``roi`` (None: every pixel), tdic_solve_pois_masked."""
     xy = np.ascontiguousarray(xy, np.float64).reshape(-1, 2)
     p0 = np.ascontiguousarray(p0, np.float64).reshape(-1, 6)
     n = xy.shape[0]
@@ -440,8 +452,15 @@ def solve_pois(ctx: Context, pair: Pair, config: L.Config, xy, p0, confidence=No
     out = np.zeros(n, dtype=np.dtype([("p", "<f8", 6), ("correlation", "<f8"), ("zncc", "<f8"), ("iterations", "<i4"),
                                       ("status", "i1"), ("valid", "i1"), ("converged", "i1"), ("pad", "i1"),
                                       ("q", "<f8", 6)]))
-    ctx.check(ctx.lib.tdic_solve_pois(ctx.handle, pair.handle, C.byref(config), inp.ctypes.data, n, out.ctypes.data,
-                                      L.HOST, None))
+    if masked:
+        rptr, rkeep = _roi_arg(roi, pair.width, pair.height)
+        if rptr == "mismatch":
+            raise ValueError("roi shape differs from the images")
+        ctx.check(ctx.lib.tdic_solve_pois_masked(ctx.handle, pair.handle, C.byref(config), rptr, inp.ctypes.data, n,
+                                                 out.ctypes.data, L.HOST, None))
+    else:
+        ctx.check(ctx.lib.tdic_solve_pois(ctx.handle, pair.handle, C.byref(config), inp.ctypes.data, n,
+                                          out.ctypes.data, L.HOST, None))
     return {"p": out["p"].copy(), "q": out["q"].copy(), "correlation": out["correlation"].copy(), "zncc": out["zncc"].copy(),
             "iterations": out["iterations"].copy(), "status": out["status"].copy(),
             "valid": out["valid"].astype(bool), "converged": out["converged"].astype(bool)}
