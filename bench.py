@@ -392,6 +392,7 @@ def run_ours(args, world, rank, local, pg):
                "sample": f"first {rr['solves']} heap-order solves of the same 2048^2 workload "
                          f"({dt:.1f} s, FP64 C++ port of the reference path, 1 thread)"}
 
+    routes = run_routes(args, ctx, stream) if (args.routes and rank == 0) else None
     batched = run_batch(args, ctx, stream) if (args.batch and rank == 0) else None
     served = run_serve(args, ctx) if (args.serve and rank == 0) else None
 
@@ -415,6 +416,8 @@ def run_ours(args, world, rank, local, pg):
             "stages_ms": {"prefilter_and_convert": 1e3 * (statistics.median(times) - t_prop),
                           "propagate": 1e3 * t_prop},
         }
+        if routes is not None:
+            line["routes"] = routes
         if batched is not None:
             line["batched_uneven"] = batched
         if served is not None:
@@ -422,6 +425,76 @@ def run_ours(args, world, rank, local, pg):
         print(json.dumps(line), flush=True)
     pair.close()
     ctx.close()
+
+
+ROUTES = [("icgn", "first_order", "znssd"), ("icgn", "first_order", "ssd"), ("icgn", "second_order", "znssd"),
+          ("icgn", "second_order", "ssd"), ("fgn", "first_order", "znssd"), ("fgn", "first_order", "ssd"),
+          ("fgn", "second_order", "znssd"), ("fgn", "second_order", "ssd")]
+
+
+def run_routes(args, ctx, stream) -> list:
+    """Every solver route (optimizer x shape function x criterion) on the same 2048^2 pair, scaled
+    to [0, 1] float32 (the range the reference's Python facade documents, so SSD values meet the
+    acceptance threshold): propagation time of one pair with device outputs, FP32-mixed and FP64,
+    the seed of each route from its own seed selection (untimed)."""
+    import torch
+    from traditional_dic_gb300 import subset as S, synthetic, _lib as L
+    pair_np = synthetic.workload(1, side=args.side)
+    ref = (pair_np.reference.astype(np.float32) / 255.0)
+    de = (pair_np.deformed.astype(np.float32) / 255.0)
+    h, w = ref.shape
+    dev = torch.device("cuda", torch.cuda.current_device())
+    ref_d, def_d = torch.from_numpy(ref).to(dev), torch.from_numpy(de).to(dev)
+    sptr = stream.cuda_stream
+    out = []
+    for opt, order, crit in ROUTES:
+        conf = dict(CONFIG, optimization=dict(CONFIG["optimization"], method=opt), correlation={"criterion": crit},
+                    shape_function={"order": order})
+        t_route = time.perf_counter()
+        _, seed = S.compute(ref, de, conf, context=ctx, return_seed=True)
+        print(f"[routes] {opt} {order} {crit}: seed {time.perf_counter() - t_route:.2f} s", file=sys.stderr, flush=True)
+        entry = {"optimizer": opt, "shape_function": order, "criterion": crit}
+        res = {}
+        for prec in ("fp32", "fp64"):
+            cfg = S.config_from_dict(dict(conf, gpu={"precision": prec, "propagation": args.mode}))
+            gw, gh = L.grid_dims(w, h, cfg.propagation_spacing)
+            n = gw * gh
+            outs = {k: torch.empty(n, dtype=torch.float64, device=dev) for k in ("x", "y", "u", "v", "du_dx", "du_dy",
+                                                                                 "dv_dx", "dv_dy", "correlation", "zncc")}
+            outs["valid"] = torch.empty(n, dtype=torch.uint8, device=dev)
+            outs["status"] = torch.empty(n, dtype=torch.int8, device=dev)
+            outs["iterations"] = torch.empty(n, dtype=torch.int32, device=dev)
+            outs["converged"] = torch.empty(n, dtype=torch.uint8, device=dev)
+            grid = L.GridOut(**{k: outs[k].data_ptr() for k in L.GRID_FIELDS})
+            pair = S.Pair(ctx, ref_d, def_d, degree=3, precision=cfg.precision, stream=stream)
+            pc = C.c_int32()
+            ts = []
+            for i in range(3):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                ctx.check(ctx.lib.tdic_propagate(ctx.handle, pair.handle, C.byref(cfg), C.byref(seed), None,
+                                                 C.byref(grid), L.DEVICE, C.byref(pc), sptr))
+                b.record(stream)
+                b.synchronize()
+                if i:
+                    ts.append(a.elapsed_time(b) / 1e3)
+            pair.close()
+            t = statistics.median(ts)
+            print(f"[routes] {opt} {order} {crit} {prec}: {1e3 * t:.1f} ms per propagation", file=sys.stderr, flush=True)
+            valid = outs["valid"].cpu().numpy() != 0
+            conv = int(np.sum(valid & (outs["converged"].cpu().numpy() != 0)))
+            res[prec] = (t, conv, valid, outs["u"].cpu().numpy(), outs["v"].cpu().numpy())
+            entry[prec] = {"ms": 1e3 * t, "converged": conv, "value": conv / t}
+        v32, v64 = res["fp32"][2], res["fp64"][2]
+        both = v32 & v64
+        du = np.abs(res["fp32"][3][both] - res["fp64"][3][both])
+        dv = np.abs(res["fp32"][4][both] - res["fp64"][4][both])
+        entry["fp32_vs_fp64"] = {"flag_agreement": float(np.mean(v32 == v64)),
+                                 "within_1e-3_px": float(np.mean((du <= 1e-3) & (dv <= 1e-3))) if both.any() else None,
+                                 "p99_abs_u_px": float(np.quantile(du, 0.99)) if both.any() else None}
+        entry["speedup_fp32_over_fp64"] = entry["fp64"]["ms"] / entry["fp32"]["ms"]
+        out.append(entry)
+    return out
 
 
 def run_batch(args, ctx, stream) -> dict:
@@ -585,6 +658,8 @@ def main():
     ap.add_argument("--ref-solves", type=int, default=20000)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--routes", action="store_true",
+                    help="also time every solver route (ICGN/FGN x first/second order x ZNSSD/SSD), FP32 and FP64")
     ap.add_argument("--batch", action="store_true",
                     help="also run the uneven 48-pair batch in one launch against per-pair launches")
     ap.add_argument("--batch-pairs", type=int, default=48)

@@ -1388,6 +1388,12 @@ bool select_seed(const float* ref, const float* def, int w, int h, const uint8_t
     return true;
 }
 
+int mirror_index(int i, int n) {  // padding.cpp:11-24
+    if (n <= 1) return 0;
+    while (i < 0 || i >= n) i = i < 0 ? -i - 1 : 2 * n - i - 1;
+    return i;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1515,14 +1521,6 @@ void orc_truncated_grid_dims(int w, int h, const orc_config* c, int* gw, int* gh
     *gw = count(w);
     *gh = count(h);
 }
-
-namespace {
-int mirror_index(int i, int n) {  // padding.cpp:11-24
-    if (n <= 1) return 0;
-    while (i < 0 || i >= n) i = i < 0 ? -i - 1 : 2 * n - i - 1;
-    return i;
-}
-}  // namespace
 
 int orc_subset_compute(const float* ref, const float* def, int w, int h, const uint8_t* roi,
                        const orc_config* cfg, orc_grid_out* out, orc_seed* seed_out) {

@@ -480,23 +480,28 @@ std::vector<std::pair<int, int>> seed_candidates(tdic_ctx* ctx, const Acc& ref, 
     const int iters = std::max(0, c.kmeans_iterations);
     if (iters > 0) {
         const int m = static_cast<int>(sp.size());
-        std::vector<int> px(m), py(m), asg(m);
+        std::vector<int> px(m), py(m);
         for (int j = 0; j < m; ++j) { px[j] = sp[j].x; py[j] = sp[j].y; }
         KmeansAssigner ka(ctx, px.data(), py.data(), m, count, s);
-        std::vector<double> sx(count), sy(count);
-        std::vector<int> cnt(count);
-        for (int it = 0; it < iters; ++it) {
-            ka.assign(cx.data(), cy.data(), asg.data());
-            std::fill(sx.begin(), sx.end(), 0.0);
-            std::fill(sy.begin(), sy.end(), 0.0);
-            std::fill(cnt.begin(), cnt.end(), 0);
-            for (int j = 0; j < m; ++j) {
-                sx[asg[j]] += px[j];
-                sy[asg[j]] += py[j];
-                ++cnt[asg[j]];
+        if (count <= 2048) {  // per-block sums in shared memory (24 bytes per centre)
+            ka.run(cx.data(), cy.data(), iters);
+        } else {
+            std::vector<int> asg(m);
+            std::vector<double> sx(count), sy(count);
+            std::vector<int> cnt(count);
+            for (int it = 0; it < iters; ++it) {
+                ka.assign(cx.data(), cy.data(), asg.data());
+                std::fill(sx.begin(), sx.end(), 0.0);
+                std::fill(sy.begin(), sy.end(), 0.0);
+                std::fill(cnt.begin(), cnt.end(), 0);
+                for (int j = 0; j < m; ++j) {
+                    sx[asg[j]] += px[j];
+                    sy[asg[j]] += py[j];
+                    ++cnt[asg[j]];
+                }
+                for (int i = 0; i < count; ++i)
+                    if (cnt[i] > 0) { cx[i] = sx[i] / cnt[i]; cy[i] = sy[i] / cnt[i]; }
             }
-            for (int i = 0; i < count; ++i)
-                if (cnt[i] > 0) { cx[i] = sx[i] / cnt[i]; cy[i] = sy[i] / cnt[i]; }
         }
     }
     for (int i = 0; i < count; ++i) {

@@ -55,8 +55,11 @@ template <typename T> struct Kahan {
     __device__ __forceinline__ T value() const { return s - c; }
 };
 
+// Group barrier.  The non-aligned form: a group reaches its barriers from lane-divergent code
+// (`if (tid < K)` blocks, strided loops over fewer entries than threads), where the aligned
+// bar.sync (every lane of a warp at the same instruction) is undefined and was seen to deadlock.
 __device__ __forceinline__ void named_bar(int id, int nthreads) {
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+    asm volatile("barrier.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
 // Reduce-scatter of K values over a warp by recursive halving: at each of log2(KP) levels a

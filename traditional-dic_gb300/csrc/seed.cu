@@ -397,6 +397,48 @@ __global__ void kmeans_assign_kernel(const int2* __restrict__ pts, int m, const 
     assign[j] = best;
 }
 
+// One k-means iteration's assignment and centre sums.  The points are integer pixels and the
+// sums stay far below 2^53, so the FP64 sums of run_kmeans (seed_selector.cpp:84-104) are exact
+// whatever the order: they are accumulated here as 64-bit integers (per block in shared memory,
+// then atomically into `acc` = [sum x, sum y, count] per centre).
+__global__ void kmeans_step_kernel(const int2* __restrict__ pts, int m, const double2* __restrict__ ctr, int k,
+                                   unsigned long long* __restrict__ acc) {
+    extern __shared__ unsigned long long s_acc[];  // 3 * k
+    for (int i = threadIdx.x; i < 3 * k; i += blockDim.x) s_acc[i] = 0ull;
+    __syncthreads();
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < m) {
+        const double x = static_cast<double>(pts[j].x), y = static_cast<double>(pts[j].y);
+        int best = 0;
+        double bd = INFINITY;
+        for (int i = 0; i < k; ++i) {
+            const double2 c = __ldg(ctr + i);
+            const double dx = __dsub_rn(x, c.x), dy = __dsub_rn(y, c.y);
+            const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+            if (d2 < bd) { bd = d2; best = i; }
+        }
+        atomicAdd(s_acc + 3 * best, static_cast<unsigned long long>(pts[j].x));
+        atomicAdd(s_acc + 3 * best + 1, static_cast<unsigned long long>(pts[j].y));
+        atomicAdd(s_acc + 3 * best + 2, 1ull);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 3 * k; i += blockDim.x)
+        if (s_acc[i]) atomicAdd(acc + i, s_acc[i]);
+}
+
+// New centres (sum / count, as on the reference's host) for every centre with members; the sums
+// are cleared for the next iteration.
+__global__ void kmeans_update_kernel(double2* __restrict__ ctr, int k, unsigned long long* __restrict__ acc) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k) return;
+    const unsigned long long n = acc[3 * i + 2];
+    if (n > 0) {
+        const double c = static_cast<double>(n);
+        ctr[i] = make_double2(__ddiv_rn(static_cast<double>(acc[3 * i]), c), __ddiv_rn(static_cast<double>(acc[3 * i + 1]), c));
+    }
+    acc[3 * i] = acc[3 * i + 1] = acc[3 * i + 2] = 0ull;
+}
+
 std::vector<short2> circle_offsets(int r, int step) {
     std::vector<short2> o;
     step = step < 1 ? 1 : step;
@@ -410,11 +452,30 @@ std::vector<short2> circle_offsets(int r, int step) {
 
 KmeansAssigner::KmeansAssigner(tdic_ctx* ctx, const int* px, const int* py, int m, int k, cudaStream_t s)
     : ctx_(ctx), s_(s), m_(m), k_(k), pts_(&ctx->pool, sizeof(int2) * std::max(m, 1)),
-      ctr_(&ctx->pool, sizeof(double2) * std::max(k, 1)), out_(&ctx->pool, sizeof(int) * std::max(m, 1)) {
+      ctr_(&ctx->pool, sizeof(double2) * std::max(k, 1)), out_(&ctx->pool, sizeof(int) * std::max(m, 1)),
+      acc_(&ctx->pool, sizeof(unsigned long long) * 3 * std::max(k, 1)) {
     std::vector<int2> p(m);
     for (int i = 0; i < m; ++i) p[i] = make_int2(px[i], py[i]);
     TDIC_CUDA_TRY(cudaMemcpyAsync(pts_.ptr, p.data(), sizeof(int2) * m, cudaMemcpyHostToDevice, s_));
     TDIC_CUDA_TRY(cudaStreamSynchronize(s_));  // p is a local
+}
+
+void KmeansAssigner::run(double* cx, double* cy, int iters) {
+    std::vector<double2> c(k_);
+    for (int i = 0; i < k_; ++i) c[i] = make_double2(cx[i], cy[i]);
+    TDIC_CUDA_TRY(cudaMemcpyAsync(ctr_.ptr, c.data(), sizeof(double2) * k_, cudaMemcpyHostToDevice, s_));
+    TDIC_CUDA_TRY(cudaMemsetAsync(acc_.ptr, 0, sizeof(unsigned long long) * 3 * k_, s_));
+    const size_t smem = sizeof(unsigned long long) * 3 * k_;
+    for (int it = 0; it < iters; ++it) {
+        kmeans_step_kernel<<<(m_ + 255) / 256, 256, smem, s_>>>(pts_.as<int2>(), m_, ctr_.as<double2>(), k_,
+                                                                acc_.as<unsigned long long>());
+        TDIC_CUDA_TRY(cudaGetLastError());
+        kmeans_update_kernel<<<(k_ + 127) / 128, 128, 0, s_>>>(ctr_.as<double2>(), k_, acc_.as<unsigned long long>());
+        TDIC_CUDA_TRY(cudaGetLastError());
+    }
+    TDIC_CUDA_TRY(cudaMemcpyAsync(c.data(), ctr_.ptr, sizeof(double2) * k_, cudaMemcpyDeviceToHost, s_));
+    TDIC_CUDA_TRY(cudaStreamSynchronize(s_));  // c is a local
+    for (int i = 0; i < k_; ++i) { cx[i] = c[i].x; cy[i] = c[i].y; }
 }
 
 void KmeansAssigner::assign(const double* cx, const double* cy, int* assign_host) {

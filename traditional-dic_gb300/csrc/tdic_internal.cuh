@@ -197,11 +197,14 @@ class KmeansAssigner {
 public:
     KmeansAssigner(tdic_ctx* ctx, const int* px, const int* py, int m, int k, cudaStream_t s);
     void assign(const double* cx, const double* cy, int* assign_host);
+    // `iters` whole iterations (assignment, sums, new centres) on the device, one sync at the end;
+    // the same centres as assign() plus the host sums in point order (the sums are exact).
+    void run(double* cx, double* cy, int iters);
 private:
     tdic_ctx* ctx_;
     cudaStream_t s_;
     int m_, k_;
-    Buffer pts_, ctr_, out_;
+    Buffer pts_, ctr_, out_, acc_;
 };
 // roi (host mask of the pair's image, or NULL): the masked search of truncate_roi_subsets.
 void integer_search_batch(tdic_ctx* ctx, tdic_pair* lazy, const tdic_config& cfg, const int* cx, const int* cy,
