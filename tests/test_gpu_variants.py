@@ -240,11 +240,15 @@ def test_compute_routes_match_oracle_pipeline(oracle, gpu_ctx, workload0, criter
     assert ("d2u_dx2" in got) == (order == "second_order")
 
 
+@pytest.mark.parametrize("precision", [1, 0])
 @pytest.mark.parametrize("opt", [0, 1])
-def test_second_order_propagation_dense_grid(oracle, gpu_ctx, opt):
-    """Second-order propagation over a 52 x 52 grid (the sinusoidal field at 256^2, step 5): many
-    concurrent four-warp solves, whose set-up reaches group barriers from lane-divergent code.
-    Against the oracle in the same (dataflow) order."""
+def test_second_order_propagation_dense_grid(oracle, gpu_ctx, opt, precision):
+    """Second-order propagation over a 52 x 52 grid (the sinusoidal field at 256^2, r = 10, step 5):
+    many concurrent four-warp solves, whose set-up reaches group barriers from lane-divergent code.
+    Against the oracle in the same (dataflow) order: the FP64 build to 1e-6 px at the 99th
+    percentile; the FP32-mixed build on flags and the median only - on this weakly determined
+    second-order fit (317 samples) about 1 % of its ICGN points settle up to ~0.07 px away from the
+    FP64 solution."""
     import __graft_entry__ as G
     from traditional_dic_gb300 import subset as S, synthetic
     p = synthetic.workload(1, side=256)
@@ -252,16 +256,19 @@ def test_second_order_propagation_dense_grid(oracle, gpu_ctx, opt):
     de = p.deformed.astype(np.float32) / 255.0
     conf = dict(G.WORKLOAD0_CONFIG, reliability_propagation={"spacing": 4, "max_znssd": 0.5})
     cfg = S.config_from_dict(conf)
-    cfg.shape_order, cfg.optimizer, cfg.propagation_mode = 2, opt, 2
+    cfg.shape_order, cfg.optimizer, cfg.propagation_mode, cfg.precision = 2, opt, 2, precision
     ocfg = oracle.as_config(cfg)
     oseed, _ = oracle.select_seed(ref, de, ocfg)
     assert oseed.found
-    pair = S.Pair(gpu_ctx, ref, de, degree=3)
+    pair = S.Pair(gpu_ctx, ref, de, degree=3, precision=precision)
     got = S.propagate(gpu_ctx, pair, cfg, S.make_seed(oseed.x, oseed.y, list(oseed.p), oseed.correlation))
     want = oracle.propagate(ref, oracle.prefilter(de, 3, 3, True), ocfg, oseed)
     assert len(got["x"]) == 52 * 52 and want["points_computed"] > 2000
     assert np.mean(got["valid"] == want["valid"]) >= 0.995
     both = got["valid"] & want["valid"]
     d = np.hypot(got["u"][both] - want["u"][both], got["v"][both] - want["v"][both])
-    assert np.quantile(d, 0.99) <= U_TOL
+    if precision == 1:
+        assert np.quantile(d, 0.99) <= 1e-6
+    else:
+        assert np.median(d) <= 1e-4
     pair.close()
