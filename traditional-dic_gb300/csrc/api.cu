@@ -721,6 +721,10 @@ tdic_status tdic_pair_create(tdic_ctx* ctx, const void* reference, const void* d
     return guarded(ctx, [&] {
         TDIC_REQUIRE(reference && deformed, TDIC_INVALID_ARG, "Cannot precompute B-spline data for an empty image.");
         TDIC_REQUIRE(width > 0 && height > 0, TDIC_INVALID_ARG, "Cannot precompute B-spline data for an empty image.");
+        // POI grids are counted and indexed in int32 (a grid point per pixel at spacing 0)
+        TDIC_REQUIRE((static_cast<int64_t>(width) + 64) * (static_cast<int64_t>(height) + 64) <= INT32_MAX, TDIC_INVALID_ARG,
+                     "image of " + std::to_string(width) + " x " + std::to_string(height) +
+                         " pixels exceeds the 2^31-point limit of the POI grid");
         TDIC_REQUIRE(degree == 1 || degree == 3 || degree == 5, TDIC_INVALID_ARG,
                      "Only B-spline degree 1, 3, and 5 are supported; got " + std::to_string(degree) + ".");
         TDIC_REQUIRE(precision == TDIC_FP32_MIXED || precision == TDIC_FP64, TDIC_INVALID_ARG, "unknown precision");
