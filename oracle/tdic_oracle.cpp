@@ -1515,6 +1515,7 @@ void orc_truncated_grid_dims(int w, int h, const orc_config* c, int* gw, int* gh
     const int pad = c->truncate_roi_subsets ? orc_subset_padding(c) : 0;
     const int step = std::max(0, c->propagation_spacing) + 1;
     auto count = [&](int n) {  // grid points gx * step - pad inside [0, n)
+        if (n <= 0) return 0;
         const int lo = (pad + step - 1) / step, hi = (n - 1 + pad) / step;
         return std::max(0, hi - lo + 1);
     };

@@ -85,3 +85,33 @@ def test_grid_dims(pkg):
     assert L.grid_dims(2048, 2048, 4) == (410, 410)
     assert L.grid_dims(5120, 5120, 2) == (1707, 1707)
     assert L.grid_dims(7, 3, -4) == (7, 3)
+
+
+def test_truncation_geometry_matches_oracle(pkg, oracle):
+    """recommended_subset_padding (padding.cpp:28-36) and the cropped output grid of
+    SubsetDIC::compute with truncate_roi_subsets (subset_dic.cpp:53-104): the library's host
+    functions against the oracle over a sweep of image sizes, spacings and radii."""
+    from traditional_dic_gb300 import _lib as L
+    rng = np.random.default_rng(11)
+    for _ in range(300):
+        cfg = L.default_config()
+        cfg.truncate_roi_subsets = int(rng.integers(0, 2))
+        cfg.subset_radius = int(rng.integers(1, 40))
+        cfg.is_subset_radius = int(rng.integers(-2, 40))
+        cfg.sp_subset_radius = int(rng.integers(-2, 40))
+        cfg.is_search_radius = int(rng.integers(-5, 80))
+        cfg.border = int(rng.integers(-2, 8))
+        cfg.propagation_spacing = int(rng.integers(-3, 12))
+        w, h = int(rng.integers(0, 300)), int(rng.integers(0, 300))
+        pad = L.load().tdic_subset_padding(C.byref(cfg))
+        # the library reports the padding subset_compute applies: none without truncation
+        assert pad == (oracle.subset_padding(cfg) if cfg.truncate_roi_subsets else 0)
+        got = L.subset_grid_dims(w, h, cfg)
+        assert got == oracle.truncated_grid_dims(w, h, cfg)
+        step = max(0, cfg.propagation_spacing) + 1
+        # the points kept are exactly the padded grid's points x = g * step - pad inside [0, w)
+        for n, g in ((w, got[0]), (h, got[1])):
+            gp = -(-(n + 2 * pad) // step)
+            assert g == sum(1 for k in range(gp) if 0 <= k * step - pad < n)
+        if not cfg.truncate_roi_subsets:
+            assert got == L.grid_dims(w, h, cfg.propagation_spacing)
