@@ -12,6 +12,10 @@ default), with device outputs.  ``value`` = converged POIs (valid, strictly conv
 seed selection, prefilter, propagation and the device->host result dict, every step.
 L2 (129 MB) is flushed with a 256 MB write between timed steps.
 
+``cpu_baseline`` is the FP64 C++ port of the reference path (oracle/) on every host thread over
+the whole workload (dataflow order, each diagonal's solves spread over the threads);
+``cpu_baseline_serial`` is the same port on one thread in the reference's heap order, on a prefix.
+
 ``--impl reference`` times the reference algorithm's CPU implementation (the FP64 C++ port in
 oracle/, the reference itself does not build without Eigen) on a bounded sample of the same
 workload: reliability-guided heap propagation, single thread as the reference runs.
@@ -236,6 +240,49 @@ def run_reference(args, world, rank, pg):
     print(json.dumps(line), flush=True)
 
 
+def host_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
+
+def cpu_baselines(reference, deformed, cfg, seed, ref_solves: int, threads: int | None = None):
+    """The FP64 C++ port of the reference path (oracle/) on the host cores, from the same seed:
+    (1) every host thread on the whole workload in dataflow order, the solves of each diagonal
+    spread over the threads (the visit order and results of one thread); (2) one thread in the
+    reference's own heap order on its first ``ref_solves`` solves.  Returns (parallel, serial)
+    ``cpu_baseline`` objects; a leg that fails reports its error instead of a value."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    threads = threads or host_threads()
+    coef = O.prefilter(deformed, 3, 3, True)
+    grads = O.reference_gradient(reference)
+    oseed = O.make_seed(seed.x, seed.y, list(seed.p), seed.correlation)
+    legs = []
+    # a full 2048^2 propagation is about 50 s of one core: below 4 threads, time a prefix
+    budget = -1 if threads >= 4 else ref_solves * threads
+    for mode, n_threads, max_solves in ((2, threads, budget), (1, 1, ref_solves)):
+        ocfg = O.as_config(cfg)
+        ocfg.propagation_mode = mode
+        try:
+            t0 = time.perf_counter()
+            rr = O.propagate(reference, coef, ocfg, oseed, gradients=grads, max_solves=max_solves, threads=n_threads)
+            dt = time.perf_counter() - t0
+        except Exception as e:  # the GPU figures above stand without the baseline
+            legs.append({"value": None, "unit": UNIT, "cores": n_threads, "kind": "port", "error": repr(e)})
+            continue
+        conv = int(np.sum(rr["valid"] & rr["converged"]))
+        what = ("the whole 2048^2 workload, dataflow order" if max_solves < 0 and mode == 2 else
+                f"first {rr['solves']} {'heap-order' if mode == 1 else 'dataflow-order'} solves of the same "
+                f"2048^2 workload")
+        legs.append({"value": conv / dt, "unit": UNIT, "cores": n_threads, "kind": "port",
+                     "sample": f"{what}: {rr['solves']} solves, {conv} converged in {dt:.1f} s "
+                               f"(FP64 C++ port of the reference path, {n_threads} thread"
+                               f"{'s' if n_threads > 1 else ''})"})
+    return legs[0], legs[1]
+
+
 def run_ours(args, world, rank, local, pg):
     import torch
     from traditional_dic_gb300 import subset as S, synthetic, _lib as L
@@ -376,21 +423,9 @@ def run_ours(args, world, rank, local, pg):
     e2e_value = sum_over_ranks(pg, float(e2e_conv)) / t_e2e
     d2h = n * (10 * 8 + 1 + 1 + 4 + 1)
 
-    cpu = None
+    cpu = cpu_serial = None
     if rank == 0 and not args.skip_cpu:
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        import oracle as O
-        ocfg = O.as_config(cfg)
-        ocfg.propagation_mode = 1
-        coef = O.prefilter(pair_np.deformed, 3, 3, True)
-        grads = O.reference_gradient(pair_np.reference)
-        oseed = O.make_seed(seed.x, seed.y, list(seed.p), seed.correlation)
-        t0 = time.perf_counter()
-        rr = O.propagate(pair_np.reference, coef, ocfg, oseed, gradients=grads, max_solves=args.ref_solves)
-        dt = time.perf_counter() - t0
-        cpu = {"value": float(np.sum(rr["valid"] & rr["converged"])) / dt, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"first {rr['solves']} heap-order solves of the same 2048^2 workload "
-                         f"({dt:.1f} s, FP64 C++ port of the reference path, 1 thread)"}
+        cpu, cpu_serial = cpu_baselines(pair_np.reference, pair_np.deformed, cfg, seed, args.ref_solves)
 
     routes = run_routes(args, ctx, stream) if (args.routes and rank == 0) else None
     batched = run_batch(args, ctx, stream) if (args.batch and rank == 0) else None
@@ -406,6 +441,7 @@ def run_ours(args, world, rank, local, pg):
             "converged_pois_per_step": conv,
             "roofline": roofline,
             "cpu_baseline": cpu,
+            "cpu_baseline_serial": cpu_serial,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(2 * h * w),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * t_e2e,
                     "includes": "H2D of both images (pinned), seed selection, prefilter, propagation, D2H of the "

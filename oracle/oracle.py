@@ -102,6 +102,9 @@ def lib():
                                                   C.POINTER(C.c_int)]
             L.orc_propagate.argtypes = [P, C.c_int, C.c_int, P, P, P, P, C.POINTER(Config), C.POINTER(Seed),
                                         C.c_int, C.POINTER(GridOut), C.POINTER(C.c_int)]
+            L.orc_propagate_threads.argtypes = [P, C.c_int, C.c_int, P, P, P, P, C.POINTER(Config),
+                                                C.POINTER(Seed), C.c_int, C.POINTER(GridOut), C.POINTER(C.c_int),
+                                                C.c_int]
             L.orc_integer_search.argtypes = [P, P, C.c_int, C.c_int, C.POINTER(Config), C.c_double, C.c_double,
                                              C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
             L.orc_select_seed.argtypes = [P, P, C.c_int, C.c_int, P, C.POINTER(Config), C.POINTER(Seed), P,
@@ -267,7 +270,11 @@ def make_seed(x, y, p, correlation) -> Seed:
     return s
 
 
-def propagate(reference, deformed_coeffs, cfg, seed: Seed, roi=None, gradients=None, max_solves: int = -1):
+def propagate(reference, deformed_coeffs, cfg, seed: Seed, roi=None, gradients=None, max_solves: int = -1,
+              threads: int = 1):
+    """ReliabilityPropagation::propagate with one seed.  ``threads`` > 1 solves each frontier wave
+    (propagation_mode 0) or dataflow diagonal (mode 2) on that many host threads; the result is
+    the same for every thread count, and the heap order (mode 1) is always serial."""
     cfg = as_config(cfg)
     ref = _img(reference)
     h, w = ref.shape
@@ -280,8 +287,9 @@ def propagate(reference, deformed_coeffs, cfg, seed: Seed, roi=None, gradients=N
     gw, gh = grid_dims(w, h, cfg.propagation_spacing)
     arrs, g = _alloc_grid(gw * gh)
     solves = C.c_int()
-    computed = lib().orc_propagate(_ptr(ref), w, h, _ptr(r), _ptr(gx), _ptr(gy), _ptr(c), C.byref(cfg),
-                                   C.byref(seed), int(max_solves), C.byref(g), C.byref(solves))
+    computed = lib().orc_propagate_threads(_ptr(ref), w, h, _ptr(r), _ptr(gx), _ptr(gy), _ptr(c), C.byref(cfg),
+                                           C.byref(seed), int(max_solves), C.byref(g), C.byref(solves),
+                                           max(1, int(threads)))
     out = _finish_grid(arrs, gw * gh)
     out["points_computed"] = computed
     out["solves"] = solves.value

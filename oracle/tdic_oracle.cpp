@@ -16,12 +16,19 @@
 #include "tdic_oracle.h"
 
 #include <algorithm>
+#include <array>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
+#include <condition_variable>
+#include <cstdint>
 #include <cstring>
+#include <functional>
 #include <limits>
+#include <mutex>
 #include <numeric>
 #include <queue>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -837,10 +844,78 @@ int nearest_grid_index(int c, int step, int limit) {  // reliability_propagation
 
 float corr_key(double c) { return static_cast<float>(c); }
 
+// A fixed team of host threads that runs one indexed loop at a time: the solves of one frontier
+// wave or one dataflow diagonal, which read only the previous wave's results.  The calling thread
+// works too; run() returns when every index is done.
+class Team {
+public:
+    explicit Team(int n) : n_(std::max(1, n)) {
+        for (int t = 1; t < n_; ++t) th_.emplace_back([this] { worker(); });
+    }
+    ~Team() {
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            stop_ = true;
+            ++gen_;
+        }
+        cv_.notify_all();
+        for (auto& t : th_) t.join();
+    }
+    void run(int count, const std::function<void(int)>& f) {
+        if (n_ == 1 || count < 2) {
+            for (int i = 0; i < count; ++i) f(i);
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            f_ = &f;
+            count_ = count;
+            next_.store(0);
+            active_ = n_ - 1;
+            ++gen_;
+        }
+        cv_.notify_all();
+        drain();
+        std::unique_lock<std::mutex> l(mu_);
+        done_.wait(l, [this] { return active_ == 0; });
+        f_ = nullptr;
+    }
+
+private:
+    void drain() {
+        for (int i = next_.fetch_add(1); i < count_; i = next_.fetch_add(1)) (*f_)(i);
+    }
+    void worker() {
+        std::uint64_t seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> l(mu_);
+                cv_.wait(l, [&] { return gen_ != seen; });
+                seen = gen_;
+                if (stop_) return;
+            }
+            drain();
+            std::lock_guard<std::mutex> l(mu_);
+            if (--active_ == 0) done_.notify_one();
+        }
+    }
+    int n_;
+    std::vector<std::thread> th_;
+    std::mutex mu_;
+    std::condition_variable cv_, done_;
+    const std::function<void(int)>* f_ = nullptr;
+    int count_ = 0, active_ = 0;
+    std::atomic<int> next_{0};
+    std::uint64_t gen_ = 0;
+    bool stop_ = false;
+};
+
 // reliability_propagation.cpp:130-394 (mode 1, heap order), the frontier-wave rule (mode 0) and
-// the dataflow order with frontier-wave cleanup (mode 2).
+// the dataflow order with frontier-wave cleanup (mode 2).  Modes 0 and 2 solve the points of a
+// wave (a diagonal) on `threads` host threads; the result does not depend on the thread count.
 int propagate(const float* ref, int w, int h, const uint8_t* roi, const GradSource& gs, const Spline& sp,
-              const orc_config& c, const orc_seed& seed, int max_solves, orc_grid_out* out, int* solves_done) {
+              const orc_config& c, const orc_seed& seed, int max_solves, orc_grid_out* out, int* solves_done,
+              int threads = 1) {
     int solves = 0;
     if (solves_done) *solves_done = 0;
     const int spacing = std::max(0, c.propagation_spacing);
@@ -950,7 +1025,18 @@ int propagate(const float* ref, int w, int h, const uint8_t* roi, const GradSour
             p0[1] = pp0[1] + pp0[4] * ddx + pp0[5] * ddy;
             p0[2] = pp0[2]; p0[3] = pp0[3]; p0[4] = pp0[4]; p0[5] = pp0[5];
             r = solve_one(ref, w, h, gs, sp, scfg, nx, ny, p0, 0.0);
-            ++solves;
+        };
+        // Solves todo[i] from parent par[i] for every i on the team (each reads only accepted
+        // points of earlier waves), then returns the results in todo order.
+        Team team(threads);
+        std::vector<orc_poi_result> res;
+        std::vector<std::array<double, 6>> res_p0;
+        auto solve_all = [&](const std::vector<int>& todo, const std::vector<int>& par) {
+            res.assign(todo.size(), orc_poi_result{});
+            res_p0.assign(todo.size(), std::array<double, 6>{});
+            team.run(static_cast<int>(todo.size()),
+                     [&](int i) { solve_from(todo[i], par[i], res[i], res_p0[i].data()); });
+            solves += static_cast<int>(todo.size());
         };
         auto keep = [&](int nidx, const orc_poi_result& r) {
             store(out, nidx, r);
@@ -984,16 +1070,18 @@ int propagate(const float* ref, int w, int h, const uint8_t* roi, const GradSour
                         next.push_back(nidx);
                     }
                 }
-                std::vector<int> acc;
+                std::vector<int> acc, todo, par;
                 for (int nidx : next) {
                     calc[nidx] = 1;
-                    if (max_solves >= 0 && solves >= max_solves) continue;
-                    orc_poi_result r;
-                    double p0[6];
-                    solve_from(nidx, best_parent[nidx], r, p0);
-                    if (accept(r, p0[0], p0[1])) {
-                        keep(nidx, r);
-                        acc.push_back(nidx);
+                    if (max_solves >= 0 && solves + static_cast<int>(todo.size()) >= max_solves) continue;
+                    todo.push_back(nidx);
+                    par.push_back(best_parent[nidx]);
+                }
+                solve_all(todo, par);
+                for (std::size_t i = 0; i < todo.size(); ++i) {
+                    if (accept(res[i], res_p0[i][0], res_p0[i][1])) {
+                        keep(todo[i], res[i]);
+                        acc.push_back(todo[i]);
                     }
                 }
                 for (int nidx : next) best_parent[nidx] = -2;  // resolved; never a candidate again
@@ -1012,7 +1100,11 @@ int propagate(const float* ref, int w, int h, const uint8_t* roi, const GradSour
             const int sgx = gxs, sgy = gys;
             const int maxd = std::max(sgx, gw - 1 - sgx) + std::max(sgy, gh - 1 - sgy);
             auto sgn = [](int v) { return v > 0 ? 1 : -1; };
+            std::vector<int> todo, par;
             for (int d = 1; d <= maxd; ++d) {
+                // the parents of diagonal d lie on diagonal d - 1: its points are independent
+                todo.clear();
+                par.clear();
                 for (int gy = 0; gy < gh; ++gy) {
                     const int rem = d - std::abs(gy - sgy);
                     if (rem < 0) continue;
@@ -1038,13 +1130,18 @@ int propagate(const float* ref, int w, int h, const uint8_t* roi, const GradSour
                         const bool admissible = roi_valid(roi, w, h, nx, ny) && nx - radius >= 0 && ny - radius >= 0 &&
                                                 nx + radius < w && ny + radius < h;
                         calc[nidx] = 1;
-                        if (!admissible || (max_solves >= 0 && solves >= max_solves)) { st[nidx] = kRej; continue; }
-                        orc_poi_result r;
-                        double p0[6];
-                        solve_from(nidx, parent, r, p0);
-                        if (accept(r, p0[0], p0[1])) { keep(nidx, r); st[nidx] = kAcc; }
-                        else st[nidx] = kRej;
+                        if (!admissible || (max_solves >= 0 && solves + static_cast<int>(todo.size()) >= max_solves)) {
+                            st[nidx] = kRej;
+                            continue;
+                        }
+                        todo.push_back(nidx);
+                        par.push_back(parent);
                     }
+                }
+                solve_all(todo, par);
+                for (std::size_t i = 0; i < todo.size(); ++i) {
+                    if (accept(res[i], res_p0[i][0], res_p0[i][1])) { keep(todo[i], res[i]); st[todo[i]] = kAcc; }
+                    else st[todo[i]] = kRej;
                 }
             }
             std::vector<int> all_acc;
@@ -1485,10 +1582,16 @@ void orc_grid_dims(int w, int h, int spacing, int* gw, int* gh) {
 int orc_propagate(const float* ref, int w, int h, const uint8_t* roi, const double* ref_gx, const double* ref_gy,
                   const double* coeffs, const orc_config* cfg, const orc_seed* seed, int max_solves,
                   orc_grid_out* out, int* solves_done) {
+    return orc_propagate_threads(ref, w, h, roi, ref_gx, ref_gy, coeffs, cfg, seed, max_solves, out, solves_done, 1);
+}
+
+int orc_propagate_threads(const float* ref, int w, int h, const uint8_t* roi, const double* ref_gx,
+                          const double* ref_gy, const double* coeffs, const orc_config* cfg, const orc_seed* seed,
+                          int max_solves, orc_grid_out* out, int* solves_done, int threads) {
     Spline sp;
     sp.init(coeffs, w, h, cfg->degree, cfg->border);
     GradSource gs{ref, w, h, ref_gx, ref_gy};
-    return propagate(ref, w, h, roi, gs, sp, *cfg, *seed, max_solves, out, solves_done);
+    return propagate(ref, w, h, roi, gs, sp, *cfg, *seed, max_solves, out, solves_done, threads);
 }
 
 int orc_integer_search(const float* ref, const float* def, int w, int h, const orc_config* cfg,

@@ -144,6 +144,13 @@ int orc_propagate(const float* ref, int w, int h, const uint8_t* roi,
                   const double* ref_gx, const double* ref_gy, const double* coeffs,
                   const orc_config* cfg, const orc_seed* seed, int max_solves, orc_grid_out* out,
                   int* solves_done);
+/* orc_propagate with the points of each frontier wave (propagation_mode 0) or dataflow diagonal
+ * (mode 2) solved on `threads` host threads; the heap order (mode 1) stays serial.  The output
+ * does not depend on `threads`. */
+int orc_propagate_threads(const float* ref, int w, int h, const uint8_t* roi,
+                          const double* ref_gx, const double* ref_gy, const double* coeffs,
+                          const orc_config* cfg, const orc_seed* seed, int max_solves,
+                          orc_grid_out* out, int* solves_done, int threads);
 
 /* integer_search.cpp:333-432 */
 int orc_integer_search(const float* ref, const float* def, int w, int h, const orc_config* cfg,

@@ -254,3 +254,24 @@ def test_heap_and_frontier_orders(oracle, workload0):
     both = heap["valid"]
     d = np.hypot(heap["u"][both] - front["u"][both], heap["v"][both] - front["v"][both])
     assert np.median(d) < 1e-4 and d.max() < 1e-2
+
+
+@pytest.mark.parametrize("mode", [0, 2])
+@pytest.mark.parametrize("max_solves", [-1, 150])
+def test_threaded_propagation_is_the_serial_one(oracle, workload0, mode, max_solves):
+    """The threaded CPU baseline solves each frontier wave (mode 0) or dataflow diagonal (mode 2)
+    on several host threads: every output array, the solve count and the point count are those
+    of one thread, with and without a solve budget."""
+    import __graft_entry__ as G
+    from traditional_dic_gb300 import subset as S
+    cfg = oracle.as_config(S.config_from_dict(G.WORKLOAD0_CONFIG))
+    cfg.propagation_mode = mode
+    seed, _ = oracle.select_seed(workload0.reference, workload0.deformed, cfg)
+    coef = oracle.prefilter(workload0.deformed, 3, 3, True)
+    grads = oracle.reference_gradient(workload0.reference)
+    one = oracle.propagate(workload0.reference, coef, cfg, seed, gradients=grads, max_solves=max_solves)
+    many = oracle.propagate(workload0.reference, coef, cfg, seed, gradients=grads, max_solves=max_solves, threads=5)
+    assert one["solves"] == many["solves"] and one["points_computed"] == many["points_computed"] > 100
+    for k, a in one.items():
+        if isinstance(a, np.ndarray):
+            assert np.array_equal(a, many[k], equal_nan=a.dtype.kind == "f"), k
