@@ -37,6 +37,14 @@ min_valid_samples = 12, ceil(0.5 * full circle)) samples are needed; the masked 
 step at 0.5 (first-order ZNSSD), 0.35 (SSD) and 0.3 (second-order ZNSSD, no damping term,
 convergence on the norm before the cap).
 
+tests/golden/subset_propagation_256.npz holds whole propagations over the small workload's grid
+(ReliabilityPropagation::propagate, src/subset/seed/reliability_propagation.cpp:130-394) with the
+first-order ZNSSD ICGN above, without and with a ROI: grid ceil(W/s) x ceil(H/s) for s = spacing
++ 1; the seed rounded (std::round), moved to the nearest grid point (llround, clamped) and solved
+there again; a min-heap on ZNSSD; 4-neighbours up, right, down, left; ROI and margin admission;
+the guess extrapolated with the parent's displacement gradients; strict acceptance (valid,
+Success, ZNSSD < propagation_max_znssd, |guess - result| < s in u and v, all finite).
+
 Run from the repository root:  python tests/golden/make_golden.py
 """
 import math
@@ -267,7 +275,7 @@ def solve_variant(ref, coef, qk, px, py, p0, optimizer, order, ssd, roi=None):
     cx, cy = int(np.round(px)), int(np.round(py))
     r = RADIUS
     p = np.zeros(npar)
-    p[:2] = p0
+    p[:len(p0)] = p0
     out = lambda st, corr, it, conv: (np.concatenate([p[:6], p[6:], np.zeros(12 - npar)]), corr, it, st, conv)
     masked = roi is not None
     if masked:
@@ -442,6 +450,109 @@ def main_masked():
     print(f"wrote {MASKED_OUT}")
 
 
+PROPAGATION_OUT = os.path.join(HERE, "subset_propagation_256.npz")
+SPACING, MAX_ZNSSD = 9, 0.5
+
+
+def round_half_away(x):
+    """std::round / std::llround: halves away from zero."""
+    return int(math.copysign(math.floor(abs(x) + 0.5), x))
+
+
+def propagate_heap(ref, coef, qk, seed_xy, seed_p, seed_corr, roi=None):
+    """ReliabilityPropagation::propagate with one seed and the first-order ZNSSD ICGN.  Returns the
+    grid arrays (p, correlation, valid, status, iterations; defaults where no result was kept), the
+    number of points kept and the number of solves."""
+    h, w = ref.shape
+    step = SPACING + 1
+    gw, gh = -(-w // step), -(-h // step)
+    n = gw * gh
+    p_out, corr_out = np.zeros((n, 6)), np.zeros(n)
+    valid, status, iters = np.zeros(n, bool), np.full(n, -1, np.int64), np.zeros(n, np.int64)
+    calc = np.zeros(n, bool)
+    roi_ok = (lambda x, y: True) if roi is None else (lambda x, y: bool(roi[y, x]))
+    solve = lambda x, y, p0: solve_variant(ref, coef, qk, float(x), float(y), np.asarray(p0, np.float64), 0, 1, False)
+    sxr, syr = round_half_away(seed_xy[0]), round_half_away(seed_xy[1])
+    if not (0 <= sxr < w and 0 <= syr < h) or not roi_ok(sxr, syr):
+        return p_out, corr_out, valid, status, iters, 0, 0
+    gxs = min(max(round_half_away(sxr / step), 0), gw - 1)
+    gys = min(max(round_half_away(syr / step), 0), gh - 1)
+    sx, sy = gxs * step, gys * step
+    if not roi_ok(sx, sy):
+        return p_out, corr_out, valid, status, iters, 0, 0
+    sidx = gys * gw + gxs
+    solves = 0
+    sp, scorr, sit = np.asarray(seed_p, np.float64), float(seed_corr), 0
+    if (sx, sy) != (sxr, syr):
+        q, scorr, sit, st, _ = solve(sx, sy, seed_p)
+        solves += 1
+        sp = q[:6]
+        if st != 0 or not (np.all(np.isfinite(sp)) and math.isfinite(scorr)):
+            return p_out, corr_out, valid, status, iters, 0, solves
+    calc[sidx] = True
+    p_out[sidx], corr_out[sidx], valid[sidx], status[sidx], iters[sidx] = sp, scorr, True, 0, sit
+    kept = 1
+    import heapq
+    heap, seq, keys = [(max(0.0, scorr), 0, gxs, gys, sp)], 1, {max(0.0, scorr)}
+    while heap:
+        _, _, gx, gy, pp = heapq.heappop(heap)
+        px, py = gx * step, gy * step
+        for nx, ny in ((px, py - step), (px + step, py), (px, py + step), (px - step, py)):
+            if not (0 <= nx < w and 0 <= ny < h):
+                continue
+            gnx, gny = nx // step, ny // step
+            if gnx >= gw or gny >= gh:
+                continue
+            nidx = gny * gw + gnx
+            if calc[nidx]:
+                continue
+            if not roi_ok(nx, ny) or nx - RADIUS < 0 or ny - RADIUS < 0 or nx + RADIUS >= w or ny + RADIUS >= h:
+                calc[nidx] = True
+                continue
+            dx, dy = float(nx - px), float(ny - py)
+            p0 = np.array([pp[0] + pp[2] * dx + pp[3] * dy, pp[1] + pp[4] * dx + pp[5] * dy,
+                           pp[2], pp[3], pp[4], pp[5]])
+            q, c, it, st, _ = solve(nx, ny, p0)
+            solves += 1
+            calc[nidx] = True
+            r = q[:6]
+            if (st == 0 and c < MAX_ZNSSD and abs(p0[0] - r[0]) < step and abs(p0[1] - r[1]) < step
+                    and np.all(np.isfinite(r)) and math.isfinite(c)):
+                p_out[nidx], corr_out[nidx], valid[nidx], status[nidx], iters[nidx] = r, c, True, st, it
+                kept += 1
+                # the heap order of equal keys is implementation-defined in std::priority_queue
+                assert c not in keys, "two equal ZNSSD keys: the visit order would be ambiguous"
+                keys.add(c)
+                heapq.heappush(heap, (c, seq, gnx, gny, r))
+                seq += 1
+    return p_out, corr_out, valid, status, iters, kept, solves
+
+
+def main_propagation():
+    from traditional_dic_gb300 import synthetic
+    qk = qk_matrix(DEGREE)
+    pair = synthetic.workload(0)
+    ref, de = pair.reference, pair.deformed
+    coef = coefficients(de, DEGREE, BORDER)
+    seed_xy = (131.4, 126.0)   # rounds to (131, 126), off the grid: the seed is solved again at (130, 130)
+    u, v = pair.field.uv(np.float64(seed_xy[0]), np.float64(seed_xy[1]))
+    seed_p = np.array([round(2 * float(u)) / 2.0, round(2 * float(v)) / 2.0, 0, 0, 0, 0])
+    yy, xx = np.mgrid[:256, :256]
+    rois = {"full": None, "roi": ((xx - 120) ** 2 + (yy - 140) ** 2 < 90 ** 2) & ~((xx > 60) & (xx < 75))}
+    arrays = {"seed_xy": np.array(seed_xy), "seed_p": seed_p, "seed_correlation": np.array(0.0),
+              "settings": np.array([DEGREE, BORDER, RADIUS, MAX_ITER, THRESHOLD, SPACING, MAX_ZNSSD])}
+    for tag, roi in rois.items():
+        p, c, val, st, it, kept, solves = propagate_heap(ref, coef, qk, seed_xy, seed_p, 0.0, roi)
+        arrays[f"p_{tag}"], arrays[f"correlation_{tag}"], arrays[f"valid_{tag}"] = p, c, val
+        arrays[f"status_{tag}"], arrays[f"iterations_{tag}"] = st, it
+        arrays[f"counts_{tag}"] = np.array([kept, solves])
+        if roi is not None:
+            arrays[f"mask_{tag}"] = roi
+        print(f"propagation {tag}: {kept} kept of {solves} solves")
+    np.savez_compressed(PROPAGATION_OUT, **arrays)
+    print(f"wrote {PROPAGATION_OUT}")
+
+
 def main():
     sys.path.insert(0, ROOT)
     import __graft_entry__ as G
@@ -466,6 +577,7 @@ def main():
     print(f"wrote {OUT}: {len(pois)} POIs, {int(sum(r[9] for r in res))} converged")
     main_variants()
     main_masked()
+    main_propagation()
 
 
 if __name__ == "__main__":

@@ -1,6 +1,7 @@
-"""Golden vectors (tests/golden/subset_icgn_256.npz, made by tests/golden/make_golden.py from an
-independent numpy transcription of the reference): the C++ oracle (CPU) and the GPU path (GPU)
-must reproduce the B-spline coefficients and the per-POI ICGN results."""
+"""Golden vectors (tests/golden/*.npz, made by tests/golden/make_golden.py from an independent
+numpy transcription of the reference): the C++ oracle (CPU) and the GPU path (GPU) must reproduce
+the B-spline coefficients and the per-POI results of every solver route, full and masked; the
+oracle must reproduce whole heap-order propagations over the grid, with and without a ROI."""
 import os
 
 import numpy as np
@@ -159,3 +160,44 @@ def test_oracle_masked_match_golden(oracle, masked, golden, name, opt, order, cr
     want = masked[name]
     assert (want[:, 14] == 0).sum() > 60 and (want[:, 14] == 2).sum() > 60   # both kinds of points present
     _check_variant(r, want, P_TOL, Q_TOL, 1e-9)
+
+
+# ---- whole propagations (tests/golden/subset_propagation_256.npz) ---------------------------
+PROPAGATION_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "subset_propagation_256.npz")
+
+
+@pytest.fixture(scope="module")
+def propagation():
+    d = np.load(PROPAGATION_FILE)
+    return {k: d[k] for k in d.files}
+
+
+@pytest.mark.parametrize("tag", ["full", "roi"])
+def test_oracle_heap_propagation_matches_golden(oracle, golden, propagation, tag):
+    """The oracle's reliability-guided propagation in the reference's heap order against an
+    independent transcription of ReliabilityPropagation::propagate: the same points solved and
+    kept, the same flags and iteration counts, and the kept results to FP64 agreement."""
+    g = propagation
+    degree, border, radius, max_iter, thr, spacing, max_znssd = g["settings"]
+    cfg = oracle.default_config()
+    cfg.subset_radius, cfg.max_iterations, cfg.convergence_threshold = int(radius), int(max_iter), float(thr)
+    cfg.degree, cfg.border, cfg.optimizer, cfg.shape_order, cfg.criterion = int(degree), int(border), 0, 1, 1
+    cfg.propagation_spacing, cfg.propagation_max_znssd, cfg.propagation_mode = int(spacing), float(max_znssd), 1
+    ref = golden["reference"].astype(np.float32)
+    coef = oracle.prefilter(golden["deformed"].astype(np.float32), int(degree), int(border), True)
+    seed = oracle.make_seed(*g["seed_xy"], list(g["seed_p"]), float(g["seed_correlation"]))
+    roi = g.get(f"mask_{tag}")
+    got = oracle.propagate(ref, coef, cfg, seed, roi=roi, gradients=oracle.reference_gradient(ref))
+    kept, solves = g[f"counts_{tag}"]
+    assert got["points_computed"] == kept and got["solves"] == solves
+    assert kept > (500 if roi is None else 150)
+    valid = g[f"valid_{tag}"]
+    assert np.array_equal(got["valid"], valid)
+    assert np.array_equal(got["status"][valid], g[f"status_{tag}"][valid])
+    assert np.array_equal(got["iterations"][valid], g[f"iterations_{tag}"][valid])
+    p = np.column_stack([got[k] for k in ("u", "v", "du_dx", "du_dy", "dv_dx", "dv_dy")])
+    assert np.max(np.abs(p[valid] - g[f"p_{tag}"][valid])) <= P_TOL
+    assert np.max(np.abs(got["correlation"][valid] - g[f"correlation_{tag}"][valid])) <= 1e-9
+    step = int(spacing) + 1
+    gh, gw = got["grid_shape"]
+    assert np.array_equal(got["x"], (np.arange(gw * gh) % gw) * float(step))
