@@ -45,6 +45,20 @@ there again; a min-heap on ZNSSD; 4-neighbours up, right, down, left; ROI and ma
 the guess extrapolated with the parent's displacement gradients; strict acceptance (valid,
 Success, ZNSSD < propagation_max_znssd, |guess - result| < s in u and v, all finite).
 
+tests/golden/subset_seed_256.npz holds seed selections on the small workload's pair, without and
+with a ROI (SeedSelector::select_best_seed and generate_candidates,
+src/subset/seed/seed_selector.cpp:146-317, 370-437): candidate pixels inside the ROI and the subset
+margin, a deterministic sample of at most kmeans_sample_limit of them (llround of i * step), seed_count
+k-means centres initialised the same way and moved kmeans_iterations times (nearest centre, lowest
+index on ties), each centre rounded and checked for ROI, margin and texture (the population standard
+deviation of the square window); then per candidate the integer search
+(src/initialization/integer_search.cpp:129-280, 333-432: a coarse scan of the whole image at
+pyramid_scale on the coarse circle, a refinement +-max(pyramid_refinement_radius, ceil(1.5 r)), a
+local scan +-search_radius, the local winner kept when within 0.02 ZNCC) and the subpixel ICGN on the
+clamp-padded raw deformed image (subset_initializer.cpp:152-204, bspline.cpp:302-318, 369-392), and
+the best candidate by ZNSSD (1e-9 tolerance, then the larger displacement).  The generator asserts
+that no decision rests on a near tie, so its numpy summation order cannot change the result.
+
 Run from the repository root:  python tests/golden/make_golden.py
 """
 import math
@@ -553,6 +567,184 @@ def main_propagation():
     print(f"wrote {PROPAGATION_OUT}")
 
 
+SEED_OUT = os.path.join(HERE, "subset_seed_256.npz")
+# integer search: subset radius, search radius, pyramid scale, pyramid refinement radius;
+# seed selection: seed count, k-means iterations, sample limit, max ZNSSD, min texture std,
+# min displacement norm.  The subpixel ICGN uses RADIUS, MAX_ITER and THRESHOLD.
+IS_RADIUS, IS_SEARCH, PYR_SCALE, PYR_REFINE = 10, 20, 4, 4
+SEED_COUNT, KMEANS_ITERS, SAMPLE_LIMIT, SEED_MAX_ZNSSD, MIN_TEXTURE, MIN_NORM = 64, 20, 20000, 0.3, 0.02, 0.0
+TIE = 1e-12
+
+
+def llround_pos(x):
+    return int(math.floor(x + 0.5))
+
+
+def texture_std(ref, x, y):
+    r = IS_RADIUS
+    h, w = ref.shape
+    if x - r < 0 or y - r < 0 or x + r >= w or y + r >= h:
+        return 0.0
+    win = ref[y - r:y + r + 1, x - r:x + r + 1].astype(np.float64)
+    n = win.size
+    mean = win.sum() / n
+    return math.sqrt(max(0.0, (win * win).sum() / n - mean * mean))
+
+
+def seed_candidates(ref, roi):
+    h, w = ref.shape
+    margin = IS_RADIUS      # max(integer-search radius, subpixel radius); no search margin without truncation
+    ok = lambda x, y: margin <= x < w - margin and margin <= y < h - margin
+    ys, xs = np.nonzero(roi)                      # row-major: y outer, x inner
+    keep = (xs >= margin) & (xs < w - margin) & (ys >= margin) & (ys < h - margin)
+    pts = np.column_stack([xs[keep], ys[keep]])
+    if len(pts) > SAMPLE_LIMIT:
+        step = (len(pts) - 1) / (SAMPLE_LIMIT - 1)
+        pts = pts[[min(llround_pos(i * step), len(pts) - 1) for i in range(SAMPLE_LIMIT)]]
+    count = min(SEED_COUNT, len(pts))
+    step = 0.0 if count == 1 else (len(pts) - 1) / (count - 1)
+    centres = pts[[min(llround_pos(i * step), len(pts) - 1) for i in range(count)]].astype(np.float64)
+    px, py = pts[:, 0].astype(np.float64), pts[:, 1].astype(np.float64)
+    for _ in range(KMEANS_ITERS):
+        d2 = (px[:, None] - centres[None, :, 0]) ** 2 + (py[:, None] - centres[None, :, 1]) ** 2
+        best = np.argmin(d2, axis=1)               # the first centre on ties
+        for i in range(count):
+            sel = best == i
+            if sel.any():
+                centres[i] = [px[sel].sum() / sel.sum(), py[sel].sum() / sel.sum()]   # integer sums: exact
+    cands = []
+    for cx, cy in centres:
+        rx, ry = llround_pos(cx), llround_pos(cy)
+        if 0 <= rx < w and 0 <= ry < h and roi[ry, rx] and ok(rx, ry) and texture_std(ref, rx, ry) >= MIN_TEXTURE:
+            cands.append((rx, ry))
+            continue
+        d = (px - cx) ** 2 + (py - cy) ** 2
+        order = np.argsort(d, kind="stable")
+        lim = min(50, len(order))
+        assert lim == len(order) or d[order[lim - 1]] != d[order[lim]], "distance tie at the 50-point cut"
+        tex = [texture_std(ref, int(pts[j, 0]), int(pts[j, 1])) for j in order[:lim]]
+        k = int(np.argmax(tex))
+        assert sum(t == tex[k] for t in tex) == 1, "texture tie among the nearest points"
+        cands.append((int(pts[order[k], 0]), int(pts[order[k], 1])))
+    return np.array(cands, np.int64)
+
+
+def circle(r, step=1):
+    return np.array([(dx, dy) for dy in range(-r, r + 1, step) for dx in range(-r, r + 1, step)
+                     if dx * dx + dy * dy <= r * r], np.int64)
+
+
+def scan(de, cx, cy, offs, fvals, us, vs):
+    """Best (u, v, zncc) over the displacements us x vs in scan order (v outer, u inner), with the
+    second best ZNCC; positions whose subset leaves the image are skipped."""
+    h, w = de.shape
+    r = IS_RADIUS
+    uu, vv = np.meshgrid(us, vs)
+    uu, vv = uu.ravel(), vv.ravel()
+    inb = (cx + uu - r >= 0) & (cy + vv - r >= 0) & (cx + uu + r < w) & (cy + vv + r < h)
+    uu, vv = uu[inb], vv[inb]
+    if uu.size == 0:
+        return None
+    fm = fvals.sum() / len(fvals)
+    fd = fvals - fm
+    fn = (fd * fd).sum()
+    if fn <= EPS:
+        return None
+    g = de[cy + vv[:, None] + offs[None, :, 1], cx + uu[:, None] + offs[None, :, 0]].astype(np.float64)
+    gd = g - (g.sum(axis=1) / g.shape[1])[:, None]
+    dn = (gd * gd).sum(axis=1)
+    z = np.where(dn <= EPS, -np.inf, (gd @ fd) / np.sqrt(fn * np.maximum(dn, EPS)))
+    k = int(np.argmax(z))
+    if not np.isfinite(z[k]):
+        return None
+    rest = np.delete(z, k)
+    second = rest.max() if rest.size else -np.inf
+    assert z[k] - second > TIE, "two integer displacements within 1e-12 ZNCC"
+    return int(uu[k]), int(vv[k]), float(z[k])
+
+
+def integer_search(ref, de, x, y):
+    h, w = ref.shape
+    r = IS_RADIUS
+    if x - r < 0 or y - r < 0 or x + r >= w or y + r >= h:
+        return None
+    full, coarse = circle(r), circle(r, PYR_SCALE)
+    f = ref[y + full[:, 1], x + full[:, 0]].astype(np.float64)
+    fc = ref[y + coarse[:, 1], x + coarse[:, 0]].astype(np.float64)
+    min_u, max_u, min_v, max_v = r - x, w - 1 - r - x, r - y, h - 1 - r - y
+    best = None
+    if min_u <= max_u and min_v <= max_v:
+        c = scan(de, x, y, coarse, fc, np.arange(min_u, max_u + 1, PYR_SCALE), np.arange(min_v, max_v + 1, PYR_SCALE))
+        if c is not None:
+            rr = max(max(PYR_REFINE, math.ceil(1.5 * r)), PYR_SCALE)
+            best = scan(de, x, y, full, f, np.arange(max(min_u, c[0] - rr), min(max_u, c[0] + rr) + 1),
+                        np.arange(max(min_v, c[1] - rr), min(max_v, c[1] + rr) + 1))
+    if IS_SEARCH > 0:
+        local = scan(de, x, y, full, f, np.arange(-IS_SEARCH, IS_SEARCH + 1), np.arange(-IS_SEARCH, IS_SEARCH + 1))
+        if local is not None:
+            if best is not None:
+                assert abs(local[2] + 0.02 - best[2]) > TIE, "local preference decided by a near tie"
+            if best is None or local[2] + 0.02 >= best[2]:
+                best = local
+    return best
+
+
+def select_seed(ref, de, roi):
+    qk = qk_matrix(DEGREE)
+    h, w = ref.shape
+    ys, xs = np.arange(-BORDER, h + BORDER), np.arange(-BORDER, w + BORDER)
+    lazy = de[np.ix_(np.clip(ys, 0, h - 1), np.clip(xs, 0, w - 1))].astype(np.float64)   # clamp padding, no deconvolution
+    cands = seed_candidates(ref, roi)
+    integer = np.full((len(cands), 4), np.nan)      # u, v, zncc, found
+    evals = np.full((len(cands), 9), np.nan)        # p[6], quality, refined, valid
+    best = -1
+    for i, (x, y) in enumerate(cands):
+        it = integer_search(ref, de, int(x), int(y))
+        integer[i] = (np.nan, np.nan, np.nan, 0) if it is None else (it[0], it[1], it[2], 1)
+        if it is None:
+            evals[i, 7:] = (0, 0)
+            continue
+        q, corr, _, st, _ = solve_variant(ref, lazy, qk, float(x), float(y), (float(it[0]), float(it[1])), 0, 1, False)
+        if st == 0 and np.all(np.isfinite(q[:6])) and math.isfinite(corr):
+            evals[i, :6], evals[i, 6], evals[i, 7] = q[:6], corr, 1
+        else:
+            zn = max(0.0, 2.0 * (1.0 - max(-1.0, min(1.0, it[2]))))
+            evals[i, :6], evals[i, 6], evals[i, 7] = (it[0], it[1], 0, 0, 0, 0), zn, 0
+        evals[i, 8] = 1
+        quality, norm = evals[i, 6], math.hypot(evals[i, 0], evals[i, 1])
+        if quality <= SEED_MAX_ZNSSD and norm >= MIN_NORM:
+            if best < 0:
+                best = i
+                continue
+            cur = evals[best, 6]
+            assert abs(abs(quality - cur) - 1e-9) > TIE, "seed ranking decided by a near tie"
+            if quality < cur - 1e-9 or (quality <= cur + 1e-9 and norm > math.hypot(evals[best, 0], evals[best, 1])):
+                best = i
+    return cands, integer, evals, best
+
+
+def main_seed():
+    from traditional_dic_gb300 import synthetic
+    assert (RADIUS, MAX_ITER, THRESHOLD) == (IS_RADIUS, 20, 1e-3)   # the subpixel ICGN settings
+    pair = synthetic.workload(0)
+    ref, de = pair.reference, pair.deformed
+    yy, xx = np.mgrid[:256, :256]
+    rois = {"full": np.ones((256, 256), bool), "roi": (xx - 150) ** 2 + (yy - 110) ** 2 < 70 ** 2}
+    arrays = {"settings": np.array([IS_RADIUS, IS_SEARCH, PYR_SCALE, PYR_REFINE, SEED_COUNT, KMEANS_ITERS,
+                                    SAMPLE_LIMIT, SEED_MAX_ZNSSD, MIN_TEXTURE, MIN_NORM, DEGREE, BORDER, RADIUS,
+                                    MAX_ITER, THRESHOLD])}
+    for tag, roi in rois.items():
+        cands, integer, evals, best = select_seed(ref, de, roi)
+        arrays[f"candidates_{tag}"], arrays[f"integer_{tag}"], arrays[f"evaluations_{tag}"] = cands, integer, evals
+        arrays[f"best_{tag}"] = np.array(best)
+        if tag != "full":
+            arrays[f"mask_{tag}"] = roi
+        print(f"seed {tag}: {len(cands)} candidates, {int(np.nansum(evals[:, 7]))} refined, best {best} at "
+              f"{tuple(cands[best]) if best >= 0 else None}")
+    np.savez_compressed(SEED_OUT, **arrays)
+    print(f"wrote {SEED_OUT}")
+
+
 def main():
     sys.path.insert(0, ROOT)
     import __graft_entry__ as G
@@ -578,6 +770,7 @@ def main():
     main_variants()
     main_masked()
     main_propagation()
+    main_seed()
 
 
 if __name__ == "__main__":

@@ -1,7 +1,8 @@
 """Golden vectors (tests/golden/*.npz, made by tests/golden/make_golden.py from an independent
 numpy transcription of the reference): the C++ oracle (CPU) and the GPU path (GPU) must reproduce
 the B-spline coefficients and the per-POI results of every solver route, full and masked; the
-oracle must reproduce whole heap-order propagations over the grid, with and without a ROI."""
+oracle must reproduce whole heap-order propagations over the grid and the seed selection (k-means
+candidates, integer search, subpixel refinement), with and without a ROI."""
 import os
 
 import numpy as np
@@ -201,3 +202,53 @@ def test_oracle_heap_propagation_matches_golden(oracle, golden, propagation, tag
     step = int(spacing) + 1
     gh, gw = got["grid_shape"]
     assert np.array_equal(got["x"], (np.arange(gw * gh) % gw) * float(step))
+
+
+# ---- seed selection (tests/golden/subset_seed_256.npz) --------------------------------------
+SEED_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "subset_seed_256.npz")
+
+
+@pytest.fixture(scope="module")
+def seed_golden():
+    d = np.load(SEED_FILE)
+    return {k: d[k] for k in d.files}
+
+
+def _seed_config(g, make_default):
+    (is_r, search, pyr_scale, pyr_ref, count, km_iters, limit, max_znssd, min_tex, min_norm, degree, border,
+     radius, max_iter, thr) = g["settings"]
+    cfg = make_default()
+    cfg.is_subset_radius, cfg.is_search_radius, cfg.pyramid_enabled = int(is_r), int(search), 1
+    cfg.pyramid_scale, cfg.pyramid_refinement_radius = int(pyr_scale), int(pyr_ref)
+    cfg.seed_count, cfg.kmeans_iterations, cfg.kmeans_sample_limit = int(count), int(km_iters), int(limit)
+    cfg.seed_max_znssd, cfg.min_texture_std, cfg.min_displacement_norm = float(max_znssd), float(min_tex), float(min_norm)
+    cfg.degree, cfg.border, cfg.subset_radius = int(degree), int(border), int(radius)
+    cfg.sp_enabled, cfg.sp_subset_radius, cfg.sp_max_iterations = 1, int(radius), int(max_iter)
+    cfg.sp_convergence_threshold = float(thr)
+    return cfg
+
+
+@pytest.mark.parametrize("tag", ["full", "roi"])
+def test_oracle_seed_selection_matches_golden(oracle, golden, seed_golden, tag):
+    """SeedSelector::select_best_seed against an independent transcription: the k-means candidate
+    list, every candidate's integer search (displacement and ZNCC), and the chosen seed with its
+    subpixel-refined parameters and ZNSSD."""
+    g = seed_golden
+    cfg = _seed_config(g, oracle.default_config)
+    ref, de = golden["reference"], golden["deformed"]
+    roi = g.get(f"mask_{tag}")
+    seed, cands = oracle.select_seed(ref, de, cfg, roi=roi)
+    want = g[f"candidates_{tag}"]
+    assert len(want) == cfg.seed_count and np.array_equal(cands, want.astype(np.float64))
+    integer = g[f"integer_{tag}"]
+    for (x, y), (u, v, z, found) in zip(want, integer):
+        got = oracle.integer_search(ref, de, cfg, x, y)
+        assert (got is not None) == bool(found)
+        if got is not None:
+            assert (got[0], got[1]) == (u, v) and abs(got[2] - z) <= 1e-12
+    best = int(g[f"best_{tag}"])
+    assert best >= 0 and seed.found
+    ev = g[f"evaluations_{tag}"][best]
+    assert (seed.x, seed.y) == tuple(want[best].astype(np.float64))
+    assert np.max(np.abs(np.array(list(seed.p)) - ev[:6])) <= P_TOL
+    assert abs(seed.correlation - ev[6]) <= 1e-9
