@@ -107,6 +107,9 @@ def lib():
                                                 C.c_int]
             L.orc_integer_search.argtypes = [P, P, C.c_int, C.c_int, C.POINTER(Config), C.c_double, C.c_double,
                                              C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+            L.orc_integer_search_masked.argtypes = [P, P, C.c_int, C.c_int, P, C.POINTER(Config), C.c_double,
+                                                    C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                                    C.POINTER(C.c_double)]
             L.orc_select_seed.argtypes = [P, P, C.c_int, C.c_int, P, C.POINTER(Config), C.POINTER(Seed), P,
                                           C.c_int, C.POINTER(C.c_int)]
             L.orc_subset_compute.argtypes = [P, P, C.c_int, C.c_int, P, C.POINTER(Config), C.POINTER(GridOut),
@@ -297,13 +300,20 @@ def propagate(reference, deformed_coeffs, cfg, seed: Seed, roi=None, gradients=N
     return out
 
 
-def integer_search(reference, deformed, cfg, x, y):
+def integer_search(reference, deformed, cfg, x, y, roi=None):
+    """IntegerSearchInitializer::estimate at (x, y); with ``roi`` the masked search.  Returns
+    (u, v, zncc) or None."""
     cfg = as_config(cfg)
     ref, de = _img(reference), _img(deformed)
     h, w = ref.shape
     u, v, z = C.c_double(), C.c_double(), C.c_double()
-    ok = lib().orc_integer_search(_ptr(ref), _ptr(de), w, h, C.byref(cfg), float(x), float(y),
-                                  C.byref(u), C.byref(v), C.byref(z))
+    if roi is None:
+        ok = lib().orc_integer_search(_ptr(ref), _ptr(de), w, h, C.byref(cfg), float(x), float(y),
+                                      C.byref(u), C.byref(v), C.byref(z))
+    else:
+        r = np.ascontiguousarray(roi != 0, np.uint8)
+        ok = lib().orc_integer_search_masked(_ptr(ref), _ptr(de), w, h, _ptr(r), C.byref(cfg), float(x), float(y),
+                                             C.byref(u), C.byref(v), C.byref(z))
     return (u.value, v.value, z.value) if ok else None
 
 

@@ -1599,6 +1599,11 @@ int orc_integer_search(const float* ref, const float* def, int w, int h, const o
     return integer_search(ref, def, w, h, *cfg, px, py, *u, *v, *zncc) ? 1 : 0;
 }
 
+int orc_integer_search_masked(const float* ref, const float* def, int w, int h, const uint8_t* roi,
+                              const orc_config* cfg, double px, double py, double* u, double* v, double* zncc) {
+    return integer_search(ref, def, w, h, *cfg, px, py, *u, *v, *zncc, roi) ? 1 : 0;
+}
+
 int orc_select_seed(const float* ref, const float* def, int w, int h, const uint8_t* roi, const orc_config* cfg,
                     orc_seed* seed, double* cand_xy, int cand_cap, int* n_candidates) {
     std::vector<std::pair<double, double>> cands;

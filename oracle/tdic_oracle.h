@@ -155,6 +155,10 @@ int orc_propagate_threads(const float* ref, int w, int h, const uint8_t* roi,
 /* integer_search.cpp:333-432 */
 int orc_integer_search(const float* ref, const float* def, int w, int h, const orc_config* cfg,
                        double px, double py, double* u, double* v, double* zncc);
+/* estimate_with_mask_interpolators (integer_search.cpp:447-545) over the ROI `roi` (h x w). */
+int orc_integer_search_masked(const float* ref, const float* def, int w, int h, const uint8_t* roi,
+                              const orc_config* cfg, double px, double py, double* u, double* v,
+                              double* zncc);
 /* seed_selector.cpp:146-317 with sift disabled; candidates (x,y) pairs are written to
  * cand_xy (capacity cand_cap) when non-NULL. */
 int orc_select_seed(const float* ref, const float* def, int w, int h, const uint8_t* roi,

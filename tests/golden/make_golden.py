@@ -45,8 +45,10 @@ there again; a min-heap on ZNSSD; 4-neighbours up, right, down, left; ROI and ma
 the guess extrapolated with the parent's displacement gradients; strict acceptance (valid,
 Success, ZNSSD < propagation_max_znssd, |guess - result| < s in u and v, all finite).
 
-tests/golden/subset_seed_256.npz holds seed selections on the small workload's pair, without and
-with a ROI (SeedSelector::select_best_seed and generate_candidates,
+tests/golden/subset_seed_256.npz holds seed selections on the small workload's pair: without a ROI,
+with a ROI, and with truncated subsets under a notched ROI, where the candidate margin adds the search
+radius and the integer search (integer_search.cpp:447-545) and the refinement are masked
+(SeedSelector::select_best_seed and generate_candidates,
 src/subset/seed/seed_selector.cpp:146-317, 370-437): candidate pixels inside the ROI and the subset
 margin, a deterministic sample of at most kmeans_sample_limit of them (llround of i * step), seed_count
 k-means centres initialised the same way and moved kmeans_iterations times (nearest centre, lowest
@@ -573,6 +575,7 @@ SEED_OUT = os.path.join(HERE, "subset_seed_256.npz")
 # min displacement norm.  The subpixel ICGN uses RADIUS, MAX_ITER and THRESHOLD.
 IS_RADIUS, IS_SEARCH, PYR_SCALE, PYR_REFINE = 10, 20, 4, 4
 SEED_COUNT, KMEANS_ITERS, SAMPLE_LIMIT, SEED_MAX_ZNSSD, MIN_TEXTURE, MIN_NORM = 64, 20, 20000, 0.3, 0.02, 0.0
+MIN_VALID_SAMPLES, MIN_VALID_RATIO = 12, 0.5   # SubsetConfig defaults; the masked ICGN above uses the same
 TIE = 1e-12
 
 
@@ -591,13 +594,25 @@ def texture_std(ref, x, y):
     return math.sqrt(max(0.0, (win * win).sum() / n - mean * mean))
 
 
-def seed_candidates(ref, roi):
+def seed_candidates(ref, roi, truncate=False):
     h, w = ref.shape
-    margin = IS_RADIUS      # max(integer-search radius, subpixel radius); no search margin without truncation
-    ok = lambda x, y: margin <= x < w - margin and margin <= y < h - margin
+    # max(integer-search radius, subpixel radius), plus the search radius with truncated subsets
+    margin = IS_RADIUS + (IS_SEARCH if truncate else 0)
+    full = len(circle(IS_RADIUS))
+
+    def ok(x, y):   # is_candidate_margin_valid (seed_selector.cpp:440-476)
+        if not (margin <= x < w - margin and margin <= y < h - margin):
+            return False
+        if not truncate:
+            return True
+        c = circle(IS_RADIUS)
+        kept = int(roi[y + c[:, 1], x + c[:, 0]].sum())
+        return kept >= max(6, max(MIN_VALID_SAMPLES, math.ceil(MIN_VALID_RATIO * full)))
+
     ys, xs = np.nonzero(roi)                      # row-major: y outer, x inner
     keep = (xs >= margin) & (xs < w - margin) & (ys >= margin) & (ys < h - margin)
     pts = np.column_stack([xs[keep], ys[keep]])
+    assert len(pts), "no candidate point"
     if len(pts) > SAMPLE_LIMIT:
         step = (len(pts) - 1) / (SAMPLE_LIMIT - 1)
         pts = pts[[min(llround_pos(i * step), len(pts) - 1) for i in range(SAMPLE_LIMIT)]]
@@ -663,17 +678,36 @@ def scan(de, cx, cy, offs, fvals, us, vs):
     return int(uu[k]), int(vv[k]), float(z[k])
 
 
-def integer_search(ref, de, x, y):
+def integer_search(ref, de, x, y, roi=None):
+    """estimate_with_interpolators, or estimate_with_mask_interpolators when ``roi`` is given:
+    samples outside the image or the ROI dropped, at least max(12, ceil(half the circle)) kept."""
     h, w = ref.shape
     r = IS_RADIUS
-    if x - r < 0 or y - r < 0 or x + r >= w or y + r >= h:
-        return None
     full, coarse = circle(r), circle(r, PYR_SCALE)
+    if roi is None:
+        if x - r < 0 or y - r < 0 or x + r >= w or y + r >= h:
+            return None
+    else:
+        if not roi[y, x]:
+            return None
+        need = lambda c: max(12, math.ceil(0.5 * len(c)))
+        keep = lambda c: c[(x + c[:, 0] >= 0) & (x + c[:, 0] < w) & (y + c[:, 1] >= 0) & (y + c[:, 1] < h)]
+        full_all, coarse_all = full, coarse
+        full, coarse = keep(full), keep(coarse)
+        full = full[roi[y + full[:, 1], x + full[:, 0]]]
+        coarse = coarse[roi[y + coarse[:, 1], x + coarse[:, 0]]]
+        if len(full) < need(full_all):
+            return None
     f = ref[y + full[:, 1], x + full[:, 0]].astype(np.float64)
     fc = ref[y + coarse[:, 1], x + coarse[:, 0]].astype(np.float64)
     min_u, max_u, min_v, max_v = r - x, w - 1 - r - x, r - y, h - 1 - r - y
     best = None
-    if min_u <= max_u and min_v <= max_v:
+    coarse_ok = roi is None or len(coarse) >= need(coarse_all)
+    if roi is not None:
+        fd = f - f.sum() / len(f)
+        if (fd * fd).sum() <= EPS:
+            return None
+    if min_u <= max_u and min_v <= max_v and coarse_ok:
         c = scan(de, x, y, coarse, fc, np.arange(min_u, max_u + 1, PYR_SCALE), np.arange(min_v, max_v + 1, PYR_SCALE))
         if c is not None:
             rr = max(max(PYR_REFINE, math.ceil(1.5 * r)), PYR_SCALE)
@@ -689,22 +723,23 @@ def integer_search(ref, de, x, y):
     return best
 
 
-def select_seed(ref, de, roi):
+def select_seed(ref, de, roi, truncate=False):
     qk = qk_matrix(DEGREE)
     h, w = ref.shape
     ys, xs = np.arange(-BORDER, h + BORDER), np.arange(-BORDER, w + BORDER)
     lazy = de[np.ix_(np.clip(ys, 0, h - 1), np.clip(xs, 0, w - 1))].astype(np.float64)   # clamp padding, no deconvolution
-    cands = seed_candidates(ref, roi)
+    cands = seed_candidates(ref, roi, truncate)
     integer = np.full((len(cands), 4), np.nan)      # u, v, zncc, found
     evals = np.full((len(cands), 9), np.nan)        # p[6], quality, refined, valid
     best = -1
     for i, (x, y) in enumerate(cands):
-        it = integer_search(ref, de, int(x), int(y))
+        it = integer_search(ref, de, int(x), int(y), roi if truncate else None)
         integer[i] = (np.nan, np.nan, np.nan, 0) if it is None else (it[0], it[1], it[2], 1)
         if it is None:
             evals[i, 7:] = (0, 0)
             continue
-        q, corr, _, st, _ = solve_variant(ref, lazy, qk, float(x), float(y), (float(it[0]), float(it[1])), 0, 1, False)
+        q, corr, _, st, _ = solve_variant(ref, lazy, qk, float(x), float(y), (float(it[0]), float(it[1])), 0, 1, False,
+                                          roi=roi if truncate else None)
         if st == 0 and np.all(np.isfinite(q[:6])) and math.isfinite(corr):
             evals[i, :6], evals[i, 6], evals[i, 7] = q[:6], corr, 1
         else:
@@ -729,12 +764,14 @@ def main_seed():
     pair = synthetic.workload(0)
     ref, de = pair.reference, pair.deformed
     yy, xx = np.mgrid[:256, :256]
-    rois = {"full": np.ones((256, 256), bool), "roi": (xx - 150) ** 2 + (yy - 110) ** 2 < 70 ** 2}
+    rois = {"full": np.ones((256, 256), bool), "roi": (xx - 150) ** 2 + (yy - 110) ** 2 < 70 ** 2,
+            # truncated subsets: masked integer search and refinement, margin radius + search radius
+            "truncated": ((xx - 128) ** 2 + (yy - 128) ** 2 < 95 ** 2) & ~((xx > 100) & (xx < 108))}
     arrays = {"settings": np.array([IS_RADIUS, IS_SEARCH, PYR_SCALE, PYR_REFINE, SEED_COUNT, KMEANS_ITERS,
                                     SAMPLE_LIMIT, SEED_MAX_ZNSSD, MIN_TEXTURE, MIN_NORM, DEGREE, BORDER, RADIUS,
                                     MAX_ITER, THRESHOLD])}
     for tag, roi in rois.items():
-        cands, integer, evals, best = select_seed(ref, de, roi)
+        cands, integer, evals, best = select_seed(ref, de, roi, truncate=tag == "truncated")
         arrays[f"candidates_{tag}"], arrays[f"integer_{tag}"], arrays[f"evaluations_{tag}"] = cands, integer, evals
         arrays[f"best_{tag}"] = np.array(best)
         if tag != "full":

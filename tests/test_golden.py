@@ -228,13 +228,16 @@ def _seed_config(g, make_default):
     return cfg
 
 
-@pytest.mark.parametrize("tag", ["full", "roi"])
+@pytest.mark.parametrize("tag", ["full", "roi", "truncated"])
 def test_oracle_seed_selection_matches_golden(oracle, golden, seed_golden, tag):
     """SeedSelector::select_best_seed against an independent transcription: the k-means candidate
     list, every candidate's integer search (displacement and ZNCC), and the chosen seed with its
-    subpixel-refined parameters and ZNSSD."""
+    subpixel-refined parameters and ZNSSD.  "truncated": truncate_roi_subsets, so the candidate
+    margin includes the search radius, and both the integer search and the refinement are masked
+    by the ROI (17 of the 64 candidates' subsets cross its edge)."""
     g = seed_golden
     cfg = _seed_config(g, oracle.default_config)
+    cfg.truncate_roi_subsets = int(tag == "truncated")
     ref, de = golden["reference"], golden["deformed"]
     roi = g.get(f"mask_{tag}")
     seed, cands = oracle.select_seed(ref, de, cfg, roi=roi)
@@ -242,7 +245,7 @@ def test_oracle_seed_selection_matches_golden(oracle, golden, seed_golden, tag):
     assert len(want) == cfg.seed_count and np.array_equal(cands, want.astype(np.float64))
     integer = g[f"integer_{tag}"]
     for (x, y), (u, v, z, found) in zip(want, integer):
-        got = oracle.integer_search(ref, de, cfg, x, y)
+        got = oracle.integer_search(ref, de, cfg, x, y, roi=roi if cfg.truncate_roi_subsets else None)
         assert (got is not None) == bool(found)
         if got is not None:
             assert (got[0], got[1]) == (u, v) and abs(got[2] - z) <= 1e-12
