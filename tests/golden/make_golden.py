@@ -58,7 +58,12 @@ deviation of the square window); then per candidate the integer search
 pyramid_scale on the coarse circle, a refinement +-max(pyramid_refinement_radius, ceil(1.5 r)), a
 local scan +-search_radius, the local winner kept when within 0.02 ZNCC) and the subpixel ICGN on the
 clamp-padded raw deformed image (subset_initializer.cpp:152-204, bspline.cpp:302-318, 369-392), and
-the best candidate by ZNSSD (1e-9 tolerance, then the larger displacement).  The generator asserts
+the best candidate by ZNSSD (1e-9 tolerance, then the larger displacement).
+
+tests/golden/subset_truncated_256.npz holds SubsetDIC::compute with truncate_roi_subsets
+(subset_dic.cpp:39-105, padding.cpp:11-90): both images mirror-padded and the ROI zero-padded by
+recommended_subset_padding, the seed selected and the grid propagated (heap order, masked subsets) on
+the padded images, and the grid points inside the original image returned shifted back.  The generator asserts
 that no decision rests on a near tie, so its numpy summation order cannot change the result.
 
 Run from the repository root:  python tests/golden/make_golden.py
@@ -475,10 +480,11 @@ def round_half_away(x):
     return int(math.copysign(math.floor(abs(x) + 0.5), x))
 
 
-def propagate_heap(ref, coef, qk, seed_xy, seed_p, seed_corr, roi=None):
-    """ReliabilityPropagation::propagate with one seed and the first-order ZNSSD ICGN.  Returns the
-    grid arrays (p, correlation, valid, status, iterations; defaults where no result was kept), the
-    number of points kept and the number of solves."""
+def propagate_heap(ref, coef, qk, seed_xy, seed_p, seed_corr, roi=None, masked=False):
+    """ReliabilityPropagation::propagate with one seed and the first-order ZNSSD ICGN (masked by
+    ``roi`` when ``masked``: solve_with_mask).  Returns the grid arrays (p, correlation, valid,
+    status, iterations; defaults where no result was kept), the number of points kept and the
+    number of solves."""
     h, w = ref.shape
     step = SPACING + 1
     gw, gh = -(-w // step), -(-h // step)
@@ -487,7 +493,8 @@ def propagate_heap(ref, coef, qk, seed_xy, seed_p, seed_corr, roi=None):
     valid, status, iters = np.zeros(n, bool), np.full(n, -1, np.int64), np.zeros(n, np.int64)
     calc = np.zeros(n, bool)
     roi_ok = (lambda x, y: True) if roi is None else (lambda x, y: bool(roi[y, x]))
-    solve = lambda x, y, p0: solve_variant(ref, coef, qk, float(x), float(y), np.asarray(p0, np.float64), 0, 1, False)
+    solve = lambda x, y, p0: solve_variant(ref, coef, qk, float(x), float(y), np.asarray(p0, np.float64), 0, 1, False,
+                                           roi=roi if masked else None)
     sxr, syr = round_half_away(seed_xy[0]), round_half_away(seed_xy[1])
     if not (0 <= sxr < w and 0 <= syr < h) or not roi_ok(sxr, syr):
         return p_out, corr_out, valid, status, iters, 0, 0
@@ -782,6 +789,68 @@ def main_seed():
     print(f"wrote {SEED_OUT}")
 
 
+TRUNCATED_OUT = os.path.join(HERE, "subset_truncated_256.npz")
+
+
+def mirror_index(i, n):
+    """padding.cpp:11-24."""
+    if n <= 1:
+        return 0
+    while i < 0 or i >= n:
+        i = -i - 1 if i < 0 else 2 * n - i - 1
+    return i
+
+
+def subset_compute_truncated(ref, de, roi):
+    """SubsetDIC::compute with truncate_roi_subsets (subset_dic.cpp:39-105): images mirror-padded
+    and the ROI zero-padded by recommended_subset_padding (padding.cpp:28-36), the seed selected and
+    the grid propagated on the padded images with masked subsets, then the grid points inside the
+    original image returned, shifted back by the padding."""
+    h, w = ref.shape
+    pad = IS_SEARCH + max(RADIUS, IS_RADIUS, RADIUS) + BORDER
+    ys = [mirror_index(y - pad, h) for y in range(h + 2 * pad)]
+    xs = [mirror_index(x - pad, w) for x in range(w + 2 * pad)]
+    pref, pdef = ref[np.ix_(ys, xs)], de[np.ix_(ys, xs)]
+    proi = np.zeros((h + 2 * pad, w + 2 * pad), bool)
+    proi[pad:pad + h, pad:pad + w] = roi
+    cands, _, evals, best = select_seed(pref, pdef, proi, truncate=True)
+    assert best >= 0, "no seed"
+    seed_xy, seed_p, seed_corr = cands[best].astype(np.float64), evals[best, :6], evals[best, 6]
+    coef = coefficients(pdef, DEGREE, BORDER)
+    p, c, val, st, it, kept, solves = propagate_heap(pref, coef, qk_matrix(DEGREE), seed_xy, seed_p, seed_corr,
+                                                      roi=proi, masked=True)
+    assert kept > 0
+    step = SPACING + 1
+    gw = -(-(w + 2 * pad) // step)
+    n = len(val)
+    gx, gy = (np.arange(n) % gw) * step - pad, (np.arange(n) // gw) * step - pad
+    inside = (gx >= 0) & (gy >= 0) & (gx < w) & (gy < h)
+    return dict(x=gx[inside].astype(np.float64), y=gy[inside].astype(np.float64), p=p[inside], correlation=c[inside],
+                valid=val[inside], iterations=it[inside], seed=np.concatenate([seed_xy, seed_p, [seed_corr]]),
+                counts=np.array([kept, solves, pad]))
+
+
+def main_truncated():
+    from traditional_dic_gb300 import synthetic
+    pair = synthetic.workload(0)
+    ref, de = pair.reference, pair.deformed
+    yy, xx = np.mgrid[:256, :256]
+    rois = {"full": np.ones((256, 256), bool),
+            "roi": ((xx - 140) ** 2 + (yy - 120) ** 2 < 110 ** 2) & ~((xx > 40) & (xx < 52) & (yy > 100))}
+    arrays = {}
+    for tag, roi in rois.items():
+        out = subset_compute_truncated(ref, de, roi)
+        for k, v in out.items():
+            arrays[f"{k}_{tag}"] = v
+        if tag != "full":
+            arrays[f"mask_{tag}"] = roi
+        edge = (out["x"] < RADIUS) | (out["y"] < RADIUS) | (out["x"] >= 256 - RADIUS) | (out["y"] >= 256 - RADIUS)
+        print(f"truncated {tag}: {len(out['x'])} points, {int(out['valid'].sum())} valid, "
+              f"{int(out['valid'][edge].sum())} valid within a radius of the image edge; kept/solves/pad {out['counts']}")
+    np.savez_compressed(TRUNCATED_OUT, **arrays)
+    print(f"wrote {TRUNCATED_OUT}")
+
+
 def main():
     sys.path.insert(0, ROOT)
     import __graft_entry__ as G
@@ -808,6 +877,7 @@ def main():
     main_masked()
     main_propagation()
     main_seed()
+    main_truncated()
 
 
 if __name__ == "__main__":

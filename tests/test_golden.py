@@ -2,7 +2,8 @@
 numpy transcription of the reference): the C++ oracle (CPU) and the GPU path (GPU) must reproduce
 the B-spline coefficients and the per-POI results of every solver route, full and masked; the
 oracle must reproduce whole heap-order propagations over the grid and the seed selection (k-means
-candidates, integer search, subpixel refinement), with and without a ROI."""
+candidates, integer search, subpixel refinement), with and without a ROI, and the whole
+SubsetDIC::compute with truncated subsets over padded images."""
 import os
 
 import numpy as np
@@ -255,3 +256,43 @@ def test_oracle_seed_selection_matches_golden(oracle, golden, seed_golden, tag):
     assert (seed.x, seed.y) == tuple(want[best].astype(np.float64))
     assert np.max(np.abs(np.array(list(seed.p)) - ev[:6])) <= P_TOL
     assert abs(seed.correlation - ev[6]) <= 1e-9
+
+
+# ---- SubsetDIC::compute with truncated subsets (tests/golden/subset_truncated_256.npz) -------
+TRUNCATED_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "subset_truncated_256.npz")
+
+
+@pytest.fixture(scope="module")
+def truncated_golden():
+    d = np.load(TRUNCATED_FILE)
+    return {k: d[k] for k in d.files}
+
+
+@pytest.mark.parametrize("tag", ["full", "roi"])
+def test_oracle_truncated_compute_matches_golden(oracle, golden, truncated_golden, tag):
+    """SubsetDIC::compute with truncate_roi_subsets against an independent transcription: mirror
+    padding, seed selection and heap-order propagation with masked subsets on the padded images,
+    the grid cropped to the image and shifted back.  Same points, flags and iteration counts;
+    parameters to FP64 agreement; the seed in image coordinates."""
+    import __graft_entry__ as G
+    from traditional_dic_gb300 import subset as S
+    g = truncated_golden
+    cfg = oracle.as_config(S.config_from_dict(G.WORKLOAD0_CONFIG))
+    cfg.truncate_roi_subsets, cfg.propagation_mode = 1, 1
+    roi = g.get(f"mask_{tag}")
+    got = oracle.subset_compute(golden["reference"], golden["deformed"], cfg, roi=roi)
+    kept, solves, pad = g[f"counts_{tag}"]
+    assert pad == oracle.subset_padding(cfg)
+    assert np.array_equal(got["x"], g[f"x_{tag}"]) and np.array_equal(got["y"], g[f"y_{tag}"])
+    valid = g[f"valid_{tag}"]
+    assert np.array_equal(got["valid"], valid) and valid.sum() == kept
+    assert np.array_equal(got["iterations"][valid], g[f"iterations_{tag}"][valid])
+    p = np.column_stack([got[k] for k in ("u", "v", "du_dx", "du_dy", "dv_dx", "dv_dy")])
+    assert np.max(np.abs(p[valid] - g[f"p_{tag}"][valid])) <= P_TOL
+    assert np.max(np.abs(got["correlation"][valid] - g[f"correlation_{tag}"][valid])) <= 1e-9
+    seed = g[f"seed_{tag}"]
+    assert (got["seed"].x, got["seed"].y) == (seed[0] - pad, seed[1] - pad)
+    assert np.max(np.abs(np.array(list(got["seed"].p)) - seed[2:8])) <= P_TOL
+    if tag == "full":   # points whose full subset would leave the image are solved
+        edge = (got["x"] < 10) | (got["y"] < 10) | (got["x"] >= 246) | (got["y"] >= 246)
+        assert valid[edge].sum() > 50
