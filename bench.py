@@ -273,9 +273,10 @@ def cpu_baselines(reference, deformed, cfg, seed, ref_solves: int, threads: int 
             legs.append({"value": None, "unit": UNIT, "cores": n_threads, "kind": "port", "error": repr(e)})
             continue
         conv = int(np.sum(rr["valid"] & rr["converged"]))
-        what = ("the whole 2048^2 workload, dataflow order" if max_solves < 0 and mode == 2 else
+        size = "x".join(str(n) for n in reversed(np.shape(reference)))
+        what = (f"the whole {size} workload, dataflow order" if max_solves < 0 and mode == 2 else
                 f"first {rr['solves']} {'heap-order' if mode == 1 else 'dataflow-order'} solves of the same "
-                f"2048^2 workload")
+                f"{size} workload")
         legs.append({"value": conv / dt, "unit": UNIT, "cores": n_threads, "kind": "port",
                      "sample": f"{what}: {rr['solves']} solves, {conv} converged in {dt:.1f} s "
                                f"(FP64 C++ port of the reference path, {n_threads} thread"

@@ -58,3 +58,20 @@ def test_two_replicas_on_gloo(oracle):
     assert abs(u[0] - 0.3) < 0.02 and abs(u[1] - 0.4) < 0.02       # each rank solved its own job
     assert all(out[r][1] == max(u) for r in range(world))           # max over ranks
     assert all(out[r][2] == 2.0 for r in range(world))              # sum over ranks
+
+
+def test_cpu_baseline_legs(oracle, workload0):
+    """bench.py's CPU baselines on the small workload: the threaded dataflow leg over the whole
+    grid and the one-thread heap-order leg on a prefix, each a complete cpu_baseline object."""
+    import __graft_entry__ as G
+    import bench
+    from traditional_dic_gb300 import subset as S
+    cfg = S.config_from_dict(G.WORKLOAD0_CONFIG)
+    seed, _ = oracle.select_seed(workload0.reference, workload0.deformed, oracle.as_config(cfg))
+    par, ser = bench.cpu_baselines(workload0.reference, workload0.deformed, cfg, seed, 100, threads=4)
+    for leg, cores in ((par, 4), (ser, 1)):
+        assert "error" not in leg, leg
+        assert leg["value"] > 0 and leg["unit"] == bench.UNIT and leg["cores"] == cores and leg["kind"] == "port"
+        assert leg["sample"]
+    assert "whole 256x256 workload" in par["sample"] and "576 solves" in par["sample"]
+    assert "first 100 heap-order solves of the same 256x256 workload" in ser["sample"]
