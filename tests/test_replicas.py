@@ -1,7 +1,8 @@
 """The multi-GPU mode of bench.py runs independent replicas (the propagation does not shard:
 each image pair's grid depends on its own seed chain).  Its host-side harness - process group,
 barrier, max / sum over ranks - is checked here with two gloo ranks on the CPU, each solving
-its own small job with the oracle."""
+its own small job with the oracle.  The CPU-baseline legs that bench.py adds to its line run here
+too, on the small workload."""
 import os
 import socket
 import sys

@@ -56,6 +56,12 @@ class Context:
             self.lib.tdic_ctx_destroy(self.handle)
             self.handle = None
 
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
     def __del__(self):
         try:
             self.close()
@@ -148,6 +154,12 @@ class Pair:
         if getattr(self, "handle", None):
             self.ctx.lib.tdic_pair_destroy(self.handle)
             self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
     def __del__(self):
         try:
@@ -566,6 +578,12 @@ class Batch:
         if getattr(self, "handle", None):
             self.ctx.lib.tdic_batch_destroy(self.handle)
             self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
     def __del__(self):
         try:
