@@ -76,3 +76,18 @@ def test_cpu_baseline_legs(oracle, workload0):
         assert leg["sample"]
     assert "whole 256x256 workload" in par["sample"] and "576 solves" in par["sample"]
     assert "first 100 heap-order solves of the same 256x256 workload" in ser["sample"]
+
+
+def test_route_comparison_counts_converged_points_apart():
+    """bench.py --routes compares the FP32-mixed and FP64 builds over the jointly valid points
+    and, separately, over the points both converged on strictly."""
+    import bench
+    valid = np.array([1, 1, 1, 1, 0], bool)
+    strict = np.array([1, 1, 0, 0, 0], bool)
+    u64 = np.zeros(5)
+    u32 = np.array([1e-4, -2e-4, 0.05, 0.0, 9.0])
+    got = bench.compare_builds((valid, u32, np.zeros(5), strict), (valid, u64, np.zeros(5), strict))
+    assert got["flag_agreement"] == 1.0
+    assert got["within_1e-3_px"] == 0.75 and got["within_1e-3_px_converged"] == 1.0
+    none = bench.compare_builds((valid & False, u32, u64, strict), (valid, u64, u64, strict & False))
+    assert none["within_1e-3_px"] is None and none["within_1e-3_px_converged"] is None
