@@ -39,7 +39,8 @@ convergence on the norm before the cap).
 
 tests/golden/subset_propagation_256.npz holds whole propagations over the small workload's grid
 (ReliabilityPropagation::propagate, src/subset/seed/reliability_propagation.cpp:130-394) with the
-first-order ZNSSD ICGN above, without and with a ROI: grid ceil(W/s) x ceil(H/s) for s = spacing
+first-order ZNSSD ICGN above, without and with a ROI, and over the full grid with the FGN and with
+the second-order ICGN (the guesses carry the six first-order parameters): grid ceil(W/s) x ceil(H/s) for s = spacing
 + 1; the seed rounded (std::round), moved to the nearest grid point (llround, clamped) and solved
 there again; a min-heap on ZNSSD; 4-neighbours up, right, down, left; ROI and margin admission;
 the guess extrapolated with the parent's displacement gradients; strict acceptance (valid,
@@ -480,21 +481,21 @@ def round_half_away(x):
     return int(math.copysign(math.floor(abs(x) + 0.5), x))
 
 
-def propagate_heap(ref, coef, qk, seed_xy, seed_p, seed_corr, roi=None, masked=False):
+def propagate_heap(ref, coef, qk, seed_xy, seed_p, seed_corr, roi=None, masked=False, optimizer=0, order=1):
     """ReliabilityPropagation::propagate with one seed and the first-order ZNSSD ICGN (masked by
-    ``roi`` when ``masked``: solve_with_mask).  Returns the grid arrays (p, correlation, valid,
-    status, iterations; defaults where no result was kept), the number of points kept and the
-    number of solves."""
+    ``roi`` when ``masked``: solve_with_mask).  Returns the grid arrays (p: the six first-order
+    then the six second-order parameters; correlation, valid, status, iterations; defaults where
+    no result was kept), the number of points kept and the number of solves."""
     h, w = ref.shape
     step = SPACING + 1
     gw, gh = -(-w // step), -(-h // step)
     n = gw * gh
-    p_out, corr_out = np.zeros((n, 6)), np.zeros(n)
+    p_out, corr_out = np.zeros((n, 12)), np.zeros(n)
     valid, status, iters = np.zeros(n, bool), np.full(n, -1, np.int64), np.zeros(n, np.int64)
     calc = np.zeros(n, bool)
     roi_ok = (lambda x, y: True) if roi is None else (lambda x, y: bool(roi[y, x]))
-    solve = lambda x, y, p0: solve_variant(ref, coef, qk, float(x), float(y), np.asarray(p0, np.float64), 0, 1, False,
-                                           roi=roi if masked else None)
+    solve = lambda x, y, p0: solve_variant(ref, coef, qk, float(x), float(y), np.asarray(p0, np.float64), optimizer,
+                                           order, False, roi=roi if masked else None)
     sxr, syr = round_half_away(seed_xy[0]), round_half_away(seed_xy[1])
     if not (0 <= sxr < w and 0 <= syr < h) or not roi_ok(sxr, syr):
         return p_out, corr_out, valid, status, iters, 0, 0
@@ -505,12 +506,12 @@ def propagate_heap(ref, coef, qk, seed_xy, seed_p, seed_corr, roi=None, masked=F
         return p_out, corr_out, valid, status, iters, 0, 0
     sidx = gys * gw + gxs
     solves = 0
-    sp, scorr, sit = np.asarray(seed_p, np.float64), float(seed_corr), 0
+    sp, scorr, sit = np.concatenate([np.asarray(seed_p, np.float64), np.zeros(6)]), float(seed_corr), 0
     if (sx, sy) != (sxr, syr):
         q, scorr, sit, st, _ = solve(sx, sy, seed_p)
         solves += 1
-        sp = q[:6]
-        if st != 0 or not (np.all(np.isfinite(sp)) and math.isfinite(scorr)):
+        sp = q[:12]
+        if st != 0 or not (np.all(np.isfinite(sp[:6])) and math.isfinite(scorr)):
             return p_out, corr_out, valid, status, iters, 0, solves
     calc[sidx] = True
     p_out[sidx], corr_out[sidx], valid[sidx], status[sidx], iters[sidx] = sp, scorr, True, 0, sit
@@ -541,7 +542,7 @@ def propagate_heap(ref, coef, qk, seed_xy, seed_p, seed_corr, roi=None, masked=F
             r = q[:6]
             if (st == 0 and c < MAX_ZNSSD and abs(p0[0] - r[0]) < step and abs(p0[1] - r[1]) < step
                     and np.all(np.isfinite(r)) and math.isfinite(c)):
-                p_out[nidx], corr_out[nidx], valid[nidx], status[nidx], iters[nidx] = r, c, True, st, it
+                p_out[nidx], corr_out[nidx], valid[nidx], status[nidx], iters[nidx] = q[:12], c, True, st, it
                 kept += 1
                 # the heap order of equal keys is implementation-defined in std::priority_queue
                 assert c not in keys, "two equal ZNSSD keys: the visit order would be ambiguous"
@@ -564,8 +565,12 @@ def main_propagation():
     rois = {"full": None, "roi": ((xx - 120) ** 2 + (yy - 140) ** 2 < 90 ** 2) & ~((xx > 60) & (xx < 75))}
     arrays = {"seed_xy": np.array(seed_xy), "seed_p": seed_p, "seed_correlation": np.array(0.0),
               "settings": np.array([DEGREE, BORDER, RADIUS, MAX_ITER, THRESHOLD, SPACING, MAX_ZNSSD])}
-    for tag, roi in rois.items():
-        p, c, val, st, it, kept, solves = propagate_heap(ref, coef, qk, seed_xy, seed_p, 0.0, roi)
+    # the full grid again with the FGN solver and with the second-order ICGN (ZNSSD both): the
+    # guesses carry the six first-order parameters, the second-order terms start at zero
+    runs = [(tag, roi, 0, 1) for tag, roi in rois.items()] + [("fgn", None, 1, 1), ("icgn2", None, 0, 2)]
+    for tag, roi, opt, order in runs:
+        p, c, val, st, it, kept, solves = propagate_heap(ref, coef, qk, seed_xy, seed_p, 0.0, roi, optimizer=opt,
+                                                         order=order)
         arrays[f"p_{tag}"], arrays[f"correlation_{tag}"], arrays[f"valid_{tag}"] = p, c, val
         arrays[f"status_{tag}"], arrays[f"iterations_{tag}"] = st, it
         arrays[f"counts_{tag}"] = np.array([kept, solves])

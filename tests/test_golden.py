@@ -174,16 +174,17 @@ def propagation():
     return {k: d[k] for k in d.files}
 
 
-@pytest.mark.parametrize("tag", ["full", "roi"])
-def test_oracle_heap_propagation_matches_golden(oracle, golden, propagation, tag):
+@pytest.mark.parametrize("tag,opt,order", [("full", 0, 1), ("roi", 0, 1), ("fgn", 1, 1), ("icgn2", 0, 2)])
+def test_oracle_heap_propagation_matches_golden(oracle, golden, propagation, tag, opt, order):
     """The oracle's reliability-guided propagation in the reference's heap order against an
     independent transcription of ReliabilityPropagation::propagate: the same points solved and
-    kept, the same flags and iteration counts, and the kept results to FP64 agreement."""
+    kept, the same flags and iteration counts, and the kept results to FP64 agreement.  ICGN over
+    the full grid and under a ROI, FGN and second-order ICGN over the full grid."""
     g = propagation
     degree, border, radius, max_iter, thr, spacing, max_znssd = g["settings"]
     cfg = oracle.default_config()
     cfg.subset_radius, cfg.max_iterations, cfg.convergence_threshold = int(radius), int(max_iter), float(thr)
-    cfg.degree, cfg.border, cfg.optimizer, cfg.shape_order, cfg.criterion = int(degree), int(border), 0, 1, 1
+    cfg.degree, cfg.border, cfg.optimizer, cfg.shape_order, cfg.criterion = int(degree), int(border), opt, order, 1
     cfg.propagation_spacing, cfg.propagation_max_znssd, cfg.propagation_mode = int(spacing), float(max_znssd), 1
     ref = golden["reference"].astype(np.float32)
     coef = oracle.prefilter(golden["deformed"].astype(np.float32), int(degree), int(border), True)
@@ -193,13 +194,17 @@ def test_oracle_heap_propagation_matches_golden(oracle, golden, propagation, tag
     kept, solves = g[f"counts_{tag}"]
     assert got["points_computed"] == kept and got["solves"] == solves
     assert kept > (500 if roi is None else 150)
+    assert (roi is None) == (f"mask_{tag}" not in g)
     valid = g[f"valid_{tag}"]
     assert np.array_equal(got["valid"], valid)
     assert np.array_equal(got["status"][valid], g[f"status_{tag}"][valid])
     assert np.array_equal(got["iterations"][valid], g[f"iterations_{tag}"][valid])
-    p = np.column_stack([got[k] for k in ("u", "v", "du_dx", "du_dy", "dv_dx", "dv_dy")])
+    p = np.column_stack([got[k] for k in ("u", "v", "du_dx", "du_dy", "dv_dx", "dv_dy", "d2u_dx2", "d2u_dxdy",
+                                          "d2u_dy2", "d2v_dx2", "d2v_dxdy", "d2v_dy2")])
     assert np.max(np.abs(p[valid] - g[f"p_{tag}"][valid])) <= P_TOL
     assert np.max(np.abs(got["correlation"][valid] - g[f"correlation_{tag}"][valid])) <= 1e-9
+    if order == 2:
+        assert np.abs(g[f"p_{tag}"][valid, 6:]).max() > 1e-6   # the curvature terms are exercised
     step = int(spacing) + 1
     gh, gw = got["grid_shape"]
     assert np.array_equal(got["x"], (np.arange(gw * gh) % gw) * float(step))
@@ -288,7 +293,7 @@ def test_oracle_truncated_compute_matches_golden(oracle, golden, truncated_golde
     assert np.array_equal(got["valid"], valid) and valid.sum() == kept
     assert np.array_equal(got["iterations"][valid], g[f"iterations_{tag}"][valid])
     p = np.column_stack([got[k] for k in ("u", "v", "du_dx", "du_dy", "dv_dx", "dv_dy")])
-    assert np.max(np.abs(p[valid] - g[f"p_{tag}"][valid])) <= P_TOL
+    assert np.max(np.abs(p[valid] - g[f"p_{tag}"][valid, :6])) <= P_TOL
     assert np.max(np.abs(got["correlation"][valid] - g[f"correlation_{tag}"][valid])) <= 1e-9
     seed = g[f"seed_{tag}"]
     assert (got["seed"].x, got["seed"].y) == (seed[0] - pad, seed[1] - pad)
