@@ -107,3 +107,44 @@ def test_gpu_strain_of_a_subset_result(gpu_ctx, workload0, tmp_path):
     P.save_least_squares_strain_csv(tmp_path / "strain.csv", pts, disp, radius=25.0, context=gpu_ctx)
     rows = list(csv.reader(open(tmp_path / "strain.csv")))
     assert rows[0][:3] == ["x", "y", "du_dx"] and len(rows) == len(pts) + 1
+
+
+def test_oracle_matches_a_brute_force_transcription():
+    """compute_least_squares_strain_2d (least_squares_strain.cpp:11-78) restated without buckets:
+    every finite point's neighbours within the radius (inclusive) by brute force, the [1, dx, dy]
+    fit by numpy's least squares, small and Green-Lagrange strains.  Scattered points, a quadratic
+    field (the fit is not exact), points with NaN coordinates or displacements, and neighbourhoods
+    below min_samples."""
+    rng = np.random.default_rng(21)
+    n = 400
+    pts = rng.uniform(0, 120, (n, 2))
+    pts[::37, 0] = np.nan
+    disp = np.column_stack([0.3 + 0.01 * pts[:, 0] - 2e-4 * pts[:, 1] ** 2,
+                            -0.2 + 3e-4 * pts[:, 0] * pts[:, 1] + 0.004 * pts[:, 1]])
+    disp[5::41, 1] = np.nan
+    radius, min_samples = 9.5, 6
+    for gl in (True, False):
+        got = SO.least_squares_strain_2d(pts, disp, radius, min_samples, gl)
+        finite = np.all(np.isfinite(pts), axis=1) & np.all(np.isfinite(disp), axis=1)
+        for i in range(n):
+            if not finite[i]:
+                assert got["sample_count"][i] == 0 and not got["valid"][i]
+                continue
+            d2 = np.sum((pts - pts[i]) ** 2, axis=1)
+            ids = np.nonzero(finite & (d2 <= radius * radius))[0]
+            assert got["sample_count"][i] == len(ids)
+            if len(ids) < min_samples:
+                assert not got["valid"][i]
+                continue
+            a = np.column_stack([np.ones(len(ids)), pts[ids, 0] - pts[i, 0], pts[ids, 1] - pts[i, 1]])
+            assert np.linalg.matrix_rank(a) == 3
+            au = np.linalg.lstsq(a, disp[ids, 0], rcond=None)[0]
+            av = np.linalg.lstsq(a, disp[ids, 1], rcond=None)[0]
+            h = np.array([[au[1], au[2]], [av[1], av[2]]])
+            e = 0.5 * (h + h.T + h.T @ h) if gl else np.array([[h[0, 0], 0.5 * (h[0, 1] + h[1, 0])],
+                                                             [0.5 * (h[0, 1] + h[1, 0]), h[1, 1]]])
+            assert got["valid"][i]
+            want = (h[0, 0], h[0, 1], h[1, 0], h[1, 1], e[0, 0], e[1, 1], e[0, 1])
+            for k, w in zip(("du_dx", "du_dy", "dv_dx", "dv_dy", "exx", "eyy", "exy"), want):
+                assert abs(got[k][i] - w) <= 1e-11, (i, k)
+        assert got["valid"].sum() > 250 and (~got["valid"] & finite).sum() > 0
