@@ -61,6 +61,10 @@ local scan +-search_radius, the local winner kept when within 0.02 ZNCC) and the
 clamp-padded raw deformed image (subset_initializer.cpp:152-204, bspline.cpp:302-318, 369-392), and
 the best candidate by ZNSSD (1e-9 tolerance, then the larger displacement).
 
+tests/golden/subset_degree5_256.npz holds the quintic spline (degree 5, the reference's default):
+coefficients and the first-order ZNSSD ICGN and FGN, second-order ZNSSD ICGN and second-order SSD
+FGN on the POIs above.
+
 tests/golden/subset_truncated_256.npz holds SubsetDIC::compute with truncate_roi_subsets
 (subset_dic.cpp:39-105, padding.cpp:11-90): both images mirror-padded and the ROI zero-padded by
 recommended_subset_padding, the seed selected and the grid propagated (heap order, masked subsets) on
@@ -289,7 +293,7 @@ def sd_rows(a, b, lx, ly, order):
     return np.column_stack(cols)
 
 
-def solve_variant(ref, coef, qk, px, py, p0, optimizer, order, ssd, roi=None):
+def solve_variant(ref, coef, qk, px, py, p0, optimizer, order, ssd, roi=None, degree=DEGREE):
     """(p[12], correlation, iterations, status, converged) of one POI on one solver route;
     roi: the masked route over that mask."""
     h, w = ref.shape
@@ -346,7 +350,7 @@ def solve_variant(ref, coef, qk, px, py, p0, optimizer, order, ssd, roi=None):
             wy = wy + p[9] * m[3] + p[10] * m[4] + p[11] * m[5]
         if np.any((wx < 0) | (wy < 0) | (wx > w - 1) | (wy > h - 1)):
             return out(2, corr, it, False)
-        g = spline_values(coef, qk, wx, wy, w, h, DEGREE, BORDER)
+        g = spline_values(coef, qk, wx, wy, w, h, degree, BORDER)
         if ssd:
             diff = f - g
         else:
@@ -360,7 +364,7 @@ def solve_variant(ref, coef, qk, px, py, p0, optimizer, order, ssd, roi=None):
             grad = (diff @ sd) * (1.0 if ssd else 2.0 / fn)
             dp = -np.linalg.solve(hess, grad)
         else:
-            dgx, dgy = spline_gradients(coef, qk, wx, wy, w, h, DEGREE, BORDER)
+            dgx, dgy = spline_gradients(coef, qk, wx, wy, w, h, degree, BORDER)
             if order == 1:
                 a00, a01, a10, a11 = 1 + p[2], p[3], p[4], 1 + p[5]
             else:
@@ -856,6 +860,37 @@ def main_truncated():
     print(f"wrote {TRUNCATED_OUT}")
 
 
+DEGREE5_OUT = os.path.join(HERE, "subset_degree5_256.npz")
+DEGREE5 = [("icgn1_znssd", 0, 1, False), ("fgn1_znssd", 1, 1, False), ("icgn2_znssd", 0, 2, False),
+           ("fgn2_ssd", 1, 2, True)]
+
+
+def main_degree5():
+    """The quintic B-spline (degree 5, the reference's default): coefficients and four routes on
+    the small workload's POIs."""
+    from traditional_dic_gb300 import synthetic
+    qk = qk_matrix(5)
+    pair = synthetic.workload(0)
+    ref, de = pair.reference, pair.deformed
+    coef = coefficients(de, 5, BORDER)
+    pts = [(x, y) for y in range(20, 240, 22) for x in range(20, 240, 22)] + [(5.0, 128.0)]
+    pois = []
+    for x, y in pts:
+        u, v = pair.field.uv(np.float64(x), np.float64(y))
+        pois.append((x, y, round(2 * float(u)) / 2.0, round(2 * float(v)) / 2.0))
+    pois = np.array(pois, np.float64)
+    arrays = {"pois": pois, "coef_crop": coef[:40, :40], "settings": np.array([5, BORDER, RADIUS, MAX_ITER, THRESHOLD])}
+    for name, opt, order, ssd in DEGREE5:
+        res = []
+        for x, y, u0, v0 in pois:
+            p, corr, iters, status, conv = solve_variant(ref, coef, qk, x, y, (u0, v0), opt, order, ssd, degree=5)
+            res.append(np.concatenate([p, [corr, iters, status, float(conv)]]))
+        arrays[name] = np.array(res, np.float64)
+        print(f"degree 5 {name}: {int(sum(r[15] for r in res))} converged")
+    np.savez_compressed(DEGREE5_OUT, **arrays)
+    print(f"wrote {DEGREE5_OUT}")
+
+
 def main():
     sys.path.insert(0, ROOT)
     import __graft_entry__ as G
@@ -883,6 +918,7 @@ def main():
     main_propagation()
     main_seed()
     main_truncated()
+    main_degree5()
 
 
 if __name__ == "__main__":

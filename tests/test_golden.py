@@ -301,3 +301,30 @@ def test_oracle_truncated_compute_matches_golden(oracle, golden, truncated_golde
     if tag == "full":   # points whose full subset would leave the image are solved
         edge = (got["x"] < 10) | (got["y"] < 10) | (got["x"] >= 246) | (got["y"] >= 246)
         assert valid[edge].sum() > 50
+
+
+# ---- the quintic B-spline (tests/golden/subset_degree5_256.npz) -----------------------------
+DEGREE5_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "subset_degree5_256.npz")
+DEGREE5 = [("icgn1_znssd", 0, 1, 1), ("fgn1_znssd", 1, 1, 1), ("icgn2_znssd", 0, 2, 1), ("fgn2_ssd", 1, 2, 0)]
+
+
+@pytest.fixture(scope="module")
+def degree5():
+    d = np.load(DEGREE5_FILE)
+    return {k: d[k] for k in d.files}
+
+
+@pytest.mark.parametrize("name,opt,order,crit", DEGREE5)
+def test_oracle_degree5_matches_golden(oracle, golden, degree5, name, opt, order, crit):
+    """Degree 5, the reference's default spline: the coefficients and four solver routes."""
+    cfg = _variant_config(degree5, oracle.default_config, opt, order, crit)
+    assert cfg.degree == 5
+    coef = oracle.prefilter(golden["deformed"].astype(np.float32), 5, cfg.border, True)
+    crop = degree5["coef_crop"]
+    assert np.max(np.abs(coef[:40, :40] - crop)) <= 1e-10 * max(1.0, np.abs(crop).max())
+    ref = golden["reference"].astype(np.float32)
+    pois = degree5["pois"]
+    p0 = np.zeros((len(pois), 6))
+    p0[:, :2] = pois[:, 2:4]
+    r = oracle.solve_pois(ref, coef, cfg, pois[:, :2], p0, gradients=oracle.reference_gradient(ref))
+    _check_variant(r, degree5[name], P_TOL, Q_TOL, 1e-9)
