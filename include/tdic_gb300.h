@@ -150,6 +150,8 @@ void tdic_grid_dims(int32_t width, int32_t height, int32_t spacing, int32_t* gri
  * (No reference counterpart: the reference builds its state per call.) */
 tdic_status tdic_ctx_create(int32_t device, tdic_ctx** out);
 void tdic_ctx_destroy(tdic_ctx* ctx);
+/* The message of the context's last failure; with ctx == NULL, that of this thread's last failed
+ * tdic_ctx_create ("null context" if none). */
 const char* tdic_last_error(const tdic_ctx* ctx);
 /* Bytes the pool holds on the device (allocated, live + cached). */
 size_t tdic_ctx_device_bytes(const tdic_ctx* ctx);

@@ -115,3 +115,19 @@ def test_truncation_geometry_matches_oracle(pkg, oracle):
             assert g == sum(1 for k in range(gp) if 0 <= k * step - pad < n)
         if not cfg.truncate_roi_subsets:
             assert got == L.grid_dims(w, h, cfg.propagation_spacing)
+
+
+def test_context_creation_failure_reports_its_cause(pkg):
+    """Without a usable device tdic_ctx_create fails, and tdic_last_error(NULL) carries the CUDA
+    message of that failure (there is no context to hold it); the facade puts it in its error."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a device is visible: context creation succeeds")
+    from traditional_dic_gb300 import _lib as L, subset as S
+    lib = L.load()
+    h = C.c_void_p()
+    assert lib.tdic_ctx_create(0, C.byref(h)) == L.TDIC_CUDA_ERROR and not h.value
+    msg = lib.tdic_last_error(None).decode()
+    assert msg != "null context" and "cudaSetDevice" in msg
+    with pytest.raises(L.TdicError, match="cudaSetDevice"):
+        S.Context(0)

@@ -661,6 +661,11 @@ void tdic_grid_dims(int32_t w, int32_t h, int32_t spacing, int32_t* gw, int32_t*
     *gh = (h + step - 1) / step;
 }
 
+namespace {
+// the message of this thread's last failed tdic_ctx_create (there is no context to hold it)
+thread_local std::string g_create_error;
+}  // namespace
+
 tdic_status tdic_ctx_create(int32_t device, tdic_ctx** out) {
     if (!out) return TDIC_INVALID_ARG;
     *out = nullptr;
@@ -676,8 +681,7 @@ tdic_status tdic_ctx_create(int32_t device, tdic_ctx** out) {
         upload_qk_constants();
     });
     if (st != TDIC_OK) {
-        static thread_local std::string msg;
-        msg = ctx->last_error;
+        g_create_error = ctx->last_error;
         delete ctx;
         return st;
     }
@@ -709,7 +713,10 @@ void tdic_ctx_destroy(tdic_ctx* ctx) {
     delete ctx;
 }
 
-const char* tdic_last_error(const tdic_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+const char* tdic_last_error(const tdic_ctx* ctx) {
+    if (ctx) return ctx->last_error.c_str();
+    return g_create_error.empty() ? "null context" : g_create_error.c_str();
+}
 
 size_t tdic_ctx_device_bytes(const tdic_ctx* ctx) { return ctx ? ctx->pool.held_bytes() : 0; }
 

@@ -18,6 +18,7 @@
 #include "tdic_internal.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <type_traits>
 
 #include <cuda.h>
@@ -2520,15 +2521,19 @@ struct TensorMaps {
 };
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
+    // looked up once; contexts on other host threads may race the first lookup and store the
+    // same pointer
+    static std::atomic<PFN_cuTensorMapEncodeTiled_v12000> fn{nullptr};
+    PFN_cuTensorMapEncodeTiled_v12000 f = fn.load(std::memory_order_acquire);
+    if (!f) {
         void* p = nullptr;
         cudaDriverEntryPointQueryResult q;
         TDIC_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
         TDIC_REQUIRE(q == cudaDriverEntryPointSuccess && p, TDIC_CUDA_ERROR, "cuTensorMapEncodeTiled unavailable");
-        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        f = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        fn.store(f, std::memory_order_release);
     }
-    return fn;
+    return f;
 }
 
 void encode_2d(CUtensorMap* m, CUtensorMapDataType dt, size_t es, const void* base, int w, int h, int pitch, int bx,

@@ -40,7 +40,8 @@ class Context:
         h = C.c_void_p()
         st = self.lib.tdic_ctx_create(int(device), C.byref(h))
         if st != L.TDIC_OK:
-            raise L.TdicError(st, f"cannot create a context on device {device} (no CUDA device visible?)")
+            why = self.lib.tdic_last_error(None).decode()
+            raise L.TdicError(st, f"cannot create a context on device {device}: {why}")
         self.handle = h
         self.device = device
 
