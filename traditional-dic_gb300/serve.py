@@ -105,8 +105,12 @@ class Server:
 
     # ---- client side -------------------------------------------------------------------------
     def submit(self, reference: np.ndarray, deformed: np.ndarray, config: dict | None = None, roi=None) -> Request:
+        """Queue one pair.  Bad images or a bad config raise here, as ``subset.compute`` would."""
         ref = S._check_image(reference, "reference")
         de = S._check_image(deformed, "deformed")
+        if config is not None and not isinstance(config, dict):
+            raise RuntimeError("config must be a dict (from YAML) or None.")
+        S.config_from_dict(config)
         with self._cv:
             req = Request(self._next_id, ref, de, config, roi, time.perf_counter())
             self._next_id += 1
@@ -227,7 +231,10 @@ class Server:
                         break
                     req = self._queue[0]
                     h, w = req.reference.shape
-                    est = _footprint(w, h, S.config_from_dict(req.config))
+                    try:
+                        est = _footprint(w, h, S.config_from_dict(req.config))
+                    except Exception:
+                        est = 0  # _prepare raises the same error and fails this request alone
                     if self._held + est > self.memory_budget and (ready or inflight is not None):
                         break  # wait for memory to free up
                     self._queue.popleft()
