@@ -112,6 +112,8 @@ class Server:
             raise RuntimeError("config must be a dict (from YAML) or None.")
         S.config_from_dict(config)
         with self._cv:
+            if self._stop:
+                raise RuntimeError("the server is closed")
             req = Request(self._next_id, ref, de, config, roi, time.perf_counter())
             self._next_id += 1
             self._queue.append(req)
@@ -198,56 +200,71 @@ class Server:
     def _loop(self) -> None:
         inflight = None
         ready: list[_Prepared] = []
-        while True:
-            with self._cv:
-                if self._stop and not self._queue and not ready and inflight is None:
-                    break
-                if not self._queue and not ready and inflight is None:
-                    self._cv.wait(0.05)
-                    continue
-            progressed = False
-            finished = None
-            if inflight is not None and inflight[2].query():
-                finished, inflight = inflight, None
-                progressed = True
-            # the next batch goes to the GPU first; the finished one's results are copied out
-            # (on the copy stream) while it runs
-            if inflight is None and ready:
-                try:
-                    inflight, ready = self._launch(ready)
-                except BaseException as exc:
-                    for p in ready:
-                        self._complete(p.req, error=exc)
-                        p.pair.close()
-                        self._held -= p.bytes
-                    ready = []
-                progressed = True
-            if finished is not None:
-                self._collect(finished)
-            # admit and prepare queued requests while the budget allows (overlaps the batch)
-            while len(ready) < self.max_batch:
+        try:
+            while True:
                 with self._cv:
-                    if not self._queue:
+                    if self._stop and not self._queue and not ready and inflight is None:
                         break
-                    req = self._queue[0]
-                    h, w = req.reference.shape
-                    try:
-                        est = _footprint(w, h, S.config_from_dict(req.config))
-                    except Exception:
-                        est = 0  # _prepare raises the same error and fails this request alone
-                    if self._held + est > self.memory_budget and (ready or inflight is not None):
-                        break  # wait for memory to free up
-                    self._queue.popleft()
-                try:
-                    prepared = self._prepare(req)
-                except BaseException as exc:
-                    self._complete(req, error=exc)
-                    prepared = None
-                progressed = True
-                if prepared is not None:
-                    self._held += prepared.bytes
-                    ready.append(prepared)
+                    if not self._queue and not ready and inflight is None:
+                        self._cv.wait(0.05)
+                        continue
+                progressed = False
+                finished = None
                 if inflight is not None and inflight[2].query():
-                    break  # launch the next batch without delay
-            if not progressed:
-                time.sleep(0.0002)
+                    finished, inflight = inflight, None
+                    progressed = True
+                # the next batch goes to the GPU first; the finished one's results are copied out
+                # (on the copy stream) while it runs
+                if inflight is None and ready:
+                    try:
+                        inflight, ready = self._launch(ready)
+                    except BaseException as exc:
+                        for p in ready:
+                            self._complete(p.req, error=exc)
+                            p.pair.close()
+                            self._held -= p.bytes
+                        ready = []
+                    progressed = True
+                if finished is not None:
+                    self._collect(finished)
+                # admit and prepare queued requests while the budget allows (overlaps the batch)
+                while len(ready) < self.max_batch:
+                    with self._cv:
+                        if not self._queue:
+                            break
+                        req = self._queue[0]
+                        h, w = req.reference.shape
+                        try:
+                            est = _footprint(w, h, S.config_from_dict(req.config))
+                        except Exception:
+                            est = 0  # _prepare raises the same error and fails this request alone
+                        if self._held + est > self.memory_budget and (ready or inflight is not None):
+                            break  # wait for memory to free up
+                        self._queue.popleft()
+                    try:
+                        prepared = self._prepare(req)
+                    except BaseException as exc:
+                        self._complete(req, error=exc)
+                        prepared = None
+                    progressed = True
+                    if prepared is not None:
+                        self._held += prepared.bytes
+                        ready.append(prepared)
+                    if inflight is not None and inflight[2].query():
+                        break  # launch the next batch without delay
+                if not progressed:
+                    time.sleep(0.0002)
+        except BaseException as exc:  # an error outside any one request (a device fault): fail them all
+            self._fail_pending(exc, ready, inflight)
+
+    def _fail_pending(self, exc: BaseException, ready, inflight) -> None:
+        with self._cv:
+            self._stop = True
+            pending = list(self._queue)
+            self._queue.clear()
+        pending += [p.req for p in ready]
+        if inflight is not None:
+            pending += [p.req for p in inflight[1]]
+        for req in pending:
+            if not req._done.is_set():
+                self._complete(req, error=exc)
