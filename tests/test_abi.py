@@ -131,3 +131,17 @@ def test_context_creation_failure_reports_its_cause(pkg):
     assert msg != "null context" and "cudaSetDevice" in msg
     with pytest.raises(L.TdicError, match="cudaSetDevice"):
         S.Context(0)
+
+
+def test_pair_update_checks_both_images(pkg):
+    """Pair.update hands both buffers to the library under one dtype: images of another shape,
+    dtype or memory kind are refused before any library call."""
+    from traditional_dic_gb300 import subset as S
+    pair = S.Pair._adopt(None, C.c_void_p(), 16, 12, 3, 0, 3)   # no device: the checks run first
+    u8 = np.zeros((12, 16), np.uint8)
+    with pytest.raises(ValueError, match="same dtype"):
+        pair.update(u8, u8.astype(np.float32))
+    with pytest.raises(ValueError, match="shape"):
+        pair.update(u8, np.zeros((12, 15), np.uint8))
+    with pytest.raises(ValueError, match="shape"):
+        pair.update(np.zeros((13, 16), np.uint8), np.zeros((13, 16), np.uint8))

@@ -133,10 +133,15 @@ class Pair:
         return self
 
     def update(self, reference, deformed, stream=None) -> None:
-        rp, w, h, dt, mem, self._keep_r = _image_arg(reference)
-        dp, _, _, _, _, self._keep_d = _image_arg(deformed)
-        if (w, h) != (self.width, self.height):
+        """New images for the pair: the pair's shape; both of one dtype and memory kind (the
+        library reads the two buffers with the one dtype it is given)."""
+        rp, w, h, dt, mem, keep_r = _image_arg(reference)
+        dp, w2, h2, dt2, mem2, keep_d = _image_arg(deformed)
+        if (w, h) != (self.width, self.height) or (w2, h2) != (self.width, self.height):
             raise ValueError("update needs images of the pair's shape")
+        if (dt, mem) != (dt2, mem2):
+            raise ValueError("reference and deformed must have the same dtype and memory")
+        self._keep_r, self._keep_d = keep_r, keep_d
         self.ctx.check(self.ctx.lib.tdic_pair_update(self.handle, rp, dp, 0, dt, mem, _stream_ptr(stream)))
 
     def coefficients(self) -> np.ndarray:
