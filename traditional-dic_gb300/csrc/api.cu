@@ -165,11 +165,16 @@ void check_config(const tdic_config& c) {
     TDIC_REQUIRE(c.max_iterations >= 0, TDIC_INVALID_ARG, "max_iterations must be >= 0");
 }
 
+void check_memory(tdic_memory mem) {
+    TDIC_REQUIRE(mem == TDIC_HOST || mem == TDIC_DEVICE, TDIC_INVALID_ARG, "memory must be TDIC_HOST or TDIC_DEVICE");
+}
+
 // Upload (or alias) one image and convert it to float32 into dst.
 void upload_convert(tdic_pair* p, const void* src, int pitch, tdic_dtype dtype, tdic_memory mem, float* dst,
                     cudaStream_t s) {
     const size_t es = dtype_size(dtype);
     TDIC_REQUIRE(es != 0, TDIC_INVALID_ARG, "unknown dtype");
+    check_memory(mem);
     const int pt = pitch > 0 ? pitch : p->w;
     TDIC_REQUIRE(pt >= p->w, TDIC_INVALID_ARG, "pitch smaller than width");
     const void* dsrc = src;
@@ -242,6 +247,7 @@ void copy_grid_back(const GridBuffers& g, const tdic_grid_out* h, int n, cudaStr
 void propagate_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const tdic_seed& seed, const uint8_t* roi,
                     const tdic_grid_out* out, tdic_memory mem, int32_t* points_computed, cudaStream_t s) {
     check_config(cfg);
+    check_memory(mem);
     TDIC_REQUIRE(pair->exact == 1, TDIC_INVALID_ARG, "propagation needs a pair with the exact prefilter");
     TDIC_REQUIRE(cfg.propagation_mode == 0 || cfg.propagation_mode == 2, TDIC_UNSUPPORTED,
                  "propagation_mode 1 (serial heap order) is not on the GPU path; use 0 (frontier waves) or 2 (dataflow)");
@@ -829,6 +835,7 @@ tdic_status tdic_solve_pois(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* c
         TDIC_REQUIRE(pair && cfg, TDIC_INVALID_ARG, "null pair or config");
         TDIC_REQUIRE(n >= 0, TDIC_INVALID_ARG, "negative POI count");
         check_config(*cfg);
+        check_memory(memory);
         if (n == 0) return;
         TDIC_REQUIRE(in && out, TDIC_INVALID_ARG, "null POI arrays");
         TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
@@ -856,6 +863,7 @@ tdic_status tdic_solve_pois_masked(tdic_ctx* ctx, tdic_pair* pair, const tdic_co
         TDIC_REQUIRE(pair && cfg, TDIC_INVALID_ARG, "null pair or config");
         TDIC_REQUIRE(n >= 0, TDIC_INVALID_ARG, "negative POI count");
         check_config(*cfg);
+        check_memory(memory);
         if (n == 0) return;
         TDIC_REQUIRE(in && out, TDIC_INVALID_ARG, "null POI arrays");
         TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
