@@ -85,6 +85,7 @@ def test_grid_dims(pkg):
     assert L.grid_dims(2048, 2048, 4) == (410, 410)
     assert L.grid_dims(5120, 5120, 2) == (1707, 1707)
     assert L.grid_dims(7, 3, -4) == (7, 3)
+    assert L.grid_dims(5, 5, 2 ** 31 - 1) == (1, 1) and L.grid_dims(2 ** 31 - 1, 1, 2 ** 31 - 2) == (1, 1)
 
 
 def test_truncation_geometry_matches_oracle(pkg, oracle):

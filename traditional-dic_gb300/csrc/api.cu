@@ -163,6 +163,7 @@ void check_config(const tdic_config& c) {
     TDIC_REQUIRE(c.criterion == 0 || c.criterion == 1, TDIC_INVALID_ARG, "criterion must be 1 (znssd) or 0 (ssd)");
     TDIC_REQUIRE(c.subset_radius >= 1 && c.subset_radius <= 100, TDIC_INVALID_ARG, "subset radius must be in [1, 100]");
     TDIC_REQUIRE(c.max_iterations >= 0, TDIC_INVALID_ARG, "max_iterations must be >= 0");
+    TDIC_REQUIRE(c.propagation_spacing < (1 << 30), TDIC_INVALID_ARG, "propagation spacing must be below 2^30");
 }
 
 void check_memory(tdic_memory mem) {
@@ -662,9 +663,9 @@ void tdic_config_default(tdic_config* c) {
 }
 
 void tdic_grid_dims(int32_t w, int32_t h, int32_t spacing, int32_t* gw, int32_t* gh) {
-    const int step = std::max(0, spacing) + 1;
-    *gw = (w + step - 1) / step;
-    *gh = (h + step - 1) / step;
+    const int64_t step = static_cast<int64_t>(std::max(0, spacing)) + 1;  // 64-bit: no overflow near INT32_MAX
+    *gw = static_cast<int32_t>((std::max<int64_t>(0, w) + step - 1) / step);
+    *gh = static_cast<int32_t>((std::max<int64_t>(0, h) + step - 1) / step);
 }
 
 namespace {
