@@ -16,9 +16,15 @@ L2 (129 MB) is flushed with a 256 MB write between timed steps.
 the whole workload (dataflow order, each diagonal's solves spread over the threads);
 ``cpu_baseline_serial`` is the same port on one thread in the reference's heap order, on a prefix.
 
+The default run also carries the uneven 48-pair batch in one graph-replayed launch
+(``batched_uneven``) and the served Poisson request stream with its p50 / p99 latency
+(``served``); ``--no-batch`` / ``--no-serve`` skip them.
+
 ``--impl reference`` times the reference algorithm's CPU implementation (the FP64 C++ port in
-oracle/, the reference itself does not build without Eigen) on a bounded sample of the same
-workload: reliability-guided heap propagation, single thread as the reference runs.
+oracle/, the reference itself does not build without Eigen) on the same workload and
+configuration: each step propagates the whole grid in the dataflow order on every host thread.
+It imports neither this build's package nor its CUDA library (the seeded input generator is
+loaded from its file on its own).
 """
 from __future__ import annotations
 
@@ -29,16 +35,13 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
-
-import __graft_entry__  # noqa: E402
-
-__graft_entry__.load_package()
 
 METRIC = "converged POIs/s, 2048^2 r=15 (FP32 vs FP64, <=1e-3 px)"
 UNIT = "POI/s"
@@ -60,6 +63,13 @@ def workload_desc(side: int) -> dict:
     g = (side + 4) // 5
     return dict(WORKLOAD, workload=f"synthetic speckle {side}x{side} uint8 (profiling case), sinusoidal u/v, "
                                    f"radius 15, POI step 5", image=[side, side], grid=[g, g])
+
+
+def run_config(side: int, mode: str) -> dict:
+    """The ``config`` object of both arms' lines: the workload and the propagation order (the
+    arithmetic and the hardware of an arm are top-level keys, so the two arms' configs compare
+    equal when they run the same work)."""
+    return dict(workload_desc(side), propagation=mode)
 
 
 CONFIG = {
@@ -93,10 +103,10 @@ class Clocks:
 
     def __init__(self):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        fd, self.path = tempfile.mkstemp(prefix="tdic_clocks_", suffix=".csv")
+        os.close(fd)
 
     def start(self):
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
@@ -113,9 +123,11 @@ class Clocks:
         self.proc.terminate()
         self.proc.wait()
         self.f.close()
+        lines = open(self.path).read().splitlines()
+        os.unlink(self.path)
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        for line in lines:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9 or parts[0] != str(device):
                 continue
@@ -195,46 +207,94 @@ def sum_over_ranks(pg, v: float) -> float:
 
 
 # ---------------------------------------------------------------------------------------
+def standalone_synthetic():
+    """The seeded workload generator (numpy only), loaded from its file as a module of its own:
+    the reference arm imports neither this build's package nor its CUDA library."""
+    import importlib.util
+    path = os.path.join(ROOT, "traditional-dic_gb300", "synthetic.py")
+    spec = importlib.util.spec_from_file_location("tdic_workload_generator", path)
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[spec.name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def oracle_config(O, d: dict, mode: int):
+    """The oracle's configuration for a config dict of this benchmark (the keys CONFIG uses),
+    over the oracle's own defaults (the reference's C++ defaults)."""
+    cfg = O.default_config()
+    cfg.subset_radius = d["subset"]["radius"]
+    cfg.max_iterations = d["optimization"]["max_iterations"]
+    cfg.convergence_threshold = d["optimization"]["convergence_threshold"]
+    cfg.degree = d["interpolation"]["degree"]
+    ini = d["initialization"]
+    cfg.is_subset_radius = ini["integer_search"]["subset_radius"]
+    cfg.is_search_radius = ini["integer_search"]["search_radius"]
+    cfg.sift_enabled = int(ini["integer_search"]["sift_enabled"])
+    cfg.pyramid_enabled = int(ini["integer_search"]["pyramid_enabled"])
+    sp = ini["subpixel_refinement"]
+    cfg.sp_enabled = int(sp["enabled"])
+    cfg.sp_subset_radius = sp["subset_radius"]
+    cfg.sp_max_iterations = sp["max_iterations"]
+    cfg.sp_convergence_threshold = sp["convergence_threshold"]
+    ss = d["seed_selection"]
+    cfg.seed_count = ss["seed_count"]
+    cfg.seed_max_znssd = ss["max_znssd"]
+    cfg.min_texture_std = ss["min_texture_std"]
+    cfg.propagation_spacing = d["reliability_propagation"]["spacing"]
+    cfg.propagation_max_znssd = d["reliability_propagation"]["max_znssd"]
+    cfg.propagation_mode = mode
+    return cfg
+
+
 def run_reference(args, world, rank, pg):
-    """Reference arm: the FP64 C++ port of the reference path on the host cores (rank 0)."""
+    """Reference arm: the FP64 C++ port of the reference path (oracle/; the reference itself
+    does not build without Eigen) on the host cores of rank 0, on the GPU arm's workload and
+    configuration.  A step propagates the whole 2048^2 grid from the seed, the solves of each
+    dataflow diagonal spread over every host thread (the same visit order, work and results as
+    one thread; the GPU arm's default order).  The reference's own serial heap order is timed
+    once on one thread over a prefix and reported beside it."""
     if rank != 0:
         return
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    from traditional_dic_gb300 import subset as S, synthetic
+    synthetic = standalone_synthetic()
     pair = synthetic.workload(1)
-    cfg = O.as_config(S.config_from_dict(CONFIG))
-    cfg.propagation_mode = 1  # reliability-guided heap order: the reference's own visit order
+    threads = host_threads()
+    cfg = oracle_config(O, CONFIG, 2)
     t0 = time.perf_counter()
     seed, _ = O.select_seed(pair.reference, pair.deformed, cfg)
     t_seed = time.perf_counter() - t0
+    assert seed.found, "no seed found"
     t0 = time.perf_counter()
     coef = O.prefilter(pair.deformed, 3, 3, True)
     grads = O.reference_gradient(pair.reference)
     t_pre = time.perf_counter() - t0
-    budget = args.ref_solves
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        O.propagate(pair.reference, coef, cfg, seed, gradients=grads, max_solves=min(200, budget))
-    rates, solved, conv_total, t_total = [], 0, 0, 0.0
+    for _ in range(args.warmup):  # warm-up steps: a bounded prefix each
+        O.propagate(pair.reference, coef, cfg, seed, gradients=grads, max_solves=2000, threads=threads)
+    conv_total, t_total = 0, 0.0
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        r = O.propagate(pair.reference, coef, cfg, seed, gradients=grads, max_solves=budget)
-        dt = time.perf_counter() - t0
-        conv = int(np.sum(r["valid"] & r["converged"]))
-        rates.append(conv / dt)
-        solved += r["solves"]
-        conv_total += conv
-        t_total += dt
+        r = O.propagate(pair.reference, coef, cfg, seed, gradients=grads, threads=threads)
+        t_total += time.perf_counter() - t0
+        conv_total += int(np.sum(r["valid"] & r["converged"]))
     value = conv_total / t_total
+    heap = oracle_config(O, CONFIG, 1)
+    t0 = time.perf_counter()
+    rh = O.propagate(pair.reference, coef, heap, seed, gradients=grads, max_solves=args.ref_solves)
+    t_heap = time.perf_counter() - t0
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": dict(WORKLOAD, propagation="reliability-guided heap (serial, reference order)"),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
-                         "sample": f"first {budget} heap-order solves of the 2048^2 workload per step "
-                                   f"(seed selection {t_seed:.2f} s and prefilter+gradients {t_pre:.2f} s "
-                                   f"untimed, once)"},
+        "config": run_config(2048, "dataflow"),
+        "precision": "fp64", "parallelism": f"{threads} host threads",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"the whole 2048x2048 workload per step: {r['solves']} solves, dataflow order, "
+                                   f"{threads} threads (FP64 C++ port of the reference path; seed selection "
+                                   f"{t_seed:.2f} s and prefilter + gradients {t_pre:.2f} s once, untimed)"},
+        "heap_order_serial": {"value": int(np.sum(rh["valid"] & rh["converged"])) / t_heap, "unit": UNIT, "cores": 1,
+                              "sample": f"first {rh['solves']} solves in the reference's heap order, one thread"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -429,16 +489,16 @@ def run_ours(args, world, rank, local, pg):
         cpu, cpu_serial = cpu_baselines(pair_np.reference, pair_np.deformed, cfg, seed, args.ref_solves)
 
     routes = run_routes(args, ctx, stream) if (args.routes and rank == 0) else None
-    batched = run_batch(args, ctx, stream) if (args.batch and rank == 0) else None
-    served = run_serve(args, ctx) if (args.serve and rank == 0) else None
+    batched = run_batch(args, ctx, stream) if (not args.no_batch and rank == 0) else None
+    served = run_serve(args, ctx) if (not args.no_serve and rank == 0) else None
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64 (mixed)" if args.precision == "fp32" else "f64",
-            "data": "synthetic", "config": dict(workload_desc(args.side), precision=args.precision, propagation=args.mode,
-                                                  parallelism=f"replicas x{world}" if world > 1 else "1 GPU"),
+            "data": "synthetic", "config": run_config(args.side, args.mode),
+            "precision": args.precision, "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
             "converged_pois_per_step": conv,
             "roofline": roofline,
             "cpu_baseline": cpu,
@@ -553,6 +613,7 @@ def run_batch(args, ctx, stream) -> dict:
     import multiprocessing as mp
     from concurrent.futures import ProcessPoolExecutor
     import torch
+    import __graft_entry__
     from traditional_dic_gb300 import subset as S, synthetic, _lib as L
     t0 = time.perf_counter()
     with ProcessPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)), mp_context=mp.get_context("spawn"),
@@ -639,6 +700,7 @@ def run_serve(args, ctx) -> dict:
     import multiprocessing as mp
     import threading
     from concurrent.futures import ProcessPoolExecutor
+    import __graft_entry__
     from traditional_dic_gb300 import subset as S, synthetic, serve
     with ProcessPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)), mp_context=mp.get_context("spawn"),
                              initializer=__graft_entry__.load_package) as ex:
@@ -708,11 +770,11 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--routes", action="store_true",
                     help="also time every solver route (ICGN/FGN x first/second order x ZNSSD/SSD), FP32 and FP64")
-    ap.add_argument("--batch", action="store_true",
-                    help="also run the uneven 48-pair batch in one launch against per-pair launches")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the uneven 48-pair batch (one launch, against per-pair launches)")
     ap.add_argument("--batch-pairs", type=int, default=48)
-    ap.add_argument("--serve", action="store_true",
-                    help="also serve the Poisson request stream (continuous batching) against per-request solves")
+    ap.add_argument("--no-serve", action="store_true",
+                    help="skip the served Poisson request stream (continuous batching, against per-request solves)")
     ap.add_argument("--serve-requests", type=int, default=40)
     ap.add_argument("--serve-reserve-sms", type=int, default=None,
                     help="SMs the served propagation leaves to request preparation (default: a tenth)")
@@ -723,6 +785,7 @@ def main():
     if args.impl == "reference":
         run_reference(args, world, rank, pg)
     else:
+        import __graft_entry__
         __graft_entry__.build()
         run_ours(args, world, rank, local, pg)
 

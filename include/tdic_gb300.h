@@ -233,13 +233,14 @@ tdic_status tdic_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cf
  * synchronisation, or a process whose device memory belongs to another allocator.  The same
  * kernel runs with its scratch in one static device array of about 11.8 MiB per device,
  * which caps the call at 131072 grid points and 32768 subset samples (radius <= 100);
- * larger calls fail with TDIC_INVALID_ARG.  out_device: device arrays of grid_w*grid_h
- * entries (NULL entries skipped); roi: host mask as for tdic_propagate.  The pair and the
- * context are made beforehand with the calls above, which do allocate.  The first call on a
- * device looks up the array's device address (set-up, once per device); make that first
- * call before any stream capture.  Every call on a device shares the array and finds the
- * previous call's contents, which it re-initialises; calls that overlapped would race, so
- * this entry point holds a process-wide lock and waits for its kernel before returning. */
+ * larger calls fail with TDIC_INVALID_ARG.  Masked subsets (cfg->truncate_roi_subsets) are
+ * not covered: TDIC_UNSUPPORTED.  out_device: device arrays of grid_w*grid_h entries (NULL
+ * entries skipped); roi: host mask as for tdic_propagate.  The pair and the context are made
+ * beforehand with the calls above, which do allocate.  The first call on a device looks up the
+ * array's device address (set-up, once per device); make that first call before any stream
+ * capture.  Every call on a device shares the array and finds the previous call's contents,
+ * which it re-initialises; calls that overlapped on the GPU would race, so this entry point
+ * holds a process-wide lock and waits for its stream before returning, also when it fails. */
 tdic_status tdic_propagate_noalloc(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cfg,
                                    const tdic_seed* seed, const uint8_t* roi,
                                    const tdic_grid_out* out_device, int32_t* points_computed,

@@ -54,7 +54,11 @@ class _Event:
 
 
 class _Pair:
+    made = 0
     closed = 0
+
+    def __init__(self):
+        _Pair.made += 1
 
     def close(self):
         _Pair.closed += 1
@@ -113,6 +117,7 @@ def test_loop_batches_requests_and_isolates_a_failing_one(pkg):
 def test_loop_fails_every_pending_request_on_a_device_error(pkg):
     srv = _looping_server(fail_query=True)
     img = np.ones((16, 16), np.float32)
+    made, closed = _Pair.made, _Pair.closed
     reqs = [srv.submit(img, img) for _ in range(7)]
     srv._thread.start()
     for r in reqs:
@@ -120,5 +125,8 @@ def test_loop_fails_every_pending_request_on_a_device_error(pkg):
             r.wait(10)
     srv._thread.join(10)
     assert not srv._thread.is_alive()
+    # the prepared pairs and those of the batch in flight are released, the budget with them
+    assert _Pair.made - made > 0 and _Pair.closed - closed == _Pair.made - made
+    assert srv._held == 0
     with pytest.raises(RuntimeError, match="closed"):
         srv.submit(img, img)

@@ -1,15 +1,12 @@
 """tdic_propagate_noalloc: propagation with its scratch in a static device array instead of the
-context's pool.  Called through the C ABI; its grid must match tdic_propagate's on two calls in
-a row (the second call finds the first call's scratch contents), and the context's device
-memory must not grow while it runs."""
+context's pool, for callers that cannot allocate device memory while they propagate.  Called
+through the C ABI; its grid must equal tdic_propagate's bit for bit (the same kernel in the same
+deterministic visit order) on two calls in a row (the second call finds the first call's scratch
+contents), and neither the context's pool nor the device's free memory may change while it runs."""
 import ctypes as C
 
 import numpy as np
 import pytest
-
-U_TOL = 1e-3       # px
-G_TOL = 1e-5       # displacement gradients
-FLAG_AGREE = 0.999
 
 DOUBLE_FIELDS = ("x", "y", "u", "v", "du_dx", "du_dy", "dv_dx", "dv_dy", "correlation", "zncc")
 
@@ -57,35 +54,34 @@ def test_noalloc_matches_propagate_on_two_calls(oracle, workload0, mode):
     pair = S.Pair(ctx, p.reference, p.deformed, degree=3)
     gw, gh = L.grid_dims(pair.width, pair.height, cfg.propagation_spacing)
     n = gw * gh
+    want = S.propagate(ctx, pair, cfg, seed, roi=roi)   # the allocating entry point (loads the kernels)
+    grids = [_device_grid(torch, n) for _ in range(2)]   # outputs made before the calls
     torch.cuda.synchronize()
     held = ctx.device_bytes
+    free_before = torch.cuda.mem_get_info()[0]
     got = []
-    for _ in range(2):
-        t = _device_grid(torch, n)
+    for t in grids:
         g = _grid_struct(L, t)
         pc = C.c_int32(-1)
         st = ctx.lib.tdic_propagate_noalloc(ctx.handle, pair.handle, C.byref(cfg), C.byref(seed), roi.ctypes.data,
                                             C.byref(g), C.byref(pc), None)
         ctx.check(st)
-        got.append(({k: v.cpu().numpy() for k, v in t.items()}, pc.value))
+        got.append(pc.value)
+    free_after = torch.cuda.mem_get_info()[0]
     assert ctx.device_bytes == held                    # nothing taken from the context's pool
-
-    want = S.propagate(ctx, pair, cfg, seed, roi=roi)
-    for out, pc in got:
+    assert free_after == free_before                   # nor from the device
+    for t, pc in zip(grids, got):
+        out = {k: v.cpu().numpy() for k, v in t.items()}
         assert pc == want["points_computed"] and pc > 1
-        assert np.array_equal(out["x"], want["x"]) and np.array_equal(out["y"], want["y"])
-        valid = out["valid"].astype(bool)
-        assert np.mean(valid == want["valid"]) >= FLAG_AGREE
-        assert np.mean(out["converged"].astype(bool) == want["converged"]) >= FLAG_AGREE
-        both = valid & want["valid"]
-        assert both.sum() > 0.5 * n
-        for k in ("u", "v"):
-            assert np.max(np.abs(out[k][both] - want[k][both])) <= U_TOL
-        for k in ("du_dx", "du_dy", "dv_dx", "dv_dy"):
-            assert np.max(np.abs(out[k][both] - want[k][both])) <= G_TOL
-        # every grid point written (the device arrays started as NaN / out-of-range codes)
-        assert np.array_equal(np.isnan(out["correlation"]), np.isnan(want["correlation"]))
-        assert np.mean(out["status"] == want["status"]) >= FLAG_AGREE
+        assert out["valid"].astype(bool).sum() > 0.5 * n
+        # every field of every grid point, bit for bit (the device arrays started as NaN and
+        # out-of-range codes, so a point left unwritten shows)
+        for k in DOUBLE_FIELDS:
+            assert np.array_equal(out[k], want[k], equal_nan=True), k
+        for k in ("valid", "converged"):
+            assert np.array_equal(out[k].astype(bool), want[k]), k
+        assert np.array_equal(out["status"], want["status"])
+        assert np.array_equal(out["iterations"], want["iterations"])
     pair.close()
     ctx.close()
 

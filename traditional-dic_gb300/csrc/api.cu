@@ -1176,17 +1176,13 @@ unsigned char* noalloc_scratch_ptr(int device) {
     return noalloc_ptr[device];
 }
 
-// Host data reach the array through a small stack buffer: a pageable host-to-device copy
-// returns once its source has been staged, so the buffer can be refilled at once.
-template <typename Fill>
-void upload_chunked(unsigned char* dst, size_t bytes, Fill&& fill, cudaStream_t s) {
-    unsigned char chunk[4096];
-    for (size_t done = 0; done < bytes; done += sizeof(chunk)) {
-        const size_t k = std::min(sizeof(chunk), bytes - done);
-        fill(chunk, done, k);
-        TDIC_CUDA_TRY(cudaMemcpyAsync(dst + done, chunk, k, cudaMemcpyHostToDevice, s));
-    }
-}
+// Host-side staging of what the kernel reads from the host (the ROI at the grid points and the
+// subset's sample offsets): one static host buffer per field, filled under noalloc_mu and sent
+// with one copy each.  A pageable host-to-device copy returns once its source has been staged,
+// and every call waits for its stream before it releases the lock, so the next call may refill
+// the buffers.
+unsigned char noalloc_host_roi[kNoAllocMaxPoints];
+short2 noalloc_host_offsets[kNoAllocMaxOffsets];
 
 void propagate_noalloc_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const tdic_seed& seed,
                             const uint8_t* roi, const tdic_grid_out* out, int32_t* points_computed, cudaStream_t s) {
@@ -1222,23 +1218,17 @@ void propagate_noalloc_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& c
     constexpr NoAllocLayout lay = noalloc_layout(kNoAllocMaxPoints, kNoAllocMaxOffsets);
     // The array keeps the previous call's contents: everything the kernel reads before it
     // writes is set here.
-    upload_chunked(base + lay.roi, n, [&](unsigned char* c, size_t at, size_t k) {
-        for (size_t j = 0; j < k; ++j) {
-            const size_t i = at + j;
-            c[j] = roi ? (roi[((i / gw) * step) * static_cast<size_t>(w) + (i % gw) * step] ? 1 : 0) : 1;
-        }
-    }, s);
+    for (int i = 0; i < n; ++i)
+        noalloc_host_roi[i] = roi ? (roi[static_cast<size_t>((i / gw) * step) * w + (i % gw) * step] ? 1 : 0) : 1;
     // the row-major order of the context's table, so the sums run in the same order
-    int ody = -r, odx = -r - 1;
-    upload_chunked(base + lay.offsets, 4 * static_cast<size_t>(n_off), [&](unsigned char* c, size_t, size_t k) {
-        for (size_t j = 0; j < k; j += 4) {
-            do {
-                if (++odx > r) { odx = -r; ++ody; }
-            } while (odx * odx + ody * ody > r * r);
-            const short2 o = make_short2(static_cast<short>(odx), static_cast<short>(ody));
-            std::memcpy(c + j, &o, 4);
-        }
-    }, s);
+    int k_off = 0;
+    for (int dy = -r; dy <= r; ++dy)
+        for (int dx = -r; dx <= r; ++dx)
+            if (dx * dx + dy * dy <= r * r)
+                noalloc_host_offsets[k_off++] = make_short2(static_cast<short>(dx), static_cast<short>(dy));
+    TDIC_CUDA_TRY(cudaMemcpyAsync(base + lay.roi, noalloc_host_roi, n, cudaMemcpyHostToDevice, s));
+    TDIC_CUDA_TRY(cudaMemcpyAsync(base + lay.offsets, noalloc_host_offsets, sizeof(short2) * n_off,
+                                  cudaMemcpyHostToDevice, s));
     TDIC_CUDA_TRY(cudaMemsetAsync(base + lay.claim, 0, sizeof(int) * n, s));
     TDIC_CUDA_TRY(cudaMemsetAsync(base + lay.key, 0xff, sizeof(unsigned long long) * n, s));
     TDIC_CUDA_TRY(cudaMemsetAsync(base + lay.fetch, 0, sizeof(int) * (n + 2), s));
@@ -1292,8 +1282,16 @@ tdic_status tdic_propagate_noalloc(tdic_ctx* ctx, tdic_pair* pair, const tdic_co
         TDIC_REQUIRE(pair && cfg && seed && out_device && points_computed, TDIC_INVALID_ARG, "null argument");
         TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
         std::lock_guard<std::mutex> lock(noalloc_mu);
-        propagate_noalloc_impl(ctx, pair, *cfg, *seed, roi, out_device, points_computed, pick(ctx, stream));
-        mark_use(pair, pick(ctx, stream));
+        cudaStream_t s = pick(ctx, stream);
+        try {
+            propagate_noalloc_impl(ctx, pair, *cfg, *seed, roi, out_device, points_computed, s);
+        } catch (...) {
+            // copies or memsets into the shared array may still be queued: let them land before
+            // the next call may touch the array
+            (void)cudaStreamSynchronize(s);
+            throw;
+        }
+        mark_use(pair, s);
     });
 }
 

@@ -258,13 +258,27 @@ class Server:
             self._fail_pending(exc, ready, inflight)
 
     def _fail_pending(self, exc: BaseException, ready, inflight) -> None:
+        """Fail every request not yet answered and release what they hold on the device: the
+        prepared pairs, the batch in flight and its pairs (each release on its own, so one that
+        fails does not keep the others)."""
         with self._cv:
             self._stop = True
             pending = list(self._queue)
             self._queue.clear()
-        pending += [p.req for p in ready]
+        held = list(ready)
         if inflight is not None:
-            pending += [p.req for p in inflight[1]]
+            held += list(inflight[1])
+            try:
+                inflight[0].close()
+            except Exception:
+                pass
+        for p in held:
+            pending.append(p.req)
+            try:
+                p.pair.close()
+            except Exception:
+                pass
+        self._held = 0
         for req in pending:
             if not req._done.is_set():
                 self._complete(req, error=exc)
