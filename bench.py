@@ -456,6 +456,7 @@ def run_ours(args, world, rank, local, pg):
                 t64.append(a.elapsed_time(b) / 1e3)
         v64 = outs["valid"].cpu().numpy() != 0
         c64 = outs["converged"].cpu().numpy() != 0
+        res64 = {k: outs[k].cpu().numpy().copy() for k in ("u", "v", "valid", "converged", "zncc")}
         both = v64 & (res32["valid"] != 0)
         du = np.abs(outs["u"].cpu().numpy()[both] - res32["u"][both])
         dv = np.abs(outs["v"].cpu().numpy()[both] - res32["v"][both])
@@ -467,6 +468,45 @@ def run_ours(args, world, rank, local, pg):
                                  "flag_agreement": float(np.mean(v64 == (res32["valid"] != 0))),
                                  "within_1e-3_px": float(np.mean((du <= 1e-3) & (dv <= 1e-3)))}}
         pair64.close()
+
+    # The reference's own visit order on the device (propagation_mode 1: heap simulation on the
+    # host, device rounds), FP32-mixed and FP64, against the dataflow order of the same build.
+    heap = None
+    if not args.skip_heap:
+        heap = {}
+        res_flow = {args.precision: res32}   # the main timed run's results
+        if fp64 is not None:
+            res_flow["fp64"] = res64
+        for prec in res_flow:
+            hcfg = S.config_from_dict(dict(CONFIG, gpu={"precision": prec, "propagation": "heap"}))
+            hpair = pair if prec == args.precision else S.Pair(ctx, ref_d, def_d, degree=3, precision=hcfg.precision,
+                                                               stream=stream)
+            th = []
+            for i in range(3):
+                torch.cuda.synchronize()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                ctx.check(ctx.lib.tdic_propagate(ctx.handle, hpair.handle, C.byref(hcfg), C.byref(seed), None,
+                                                 C.byref(grid), L.DEVICE, C.byref(pc), sptr))
+                b.record(stream)
+                b.synchronize()
+                if i:
+                    th.append(a.elapsed_time(b) / 1e3)
+            if hpair is not pair:
+                hpair.close()
+            hv = outs["valid"].cpu().numpy() != 0
+            hc = outs["converged"].cpu().numpy() != 0
+            f = res_flow[prec]
+            both = hv & (f["valid"] != 0)
+            d = np.maximum(np.abs(outs["u"].cpu().numpy()[both] - f["u"][both]),
+                           np.abs(outs["v"].cpu().numpy()[both] - f["v"][both]))
+            t_h = statistics.median(th)
+            rounds, solves = ctx.heap_stats()
+            heap[prec] = {"ms": 1e3 * t_h, "value": float(np.sum(hv & hc)) / t_h, "unit": UNIT,
+                          "device_rounds": rounds, "round_solves": solves,
+                          "dataflow_vs_heap": {"flag_agreement": float(np.mean(hv == (f["valid"] != 0))),
+                                               "within_1e-3_px": float(np.mean(d <= 1e-3)),
+                                               "max_abs_px": float(d.max()), "p99_abs_px": float(np.quantile(d, 0.99))}}
 
     # e2e through the public API with pinned host images.
     ref_pin = torch.from_numpy(pair_np.reference).pin_memory()
@@ -508,6 +548,7 @@ def run_ours(args, world, rank, local, pg):
                     "includes": "H2D of both images (pinned), seed selection, prefilter, propagation, D2H of the "
                                 "result dict"},
             "fp64_path": fp64,
+            "heap_order": heap,
             "gpu_launches": 5 * args.steps,
             "clocks": clk,
             "stages_ms": {"prefilter_and_convert": 1e3 * (statistics.median(times) - t_prop),
@@ -633,7 +674,7 @@ def run_batch(args, ctx, stream) -> dict:
         cfgs.append(cfg)
         seeds.append(seed)
     batch = S.Batch(ctx, pairs, cfgs, seeds)
-    g, k = batch.tune()
+    g, k, staging = batch.tune()
     side = torch.cuda.Stream()
     graph = torch.cuda.CUDAGraph()
     with torch.cuda.graph(graph, stream=side):
@@ -677,7 +718,8 @@ def run_batch(args, ctx, stream) -> dict:
             "value": conv / t_batch, "unit": UNIT, "ms_per_launch": 1e3 * t_batch,
             "per_pair_launches": {"value": conv / t_pairs, "ms_total": 1e3 * t_pairs},
             "speedup_over_per_pair": t_pairs / t_batch,
-            "launch_config": {"warps_per_poi": g, "groups_per_block": k, "tuned": True, "cuda_graph": True},
+            "launch_config": {"warps_per_poi": g, "groups_per_block": k, "staging": staging, "tuned": True,
+                              "cuda_graph": True},
             "generation_s": t_gen}
 
 
@@ -768,6 +810,8 @@ def main():
     ap.add_argument("--ref-solves", type=int, default=20000)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-heap", action="store_true",
+                    help="skip the reference's heap order on the device (FP32 and FP64, against dataflow)")
     ap.add_argument("--routes", action="store_true",
                     help="also time every solver route (ICGN/FGN x first/second order x ZNSSD/SSD), FP32 and FP64")
     ap.add_argument("--no-batch", action="store_true",

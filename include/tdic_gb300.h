@@ -41,6 +41,17 @@ typedef enum tdic_memory { TDIC_HOST = 0, TDIC_DEVICE = 1 } tdic_memory;
 
 typedef enum tdic_precision { TDIC_FP32_MIXED = 0, TDIC_FP64 = 1 } tdic_precision;
 
+/* Shared-memory staging of a solver group (first-order ZNSSD route; the other routes always
+ * stage in full).  FULL: the coefficient window under the warped subset and four per-sample
+ * arrays; LEAN: only the per-sample arrays the iterations write, the reference values and
+ * gradients re-read from the staged reference window; LEAN_NO_WINDOW: LEAN, and the spline
+ * stencils read from the (L2-resident) coefficient image.  AUTO takes the mode that keeps the
+ * most solver groups resident (the fullest staging among equals); a mode whose shared memory
+ * does not fit returns TDIC_UNSUPPORTED. */
+typedef enum tdic_staging {
+    TDIC_STAGING_AUTO = 0, TDIC_STAGING_FULL = 1, TDIC_STAGING_LEAN = 2, TDIC_STAGING_LEAN_NO_WINDOW = 3
+} tdic_staging;
+
 /* Per-POI status ordinals = dic::SolverStatus (include/dic/core/types.hpp:35-40). */
 enum { TDIC_SUCCESS = 0, TDIC_NOT_CONVERGED = 1, TDIC_INVALID_INPUT = 2, TDIC_NUMERICAL_FAILURE = 3 };
 
@@ -48,9 +59,9 @@ enum { TDIC_SUCCESS = 0, TDIC_NOT_CONVERGED = 1, TDIC_INVALID_INPUT = 2, TDIC_NU
  * (include/dic/subset/subset_config.hpp:33-50, include/dic/initialization/seed_config.hpp:32-68,
  * include/dic/interpolation/bspline.hpp:42-67), C++ defaults from tdic_config_default().
  * propagation_mode and precision are GPU-only knobs (the reference has neither).  The visit
- * order of the propagation: 2 = dataflow (a grid point is solved as soon as its parent one step
- * toward the seed is accepted), 0 = frontier waves; 1 = the reference's serial heap order
- * exists in the CPU oracle only (TDIC_UNSUPPORTED here). */
+ * order of the propagation: 1 = the reference's own serial heap order (its results, reproduced
+ * on the device in rounds), 2 = dataflow (a grid point is solved as soon as its parent one step
+ * toward the seed is accepted; the fastest), 0 = frontier waves. */
 typedef struct tdic_config {
     int32_t subset_radius;             /* subset.radius                               15 */
     int32_t max_iterations;            /* optimization.max_iterations                 30 */
@@ -79,13 +90,17 @@ typedef struct tdic_config {
     double min_displacement_norm;      /* seed_selection.min_displacement_norm          0 */
     double min_texture_std;            /* seed_selection.min_texture_std                0 */
     int32_t kmeans_sample_limit;       /* seed_selection.kmeans_sample_limit        20000 */
-    int32_t propagation_mode;          /* 2 dataflow, 0 frontier waves (GPU orders)     2 */
+    int32_t propagation_mode;          /* 1 heap (reference), 2 dataflow, 0 waves       2 */
     /* Masked subsets (SubsetConfig, subset_config.hpp:40-42; set from the YAML subset section,
      * yaml_parser.cpp:103-111, not from the pybind dict): samples outside the ROI are left out of
      * each subset, and SubsetDIC::compute pads the images (subset_dic.cpp:53-56). */
     int32_t truncate_roi_subsets;      /* subset.truncate_roi_subsets                    0 */
     int32_t min_valid_samples;         /* subset.min_valid_samples                       12 */
     double min_valid_sample_ratio;     /* subset.min_valid_sample_ratio                 0.5 */
+    /* GPU only: shared-memory staging of the first-order ZNSSD solves (tdic_staging); the choice
+     * changes speed and shared-memory needs, never a result. */
+    int32_t staging;                   /* tdic_staging                                AUTO */
+    int32_t pad_;
 } tdic_config;
 
 /* One POI for a batched solve: centre (rounded to the nearest pixel as icgn.cpp:472-473),
@@ -155,6 +170,9 @@ void tdic_ctx_destroy(tdic_ctx* ctx);
 const char* tdic_last_error(const tdic_ctx* ctx);
 /* Bytes the pool holds on the device (allocated, live + cached). */
 size_t tdic_ctx_device_bytes(const tdic_ctx* ctx);
+/* The last heap-order propagation (propagation_mode 1) on this context: device rounds after
+ * the dataflow pass and the solves they ran.  No counterpart in the reference. */
+tdic_status tdic_ctx_heap_stats(const tdic_ctx* ctx, int32_t* rounds, int64_t* solves);
 
 /* Image pair on the device: the reference image (float32, as dic::Image stores it,
  * image.hpp:58-81) and the deformed image's B-spline coefficients of `degree` with `border`
@@ -216,10 +234,16 @@ void tdic_subset_grid_dims(int32_t width, int32_t height, const tdic_config* cfg
  * used as given (SubsetDIC::compute pads them first: tdic_subset_compute does).  The grid
  * geometry, seed alignment (:201-264), neighbour admission (:303-323), guess extrapolation
  * (:326-329) and acceptance rule (:359-368) are the reference's; the visit order is
- * cfg->propagation_mode: dataflow (each point solved from its parent one step toward the seed
- * as soon as that parent is accepted, the other axis's parent if it failed; unreached points
- * swept by waves) or frontier waves (every admissible neighbour of wave w's accepted set is
- * solved in wave w+1 from the parent with the lowest ZNSSD, ties to the lowest parent index).
+ * cfg->propagation_mode:
+ *   1  the reference's heap order (:270-389), with its results: rounds of a host simulation of
+ *      the heap over a device result table and device solves of the points whose parent or
+ *      guess changed, until the simulation meets no stale result (two or three rounds);
+ *   2  dataflow (each point solved from its parent one step toward the seed as soon as that
+ *      parent is accepted, the other axis's parent if it failed; unreached points swept by
+ *      waves): one launch, the fastest; results differ from the heap order's at the
+ *      convergence threshold's level, as the guesses come from other neighbours;
+ *   0  frontier waves (every admissible neighbour of wave w's accepted set is solved in wave
+ *      w+1 from the parent with the lowest ZNSSD, ties to the lowest parent index).
  * roi: host uint8 H x W mask (NULL = all valid).  out: host or device arrays per `memory`
  * of grid_w*grid_h entries.  *points_computed = accepted points including the seed (0 means
  * the seed could not be placed: SubsetDIC::compute then returns the empty result). */
@@ -237,8 +261,9 @@ tdic_status tdic_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cf
  * not covered: TDIC_UNSUPPORTED.  out_device: device arrays of grid_w*grid_h entries (NULL
  * entries skipped); roi: host mask as for tdic_propagate.  The pair and the context are made
  * beforehand with the calls above, which do allocate.  The first call on a device looks up the
- * array's device address (set-up, once per device); make that first call before any stream
- * capture.  Every call on a device shares the array and finds the previous call's contents,
+ * array's device address (set-up, once per device; under the driver's lazy module loading this
+ * is also when the array's memory is committed on the device); make that first call before any
+ * stream capture.  Every call on a device shares the array and finds the previous call's contents,
  * which it re-initialises; calls that overlapped on the GPU would race, so this entry point
  * holds a process-wide lock and waits for its stream before returning, also when it fails. */
 tdic_status tdic_propagate_noalloc(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cfg,
@@ -278,8 +303,10 @@ tdic_status tdic_batch_results(tdic_batch* batch, int32_t job, const tdic_grid_o
  * propagation holds its SMs for its whole duration, so leaving some free lets kernels on other
  * streams (the preparation of the next requests in a serving loop) run alongside it. */
 tdic_status tdic_batch_set_sms(tdic_batch* batch, int32_t sms);
-/* The launch configuration in use: warps per POI and solver groups per thread block. */
-tdic_status tdic_batch_config(tdic_batch* batch, int32_t* warps_per_poi, int32_t* groups_per_block);
+/* The launch configuration in use: warps per POI, solver groups per thread block and the
+ * shared-memory staging (tdic_staging; staging may be NULL). */
+tdic_status tdic_batch_config(tdic_batch* batch, int32_t* warps_per_poi, int32_t* groups_per_block,
+                              int32_t* staging);
 void tdic_batch_destroy(tdic_batch* batch);
 
 /* Seed selection: SeedSelector::select_best_seed (seed_selector.cpp:146-205) with k-means

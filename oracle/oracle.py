@@ -38,6 +38,7 @@ CONFIG_FIELDS = [
     ("kmeans_iterations", C.c_int32), ("seed_max_znssd", C.c_double), ("min_displacement_norm", C.c_double),
     ("min_texture_std", C.c_double), ("kmeans_sample_limit", C.c_int32), ("propagation_mode", C.c_int32),
     ("truncate_roi_subsets", C.c_int32), ("min_valid_samples", C.c_int32), ("min_valid_sample_ratio", C.c_double),
+    ("staging", C.c_int32), ("pad_", C.c_int32),
 ]
 
 

@@ -1508,6 +1508,7 @@ void orc_config_default(orc_config* c) {
     c->min_displacement_norm = 0.0; c->min_texture_std = 0.0; c->kmeans_sample_limit = 20000;
     c->propagation_mode = 1;
     c->truncate_roi_subsets = 0; c->min_valid_samples = 12; c->min_valid_sample_ratio = 0.5;
+    c->staging = 0; c->pad_ = 0;
 }
 
 double orc_bspline_basis(double x, int r, int d) { return valid_degree(d) ? basis(x, r, d) : kNaN; }

@@ -66,6 +66,8 @@ typedef struct orc_config {
     int32_t truncate_roi_subsets;      /* subset.truncate_roi_subsets (YAML only)        0 */
     int32_t min_valid_samples;         /* subset.min_valid_samples                       12 */
     double min_valid_sample_ratio;     /* subset.min_valid_sample_ratio                 0.5 */
+    int32_t staging;                   /* product-only knob (shared-memory staging); unused here */
+    int32_t pad_;
 } orc_config;
 
 /* Per-POI solver result; mirrors dic::Displacement2D (result.hpp:32-51) plus the additive

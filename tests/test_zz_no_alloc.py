@@ -55,18 +55,22 @@ def test_noalloc_matches_propagate_on_two_calls(oracle, workload0, mode):
     gw, gh = L.grid_dims(pair.width, pair.height, cfg.propagation_spacing)
     n = gw * gh
     want = S.propagate(ctx, pair, cfg, seed, roi=roi)   # the allocating entry point (loads the kernels)
-    grids = [_device_grid(torch, n) for _ in range(2)]   # outputs made before the calls
+    grids = [_device_grid(torch, n) for _ in range(3)]   # outputs made before the calls
     torch.cuda.synchronize()
     held = ctx.device_bytes
-    free_before = torch.cuda.mem_get_info()[0]
-    got = []
-    for t in grids:
+
+    def call(t):
         g = _grid_struct(L, t)
         pc = C.c_int32(-1)
-        st = ctx.lib.tdic_propagate_noalloc(ctx.handle, pair.handle, C.byref(cfg), C.byref(seed), roi.ctypes.data,
-                                            C.byref(g), C.byref(pc), None)
-        ctx.check(st)
-        got.append(pc.value)
+        ctx.check(ctx.lib.tdic_propagate_noalloc(ctx.handle, pair.handle, C.byref(cfg), C.byref(seed),
+                                                 roi.ctypes.data, C.byref(g), C.byref(pc), None))
+        return pc.value
+
+    # the first call on the device is the set-up: looking up the static array makes the driver
+    # load it (its ~12 MiB appear in the device's used memory then, once)
+    got = [call(grids[0])]
+    free_before = torch.cuda.mem_get_info()[0]
+    got += [call(t) for t in grids[1:]]                 # two calls in a row
     free_after = torch.cuda.mem_get_info()[0]
     assert ctx.device_bytes == held                    # nothing taken from the context's pool
     assert free_after == free_before                   # nor from the device

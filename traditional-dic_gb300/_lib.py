@@ -29,6 +29,7 @@ CONFIG_FIELDS = [
     ("kmeans_iterations", C.c_int32), ("seed_max_znssd", C.c_double), ("min_displacement_norm", C.c_double),
     ("min_texture_std", C.c_double), ("kmeans_sample_limit", C.c_int32), ("propagation_mode", C.c_int32),
     ("truncate_roi_subsets", C.c_int32), ("min_valid_samples", C.c_int32), ("min_valid_sample_ratio", C.c_double),
+    ("staging", C.c_int32), ("pad_", C.c_int32),
 ]
 
 
@@ -104,7 +105,8 @@ SIGNATURES = {
     "tdic_batch_outputs": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(GridOut)]),
     "tdic_batch_results": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(GridOut), C.c_void_p]),
     "tdic_batch_set_sms": (C.c_int, [C.c_void_p, C.c_int32]),
-    "tdic_batch_config": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "tdic_ctx_heap_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
+    "tdic_batch_config": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "tdic_batch_destroy": (None, [C.c_void_p]),
     "tdic_subset_prepare": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int, C.c_void_p,
                                       C.POINTER(Config), C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(Seed)]),

@@ -1,7 +1,9 @@
 """Build libtdic_gb300.so: hand-written CUDA for sm_103a plus the C ABI.
 
 nvcc compiles each translation unit in parallel (one -gencode, sm_103a) and links a shared
-library into _build/ next to this file.  variants.cu is compiled once per solver route other than
+library into _build/ next to this file.  hotpath.cu holds the single-pair first-order ZNSSD
+kernels, batch.cu the batched propagation (once per precision), heap_order.cu the host rounds of
+the heap order.  variants.cu is compiled once per solver route other than
 first-order ZNSSD (-DTDIC_ROUTE=1 SSD, 2 second order, 3 second-order SSD, 4 masked first-order
 ZNSSD), so the routes' kernels build side by side.  No torch types cross the ABI, so the library is built with plain nvcc, not
 torch.utils.cpp_extension.
@@ -18,6 +20,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libtdic_gb300.so")
 # (source, object, extra nvcc flags)
 UNITS = [("api.cu", "api.o", []), ("prefilter.cu", "prefilter.o", []), ("hotpath.cu", "hotpath.o", []),
+         ("heap_order.cu", "heap_order.o", []), ("batch.cu", "batch_f32.o", ["-DTDIC_BATCH_FP64=0"]),
+         ("batch.cu", "batch_f64.o", ["-DTDIC_BATCH_FP64=1"]),
          ("seed.cu", "seed.o", []), ("strain.cu", "strain.o", []),
          ("variants.cu", "route1.o", ["-DTDIC_ROUTE=1"]), ("variants.cu", "route2.o", ["-DTDIC_ROUTE=2"]),
          ("variants.cu", "route3.o", ["-DTDIC_ROUTE=3"]), ("variants.cu", "route4.o", ["-DTDIC_ROUTE=4"])]

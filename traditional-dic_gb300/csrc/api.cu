@@ -250,8 +250,8 @@ void propagate_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, cons
     check_config(cfg);
     check_memory(mem);
     TDIC_REQUIRE(pair->exact == 1, TDIC_INVALID_ARG, "propagation needs a pair with the exact prefilter");
-    TDIC_REQUIRE(cfg.propagation_mode == 0 || cfg.propagation_mode == 2, TDIC_UNSUPPORTED,
-                 "propagation_mode 1 (serial heap order) is not on the GPU path; use 0 (frontier waves) or 2 (dataflow)");
+    TDIC_REQUIRE(cfg.propagation_mode >= 0 && cfg.propagation_mode <= 2, TDIC_INVALID_ARG,
+                 "propagation_mode must be 0 (frontier waves), 1 (heap order) or 2 (dataflow)");
     const int w = pair->w, h = pair->h;
     const int step = std::max(0, cfg.propagation_spacing) + 1;
     int32_t gw, gh;
@@ -273,6 +273,12 @@ void propagate_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, cons
         for (int i = 0; i < n; ++i) roi_grid[i] = roi[static_cast<size_t>((i / gw) * step) * w + (i % gw) * step] ? 1 : 0;
     GridBuffers gb;
     if (mem == TDIC_DEVICE) gb.dev = *out; else alloc_grid(ctx, gb, n, out);
+    if (cfg.propagation_mode == 1) {  // the reference's own visit order, in rounds (heap_order.cu)
+        heap_propagate(ctx, pair, cfg, seed, roi, gb.dev, points_computed, s);
+        if (mem == TDIC_HOST) copy_grid_back(gb, out, n, s);
+        TDIC_CUDA_TRY(cudaStreamSynchronize(s));
+        return;
+    }
     Buffer d_roi(&ctx->pool, n);
     Buffer claim(&ctx->pool, sizeof(int) * n);
     Buffer keyparams(&ctx->pool, (sizeof(unsigned long long) + propagate_param_bytes(pair->precision)) * n);
@@ -660,6 +666,7 @@ void tdic_config_default(tdic_config* c) {
     c->min_displacement_norm = 0.0; c->min_texture_std = 0.0; c->kmeans_sample_limit = 20000;
     c->propagation_mode = 2;
     c->truncate_roi_subsets = 0; c->min_valid_samples = 12; c->min_valid_sample_ratio = 0.5;
+    c->staging = TDIC_STAGING_AUTO; c->pad_ = 0;
 }
 
 void tdic_grid_dims(int32_t w, int32_t h, int32_t spacing, int32_t* gw, int32_t* gh) {
@@ -726,6 +733,13 @@ const char* tdic_last_error(const tdic_ctx* ctx) {
 }
 
 size_t tdic_ctx_device_bytes(const tdic_ctx* ctx) { return ctx ? ctx->pool.held_bytes() : 0; }
+
+tdic_status tdic_ctx_heap_stats(const tdic_ctx* ctx, int32_t* rounds, int64_t* solves) {
+    if (!ctx || !rounds || !solves) return TDIC_INVALID_ARG;
+    *rounds = ctx->heap_rounds;
+    *solves = ctx->heap_solves;
+    return TDIC_OK;
+}
 
 tdic_status tdic_pair_create(tdic_ctx* ctx, const void* reference, const void* deformed, int32_t width, int32_t height,
                              int32_t pitch, tdic_dtype dtype, tdic_memory memory, int32_t degree, int32_t border,
@@ -1190,7 +1204,8 @@ void propagate_noalloc_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& c
     TDIC_REQUIRE(!cfg.truncate_roi_subsets, TDIC_UNSUPPORTED, "no-allocation propagation: masked subsets not covered");
     TDIC_REQUIRE(pair->exact == 1, TDIC_INVALID_ARG, "propagation needs a pair with the exact prefilter");
     TDIC_REQUIRE(cfg.propagation_mode == 0 || cfg.propagation_mode == 2, TDIC_UNSUPPORTED,
-                 "propagation_mode 1 (serial heap order) is not on the GPU path; use 0 (frontier waves) or 2 (dataflow)");
+                 "no-allocation propagation: propagation_mode 0 (frontier waves) or 2 (dataflow) only (the heap order's "
+                 "rounds keep a result table and a tree per call)");
     const int w = pair->w, h = pair->h;
     const int step = std::max(0, cfg.propagation_spacing) + 1;
     int32_t gw, gh;
@@ -1473,14 +1488,15 @@ tdic_status tdic_batch_set_sms(tdic_batch* b, int32_t sms) {
     return guarded(b->ctx, [&] { batch_set_sms(b->plan.get(), sms); });
 }
 
-tdic_status tdic_batch_config(tdic_batch* b, int32_t* warps_per_poi, int32_t* groups_per_block) {
+tdic_status tdic_batch_config(tdic_batch* b, int32_t* warps_per_poi, int32_t* groups_per_block, int32_t* staging) {
     if (!b) return TDIC_INVALID_ARG;
     return guarded(b->ctx, [&] {
         TDIC_REQUIRE(warps_per_poi && groups_per_block, TDIC_INVALID_ARG, "null argument");
-        int g = 0, k = 0;
-        batch_config_info(b->plan.get(), b->config, &g, &k);
+        int g = 0, k = 0, st = 0;
+        batch_config_info(b->plan.get(), b->config, &g, &k, &st);
         *warps_per_poi = g;
         *groups_per_block = k;
+        if (staging) *staging = st;
     });
 }
 

@@ -1,7 +1,7 @@
 // External entry points of the hot path.  This unit holds the first-order ZNSSD kernels (route
-// 0) and the batched propagation; variants.cu is compiled once per other solver route (1: SSD,
-// 2: second order, 3: second-order SSD, 4: first-order ZNSSD on the generic solver, which masked
-// subsets use), so the routes build in parallel.  Routes 1-3 handle masked subsets themselves.
+// 0) of single pairs; batch.cu the batched propagation; variants.cu is compiled once per other
+// solver route (1: SSD, 2: second order, 3: second-order SSD, 4: first-order ZNSSD on the generic
+// solver, which masked subsets use), so the routes build in parallel.  Routes 1-3 handle masked subsets themselves.
 #include "hotpath.cuh"
 
 namespace tdic {
@@ -31,6 +31,22 @@ void upload_qk_constants() {
 void launch_init_grid(const tdic_grid_out& out, int gw, int gh, int step, cudaStream_t s) {
     const int n = gw * gh;
     init_grid_kernel<<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, s>>>(out, gw, gh, step);
+    TDIC_CUDA_TRY(cudaGetLastError());
+}
+
+void launch_emit_tree(const tdic_grid_out& out, int gw, int gh, int step, int precision, const void* params,
+                      const void* rcorr, const void* rq, const unsigned char* rmeta, const int* riters,
+                      const unsigned char* accepted, cudaStream_t s) {
+    const int n = gw * gh;
+    const int blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+    if (precision == TDIC_FP64)
+        emit_tree_kernel<double><<<blocks, 256, 0, s>>>(out, gw, gh, step, static_cast<const double*>(params),
+                                                         static_cast<const double*>(rcorr),
+                                                         static_cast<const double*>(rq), rmeta, riters, accepted);
+    else
+        emit_tree_kernel<float><<<blocks, 256, 0, s>>>(out, gw, gh, step, static_cast<const float*>(params),
+                                                        static_cast<const float*>(rcorr),
+                                                        static_cast<const float*>(rq), rmeta, riters, accepted);
     TDIC_CUDA_TRY(cudaGetLastError());
 }
 
@@ -64,67 +80,6 @@ void launch_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, co
         case 3: launch_propagate_route3(ctx, pair, cfg, L, s); break;
         case 4: launch_propagate_route4(ctx, pair, cfg, L, s); break;
         default: propagate_route<0>(ctx, pair, cfg, L, s); break;
-    }
-}
-
-std::unique_ptr<BatchPlanBase> batch_build(tdic_ctx* ctx, int n, tdic_pair* const* pairs, const tdic_config* cfgs,
-                                           const BatchSeed* seeds, const std::vector<std::vector<uint8_t>>& rois,
-                                           cudaStream_t s) {
-    if (pairs[0]->precision == TDIC_FP64) return batch_plan_build<double>(ctx, n, pairs, cfgs, seeds, rois, s);
-    return batch_plan_build<float>(ctx, n, pairs, cfgs, seeds, rois, s);
-}
-
-int batch_config_count(BatchPlanBase* p) {
-    if (auto* b = dynamic_cast<BatchPlan<double>*>(p)) return static_cast<int>(b->configs.size());
-    return static_cast<int>(static_cast<BatchPlan<float>*>(p)->configs.size());
-}
-
-void batch_launch(BatchPlanBase* p, int config, cudaStream_t s) {
-    if (auto* b = dynamic_cast<BatchPlan<double>*>(p)) batch_plan_launch(*b, config, s);
-    else batch_plan_launch(*static_cast<BatchPlan<float>*>(p), config, s);
-}
-
-template <typename T>
-void batch_read(BatchPlan<T>& b, int32_t* computed, int* err, cudaStream_t s) {
-    std::vector<int> flags(4 * static_cast<size_t>(b.n));
-    int e = 0;
-    TDIC_CUDA_TRY(cudaMemcpyAsync(flags.data(), b.d_flags.ptr, sizeof(int) * flags.size(), cudaMemcpyDeviceToHost, s));
-    TDIC_CUDA_TRY(cudaMemcpyAsync(&e, b.d_misc.template as<int>() + 12, sizeof(int), cudaMemcpyDeviceToHost, s));
-    TDIC_CUDA_TRY(cudaStreamSynchronize(s));
-    *err = e;
-    for (int j = 0; j < b.n; ++j)
-        computed[j] = (b.seed_ok[j] && !flags[4 * j + 1]) ? flags[4 * j + 2] : 0;
-}
-
-void batch_finish(BatchPlanBase* p, int32_t* computed, int* err, cudaStream_t s) {
-    if (auto* b = dynamic_cast<BatchPlan<double>*>(p)) batch_read(*b, computed, err, s);
-    else batch_read(*static_cast<BatchPlan<float>*>(p), computed, err, s);
-}
-
-tdic_grid_out batch_outputs(BatchPlanBase* p, int job) {
-    if (auto* b = dynamic_cast<BatchPlan<double>*>(p)) return b->outs[job];
-    return static_cast<BatchPlan<float>*>(p)->outs[job];
-}
-
-void batch_set_sms(BatchPlanBase* p, int sms) {
-    if (auto* b = dynamic_cast<BatchPlan<double>*>(p)) { b->sms = sms <= 0 ? b->num_sms : std::min(sms, b->num_sms); return; }
-    auto* f = static_cast<BatchPlan<float>*>(p);
-    f->sms = sms <= 0 ? f->num_sms : std::min(sms, f->num_sms);
-}
-
-void batch_grid(BatchPlanBase* p, int job, int32_t* gw, int32_t* gh) {
-    if (auto* b = dynamic_cast<BatchPlan<double>*>(p)) { *gw = b->gw[job]; *gh = b->gh[job]; return; }
-    auto* f = static_cast<BatchPlan<float>*>(p);
-    *gw = f->gw[job];
-    *gh = f->gh[job];
-}
-
-void batch_config_info(BatchPlanBase* p, int config, int* warps_per_poi, int* groups_per_block) {
-    if (auto* b = dynamic_cast<BatchPlan<double>*>(p)) {
-        *warps_per_poi = b->configs[config].G; *groups_per_block = b->configs[config].gpb;
-    } else {
-        auto* f = static_cast<BatchPlan<float>*>(p);
-        *warps_per_poi = f->configs[config].G; *groups_per_block = f->configs[config].gpb;
     }
 }
 

@@ -100,13 +100,41 @@ __device__ __forceinline__ T warp_scatter_sum(const T (&v)[K], int lane) {
 
 // All-reduce K values over the group: every thread ends with the same sums (summed in the same
 // order), so redundant scalar math stays bit-identical across the group's warps.  A warp
-// reduce-scatter, then thread k < K adds the G warp partials of value k, then everyone reads
-// the K totals.  `red` holds two buffers of 32*G values used alternately (parity `rp`): a
-// buffer is rewritten only after every thread has passed the barriers of the reduction in
-// between.
+// reduce-scatter writes each warp's K partials (rows of KS = K rounded up to 4 values, so a
+// row reads as 16-byte vectors), one barrier, then every thread adds the G partials of every
+// value in warp order itself (broadcast reads; no second barrier and no dependent round trip
+// through a K-thread sum).  `red` holds two buffers of 32*G values used alternately (parity
+// `rp`): a buffer is rewritten two reductions later, after every thread has passed the barrier
+// of the reduction in between, so its readers are done.
+template <int K, typename T>
+__device__ __forceinline__ void load_row(const T* row, T (&v)[K]) {
+    constexpr int KS = (K + 3) / 4 * 4;
+    if constexpr (sizeof(T) == 4 && K >= 8) {
+#pragma unroll
+        for (int k = 0; k < KS / 4; ++k) {
+            const float4 q = reinterpret_cast<const float4*>(row)[k];
+            if (4 * k + 0 < K) v[4 * k + 0] = q.x;
+            if (4 * k + 1 < K) v[4 * k + 1] = q.y;
+            if (4 * k + 2 < K) v[4 * k + 2] = q.z;
+            if (4 * k + 3 < K) v[4 * k + 3] = q.w;
+        }
+    } else if constexpr (sizeof(T) == 8 && K >= 8) {
+#pragma unroll
+        for (int k = 0; k < KS / 2; ++k) {
+            const double2 q = reinterpret_cast<const double2*>(row)[k];
+            if (2 * k + 0 < K) v[2 * k + 0] = q.x;
+            if (2 * k + 1 < K) v[2 * k + 1] = q.y;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < K; ++k) v[k] = row[k];
+    }
+}
+
 template <int G, int K, typename T>
 __device__ __forceinline__ void group_sum(T (&v)[K], T* red_base, int& rp, int tid, int bar_id) {
-    static_assert(G == 1 || K * (G + 1) <= 32 * G, "reduction scratch: G*K partials + K totals per buffer");
+    constexpr int KS = (K + 3) / 4 * 4;
+    static_assert(G == 1 || KS <= 32, "reduction scratch: G rows of KS partials per buffer");
     constexpr int LG = Pow2Ceil<K>::log2;
     const int lane = tid & 31;
     const T r = warp_scatter_sum<K, T>(v, lane);
@@ -116,20 +144,18 @@ __device__ __forceinline__ void group_sum(T (&v)[K], T* red_base, int& rp, int t
         for (int k = 0; k < K; ++k) v[k] = __shfl_sync(0xffffffffu, r, k << (5 - LG));
     } else {
         T* red = red_base + rp * 32 * G;
-        T* tot = red + G * K;
         rp ^= 1;
         const int warp = tid >> 5;
-        if ((lane & ((1 << (5 - LG)) - 1)) == 0 && idx < K) red[warp * K + idx] = r;
+        if ((lane & ((1 << (5 - LG)) - 1)) == 0 && idx < K) red[warp * KS + idx] = r;
         named_bar(bar_id, 32 * G);
-        if (tid < K) {
-            T acc = red[tid];
+        load_row<K, T>(red, v);
 #pragma unroll
-            for (int w = 1; w < G; ++w) acc += red[w * K + tid];
-            tot[tid] = acc;
+        for (int w = 1; w < G; ++w) {
+            T part[K];
+            load_row<K, T>(red + w * KS, part);
+#pragma unroll
+            for (int k = 0; k < K; ++k) v[k] += part[k];
         }
-        named_bar(bar_id, 32 * G);
-#pragma unroll
-        for (int k = 0; k < K; ++k) v[k] = tot[k];
     }
 }
 
@@ -336,6 +362,13 @@ __device__ __forceinline__ void dweights(T t, T (&w)[DEG + 1]) {
     }
 }
 
+// Shared-memory staging modes of a solve (bits; see group_smem_bytes) and the per-sample arrays
+// each keeps.
+enum { kStageFull = 0, kStageLean = 1, kStageNoCoefWindow = 2 };
+__host__ __device__ __forceinline__ int sample_arrays(int opt, int stage) {
+    return (stage & kStageLean) ? (opt == 1 ? 3 : 1) : 4;
+}
+
 template <typename T>
 struct Env {
     const float* ref;      // H x W float32 reference
@@ -354,6 +387,10 @@ struct Env {
     // min_keep = max(NP, min_valid_samples, ceil(min_valid_sample_ratio * n))
     const uint8_t* roi;
     int min_keep;
+    // shared-memory staging of the single-pair kernels (a batched launch takes its own from
+    // the launch's Shape): kStage* bits and the per-sample arrays it keeps
+    int stage = kStageFull;
+    int narr = 4;
 };
 
 // Per-POI result in the solve's own precision (float on the FP32-mixed path); outputs are
@@ -844,16 +881,27 @@ __host__ __device__ __forceinline__ size_t round128(size_t b) { return (b + 127)
 // Per-group shared memory, each part 128-byte aligned (TMA destinations):
 // [coefficient window cbx*cby T][reference window rbx*rby float][mbarrier + matrix region of
 // `mat` doubles (the 6x6 inverse: 36; second order: the 12x12 factor and inverse) + ints]
-// [2 x 32*G T reduction scratch][4*nmax T samples f^, a, b, g].
+// [2 x 32*G T reduction scratch][narr*nmax T per-sample arrays].
+//
+// Staging modes (a layout choice only: the results are the same bit for bit):
+//   full (0)        the coefficient window and four per-sample arrays: f^, the two gradients
+//                   (ICGN: reference gradients; FGN: deformed spline gradients) and g;
+//   lean (1)        the per-sample arrays the iterations write (ICGN: g; FGN: g and the two
+//                   deformed gradients); f^ and the reference gradients are recomputed from the
+//                   staged reference window when they are read;
+//   lean, no coefficient window (3)   as lean, and every spline stencil is read from the
+//                   L2-resident coefficient image instead of a staged window.
+// Lean staging is the first-order ZNSSD solver's (route 0); it lets large subsets fit (FP64 at
+// radius 41) and more solver groups share an SM.
 constexpr int kMat6 = 36;
 constexpr int kMat12 = 2 * 144 + 12 + 52;  // factor, inverse (or copy), 1 / D, the 45 Hessian sums
 template <typename T>
 __host__ __device__ __forceinline__ size_t group_smem_bytes(int nmax, int G, int rbx, int rby, int cbx, int cby,
-                                                            int mat = kMat6) {
-    size_t b = round128(static_cast<size_t>(cbx) * cby * sizeof(T));
+                                                            int mat = kMat6, int stage = kStageFull, int narr = 4) {
+    size_t b = (stage & kStageNoCoefWindow) ? 0 : round128(static_cast<size_t>(cbx) * cby * sizeof(T));
     b += round128(static_cast<size_t>(rbx) * rby * sizeof(float));
     b += round128(16 + static_cast<size_t>(mat) * sizeof(double) + 16);
-    b += round128((static_cast<size_t>(64) * G + static_cast<size_t>(4) * nmax) * sizeof(T));
+    b += round128((static_cast<size_t>(64) * G + static_cast<size_t>(narr) * nmax) * sizeof(T));
     return b;
 }
 // CTA prefix: the sample-offset table shared by all groups.
@@ -861,18 +909,24 @@ __host__ __device__ __forceinline__ size_t cta_prefix_bytes(int nmax) { return r
 
 template <typename T>
 struct GroupSmem {
-    T* cwin;
+    T* cwin;       // nullptr without a coefficient window
     float* rwin;
     uint64_t* bar;
     double* hinv;
     int* ints;
     T* red;
     T* sm;
+    int stage;
     __device__ GroupSmem(unsigned char* base, int gi, int nmax, int G, int rbx, int rby, int cbx, int cby,
-                         int mat = kMat6) {
-        unsigned char* g = base + gi * group_smem_bytes<T>(nmax, G, rbx, rby, cbx, cby, mat);
-        cwin = reinterpret_cast<T*>(g);
-        g += round128(static_cast<size_t>(cbx) * cby * sizeof(T));
+                         int mat = kMat6, int stage_ = kStageFull, int narr = 4) {
+        stage = stage_;
+        unsigned char* g = base + gi * group_smem_bytes<T>(nmax, G, rbx, rby, cbx, cby, mat, stage_, narr);
+        if (stage_ & kStageNoCoefWindow) {
+            cwin = nullptr;
+        } else {
+            cwin = reinterpret_cast<T*>(g);
+            g += round128(static_cast<size_t>(cbx) * cby * sizeof(T));
+        }
         rwin = reinterpret_cast<float*>(g);
         g += round128(static_cast<size_t>(rbx) * rby * sizeof(float));
         bar = reinterpret_cast<uint64_t*>(g);
@@ -895,7 +949,7 @@ template <int DEG, typename T, bool GRAD, int NP = 6, bool SUMS = true>
 __device__ __forceinline__ bool warp_interp(const Env<T>& e, int cx, int cy, const T (&p)[NP], T fm, T* s_g, T* s_gx,
                                             T* s_gy, const short2* off, const T* cwin, int wc0, int wr0, int tid,
                                             int nt, Kahan<T>& sg, Kahan<T>& sg2, const T* s_chk = nullptr) {
-    const int ww = e.cbx, wh = e.cby;
+    const int ww = cwin ? e.cbx : 0, wh = cwin ? e.cby : 0;  // no window: every stencil from global memory
     constexpr int NB = DEG + 1, OFF = DEG / 2;
     bool ok = true;
     const T xlo = T(-cx), ylo = T(-cy), xhi = T(e.w - 1 - cx), yhi = T(e.h - 1 - cy);
@@ -1019,9 +1073,10 @@ __device__ __forceinline__ bool stage_windows(const Env<T>& e, const CUtensorMap
     group_sync<G>(bar_id);  // previous readers of the windows are done
     if (tid == 0) {
         fence_proxy_async();
-        mbar_expect_tx(gs.bar, static_cast<uint32_t>(e.rbx * e.rby * sizeof(float) + e.cbx * e.cby * sizeof(T)));
+        mbar_expect_tx(gs.bar, static_cast<uint32_t>(e.rbx * e.rby * sizeof(float) +
+                                                     (gs.cwin ? e.cbx * e.cby * sizeof(T) : 0)));
         tma_load_2d(gs.rwin, tm_ref, rx0, ry0, gs.bar);
-        tma_load_2d(gs.cwin, tm_coef, wc0, wr0, gs.bar);
+        if (gs.cwin) tma_load_2d(gs.cwin, tm_coef, wc0, wr0, gs.bar);
     }
     long long spins = 0;
     while (!mbar_try_wait(gs.bar, phase)) {
@@ -1032,6 +1087,24 @@ __device__ __forceinline__ bool stage_windows(const Env<T>& e, const CUtensorMap
     }
     phase ^= 1u;
     return true;
+}
+
+// Products that must round on their own (no contraction into a following add), so that a value
+// recomputed in a register equals the one the full staging mode stores and reloads.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
+// Reference sample at (x, y) from the staged reference window: the raw value and the gradient of
+// the reference gradient cache (reliability_propagation.cpp:84-112: central differences, one-sided
+// at the image border; multiplying by 0.5 or 1 is exact).
+template <typename T>
+__device__ __forceinline__ void ref_gradient(const float* rwin, int rww, int rx0, int ry0, int W, int H, int x, int y,
+                                             T& a, T& b) {
+    const int xm = max(0, x - 1), xp = min(W - 1, x + 1), ym = max(0, y - 1), yp = min(H - 1, y + 1);
+    a = (T(rwin[(y - ry0) * rww + (xp - rx0)]) - T(rwin[(y - ry0) * rww + (xm - rx0)])) *
+        (xp - xm == 2 ? T(0.5) : T(1));
+    b = (T(rwin[(yp - ry0) * rww + (x - rx0)]) - T(rwin[(ym - ry0) * rww + (x - rx0)])) *
+        (yp - ym == 2 ? T(0.5) : T(1));
 }
 
 // The per-POI solve.  OPT 0 = ICGN (icgn.cpp:446-627), 1 = FGN (forward_gauss_newton.cpp:188-399).
@@ -1053,10 +1126,12 @@ __device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUte
     if (e.w <= 0 || r < 1 || e.max_iter < 0) return true;
     if (cx - r < 0 || cy - r < 0 || cx + r >= e.w || cy + r >= e.h) return true;
     if (e.n < 6) return true;
-    T* s_fn = gs.sm;
-    T* s_a = gs.sm + e.nmax;      // ICGN: reference gx; FGN: deformed gx
-    T* s_b = gs.sm + 2 * e.nmax;  // ICGN: reference gy; FGN: deformed gy
-    T* s_g = gs.sm + 3 * e.nmax;
+    // per-sample arrays (full staging: f^, gradients, g; lean: what the iterations write)
+    const bool lean = (gs.stage & kStageLean) != 0;
+    T* s_fn = lean ? nullptr : gs.sm;
+    T* s_a = lean ? (OPT == 1 ? gs.sm : nullptr) : gs.sm + e.nmax;            // ICGN: reference gx; FGN: deformed gx
+    T* s_b = lean ? (OPT == 1 ? gs.sm + e.nmax : nullptr) : gs.sm + 2 * e.nmax;  // ICGN: reference gy; FGN: deformed gy
+    T* s_g = lean ? (OPT == 1 ? gs.sm + 2 * e.nmax : gs.sm) : gs.sm + 3 * e.nmax;
     const int W = e.w, H = e.h;
 
     int rx0, ry0, wc0, wr0;
@@ -1074,20 +1149,17 @@ __device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUte
         const short2 o = off[i];
         const int x = cx + o.x, y = cy + o.y;
         const float f = gs.rwin[(y - ry0) * rww + (x - rx0)];
-        s_fn[i] = T(f);
+        if (!lean) s_fn[i] = T(f);
         const T fd = T(f) - T(fshift);
         k1.add(fd);
         k2.add(fd * fd);
         if constexpr (OPT == 0) {
-            // reference gradient cache, reliability_propagation.cpp:84-112
-            const int xm = max(0, x - 1), xp = min(W - 1, x + 1), ym = max(0, y - 1), yp = min(H - 1, y + 1);
-            // the divisor is 1 (one-sided) or 2 (central): multiplying by 1 or 0.5 is exact
-            const T a = (T(gs.rwin[(y - ry0) * rww + (xp - rx0)]) - T(gs.rwin[(y - ry0) * rww + (xm - rx0)])) *
-                        (xp - xm == 2 ? T(0.5) : T(1));
-            const T b = (T(gs.rwin[(yp - ry0) * rww + (x - rx0)]) - T(gs.rwin[(ym - ry0) * rww + (x - rx0)])) *
-                        (yp - ym == 2 ? T(0.5) : T(1));
-            s_a[i] = a;
-            s_b[i] = b;
+            T a, b;
+            ref_gradient<T>(gs.rwin, rww, rx0, ry0, W, H, x, y, a, b);
+            if (!lean) {
+                s_a[i] = a;
+                s_b[i] = b;
+            }
             const T lx = T(o.x), ly = T(o.y);
             const T q[3] = {a * a, a * b, b * b};
             const T m6[6] = {T(1), lx, ly, lx * lx, lx * ly, ly * ly};
@@ -1120,7 +1192,8 @@ __device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUte
     if (!(ss > M(kEps * kEps))) { R.status = TDIC_NUMERICAL_FAILURE; return true; }  // |f - mean| <= 1e-12
     const T fm = T(M(fshift) + mshift);
     const T inv_norm = T(1) / sqrt(T(ss));
-    for (int i = tid; i < e.n; i += NT) s_fn[i] = (s_fn[i] - fm) * inv_norm;
+    if (!lean)
+        for (int i = tid; i < e.n; i += NT) s_fn[i] = mul_rn(s_fn[i] - fm, inv_norm);
     if constexpr (OPT == 0) {
         M S[18];
 #pragma unroll
@@ -1160,13 +1233,29 @@ __device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUte
             T q[7];
 #pragma unroll
             for (int k = 0; k < 7; ++k) q[k] = T(0);
-            for (int i = tid; i < e.n; i += NT) {
-                const short2 o = off[i];
-                const T lx = T(o.x), ly = T(o.y);
-                const T diff = s_fn[i] - ((s_g[i] - fm) - gsh) * inv_gn;
-                const T da = diff * s_a[i], db = diff * s_b[i];
-                q[0] += da; q[1] += db; q[2] += da * lx; q[3] += da * ly; q[4] += db * lx; q[5] += db * ly;
-                q[6] += diff * diff;
+            if (!lean) {
+                for (int i = tid; i < e.n; i += NT) {
+                    const short2 o = off[i];
+                    const T lx = T(o.x), ly = T(o.y);
+                    const T diff = s_fn[i] - ((s_g[i] - fm) - gsh) * inv_gn;
+                    const T da = diff * s_a[i], db = diff * s_b[i];
+                    q[0] += da; q[1] += db; q[2] += da * lx; q[3] += da * ly; q[4] += db * lx; q[5] += db * ly;
+                    q[6] += diff * diff;
+                }
+            } else {
+                // f^ and the reference gradients from the staged window, as the set-up made them
+                for (int i = tid; i < e.n; i += NT) {
+                    const short2 o = off[i];
+                    const int x = cx + o.x, y = cy + o.y;
+                    const T lx = T(o.x), ly = T(o.y);
+                    const T fn = mul_rn(T(gs.rwin[(y - ry0) * rww + (x - rx0)]) - fm, inv_norm);
+                    T a, b;
+                    ref_gradient<T>(gs.rwin, rww, rx0, ry0, W, H, x, y, a, b);
+                    const T diff = fn - ((s_g[i] - fm) - gsh) * inv_gn;
+                    const T da = diff * a, db = diff * b;
+                    q[0] += da; q[1] += db; q[2] += da * lx; q[3] += da * ly; q[4] += db * lx; q[5] += db * ly;
+                    q[6] += diff * diff;
+                }
             }
             group_sum<G, 7>(q, red, rp, tid, bar_id);
             corr = static_cast<M>(q[6]);
@@ -1192,7 +1281,9 @@ __device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUte
                 const T gx = s_a[i], gy = s_b[i];
                 const T ae = gx * (T(1) + p2) + gy * p4;
                 const T be = gx * p3 + gy * (T(1) + p5);
-                const T diff = s_fn[i] - ((s_g[i] - fm) - gsh) * inv_gn;
+                const T fn = lean ? mul_rn(T(gs.rwin[(cy + o.y - ry0) * rww + (cx + o.x - rx0)]) - fm, inv_norm)
+                                  : s_fn[i];
+                const T diff = fn - ((s_g[i] - fm) - gsh) * inv_gn;
                 const T qq[3] = {ae * ae, ae * be, be * be};
                 const T m6[6] = {T(1), lx, ly, lx * lx, lx * ly, ly * ly};
 #pragma unroll
@@ -1680,16 +1771,19 @@ struct Shape {
     int nmax, rbx, rby, cbx, cby;
     int total;
     int mat = kMat6;  // doubles of each group's matrix region
+    int stage = kStageFull;  // staging mode of the groups' shared memory
+    int narr = 4;            // per-sample arrays of each group (sample_arrays)
 };
 
 template <typename T>
 __host__ __device__ inline Shape shape_of(const Env<T>& e, int total, int mat = kMat6) {
-    return Shape{e.off, e.n, e.nmax, e.rbx, e.rby, e.cbx, e.cby, total, mat};
+    return Shape{e.off, e.n, e.nmax, e.rbx, e.rby, e.cbx, e.cby, total, mat, e.stage, e.narr};
 }
 
 template <typename T, int G>
 __device__ __forceinline__ GroupSmem<T> group_smem(unsigned char* smem_raw, const Shape& sh, int gi) {
-    return GroupSmem<T>(smem_raw + cta_prefix_bytes(sh.ntab), gi, sh.nmax, G, sh.rbx, sh.rby, sh.cbx, sh.cby, sh.mat);
+    return GroupSmem<T>(smem_raw + cta_prefix_bytes(sh.ntab), gi, sh.nmax, G, sh.rbx, sh.rby, sh.cbx, sh.cby, sh.mat,
+                        sh.stage, sh.narr);
 }
 
 // Kernel preamble: copy the sample-offset tables into shared memory (CTA-wide) and initialise
@@ -1781,9 +1875,20 @@ struct PropEnv {
     int* dcnt;                    // parents resolved so far
     unsigned long long* dq;       // queue items: parent (high 32, -1 = orphan) : point (low 32)
     float* kcorr;                 // ZNSSD of accepted points (wave keys of the clean-up)
+    // explicit tree (mode 3, a round of the heap order): every queued point is solved from its
+    // tree parent and its tree children are queued after it; the raw result of every solve
+    // (accepted or not) goes to the result table, the host decides acceptance
+    const int* tchild_off;        // children of point n: tchild[tchild_off[n] .. tchild_off[n+1])
+    const int* tchild;
+    const int* tcont;             // the child the solving group continues with (-1: none)
+    void* rcorr;                  // correlation of each solve, in the solve's precision
+    void* rq;                     // second-order terms of each solve (6 per point), or NULL
+    unsigned char* rmeta;         // status | valid << 2 | converged << 3
+    int* riters;                  // iterations of each solve
 };
 
 enum { kDfPending = 0, kDfAccepted = 2, kDfRejected = 3, kDfOrphan = 4 };
+enum { kModeWaves = 0, kModeDataflow = 2, kModeTree = 3 };
 
 // A launch over several jobs (image pairs) tags the grid points of its queue items and wave
 // lists with the job: point index in the low kJobShift bits, job above.
@@ -2030,6 +2135,18 @@ __device__ void df_resolve(const PropEnv& pe, int n, bool accepted, int self_in_
     df_publish(pe, push, k2, k2 - (self_in_flight - handed));
 }
 
+// Tree mode: n has been solved; queue its tree children except `cont` (which the solving group
+// continues with and which inherits n's in-flight count).
+__device__ void tree_resolve(const PropEnv& pe, int n, int cont) {
+    unsigned long long push[4];
+    int k = 0;
+    for (int i = pe.tchild_off[n]; i < pe.tchild_off[n + 1] && k < 4; ++i) {
+        const int c = pe.tchild[i];
+        if (c != cont) push[k++] = df_item(n, c | pe.jtag);
+    }
+    df_publish(pe, push, k, k - (cont >= 0 ? 0 : 1));
+}
+
 // Propagation groups: 4 warps per POI, two groups and one resolver warp per CTA, two CTAs per
 // SM.  Per-POI latency on the dataflow critical path bounds the propagation; measured on
 // 2048^2, r = 15: 8 warps per POI were 14% slower (the two-stage group reductions and barriers
@@ -2046,6 +2163,7 @@ struct DfSlot {
     int want;    // 1: the group waits for a queued item
     int ready;   // 1: item in (c, par); 2: propagation finished; 3: error
     int n, state, cont, iters, conv;
+    int status, valid;  // the raw solve outcome (tree mode)
     int c, par;
     P p[6];
     P q[6];  // second-order terms
@@ -2119,16 +2237,27 @@ __device__ void df_resolver_lane(const Src& src, DfSlot<P>* slot, int* s_done, i
             R.corr = slot->corr;
             R.iters = slot->iters;
             R.conv = slot->conv != 0;
-            const bool acc = st == kDfAccepted;
-            if (acc) {
+            if (pe.mode == kModeTree) {
+                // every solve's raw result; the host's heap simulation decides acceptance
                 store_params(params, n, R);
-                pe.kcorr[n] = static_cast<float>(R.corr);
-            }
-            pe.dstate[n] = st;
-            df_resolve(pe, n, acc, 1, cont);
-            if (acc) {
-                store_outputs<P, SO>(pe, n, R);
-                atomicAdd(pe.flags + 2, 1);
+                reinterpret_cast<P*>(pe.rcorr)[n] = R.corr;
+                if constexpr (SO)
+                    for (int k = 0; k < 6; ++k) reinterpret_cast<P*>(pe.rq)[static_cast<size_t>(n) * 6 + k] = R.q[k];
+                pe.rmeta[n] = static_cast<unsigned char>((slot->status & 3) | (slot->valid ? 4 : 0) | (R.conv ? 8 : 0));
+                pe.riters[n] = R.iters;
+                tree_resolve(pe, n, cont);
+            } else {
+                const bool acc = st == kDfAccepted;
+                if (acc) {
+                    store_params(params, n, R);
+                    pe.kcorr[n] = static_cast<float>(R.corr);
+                }
+                pe.dstate[n] = st;
+                df_resolve(pe, n, acc, 1, cont);
+                if (acc) {
+                    store_outputs<P, SO>(pe, n, R);
+                    atomicAdd(pe.flags + 2, 1);
+                }
             }
             __threadfence_block();
             vst(&slot->post, 0);
@@ -2213,7 +2342,7 @@ __device__ __forceinline__ void propagate_body(const Src& src, const Shape& sh) 
     const int bar_id = 1 + gi;
     uint32_t phase = 0;
     unsigned char* ctl = smem_raw + cta_prefix_bytes(sh.ntab) +
-                         gpb * group_smem_bytes<T>(sh.nmax, G, sh.rbx, sh.rby, sh.cbx, sh.cby, sh.mat);
+                         gpb * group_smem_bytes<T>(sh.nmax, G, sh.rbx, sh.rby, sh.cbx, sh.cby, sh.mat, sh.stage, sh.narr);
     DfSlot<P>* slots = reinterpret_cast<DfSlot<P>*>(ctl);
     int* s_done = reinterpret_cast<int*>(ctl + round128(gpb * sizeof(DfSlot<P>)));
     if (threadIdx.x < gpb) {
@@ -2271,7 +2400,7 @@ __device__ __forceinline__ void propagate_body(const Src& src, const Shape& sh) 
     if (!grid_barrier(g.barrier, g.err, g.counters)) return;
     if (one && *reinterpret_cast<volatile int*>(g.flags + 1)) return;
 
-    if (g.mode == 2) {
+    if (g.mode == kModeDataflow || g.mode == kModeTree) {
         // ---- dataflow phase: no grid-wide synchronisation ------------------------------------
         if (solver) {
             DfSlot<P>* slot = slots + gi;
@@ -2313,6 +2442,10 @@ __device__ __forceinline__ void propagate_body(const Src& src, const Shape& sh) 
                 Result<P> R;
                 R.iters = 0;
                 R.conv = false;
+                R.status = TDIC_INVALID_INPUT;
+                R.valid = false;
+                R.corr = P(0);
+                for (int k = 0; k < 6; ++k) R.p[k] = R.q[k] = P(0);
                 if (item_p >= 0) {
                     const bool admissible = pe.roi_grid[n] != 0 && nx - e.radius >= 0 && ny - e.radius >= 0 &&
                                             nx + e.radius < e.w && ny + e.radius < e.h;
@@ -2337,7 +2470,7 @@ __device__ __forceinline__ void propagate_body(const Src& src, const Shape& sh) 
                         if (accepted) new_state = kDfAccepted;
                     }
                 }
-                const int next = df_pick_cont(pe, n, accepted);
+                const int next = pe.mode == kModeTree ? pe.tcont[n] : df_pick_cont(pe, n, accepted);
                 if (tid == 0) {
                     // hand n to the resolver lane (its slot holds one point; normally long free)
                     unsigned long long spins = 0;
@@ -2347,6 +2480,7 @@ __device__ __forceinline__ void propagate_body(const Src& src, const Shape& sh) 
                     }
                     slot->n = item_c; slot->state = new_state; slot->cont = next;
                     slot->iters = R.iters; slot->conv = R.conv ? 1 : 0;
+                    slot->status = R.status; slot->valid = R.valid ? 1 : 0;
                     for (int k = 0; k < 6; ++k) slot->p[k] = R.p[k];
                     if constexpr ((VAR & 2) != 0)
                         for (int k = 0; k < 6; ++k) slot->q[k] = R.q[k];
@@ -2364,6 +2498,7 @@ __device__ __forceinline__ void propagate_body(const Src& src, const Shape& sh) 
             if (lane < gpb) df_resolver_lane<P, Src, (VAR & 2) != 0>(src, slots + lane, s_done, sh.total);
             __syncwarp();
         }
+        if (g.mode == kModeTree) return;  // a tree round ends with its queue: no clean-up waves
         if (!grid_barrier(g.barrier, g.err)) return;
         // ---- clean-up: orphans are reached by frontier waves from every accepted point ------
         for (int j = 0; j < src.count(); ++j) {
@@ -2469,6 +2604,43 @@ __global__ void init_grid_kernel(tdic_grid_out o, int gw, int gh, int step) {
     }
 }
 
+// The grid outputs of a heap-order propagation: the raw result of each point the host's heap
+// simulation accepted (reliability_propagation.cpp:359-368: stored with status Success and
+// valid), the defaults of init_grid_kernel elsewhere.
+template <typename P>
+__global__ void emit_tree_kernel(tdic_grid_out o, int gw, int gh, int step, const P* params, const P* rcorr,
+                                 const P* rq, const unsigned char* rmeta, const int* riters,
+                                 const unsigned char* accepted) {
+    const int n = gw * gh;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const bool a = accepted[i] != 0;
+        const size_t b6 = static_cast<size_t>(i) * 6;
+        auto pv = [&](int k) { return a ? static_cast<double>(params[b6 + k]) : 0.0; };
+        auto qv = [&](int k) { return (a && rq) ? static_cast<double>(rq[b6 + k]) : 0.0; };
+        const double corr = a ? static_cast<double>(rcorr[i]) : 0.0;
+        if (o.x) o.x[i] = static_cast<double>((i % gw) * step);
+        if (o.y) o.y[i] = static_cast<double>((i / gw) * step);
+        if (o.u) o.u[i] = pv(0);
+        if (o.v) o.v[i] = pv(1);
+        if (o.du_dx) o.du_dx[i] = pv(2);
+        if (o.du_dy) o.du_dy[i] = pv(3);
+        if (o.dv_dx) o.dv_dx[i] = pv(4);
+        if (o.dv_dy) o.dv_dy[i] = pv(5);
+        if (o.correlation) o.correlation[i] = corr;
+        if (o.zncc) o.zncc[i] = a ? fmax(-1.0, fmin(1.0, 1.0 - 0.5 * corr)) : 1.0;
+        if (o.valid) o.valid[i] = a ? 1 : 0;
+        if (o.status) o.status[i] = a ? TDIC_SUCCESS : TDIC_INVALID_INPUT;
+        if (o.iterations) o.iterations[i] = a ? riters[i] : 0;
+        if (o.converged) o.converged[i] = (a && (rmeta[i] & 8)) ? 1 : 0;
+        if (o.d2u_dx2) o.d2u_dx2[i] = qv(0);
+        if (o.d2u_dxdy) o.d2u_dxdy[i] = qv(1);
+        if (o.d2u_dy2) o.d2u_dy2[i] = qv(2);
+        if (o.d2v_dx2) o.d2v_dx2[i] = qv(3);
+        if (o.d2v_dxdy) o.d2v_dxdy[i] = qv(4);
+        if (o.d2v_dy2) o.d2v_dy2[i] = qv(5);
+    }
+}
+
 // ---------------------------------------------------------------------------------------
 // Dispatch
 // ---------------------------------------------------------------------------------------
@@ -2557,6 +2729,59 @@ TensorMaps make_tensor_maps(const tdic_pair* pair, const Env<T>& e) {
     return t;
 }
 
+// Shared-memory staging of a launch: each mode the request allows (tdic_staging; routes other
+// than first-order ZNSSD stage in full) with its groups per block (at most gpb_max, shrunk until
+// the block fits) and resident blocks per SM.  The mode with the most resident solver groups
+// wins, the fullest staging among equals.  The kernel's dynamic shared-memory attribute is left
+// at the chosen size (raised only, when `raise_only`: a batch keeps one bound for all its
+// configurations).
+struct StageChoice {
+    int stage = -1, narr = 4, gpb = 0, per_sm = 0;
+    size_t smem = 0;
+};
+
+template <typename T, typename K>
+StageChoice choose_staging(tdic_ctx* ctx, K kern, int requested, bool lean_ok, int opt, int nmax, int G, int rbx,
+                           int rby, int cbx, int cby, int mat, size_t prefix, size_t ctl, int gpb_max,
+                           int extra_threads, bool raise_only = false) {
+    int cands[3], nc = 0;
+    if (!lean_ok || requested == TDIC_STAGING_FULL) {
+        cands[nc++] = kStageFull;
+    } else if (requested == TDIC_STAGING_LEAN) {
+        cands[nc++] = kStageLean;
+    } else if (requested == TDIC_STAGING_LEAN_NO_WINDOW) {
+        cands[nc++] = kStageLean | kStageNoCoefWindow;
+    } else {
+        cands[nc++] = kStageFull;
+        cands[nc++] = kStageLean;
+        cands[nc++] = kStageLean | kStageNoCoefWindow;
+    }
+    StageChoice best;
+    cudaFuncAttributes fa{};
+    TDIC_CUDA_TRY(cudaFuncGetAttributes(&fa, kern));
+    int attr = fa.maxDynamicSharedSizeBytes;
+    for (int c = 0; c < nc; ++c) {
+        const int stage = cands[c], narr = sample_arrays(opt, stage);
+        const size_t per_group = group_smem_bytes<T>(nmax, G, rbx, rby, cbx, cby, mat, stage, narr);
+        int gpb = gpb_max;
+        while (gpb > 1 && prefix + gpb * per_group + ctl > static_cast<size_t>(ctx->max_smem_optin)) --gpb;
+        const size_t smem = prefix + gpb * per_group + ctl;
+        if (smem > static_cast<size_t>(ctx->max_smem_optin)) continue;
+        if (static_cast<int>(smem) > attr) {
+            TDIC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+            attr = static_cast<int>(smem);
+        }
+        int per_sm = 0;
+        TDIC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * G * gpb + extra_threads, smem));
+        if (per_sm <= 0) continue;
+        if (best.stage < 0 || per_sm * gpb > best.per_sm * best.gpb) best = StageChoice{stage, narr, gpb, per_sm, smem};
+    }
+    TDIC_REQUIRE(best.stage >= 0, TDIC_UNSUPPORTED, "subset radius too large for shared memory");
+    if (!raise_only)
+        TDIC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(best.smem)));
+    return best;
+}
+
 constexpr int kGroupsPerBlockBatch = 4;  // 4 warps of 1-warp groups
 
 template <int OPT, int DEG, typename T, int VAR = 0>
@@ -2565,23 +2790,18 @@ void solve_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const S
     Env<T> e = make_env<T>(ctx, pair, cfg, cfg.subset_radius, cfg.max_iterations, cfg.convergence_threshold,
                            nullptr, 0, L.roi);
     const TensorMaps tm = make_tensor_maps<T>(pair, e);
-    const size_t per_group = group_smem_bytes<T>(e.nmax, G, e.rbx, e.rby, e.cbx, e.cby, (VAR & 2) ? kMat12 : kMat6);
-    const size_t prefix = cta_prefix_bytes(e.nmax);
-    int gpb = kGroupsPerBlockBatch;
-    while (gpb > 1 && prefix + gpb * per_group > static_cast<size_t>(ctx->max_smem_optin)) --gpb;
-    TDIC_REQUIRE(prefix + per_group <= static_cast<size_t>(ctx->max_smem_optin), TDIC_UNSUPPORTED,
-                 "subset radius too large for shared memory");
-    const size_t smem = prefix + gpb * per_group;
     auto kern = solve_batch_kernel<OPT, DEG, T, G, VAR>;
-    TDIC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-    int per_sm = 0;
-    TDIC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * G * gpb, smem));
-    TDIC_REQUIRE(per_sm > 0, TDIC_UNSUPPORTED, "subset radius too large for shared memory");
-    int blocks = per_sm * ctx->num_sms;
+    const StageChoice sc = choose_staging<T>(ctx, kern, cfg.staging, VAR == 0, OPT, e.nmax, G, e.rbx, e.rby, e.cbx,
+                                             e.cby, (VAR & 2) ? kMat12 : kMat6, cta_prefix_bytes(e.nmax), 0,
+                                             kGroupsPerBlockBatch, 0);
+    e.stage = sc.stage;
+    e.narr = sc.narr;
+    const int gpb = sc.gpb;
+    int blocks = sc.per_sm * ctx->num_sms;
     const int need = (L.n + gpb - 1) / gpb;
     if (blocks > need) blocks = need < 1 ? 1 : need;
     TDIC_CUDA_TRY(cudaMemsetAsync(L.fetch, 0, sizeof(int), s));
-    kern<<<blocks, 32 * G * gpb, smem, s>>>(e, tm.ref, tm.coef, L.in, L.out, L.n, L.fetch);
+    kern<<<blocks, 32 * G * gpb, sc.smem, s>>>(e, tm.ref, tm.coef, L.in, L.out, L.n, L.fetch);
     TDIC_CUDA_TRY(cudaGetLastError());
 }
 
@@ -2600,23 +2820,17 @@ void propagate_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, con
     Env<T> e = make_env<T>(ctx, pair, cfg, cfg.subset_radius, cfg.max_iterations, cfg.convergence_threshold,
                            L.offsets, L.n_offsets, L.roi_px);
     TensorMaps tm = make_tensor_maps<T>(pair, e);
-    const size_t per_group =
-        group_smem_bytes<T>(e.nmax, G, e.rbx, e.rby, e.cbx, e.cby, (VAR & 2) ? kMat12 : kMat6);
-    const size_t prefix = cta_prefix_bytes(e.nmax);
-    int gpb = kPropGroupsPerBlock;
     using P = typename MixedOf<T>::type;
     const size_t ctl = round128(kPropGroupsPerBlock * sizeof(DfSlot<P>)) + 128;  // resolver hand-over
-    while (gpb > 1 && prefix + gpb * per_group + ctl > static_cast<size_t>(ctx->max_smem_optin)) --gpb;
-    TDIC_REQUIRE(prefix + per_group + ctl <= static_cast<size_t>(ctx->max_smem_optin), TDIC_UNSUPPORTED,
-                 "subset radius too large for shared memory");
-    const size_t smem = prefix + gpb * per_group + ctl;
-    const int threads = 32 * G * gpb + 32;  // solver groups + the resolver warp
     auto kern = propagate_kernel<OPT, DEG, T, G, VAR>;
-    TDIC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-    int per_sm = 0;
-    TDIC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
-    TDIC_REQUIRE(per_sm > 0, TDIC_UNSUPPORTED, "subset radius too large for shared memory");
-    const int blocks = per_sm * ctx->num_sms;
+    const StageChoice sc = choose_staging<T>(ctx, kern, cfg.staging, VAR == 0, OPT, e.nmax, G, e.rbx, e.rby, e.cbx,
+                                             e.cby, (VAR & 2) ? kMat12 : kMat6, cta_prefix_bytes(e.nmax), ctl,
+                                             kPropGroupsPerBlock, 32);
+    e.stage = sc.stage;
+    e.narr = sc.narr;
+    const size_t smem = sc.smem;
+    const int threads = 32 * G * sc.gpb + 32;  // solver groups + the resolver warp
+    const int blocks = sc.per_sm * ctx->num_sms;
     PropEnv pe;
     pe.gw = L.gw; pe.gh = L.gh; pe.step = L.step;
     pe.roi_grid = L.roi_grid;
@@ -2631,9 +2845,14 @@ void propagate_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, con
     pe.mode = L.mode; pe.sgx = L.sgx; pe.sgy = L.sgy;
     pe.dstate = L.dstate; pe.dcnt = L.dcnt; pe.dq = L.dq; pe.kcorr = L.kcorr;
     pe.qword = reinterpret_cast<unsigned long long*>(L.counters + 4);
+    pe.tchild_off = L.tchild_off; pe.tchild = L.tchild; pe.tcont = L.tcont;
+    pe.rcorr = L.rcorr; pe.rq = L.rq; pe.rmeta = L.rmeta; pe.riters = L.riters;
+    if (L.params) pe.params = L.params;  // a heap-order round keeps its parameters across rounds
     const int n = L.gw * L.gh;
-    init_grid_kernel<<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, s>>>(L.out, L.gw, L.gh, L.step);
-    TDIC_CUDA_TRY(cudaGetLastError());
+    if (L.mode != kModeTree) {  // a tree round writes only its result table
+        init_grid_kernel<<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, s>>>(L.out, L.gw, L.gh, L.step);
+        TDIC_CUDA_TRY(cudaGetLastError());
+    }
     void* args[] = {&e, &tm.ref, &tm.coef, &pe};
     TDIC_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kern), dim3(blocks), dim3(threads), args,
                                               smem, s));
@@ -2655,31 +2874,52 @@ struct BatchPlan final : BatchPlanBase {
     Buffer d_jobs, d_maps, d_tab, d_roi, d_claim, d_key, d_params, d_dstate, d_dcnt, d_kcorr, d_dq, d_order, d_fetch,
         d_misc, d_flags, d_out;
     // launch configurations: (warps per POI, groups per CTA) -> grid size and shared memory
-    struct Config { int G, gpb, blocks, threads; size_t smem; int per_sm; };
+    struct Config { int G, gpb, blocks, threads; size_t smem; int per_sm; int stage, narr; };
     std::vector<Config> configs;
     int chosen = 0;
     int sms = 0;      // SMs' worth of blocks a launch uses (fewer than the device leaves room for other work)
     int num_sms = 0;
+    // BatchPlanBase (defined in batch.cu, the only unit that builds plans)
+    int config_count() const override;
+    void config_info(int config, int* warps_per_poi, int* groups_per_block, int* staging) const override;
+    void launch(int config, cudaStream_t s) override;
+    void finish(int32_t* computed, int* err, cudaStream_t s) override;
+    tdic_grid_out outputs(int job) const override;
+    void grid(int job, int32_t* gw_out, int32_t* gh_out) const override;
+    void set_sms(int sms_) override;
 };
 
+// The launch configurations of (G warps per POI, gpb groups per block): each staging mode the
+// request allows that fits, kept when it makes more groups resident than the fuller modes before
+// it (a leaner mode that fits no more groups only re-reads what the fuller one stages).
 template <int OPT, int DEG, typename T, int G>
-void batch_kernel_setup(BatchPlan<T>& b, tdic_ctx* ctx, int gpb) {
-    const size_t per_group = group_smem_bytes<T>(b.sh.nmax, G, b.sh.rbx, b.sh.rby, b.sh.cbx, b.sh.cby);
+void batch_kernel_setup(BatchPlan<T>& b, tdic_ctx* ctx, int gpb, int requested) {
     const size_t prefix = cta_prefix_bytes(b.sh.ntab);
     const size_t ctl = round128(kPropGroupsPerBlock * sizeof(DfSlot<typename MixedOf<T>::type>)) + 128;
-    const size_t smem = prefix + gpb * per_group + ctl;
-    if (smem > static_cast<size_t>(ctx->max_smem_optin)) return;
     const int threads = 32 * G * gpb + 32;
     auto kern = propagate_batch_kernel<OPT, DEG, T, G>;
-    // the attribute is an upper bound shared by every configuration of this kernel: only raise it
-    cudaFuncAttributes fa{};
-    TDIC_CUDA_TRY(cudaFuncGetAttributes(&fa, kern));
-    if (static_cast<int>(smem) > fa.maxDynamicSharedSizeBytes)
-        TDIC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-    int per_sm = 0;
-    TDIC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
-    if (per_sm <= 0) return;
-    b.configs.push_back({G, gpb, per_sm * ctx->num_sms, threads, smem, per_sm});
+    const int stages[3] = {kStageFull, kStageLean, kStageLean | kStageNoCoefWindow};
+    const int want = requested == TDIC_STAGING_FULL ? 0 : requested == TDIC_STAGING_LEAN ? 1
+                   : requested == TDIC_STAGING_LEAN_NO_WINDOW ? 2 : -1;
+    int best_groups = 0;
+    for (int k = 0; k < 3; ++k) {
+        if (want >= 0 && k != want) continue;
+        const int stage = stages[k], narr = sample_arrays(OPT, stage);
+        const size_t per_group = group_smem_bytes<T>(b.sh.nmax, G, b.sh.rbx, b.sh.rby, b.sh.cbx, b.sh.cby, kMat6, stage,
+                                                     narr);
+        const size_t smem = prefix + gpb * per_group + ctl;
+        if (smem > static_cast<size_t>(ctx->max_smem_optin)) continue;
+        // the attribute is an upper bound shared by every configuration of this kernel: only raise it
+        cudaFuncAttributes fa{};
+        TDIC_CUDA_TRY(cudaFuncGetAttributes(&fa, kern));
+        if (static_cast<int>(smem) > fa.maxDynamicSharedSizeBytes)
+            TDIC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+        int per_sm = 0;
+        TDIC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+        if (per_sm <= 0 || per_sm * gpb <= best_groups) continue;
+        best_groups = per_sm * gpb;
+        b.configs.push_back({G, gpb, per_sm * ctx->num_sms, threads, smem, per_sm, stage, narr});
+    }
 }
 
 template <int OPT, int DEG, typename T, int G>
@@ -2694,16 +2934,19 @@ void batch_kernel_launch(BatchPlan<T>& b, const typename BatchPlan<T>::Config& c
     attr[0].val.cooperative = 1;
     lc.attrs = attr;
     lc.numAttrs = 1;
+    Shape sh = b.sh;
+    sh.stage = c.stage;
+    sh.narr = c.narr;
     TDIC_CUDA_TRY(cudaLaunchKernelEx(&lc, propagate_batch_kernel<OPT, DEG, T, G>, b.d_jobs.template as<BatchJob<T>>(),
-                                     b.n, b.d_maps.template as<CUtensorMap>(), b.sh));
+                                     b.n, b.d_maps.template as<CUtensorMap>(), sh));
 }
 
 template <int OPT, int DEG, typename T>
-void batch_configs(BatchPlan<T>& b, tdic_ctx* ctx) {
+void batch_configs(BatchPlan<T>& b, tdic_ctx* ctx, int requested) {
     b.configs.clear();
-    batch_kernel_setup<OPT, DEG, T, 4>(b, ctx, 2);
-    batch_kernel_setup<OPT, DEG, T, 4>(b, ctx, 1);
-    batch_kernel_setup<OPT, DEG, T, 8>(b, ctx, 1);
+    batch_kernel_setup<OPT, DEG, T, 4>(b, ctx, 2, requested);
+    batch_kernel_setup<OPT, DEG, T, 4>(b, ctx, 1, requested);
+    batch_kernel_setup<OPT, DEG, T, 8>(b, ctx, 1, requested);
     TDIC_REQUIRE(!b.configs.empty(), TDIC_UNSUPPORTED, "batch: subset radius too large for shared memory");
 }
 
@@ -2863,7 +3106,9 @@ std::unique_ptr<BatchPlanBase> batch_plan_build(tdic_ctx* ctx, int n, tdic_pair*
     TDIC_CUDA_TRY(cudaMemcpyAsync(b->d_jobs.ptr, b->jobs.data(), sizeof(BatchJob<T>) * n, cudaMemcpyHostToDevice, s));
     TDIC_CUDA_TRY(cudaMemcpyAsync(b->d_maps.ptr, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice, s));
     TDIC_CUDA_TRY(cudaStreamSynchronize(s));  // host staging vectors go out of scope
-    with_opt_deg<T>(b->opt, b->deg, [&](auto O, auto D) { batch_configs<decltype(O)::value, decltype(D)::value, T>(*b, ctx); });
+    with_opt_deg<T>(b->opt, b->deg, [&](auto O, auto D) {
+        batch_configs<decltype(O)::value, decltype(D)::value, T>(*b, ctx, cfgs[0].staging);
+    });
     b->num_sms = ctx->num_sms;
     b->sms = ctx->num_sms;
     return b;

@@ -104,6 +104,9 @@ struct tdic_ctx {
     // tdic_ctx_destroy with live pairs only marks the context; the last tdic_pair_destroy frees it.
     int live_pairs = 0;
     bool destroy_requested = false;
+    // the last heap-order propagation: device rounds after the dataflow pass, and solves in them
+    int heap_rounds = 0;
+    long long heap_solves = 0;
 };
 
 struct tdic_pair {
@@ -183,11 +186,23 @@ struct PropagateLaunch {
     const short2* offsets; int n_offsets;
     // masked subsets (truncate_roi_subsets): device ROI of the pair's image (w x h bytes), or NULL
     const uint8_t* roi_px = nullptr;
+    // a round of the heap order (mode 3): the tree of this round, the result table
+    const int* tchild_off = nullptr; const int* tchild = nullptr; const int* tcont = nullptr;
+    void* rcorr = nullptr; void* rq = nullptr; unsigned char* rmeta = nullptr; int* riters = nullptr;
 };
 void launch_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const PropagateLaunch& L,
                       cudaStream_t s);
 size_t propagate_param_bytes(int precision);
 void launch_init_grid(const tdic_grid_out& out, int gw, int gh, int step, cudaStream_t s);
+// Outputs of a heap-order propagation from its result table (parameters and correlations in the
+// pair's precision) and the host's acceptance flags (heap_order.cu).
+void launch_emit_tree(const tdic_grid_out& out, int gw, int gh, int step, int precision, const void* params,
+                      const void* rcorr, const void* rq, const unsigned char* rmeta, const int* riters,
+                      const unsigned char* accepted, cudaStream_t s);
+// ReliabilityPropagation::propagate in the reference's own heap order on the device
+// (heap_order.cu); the arguments of propagate_impl.
+void heap_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const tdic_seed& seed,
+                    const uint8_t* roi, const tdic_grid_out& out_dev, int32_t* points_computed, cudaStream_t s);
 
 // Seed search (seed.cu) -------------------------------------------------------------------
 struct SearchResult { int u, v; double zncc; int ok; };
@@ -224,18 +239,38 @@ struct BatchSeed {
     double p[6];
     double corr;
 };
+// A batch plan of one precision (batch.cu is compiled once per precision).
 struct BatchPlanBase {
     virtual ~BatchPlanBase() = default;
+    virtual int config_count() const = 0;
+    // warps per POI, groups per block, tdic_staging of launch configuration `config`
+    virtual void config_info(int config, int* warps_per_poi, int* groups_per_block, int* staging) const = 0;
+    virtual void launch(int config, cudaStream_t s) = 0;
+    virtual void finish(int32_t* computed, int* err, cudaStream_t s) = 0;
+    virtual tdic_grid_out outputs(int job) const = 0;
+    virtual void grid(int job, int32_t* gw, int32_t* gh) const = 0;
+    virtual void set_sms(int sms) = 0;
 };
-std::unique_ptr<BatchPlanBase> batch_build(tdic_ctx* ctx, int n, tdic_pair* const* pairs, const tdic_config* cfgs,
-                                           const BatchSeed* seeds, const std::vector<std::vector<uint8_t>>& rois,
-                                           cudaStream_t s);
-int batch_config_count(BatchPlanBase* p);
-void batch_config_info(BatchPlanBase* p, int config, int* warps_per_poi, int* groups_per_block);
-void batch_launch(BatchPlanBase* p, int config, cudaStream_t s);
-void batch_finish(BatchPlanBase* p, int32_t* computed, int* err, cudaStream_t s);
-tdic_grid_out batch_outputs(BatchPlanBase* p, int job);
-void batch_grid(BatchPlanBase* p, int job, int32_t* gw, int32_t* gh);
-void batch_set_sms(BatchPlanBase* p, int sms);
+std::unique_ptr<BatchPlanBase> batch_build_f32(tdic_ctx* ctx, int n, tdic_pair* const* pairs, const tdic_config* cfgs,
+                                               const BatchSeed* seeds, const std::vector<std::vector<uint8_t>>& rois,
+                                               cudaStream_t s);
+std::unique_ptr<BatchPlanBase> batch_build_f64(tdic_ctx* ctx, int n, tdic_pair* const* pairs, const tdic_config* cfgs,
+                                               const BatchSeed* seeds, const std::vector<std::vector<uint8_t>>& rois,
+                                               cudaStream_t s);
+inline std::unique_ptr<BatchPlanBase> batch_build(tdic_ctx* ctx, int n, tdic_pair* const* pairs,
+                                                  const tdic_config* cfgs, const BatchSeed* seeds,
+                                                  const std::vector<std::vector<uint8_t>>& rois, cudaStream_t s) {
+    return pairs[0]->precision == TDIC_FP64 ? batch_build_f64(ctx, n, pairs, cfgs, seeds, rois, s)
+                                            : batch_build_f32(ctx, n, pairs, cfgs, seeds, rois, s);
+}
+inline int batch_config_count(BatchPlanBase* p) { return p->config_count(); }
+inline void batch_config_info(BatchPlanBase* p, int config, int* warps_per_poi, int* groups_per_block, int* staging) {
+    p->config_info(config, warps_per_poi, groups_per_block, staging);
+}
+inline void batch_launch(BatchPlanBase* p, int config, cudaStream_t s) { p->launch(config, s); }
+inline void batch_finish(BatchPlanBase* p, int32_t* computed, int* err, cudaStream_t s) { p->finish(computed, err, s); }
+inline tdic_grid_out batch_outputs(BatchPlanBase* p, int job) { return p->outputs(job); }
+inline void batch_grid(BatchPlanBase* p, int job, int32_t* gw, int32_t* gh) { p->grid(job, gw, gh); }
+inline void batch_set_sms(BatchPlanBase* p, int sms) { p->set_sms(sms); }
 
 }  // namespace tdic

@@ -10,7 +10,9 @@ Both run on the GPU through libtdic_gb300.so; there is no CPU fallback.
 Additive result keys (not in the reference): ``zncc`` = clamp(1 - correlation / 2),
 ``iterations``, ``converged`` (strict |dp| < threshold) and ``status`` (dic::SolverStatus).
 GPU-only settings live under a separate ``"gpu"`` section of the config dict, which the
-reference parser ignores: ``{"gpu": {"precision": "fp32" | "fp64", "propagation": "dataflow" | "waves"}}``.
+reference parser ignores: ``{"gpu": {"precision": "fp32" | "fp64", "propagation": "dataflow" | "waves",
+"staging": "auto" | "full" | "lean" | "lean_no_window"}}`` (staging changes speed and shared-memory
+needs, never a result).
 """
 from __future__ import annotations
 
@@ -24,9 +26,13 @@ import numpy as np
 from . import _lib as L
 
 RESULT_KEYS = ("x", "y", "u", "v", "du_dx", "du_dy", "dv_dx", "dv_dy", "correlation", "valid")
-# GPU visit orders of the propagation (the reference's serial heap order is mode 1, CPU only)
-PROPAGATION_MODES = {"waves": 0, "dataflow": 2}
+# Visit orders of the propagation: the reference's heap order (reproduced exactly on the device
+# in rounds), frontier waves, dataflow (the default)
+PROPAGATION_MODES = {"waves": 0, "heap": 1, "dataflow": 2}
 EXTRA_KEYS = ("zncc", "iterations", "converged", "status")
+# shared-memory staging of the first-order ZNSSD solves (tdic_staging); "gpu": {"staging": ...}
+STAGING = {"auto": 0, "full": 1, "lean": 2, "lean_no_window": 3}
+STAGING_NAMES = {v: k for k, v in STAGING.items()}
 
 
 # ---------------------------------------------------------------------------------------------
@@ -51,6 +57,12 @@ class Context:
     @property
     def device_bytes(self) -> int:
         return int(self.lib.tdic_ctx_device_bytes(self.handle))
+
+    def heap_stats(self) -> tuple:
+        """(device rounds, solves in them) of the last heap-order propagation on this context."""
+        r, n = C.c_int32(), C.c_int64()
+        self.check(self.lib.tdic_ctx_heap_stats(self.handle, C.byref(r), C.byref(n)))
+        return r.value, n.value
 
     def close(self) -> None:
         if getattr(self, "handle", None):
@@ -299,8 +311,13 @@ def config_from_dict(d: dict | None) -> L.Config:
     if "propagation" in gpu:
         m = str(gpu["propagation"]).lower()
         if m not in PROPAGATION_MODES:
-            raise RuntimeError("gpu.propagation must be 'waves' or 'dataflow'.")
+            raise RuntimeError("gpu.propagation must be 'heap', 'waves' or 'dataflow'.")
         cfg.propagation_mode = PROPAGATION_MODES[m]
+    if "staging" in gpu:
+        m = str(gpu["staging"]).lower()
+        if m not in STAGING:
+            raise RuntimeError("gpu.staging must be 'auto', 'full', 'lean' or 'lean_no_window'.")
+        cfg.staging = STAGING[m]
     return cfg
 
 
@@ -554,9 +571,10 @@ class Batch:
         self.ctx.check(self.ctx.lib.tdic_batch_set_sms(self.handle, int(sms)))
 
     def config(self) -> tuple:
-        g, k = C.c_int32(), C.c_int32()
-        self.ctx.check(self.ctx.lib.tdic_batch_config(self.handle, C.byref(g), C.byref(k)))
-        return g.value, k.value
+        """(warps per POI, solver groups per block, staging name) of the launch in use."""
+        g, k, st = C.c_int32(), C.c_int32(), C.c_int32()
+        self.ctx.check(self.ctx.lib.tdic_batch_config(self.handle, C.byref(g), C.byref(k), C.byref(st)))
+        return g.value, k.value, STAGING_NAMES.get(st.value, str(st.value))
 
     def launch(self, stream=None) -> None:
         self.ctx.check(self.ctx.lib.tdic_batch_launch(self.handle, _stream_ptr(stream)))
