@@ -70,6 +70,13 @@ void BatchPlan<T>::set_sms(int sms_) {
 
 }  // namespace
 
+// This unit's copy of the B-spline constant tables (each unit that includes hotpath.cuh has its own).
+#if TDIC_BATCH_FP64
+void upload_qk_batch_f64() { upload_qk_local(); }
+#else
+void upload_qk_batch_f32() { upload_qk_local(); }
+#endif
+
 #if TDIC_BATCH_FP64
 std::unique_ptr<BatchPlanBase> batch_build_f64(tdic_ctx* ctx, int n, tdic_pair* const* pairs, const tdic_config* cfgs,
                                                const BatchSeed* seeds, const std::vector<std::vector<uint8_t>>& rois,

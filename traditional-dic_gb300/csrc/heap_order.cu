@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <queue>
 
 namespace tdic {
@@ -62,6 +63,16 @@ struct HeapTable {
     std::vector<int> newpar;            // parent of every solve (-1 seed, -2 not solved)
     std::vector<uint8_t> accepted;
     std::vector<int> dirty;
+    // What the simulation reads of a solved point, packed (refresh() after a table change): its
+    // key, displacement, where its result came from, and the parent-independent part of the
+    // acceptance rule (valid, Success, correlation < max_znssd, finite).
+    struct Rec {
+        double corr;
+        P u, v;
+        int par, src;
+        uint8_t have, ok;
+    };
+    std::vector<Rec> rec;
 
     void init(int n) {
         p.assign(6 * static_cast<size_t>(n), P(0));
@@ -73,48 +84,205 @@ struct HeapTable {
         src.assign(n, -1);
         newpar.assign(n, -2);
         accepted.assign(n, 0);
+        rec.assign(n, Rec{0.0, P(0), P(0), -2, -1, 0, 0});
     }
 
-    // The guess of reliability_propagation.cpp:326-329 as the device computes it.
-    void guess(int from, int to, P (&g)[2]) const {
-        const P* pp = &p[static_cast<size_t>(from) * 6];
-        const P ddx = static_cast<P>((to % gw - from % gw) * step), ddy = static_cast<P>((to / gw - from / gw) * step);
+    void refresh(int i) {
+        const P* r = &p[static_cast<size_t>(i) * 6];
+        const bool finite = std::isfinite(r[0]) && std::isfinite(r[1]) && std::isfinite(r[2]) && std::isfinite(r[3]) &&
+                            std::isfinite(r[4]) && std::isfinite(r[5]) && std::isfinite(corr[i]);
+        Rec& q = rec[i];
+        q.corr = static_cast<double>(corr[i]);
+        q.u = r[0];
+        q.v = r[1];
+        q.par = par[i];
+        q.src = src[i];
+        q.have = have[i];
+        q.ok = (meta[i] & 4) && (meta[i] & 3) == TDIC_SUCCESS && corr[i] < max_znssd && finite;
+    }
+
+    // The guess of reliability_propagation.cpp:326-329 as the device computes it, from parameters
+    // pp of the parent, ddx / ddy px away.
+    static void guess(const P* pp, P ddx, P ddy, P (&g)[2]) {
         g[0] = std::fma(pp[3], ddy, std::fma(pp[2], ddx, pp[0]));
         g[1] = std::fma(pp[5], ddy, std::fma(pp[4], ddx, pp[1]));
     }
 
-    // The acceptance rule of reliability_propagation.cpp:359-368 on the table's result of `n`.
-    bool acceptable(int n, const P (&g)[2]) const {
-        const P* r = &p[static_cast<size_t>(n) * 6];
-        const bool finite = std::isfinite(r[0]) && std::isfinite(r[1]) && std::isfinite(r[2]) && std::isfinite(r[3]) &&
-                            std::isfinite(r[4]) && std::isfinite(r[5]) && std::isfinite(corr[n]);
-        const P cutoff = static_cast<P>(step);
-        return (meta[n] & 4) && (meta[n] & 3) == TDIC_SUCCESS && corr[n] < max_znssd &&
-               std::fabs(g[0] - r[0]) < cutoff && std::fabs(g[1] - r[1]) < cutoff && finite;
+    // Every pop is recorded (pop_step, calc_step), so the next simulation can start at the first
+    // pop that meets a result the round in between changed: the pops before it are the same.
+    std::vector<int> calc_step;         // pop at which a point was marked calculated (-1: never)
+    std::vector<int> pop_step;          // pop at which a point was popped (-1: never)
+    bool sim_valid = false;             // calc_step / pop_step describe the table's last simulation
+
+    struct Item {
+        double corrcoef;
+        int n;
+        bool operator<(const Item& o) const { return corrcoef > o.corrcoef; }  // QueueItem, :44-53
+    };
+
+    // Bucket queue over non-negative keys (ZNSSD and SSD values): the bit pattern of a
+    // non-negative double orders like the value; the span of the patterns the simulation can
+    // push (the table's keys) is cut into 2^20 buckets of equal width, a bucket holds its points
+    // in a list and a three-level bitmap finds the lowest non-empty bucket.  A pop takes the
+    // bucket's smallest key; two equal keys in the queue at once would leave the order to
+    // std::priority_queue's tie rule, so the queue reports a tie and the caller repeats the
+    // simulation with std::priority_queue itself.
+    struct BucketQueue {
+        static constexpr int kBits = 20;
+        std::vector<int> head, next;
+        std::vector<uint64_t> key, l0, l1;
+        uint64_t l2[4] = {0, 0, 0, 0};
+        size_t count = 0;
+        bool tie = false;
+        uint64_t lo = 0, hi = 0;
+        int shift = 0;
+        static uint64_t bits_of(double k) {
+            uint64_t b;
+            std::memcpy(&b, &k, sizeof(b));
+            return k == 0.0 ? 0 : b;  // -0.0 is 0
+        }
+        // keys to come lie in [klo, khi] (both >= 0)
+        void init(int n, double klo, double khi) {
+            lo = bits_of(klo);
+            hi = bits_of(khi);
+            shift = 0;
+            while (((hi - lo) >> shift) >= (uint64_t(1) << kBits)) ++shift;
+            head.assign(size_t(1) << kBits, -1);
+            next.assign(n, -1);
+            key.assign(n, 0);
+            l0.assign((size_t(1) << kBits) / 64, 0);
+            l1.assign(l0.size() / 64, 0);
+            l2[0] = l2[1] = l2[2] = l2[3] = 0;
+            count = 0;
+            tie = false;
+        }
+        bool push(double k, int n) {
+            if (!(k >= 0.0)) return false;  // negative or NaN: not orderable here
+            const uint64_t b = bits_of(k);
+            if (b < lo || b > hi) return false;
+            key[n] = b;
+            const size_t bk = static_cast<size_t>((b - lo) >> shift);
+            next[n] = head[bk];
+            head[bk] = n;
+            l0[bk >> 6] |= 1ull << (bk & 63);
+            l1[bk >> 12] |= 1ull << ((bk >> 6) & 63);
+            l2[bk >> 18] |= 1ull << ((bk >> 12) & 63);
+            ++count;
+            return true;
+        }
+        int pop() {
+            int w2 = 0;
+            while (l2[w2] == 0) ++w2;
+            const size_t i1 = static_cast<size_t>(w2) * 64 + __builtin_ctzll(l2[w2]);
+            const size_t i0 = i1 * 64 + __builtin_ctzll(l1[i1]);
+            const size_t bk = i0 * 64 + __builtin_ctzll(l0[i0]);
+            int best = head[bk], best_prev = -1, prev = best;
+            for (int it = next[best]; it >= 0; prev = it, it = next[it])
+                if (key[it] < key[best]) { best = it; best_prev = prev; }
+            for (int it = head[bk]; it >= 0; it = next[it])
+                if (it != best && key[it] == key[best]) tie = true;
+            if (best_prev < 0) head[bk] = next[best]; else next[best_prev] = next[best];
+            if (head[bk] < 0) {
+                l0[i0] &= ~(1ull << (bk & 63));
+                if (l0[i0] == 0) {
+                    l1[i1] &= ~(1ull << (i0 & 63));
+                    if (l1[i1] == 0) l2[w2] &= ~(1ull << (i1 & 63));
+                }
+            }
+            --count;
+            return best;
+        }
+        bool empty() const { return count == 0; }
+    };
+    BucketQueue bq;
+
+    // The heap loop of reliability_propagation.cpp:270-389 over the table, from the start of the
+    // pop sequence or, given the points the last round changed, from the first pop that meets
+    // one of them.
+    void simulate(const std::vector<int>* changed = nullptr) {
+        const int total = gw * gh;
+        int k0 = 0;
+        if (changed && sim_valid) {
+            k0 = std::numeric_limits<int>::max();
+            for (const int x : *changed)
+                if (calc_step[x] >= 0) k0 = std::min(k0, calc_step[x]);  // the pop of its parent
+            k0 = std::min(k0, total);
+        }
+        if (simulate_from(total, k0, false)) return;
+        simulate_from(total, 0, true);  // a tie: the reference's own queue decides, from the start
     }
 
-    // The heap loop of reliability_propagation.cpp:270-389 over the table.
-    void simulate() {
-        struct Item {
-            double corrcoef;
-            int n;
-            bool operator<(const Item& o) const { return corrcoef > o.corrcoef; }  // QueueItem, :44-53
-        };
-        const int total = gw * gh;
+    // Returns false when the bucket queue met a tie (nothing usable was produced).
+    bool simulate_from(int total, int k0, bool exact_queue) {
         std::vector<uint8_t> calculated(total, 0);
-        std::fill(newpar.begin(), newpar.end(), -2);
-        std::fill(accepted.begin(), accepted.end(), 0);
-        dirty.clear();
-        calculated[seed] = 1;
-        accepted[seed] = 1;
-        newpar[seed] = -1;
-        std::priority_queue<Item> q;
-        q.push(Item{std::max(0.0, static_cast<double>(corr[seed])), seed});
+        if (k0 > 0) {
+            // the state after the first k0 pops of the last simulation: every point met before
+            // pop k0 kept its result (the round solved only points met later), so it is clean
+            for (int i = 0; i < total; ++i) {
+                if (calc_step[i] >= 0 && calc_step[i] < k0) {
+                    calculated[i] = 1;
+                } else {
+                    calc_step[i] = -1;
+                    newpar[i] = i == seed ? -1 : -2;
+                    accepted[i] = i == seed;
+                }
+                if (pop_step[i] >= k0) pop_step[i] = -1;
+            }
+            calculated[seed] = 1;
+            dirty.clear();
+        } else {
+            std::fill(newpar.begin(), newpar.end(), -2);
+            std::fill(accepted.begin(), accepted.end(), 0);
+            calc_step.assign(total, -1);
+            pop_step.assign(total, -1);
+            dirty.clear();
+            calculated[seed] = 1;
+            accepted[seed] = 1;
+            newpar[seed] = -1;
+        }
+        std::priority_queue<Item> pq;
+        const double seed_key = std::max(0.0, static_cast<double>(corr[seed]));
+        if (!exact_queue) {
+            double klo = seed_key, khi = seed_key;
+            for (int i = 0; i < total; ++i)
+                if (rec[i].have && rec[i].corr >= 0.0) {
+                    klo = std::min(klo, rec[i].corr);
+                    khi = std::max(khi, rec[i].corr);
+                }
+            bq.init(total, klo, khi);
+        }
+        auto push = [&](double k, int n) -> bool {
+            if (exact_queue) { pq.push(Item{k, n}); return true; }
+            return bq.push(k, n);
+        };
+        int pops = 0;
+        if (k0 == 0) {
+            if (!push(seed_key, seed)) return false;
+        } else {
+            // in the queue after k0 pops: points accepted before pop k0 and not popped by then
+            pops = k0;
+            for (int i = 0; i < total; ++i)
+                if (accepted[i] && pop_step[i] < 0 && (i == seed || calc_step[i] >= 0))
+                    if (!push(i == seed ? seed_key : rec[i].corr, i)) return false;
+        }
         const int dxs[4] = {0, step, 0, -step}, dys[4] = {-step, 0, step, 0};  // up, right, down, left
-        while (!q.empty()) {
-            const Item it = q.top();
-            q.pop();
-            const int px = (it.n % gw) * step, py = (it.n / gw) * step;
+        const P cutoff = static_cast<P>(step);
+        for (;;) {
+            int n;
+            if (exact_queue) {
+                if (pq.empty()) break;
+                n = pq.top().n;
+                pq.pop();
+            } else {
+                if (bq.empty()) break;
+                n = bq.pop();
+                if (bq.tie) return false;
+            }
+            const int k = pops++;
+            pop_step[n] = k;
+            const int px = (n % gw) * step, py = (n / gw) * step;
+            const int vn = ver[n];
+            const P* pp = &p[static_cast<size_t>(n) * 6];
             for (int d = 0; d < 4; ++d) {
                 const int nx = px + dxs[d], ny = py + dys[d];
                 if (nx < 0 || ny < 0 || nx >= w || ny >= h) continue;
@@ -123,19 +291,23 @@ struct HeapTable {
                 const int m = gny * gw + gnx;
                 if (calculated[m]) continue;
                 calculated[m] = 1;
+                calc_step[m] = k;
                 if (!roi_grid[m]) continue;
                 if (nx - radius < 0 || ny - radius < 0 || nx + radius >= w || ny + radius >= h) continue;
-                newpar[m] = it.n;
-                if (!(have[m] && par[m] == it.n && src[m] == ver[it.n])) dirty.push_back(m);
-                if (!have[m]) continue;  // never solved: no result to go on with
+                newpar[m] = n;
+                const Rec& r = rec[m];
+                if (!(r.have && r.par == n && r.src == vn)) dirty.push_back(m);
+                if (!r.have || !r.ok) continue;  // never solved, or refused whatever the guess
                 P g[2];
-                guess(it.n, m, g);
-                if (acceptable(m, g)) {
+                guess(pp, static_cast<P>(dxs[d]), static_cast<P>(dys[d]), g);
+                if (std::fabs(g[0] - r.u) < cutoff && std::fabs(g[1] - r.v) < cutoff) {  // :359-368
                     accepted[m] = 1;
-                    q.push(Item{static_cast<double>(corr[m]), m});
+                    if (!push(r.corr, m)) return false;
                 }
             }
         }
+        sim_valid = true;
+        return true;
     }
 };
 
@@ -317,6 +489,7 @@ void heap_rounds(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const t
     }
     t.par[sidx] = -1;
     t.ver[sidx] = 1;
+    for (int i = 0; i < n; ++i) t.refresh(i);
     // the seed's entry of the device result table (the rounds never solve it again; its
     // first-order parameters are in the parameter table already)
     {
@@ -347,8 +520,9 @@ void heap_rounds(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const t
     int rounds = 0;
     ctx->heap_rounds = 0;
     ctx->heap_solves = 0;
+    std::vector<int> changed;  // points the last round solved again
     for (;;) {
-        t.simulate();
+        t.simulate(rounds > 0 ? &changed : nullptr);
         if (t.dirty.empty()) break;
         TDIC_REQUIRE(++rounds <= kMaxRounds, TDIC_TIMEOUT, "heap-order propagation did not settle");
         build_round(t.newpar, t.dirty, sidx, n, rt);
@@ -379,6 +553,7 @@ void heap_rounds(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const t
         TDIC_REQUIRE(flags[0] == 0, TDIC_TIMEOUT, "propagation: a bounded in-kernel wait timed out");
         ctx->heap_rounds = rounds;
         ctx->heap_solves += static_cast<long long>(rt.order.size());
+        changed = rt.order;
         for (const int x : rt.order) {  // parents first: a child records its parent's new version
             t.corr[x] = rc[x];
             t.meta[x] = rm[x];
@@ -386,6 +561,7 @@ void heap_rounds(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const t
             t.par[x] = t.newpar[x];
             t.ver[x] += 1;
             t.src[x] = t.ver[t.newpar[x]];
+            t.refresh(x);
         }
     }
     // ---- outputs: the accepted points of the last simulation -------------------------------

@@ -11,6 +11,8 @@ void upload_qk_route1();
 void upload_qk_route2();
 void upload_qk_route3();
 void upload_qk_route4();
+void upload_qk_batch_f32();
+void upload_qk_batch_f64();
 void launch_solve_route1(tdic_ctx*, tdic_pair*, const tdic_config&, const SolveLaunch&, cudaStream_t);
 void launch_solve_route2(tdic_ctx*, tdic_pair*, const tdic_config&, const SolveLaunch&, cudaStream_t);
 void launch_solve_route3(tdic_ctx*, tdic_pair*, const tdic_config&, const SolveLaunch&, cudaStream_t);
@@ -26,6 +28,8 @@ void upload_qk_constants() {
     upload_qk_route2();
     upload_qk_route3();
     upload_qk_route4();
+    upload_qk_batch_f32();
+    upload_qk_batch_f64();
 }
 
 void launch_init_grid(const tdic_grid_out& out, int gw, int gh, int step, cudaStream_t s) {

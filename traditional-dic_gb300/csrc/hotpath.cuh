@@ -100,41 +100,13 @@ __device__ __forceinline__ T warp_scatter_sum(const T (&v)[K], int lane) {
 
 // All-reduce K values over the group: every thread ends with the same sums (summed in the same
 // order), so redundant scalar math stays bit-identical across the group's warps.  A warp
-// reduce-scatter writes each warp's K partials (rows of KS = K rounded up to 4 values, so a
-// row reads as 16-byte vectors), one barrier, then every thread adds the G partials of every
-// value in warp order itself (broadcast reads; no second barrier and no dependent round trip
-// through a K-thread sum).  `red` holds two buffers of 32*G values used alternately (parity
-// `rp`): a buffer is rewritten two reductions later, after every thread has passed the barrier
-// of the reduction in between, so its readers are done.
-template <int K, typename T>
-__device__ __forceinline__ void load_row(const T* row, T (&v)[K]) {
-    constexpr int KS = (K + 3) / 4 * 4;
-    if constexpr (sizeof(T) == 4 && K >= 8) {
-#pragma unroll
-        for (int k = 0; k < KS / 4; ++k) {
-            const float4 q = reinterpret_cast<const float4*>(row)[k];
-            if (4 * k + 0 < K) v[4 * k + 0] = q.x;
-            if (4 * k + 1 < K) v[4 * k + 1] = q.y;
-            if (4 * k + 2 < K) v[4 * k + 2] = q.z;
-            if (4 * k + 3 < K) v[4 * k + 3] = q.w;
-        }
-    } else if constexpr (sizeof(T) == 8 && K >= 8) {
-#pragma unroll
-        for (int k = 0; k < KS / 2; ++k) {
-            const double2 q = reinterpret_cast<const double2*>(row)[k];
-            if (2 * k + 0 < K) v[2 * k + 0] = q.x;
-            if (2 * k + 1 < K) v[2 * k + 1] = q.y;
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < K; ++k) v[k] = row[k];
-    }
-}
-
+// reduce-scatter, then thread k < K adds the G warp partials of value k, then everyone reads
+// the K totals.  `red` holds two buffers of 32*G values used alternately (parity `rp`): a
+// buffer is rewritten only after every thread has passed the barriers of the reduction in
+// between.
 template <int G, int K, typename T>
 __device__ __forceinline__ void group_sum(T (&v)[K], T* red_base, int& rp, int tid, int bar_id) {
-    constexpr int KS = (K + 3) / 4 * 4;
-    static_assert(G == 1 || KS <= 32, "reduction scratch: G rows of KS partials per buffer");
+    static_assert(G == 1 || K * (G + 1) <= 32 * G, "reduction scratch: G*K partials + K totals per buffer");
     constexpr int LG = Pow2Ceil<K>::log2;
     const int lane = tid & 31;
     const T r = warp_scatter_sum<K, T>(v, lane);
@@ -144,18 +116,20 @@ __device__ __forceinline__ void group_sum(T (&v)[K], T* red_base, int& rp, int t
         for (int k = 0; k < K; ++k) v[k] = __shfl_sync(0xffffffffu, r, k << (5 - LG));
     } else {
         T* red = red_base + rp * 32 * G;
+        T* tot = red + G * K;
         rp ^= 1;
         const int warp = tid >> 5;
-        if ((lane & ((1 << (5 - LG)) - 1)) == 0 && idx < K) red[warp * KS + idx] = r;
+        if ((lane & ((1 << (5 - LG)) - 1)) == 0 && idx < K) red[warp * K + idx] = r;
         named_bar(bar_id, 32 * G);
-        load_row<K, T>(red, v);
+        if (tid < K) {
+            T acc = red[tid];
 #pragma unroll
-        for (int w = 1; w < G; ++w) {
-            T part[K];
-            load_row<K, T>(red + w * KS, part);
-#pragma unroll
-            for (int k = 0; k < K; ++k) v[k] += part[k];
+            for (int w = 1; w < G; ++w) acc += red[w * K + tid];
+            tot[tid] = acc;
         }
+        named_bar(bar_id, 32 * G);
+#pragma unroll
+        for (int k = 0; k < K; ++k) v[k] = tot[k];
     }
 }
 
