@@ -501,9 +501,9 @@ def run_ours(args, world, rank, local, pg):
             d = np.maximum(np.abs(outs["u"].cpu().numpy()[both] - f["u"][both]),
                            np.abs(outs["v"].cpu().numpy()[both] - f["v"][both]))
             t_h = statistics.median(th)
-            rounds, solves = ctx.heap_stats()
+            rounds, solves, sim_ms = ctx.heap_stats()
             heap[prec] = {"ms": 1e3 * t_h, "value": float(np.sum(hv & hc)) / t_h, "unit": UNIT,
-                          "device_rounds": rounds, "round_solves": solves,
+                          "device_rounds": rounds, "round_solves": solves, "host_simulation_ms": sim_ms,
                           "dataflow_vs_heap": {"flag_agreement": float(np.mean(hv == (f["valid"] != 0))),
                                                "within_1e-3_px": float(np.mean(d <= 1e-3)),
                                                "max_abs_px": float(d.max()), "p99_abs_px": float(np.quantile(d, 0.99))}}

@@ -171,8 +171,9 @@ const char* tdic_last_error(const tdic_ctx* ctx);
 /* Bytes the pool holds on the device (allocated, live + cached). */
 size_t tdic_ctx_device_bytes(const tdic_ctx* ctx);
 /* The last heap-order propagation (propagation_mode 1) on this context: device rounds after
- * the dataflow pass and the solves they ran.  No counterpart in the reference. */
-tdic_status tdic_ctx_heap_stats(const tdic_ctx* ctx, int32_t* rounds, int64_t* solves);
+ * the dataflow pass, the solves they ran and the host time of the heap simulations
+ * (host_sim_ms may be NULL).  No counterpart in the reference. */
+tdic_status tdic_ctx_heap_stats(const tdic_ctx* ctx, int32_t* rounds, int64_t* solves, double* host_sim_ms);
 
 /* Image pair on the device: the reference image (float32, as dic::Image stores it,
  * image.hpp:58-81) and the deformed image's B-spline coefficients of `degree` with `border`

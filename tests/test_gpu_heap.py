@@ -172,7 +172,7 @@ def test_dataflow_against_heap_order(oracle, gpu_ctx, workload0):
     cfg.propagation_mode = 2
     flow = S.propagate(gpu_ctx, pair, cfg, seed)
     pair.close()
-    rounds, solves = gpu_ctx.heap_stats()
+    rounds, solves, sim_ms = gpu_ctx.heap_stats()
     assert 1 <= rounds <= 10 and solves >= heap["points_computed"] - 1
     assert np.mean(flow["valid"] == heap["valid"]) >= 0.99
     both = flow["valid"] & heap["valid"]

@@ -105,7 +105,8 @@ SIGNATURES = {
     "tdic_batch_outputs": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(GridOut)]),
     "tdic_batch_results": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(GridOut), C.c_void_p]),
     "tdic_batch_set_sms": (C.c_int, [C.c_void_p, C.c_int32]),
-    "tdic_ctx_heap_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
+    "tdic_ctx_heap_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int64),
+                                      C.POINTER(C.c_double)]),
     "tdic_batch_config": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "tdic_batch_destroy": (None, [C.c_void_p]),
     "tdic_subset_prepare": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int, C.c_void_p,

@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <mutex>
@@ -102,6 +103,43 @@ void check_device_error(tdic_ctx* ctx, cudaStream_t s) {
         TDIC_CUDA_TRY(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), s));
         throw Error{TDIC_TIMEOUT, "a bounded in-kernel wait (TMA copy) timed out"};
     }
+}
+
+void setup_cache_prepare(tdic_ctx* ctx, tdic_pair* pair, int gw, int gh, int sgx, int sgy, SetupCache& c,
+                         PropagateLaunch& L, cudaStream_t s) {
+    const size_t n = static_cast<size_t>(gw) * gh;
+    const size_t m = pair->precision == TDIC_FP64 ? sizeof(double) : sizeof(float);
+    c.hinv = Buffer(&ctx->pool, 36 * m * n);
+    c.fmn = Buffer(&ctx->pool, 2 * m * n);
+    c.state = Buffer(&ctx->pool, sizeof(int) * n);
+    c.ticket = Buffer(&ctx->pool, sizeof(int));
+    TDIC_CUDA_TRY(cudaMemsetAsync(c.state.ptr, 0, sizeof(int) * n, s));
+    TDIC_CUDA_TRY(cudaMemsetAsync(c.ticket.ptr, 0, sizeof(int), s));
+    const int key[3] = {gw, gh, sgy * gw + sgx};
+    if (!(key[0] == ctx->pre_key[0] && key[1] == ctx->pre_key[1] && key[2] == ctx->pre_key[2])) {
+        // counting sort of the grid points by Manhattan distance from the seed (index order within)
+        const int dmax = gw + gh;
+        std::vector<int> count(dmax + 2, 0), order(n);
+        for (size_t i = 0; i < n; ++i)
+            ++count[std::abs(static_cast<int>(i % gw) - sgx) + std::abs(static_cast<int>(i / gw) - sgy) + 1];
+        for (int d = 0; d <= dmax; ++d) count[d + 1] += count[d];
+        for (size_t i = 0; i < n; ++i)
+            order[count[std::abs(static_cast<int>(i % gw) - sgx) + std::abs(static_cast<int>(i / gw) - sgy)]++] =
+                static_cast<int>(i);
+        // the copy must land before `order` goes out of scope
+        ctx->pre_key[0] = -1;
+        ctx->pre_order = Buffer(&ctx->pool, sizeof(int) * n);
+        TDIC_CUDA_TRY(cudaMemcpyAsync(ctx->pre_order.ptr, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+        TDIC_CUDA_TRY(cudaStreamSynchronize(s));
+        ctx->pre_key[0] = key[0]; ctx->pre_key[1] = key[1]; ctx->pre_key[2] = key[2];
+        ctx->pre_count = static_cast<int>(n);
+    }
+    L.sc_hinv = c.hinv.ptr;
+    L.sc_fmn = c.fmn.ptr;
+    L.sc_state = c.state.as<int>();
+    L.pre_order = ctx->pre_order.as<int>();
+    L.pre_count = ctx->pre_count;
+    L.pre_ticket = c.ticket.as<int>();
 }
 
 const SampleTable& sample_table(tdic_ctx* ctx, int radius) {
@@ -337,6 +375,8 @@ void propagate_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, cons
         L.seed_idx = 0;
         L.seed_solve = 0;
     }
+    SetupCache cache;
+    if (seed_ok && setup_cache_applies(cfg)) setup_cache_prepare(ctx, pair, gw, gh, gxs, gys, cache, L, s);
     if (seed_ok) launch_propagate(ctx, pair, cfg, L, s);
     else launch_init_grid(L.out, gw, gh, step, s);  // every grid point with its defaults
     int flags[3] = {0, 0, 0};
@@ -734,10 +774,11 @@ const char* tdic_last_error(const tdic_ctx* ctx) {
 
 size_t tdic_ctx_device_bytes(const tdic_ctx* ctx) { return ctx ? ctx->pool.held_bytes() : 0; }
 
-tdic_status tdic_ctx_heap_stats(const tdic_ctx* ctx, int32_t* rounds, int64_t* solves) {
+tdic_status tdic_ctx_heap_stats(const tdic_ctx* ctx, int32_t* rounds, int64_t* solves, double* host_sim_ms) {
     if (!ctx || !rounds || !solves) return TDIC_INVALID_ARG;
     *rounds = ctx->heap_rounds;
     *solves = ctx->heap_solves;
+    if (host_sim_ms) *host_sim_ms = ctx->heap_sim_ms;
     return TDIC_OK;
 }
 

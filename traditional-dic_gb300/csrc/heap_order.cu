@@ -25,6 +25,7 @@
 #include "tdic_internal.cuh"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -432,6 +433,8 @@ void heap_rounds(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const t
     L.sgx = gxs; L.sgy = gys;
     L.dstate = dstate.as<int>(); L.dcnt = dcnt.as<int>();
     L.dq = dq.as<unsigned long long>(); L.kcorr = kcorr.as<float>();
+    SetupCache cache;  // shared by every round: a point's set-up does not change
+    if (setup_cache_applies(cfg)) setup_cache_prepare(ctx, pair, gw, gh, gxs, gys, cache, L, s);
 
     // ---- round 0: the dataflow propagation (its parents are not the heap's) ---------------------
     tdic_grid_out o0{};
@@ -520,9 +523,12 @@ void heap_rounds(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const t
     int rounds = 0;
     ctx->heap_rounds = 0;
     ctx->heap_solves = 0;
+    ctx->heap_sim_ms = 0.0;
     std::vector<int> changed;  // points the last round solved again
     for (;;) {
+        const auto t_sim = std::chrono::steady_clock::now();
         t.simulate(rounds > 0 ? &changed : nullptr);
+        ctx->heap_sim_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_sim).count();
         if (t.dirty.empty()) break;
         TDIC_REQUIRE(++rounds <= kMaxRounds, TDIC_TIMEOUT, "heap-order propagation did not settle");
         build_round(t.newpar, t.dirty, sidx, n, rt);

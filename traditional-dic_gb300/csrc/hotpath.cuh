@@ -175,6 +175,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ int ld_acquire_s32(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_s32(int* p, int v) {
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
     asm volatile(
         "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
@@ -365,6 +373,13 @@ struct Env {
     // the launch's Shape): kStage* bits and the per-sample arrays it keeps
     int stage = kStageFull;
     int narr = 4;
+    // Set-up cache of a propagation grid (first-order ZNSSD ICGN), or NULL: per grid point the
+    // reference side of the solve -- inverse Hessian (36 values of the solve's scalar type),
+    // mean and inverse norm of the subset (2 values of T) and a state (0 not computed, 1 ready,
+    // 2 the set-up fails: NumericalFailure).  Idle solver groups fill it ahead of the solves.
+    void* sc_hinv = nullptr;
+    T* sc_fmn = nullptr;
+    int* sc_state = nullptr;
 };
 
 // Per-POI result in the solve's own precision (float on the FP32-mixed path); outputs are
@@ -874,7 +889,7 @@ __host__ __device__ __forceinline__ size_t group_smem_bytes(int nmax, int G, int
                                                             int mat = kMat6, int stage = kStageFull, int narr = 4) {
     size_t b = (stage & kStageNoCoefWindow) ? 0 : round128(static_cast<size_t>(cbx) * cby * sizeof(T));
     b += round128(static_cast<size_t>(rbx) * rby * sizeof(float));
-    b += round128(16 + static_cast<size_t>(mat) * sizeof(double) + 16);
+    b += round128(16 + static_cast<size_t>(mat) * sizeof(double) + 32);
     b += round128((static_cast<size_t>(64) * G + static_cast<size_t>(narr) * nmax) * sizeof(T));
     return b;
 }
@@ -906,7 +921,7 @@ struct GroupSmem {
         bar = reinterpret_cast<uint64_t*>(g);
         hinv = reinterpret_cast<double*>(g + 16);
         ints = reinterpret_cast<int*>(g + 16 + static_cast<size_t>(mat) * sizeof(double));
-        g += round128(16 + static_cast<size_t>(mat) * sizeof(double) + 16);
+        g += round128(16 + static_cast<size_t>(mat) * sizeof(double) + 32);
         red = reinterpret_cast<T*>(g);
         sm = red + 64 * G;
     }
@@ -925,6 +940,10 @@ __device__ __forceinline__ bool warp_interp(const Env<T>& e, int cx, int cy, con
                                             int nt, Kahan<T>& sg, Kahan<T>& sg2, const T* s_chk = nullptr) {
     const int ww = cwin ? e.cbx : 0, wh = cwin ? e.cby : 0;  // no window: every stencil from global memory
     constexpr int NB = DEG + 1, OFF = DEG / 2;
+    // window position of the stencil corner of a sample at integer offset (ix, iy) from the centre
+    const int lc0 = cx + e.border - OFF - wc0, lr0 = cy + e.border - OFF - wr0;
+    const bool has_win = cwin != nullptr;
+    const unsigned uw = has_win ? static_cast<unsigned>(ww - NB) : 0u, uh = has_win ? static_cast<unsigned>(wh - NB) : 0u;
     bool ok = true;
     const T xlo = T(-cx), ylo = T(-cy), xhi = T(e.w - 1 - cx), yhi = T(e.h - 1 - cy);
 #pragma unroll 2
@@ -946,16 +965,17 @@ __device__ __forceinline__ bool warp_interp(const Env<T>& e, int cx, int cy, con
         T wx[NB], wy[NB];
         weights<DEG, T>(dx, wx);
         weights<DEG, T>(dy, wy);
-        const int col = cx + ix + e.border - OFF, row = cy + iy + e.border - OFF;  // stencil corner
-        const int lc = col - wc0, lr = row - wr0;
+        const int lc = ix + lc0, lr = iy + lr0;  // stencil corner in the window
         T c[NB][NB];
-        if (lc >= 0 && lr >= 0 && lc + NB <= ww && lr + NB <= wh) {
+        // a window, 0 <= lc <= ww - NB and 0 <= lr <= wh - NB (unsigned compares)
+        if (has_win && static_cast<unsigned>(lc) <= uw && static_cast<unsigned>(lr) <= uh) {
             const T* b = cwin + lr * ww + lc;
 #pragma unroll
             for (int m = 0; m < NB; ++m)
 #pragma unroll
                 for (int q = 0; q < NB; ++q) c[m][q] = b[m * ww + q];
         } else {
+            const int col = lc + wc0, row = lr + wr0;  // stencil corner in the coefficient image
             const T* b = e.coef + static_cast<size_t>(row) * e.cpitch + col;
 #pragma unroll
             for (int m = 0; m < NB; ++m)
@@ -1021,7 +1041,7 @@ template <int DEG, typename T, int G, typename M>
 __device__ __forceinline__ bool stage_windows(const Env<T>& e, const CUtensorMap* tm_ref, const CUtensorMap* tm_coef,
                                               int cx, int cy, const M (&p0)[6], const GroupSmem<T>& gs,
                                               uint32_t& phase, int tid, int bar_id, int& rx0, int& ry0, int& wc0,
-                                              int& wr0) {
+                                              int& wr0, bool with_coef = true) {
     constexpr int OFF = DEG / 2;
     const int r = e.radius;
     rx0 = floor_to(cx - r - 1, 4);  // 16-byte aligned x (float)
@@ -1045,12 +1065,13 @@ __device__ __forceinline__ bool stage_windows(const Env<T>& e, const CUtensorMap
         wr0 = min(max(r0, -e.cby), e.h + 2 * e.border);
     }
     group_sync<G>(bar_id);  // previous readers of the windows are done
+    const bool coef = with_coef && gs.cwin != nullptr;
     if (tid == 0) {
         fence_proxy_async();
         mbar_expect_tx(gs.bar, static_cast<uint32_t>(e.rbx * e.rby * sizeof(float) +
-                                                     (gs.cwin ? e.cbx * e.cby * sizeof(T) : 0)));
+                                                     (coef ? e.cbx * e.cby * sizeof(T) : 0)));
         tma_load_2d(gs.rwin, tm_ref, rx0, ry0, gs.bar);
-        if (gs.cwin) tma_load_2d(gs.cwin, tm_coef, wc0, wr0, gs.bar);
+        if (coef) tma_load_2d(gs.cwin, tm_coef, wc0, wr0, gs.bar);
     }
     long long spins = 0;
     while (!mbar_try_wait(gs.bar, phase)) {
@@ -1081,39 +1102,20 @@ __device__ __forceinline__ void ref_gradient(const float* rwin, int rww, int rx0
         (yp - ym == 2 ? T(0.5) : T(1));
 }
 
-// The per-POI solve.  OPT 0 = ICGN (icgn.cpp:446-627), 1 = FGN (forward_gauss_newton.cpp:188-399).
-// `off` is the sample-offset table in shared memory; `phase` the parity of the group's
-// mbarrier (flips once per staged POI).  Returns false only when a TMA wait timed out (the
-// kernel must then leave: the copy may still land in shared memory).
-template <int OPT, int DEG, typename T, int G>
-__device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUtensorMap* tm_coef, const short2* off,
-                          int cx, int cy, const typename MixedOf<T>::type (&p0)[6],
-                          typename MixedOf<T>::type conf, const GroupSmem<T>& gs, uint32_t& phase, int tid,
-                          int bar_id, Result<typename MixedOf<T>::type>& R) {
-    using M = typename MixedOf<T>::type;
+// The reference side of a solve (icgn.cpp:470-545; forward_gauss_newton.cpp:230-262): the
+// subset's mean and norm from compensated shifted sums and, for ICGN, the Hessian from 18 sums
+// and its inverse in the group's s_hinv.  With `store`, the raw reference values and (ICGN) the
+// reference gradients go to s_fn, s_a, s_b and f^ is formed in s_fn.  Returns TDIC_SUCCESS or
+// TDIC_NUMERICAL_FAILURE.  A solve and the set-up precompute run this same code, so a cached
+// set-up holds the values the solve would compute.
+template <int OPT, int G, typename T, typename M>
+__device__ __forceinline__ int ref_setup(const Env<T>& e, const short2* off, int cx, int cy, const GroupSmem<T>& gs,
+                                         int rx0, int ry0, bool store, T* s_fn, T* s_a, T* s_b, int& rp, int tid,
+                                         int bar_id, T& fm, T& inv_norm) {
     constexpr int NT = 32 * G;
     M* s_hinv = reinterpret_cast<M*>(gs.hinv);
     T* red = gs.red;
-    result_init(R, p0, conf);
-    int rp = 0;  // reduction-buffer parity
-    const int r = e.radius;
-    if (e.w <= 0 || r < 1 || e.max_iter < 0) return true;
-    if (cx - r < 0 || cy - r < 0 || cx + r >= e.w || cy + r >= e.h) return true;
-    if (e.n < 6) return true;
-    // per-sample arrays (full staging: f^, gradients, g; lean: what the iterations write)
-    const bool lean = (gs.stage & kStageLean) != 0;
-    T* s_fn = lean ? nullptr : gs.sm;
-    T* s_a = lean ? (OPT == 1 ? gs.sm : nullptr) : gs.sm + e.nmax;            // ICGN: reference gx; FGN: deformed gx
-    T* s_b = lean ? (OPT == 1 ? gs.sm + e.nmax : nullptr) : gs.sm + 2 * e.nmax;  // ICGN: reference gy; FGN: deformed gy
-    T* s_g = lean ? (OPT == 1 ? gs.sm + 2 * e.nmax : gs.sm) : gs.sm + 3 * e.nmax;
-    const int W = e.w, H = e.h;
-
-    int rx0, ry0, wc0, wr0;
-    if (!stage_windows<DEG, T, G, M>(e, tm_ref, tm_coef, cx, cy, p0, gs, phase, tid, bar_id, rx0, ry0, wc0, wr0))
-        return false;
-
-    // --- one pass: reference values, gradients, shifted sums and Hessian sums ------------------
-    const int rww = e.rbx;
+    const int W = e.w, H = e.h, rww = e.rbx;
     const float fshift = gs.rwin[(cy - ry0) * rww + (cx - rx0)];  // centre pixel: sums of f - fshift
     Kahan<T> k1, k2;
     T hs[18];
@@ -1123,14 +1125,14 @@ __device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUte
         const short2 o = off[i];
         const int x = cx + o.x, y = cy + o.y;
         const float f = gs.rwin[(y - ry0) * rww + (x - rx0)];
-        if (!lean) s_fn[i] = T(f);
+        if (store) s_fn[i] = T(f);
         const T fd = T(f) - T(fshift);
         k1.add(fd);
         k2.add(fd * fd);
         if constexpr (OPT == 0) {
             T a, b;
             ref_gradient<T>(gs.rwin, rww, rx0, ry0, W, H, x, y, a, b);
-            if (!lean) {
+            if (store) {
                 s_a[i] = a;
                 s_b[i] = b;
             }
@@ -1159,14 +1161,14 @@ __device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUte
     // normalisation: mean = shift + S1/N, sum (f - mean)^2 = S2 - S1 * (S1/N), the latter as one
     // fused multiply-add (a single rounding of the exact difference); the compensated sums
     // S1, S2 carry the accuracy.
-    const M inv_n = M(e.inv_n), thr = M(e.thr);
+    const M inv_n = M(e.inv_n);
     const M s1 = static_cast<M>(v20[0]), s2 = static_cast<M>(v20[1]);
     const M mshift = s1 * inv_n;
     const M ss = fma(-s1, mshift, s2);
-    if (!(ss > M(kEps * kEps))) { R.status = TDIC_NUMERICAL_FAILURE; return true; }  // |f - mean| <= 1e-12
-    const T fm = T(M(fshift) + mshift);
-    const T inv_norm = T(1) / sqrt(T(ss));
-    if (!lean)
+    if (!(ss > M(kEps * kEps))) return TDIC_NUMERICAL_FAILURE;  // |f - mean| <= 1e-12
+    fm = T(M(fshift) + mshift);
+    inv_norm = T(1) / sqrt(T(ss));
+    if (store)
         for (int i = tid; i < e.n; i += NT) s_fn[i] = mul_rn(s_fn[i] - fm, inv_norm);
     if constexpr (OPT == 0) {
         M S[18];
@@ -1174,10 +1176,125 @@ __device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUte
         for (int k = 0; k < 18; ++k) S[k] = static_cast<M>(v20[2 + k]);
         M Hm[6][6];
         hessian_from_sums<M>(S, M(2) * inv_norm * inv_norm, Hm);
-        const bool good = factor_inverse<G, M>(Hm, s_hinv, tid, bar_id);
-        if (!good) { R.status = TDIC_NUMERICAL_FAILURE; return true; }
+        if (!factor_inverse<G, M>(Hm, s_hinv, tid, bar_id)) return TDIC_NUMERICAL_FAILURE;
     }
+    return TDIC_SUCCESS;
+}
+
+// Fill the set-up cache entry of grid point `idx` at (cx, cy) (ICGN, first-order ZNSSD): stage the
+// reference window, run ref_setup, store the inverse Hessian, mean and norm, then publish the
+// state with release semantics.  Points the solve never sets up (outside the margin, too few
+// samples) are left alone.  Returns false only when the TMA wait timed out.
+template <int DEG, typename T, int G>
+__device__ bool precompute_setup(const Env<T>& e, const CUtensorMap* tm_ref, const short2* off, int cx, int cy,
+                                 const GroupSmem<T>& gs, uint32_t& phase, int tid, int bar_id, int idx) {
+    using M = typename MixedOf<T>::type;
+    constexpr int NT = 32 * G;
+    const int r = e.radius;
+    if (e.w <= 0 || r < 1 || e.max_iter < 0 || e.n < 6) return true;
+    if (cx - r < 0 || cy - r < 0 || cx + r >= e.w || cy + r >= e.h) return true;
+    const M p0[6] = {M(0), M(0), M(0), M(0), M(0), M(0)};
+    int rx0, ry0, wc0, wr0;
+    if (!stage_windows<DEG, T, G, M>(e, tm_ref, nullptr, cx, cy, p0, gs, phase, tid, bar_id, rx0, ry0, wc0, wr0,
+                                     false))
+        return false;
+    int rp = 0;
+    T fm, inv_norm;
+    const int st = ref_setup<0, G, T, M>(e, off, cx, cy, gs, rx0, ry0, false, nullptr, nullptr, nullptr, rp, tid,
+                                         bar_id, fm, inv_norm);
+    group_sync<G>(bar_id);  // the inverse is complete in shared memory
+    if (st == TDIC_SUCCESS) {
+        const M* s_hinv = reinterpret_cast<const M*>(gs.hinv);
+        M* hin = reinterpret_cast<M*>(e.sc_hinv) + 36 * static_cast<size_t>(idx);
+        for (int k = tid; k < 36; k += NT) hin[k] = s_hinv[k];
+        if (tid == 0) {
+            e.sc_fmn[2 * static_cast<size_t>(idx)] = fm;
+            e.sc_fmn[2 * static_cast<size_t>(idx) + 1] = inv_norm;
+        }
+    }
+    group_sync<G>(bar_id);  // every thread's stores precede thread 0's release
+    if (tid == 0) {
+        __threadfence();
+        st_release_s32(e.sc_state + idx, st == TDIC_SUCCESS ? 1 : 2);
+    }
+    return true;
+}
+
+// The per-POI solve.  OPT 0 = ICGN (icgn.cpp:446-627), 1 = FGN (forward_gauss_newton.cpp:188-399).
+// `off` is the sample-offset table in shared memory; `phase` the parity of the group's
+// mbarrier (flips once per staged POI).  Returns false only when a TMA wait timed out (the
+// kernel must then leave: the copy may still land in shared memory).
+template <int OPT, int DEG, typename T, int G>
+__device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUtensorMap* tm_coef, const short2* off,
+                          int cx, int cy, const typename MixedOf<T>::type (&p0)[6],
+                          typename MixedOf<T>::type conf, const GroupSmem<T>& gs, uint32_t& phase, int tid,
+                          int bar_id, Result<typename MixedOf<T>::type>& R, int sc_idx = -1) {
+    using M = typename MixedOf<T>::type;
+    constexpr int NT = 32 * G;
+    M* s_hinv = reinterpret_cast<M*>(gs.hinv);
+    T* red = gs.red;
+    result_init(R, p0, conf);
+    int rp = 0;  // reduction-buffer parity
+    const int r = e.radius;
+    if (e.w <= 0 || r < 1 || e.max_iter < 0) return true;
+    if (cx - r < 0 || cy - r < 0 || cx + r >= e.w || cy + r >= e.h) return true;
+    if (e.n < 6) return true;
+    // per-sample arrays (full staging: f^, gradients, g; lean: what the iterations write)
+    const bool lean = (gs.stage & kStageLean) != 0;
+    T* s_fn = lean ? nullptr : gs.sm;
+    T* s_a = lean ? (OPT == 1 ? gs.sm : nullptr) : gs.sm + e.nmax;            // ICGN: reference gx; FGN: deformed gx
+    T* s_b = lean ? (OPT == 1 ? gs.sm + e.nmax : nullptr) : gs.sm + 2 * e.nmax;  // ICGN: reference gy; FGN: deformed gy
+    T* s_g = lean ? (OPT == 1 ? gs.sm + 2 * e.nmax : gs.sm) : gs.sm + 3 * e.nmax;
+    const int W = e.w, H = e.h;
+
+    // a cached set-up of this grid point (ICGN): thread 0 reads its state before the staging,
+    // whose first barrier publishes it to the group (one decision for the whole group)
+    const bool cache = OPT == 0 && e.sc_state != nullptr && sc_idx >= 0;
+    if (cache && tid == 0) gs.ints[4] = ld_acquire_s32(e.sc_state + sc_idx);
+    int rx0, ry0, wc0, wr0;
+    if (!stage_windows<DEG, T, G, M>(e, tm_ref, tm_coef, cx, cy, p0, gs, phase, tid, bar_id, rx0, ry0, wc0, wr0))
+        return false;
+    const int cstate = cache ? gs.ints[4] : 0;
+    const int rww = e.rbx;
+    T fm, inv_norm;
+    if (cstate == 2) { R.status = TDIC_NUMERICAL_FAILURE; return true; }
+    if (cstate == 1) {
+        // the values ref_setup gives, computed by another group: mean, norm, inverse Hessian
+        fm = __ldcg(e.sc_fmn + 2 * static_cast<size_t>(sc_idx));
+        inv_norm = __ldcg(e.sc_fmn + 2 * static_cast<size_t>(sc_idx) + 1);
+        const M* hin = reinterpret_cast<const M*>(e.sc_hinv) + 36 * static_cast<size_t>(sc_idx);
+        for (int k = tid; k < 36; k += NT) s_hinv[k] = __ldcg(hin + k);
+        if (!lean)
+            for (int i = tid; i < e.n; i += NT) {
+                const short2 o = off[i];
+                const int x = cx + o.x, y = cy + o.y;
+                s_fn[i] = mul_rn(T(gs.rwin[(y - ry0) * rww + (x - rx0)]) - fm, inv_norm);
+                T a, b;
+                ref_gradient<T>(gs.rwin, rww, rx0, ry0, W, H, x, y, a, b);
+                s_a[i] = a;
+                s_b[i] = b;
+            }
+    } else {
+        const int st = ref_setup<OPT, G, T, M>(e, off, cx, cy, gs, rx0, ry0, !lean, s_fn, s_a, s_b, rp, tid, bar_id,
+                                               fm, inv_norm);
+        if (st != TDIC_SUCCESS) { R.status = st; return true; }
+    }
+    const M inv_n = M(e.inv_n), thr = M(e.thr);
     group_sync<G>(bar_id);  // f^ (and the inverse) visible to the whole group
+    if (cache && cstate == 0 && tid < 32) {
+        // publish this set-up for later solves of the point (warp 0; the others go on)
+        M* hin = reinterpret_cast<M*>(e.sc_hinv) + 36 * static_cast<size_t>(sc_idx);
+        for (int k = tid; k < 36; k += 32) hin[k] = s_hinv[k];
+        if (tid == 0) {
+            e.sc_fmn[2 * static_cast<size_t>(sc_idx)] = fm;
+            e.sc_fmn[2 * static_cast<size_t>(sc_idx) + 1] = inv_norm;
+        }
+        __syncwarp();
+        if (tid == 0) {
+            __threadfence();
+            st_release_s32(e.sc_state + sc_idx, 1);
+        }
+    }
 
     M p[6];
     for (int k = 0; k < 6; ++k) p[k] = p0[k];
@@ -1686,8 +1803,9 @@ __device__ __forceinline__ bool solve_any(const Env<T>& e, const CUtensorMap* tm
                                           const short2* off, int cx, int cy,
                                           const typename MixedOf<T>::type (&p0)[6], typename MixedOf<T>::type conf,
                                           const GroupSmem<T>& gs, uint32_t& phase, int tid, int bar_id,
-                                          Result<typename MixedOf<T>::type>& R) {
-    if constexpr (VAR == 0) return solve_poi<OPT, DEG, T, G>(e, tm_ref, tm_coef, off, cx, cy, p0, conf, gs, phase, tid, bar_id, R);
+                                          Result<typename MixedOf<T>::type>& R, int sc_idx = -1) {
+    if constexpr (VAR == 0)
+        return solve_poi<OPT, DEG, T, G>(e, tm_ref, tm_coef, off, cx, cy, p0, conf, gs, phase, tid, bar_id, R, sc_idx);
     else return solve_poi_var<OPT, DEG, T, G, VAR>(e, tm_ref, tm_coef, off, cx, cy, p0, conf, gs, phase, tid, bar_id, R);
 }
 
@@ -1849,6 +1967,11 @@ struct PropEnv {
     int* dcnt;                    // parents resolved so far
     unsigned long long* dq;       // queue items: parent (high 32, -1 = orphan) : point (low 32)
     float* kcorr;                 // ZNSSD of accepted points (wave keys of the clean-up)
+    // set-up precompute (single pair, ICGN, the Env's set-up cache): grid points in the order
+    // idle solver groups set them up (nearest the seed first), their count and the ticket counter
+    const int* pre_order;
+    int pre_count;
+    int* pre_ticket;
     // explicit tree (mode 3, a round of the heap order): every queued point is solved from its
     // tree parent and its tree children are queued after it; the raw result of every solve
     // (accepted or not) goes to the result table, the host decides acceptance
@@ -2382,13 +2505,19 @@ __device__ __forceinline__ void propagate_body(const Src& src, const Shape& sh) 
             // thread derives the same child); otherwise it asks its resolver lane for an item.
             int cont_c = -1, cont_p = -1;
             P cp[6];
+            bool asked = false;          // thread 0: a request to the resolver lane is open
+            bool precompute = one && OPT == 0 && VAR == 0 && src.env(0).sc_state != nullptr && g.pre_order != nullptr;
             while (true) {
-                int item_c = cont_c, item_p = cont_p, state = 0;  // state: 0 item, 1 done, 2 error
+                // state: 0 item, 1 done, 2 error, 3 precompute the set-up of point item_c
+                int item_c = cont_c, item_p = cont_p, state = 0;
                 if (cont_c < 0) {
                     if (tid == 0) {
-                        vst(&slot->ready, 0);
-                        __threadfence_block();
-                        vst(&slot->want, 1);
+                        if (!asked) {
+                            vst(&slot->ready, 0);
+                            __threadfence_block();
+                            vst(&slot->want, 1);
+                            asked = true;
+                        }
                         unsigned long long spins = 0;
                         while (true) {
                             const int r = vld(&slot->ready);
@@ -2397,13 +2526,34 @@ __device__ __forceinline__ void propagate_body(const Src& src, const Shape& sh) 
                                 state = r == 1 ? 0 : (r == 2 ? 1 : 2);
                                 item_c = slot->c;
                                 item_p = slot->par;
+                                asked = false;
                                 break;
+                            }
+                            if (precompute) {
+                                // nothing to solve yet: set up a point ahead of the wavefront
+                                const int k = atomicAdd(g.pre_ticket, 1);
+                                if (k < g.pre_count) {
+                                    state = 3;
+                                    item_c = g.pre_order[k];
+                                    break;
+                                }
+                                precompute = false;
                             }
                             if (++spins > kSpinLimit) { atomicExch(g.err, 1); state = 2; break; }
                             __nanosleep(spins < 64 ? 20 : 200);
                         }
                     }
                     group_bcast3<G>(state, item_c, item_p, ints + 1, tid, bar_id);
+                    if (state == 3) {
+                        const PropEnv& pe = src.prop(0);
+                        const int nx = (item_c % pe.gw) * pe.step, ny = (item_c / pe.gw) * pe.step;
+                        if (pe.roi_grid[item_c] != 0 && !precompute_setup<DEG, T, G>(src.env(0), src.tm_ref(0), s_tab + src.table(0), nx, ny, gs,
+                                                         phase, tid, bar_id, item_c)) {
+                            if (tid == 0) atomicExch(g.err, 1);
+                            return;  // TMA wait timed out
+                        }
+                        continue;
+                    }
                     if (state != 0) break;
                 }
                 const int j = src.job_of(item_c), n = src.point_of(item_c);
@@ -2436,7 +2586,7 @@ __device__ __forceinline__ void propagate_body(const Src& src, const Shape& sh) 
                         extrapolate(pp, static_cast<P>(nx - (item_p % pe.gw) * pe.step),
                                     static_cast<P>(ny - (item_p / pe.gw) * pe.step), p0);
                         if (!solve_any<OPT, DEG, T, G, VAR>(e, src.tm_ref(j), src.tm_coef(j), s_tab + src.table(j), nx,
-                                                            ny, p0, P(0), gs, phase, tid, bar_id, R)) {
+                                                            ny, p0, P(0), gs, phase, tid, bar_id, R, n)) {
                             if (tid == 0) atomicExch(g.err, 1);
                             return;  // TMA wait timed out
                         }
@@ -2520,7 +2670,7 @@ __device__ __forceinline__ void propagate_body(const Src& src, const Shape& sh) 
                         static_cast<P>(ny - (parent / pe.gw) * pe.step), p0);
             Result<P> R;
             if (!solve_any<OPT, DEG, T, G, VAR>(e, src.tm_ref(j), src.tm_coef(j), s_tab + src.table(j), nx, ny, p0,
-                                                P(0), gs, phase, tid, bar_id, R)) {
+                                                P(0), gs, phase, tid, bar_id, R, n)) {
                 if (tid == 0) atomicExch(g.err, 1);
                 return;  // TMA wait timed out
             }
@@ -2802,6 +2952,11 @@ void propagate_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, con
                                              kPropGroupsPerBlock, 32);
     e.stage = sc.stage;
     e.narr = sc.narr;
+    if (VAR == 0 && OPT == 0 && L.sc_state != nullptr) {
+        e.sc_hinv = L.sc_hinv;
+        e.sc_fmn = static_cast<T*>(L.sc_fmn);
+        e.sc_state = L.sc_state;
+    }
     const size_t smem = sc.smem;
     const int threads = 32 * G * sc.gpb + 32;  // solver groups + the resolver warp
     const int blocks = sc.per_sm * ctx->num_sms;
@@ -2820,6 +2975,9 @@ void propagate_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, con
     pe.dstate = L.dstate; pe.dcnt = L.dcnt; pe.dq = L.dq; pe.kcorr = L.kcorr;
     pe.qword = reinterpret_cast<unsigned long long*>(L.counters + 4);
     pe.tchild_off = L.tchild_off; pe.tchild = L.tchild; pe.tcont = L.tcont;
+    pe.pre_order = e.sc_state != nullptr ? L.pre_order : nullptr;
+    pe.pre_count = L.pre_count;
+    pe.pre_ticket = L.pre_ticket;
     pe.rcorr = L.rcorr; pe.rq = L.rq; pe.rmeta = L.rmeta; pe.riters = L.riters;
     if (L.params) pe.params = L.params;  // a heap-order round keeps its parameters across rounds
     const int n = L.gw * L.gh;

@@ -107,6 +107,11 @@ struct tdic_ctx {
     // the last heap-order propagation: device rounds after the dataflow pass, and solves in them
     int heap_rounds = 0;
     long long heap_solves = 0;
+    double heap_sim_ms = 0.0;  // host time in the heap simulations
+    // the set-up precompute order of the last grid and seed (grid points by distance from it)
+    tdic::Buffer pre_order;
+    int pre_key[3] = {-1, -1, -1};
+    int pre_count = 0;
 };
 
 struct tdic_pair {
@@ -188,10 +193,28 @@ struct PropagateLaunch {
     const uint8_t* roi_px = nullptr;
     // a round of the heap order (mode 3): the tree of this round, the result table
     const int* tchild_off = nullptr; const int* tchild = nullptr; const int* tcont = nullptr;
+    // set-up cache of the grid (first-order ZNSSD ICGN; see Env::sc_*) and the order in which
+    // idle solver groups fill it, with its ticket counter (zeroed by the caller); NULL = none
+    void* sc_hinv = nullptr; void* sc_fmn = nullptr; int* sc_state = nullptr;
+    const int* pre_order = nullptr; int pre_count = 0; int* pre_ticket = nullptr;
     void* rcorr = nullptr; void* rq = nullptr; unsigned char* rmeta = nullptr; int* riters = nullptr;
 };
 void launch_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const PropagateLaunch& L,
                       cudaStream_t s);
+
+// The set-up cache of a propagation grid (first-order ZNSSD ICGN without masked subsets): per
+// grid point the reference side of the solve, filled by idle solver groups ahead of the solves
+// and by every solve that computes it.  setup_cache_prepare sizes it in the pair's precision,
+// zeroes its states and ticket on `s` and sets the fields of L (the precompute order, grid
+// points by Manhattan distance from the seed, is kept by the context for the next call).
+struct SetupCache {
+    Buffer hinv, fmn, state, ticket;
+};
+inline bool setup_cache_applies(const tdic_config& c) {
+    return c.optimizer == 0 && c.shape_order == 1 && c.criterion == 1 && !c.truncate_roi_subsets;
+}
+void setup_cache_prepare(tdic_ctx* ctx, tdic_pair* pair, int gw, int gh, int sgx, int sgy, SetupCache& c,
+                         PropagateLaunch& L, cudaStream_t s);
 size_t propagate_param_bytes(int precision);
 void launch_init_grid(const tdic_grid_out& out, int gw, int gh, int step, cudaStream_t s);
 // Outputs of a heap-order propagation from its result table (parameters and correlations in the

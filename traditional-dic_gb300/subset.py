@@ -59,10 +59,11 @@ class Context:
         return int(self.lib.tdic_ctx_device_bytes(self.handle))
 
     def heap_stats(self) -> tuple:
-        """(device rounds, solves in them) of the last heap-order propagation on this context."""
-        r, n = C.c_int32(), C.c_int64()
-        self.check(self.lib.tdic_ctx_heap_stats(self.handle, C.byref(r), C.byref(n)))
-        return r.value, n.value
+        """(device rounds, solves in them, host ms in the heap simulations) of the last
+        heap-order propagation on this context."""
+        r, n, ms = C.c_int32(), C.c_int64(), C.c_double()
+        self.check(self.lib.tdic_ctx_heap_stats(self.handle, C.byref(r), C.byref(n), C.byref(ms)))
+        return r.value, n.value, ms.value
 
     def close(self) -> None:
         if getattr(self, "handle", None):
