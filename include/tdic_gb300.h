@@ -348,6 +348,18 @@ tdic_status tdic_ls_strain_2d(tdic_ctx* ctx, const double* points, const double*
                               int32_t n, double radius, int32_t min_samples, int32_t green_lagrange,
                               tdic_ls_strain* out, void* stream);
 
+/* The displacement CSV of the subset workflow, save_subset_csv
+ * (python/traditional_dic/workflows/subset_2d.py:34-54), byte for byte: the header
+ * "x,y,u,v,du_dx,du_dy,dv_dx,dv_dy,correlation,valid", then one row per grid point with each
+ * float64 as Python's str() writes it (shortest round-trip digits; positional for decimal
+ * exponents -4 .. 15, else scientific) and valid as 0 or 1, CRLF line ends as csv.writer ends
+ * them.  grid: the arrays x .. correlation and valid of n points, host or device per `memory`
+ * (device arrays are read straight from the device); formatted on every host thread.  ctx may
+ * be NULL for host arrays (no device is touched; tdic_last_error(NULL) then holds a failure's
+ * message). */
+tdic_status tdic_write_subset_csv(tdic_ctx* ctx, const char* path, const tdic_grid_out* grid, tdic_memory memory,
+                                  int32_t n);
+
 /* Whole pybind path: _traditional_dic.subset.compute (bind_subset.cpp:253-315) ->
  * SubsetDIC::compute (subset_dic.cpp:39-105).  Host images of `dtype`, host roi (NULL = full
  * image), host outputs of grid_w*grid_h entries (tdic_subset_grid_dims).  *n_points =

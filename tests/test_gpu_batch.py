@@ -76,6 +76,22 @@ def test_batch_matches_single_propagation(gpu_ctx, batch_inputs):
     b.close()
 
 
+def test_batch_device_outputs_to_csv(gpu_ctx, batch_inputs, tmp_path):
+    """The subset CSV written straight from a job's device arrays equals the one written from
+    its host copy, byte for byte."""
+    from traditional_dic_gb300 import subset as S, results
+    pairs, cfgs, seeds, rois = batch_inputs
+    b = S.Batch(gpu_ctx, pairs, cfgs, seeds, rois)
+    b.launch()
+    b.finish()
+    for j in (0, 2):
+        gh, gw = b.grid_shapes[j]
+        results.save_subset_csv_device(b.device_outputs(j), gh * gw, tmp_path / f"dev{j}.csv", context=gpu_ctx)
+        results.save_subset_csv(b.outputs(j), tmp_path / f"host{j}.csv")
+        assert (tmp_path / f"dev{j}.csv").read_bytes() == (tmp_path / f"host{j}.csv").read_bytes(), j
+    b.close()
+
+
 def test_batch_job_without_seed_keeps_defaults(gpu_ctx, batch_inputs):
     from traditional_dic_gb300 import subset as S, _lib as L
     pairs, cfgs, seeds, _ = batch_inputs

@@ -64,6 +64,52 @@ def test_result_writers(tmp_path, pkg):
     assert st["u_mean"] == pytest.approx(res["u"][res["valid"]].mean())
 
 
+def _python_csv(res, path):
+    """The reference's writer loop (csv.writer, str() of each float, int valid) as the checker."""
+    from traditional_dic_gb300 import results
+    cols = [np.asarray(res[k]) for k in results.SUBSET_COLUMNS]
+    with open(path, "w", newline="", encoding="utf-8") as f:
+        w = csv.writer(f)
+        w.writerow(results.SUBSET_COLUMNS)
+        for i in range(len(cols[0])):
+            w.writerow([float(c[i]) for c in cols[:-1]] + [int(cols[-1][i])])
+
+
+def test_subset_csv_bytes_equal_csv_writer(tmp_path, pkg):
+    """The library's CSV writer against csv.writer byte for byte: random doubles over every
+    decimal exponent, the positional/scientific switches (1e-4 / 1e-5, 1e15 / 1e16), integers,
+    signed zeros, NaN and infinities, denormals and the extremes, and an empty grid."""
+    from traditional_dic_gb300 import results
+    rng = np.random.default_rng(11)
+    special = np.array([0.0, -0.0, 1.0, -1.0, 0.1, 1e-4, 9.999e-5, 1e-5, 1.5e-5, 123456789012345.0,
+                        1e15, 9999999999999998.0, 1e16, 1.5e16, 1e22, 1e100, 5e-324, 2.2250738585072014e-308,
+                        1.7976931348623157e308, np.nan, np.inf, -np.inf, 1234567.0, 0.30000000000000004,
+                        100.0, 2.5, -3.75e-7, 6.02214076e23, 1 / 3, 2 / 3])
+    n = 5000
+    mant = rng.uniform(-10, 10, n) * 10.0 ** rng.integers(-30, 30, n)
+    for k, name in enumerate(results.SUBSET_COLUMNS[:-1]):
+        col = rng.permutation(np.concatenate([special, mant[: n - len(special)]]))
+        if k == 0:
+            col[:len(special)] = special
+        res_k = col
+        if name in ("x", "y"):
+            res_k = np.where(rng.random(n) < 0.5, np.round(col), col)
+        if k == 0:
+            res = {}
+        res[name] = res_k
+    res["u"][: 64] = rng.standard_normal(64).astype(np.float32)  # float32 values widened to double
+    res["valid"] = rng.random(n) < 0.7
+    results.save_subset_csv(res, tmp_path / "native.csv")
+    _python_csv(res, tmp_path / "python.csv")
+    assert (tmp_path / "native.csv").read_bytes() == (tmp_path / "python.csv").read_bytes()
+    empty = {k: np.zeros(0) for k in results.SUBSET_COLUMNS}
+    results.save_subset_csv(empty, tmp_path / "e.csv")
+    _python_csv(empty, tmp_path / "pe.csv")
+    assert (tmp_path / "e.csv").read_bytes() == (tmp_path / "pe.csv").read_bytes()
+    with pytest.raises(Exception, match="cannot open"):
+        results.save_subset_csv(res, tmp_path / "missing_dir" / "x" / "..")
+
+
 def _compare(got, want, tol=1e-9):
     assert np.array_equal(got.valid, want["valid"])
     assert np.array_equal(got.sample_count, want["sample_count"])

@@ -111,6 +111,7 @@ SIGNATURES = {
     "tdic_batch_destroy": (None, [C.c_void_p]),
     "tdic_subset_prepare": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int, C.c_void_p,
                                       C.POINTER(Config), C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(Seed)]),
+    "tdic_write_subset_csv": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p, C.c_int, C.c_int32]),
     "tdic_ls_strain_2d": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.c_int32,
                                     C.c_void_p, C.c_void_p]),
     "tdic_select_seed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Config),
@@ -170,5 +171,5 @@ def subset_grid_dims(w: int, h: int, cfg: Config):
 
 def check(status: int, ctx) -> None:
     if status != TDIC_OK:
-        msg = load().tdic_last_error(ctx).decode() if ctx else ""
+        msg = load().tdic_last_error(ctx).decode()  # NULL: this thread's context-free message
         raise TdicError(status, msg)

@@ -716,7 +716,8 @@ void tdic_grid_dims(int32_t w, int32_t h, int32_t spacing, int32_t* gw, int32_t*
 }
 
 namespace {
-// the message of this thread's last failed tdic_ctx_create (there is no context to hold it)
+// the message of this thread's last failed tdic_ctx_create or context-free call (there is no
+// context to hold it)
 thread_local std::string g_create_error;
 }  // namespace
 
@@ -1103,6 +1104,32 @@ static void truncated_compute(tdic_ctx* ctx, const void* reference, const void* 
         ++k;
     }
     *n_points = k;
+}
+
+tdic_status tdic_write_subset_csv(tdic_ctx* ctx, const char* path, const tdic_grid_out* grid, tdic_memory memory,
+                                  int32_t n) {
+    auto body = [&] {
+        TDIC_REQUIRE(grid != nullptr, TDIC_INVALID_ARG, "null argument");
+        check_memory(memory);
+        if (memory == TDIC_DEVICE) {
+            TDIC_REQUIRE(ctx != nullptr, TDIC_INVALID_ARG, "device arrays need a context");
+            TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
+        }
+        write_subset_csv(path, *grid, memory, n);
+    };
+    if (ctx) return guarded(ctx, body);
+    // host arrays without a context: the message goes where tdic_last_error(NULL) reads it
+    g_create_error.clear();
+    try {
+        body();
+        return TDIC_OK;
+    } catch (const Error& e) {
+        g_create_error = e.msg;
+        return e.code;
+    } catch (const std::exception& e) {
+        g_create_error = e.what();
+        return TDIC_INVALID_ARG;
+    }
 }
 
 tdic_status tdic_ls_strain_2d(tdic_ctx* ctx, const double* points, const double* displacement, int32_t n,

@@ -248,6 +248,9 @@ private:
 void integer_search_batch(tdic_ctx* ctx, tdic_pair* lazy, const tdic_config& cfg, const int* cx, const int* cy,
                           int n, SearchResult* out, cudaStream_t s, const uint8_t* roi = nullptr);
 
+// The subset workflow's displacement CSV (results.cpp) from host or device arrays.
+void write_subset_csv(const char* path, const tdic_grid_out& grid, tdic_memory memory, int32_t n);
+
 // Least-squares strain (strain.cu).
 void ls_strain_2d(tdic_ctx* ctx, const double* points, const double* disp, int n, double radius, int min_samples,
                   int green, tdic_ls_strain* out, cudaStream_t s);

@@ -1,27 +1,47 @@
 """Result files of the subset workflow, mirroring python/traditional_dic/workflows/subset_2d.py:
-the displacement CSV (save_subset_csv, :34-54) and the statistics JSON (write_stats, :94-113),
-written from a result dict of ``subset.compute`` (host arrays) or of a batch job."""
+the displacement CSV (save_subset_csv, :34-54) and the statistics JSON (write_stats, :94-113).
+
+The CSV is written by the library (tdic_write_subset_csv): byte for byte the file the reference's
+csv.writer loop writes, formatted on every host thread, from host arrays (a result dict of
+``subset.compute``) or straight from device arrays (``save_subset_csv_device``: a batch job's or a
+propagation's device outputs)."""
 from __future__ import annotations
 
-import csv
+import ctypes as C
 import json
 from pathlib import Path
 
 import numpy as np
 
+from . import _lib as L
+
 SUBSET_COLUMNS = ["x", "y", "u", "v", "du_dx", "du_dy", "dv_dx", "dv_dy", "correlation", "valid"]
 
 
-def save_subset_csv(result: dict, path) -> None:
+def save_subset_csv(result: dict, path, context=None) -> None:
     """One row per grid point: x, y, u, v, the four displacement gradients, correlation, valid."""
     path = Path(path)
     path.parent.mkdir(parents=True, exist_ok=True)
-    cols = [np.asarray(result[k]) for k in SUBSET_COLUMNS]
-    with path.open("w", newline="", encoding="utf-8") as f:
-        writer = csv.writer(f)
-        writer.writerow(SUBSET_COLUMNS)
-        for i in range(len(cols[0])):
-            writer.writerow([float(c[i]) for c in cols[:-1]] + [int(cols[-1][i])])
+    cols = {k: np.ascontiguousarray(result[k], dtype=np.float64) for k in SUBSET_COLUMNS[:-1]}
+    cols["valid"] = np.ascontiguousarray(result["valid"], dtype=np.uint8)
+    n = len(cols["x"])
+    if any(len(c) != n for c in cols.values()):
+        raise ValueError("result columns differ in length")
+    g = L.GridOut(**{k: cols[k].ctypes.data for k in SUBSET_COLUMNS})
+    lib = L.load()
+    handle = context.handle if context is not None else None  # host arrays need no device
+    L.check(lib.tdic_write_subset_csv(handle, str(path).encode(), C.byref(g), L.HOST, n), handle)
+
+
+def save_subset_csv_device(grid: "L.GridOut", n: int, path, context=None) -> None:
+    """The same file from device arrays (x .. correlation float64, valid uint8, n points)."""
+    path = Path(path)
+    path.parent.mkdir(parents=True, exist_ok=True)
+    if context is None:
+        from . import subset as S
+        context = S.default_context()
+    context.check(context.lib.tdic_write_subset_csv(context.handle, str(path).encode(), C.byref(grid), L.DEVICE,
+                                                    int(n)))
 
 
 def subset_stats(result: dict, metric: str = "znssd") -> dict:
