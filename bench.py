@@ -5,9 +5,9 @@ u = 0.5 sin(2 pi x / 256), v = 0.3 cos(2 pi y / 192), noise 1), first-order ZNSS
 B-spline, subset radius 15, POI step 5 (410 x 410 grid, 163,216 interior POIs), threshold 1e-3,
 20 iterations, seed from the reference initializer.
 
-One step = the hot path over one image pair with the inputs resident in HBM: image conversion
-and B-spline prefilter (K1), then the propagation over every grid POI (K3, dataflow order by
-default), with device outputs.  ``value`` = converged POIs (valid, strictly converged, accepted) / step time.
+One step = the hot path over one image pair with the inputs resident in HBM: the pair set-up
+(K1, one launch: float32 copies of both images and the B-spline prefilter), then the
+propagation over every grid POI (K3, dataflow order by default), with device outputs.  ``value`` = converged POIs (valid, strictly converged, accepted) / step time.
 ``e2e`` = the same through the public API ``subset.compute`` with pinned host images: upload,
 seed selection, prefilter, propagation and the device->host result dict, every step.
 L2 (129 MB) is flushed with a 256 MB write between timed steps.
@@ -15,6 +15,9 @@ L2 (129 MB) is flushed with a 256 MB write between timed steps.
 ``cpu_baseline`` is the FP64 C++ port of the reference path (oracle/) on every host thread over
 the whole workload (dataflow order, each diagonal's solves spread over the threads);
 ``cpu_baseline_serial`` is the same port on one thread in the reference's heap order, on a prefix.
+
+``prefilter`` times the pair set-up launch alone (L2 flushed before each) on the benchmark pair
+and on a 5120 x 5120 uint16 pair, against the measured HBM bandwidth.
 
 The default run also carries the uneven 48-pair batch in one graph-replayed launch
 (``batched_uneven``) and the served Poisson request stream with its p50 / p99 latency
@@ -84,6 +87,56 @@ CONFIG = {
     "seed_selection": {"seed_count": 64, "max_znssd": 0.3, "min_texture_std": 0.02},
     "reliability_propagation": {"spacing": 4, "max_znssd": 0.5},
 }
+
+
+def prefilter_bytes(side: int, in_bytes: int, coef_bytes: int, border: int = 3) -> int:
+    """Algorithmic bytes of one pair set-up launch on a side x side pair: both raw images read,
+    both float32 images and the (side + 2 border)^2 coefficients written."""
+    c = side + 2 * border
+    return 2 * side * side * in_bytes + 2 * side * side * 4 + c * c * coef_bytes
+
+
+def run_prefilter(ctx, stream, flush, pair, ref_d, def_d, hbm_gbs) -> dict:
+    """The pair set-up launch (prefilter_fused_kernel) alone, CUDA events on its stream, L2
+    flushed before each launch: the benchmark pair and a 5120^2 uint16 pair (seeded uniform
+    pixels; the kernel's work does not depend on the pixel values)."""
+    import torch
+    from traditional_dic_gb300 import subset as S
+
+    def timed(p, r, d, reps=20):
+        for _ in range(3):
+            p.update(r, d, stream=stream)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                p.update(r, d, stream=stream)
+                b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b) * 1e-3)
+        return statistics.median(ts)
+
+    out = []
+    side = int(ref_d.shape[0])
+    t = timed(pair, ref_d, def_d)
+    nb = prefilter_bytes(side, ref_d.element_size(), 4)
+    out.append({"image": f"{side}x{side} uint8", "coefficients": "float32", "us": 1e6 * t, "algorithmic_bytes": nb,
+                "achieved_gbs": nb / t / 1e9, "frac": nb / t / 1e9 / hbm_gbs})
+    rng = np.random.default_rng(5120)
+    big = [torch.from_numpy(rng.integers(0, 65536, (5120, 5120), dtype=np.uint16)).to(ref_d.device) for _ in range(2)]
+    p5 = S.Pair(ctx, big[0], big[1], degree=3, stream=stream)
+    t = timed(p5, big[0], big[1])
+    p5.close()
+    nb = prefilter_bytes(5120, 2, 4)
+    out.append({"image": "5120x5120 uint16", "coefficients": "float32", "us": 1e6 * t, "algorithmic_bytes": nb,
+                "achieved_gbs": nb / t / 1e9, "frac": nb / t / 1e9 / hbm_gbs})
+    del big
+    return {"kernel": "prefilter_fused_kernel<In, float, 3> (pair set-up: both images to float32 + "
+                      "B-spline coefficients)", "bound": "hbm", "peak_gbs": hbm_gbs,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth, of measured)", "workloads": out}
 
 
 def icgn_flops(iterations: np.ndarray, n_samples: int) -> float:
@@ -435,6 +488,8 @@ def run_ours(args, world, rank, local, pg):
                 "traffic": PROPAGATE_DRAM_BYTES if args.side == 2048 else None,
                 "hbm_peak_gbs": peaks.get("hbm_gbs")}
 
+    pre = run_prefilter(ctx, stream, flush, pair, ref_d, def_d, peaks.get("hbm_gbs") or 6795.8)
+
     # FP64 GPU path on the same configuration, for the precision comparison.
     res32 = {k: outs[k].cpu().numpy().copy() for k in ("u", "v", "valid", "converged", "zncc")}
     fp64 = None
@@ -551,8 +606,9 @@ def run_ours(args, world, rank, local, pg):
             "heap_order": heap,
             "gpu_launches": 5 * args.steps,
             "clocks": clk,
-            "stages_ms": {"prefilter_and_convert": 1e3 * (statistics.median(times) - t_prop),
+            "stages_ms": {"pair_setup": 1e3 * (statistics.median(times) - t_prop),
                           "propagate": 1e3 * t_prop},
+            "prefilter": pre,
         }
         if routes is not None:
             line["routes"] = routes

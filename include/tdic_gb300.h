@@ -196,6 +196,10 @@ void tdic_pair_destroy(tdic_pair* pair);
 /* Copy the coefficient image ((H+2B) x (W+2B), float32 or float64 per the pair's precision)
  * into a host buffer of `bytes` bytes; for tests. */
 tdic_status tdic_pair_coefficients(tdic_pair* pair, void* host_out, size_t bytes);
+/* Copy the pair's float32 reference and deformed images (H x W each, what dic::Image holds:
+ * integer pixels exactly, float64 pixels rounded to float32) into host buffers of W*H floats;
+ * either pointer may be NULL; for tests. */
+tdic_status tdic_pair_images(tdic_pair* pair, float* reference_out, float* deformed_out);
 
 /* Reference-image gradients, kernel K2 (build_reference_gradient_cache,
  * reliability_propagation.cpp:84-112): central differences on raw pixels, one-sided at the

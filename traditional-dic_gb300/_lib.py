@@ -90,6 +90,7 @@ SIGNATURES = {
     "tdic_pair_update": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int, C.c_int, C.c_void_p]),
     "tdic_pair_destroy": (None, [C.c_void_p]),
     "tdic_pair_coefficients": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "tdic_pair_images": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "tdic_reference_gradient": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "tdic_solve_pois": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Config), C.c_void_p, C.c_int32, C.c_void_p,
                                   C.c_int, C.c_void_p]),

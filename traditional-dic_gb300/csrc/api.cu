@@ -208,28 +208,34 @@ void check_memory(tdic_memory mem) {
     TDIC_REQUIRE(mem == TDIC_HOST || mem == TDIC_DEVICE, TDIC_INVALID_ARG, "memory must be TDIC_HOST or TDIC_DEVICE");
 }
 
-// Upload (or alias) one image and convert it to float32 into dst.
-void upload_convert(tdic_pair* p, const void* src, int pitch, tdic_dtype dtype, tdic_memory mem, float* dst,
-                    cudaStream_t s) {
+// The pair's device images from the caller's (host: staged through one upload buffer holding
+// both; device: read in place): exact cubic / quintic pairs in one fused launch (float32
+// reference, float32 deformed copy, coefficients), others by conversion plus a padded copy.
+void pair_compute(tdic_pair* p, const void* ref, const void* def, int pitch, tdic_dtype dtype, tdic_memory mem,
+                  cudaStream_t s) {
     const size_t es = dtype_size(dtype);
     TDIC_REQUIRE(es != 0, TDIC_INVALID_ARG, "unknown dtype");
     check_memory(mem);
     const int pt = pitch > 0 ? pitch : p->w;
     TDIC_REQUIRE(pt >= p->w, TDIC_INVALID_ARG, "pitch smaller than width");
-    const void* dsrc = src;
+    const void* dref = ref;
+    const void* ddef = def;
     if (mem == TDIC_HOST) {
         const size_t bytes = es * static_cast<size_t>(pt) * p->h;
-        if (p->staging.bytes < bytes) p->staging = Buffer(&p->ctx->pool, bytes);
-        TDIC_CUDA_TRY(cudaMemcpyAsync(p->staging.ptr, src, bytes, cudaMemcpyHostToDevice, s));
-        dsrc = p->staging.ptr;
+        const size_t slot = (bytes + 255) / 256 * 256;
+        if (p->staging.bytes < 2 * slot) p->staging = Buffer(&p->ctx->pool, 2 * slot);
+        auto* base = static_cast<unsigned char*>(p->staging.ptr);
+        TDIC_CUDA_TRY(cudaMemcpyAsync(base, ref, bytes, cudaMemcpyHostToDevice, s));
+        TDIC_CUDA_TRY(cudaMemcpyAsync(base + slot, def, bytes, cudaMemcpyHostToDevice, s));
+        dref = base;
+        ddef = base + slot;
     }
-    launch_convert(dsrc, p->w, p->h, pt, dtype, dst, p->rpitch, s);
-}
-
-void pair_compute(tdic_pair* p, const void* ref, const void* def, int pitch, tdic_dtype dtype, tdic_memory mem,
-                  cudaStream_t s) {
-    upload_convert(p, ref, pitch, dtype, mem, p->ref.as<float>(), s);
-    upload_convert(p, def, pitch, dtype, mem, p->def_f.as<float>(), s);
+    if (p->exact && p->degree != 1) {
+        launch_pair_setup(p, dref, ddef, pt, dtype, s);
+        return;
+    }
+    launch_convert(dref, p->w, p->h, pt, dtype, p->ref.as<float>(), p->rpitch, s);
+    launch_convert(ddef, p->w, p->h, pt, dtype, p->def_f.as<float>(), p->rpitch, s);
     launch_prefilter(p, p->def_f.as<float>(), s);
 }
 
@@ -867,6 +873,18 @@ tdic_status tdic_pair_coefficients(tdic_pair* pair, void* host_out, size_t bytes
         TDIC_CUDA_TRY(cudaDeviceSynchronize());
         TDIC_CUDA_TRY(cudaMemcpy2D(host_out, es * pair->cw, pair->coef.ptr, es * pair->cpitch, es * pair->cw, pair->ch,
                                    cudaMemcpyDeviceToHost));
+    });
+}
+
+tdic_status tdic_pair_images(tdic_pair* pair, float* reference_out, float* deformed_out) {
+    if (!pair) return TDIC_INVALID_ARG;
+    return guarded(pair->ctx, [&] {
+        TDIC_CUDA_TRY(cudaDeviceSynchronize());
+        const size_t row = sizeof(float) * pair->w, dpitch = sizeof(float) * pair->rpitch;
+        if (reference_out)
+            TDIC_CUDA_TRY(cudaMemcpy2D(reference_out, row, pair->ref.ptr, dpitch, row, pair->h, cudaMemcpyDeviceToHost));
+        if (deformed_out)
+            TDIC_CUDA_TRY(cudaMemcpy2D(deformed_out, row, pair->def_f.ptr, dpitch, row, pair->h, cudaMemcpyDeviceToHost));
     });
 }
 

@@ -100,10 +100,12 @@ __device__ __forceinline__ T warp_scatter_sum(const T (&v)[K], int lane) {
 
 // All-reduce K values over the group: every thread ends with the same sums (summed in the same
 // order), so redundant scalar math stays bit-identical across the group's warps.  A warp
-// reduce-scatter, then thread k < K adds the G warp partials of value k, then everyone reads
-// the K totals.  `red` holds two buffers of 32*G values used alternately (parity `rp`): a
-// buffer is rewritten only after every thread has passed the barriers of the reduction in
-// between.
+// reduce-scatter, then, for K <= 8, every thread adds the G warp partials of each value itself
+// (one barrier); for larger K thread k < K adds those of value k and everyone reads the K
+// totals after a second barrier (summing K*G partials in every thread would spill).  Both
+// forms add the partials in warp order.  `red` holds two buffers of 32*G values used
+// alternately (parity `rp`): a buffer is rewritten only after every thread has passed the
+// barrier of the reduction in between, which it reaches after its last read of the buffer.
 template <int G, int K, typename T>
 __device__ __forceinline__ void group_sum(T (&v)[K], T* red_base, int& rp, int tid, int bar_id) {
     static_assert(G == 1 || K * (G + 1) <= 32 * G, "reduction scratch: G*K partials + K totals per buffer");
@@ -116,20 +118,30 @@ __device__ __forceinline__ void group_sum(T (&v)[K], T* red_base, int& rp, int t
         for (int k = 0; k < K; ++k) v[k] = __shfl_sync(0xffffffffu, r, k << (5 - LG));
     } else {
         T* red = red_base + rp * 32 * G;
-        T* tot = red + G * K;
         rp ^= 1;
         const int warp = tid >> 5;
         if ((lane & ((1 << (5 - LG)) - 1)) == 0 && idx < K) red[warp * K + idx] = r;
         named_bar(bar_id, 32 * G);
-        if (tid < K) {
-            T acc = red[tid];
+        if constexpr (K <= 8) {
 #pragma unroll
-            for (int w = 1; w < G; ++w) acc += red[w * K + tid];
-            tot[tid] = acc;
+            for (int k = 0; k < K; ++k) {
+                T acc = red[k];
+#pragma unroll
+                for (int w = 1; w < G; ++w) acc += red[w * K + k];
+                v[k] = acc;
+            }
+        } else {
+            T* tot = red + G * K;
+            if (tid < K) {
+                T acc = red[tid];
+#pragma unroll
+                for (int w = 1; w < G; ++w) acc += red[w * K + tid];
+                tot[tid] = acc;
+            }
+            named_bar(bar_id, 32 * G);
+#pragma unroll
+            for (int k = 0; k < K; ++k) v[k] = tot[k];
         }
-        named_bar(bar_id, 32 * G);
-#pragma unroll
-        for (int k = 0; k < K; ++k) v[k] = tot[k];
     }
 }
 

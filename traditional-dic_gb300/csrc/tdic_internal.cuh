@@ -122,8 +122,8 @@ struct tdic_pair {
     int cpitch = 0;            // elements per row of coef (128-byte multiple)
     tdic::Buffer ref;          // float32 H x W reference, row pitch rpitch (dic::Image stores float)
     tdic::Buffer coef;         // T coefficients of the deformed image, ch rows of cpitch
-    tdic::Buffer def_f;        // float32 H x W deformed, row pitch rpitch (prefilter input, seed search)
-    tdic::Buffer staging;      // raw input staging for host uploads
+    tdic::Buffer def_f;        // float32 H x W deformed, row pitch rpitch (seed search, lazy pairs)
+    tdic::Buffer staging;      // raw input staging for host uploads (reference, then deformed)
     cudaEvent_t last_use = nullptr;  // recorded after the last work enqueued on the pair
     ~tdic_pair() {
         if (last_use) cudaEventDestroy(last_use);
@@ -154,6 +154,8 @@ inline void mark_use(tdic_pair* p, cudaStream_t s) {
 void launch_convert(const void* src, int w, int h, int pitch, tdic_dtype dtype, float* dst, int dst_pitch,
                     cudaStream_t s);
 void launch_prefilter(tdic_pair* pair, const float* image, cudaStream_t s);
+void launch_pair_setup(tdic_pair* pair, const void* ref, const void* def, int pitch, tdic_dtype dtype,
+                       cudaStream_t s);
 void launch_reference_gradient(const float* img, int w, int h, int pitch, double* gx, double* gy, cudaStream_t s);
 
 // Hot path (hotpath.cu) -------------------------------------------------------------------

@@ -163,6 +163,13 @@ class Pair:
         self.ctx.check(self.ctx.lib.tdic_pair_coefficients(self.handle, out.ctypes.data, out.nbytes))
         return out
 
+    def images(self) -> tuple:
+        """The float32 reference and deformed images the pair holds."""
+        r = np.empty((self.height, self.width), np.float32)
+        d = np.empty_like(r)
+        self.ctx.check(self.ctx.lib.tdic_pair_images(self.handle, r.ctypes.data, d.ctypes.data))
+        return r, d
+
     def reference_gradient(self):
         gx = np.empty((self.height, self.width), np.float64)
         gy = np.empty_like(gx)
