@@ -214,22 +214,19 @@ __global__ void __launch_bounds__(kRS) prefilter_fused_kernel(
     // Column sweep, causal (downwards) from a zero state at the top margin, 16 rows per batch:
     // every load of a batch (deformed rows, and the reference pixels this thread converts) is
     // issued before the first use, so a warp waits for memory once per batch, not once per row.
-    // Four forms of straight-line code, one branch per CTA: staged rows with one common
-    // alignment shift (the row pitch a multiple of 16 bytes) and every central row inside the
-    // image; the same with rows checked; staged rows with per-row shifts; per-element loads.
+    // Three forms of straight-line code, one branch per CTA: staged rows with one common
+    // alignment shift (the row pitch a multiple of 16 bytes); staged rows with per-row shifts;
+    // per-element loads, which also write the float32 copies of the owned pixels (staged tiles
+    // write theirs at the end, with 16-byte stores).
     // The gain g2 is applied once, when the row pass stores the coefficients.
     const int iy0 = y0 - M - border;  // image row of tile row r: iy0 + r (central rows are not wrapped)
-    const bool rows_in = iy0 + M >= 0 && iy0 + M + TH <= h;
     const bool uni = (static_cast<long long>(pitch) * es) % 16 == 0;
-    const int sd0 = staged ? static_cast<int>(reinterpret_cast<uintptr_t>(def + xs) & 15) : 0;  // the common shifts
-    const int sr0 = staged ? static_cast<int>(reinterpret_cast<uintptr_t>(ref + xs) & 15) : 0;
+    const int sd0 = staged ? static_cast<int>(reinterpret_cast<uintptr_t>(def + xs) & 15) : 0;  // the common shift
     const unsigned char* dcol = sdef + sd0 + c * es;  // this thread's column in the staged rows
-    const unsigned char* rcol = sref + sr0 + c * es;
     float* dfo = def_f + ix;
     float* rfo = ref_f + ix;
     T yc0 = T(0), yc1 = T(0);
-    // form: 0 staged, common shift, rows inside; 1 staged, common shift; 2 staged, per-row shifts;
-    // 3 per element
+    // form: 1 staged, common shift; 2 staged, per-row shifts; 3 per element
     auto sweep = [&](auto form_tag) {
         constexpr int F = decltype(form_tag)::value;
 #pragma unroll
@@ -242,10 +239,8 @@ __global__ void __launch_bounds__(kRS) prefilter_fused_kernel(
                 else if constexpr (F == 2) v[i] = px_float(*reinterpret_cast<const In*>(sdef + dsh[r] + c * es));
                 else v[i] = px_float(__ldg(def + srow[r] + sx));
                 rv[i] = 0.0f;
-                if (r >= M && r < M + TH) {
-                    if constexpr (F <= 1) rv[i] = px_float(*reinterpret_cast<const In*>(rcol + (r - M) * NCH * 16));
-                    else if constexpr (F == 2) rv[i] = px_float(*reinterpret_cast<const In*>(sref + rsh[r - M] + c * es));
-                    else if (own && static_cast<unsigned>(iy0 + r) < static_cast<unsigned>(h))
+                if constexpr (F == 3) {
+                    if (r >= M && r < M + TH && own && static_cast<unsigned>(iy0 + r) < static_cast<unsigned>(h))
                         rv[i] = px_float(__ldg(ref + srow[r] + sx));
                 }
             }
@@ -259,7 +254,7 @@ __global__ void __launch_bounds__(kRS) prefilter_fused_kernel(
                     o = yc1;
                 }
                 if (r >= M) buf[(r - M) * kRS + pc] = o;
-                if (r >= M && r < M + TH && own && (F == 0 || static_cast<unsigned>(iy0 + r) < static_cast<unsigned>(h))) {
+                if (F == 3 && r >= M && r < M + TH && own && static_cast<unsigned>(iy0 + r) < static_cast<unsigned>(h)) {
                     const int at = (iy0 + r) * fpitch;
                     dfo[at] = v[i];
                     rfo[at] = rv[i];
@@ -267,8 +262,7 @@ __global__ void __launch_bounds__(kRS) prefilter_fused_kernel(
             }
         }
     };
-    if (ST::on && staged && uni && rows_in) sweep(std::integral_constant<int, 0>{});
-    else if (ST::on && staged && uni) sweep(std::integral_constant<int, 1>{});
+    if (ST::on && staged && uni) sweep(std::integral_constant<int, 1>{});
     else if (ST::on && staged) sweep(std::integral_constant<int, 2>{});
     else sweep(std::integral_constant<int, 3>{});
     // Anti-causal (upwards) from a zero state at the bottom margin; the TH central rows stay.
@@ -322,6 +316,31 @@ __global__ void __launch_bounds__(kRS) prefilter_fused_kernel(
 #pragma unroll
                 for (int i = 0; i < kSR; ++i)
                     if (cx + i < cw) dst[i] = a[i];
+            }
+        }
+    }
+    // Float32 copies of the owned pixels of a staged tile from its staged rows: 4 columns per
+    // lane and 16-byte stores over the aligned column groups that cover the owned columns (a
+    // group shared with the next tile is written by both, with the same values).
+    if constexpr (ST::on) {
+        if (staged) {
+            const int g0 = (x0 - border) & ~3, ng = (((x0 - border + TW) + 3 & ~3) - g0) >> 2;
+            for (int q = warp; q < 2 * TH; q += kRS / 32) {
+                const int rr = q >> 1;
+                const int iy = y0 - border + rr;
+                if (static_cast<unsigned>(iy) >= static_cast<unsigned>(h)) continue;
+                const unsigned char* srow_b = (q & 1) ? sref + rsh[rr] : sdef + dsh[M + rr];
+                float* drow = ((q & 1) ? ref_f : def_f) + static_cast<size_t>(iy) * fpitch;
+                for (int gq = lane; gq < ng; gq += 32) {
+                    const int col = g0 + 4 * gq;
+                    const unsigned char* sp = srow_b + (col - xs) * es;
+                    float4 f;
+                    f.x = px_float(*reinterpret_cast<const In*>(sp));
+                    f.y = px_float(*reinterpret_cast<const In*>(sp + es));
+                    f.z = px_float(*reinterpret_cast<const In*>(sp + 2 * es));
+                    f.w = px_float(*reinterpret_cast<const In*>(sp + 3 * es));
+                    *reinterpret_cast<float4*>(drow + col) = f;
+                }
             }
         }
     }
