@@ -2256,14 +2256,25 @@ __device__ void tree_resolve(const PropEnv& pe, int n, int cont) {
     df_publish(pe, push, k, k - (cont >= 0 ? 0 : 1));
 }
 
-// Propagation groups: 4 warps per POI, two groups and one resolver warp per CTA, two CTAs per
-// SM.  Per-POI latency on the dataflow critical path bounds the propagation; measured on
-// 2048^2, r = 15: 8 warps per POI were 14% slower (the two-stage group reductions and barriers
-// grow with the group), four groups sharing one resolver warp 5% slower.
+// Propagation groups: 4 warps per POI and one resolver warp per CTA, one CTA per SM.  FP32:
+// three groups per CTA (456 groups on 152 SMs).  Per-POI latency on the dataflow critical path
+// bounds the propagation, and a solve shares its SM's issue slots with the other groups there:
+// measured on 2048^2, r = 15 (dataflow, FP32), four groups per SM (two CTAs of two, or one of
+// four) took 9.1-9.2 ms, three 8.4 ms (the register budget of one 416-thread CTA also removes
+// the spills), two 10.0 ms (too few groups for the widest wavefronts); 8 warps per POI were
+// 14-17% slower.  FP64: two groups per CTA, whose 288 threads leave room for the FP64 registers.
 constexpr int kPropG = 4;
-constexpr int kPropGroupsPerBlock = 2;
-constexpr int kPropMinBlocks = 2;  // resident CTAs per SM the register budget is sized for
-constexpr int kPropMaxThreads = 32 * kPropG * kPropGroupsPerBlock + 32;  // also 8-warp groups, one per CTA
+template <typename T> struct PropShape {
+    static constexpr int groups = sizeof(T) == 4 ? 3 : 2;         // solver groups per CTA
+    static constexpr int threads = 32 * kPropG * groups + 32;    // with the resolver warp
+    static constexpr int min_blocks = 1;                         // resident CTAs per SM
+};
+
+// The batched launch keeps its own shape: up to 288 threads (two 4-warp groups or one 8-warp
+// group and the resolver warp), two CTAs per SM.
+constexpr int kBatchMaxThreads = 288;
+constexpr int kBatchMinBlocks = 2;
+constexpr int kBatchGroupsPerBlockMax = 2;
 
 // Dataflow hand-over between a solver group and the resolver warp of its block (shared memory).
 template <typename P>
@@ -2700,7 +2711,7 @@ __device__ __forceinline__ void propagate_body(const Src& src, const Shape& sh) 
 }
 
 template <int OPT, int DEG, typename T, int G, int VAR = 0>
-__global__ void __launch_bounds__(kPropMaxThreads, sizeof(T) == 4 ? kPropMinBlocks : 1)
+__global__ void __launch_bounds__(PropShape<T>::threads, PropShape<T>::min_blocks)
     propagate_kernel(const __grid_constant__ Env<T> e, const __grid_constant__ CUtensorMap tm_ref,
                      const __grid_constant__ CUtensorMap tm_coef, const __grid_constant__ PropEnv pe) {
     propagate_body<OPT, DEG, T, G, OneJob<T>, VAR>(OneJob<T>{e, pe, &tm_ref, &tm_coef},
@@ -2708,7 +2719,7 @@ __global__ void __launch_bounds__(kPropMaxThreads, sizeof(T) == 4 ? kPropMinBloc
 }
 
 template <int OPT, int DEG, typename T, int G>
-__global__ void __launch_bounds__(kPropMaxThreads, sizeof(T) == 4 ? kPropMinBlocks : 1)
+__global__ void __launch_bounds__(kBatchMaxThreads, sizeof(T) == 4 ? kBatchMinBlocks : 1)
     propagate_batch_kernel(const BatchJob<T>* __restrict__ jobs, int njobs, const CUtensorMap* __restrict__ maps,
                            const __grid_constant__ Shape sh) {
     propagate_body<OPT, DEG, T, G>(JobTable<T>{jobs, njobs, maps}, sh);
@@ -2957,11 +2968,11 @@ void propagate_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, con
                            L.offsets, L.n_offsets, L.roi_px);
     TensorMaps tm = make_tensor_maps<T>(pair, e);
     using P = typename MixedOf<T>::type;
-    const size_t ctl = round128(kPropGroupsPerBlock * sizeof(DfSlot<P>)) + 128;  // resolver hand-over
+    const size_t ctl = round128(PropShape<T>::groups * sizeof(DfSlot<P>)) + 128;  // resolver hand-over
     auto kern = propagate_kernel<OPT, DEG, T, G, VAR>;
     const StageChoice sc = choose_staging<T>(ctx, kern, cfg.staging, VAR == 0, OPT, e.nmax, G, e.rbx, e.rby, e.cbx,
                                              e.cby, (VAR & 2) ? kMat12 : kMat6, cta_prefix_bytes(e.nmax), ctl,
-                                             kPropGroupsPerBlock, 32);
+                                             PropShape<T>::groups, 32);
     e.stage = sc.stage;
     e.narr = sc.narr;
     if (VAR == 0 && OPT == 0 && L.sc_state != nullptr) {
@@ -3039,7 +3050,7 @@ struct BatchPlan final : BatchPlanBase {
 template <int OPT, int DEG, typename T, int G>
 void batch_kernel_setup(BatchPlan<T>& b, tdic_ctx* ctx, int gpb, int requested) {
     const size_t prefix = cta_prefix_bytes(b.sh.ntab);
-    const size_t ctl = round128(kPropGroupsPerBlock * sizeof(DfSlot<typename MixedOf<T>::type>)) + 128;
+    const size_t ctl = round128(kBatchGroupsPerBlockMax * sizeof(DfSlot<typename MixedOf<T>::type>)) + 128;
     const int threads = 32 * G * gpb + 32;
     auto kern = propagate_batch_kernel<OPT, DEG, T, G>;
     const int stages[3] = {kStageFull, kStageLean, kStageLean | kStageNoCoefWindow};
