@@ -56,7 +56,7 @@ WORKLOAD = {
 }
 
 
-PROPAGATE_DRAM_BYTES = 36_848_896 + 500_992  # ncu, propagate_kernel, 2048^2 r=15, one launch
+PROPAGATE_DRAM_BYTES = 37_934_080 + 6_583_552  # ncu, propagate_kernel, 2048^2 r=15, one launch
 
 
 def workload_desc(side: int) -> dict:
