@@ -2270,11 +2270,13 @@ template <typename T> struct PropShape {
     static constexpr int min_blocks = 1;                         // resident CTAs per SM
 };
 
-// The batched launch keeps its own shape: up to 288 threads (two 4-warp groups or one 8-warp
-// group and the resolver warp), two CTAs per SM.
-constexpr int kBatchMaxThreads = 288;
-constexpr int kBatchMinBlocks = 2;
-constexpr int kBatchGroupsPerBlockMax = 2;
+// The batched launch's kernel shapes: narrow, up to 288 threads (two 4-warp groups or one 8-warp
+// group and the resolver warp) and two CTAs per SM; wide (FP32), three 4-warp groups and the
+// resolver warp in one 416-thread CTA per SM, as the single-pair launch.  The tuner times both.
+template <int WIDE> struct BatchBounds {
+    static constexpr int threads = WIDE ? 416 : 288;
+    static constexpr int min_blocks = WIDE ? 1 : 2;
+};
 
 // Dataflow hand-over between a solver group and the resolver warp of its block (shared memory).
 template <typename P>
@@ -2718,8 +2720,8 @@ __global__ void __launch_bounds__(PropShape<T>::threads, PropShape<T>::min_block
                                                    shape_of(e, pe.gw * pe.gh, (VAR & 2) ? kMat12 : kMat6));
 }
 
-template <int OPT, int DEG, typename T, int G>
-__global__ void __launch_bounds__(kBatchMaxThreads, sizeof(T) == 4 ? kBatchMinBlocks : 1)
+template <int OPT, int DEG, typename T, int G, int WIDE>
+__global__ void __launch_bounds__(BatchBounds<WIDE>::threads, sizeof(T) == 4 ? BatchBounds<WIDE>::min_blocks : 1)
     propagate_batch_kernel(const BatchJob<T>* __restrict__ jobs, int njobs, const CUtensorMap* __restrict__ maps,
                            const __grid_constant__ Shape sh) {
     propagate_body<OPT, DEG, T, G>(JobTable<T>{jobs, njobs, maps}, sh);
@@ -3029,7 +3031,7 @@ struct BatchPlan final : BatchPlanBase {
     Buffer d_jobs, d_maps, d_tab, d_roi, d_claim, d_key, d_params, d_dstate, d_dcnt, d_kcorr, d_dq, d_order, d_fetch,
         d_misc, d_flags, d_out;
     // launch configurations: (warps per POI, groups per CTA) -> grid size and shared memory
-    struct Config { int G, gpb, blocks, threads; size_t smem; int per_sm; int stage, narr; };
+    struct Config { int G, gpb, blocks, threads; size_t smem; int per_sm; int stage, narr, wide; };
     std::vector<Config> configs;
     int chosen = 0;
     int sms = 0;      // SMs' worth of blocks a launch uses (fewer than the device leaves room for other work)
@@ -3047,12 +3049,14 @@ struct BatchPlan final : BatchPlanBase {
 // The launch configurations of (G warps per POI, gpb groups per block): each staging mode the
 // request allows that fits, kept when it makes more groups resident than the fuller modes before
 // it (a leaner mode that fits no more groups only re-reads what the fuller one stages).
-template <int OPT, int DEG, typename T, int G>
+template <int OPT, int DEG, typename T, int G, int WIDE>
 void batch_kernel_setup(BatchPlan<T>& b, tdic_ctx* ctx, int gpb, int requested) {
     const size_t prefix = cta_prefix_bytes(b.sh.ntab);
-    const size_t ctl = round128(kBatchGroupsPerBlockMax * sizeof(DfSlot<typename MixedOf<T>::type>)) + 128;
+    const size_t ctl = round128(gpb * sizeof(DfSlot<typename MixedOf<T>::type>)) + 128;
     const int threads = 32 * G * gpb + 32;
-    auto kern = propagate_batch_kernel<OPT, DEG, T, G>;
+    static_assert(G * 32 + 32 <= BatchBounds<WIDE>::threads, "a group and the resolver fit the kernel's bound");
+    if (threads > BatchBounds<WIDE>::threads) return;
+    auto kern = propagate_batch_kernel<OPT, DEG, T, G, WIDE>;
     const int stages[3] = {kStageFull, kStageLean, kStageLean | kStageNoCoefWindow};
     const int want = requested == TDIC_STAGING_FULL ? 0 : requested == TDIC_STAGING_LEAN ? 1
                    : requested == TDIC_STAGING_LEAN_NO_WINDOW ? 2 : -1;
@@ -3073,11 +3077,11 @@ void batch_kernel_setup(BatchPlan<T>& b, tdic_ctx* ctx, int gpb, int requested) 
         TDIC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
         if (per_sm <= 0 || per_sm * gpb <= best_groups) continue;
         best_groups = per_sm * gpb;
-        b.configs.push_back({G, gpb, per_sm * ctx->num_sms, threads, smem, per_sm, stage, narr});
+        b.configs.push_back({G, gpb, per_sm * ctx->num_sms, threads, smem, per_sm, stage, narr, WIDE});
     }
 }
 
-template <int OPT, int DEG, typename T, int G>
+template <int OPT, int DEG, typename T, int G, int WIDE>
 void batch_kernel_launch(BatchPlan<T>& b, const typename BatchPlan<T>::Config& c, cudaStream_t s) {
     cudaLaunchConfig_t lc = {};
     lc.gridDim = dim3(std::min(c.blocks, c.per_sm * std::max(1, b.sms)));
@@ -3092,23 +3096,25 @@ void batch_kernel_launch(BatchPlan<T>& b, const typename BatchPlan<T>::Config& c
     Shape sh = b.sh;
     sh.stage = c.stage;
     sh.narr = c.narr;
-    TDIC_CUDA_TRY(cudaLaunchKernelEx(&lc, propagate_batch_kernel<OPT, DEG, T, G>, b.d_jobs.template as<BatchJob<T>>(),
+    TDIC_CUDA_TRY(cudaLaunchKernelEx(&lc, propagate_batch_kernel<OPT, DEG, T, G, WIDE>, b.d_jobs.template as<BatchJob<T>>(),
                                      b.n, b.d_maps.template as<CUtensorMap>(), sh));
 }
 
 template <int OPT, int DEG, typename T>
 void batch_configs(BatchPlan<T>& b, tdic_ctx* ctx, int requested) {
     b.configs.clear();
-    batch_kernel_setup<OPT, DEG, T, 4>(b, ctx, 2, requested);
-    batch_kernel_setup<OPT, DEG, T, 4>(b, ctx, 1, requested);
-    batch_kernel_setup<OPT, DEG, T, 8>(b, ctx, 1, requested);
+    batch_kernel_setup<OPT, DEG, T, 4, 0>(b, ctx, 2, requested);
+    batch_kernel_setup<OPT, DEG, T, 4, 0>(b, ctx, 1, requested);
+    batch_kernel_setup<OPT, DEG, T, 8, 0>(b, ctx, 1, requested);
+    if constexpr (sizeof(T) == 4) batch_kernel_setup<OPT, DEG, T, 4, 1>(b, ctx, 3, requested);
     TDIC_REQUIRE(!b.configs.empty(), TDIC_UNSUPPORTED, "batch: subset radius too large for shared memory");
 }
 
 template <int OPT, int DEG, typename T>
 void batch_dispatch(BatchPlan<T>& b, const typename BatchPlan<T>::Config& c, cudaStream_t s) {
-    if (c.G == 8) batch_kernel_launch<OPT, DEG, T, 8>(b, c, s);
-    else batch_kernel_launch<OPT, DEG, T, 4>(b, c, s);
+    if (c.G == 8) batch_kernel_launch<OPT, DEG, T, 8, 0>(b, c, s);
+    else if (c.wide) batch_kernel_launch<OPT, DEG, T, 4, 1>(b, c, s);
+    else batch_kernel_launch<OPT, DEG, T, 4, 0>(b, c, s);
 }
 
 template <typename T, typename F>
