@@ -285,7 +285,8 @@ tdic_status tdic_propagate_noalloc(tdic_ctx* ctx, tdic_pair* pair, const tdic_co
  * 2^22 grid points per job.  The batch owns device outputs (tdic_batch_outputs) and scratch;
  * its pairs must outlive it.
  *   tdic_batch_tune    times each launch configuration (warps per POI, groups per block) on
- *                      this batch and keeps the fastest; optional.
+ *                      this batch and keeps the fastest; optional (untuned, FP32 batches use
+ *                      three 4-warp groups per block, one block per SM: the single-pair shape).
  *   tdic_batch_launch  enqueues one propagation of every job on `stream` and returns without
  *                      waiting: device memsets and kernel launches only, so it can be captured
  *                      in a CUDA graph and replayed (synchronise the replay stream before

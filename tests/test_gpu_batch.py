@@ -63,7 +63,7 @@ def test_batch_matches_single_propagation(gpu_ctx, batch_inputs):
     from traditional_dic_gb300 import subset as S
     pairs, cfgs, seeds, rois = batch_inputs
     b = S.Batch(gpu_ctx, pairs, cfgs, seeds, rois)
-    assert b.config() == (4, 2, "full")  # untuned: 4-warp groups, two per block, as the single path
+    assert b.config() == (4, 3, "full")  # untuned: 4-warp groups, three per block, as the single path
     for _ in range(2):           # the second launch reuses (and re-initialises) the scratch
         b.launch()
         pc = b.finish()

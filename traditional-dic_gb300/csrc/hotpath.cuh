@@ -3103,10 +3103,11 @@ void batch_kernel_launch(BatchPlan<T>& b, const typename BatchPlan<T>::Config& c
 template <int OPT, int DEG, typename T>
 void batch_configs(BatchPlan<T>& b, tdic_ctx* ctx, int requested) {
     b.configs.clear();
+    // the first configuration is the untuned default: in FP32 the single-pair launch's shape
+    if constexpr (sizeof(T) == 4) batch_kernel_setup<OPT, DEG, T, 4, 1>(b, ctx, 3, requested);
     batch_kernel_setup<OPT, DEG, T, 4, 0>(b, ctx, 2, requested);
     batch_kernel_setup<OPT, DEG, T, 4, 0>(b, ctx, 1, requested);
     batch_kernel_setup<OPT, DEG, T, 8, 0>(b, ctx, 1, requested);
-    if constexpr (sizeof(T) == 4) batch_kernel_setup<OPT, DEG, T, 4, 1>(b, ctx, 3, requested);
     TDIC_REQUIRE(!b.configs.empty(), TDIC_UNSUPPORTED, "batch: subset radius too large for shared memory");
 }
 
