@@ -542,7 +542,7 @@ std::vector<std::pair<int, int>> seed_candidates(tdic_ctx* ctx, const Acc& ref, 
         std::vector<int> px(m), py(m);
         for (int j = 0; j < m; ++j) { px[j] = sp[j].x; py[j] = sp[j].y; }
         KmeansAssigner ka(ctx, px.data(), py.data(), m, count, s);
-        if (count <= 2048) {  // per-block sums in shared memory (24 bytes per centre)
+        if (count <= 2048) {  // per-block sums in shared memory (12 bytes per centre)
             ka.run(cx.data(), cy.data(), iters);
         } else {
             std::vector<int> asg(m);

@@ -399,31 +399,49 @@ __global__ void kmeans_assign_kernel(const int2* __restrict__ pts, int m, const 
 
 // One k-means iteration's assignment and centre sums.  The points are integer pixels and the
 // sums stay far below 2^53, so the FP64 sums of run_kmeans (seed_selector.cpp:84-104) are exact
-// whatever the order: they are accumulated here as 64-bit integers (per block in shared memory,
-// then atomically into `acc` = [sum x, sum y, count] per centre).
+// whatever the order: they are accumulated here as integers (per block in shared memory, 32-bit,
+// then atomically into the 64-bit `acc` = [sum x, sum y, count] per centre).  kKmeansLanes lanes
+// share a point: each scans every kKmeansLanes-th centre, and the lanes' (distance, index) minima
+// combine to the first centre at the smallest distance, which is the sequential scan's choice.
+constexpr int kKmeansLanes = 8;
+
 __global__ void kmeans_step_kernel(const int2* __restrict__ pts, int m, const double2* __restrict__ ctr, int k,
                                    unsigned long long* __restrict__ acc) {
-    extern __shared__ unsigned long long s_acc[];  // 3 * k
-    for (int i = threadIdx.x; i < 3 * k; i += blockDim.x) s_acc[i] = 0ull;
+    extern __shared__ unsigned int s_acc[];  // 3 * k
+    for (int i = threadIdx.x; i < 3 * k; i += blockDim.x) s_acc[i] = 0u;
     __syncthreads();
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = gt / kKmeansLanes, sub = gt % kKmeansLanes;
+    int best = -1;
+    double bd = INFINITY;
+    int2 pt = make_int2(0, 0);
     if (j < m) {
-        const double x = static_cast<double>(pts[j].x), y = static_cast<double>(pts[j].y);
-        int best = 0;
-        double bd = INFINITY;
-        for (int i = 0; i < k; ++i) {
+        pt = pts[j];
+        const double x = static_cast<double>(pt.x), y = static_cast<double>(pt.y);
+        for (int i = sub; i < k; i += kKmeansLanes) {
             const double2 c = __ldg(ctr + i);
             const double dx = __dsub_rn(x, c.x), dy = __dsub_rn(y, c.y);
             const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
             if (d2 < bd) { bd = d2; best = i; }
         }
-        atomicAdd(s_acc + 3 * best, static_cast<unsigned long long>(pts[j].x));
-        atomicAdd(s_acc + 3 * best + 1, static_cast<unsigned long long>(pts[j].y));
-        atomicAdd(s_acc + 3 * best + 2, 1ull);
+    }
+#pragma unroll
+    for (int o = kKmeansLanes / 2; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, bd, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, best, o);
+        if (ob < bd || (ob == bd && static_cast<unsigned>(oi) < static_cast<unsigned>(best))) {
+            bd = ob;
+            best = oi;
+        }
+    }
+    if (j < m && sub == 0 && best >= 0) {
+        atomicAdd(s_acc + 3 * best, static_cast<unsigned int>(pt.x));
+        atomicAdd(s_acc + 3 * best + 1, static_cast<unsigned int>(pt.y));
+        atomicAdd(s_acc + 3 * best + 2, 1u);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < 3 * k; i += blockDim.x)
-        if (s_acc[i]) atomicAdd(acc + i, s_acc[i]);
+        if (s_acc[i]) atomicAdd(acc + i, static_cast<unsigned long long>(s_acc[i]));
 }
 
 // New centres (sum / count, as on the reference's host) for every centre with members; the sums
@@ -465,10 +483,12 @@ void KmeansAssigner::run(double* cx, double* cy, int iters) {
     for (int i = 0; i < k_; ++i) c[i] = make_double2(cx[i], cy[i]);
     TDIC_CUDA_TRY(cudaMemcpyAsync(ctr_.ptr, c.data(), sizeof(double2) * k_, cudaMemcpyHostToDevice, s_));
     TDIC_CUDA_TRY(cudaMemsetAsync(acc_.ptr, 0, sizeof(unsigned long long) * 3 * k_, s_));
-    const size_t smem = sizeof(unsigned long long) * 3 * k_;
+    const size_t smem = sizeof(unsigned int) * 3 * k_;
+    const long long threads = static_cast<long long>(m_) * kKmeansLanes;
+    const int blocks = static_cast<int>((threads + 255) / 256);
     for (int it = 0; it < iters; ++it) {
-        kmeans_step_kernel<<<(m_ + 255) / 256, 256, smem, s_>>>(pts_.as<int2>(), m_, ctr_.as<double2>(), k_,
-                                                                acc_.as<unsigned long long>());
+        kmeans_step_kernel<<<blocks, 256, smem, s_>>>(pts_.as<int2>(), m_, ctr_.as<double2>(), k_,
+                                                      acc_.as<unsigned long long>());
         TDIC_CUDA_TRY(cudaGetLastError());
         kmeans_update_kernel<<<(k_ + 127) / 128, 128, 0, s_>>>(ctr_.as<double2>(), k_, acc_.as<unsigned long long>());
         TDIC_CUDA_TRY(cudaGetLastError());
