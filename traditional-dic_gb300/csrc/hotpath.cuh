@@ -1053,7 +1053,8 @@ template <int DEG, typename T, int G, typename M>
 __device__ __forceinline__ bool stage_windows(const Env<T>& e, const CUtensorMap* tm_ref, const CUtensorMap* tm_coef,
                                               int cx, int cy, const M (&p0)[6], const GroupSmem<T>& gs,
                                               uint32_t& phase, int tid, int bar_id, int& rx0, int& ry0, int& wc0,
-                                              int& wr0, bool with_coef = true) {
+                                              int& wr0, bool with_coef = true, const int* acquire_state = nullptr,
+                                              bool early = false) {
     constexpr int OFF = DEG / 2;
     const int r = e.radius;
     rx0 = floor_to(cx - r - 1, 4);  // 16-byte aligned x (float)
@@ -1076,7 +1077,10 @@ __device__ __forceinline__ bool stage_windows(const Env<T>& e, const CUtensorMap
         wc0 = floor_to(min(max(c0, -e.cbx), e.cw), kAlign);
         wr0 = min(max(r0, -e.cby), e.h + 2 * e.border);
     }
-    group_sync<G>(bar_id);  // previous readers of the windows are done
+    // early: the caller's every read of the windows precedes a group barrier it has passed, so
+    // thread 0 issues the copies at once; the barrier below then publishes what thread 0 read
+    // with acquire order (acquire_state -> ints[4]) while the copies are in flight
+    if (!early) group_sync<G>(bar_id);  // previous readers of the windows are done
     const bool coef = with_coef && gs.cwin != nullptr;
     if (tid == 0) {
         fence_proxy_async();
@@ -1084,7 +1088,9 @@ __device__ __forceinline__ bool stage_windows(const Env<T>& e, const CUtensorMap
                                                      (coef ? e.cbx * e.cby * sizeof(T) : 0)));
         tma_load_2d(gs.rwin, tm_ref, rx0, ry0, gs.bar);
         if (coef) tma_load_2d(gs.cwin, tm_coef, wc0, wr0, gs.bar);
+        if (acquire_state != nullptr) gs.ints[4] = ld_acquire_s32(acquire_state);
     }
+    if (early) group_sync<G>(bar_id);
     long long spins = 0;
     while (!mbar_try_wait(gs.bar, phase)) {
         if (++spins > kTmaSpinLimit) {
@@ -1259,12 +1265,14 @@ __device__ bool solve_poi(const Env<T>& e, const CUtensorMap* tm_ref, const CUte
     T* s_g = lean ? (OPT == 1 ? gs.sm + 2 * e.nmax : gs.sm) : gs.sm + 3 * e.nmax;
     const int W = e.w, H = e.h;
 
-    // a cached set-up of this grid point (ICGN): thread 0 reads its state before the staging,
-    // whose first barrier publishes it to the group (one decision for the whole group)
+    // a cached set-up of this grid point (ICGN): thread 0 reads its state while the staging
+    // copies fly, and the staging's barrier publishes it to the group (one decision for the
+    // whole group).  The staging starts at once: every read of the windows by this group
+    // precedes a group barrier (the reductions of the set-up and of every iteration).
     const bool cache = OPT == 0 && e.sc_state != nullptr && sc_idx >= 0;
-    if (cache && tid == 0) gs.ints[4] = ld_acquire_s32(e.sc_state + sc_idx);
     int rx0, ry0, wc0, wr0;
-    if (!stage_windows<DEG, T, G, M>(e, tm_ref, tm_coef, cx, cy, p0, gs, phase, tid, bar_id, rx0, ry0, wc0, wr0))
+    if (!stage_windows<DEG, T, G, M>(e, tm_ref, tm_coef, cx, cy, p0, gs, phase, tid, bar_id, rx0, ry0, wc0, wr0, true,
+                                     cache ? e.sc_state + sc_idx : nullptr, true))
         return false;
     const int cstate = cache ? gs.ints[4] : 0;
     const int rww = e.rbx;
