@@ -281,8 +281,9 @@ tdic_status tdic_propagate_noalloc(tdic_ctx* ctx, tdic_pair* pair, const tdic_co
  * Job j propagates pairs[j] from seeds[j] with cfgs[j] exactly as tdic_propagate does in the
  * dataflow order (same results); subset radius, spacing, iterations, thresholds and ROI
  * (rois[j]: host H x W mask or NULL; rois may be NULL) may differ between jobs, the spline
- * degree, precision and optimizer may not; propagation_mode must be 2.  At most 512 jobs and
- * 2^22 grid points per job.  The batch owns device outputs (tdic_batch_outputs) and scratch;
+ * degree, precision and optimizer may not; propagation_mode must be 2.  With
+ * truncate_roi_subsets (in every job or in none) the solves are masked by each job's ROI, as
+ * tdic_propagate's.  At most 512 jobs and 2^22 grid points per job.  The batch owns device outputs (tdic_batch_outputs) and scratch;
  * its pairs must outlive it.
  *   tdic_batch_tune    times each launch configuration (warps per POI, groups per block) on
  *                      this batch and keeps the fastest; optional (untuned, FP32 batches use

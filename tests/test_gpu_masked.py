@@ -140,16 +140,42 @@ def test_truncated_compute_matches_oracle(oracle, gpu_ctx, workload0, precision,
         assert got["valid"][edge].mean() > 0.5
 
 
-def test_truncate_rejected_where_not_covered(gpu_ctx, workload0):
-    """The batched launch, the preparation step and the no-allocation propagation do not take
-    masked subsets: they say so."""
+def test_masked_batch_matches_single(gpu_ctx, workload0):
+    """Masked subsets in the batched launch: a job with a ROI that has holes (one touches the
+    seed's neighbourhood) and a job without a ROI each give tdic_propagate's masked result bit for
+    bit, untuned and tuned; a batch mixing masked and plain jobs is refused."""
     import __graft_entry__ as G
-    from traditional_dic_gb300 import subset as S, _lib as L
+    from traditional_dic_gb300 import subset as S
+    p = workload0
+    _, seed = S.compute(p.reference, p.deformed, G.WORKLOAD0_CONFIG, context=gpu_ctx, return_seed=True)
+    assert seed.found
     cfg = S.config_from_dict(G.WORKLOAD0_CONFIG)
     cfg.truncate_roi_subsets = 1
-    p = workload0
+    cfg.propagation_mode = S.PROPAGATION_MODES["dataflow"]
+    h, w = p.reference.shape
+    roi = np.ones((h, w), bool)
+    sx, sy = int(round(seed.x)), int(round(seed.y))
+    roi[max(0, sy - 30):sy - 12, max(0, sx - 40):sx + 40] = False   # a band just above the seed
+    roi[h // 8: h // 4, w // 2: w // 2 + 30] = False
+    rois = [roi, None]
     pair = S.Pair(gpu_ctx, p.reference, p.deformed, degree=3)
-    seed = S.make_seed(128, 128, [0.0] * 6, 0.0)
-    with pytest.raises(Exception, match="UNSUPPORTED|masked"):
-        S.Batch(gpu_ctx, [pair], [cfg], [seed])
+    keys = ("x", "y", "u", "v", "du_dx", "du_dy", "dv_dx", "dv_dy", "correlation", "zncc", "valid", "converged",
+            "iterations", "status")
+    want = [S.propagate(gpu_ctx, pair, cfg, seed, roi=r) for r in rois]
+    b = S.Batch(gpu_ctx, [pair, pair], [cfg, cfg], [seed, seed], rois)
+    for tuned in (False, True):
+        if tuned:
+            b.tune()
+        b.launch()
+        pc = b.finish()
+        for j in range(2):
+            got = b.outputs(j)
+            assert pc[j] == want[j]["points_computed"] and pc[j] > 1, j
+            for k in keys:
+                assert np.array_equal(got[k], want[j][k], equal_nan=True), (tuned, j, k)
+    b.close()
+    plain = S.config_from_dict(G.WORKLOAD0_CONFIG)
+    plain.propagation_mode = S.PROPAGATION_MODES["dataflow"]
+    with pytest.raises(Exception, match="masked"):
+        S.Batch(gpu_ctx, [pair, pair], [cfg, plain], [seed, seed])
     pair.close()

@@ -20,8 +20,12 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libtdic_gb300.so")
 # (source, object, extra nvcc flags)
 UNITS = [("api.cu", "api.o", []), ("prefilter.cu", "prefilter.o", []), ("hotpath.cu", "hotpath.o", []),
-         ("heap_order.cu", "heap_order.o", []), ("batch.cu", "batch_f32.o", ["-DTDIC_BATCH_FP64=0"]),
-         ("batch.cu", "batch_f64.o", ["-DTDIC_BATCH_FP64=1"]), ("results.cpp", "results.o", []),
+         ("heap_order.cu", "heap_order.o", []),
+         ("batch.cu", "batch_f32.o", ["-DTDIC_BATCH_FP64=0", "-DTDIC_BATCH_VAR=0"]),
+         ("batch.cu", "batch_f64.o", ["-DTDIC_BATCH_FP64=1", "-DTDIC_BATCH_VAR=0"]),
+         ("batch.cu", "batch_f32_masked.o", ["-DTDIC_BATCH_FP64=0", "-DTDIC_BATCH_VAR=4"]),
+         ("batch.cu", "batch_f64_masked.o", ["-DTDIC_BATCH_FP64=1", "-DTDIC_BATCH_VAR=4"]),
+         ("results.cpp", "results.o", []),
          ("seed.cu", "seed.o", []), ("strain.cu", "strain.o", []),
          ("variants.cu", "route1.o", ["-DTDIC_ROUTE=1"]), ("variants.cu", "route2.o", ["-DTDIC_ROUTE=2"]),
          ("variants.cu", "route3.o", ["-DTDIC_ROUTE=3"]), ("variants.cu", "route4.o", ["-DTDIC_ROUTE=4"])]

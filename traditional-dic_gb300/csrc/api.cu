@@ -1440,8 +1440,10 @@ void batch_create_impl(tdic_ctx* ctx, int n, tdic_pair* const* pairs, const tdic
         TDIC_REQUIRE(p->degree == p0->degree && p->precision == p0->precision, TDIC_INVALID_ARG,
                      "batch: every pair must have the same spline degree and precision");
         TDIC_REQUIRE(c.optimizer == cfgs[0].optimizer, TDIC_INVALID_ARG, "batch: every job must use the same optimizer");
-        TDIC_REQUIRE(first_order_znssd(c) && !c.truncate_roi_subsets, TDIC_UNSUPPORTED,
-                     "batch: only the first-order ZNSSD route without masked subsets (propagate others one pair at a time)");
+        TDIC_REQUIRE(first_order_znssd(c), TDIC_UNSUPPORTED,
+                     "batch: only the first-order ZNSSD route (propagate others one pair at a time)");
+        TDIC_REQUIRE((c.truncate_roi_subsets != 0) == (cfgs[0].truncate_roi_subsets != 0), TDIC_INVALID_ARG,
+                     "batch: every job must use masked subsets, or none");
         TDIC_REQUIRE(c.propagation_mode == 2, TDIC_UNSUPPORTED, "batch: only the dataflow order (propagation_mode 2)");
         // seed alignment (reliability_propagation.cpp:201-216), as tdic_propagate
         const uint8_t* roi = rois ? rois[j] : nullptr;

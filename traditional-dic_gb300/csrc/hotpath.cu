@@ -13,6 +13,8 @@ void upload_qk_route3();
 void upload_qk_route4();
 void upload_qk_batch_f32();
 void upload_qk_batch_f64();
+void upload_qk_batch_f32_masked();
+void upload_qk_batch_f64_masked();
 void launch_solve_route1(tdic_ctx*, tdic_pair*, const tdic_config&, const SolveLaunch&, cudaStream_t);
 void launch_solve_route2(tdic_ctx*, tdic_pair*, const tdic_config&, const SolveLaunch&, cudaStream_t);
 void launch_solve_route3(tdic_ctx*, tdic_pair*, const tdic_config&, const SolveLaunch&, cudaStream_t);
@@ -30,6 +32,8 @@ void upload_qk_constants() {
     upload_qk_route4();
     upload_qk_batch_f32();
     upload_qk_batch_f64();
+    upload_qk_batch_f32_masked();
+    upload_qk_batch_f64_masked();
 }
 
 void launch_init_grid(const tdic_grid_out& out, int gw, int gh, int step, cudaStream_t s) {

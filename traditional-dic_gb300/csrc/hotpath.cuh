@@ -2728,11 +2728,11 @@ __global__ void __launch_bounds__(PropShape<T>::threads, PropShape<T>::min_block
                                                    shape_of(e, pe.gw * pe.gh, (VAR & 2) ? kMat12 : kMat6));
 }
 
-template <int OPT, int DEG, typename T, int G, int WIDE>
+template <int OPT, int DEG, typename T, int G, int WIDE, int VAR>
 __global__ void __launch_bounds__(BatchBounds<WIDE>::threads, sizeof(T) == 4 ? BatchBounds<WIDE>::min_blocks : 1)
     propagate_batch_kernel(const BatchJob<T>* __restrict__ jobs, int njobs, const CUtensorMap* __restrict__ maps,
                            const __grid_constant__ Shape sh) {
-    propagate_body<OPT, DEG, T, G>(JobTable<T>{jobs, njobs, maps}, sh);
+    propagate_body<OPT, DEG, T, G, JobTable<T>, VAR>(JobTable<T>{jobs, njobs, maps}, sh);
 }
 
 __global__ void init_grid_kernel(tdic_grid_out o, int gw, int gh, int step) {
@@ -3026,7 +3026,8 @@ void propagate_typed(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, con
 // ---------------------------------------------------------------------------------------
 // Batched propagation: several image pairs in one persistent launch.
 // ---------------------------------------------------------------------------------------
-template <typename T>
+// VAR: the solver route of every job (0 first-order ZNSSD; 4 the same with masked subsets).
+template <typename T, int VAR>
 struct BatchPlan final : BatchPlanBase {
     using P = typename MixedOf<T>::type;
     int n = 0, opt = 0, deg = 3;
@@ -3038,6 +3039,7 @@ struct BatchPlan final : BatchPlanBase {
     Shape sh{};
     Buffer d_jobs, d_maps, d_tab, d_roi, d_claim, d_key, d_params, d_dstate, d_dcnt, d_kcorr, d_dq, d_order, d_fetch,
         d_misc, d_flags, d_out;
+    std::vector<Buffer> d_roi_px;       // masked subsets: each job's pixel ROI (W x H bytes)
     // launch configurations: (warps per POI, groups per CTA) -> grid size and shared memory
     struct Config { int G, gpb, blocks, threads; size_t smem; int per_sm; int stage, narr, wide; };
     std::vector<Config> configs;
@@ -3057,16 +3059,17 @@ struct BatchPlan final : BatchPlanBase {
 // The launch configurations of (G warps per POI, gpb groups per block): each staging mode the
 // request allows that fits, kept when it makes more groups resident than the fuller modes before
 // it (a leaner mode that fits no more groups only re-reads what the fuller one stages).
-template <int OPT, int DEG, typename T, int G, int WIDE>
-void batch_kernel_setup(BatchPlan<T>& b, tdic_ctx* ctx, int gpb, int requested) {
+template <int OPT, int DEG, typename T, int G, int WIDE, int VAR>
+void batch_kernel_setup(BatchPlan<T, VAR>& b, tdic_ctx* ctx, int gpb, int requested) {
     const size_t prefix = cta_prefix_bytes(b.sh.ntab);
     const size_t ctl = round128(gpb * sizeof(DfSlot<typename MixedOf<T>::type>)) + 128;
     const int threads = 32 * G * gpb + 32;
     static_assert(G * 32 + 32 <= BatchBounds<WIDE>::threads, "a group and the resolver fit the kernel's bound");
     if (threads > BatchBounds<WIDE>::threads) return;
-    auto kern = propagate_batch_kernel<OPT, DEG, T, G, WIDE>;
+    auto kern = propagate_batch_kernel<OPT, DEG, T, G, WIDE, VAR>;
     const int stages[3] = {kStageFull, kStageLean, kStageLean | kStageNoCoefWindow};
-    const int want = requested == TDIC_STAGING_FULL ? 0 : requested == TDIC_STAGING_LEAN ? 1
+    // the masked route stages in full only
+    const int want = VAR != 0 ? 0 : requested == TDIC_STAGING_FULL ? 0 : requested == TDIC_STAGING_LEAN ? 1
                    : requested == TDIC_STAGING_LEAN_NO_WINDOW ? 2 : -1;
     int best_groups = 0;
     for (int k = 0; k < 3; ++k) {
@@ -3089,8 +3092,8 @@ void batch_kernel_setup(BatchPlan<T>& b, tdic_ctx* ctx, int gpb, int requested) 
     }
 }
 
-template <int OPT, int DEG, typename T, int G, int WIDE>
-void batch_kernel_launch(BatchPlan<T>& b, const typename BatchPlan<T>::Config& c, cudaStream_t s) {
+template <int OPT, int DEG, typename T, int G, int WIDE, int VAR>
+void batch_kernel_launch(BatchPlan<T, VAR>& b, const typename BatchPlan<T, VAR>::Config& c, cudaStream_t s) {
     cudaLaunchConfig_t lc = {};
     lc.gridDim = dim3(std::min(c.blocks, c.per_sm * std::max(1, b.sms)));
     lc.blockDim = dim3(c.threads);
@@ -3104,26 +3107,26 @@ void batch_kernel_launch(BatchPlan<T>& b, const typename BatchPlan<T>::Config& c
     Shape sh = b.sh;
     sh.stage = c.stage;
     sh.narr = c.narr;
-    TDIC_CUDA_TRY(cudaLaunchKernelEx(&lc, propagate_batch_kernel<OPT, DEG, T, G, WIDE>, b.d_jobs.template as<BatchJob<T>>(),
+    TDIC_CUDA_TRY(cudaLaunchKernelEx(&lc, propagate_batch_kernel<OPT, DEG, T, G, WIDE, VAR>, b.d_jobs.template as<BatchJob<T>>(),
                                      b.n, b.d_maps.template as<CUtensorMap>(), sh));
 }
 
-template <int OPT, int DEG, typename T>
-void batch_configs(BatchPlan<T>& b, tdic_ctx* ctx, int requested) {
+template <int OPT, int DEG, typename T, int VAR>
+void batch_configs(BatchPlan<T, VAR>& b, tdic_ctx* ctx, int requested) {
     b.configs.clear();
     // the first configuration is the untuned default: in FP32 the single-pair launch's shape
-    if constexpr (sizeof(T) == 4) batch_kernel_setup<OPT, DEG, T, 4, 1>(b, ctx, 3, requested);
-    batch_kernel_setup<OPT, DEG, T, 4, 0>(b, ctx, 2, requested);
-    batch_kernel_setup<OPT, DEG, T, 4, 0>(b, ctx, 1, requested);
-    batch_kernel_setup<OPT, DEG, T, 8, 0>(b, ctx, 1, requested);
+    if constexpr (sizeof(T) == 4) batch_kernel_setup<OPT, DEG, T, 4, 1, VAR>(b, ctx, 3, requested);
+    batch_kernel_setup<OPT, DEG, T, 4, 0, VAR>(b, ctx, 2, requested);
+    batch_kernel_setup<OPT, DEG, T, 4, 0, VAR>(b, ctx, 1, requested);
+    batch_kernel_setup<OPT, DEG, T, 8, 0, VAR>(b, ctx, 1, requested);
     TDIC_REQUIRE(!b.configs.empty(), TDIC_UNSUPPORTED, "batch: subset radius too large for shared memory");
 }
 
-template <int OPT, int DEG, typename T>
-void batch_dispatch(BatchPlan<T>& b, const typename BatchPlan<T>::Config& c, cudaStream_t s) {
-    if (c.G == 8) batch_kernel_launch<OPT, DEG, T, 8, 0>(b, c, s);
-    else if (c.wide) batch_kernel_launch<OPT, DEG, T, 4, 1>(b, c, s);
-    else batch_kernel_launch<OPT, DEG, T, 4, 0>(b, c, s);
+template <int OPT, int DEG, typename T, int VAR>
+void batch_dispatch(BatchPlan<T, VAR>& b, const typename BatchPlan<T, VAR>::Config& c, cudaStream_t s) {
+    if (c.G == 8) batch_kernel_launch<OPT, DEG, T, 8, 0, VAR>(b, c, s);
+    else if (c.wide) batch_kernel_launch<OPT, DEG, T, 4, 1, VAR>(b, c, s);
+    else batch_kernel_launch<OPT, DEG, T, 4, 0, VAR>(b, c, s);
 }
 
 template <typename T, typename F>
@@ -3139,12 +3142,12 @@ void with_opt_deg(int opt, int deg, F&& f) {
     }
 }
 
-template <typename T>
+template <typename T, int VAR>
 std::unique_ptr<BatchPlanBase> batch_plan_build(tdic_ctx* ctx, int n, tdic_pair* const* pairs, const tdic_config* cfgs,
                                                 const BatchSeed* seeds, const std::vector<std::vector<uint8_t>>& rois,
                                                 cudaStream_t s) {
     using P = typename MixedOf<T>::type;
-    auto b = std::make_unique<BatchPlan<T>>();
+    auto b = std::make_unique<BatchPlan<T, VAR>>();
     b->n = n;
     b->opt = cfgs[0].optimizer;
     b->deg = pairs[0]->degree;
@@ -3209,10 +3212,23 @@ std::unique_ptr<BatchPlanBase> batch_plan_build(tdic_ctx* ctx, int n, tdic_pair*
     // environments, capacities and tensor maps
     Shape sh{b->d_tab.template as<short2>(), static_cast<int>(tab.size()), 0, 0, 0, 0, 0, static_cast<int>(total)};
     std::vector<Env<T>> envs(n);
+    if constexpr (VAR != 0) b->d_roi_px.resize(n);
     for (int j = 0; j < n; ++j) {
         const int k = static_cast<int>(std::lower_bound(radii.begin(), radii.end(), cfgs[j].subset_radius) - radii.begin());
+        const uint8_t* roi_px = nullptr;
+        if constexpr (VAR != 0) {
+            // masked subsets: the pixel ROI on the device (every pixel valid when none is given)
+            const size_t np = static_cast<size_t>(pairs[j]->w) * pairs[j]->h;
+            b->d_roi_px[j] = Buffer(&ctx->pool, np);
+            if (!rois[j].empty())
+                TDIC_CUDA_TRY(cudaMemcpyAsync(b->d_roi_px[j].ptr, rois[j].data(), np, cudaMemcpyHostToDevice, s));
+            else
+                TDIC_CUDA_TRY(cudaMemsetAsync(b->d_roi_px[j].ptr, 1, np, s));
+            roi_px = b->d_roi_px[j].template as<uint8_t>();
+        }
         envs[j] = make_env<T>(ctx, pairs[j], cfgs[j], cfgs[j].subset_radius, cfgs[j].max_iterations,
-                              cfgs[j].convergence_threshold, b->d_tab.template as<short2>() + tab_off[k], tab_n[k]);
+                              cfgs[j].convergence_threshold, b->d_tab.template as<short2>() + tab_off[k], tab_n[k],
+                              roi_px);
         sh.nmax = std::max(sh.nmax, envs[j].n);
         sh.rbx = std::max(sh.rbx, envs[j].rbx); sh.rby = std::max(sh.rby, envs[j].rby);
         sh.cbx = std::max(sh.cbx, envs[j].cbx); sh.cby = std::max(sh.cby, envs[j].cby);
@@ -3277,7 +3293,7 @@ std::unique_ptr<BatchPlanBase> batch_plan_build(tdic_ctx* ctx, int n, tdic_pair*
     TDIC_CUDA_TRY(cudaMemcpyAsync(b->d_maps.ptr, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice, s));
     TDIC_CUDA_TRY(cudaStreamSynchronize(s));  // host staging vectors go out of scope
     with_opt_deg<T>(b->opt, b->deg, [&](auto O, auto D) {
-        batch_configs<decltype(O)::value, decltype(D)::value, T>(*b, ctx, cfgs[0].staging);
+        batch_configs<decltype(O)::value, decltype(D)::value, T, VAR>(*b, ctx, cfgs[0].staging);
     });
     b->num_sms = ctx->num_sms;
     b->sms = ctx->num_sms;
@@ -3285,8 +3301,8 @@ std::unique_ptr<BatchPlanBase> batch_plan_build(tdic_ctx* ctx, int n, tdic_pair*
 }
 
 // Everything one propagation of the batch needs, enqueued on `s` without a host wait.
-template <typename T>
-void batch_plan_launch(BatchPlan<T>& b, int config, cudaStream_t s) {
+template <typename T, int VAR>
+void batch_plan_launch(BatchPlan<T, VAR>& b, int config, cudaStream_t s) {
     const size_t total = b.total;
     TDIC_CUDA_TRY(cudaMemsetAsync(b.d_claim.ptr, 0, sizeof(int) * total, s));
     TDIC_CUDA_TRY(cudaMemsetAsync(b.d_key.ptr, 0xff, sizeof(unsigned long long) * total, s));
@@ -3303,7 +3319,7 @@ void batch_plan_launch(BatchPlan<T>& b, int config, cudaStream_t s) {
     }
     TDIC_CUDA_TRY(cudaGetLastError());
     const auto& c = b.configs[config];
-    with_opt_deg<T>(b.opt, b.deg, [&](auto O, auto D) { batch_dispatch<decltype(O)::value, decltype(D)::value, T>(b, c, s); });
+    with_opt_deg<T>(b.opt, b.deg, [&](auto O, auto D) { batch_dispatch<decltype(O)::value, decltype(D)::value, T, VAR>(b, c, s); });
 }
 
 template <int OPT, typename T, int VAR = 0>

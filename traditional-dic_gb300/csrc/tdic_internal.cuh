@@ -279,17 +279,25 @@ struct BatchPlanBase {
     virtual void grid(int job, int32_t* gw, int32_t* gh) const = 0;
     virtual void set_sms(int sms) = 0;
 };
-std::unique_ptr<BatchPlanBase> batch_build_f32(tdic_ctx* ctx, int n, tdic_pair* const* pairs, const tdic_config* cfgs,
-                                               const BatchSeed* seeds, const std::vector<std::vector<uint8_t>>& rois,
-                                               cudaStream_t s);
-std::unique_ptr<BatchPlanBase> batch_build_f64(tdic_ctx* ctx, int n, tdic_pair* const* pairs, const tdic_config* cfgs,
-                                               const BatchSeed* seeds, const std::vector<std::vector<uint8_t>>& rois,
-                                               cudaStream_t s);
+// plan builders of the four batch units (precision x plain / masked-subset route)
+#define TDIC_BATCH_BUILDER(name)                                                                              \
+    std::unique_ptr<BatchPlanBase> name(tdic_ctx* ctx, int n, tdic_pair* const* pairs, const tdic_config* cfgs, \
+                                        const BatchSeed* seeds, const std::vector<std::vector<uint8_t>>& rois,  \
+                                        cudaStream_t s);
+TDIC_BATCH_BUILDER(batch_build_f32)
+TDIC_BATCH_BUILDER(batch_build_f64)
+TDIC_BATCH_BUILDER(batch_build_f32_masked)
+TDIC_BATCH_BUILDER(batch_build_f64_masked)
+#undef TDIC_BATCH_BUILDER
 inline std::unique_ptr<BatchPlanBase> batch_build(tdic_ctx* ctx, int n, tdic_pair* const* pairs,
                                                   const tdic_config* cfgs, const BatchSeed* seeds,
                                                   const std::vector<std::vector<uint8_t>>& rois, cudaStream_t s) {
-    return pairs[0]->precision == TDIC_FP64 ? batch_build_f64(ctx, n, pairs, cfgs, seeds, rois, s)
-                                            : batch_build_f32(ctx, n, pairs, cfgs, seeds, rois, s);
+    const bool fp64 = pairs[0]->precision == TDIC_FP64;
+    if (cfgs[0].truncate_roi_subsets)
+        return fp64 ? batch_build_f64_masked(ctx, n, pairs, cfgs, seeds, rois, s)
+                    : batch_build_f32_masked(ctx, n, pairs, cfgs, seeds, rois, s);
+    return fp64 ? batch_build_f64(ctx, n, pairs, cfgs, seeds, rois, s)
+                : batch_build_f32(ctx, n, pairs, cfgs, seeds, rois, s);
 }
 inline int batch_config_count(BatchPlanBase* p) { return p->config_count(); }
 inline void batch_config_info(BatchPlanBase* p, int config, int* warps_per_poi, int* groups_per_block, int* staging) {
