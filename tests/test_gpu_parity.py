@@ -181,6 +181,32 @@ def test_compute_matches_oracle_pipeline(oracle, gpu_ctx, workload0):
     assert d.max() <= 10 * U_TOL
 
 
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_compute_heap_order_matches_oracle_pipeline(oracle, gpu_ctx, workload0, precision):
+    """The drop-in path in the reference's own visit order (propagation "heap": seed selection,
+    then the heap loop reproduced on the device) against the oracle's reference pipeline: the
+    same seed, the same grid, and results within FP32 rounding (FP64: to 1e-7 px, flags and
+    iteration counts identical)."""
+    import __graft_entry__ as G
+    from traditional_dic_gb300 import subset as S
+    p = workload0
+    conf = dict(G.WORKLOAD0_CONFIG, gpu={"precision": precision, "propagation": "heap"})
+    got, seed = S.compute(p.reference, p.deformed, conf, return_seed=True)
+    cfg = S.config_from_dict(G.WORKLOAD0_CONFIG)
+    want = oracle.subset_compute(p.reference, p.deformed, _heap(oracle, cfg))
+    assert seed.found and want["seed"].found
+    assert (seed.x, seed.y) == (want["seed"].x, want["seed"].y)
+    assert len(got["x"]) == len(want["x"])
+    both = got["valid"] & want["valid"]
+    d = np.hypot(got["u"][both] - want["u"][both], got["v"][both] - want["v"][both])
+    if precision == "fp64":
+        assert np.array_equal(got["valid"], want["valid"])
+        assert d.max() <= 1e-7
+        return
+    assert np.mean(got["valid"] == want["valid"]) >= FLAG_AGREE
+    assert np.mean(d <= U_TOL) >= 0.999 and np.quantile(d, 0.99) <= 1e-5
+
+
 @pytest.mark.parametrize("with_roi", [False, True])
 def test_select_seed_matches_oracle(oracle, gpu_ctx, workload0, with_roi):
     """Seed selection (sampled candidate points, k-means, integer search, subpixel refinement)
