@@ -123,13 +123,14 @@ struct HeapTable {
 
     // Bucket queue over non-negative keys (ZNSSD and SSD values): the bit pattern of a
     // non-negative double orders like the value; the span of the patterns the simulation can
-    // push (the table's keys) is cut into 2^20 buckets of equal width, a bucket holds its points
-    // in a list and a three-level bitmap finds the lowest non-empty bucket.  A pop takes the
+    // push (the table's keys) is cut into 2^18 buckets of equal width (a 1 MB head array to reset per
+    // simulation), a bucket holds its points in a list and a three-level bitmap finds the lowest
+    // non-empty bucket.  A pop takes the
     // bucket's smallest key; two equal keys in the queue at once would leave the order to
     // std::priority_queue's tie rule, so the queue reports a tie and the caller repeats the
     // simulation with std::priority_queue itself.
     struct BucketQueue {
-        static constexpr int kBits = 20;
+        static constexpr int kBits = 18;
         std::vector<int> head, next;
         std::vector<uint64_t> key, l0, l1;
         uint64_t l2[4] = {0, 0, 0, 0};
