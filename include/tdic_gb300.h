@@ -260,11 +260,11 @@ tdic_status tdic_propagate(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cf
  * propagation has nothing to allocate on a device).  For callers that cannot allocate device
  * memory at propagation time: a real-time loop that must not stall on cudaMalloc's device
  * synchronisation, or a process whose device memory belongs to another allocator.  The same
- * kernel runs with its scratch in one static device array of about 11.8 MiB per device,
- * which caps the call at 131072 grid points and 32768 subset samples (radius <= 100);
- * larger calls fail with TDIC_INVALID_ARG.  Masked subsets (cfg->truncate_roi_subsets) are
- * not covered: TDIC_UNSUPPORTED.  out_device: device arrays of grid_w*grid_h entries (NULL
- * entries skipped); roi: host mask as for tdic_propagate.  The pair and the context are made
+ * kernel runs with its scratch in one static device array of about 15.8 MiB per device,
+ * which caps the call at 131072 grid points and 32768 subset samples (radius <= 100), and a
+ * call with masked subsets (cfg->truncate_roi_subsets, solved as tdic_propagate solves them)
+ * at 2^22 image pixels; larger calls fail with TDIC_INVALID_ARG.  out_device: device arrays
+ * of grid_w*grid_h entries (NULL entries skipped); roi: host mask as for tdic_propagate.  The pair and the context are made
  * beforehand with the calls above, which do allocate.  The first call on a device looks up the
  * array's device address (set-up, once per device; under the driver's lazy module loading this
  * is also when the array's memory is committed on the device); make that first call before any
@@ -325,12 +325,16 @@ tdic_status tdic_select_seed(tdic_ctx* ctx, tdic_pair* lazy, const float* refere
                              const uint8_t* roi, const tdic_config* cfg, tdic_seed* seed,
                              void* stream);
 
-/* SubsetDIC::compute up to the propagation (subset_dic.cpp:39-64), without truncate_roi_subsets
- * (TDIC_UNSUPPORTED): creates the pair from host
+/* SubsetDIC::compute up to the propagation (subset_dic.cpp:39-64): creates the pair from host
  * images (as tdic_pair_create with the exact prefilter) and selects its seed (as
  * tdic_select_seed, on a seed spline built from the uploaded images; texture statistics on the
  * raw host images).  The caller propagates (tdic_propagate, or one job of a tdic_batch) and
- * destroys *pair_out.  seed_out->found = 0 means SubsetDIC::compute's empty result. */
+ * destroys *pair_out.  seed_out->found = 0 means SubsetDIC::compute's empty result.
+ * With cfg->truncate_roi_subsets the pair is the padded one tdic_subset_compute works on: both
+ * images mirror-padded by pad = tdic_subset_padding(cfg) on every side (float32, (width + 2 pad)
+ * x (height + 2 pad)), the seed in padded coordinates.  Propagate it with the padded ROI (0 in
+ * the padding, roi or all ones inside) and keep the grid points with 0 <= x - pad < width and
+ * 0 <= y - pad < height, shifted back by pad: tdic_subset_compute's result. */
 tdic_status tdic_subset_prepare(tdic_ctx* ctx, const void* reference, const void* deformed,
                                 int32_t width, int32_t height, tdic_dtype dtype,
                                 const uint8_t* roi, const tdic_config* cfg, void* stream,

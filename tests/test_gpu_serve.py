@@ -54,3 +54,50 @@ def test_served_results_equal_alone(gpu_ctx):
             assert np.array_equal(got[key], want[key], equal_nan=True), (k, key)
     assert len(served[-1]["x"]) == 0
     assert all(q.latency > 0 for q in reqs)
+
+
+def test_served_masked_requests_equal_alone(gpu_ctx):
+    """Masked subsets (truncate_roi_subsets, a full Config structure) through the serving loop:
+    tdic_subset_prepare pads the pair as tdic_subset_compute does, the batch propagates it with the
+    padded ROI and the loop crops the grid back; every result equals subset.compute_config of
+    the same request alone, bit for bit, with plain requests served beside them."""
+    from traditional_dic_gb300 import serve, subset as S
+    work = []
+    for k, (shape, dtype, radius, step, (u0, v0)) in enumerate(REQUESTS[:5]):
+        p = small_speckle(shape, n=int(shape[0] * shape[1] / 45), seed=60 + k, u0=u0, v0=v0, dtype=dtype)
+        cfg = S.config_from_dict(_config(radius, step))
+        cfg.truncate_roi_subsets = 1
+        h, w = shape
+        roi = None
+        if k % 2 == 0:   # a hole right of the centre, and a corner cut off
+            roi = np.ones(shape, bool)
+            roi[h // 3: h // 3 + h // 6, w // 2 + 10: w // 2 + 10 + w // 5] = False
+            roi[: h // 6, : w // 6] = False
+        work.append((p.reference, p.deformed, cfg, roi))
+    plain = small_speckle(REQUESTS[1][0], n=1100, seed=70, dtype=np.uint16)
+    work.insert(2, (plain.reference, plain.deformed, _config(11, 5), None))   # a plain request between them
+
+    def alone(r, d, c, roi):
+        if isinstance(c, dict):
+            return S.compute(r, d, c, roi, context=gpu_ctx)
+        return S.compute_config(r, d, c, roi, context=gpu_ctx)
+
+    want = [alone(*w_) for w_ in work]
+    # the prepared pair is the padded one, its seed in padded coordinates
+    r0, d0, c0, roi0 = work[0]
+    _, seed0 = S.compute_config(r0, d0, c0, roi0, context=gpu_ctx, return_seed=True)
+    pair, seed = S.prepare(gpu_ctx, r0, d0, c0, roi=roi0)
+    pad = S.padding(c0)
+    assert pad > 0 and (pair.height, pair.width) == (r0.shape[0] + 2 * pad, r0.shape[1] + 2 * pad)
+    assert seed.found and (seed.x - pad, seed.y - pad) == (seed0.x, seed0.y)
+    pair.close()
+    with serve.Server(gpu_ctx) as srv:
+        reqs = [srv.submit(r, d, c, roi) for r, d, c, roi in work]
+        served = [q.wait(300) for q in reqs]
+        sizes = list(srv.batches)
+    assert sum(sizes) == len(work) and max(sizes) > 1
+    for k, (got, exp) in enumerate(zip(served, want)):
+        assert len(exp["x"]) > 0, k
+        assert set(got) >= set(S.RESULT_KEYS + S.EXTRA_KEYS), k
+        for key in S.RESULT_KEYS + S.EXTRA_KEYS:
+            assert np.array_equal(got[key], exp[key], equal_nan=True), (k, key)

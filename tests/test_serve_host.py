@@ -130,3 +130,62 @@ def test_loop_fails_every_pending_request_on_a_device_error(pkg):
     assert srv._held == 0
     with pytest.raises(RuntimeError, match="closed"):
         srv.submit(img, img)
+
+
+def test_submit_takes_a_config_structure_by_copy(pkg):
+    from traditional_dic_gb300 import _lib as L
+    srv = _bare_server()
+    img = np.zeros((32, 32), np.float32)
+    cfg = L.default_config()
+    cfg.truncate_roi_subsets = 1
+    req = srv.submit(img, img, config=cfg)
+    cfg.subset_radius = 3                                   # the caller's later change stays theirs
+    assert isinstance(req.config, L.Config) and req.config.truncate_roi_subsets == 1
+    assert req.config.subset_radius == L.default_config().subset_radius
+
+
+def test_masked_footprint_counts_the_padded_pair(pkg):
+    from traditional_dic_gb300 import serve, subset as S
+    cfg = S.config_from_dict({"reliability_propagation": {"spacing": 4}})
+    plain = serve._footprint(100, 80, cfg)
+    cfg.truncate_roi_subsets = 1
+    pad = S.padding(cfg)
+    assert pad > 0
+    assert serve._footprint(100, 80, cfg) == serve._footprint(100 + 2 * pad, 80 + 2 * pad, S.config_from_dict(
+        {"reliability_propagation": {"spacing": 4}})) > plain
+
+
+@pytest.mark.parametrize("shape,radius,spacing", [((100, 80), 15, 4), ((64, 97), 7, 2), ((33, 50), 21, 9)])
+def test_padded_roi_and_crop_give_the_truncated_grid(pkg, oracle, shape, radius, spacing):
+    """The serving loop's masked collection: the padded pair's grid (gx * step, gy * step over the
+    padded image) cropped to the image and shifted back is the truncated grid of
+    SubsetDIC::compute (the oracle's dimensions, row-major, x = gx * step - pad)."""
+    from traditional_dic_gb300 import _lib as L, subset as S
+    h, w = shape
+    cfg = L.default_config()
+    cfg.subset_radius, cfg.propagation_spacing, cfg.truncate_roi_subsets = radius, spacing, 1
+    pad = S.padding(cfg)
+    assert pad == oracle.subset_padding(cfg)
+    roi = np.zeros(shape, bool)
+    roi[5:, 3:] = True
+    proi = S.padded_roi(roi, w, h, pad)
+    assert proi.shape == (h + 2 * pad, w + 2 * pad) and proi.sum() == roi.sum()
+    assert np.array_equal(proi[pad:pad + h, pad:pad + w], roi)
+    assert S.padded_roi(None, w, h, pad).sum() == w * h
+    step = spacing + 1
+    pgw, pgh = L.grid_dims(w + 2 * pad, h + 2 * pad, spacing)
+    gy, gx = np.divmod(np.arange(pgw * pgh), pgw)
+    padded = {"x": (gx * step).astype(np.float64), "y": (gy * step).astype(np.float64),
+              "u": np.arange(pgw * pgh, dtype=np.float64), "valid": (gx % 2).astype(bool)}
+    got = S.crop_padded(padded, w, h, pad)
+    gw, gh = oracle.truncated_grid_dims(w, h, cfg)
+    assert (gw, gh) == L.subset_grid_dims(w, h, cfg)
+    assert len(got["x"]) == gw * gh
+    xs = np.unique(got["x"])
+    ys = np.unique(got["y"])
+    assert len(xs) == gw and len(ys) == gh
+    assert xs[0] == (-pad) % step and ys[0] == (-pad) % step and xs[-1] < w and ys[-1] < h
+    assert np.array_equal(got["x"], np.tile(xs, gh)) and np.array_equal(got["y"], np.repeat(ys, gw))
+    keep = got["u"].astype(int)                             # the rows kept, in grid order
+    assert np.all(np.diff(keep) > 0)
+    assert np.array_equal(got["valid"], padded["valid"][keep])

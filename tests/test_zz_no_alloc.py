@@ -2,7 +2,8 @@
 context's pool, for callers that cannot allocate device memory while they propagate.  Called
 through the C ABI; its grid must equal tdic_propagate's bit for bit (the same kernel in the same
 deterministic visit order) on two calls in a row (the second call finds the first call's scratch
-contents), and neither the context's pool nor the device's free memory may change while it runs."""
+contents), and neither the context's pool nor the device's free memory may change while it runs;
+with masked subsets too (the pixel ROI in its own region of the array)."""
 import ctypes as C
 
 import numpy as np
@@ -36,8 +37,8 @@ def _roi(shape, sx, sy):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("mode", [2, 0])
-def test_noalloc_matches_propagate_on_two_calls(oracle, workload0, mode):
+@pytest.mark.parametrize("mode,masked", [(2, 0), (0, 0), (2, 1)])
+def test_noalloc_matches_propagate_on_two_calls(oracle, workload0, mode, masked):
     import torch
     import __graft_entry__ as G
     from traditional_dic_gb300 import subset as S, _lib as L
@@ -45,6 +46,7 @@ def test_noalloc_matches_propagate_on_two_calls(oracle, workload0, mode):
     cfg = S.config_from_dict(G.WORKLOAD0_CONFIG)
     cfg.propagation_spacing = 2                        # 86 x 86 grid points: two 4 KiB upload chunks
     cfg.propagation_mode = mode
+    cfg.truncate_roi_subsets = masked                 # masked subsets read the pixel ROI
     seed_o, _ = oracle.select_seed(p.reference, p.deformed, oracle.as_config(cfg))
     assert seed_o.found
     seed = S.make_seed(seed_o.x, seed_o.y, list(seed_o.p), seed_o.correlation)
@@ -67,7 +69,7 @@ def test_noalloc_matches_propagate_on_two_calls(oracle, workload0, mode):
         return pc.value
 
     # the first call on the device is the set-up: looking up the static array makes the driver
-    # load it (its ~12 MiB appear in the device's used memory then, once)
+    # load it (its ~16 MiB appear in the device's used memory then, once)
     got = [call(grids[0])]
     free_before = torch.cuda.mem_get_info()[0]
     got += [call(t) for t in grids[1:]]                 # two calls in a row

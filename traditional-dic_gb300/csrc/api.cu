@@ -1039,38 +1039,57 @@ static void prepare_impl(tdic_ctx* ctx, const void* reference, const void* defor
     *pair_out = pair;
 }
 
-// SubsetDIC::compute with truncate_roi_subsets (subset_dic.cpp:53-104): the images mirror-padded
-// and the ROI zero-padded by recommended_subset_padding (padding.cpp:11-24, 28-36, 55-85), seed
-// and propagation over the padded pair, then the grid points inside the original image, shifted
-// back (a padded grid point gx * step is the image point gx * step - pad).
-static void truncated_compute(tdic_ctx* ctx, const void* reference, const void* deformed, int w, int h,
-                              tdic_dtype dtype, const uint8_t* roi, const tdic_config& cfg, tdic_grid_out* out,
-                              int32_t* n_points, tdic_seed* seed_out, cudaStream_t s) {
-    const int pad = tdic_subset_padding(&cfg);
-    const int pw = w + 2 * pad, ph = h + 2 * pad;
+// The inputs of SubsetDIC::compute with truncate_roi_subsets (subset_dic.cpp:53-65): both
+// images mirror-padded and the ROI zero-padded by recommended_subset_padding (padding.cpp:11-24,
+// 28-36, 55-85) on every side, the images as float32.
+struct PaddedInputs {
+    int pad = 0, pw = 0, ph = 0;
+    std::vector<float> reference, deformed;
+    std::vector<uint8_t> roi;  // ph x pw: 0 in the padding, the caller's ROI (or 1) inside
+};
+
+static PaddedInputs pad_inputs(const void* reference, const void* deformed, int w, int h, tdic_dtype dtype,
+                               const uint8_t* roi, const tdic_config& cfg) {
+    PaddedInputs P;
+    P.pad = tdic_subset_padding(&cfg);
+    P.pw = w + 2 * P.pad;
+    P.ph = h + 2 * P.pad;
+    const int pad = P.pad, pw = P.pw, ph = P.ph;
     const HostImage ri{reference, dtype}, di{deformed, dtype};
     auto mirror = [](int i, int n) {
         if (n <= 1) return 0;
         while (i < 0 || i >= n) i = i < 0 ? -i - 1 : 2 * n - i - 1;
         return i;
     };
-    std::vector<float> pr(static_cast<size_t>(pw) * ph), pd(pr.size());
-    std::vector<uint8_t> pm(pr.size(), 0);
+    P.reference.resize(static_cast<size_t>(pw) * ph);
+    P.deformed.resize(P.reference.size());
+    P.roi.assign(P.reference.size(), 0);
     std::vector<int> mx(pw);
     for (int x = 0; x < pw; ++x) mx[x] = mirror(x - pad, w);
     for (int y = 0; y < ph; ++y) {
         const size_t row = static_cast<size_t>(mirror(y - pad, h)) * w;
         for (int x = 0; x < pw; ++x) {
-            pr[static_cast<size_t>(y) * pw + x] = ri(row + mx[x]);
-            pd[static_cast<size_t>(y) * pw + x] = di(row + mx[x]);
+            P.reference[static_cast<size_t>(y) * pw + x] = ri(row + mx[x]);
+            P.deformed[static_cast<size_t>(y) * pw + x] = di(row + mx[x]);
         }
     }
     for (int y = 0; y < h; ++y)
         for (int x = 0; x < w; ++x)
-            pm[static_cast<size_t>(y + pad) * pw + x + pad] = roi ? (roi[static_cast<size_t>(y) * w + x] != 0) : 1;
+            P.roi[static_cast<size_t>(y + pad) * pw + x + pad] = roi ? (roi[static_cast<size_t>(y) * w + x] != 0) : 1;
+    return P;
+}
+
+// SubsetDIC::compute with truncate_roi_subsets (subset_dic.cpp:53-104): seed and propagation
+// over the padded pair, then the grid points inside the original image, shifted back (a padded
+// grid point gx * step is the image point gx * step - pad).
+static void truncated_compute(tdic_ctx* ctx, const void* reference, const void* deformed, int w, int h,
+                              tdic_dtype dtype, const uint8_t* roi, const tdic_config& cfg, tdic_grid_out* out,
+                              int32_t* n_points, tdic_seed* seed_out, cudaStream_t s) {
+    const PaddedInputs P = pad_inputs(reference, deformed, w, h, dtype, roi, cfg);
+    const int pad = P.pad, pw = P.pw, ph = P.ph;
     tdic_pair* pair = nullptr;
     tdic_seed seed{};
-    prepare_impl(ctx, pr.data(), pd.data(), pw, ph, TDIC_F32, pm.data(), cfg, s, &pair, &seed);
+    prepare_impl(ctx, P.reference.data(), P.deformed.data(), pw, ph, TDIC_F32, P.roi.data(), cfg, s, &pair, &seed);
     int32_t gw, gh;
     tdic_grid_dims(pw, ph, cfg.propagation_spacing, &gw, &gh);
     const size_t n = static_cast<size_t>(gw) * gh;
@@ -1094,7 +1113,7 @@ static void truncated_compute(tdic_ctx* ctx, const void* reference, const void* 
     int32_t computed = 0;
     try {
         if (seed.found) {
-            propagate_impl(ctx, pair, cfg, seed, pm.data(), &t, TDIC_HOST, &computed, s);
+            propagate_impl(ctx, pair, cfg, seed, P.roi.data(), &t, TDIC_HOST, &computed, s);
             mark_use(pair, s);
         }
     } catch (...) {
@@ -1173,9 +1192,15 @@ tdic_status tdic_subset_prepare(tdic_ctx* ctx, const void* reference, const void
         *pair_out = nullptr;
         std::memset(seed_out, 0, sizeof(*seed_out));
         check_config(*cfg);
-        TDIC_REQUIRE(!cfg->truncate_roi_subsets, TDIC_UNSUPPORTED,
-                     "prepare: masked subsets pad the images; use tdic_subset_compute");
         TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
+        if (cfg->truncate_roi_subsets) {
+            // the padded pair and its seed (padded coordinates), as tdic_subset_compute makes them;
+            // the host copies of the padded images are staged before their copies return
+            const PaddedInputs P = pad_inputs(reference, deformed, width, height, dtype, roi, *cfg);
+            prepare_impl(ctx, P.reference.data(), P.deformed.data(), P.pw, P.ph, TDIC_F32, P.roi.data(), *cfg,
+                         pick(ctx, stream), pair_out, seed_out);
+            return;
+        }
         prepare_impl(ctx, reference, deformed, width, height, dtype, roi, *cfg, pick(ctx, stream), pair_out, seed_out);
     });
 }
@@ -1231,14 +1256,15 @@ namespace {
 
 constexpr int kNoAllocMaxPoints = 131072;   // grid points per call (e.g. a 362 x 362 grid)
 constexpr int kNoAllocMaxOffsets = 32768;   // subset samples (a circle of radius 100 has 31417)
+constexpr int kNoAllocMaxPixels = 1 << 22;  // image pixels of a masked call (e.g. 2048 x 2048)
 
 struct NoAllocLayout {
-    size_t roi, claim, key, order, fetch, misc, dstate, dcnt, dq, kcorr, offsets, total;
+    size_t roi, claim, key, order, fetch, misc, dstate, dcnt, dq, kcorr, offsets, roi_px, total;
 };
 
 constexpr size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 
-constexpr NoAllocLayout noalloc_layout(size_t n, size_t n_off) {
+constexpr NoAllocLayout noalloc_layout(size_t n, size_t n_off, size_t px) {
     NoAllocLayout l{};
     size_t o = 0;
     l.roi = o;     o = align256(o + n);
@@ -1252,11 +1278,13 @@ constexpr NoAllocLayout noalloc_layout(size_t n, size_t n_off) {
     l.dq = o;      o = align256(o + 8 * n);
     l.kcorr = o;   o = align256(o + 4 * n);
     l.offsets = o; o = align256(o + 4 * n_off);
+    l.roi_px = o;  o = align256(o + px);                 // masked subsets: the pixel ROI
     l.total = o;
     return l;
 }
 
-constexpr size_t kNoAllocBytes = noalloc_layout(kNoAllocMaxPoints, kNoAllocMaxOffsets).total;  // about 11.8 MiB
+constexpr size_t kNoAllocBytes =
+    noalloc_layout(kNoAllocMaxPoints, kNoAllocMaxOffsets, kNoAllocMaxPixels).total;  // about 15.8 MiB
 
 // One instance per device, created when the module is loaded on that device.
 static __device__ __align__(256) unsigned char noalloc_scratch[kNoAllocBytes];
@@ -1287,7 +1315,6 @@ short2 noalloc_host_offsets[kNoAllocMaxOffsets];
 void propagate_noalloc_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& cfg, const tdic_seed& seed,
                             const uint8_t* roi, const tdic_grid_out* out, int32_t* points_computed, cudaStream_t s) {
     check_config(cfg);
-    TDIC_REQUIRE(!cfg.truncate_roi_subsets, TDIC_UNSUPPORTED, "no-allocation propagation: masked subsets not covered");
     TDIC_REQUIRE(pair->exact == 1, TDIC_INVALID_ARG, "propagation needs a pair with the exact prefilter");
     TDIC_REQUIRE(cfg.propagation_mode == 0 || cfg.propagation_mode == 2, TDIC_UNSUPPORTED,
                  "no-allocation propagation: propagation_mode 0 (frontier waves) or 2 (dataflow) only (the heap order's "
@@ -1306,6 +1333,10 @@ void propagate_noalloc_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& c
                      std::to_string(kNoAllocMaxPoints) + " (use tdic_propagate)");
     TDIC_REQUIRE(n_off <= kNoAllocMaxOffsets, TDIC_INVALID_ARG,
                  "tdic_propagate_noalloc: the subset has more samples than its static scratch holds");
+    const bool masked = cfg.truncate_roi_subsets != 0;
+    TDIC_REQUIRE(!masked || static_cast<size_t>(w) * h <= static_cast<size_t>(kNoAllocMaxPixels), TDIC_INVALID_ARG,
+                 "tdic_propagate_noalloc: masked subsets need the image's pixel ROI; its static scratch holds at most " +
+                     std::to_string(kNoAllocMaxPixels) + " pixels (use tdic_propagate)");
     *points_computed = 0;
     const int sxr = static_cast<int>(std::round(seed.x)), syr = static_cast<int>(std::round(seed.y));
     bool seed_ok = seed.found != 0 && roi_ok(roi, w, h, sxr, syr);
@@ -1316,7 +1347,7 @@ void propagate_noalloc_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& c
         seed_ok = roi_ok(roi, w, h, gxs * step, gys * step);
     }
     unsigned char* base = noalloc_scratch_ptr(ctx->device);
-    constexpr NoAllocLayout lay = noalloc_layout(kNoAllocMaxPoints, kNoAllocMaxOffsets);
+    constexpr NoAllocLayout lay = noalloc_layout(kNoAllocMaxPoints, kNoAllocMaxOffsets, kNoAllocMaxPixels);
     // The array keeps the previous call's contents: everything the kernel reads before it
     // writes is set here.
     for (int i = 0; i < n; ++i)
@@ -1338,9 +1369,17 @@ void propagate_noalloc_impl(tdic_ctx* ctx, tdic_pair* pair, const tdic_config& c
     TDIC_CUDA_TRY(cudaMemsetAsync(base + lay.dstate, 0, sizeof(int) * n, s));
     TDIC_CUDA_TRY(cudaMemsetAsync(base + lay.dcnt, 0, sizeof(int) * n, s));
     TDIC_CUDA_TRY(cudaMemsetAsync(base + lay.dq, 0xff, sizeof(unsigned long long) * n, s));
+    // truncate_roi_subsets: the masked routes read the pixel ROI, as tdic_propagate's (a pageable
+    // source is staged before the copy returns; the call waits for its stream in any case)
+    const size_t px = static_cast<size_t>(w) * h;
+    if (masked) {
+        if (roi) TDIC_CUDA_TRY(cudaMemcpyAsync(base + lay.roi_px, roi, px, cudaMemcpyHostToDevice, s));
+        else TDIC_CUDA_TRY(cudaMemsetAsync(base + lay.roi_px, 1, px, s));
+    }
     PropagateLaunch L{};
     L.gw = gw; L.gh = gh; L.step = step;
     L.roi_grid = base + lay.roi;
+    L.roi_px = masked ? base + lay.roi_px : nullptr;
     L.seed_idx = seed_ok ? gys * gw + gxs : 0;
     L.seed_solve = seed_ok && (gxs * step != sxr || gys * step != syr) ? 1 : 0;
     for (int k = 0; k < 6; ++k) L.seed_p[k] = seed.p[k];

@@ -7,7 +7,9 @@ propagates all prepared requests in one batched persistent launch (``subset.Batc
 propagation stream.  Requests that arrive while a batch is on the GPU are prepared meanwhile
 and go into the next batch, so preparation kernels overlap the running propagation.  Each
 request's result equals ``subset.compute`` of the same pair and configuration alone (the batch
-gives every job the single-pair result).
+gives every job the single-pair result).  A request with a full ``Config`` structure and masked
+subsets (``truncate_roi_subsets``) is prepared as the padded pair, propagated with the padded ROI
+in a batch of masked requests, and its grid cropped back: ``subset.compute_config``'s result.
 
 Device memory comes from the context's caching pool, so the loop allocates none once warm.
 """
@@ -60,11 +62,25 @@ class _Prepared:
     cfg: L.Config
     seed: L.Seed
     bytes: int
+    roi: np.ndarray | None = None   # the ROI of the propagation (the padded pair's, masked subsets)
+    pad: int = 0                    # masked subsets: the padding of the pair's images
+
+
+def _config(config) -> L.Config:
+    """The request's configuration: a config dict (``subset.compute``) or a full ``Config``
+    structure (``subset.compute_config``, e.g. masked subsets); a copy either way."""
+    if isinstance(config, L.Config):
+        return L.Config.from_buffer_copy(config)
+    return S.config_from_dict(config)
 
 
 def _footprint(w: int, h: int, cfg: L.Config) -> int:
     """Device bytes of one request: its pair (float32 images, coefficients, upload staging) and
-    the propagation scratch and outputs of its grid points."""
+    the propagation scratch and outputs of its grid points (masked subsets: of the padded pair,
+    with its pixel ROI)."""
+    if cfg.truncate_roi_subsets:
+        pad = S.padding(cfg)
+        w, h = w + 2 * pad, h + 2 * pad
     gw, gh = L.grid_dims(w, h, cfg.propagation_spacing)
     coef = 8 if cfg.precision == L.FP64 else 4
     return 2 * 4 * w * h + coef * (w + 8) * (h + 8) + 8 * w * h + 260 * gw * gh
@@ -104,13 +120,18 @@ class Server:
         self._thread.start()
 
     # ---- client side -------------------------------------------------------------------------
-    def submit(self, reference: np.ndarray, deformed: np.ndarray, config: dict | None = None, roi=None) -> Request:
-        """Queue one pair.  Bad images or a bad config raise here, as ``subset.compute`` would."""
+    def submit(self, reference: np.ndarray, deformed: np.ndarray, config: dict | L.Config | None = None,
+               roi=None) -> Request:
+        """Queue one pair.  Bad images or a bad config raise here, as ``subset.compute`` would.
+        ``config`` is a config dict, or a full ``Config`` structure as ``subset.compute_config``
+        takes (the result is then ``compute_config``'s, e.g. with masked subsets)."""
         ref = S._check_image(reference, "reference")
         de = S._check_image(deformed, "deformed")
-        if config is not None and not isinstance(config, dict):
+        if config is not None and not isinstance(config, (dict, L.Config)):
             raise RuntimeError("config must be a dict (from YAML) or None.")
-        S.config_from_dict(config)
+        if isinstance(config, L.Config):
+            config = L.Config.from_buffer_copy(config)   # the caller may change theirs meanwhile
+        _config(config)
         with self._cv:
             if self._stop:
                 raise RuntimeError("the server is closed")
@@ -137,7 +158,7 @@ class Server:
         """Upload, prefilter and seed selection on the preparation stream.  None when the
         request finished here (no seed: the reference's empty result)."""
         req.started = time.perf_counter()
-        cfg = S.config_from_dict(req.config)
+        cfg = _config(req.config)
         cfg.propagation_mode = S.PROPAGATION_MODES["dataflow"]
         h, w = req.reference.shape
         if req.roi is not None and np.asarray(req.roi).shape != (h, w):
@@ -149,7 +170,10 @@ class Server:
             pair.close()
             self._complete(req, S._empty_result())
             return None
-        return _Prepared(req, pair, cfg, seed, _footprint(w, h, cfg))
+        if cfg.truncate_roi_subsets:   # the padded pair: its ROI, and the crop at collection
+            pad = S.padding(cfg)
+            return _Prepared(req, pair, cfg, seed, _footprint(w, h, cfg), S.padded_roi(req.roi, w, h, pad), pad)
+        return _Prepared(req, pair, cfg, seed, _footprint(w, h, cfg), req.roi)
 
     def _complete(self, req: Request, result=None, error=None) -> None:
         req.result, req.error = result, error
@@ -158,12 +182,14 @@ class Server:
 
     def _launch(self, ready: list[_Prepared]):
         first = ready[0]
-        sig = (first.pair.degree, first.pair.precision, first.cfg.optimizer)
-        group = [p for p in ready if (p.pair.degree, p.pair.precision, p.cfg.optimizer) == sig][:self.max_batch]
+        def sig(p):   # what every job of one batched launch shares
+            return p.pair.degree, p.pair.precision, p.cfg.optimizer, p.cfg.truncate_roi_subsets != 0
+
+        group = [p for p in ready if sig(p) == sig(first)][:self.max_batch]
         rest = [p for p in ready if p not in group]
         self._prep.synchronize()  # the group's pairs and seeds are ready
         batch = S.Batch(self.ctx, [p.pair for p in group], [p.cfg for p in group], [p.seed for p in group],
-                        [p.req.roi for p in group], stream=self._main)
+                        [p.roi for p in group], stream=self._main)
         batch.set_sms(self._sms)
         start = self._torch.cuda.Event(enable_timing=True)
         done = self._torch.cuda.Event(enable_timing=True)
@@ -185,7 +211,11 @@ class Server:
                     self._complete(p.req, S._empty_result())
                 else:
                     out = batch.outputs(j, stream=self._copy)
-                    self._complete(p.req, {k: out[k] for k in S.RESULT_KEYS + S.EXTRA_KEYS})
+                    res = {k: out[k] for k in S.RESULT_KEYS + S.EXTRA_KEYS}
+                    if p.cfg.truncate_roi_subsets:
+                        h, w = p.req.reference.shape
+                        res = S.crop_padded(res, w, h, p.pad)
+                    self._complete(p.req, res)
         except BaseException as exc:  # every request of the batch learns of the failure
             for p in group:
                 if not p.req._done.is_set():
@@ -235,7 +265,7 @@ class Server:
                         req = self._queue[0]
                         h, w = req.reference.shape
                         try:
-                            est = _footprint(w, h, S.config_from_dict(req.config))
+                            est = _footprint(w, h, _config(req.config))
                         except Exception:
                             est = 0  # _prepare raises the same error and fails this request alone
                         if self._held + est > self.memory_budget and (ready or inflight is not None):

@@ -626,7 +626,10 @@ class Batch:
 
 def prepare(ctx: Context, reference: np.ndarray, deformed: np.ndarray, config: L.Config, roi=None, stream=None):
     """SubsetDIC::compute up to the propagation (tdic_subset_prepare): the pair on the device and
-    its seed.  Returns (Pair, Seed); seed.found == 0 is the reference's empty result."""
+    its seed.  Returns (Pair, Seed); seed.found == 0 is the reference's empty result.  With
+    ``truncate_roi_subsets`` the pair holds the images padded by ``padding(config)`` on every side
+    and the seed is in padded coordinates: propagate it with ``padded_roi`` and keep the grid
+    points inside the image with ``crop_padded`` (what ``compute_config`` returns)."""
     ref = _check_image(reference, "reference")
     de = _check_image(deformed, "deformed")
     if ref.shape != de.shape or ref.dtype != de.dtype:
@@ -639,7 +642,34 @@ def prepare(ctx: Context, reference: np.ndarray, deformed: np.ndarray, config: L
     ctx.check(ctx.lib.tdic_subset_prepare(ctx.handle, ref.ctypes.data, de.ctypes.data, w, h, L.DTYPES[ref.dtype.name],
                                           rptr, C.byref(config), _stream_ptr(stream), C.byref(hnd), C.byref(seed)))
     degree = config.degree if config.degree in (1, 3) else 5
-    return Pair._adopt(ctx, hnd, w, h, degree, config.precision, config.border), seed
+    pad = padding(config) if config.truncate_roi_subsets else 0
+    return Pair._adopt(ctx, hnd, w + 2 * pad, h + 2 * pad, degree, config.precision, config.border), seed
+
+
+def padding(config: L.Config) -> int:
+    """Pixels added on every side of the images for masked subsets (recommended_subset_padding,
+    padding.cpp:11-24; tdic_subset_padding)."""
+    return int(L.load().tdic_subset_padding(C.byref(config)))
+
+
+def padded_roi(roi, w: int, h: int, pad: int) -> np.ndarray:
+    """The ROI of the padded pair: 0 in the padding, the caller's mask (all ones if None) inside
+    (subset_dic.cpp:58-65)."""
+    out = np.zeros((h + 2 * pad, w + 2 * pad), np.uint8)
+    out[pad: pad + h, pad: pad + w] = 1 if roi is None else (np.asarray(roi) != 0)
+    return out
+
+
+def crop_padded(result: dict, w: int, h: int, pad: int) -> dict:
+    """The grid points of a padded pair's result that lie inside the w x h image, shifted back by
+    the padding, in grid order (subset_dic.cpp:84-104), as ``compute_config`` returns them."""
+    x = result["x"] - pad
+    y = result["y"] - pad
+    keep = (x >= 0.0) & (y >= 0.0) & (x < w) & (y < h)
+    out = {k: v[keep] for k, v in result.items()}
+    out["x"] = x[keep]
+    out["y"] = y[keep]
+    return out
 
 
 def select_seed(ctx: Context, lazy_pair: Pair, reference: np.ndarray, config: L.Config, roi=None,
