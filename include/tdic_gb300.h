@@ -325,6 +325,17 @@ tdic_status tdic_select_seed(tdic_ctx* ctx, tdic_pair* lazy, const float* refere
                              const uint8_t* roi, const tdic_config* cfg, tdic_seed* seed,
                              void* stream);
 
+/* Integer search: IntegerSearchInitializer::estimate (integer_search.cpp:333-432, kernel K5) at
+ * n integer points (x[i], y[i]) of the pair's reference, searching its deformed image (the
+ * pair's float32 images; either prefilter): the pyramid (multigrid) stage, the full-sample
+ * refinement around its optimum, the local +-search window and the local-preference rule.
+ * Out, per point: the integer displacement (u, v), its ZNCC (FP64, rounded as the reference's)
+ * and ok = 0 where the reference returns no estimate.  With cfg->truncate_roi_subsets the
+ * masked search over roi (host H x W mask; every pixel when NULL), as seed selection uses it. */
+tdic_status tdic_integer_search(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cfg,
+                                const int32_t* x, const int32_t* y, int32_t n, const uint8_t* roi,
+                                double* u, double* v, double* zncc, uint8_t* ok, void* stream);
+
 /* SubsetDIC::compute up to the propagation (subset_dic.cpp:39-64): creates the pair from host
  * images (as tdic_pair_create with the exact prefilter) and selects its seed (as
  * tdic_select_seed, on a seed spline built from the uploaded images; texture statistics on the

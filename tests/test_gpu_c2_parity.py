@@ -62,3 +62,27 @@ def test_c2_propagation_matches_oracle(gpu_ctx, c2, precision):
     for k in PARAMS[2:]:
         assert np.mean(np.abs(got[k] - want[k])[both] <= 1e-5) >= 0.999, k
     assert np.mean(np.abs(got["zncc"] - want["zncc"])[both] <= 1e-5) >= 0.9999
+
+
+def test_c2_integer_search_matches_oracle(oracle, gpu_ctx):
+    """The integer search at the benchmark's size (one coarse pass over 2028 / 4 x 2028 / 4
+    positions per candidate): every one of the oracle's 64 seed candidates, displacement exactly,
+    FP64 ZNCC to 1e-12."""
+    from traditional_dic_gb300 import subset as S, synthetic
+    import bench
+    p = synthetic.workload(1)
+    ocfg = bench.oracle_config(oracle, bench.CONFIG, 2)
+    _, cand = oracle.select_seed(p.reference, p.deformed, ocfg)
+    assert len(cand) == 64
+    xs = np.array([int(round(c[0])) for c in cand], np.int32)
+    ys = np.array([int(round(c[1])) for c in cand], np.int32)
+    cfg = S.config_from_dict(bench.CONFIG)
+    pair = S.Pair(gpu_ctx, p.reference, p.deformed, degree=3, exact=False)
+    got = S.integer_search(gpu_ctx, pair, cfg, xs, ys)
+    pair.close()
+    assert got["ok"].all()
+    for i in range(len(xs)):
+        want = oracle.integer_search(p.reference, p.deformed, ocfg, xs[i], ys[i])
+        assert want is not None
+        assert (got["u"][i], got["v"][i]) == (want[0], want[1]), i
+        assert abs(got["zncc"][i] - want[2]) <= 1e-12, i

@@ -229,6 +229,49 @@ def test_select_seed_matches_oracle(oracle, gpu_ctx, workload0, with_roi):
         assert roi[int(got.y), int(got.x)]
 
 
+def _search_points(oracle, p, cfg, roi):
+    """The oracle's seed candidates plus points at and near the image border (no estimate, or a
+    search window cut by the border)."""
+    _, cand = oracle.select_seed(p.reference, p.deformed, oracle.as_config(cfg), roi=roi)
+    h, w = p.reference.shape
+    r = cfg.is_subset_radius
+    extra = [(r, r), (r - 1, 40), (w - 1 - r, h // 2), (w - r, h // 3), (w // 2, h - 1 - r), (0, 0),
+             (r + 3, h - r - 4), (w // 3, r + 1)]
+    xs = np.array([int(round(c[0])) for c in cand] + [e[0] for e in extra], np.int32)
+    ys = np.array([int(round(c[1])) for c in cand] + [e[1] for e in extra], np.int32)
+    return xs, ys, len(cand)
+
+
+@pytest.mark.parametrize("with_roi", [False, True])
+def test_integer_search_matches_oracle(oracle, gpu_ctx, workload0, with_roi):
+    """IntegerSearchInitializer::estimate point by point (tdic_integer_search): the integer
+    displacement exactly, its FP64 ZNCC to 1e-12 and the no-estimate points, at the oracle's seed
+    candidates and at the border; with a ROI, the masked search."""
+    import __graft_entry__ as G
+    from traditional_dic_gb300 import subset as S
+    p = workload0
+    roi = None
+    cfg = S.config_from_dict(G.WORKLOAD0_CONFIG)
+    if with_roi:
+        yy, xx = np.mgrid[:256, :256]
+        roi = (((xx - 150) ** 2 + (yy - 120) ** 2) < 90 ** 2) | ((xx < 60) & (yy > 100))
+        cfg.truncate_roi_subsets = 1
+    xs, ys, ncand = _search_points(oracle, p, cfg, roi)
+    assert ncand > 8
+    for exact in (False, True):   # either prefilter: the search reads the pair's float32 images
+        pair = S.Pair(gpu_ctx, p.reference, p.deformed, degree=3, exact=exact)
+        got = S.integer_search(gpu_ctx, pair, cfg, xs, ys, roi=roi)
+        pair.close()
+        for i in range(len(xs)):
+            want = oracle.integer_search(p.reference, p.deformed, oracle.as_config(cfg), xs[i], ys[i], roi=roi)
+            assert got["ok"][i] == (want is not None), (exact, i, xs[i], ys[i])
+            if want is None:
+                continue
+            assert (got["u"][i], got["v"][i]) == (want[0], want[1]), (exact, i)
+            assert abs(got["zncc"][i] - want[2]) <= 1e-12, (exact, i)
+        assert got["ok"][:ncand].all()
+
+
 def _heap(oracle, cfg):
     c = oracle.as_config(cfg)
     c.propagation_mode = 1

@@ -117,6 +117,8 @@ SIGNATURES = {
                                     C.c_void_p, C.c_void_p]),
     "tdic_select_seed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Config),
                                    C.POINTER(Seed), C.c_void_p]),
+    "tdic_integer_search": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Config), C.c_void_p, C.c_void_p, C.c_int32,
+                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "tdic_subset_compute": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int, C.c_void_p,
                                       C.POINTER(Config), C.POINTER(GridOut), C.POINTER(C.c_int32), C.POINTER(Seed),
                                       C.c_void_p]),

@@ -1005,6 +1005,34 @@ tdic_status tdic_select_seed(tdic_ctx* ctx, tdic_pair* lazy, const float* refere
     });
 }
 
+tdic_status tdic_integer_search(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cfg, const int32_t* x,
+                                const int32_t* y, int32_t n, const uint8_t* roi, double* u, double* v, double* zncc,
+                                uint8_t* ok, void* stream) {
+    return guarded(ctx, [&] {
+        TDIC_REQUIRE(pair && cfg && n >= 0, TDIC_INVALID_ARG, "null argument");
+        if (n == 0) return;
+        TDIC_REQUIRE(x && y && u && v && zncc && ok, TDIC_INVALID_ARG, "null argument");
+        check_config(*cfg);
+        TDIC_CUDA_TRY(cudaSetDevice(ctx->device));
+        // masked subsets search over the ROI (every pixel when none is given), as seed selection
+        std::vector<uint8_t> ones;
+        const uint8_t* mroi = nullptr;
+        if (cfg->truncate_roi_subsets) {
+            if (!roi) ones.assign(static_cast<size_t>(pair->w) * pair->h, 1);
+            mroi = roi ? roi : ones.data();
+        }
+        std::vector<SearchResult> sr(n);
+        integer_search_batch(ctx, pair, *cfg, x, y, n, sr.data(), pick(ctx, stream), mroi);
+        mark_use(pair, pick(ctx, stream));
+        for (int i = 0; i < n; ++i) {
+            u[i] = sr[i].u;
+            v[i] = sr[i].v;
+            zncc[i] = sr[i].zncc;
+            ok[i] = sr[i].ok ? 1 : 0;
+        }
+    });
+}
+
 // SubsetDIC::compute up to the propagation (subset_dic.cpp:39-64): the pair from the host
 // images, the seed on the clamp-padded non-deconvolved spline of the same images
 // (seed_selector.cpp:166-173; the seed pair reuses the uploaded images), host texture statistics

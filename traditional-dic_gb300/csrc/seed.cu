@@ -196,69 +196,63 @@ size_t search_smem_bytes(size_t n) {
 }
 
 // Coarse search (search_ncorr_multigrid's first stage, :208-247): grid.y = candidate, grid.x
-// tiles the positions.  Pass 1: the FP32 maximum of each tile.
-__global__ void coarse_max_kernel(const float* __restrict__ ref, const float* __restrict__ def, int pitch,
-                                  const CandGeom* __restrict__ geo, const short2* __restrict__ coff, int cn, int cstep,
-                                  float* __restrict__ tile_max, int tiles) {
+// tiles the positions, kCoarsePerThread consecutive blocks' worth per block.  One pass: every
+// thread keeps the FP32 scores of its positions in registers, the block takes their maximum
+// and rescores in FP64 the positions within kScoreMargin of it (or nearly flat), and writes the
+// tile's best (FP64 score, first in scan order).  The tile's maximum is at most the candidate's,
+// so every position near the candidate's FP32 maximum is rescored in its tile; a position
+// rescored only because its tile's maximum is lower scores, in FP64, more than kScoreMargin / 2
+// below the winner and cannot win.  The best over the tiles is the two-pass search's winner.
+constexpr int kCoarsePerThread = 16;
+constexpr int kCoarseThreads = 256;
+
+__global__ void __launch_bounds__(kCoarseThreads)
+coarse_kernel(const float* __restrict__ ref, const float* __restrict__ def, int pitch,
+              const CandGeom* __restrict__ geo, const short2* __restrict__ coff, int cn, int cstep,
+              Best* __restrict__ partial, int tiles) {
     extern __shared__ __align__(16) unsigned char smem[];
     const CandGeom g = geo[blockIdx.y];
     cn = g.c_n;
     coff += g.c_start;
     SearchSmem sm(smem, cn);
     if (!g.inside) {  // uniform per block: no reference read outside the image
-        if (threadIdx.x == 0) tile_max[blockIdx.y * tiles + blockIdx.x] = -INFINITY;
-        return;
-    }
-    for (int i = threadIdx.x; i < cn; i += blockDim.x) sm.off[i] = coff[i];
-    __syncthreads();
-    load_ref(ref, pitch, sm.off, cn, g.cx, g.cy, sm.rs);
-    const int nu = g.max_u >= g.min_u ? (g.max_u - g.min_u) / cstep + 1 : 0;
-    const int nv = g.max_v >= g.min_v ? (g.max_v - g.min_v) / cstep + 1 : 0;
-    const float rm = sm.rs.fstats[0], rn = sm.rs.fstats[1], sr = sm.rs.fstats[2];
-    float best = -INFINITY;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nu * nv; t += tiles * blockDim.x) {
-        const int vi = t / nu, ui = t - vi * nu;
-        bool flat;
-        const float z = zncc32(def, pitch, sm.off, sm.rs.r32, cn, rm, rn, sr, g.cx, g.cy, g.min_u + ui * cstep,
-                               g.min_v + vi * cstep, flat);
-        best = fmaxf(best, z);
-    }
-    best = block_max(best, sm.sf);
-    if (threadIdx.x == 0) tile_max[blockIdx.y * tiles + blockIdx.x] = best;
-}
-
-// Pass 2: rescore the positions near the candidate's FP32 maximum in FP64; the first of the
-// best in scan order per tile.
-__global__ void coarse_pick_kernel(const float* __restrict__ ref, const float* __restrict__ def, int pitch,
-                                   const CandGeom* __restrict__ geo, const short2* __restrict__ coff, int cn, int cstep,
-                                   const float* __restrict__ tile_max, Best* __restrict__ partial, int tiles) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const CandGeom g = geo[blockIdx.y];
-    cn = g.c_n;
-    coff += g.c_start;
-    SearchSmem sm(smem, cn);
-    if (!g.inside) {
         if (threadIdx.x == 0) partial[blockIdx.y * tiles + blockIdx.x] = Best{-INFINITY, 0x7fffffff};
         return;
     }
     for (int i = threadIdx.x; i < cn; i += blockDim.x) sm.off[i] = coff[i];
     __syncthreads();
     load_ref(ref, pitch, sm.off, cn, g.cx, g.cy, sm.rs);
-    float m32 = -INFINITY;
-    for (int b = 0; b < tiles; ++b) m32 = fmaxf(m32, __ldg(tile_max + blockIdx.y * tiles + b));
-    const float thr = m32 - kScoreMargin;
     const int nu = g.max_u >= g.min_u ? (g.max_u - g.min_u) / cstep + 1 : 0;
     const int nv = g.max_v >= g.min_v ? (g.max_v - g.min_v) / cstep + 1 : 0;
+    const int npos = nu * nv;
     const float rm = sm.rs.fstats[0], rn = sm.rs.fstats[1], sr = sm.rs.fstats[2];
+    const int t0 = blockIdx.x * (kCoarsePerThread * kCoarseThreads) + threadIdx.x;
+    float z32[kCoarsePerThread];
+    unsigned flat_bits = 0;
+    float best = -INFINITY;
+#pragma unroll
+    for (int k = 0; k < kCoarsePerThread; ++k) {
+        const int t = t0 + k * kCoarseThreads;
+        z32[k] = -INFINITY;
+        if (t < npos) {
+            const int vi = t / nu, ui = t - vi * nu;
+            bool flat;
+            z32[k] = zncc32(def, pitch, sm.off, sm.rs.r32, cn, rm, rn, sr, g.cx, g.cy, g.min_u + ui * cstep,
+                            g.min_v + vi * cstep, flat);
+            flat_bits |= flat ? 1u << k : 0u;
+            best = fmaxf(best, z32[k]);
+        }
+    }
+    const float thr = block_max(best, sm.sf) - kScoreMargin;
     double bz = -INFINITY;
     int bi = 0x7fffffff;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nu * nv; t += tiles * blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < kCoarsePerThread; ++k) {
+        const int t = t0 + k * kCoarseThreads;
+        if (t >= npos || !((flat_bits >> k & 1u) || z32[k] >= thr)) continue;
         const int vi = t / nu, ui = t - vi * nu;
-        const int u = g.min_u + ui * cstep, v = g.min_v + vi * cstep;
-        bool flat;
-        const float z32 = zncc32(def, pitch, sm.off, sm.rs.r32, cn, rm, rn, sr, g.cx, g.cy, u, v, flat);
-        if (!(flat || z32 >= thr)) continue;
-        const double z = zncc64(def, pitch, sm.off, sm.rs.r64, cn, sm.rs.stats[0], sm.rs.stats[1], g.cx, g.cy, u, v);
+        const double z = zncc64(def, pitch, sm.off, sm.rs.r64, cn, sm.rs.stats[0], sm.rs.stats[1], g.cx, g.cy,
+                                g.min_u + ui * cstep, g.min_v + vi * cstep);
         if (better(z, t, bz, bi)) { bz = z; bi = t; }
     }
     block_argmax(bz, bi, sm.sz, sm.si);
@@ -296,7 +290,9 @@ __device__ void window_argmax(const float* __restrict__ def, int w, int h, int p
 
 // Full-sample refinement around the coarse optimum and the local +-search window, then the
 // local-preference rule.  One block per candidate.
-__global__ void fine_kernel(const float* __restrict__ ref, const float* __restrict__ def, int w, int h, int pitch, int r,
+constexpr int kFineThreads = 1024;
+
+__global__ void __launch_bounds__(kFineThreads) fine_kernel(const float* __restrict__ ref, const float* __restrict__ def, int w, int h, int pitch, int r,
                             const CandGeom* __restrict__ geo, const short2* __restrict__ foff, int fn,
                             const Best* __restrict__ partial, int tiles, int cstep, int rr, int search, int coarse_ok_all,
                             const int* __restrict__ coarse_ok, SearchResult* __restrict__ out) {
@@ -575,27 +571,33 @@ void integer_search_batch(tdic_ctx* ctx, tdic_pair* lazy, const tdic_config& cfg
     Buffer d_geo(&ctx->pool, sizeof(CandGeom) * n), d_coff(&ctx->pool, sizeof(short2) * coff.size()),
         d_foff(&ctx->pool, sizeof(short2) * foff.size()), d_cok(&ctx->pool, sizeof(int) * n),
         d_out(&ctx->pool, sizeof(SearchResult) * n);
-    const int tiles = 64;
+    // coarse tiles: enough for the candidate with the most positions
+    long long npos_max = 1;
+    for (const CandGeom& g : geo) {
+        const long long nu = g.max_u >= g.min_u ? (g.max_u - g.min_u) / cstep + 1 : 0;
+        const long long nv = g.max_v >= g.min_v ? (g.max_v - g.min_v) / cstep + 1 : 0;
+        npos_max = std::max(npos_max, nu * nv);
+    }
+    constexpr long long kPerTile = static_cast<long long>(kCoarsePerThread) * kCoarseThreads;
+    TDIC_REQUIRE(npos_max < (1LL << 31) - kPerTile, TDIC_INVALID_ARG, "integer search: too many positions");
+    const int tiles = static_cast<int>((npos_max + kPerTile - 1) / kPerTile);
     Buffer d_part(&ctx->pool, sizeof(Best) * static_cast<size_t>(tiles) * n);
-    Buffer d_tmax(&ctx->pool, sizeof(float) * static_cast<size_t>(tiles) * n);
     TDIC_CUDA_TRY(cudaMemcpyAsync(d_geo.ptr, geo.data(), sizeof(CandGeom) * n, cudaMemcpyHostToDevice, s));
     TDIC_CUDA_TRY(cudaMemcpyAsync(d_coff.ptr, coff.data(), sizeof(short2) * coff.size(), cudaMemcpyHostToDevice, s));
     TDIC_CUDA_TRY(cudaMemcpyAsync(d_foff.ptr, foff.data(), sizeof(short2) * foff.size(), cudaMemcpyHostToDevice, s));
     TDIC_CUDA_TRY(cudaMemcpyAsync(d_cok.ptr, cok.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
     const size_t csm = search_smem_bytes(static_cast<size_t>(cmax)), fsm = search_smem_bytes(static_cast<size_t>(fmax));
-    TDIC_CUDA_TRY(cudaFuncSetAttribute(coarse_max_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(csm)));
-    TDIC_CUDA_TRY(cudaFuncSetAttribute(coarse_pick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(csm)));
+    TDIC_CUDA_TRY(cudaFuncSetAttribute(coarse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(csm)));
     TDIC_CUDA_TRY(cudaFuncSetAttribute(fine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(fsm)));
     const float* dref = lazy->ref.as<float>();
     const float* ddef = lazy->def_f.as<float>();
-    coarse_max_kernel<<<dim3(tiles, n), 256, csm, s>>>(dref, ddef, lazy->rpitch, d_geo.as<CandGeom>(), d_coff.as<short2>(),
-                                                       static_cast<int>(coff.size()), cstep, d_tmax.as<float>(), tiles);
+    coarse_kernel<<<dim3(tiles, n), kCoarseThreads, csm, s>>>(dref, ddef, lazy->rpitch, d_geo.as<CandGeom>(),
+                                                              d_coff.as<short2>(), static_cast<int>(coff.size()), cstep,
+                                                              d_part.as<Best>(), tiles);
     TDIC_CUDA_TRY(cudaGetLastError());
-    coarse_pick_kernel<<<dim3(tiles, n), 256, csm, s>>>(dref, ddef, lazy->rpitch, d_geo.as<CandGeom>(), d_coff.as<short2>(),
-                                                        static_cast<int>(coff.size()), cstep, d_tmax.as<float>(),
-                                                        d_part.as<Best>(), tiles);
-    TDIC_CUDA_TRY(cudaGetLastError());
-    fine_kernel<<<n, 256, fsm, s>>>(dref, ddef, w, h, lazy->rpitch, r, d_geo.as<CandGeom>(), d_foff.as<short2>(),
+    // one block per candidate: 1024 threads (the search windows' positions over every warp the
+    // block can hold; the argmax and its scan-order tie rule do not depend on the block size)
+    fine_kernel<<<n, kFineThreads, fsm, s>>>(dref, ddef, w, h, lazy->rpitch, r, d_geo.as<CandGeom>(), d_foff.as<short2>(),
                                     static_cast<int>(foff.size()), d_part.as<Best>(), tiles, cstep, rr, search, 1,
                                     d_cok.as<int>(), d_out.as<SearchResult>());
     TDIC_CUDA_TRY(cudaGetLastError());

@@ -672,6 +672,26 @@ def crop_padded(result: dict, w: int, h: int, pad: int) -> dict:
     return out
 
 
+def integer_search(ctx: Context, pair: Pair, config: L.Config, x, y, roi=None, stream=None) -> dict:
+    """IntegerSearchInitializer::estimate at integer points (tdic_integer_search): per point the
+    integer displacement u, v, its ZNCC and ok (False where the reference gives no estimate)."""
+    xs = np.ascontiguousarray(x, np.int32)
+    ys = np.ascontiguousarray(y, np.int32)
+    if xs.shape != ys.shape or xs.ndim != 1:
+        raise ValueError("x and y must be 1-D arrays of the same length")
+    n = len(xs)
+    rptr, rkeep = _roi_arg(roi, pair.width, pair.height)
+    if rptr == "mismatch":
+        raise ValueError("roi shape differs from the images")
+    out = {k: np.zeros(n, np.float64) for k in ("u", "v", "zncc")}
+    ok = np.zeros(n, np.uint8)
+    ctx.check(ctx.lib.tdic_integer_search(ctx.handle, pair.handle, C.byref(config), xs.ctypes.data, ys.ctypes.data,
+                                          n, rptr, out["u"].ctypes.data, out["v"].ctypes.data,
+                                          out["zncc"].ctypes.data, ok.ctypes.data, _stream_ptr(stream)))
+    out["ok"] = ok.astype(bool)
+    return out
+
+
 def select_seed(ctx: Context, lazy_pair: Pair, reference: np.ndarray, config: L.Config, roi=None,
                 stream=None) -> L.Seed:
     ref = np.ascontiguousarray(reference, np.float32)
