@@ -206,20 +206,31 @@ size_t search_smem_bytes(size_t n) {
 constexpr int kCoarsePerThread = 16;
 constexpr int kCoarseThreads = 256;
 
+//
+// Every deformed sample of the coarse stage lies on the lattice x, y = 0 mod cstep: position
+// u = r - cx + cstep * ui and offset dx = -r + cstep * a give x = cx + u + dx = cstep * (ui + a).
+// The kernel reads them from `dec` (dec[j * dpitch + i] = def[cstep * j][cstep * i]) at the
+// lattice offsets doff = ((dx + r) / cstep, (dy + r) / cstep), in the order of coff: the same
+// values in the same order, with a warp's positions on consecutive floats.
 __global__ void __launch_bounds__(kCoarseThreads)
-coarse_kernel(const float* __restrict__ ref, const float* __restrict__ def, int pitch,
-              const CandGeom* __restrict__ geo, const short2* __restrict__ coff, int cn, int cstep,
-              Best* __restrict__ partial, int tiles) {
+coarse_kernel(const float* __restrict__ ref, int pitch, const float* __restrict__ dec, int dpitch,
+              const CandGeom* __restrict__ geo, const short2* __restrict__ coff, const short2* __restrict__ doff,
+              int cn, int cstep, Best* __restrict__ partial, int tiles) {
     extern __shared__ __align__(16) unsigned char smem[];
     const CandGeom g = geo[blockIdx.y];
     cn = g.c_n;
     coff += g.c_start;
+    doff += g.c_start;
     SearchSmem sm(smem, cn);
+    short2* const soff = sm.off + cn;  // lattice offsets, after the reference offsets
     if (!g.inside) {  // uniform per block: no reference read outside the image
         if (threadIdx.x == 0) partial[blockIdx.y * tiles + blockIdx.x] = Best{-INFINITY, 0x7fffffff};
         return;
     }
-    for (int i = threadIdx.x; i < cn; i += blockDim.x) sm.off[i] = coff[i];
+    for (int i = threadIdx.x; i < cn; i += blockDim.x) {
+        sm.off[i] = coff[i];
+        soff[i] = doff[i];
+    }
     __syncthreads();
     load_ref(ref, pitch, sm.off, cn, g.cx, g.cy, sm.rs);
     const int nu = g.max_u >= g.min_u ? (g.max_u - g.min_u) / cstep + 1 : 0;
@@ -237,8 +248,7 @@ coarse_kernel(const float* __restrict__ ref, const float* __restrict__ def, int 
         if (t < npos) {
             const int vi = t / nu, ui = t - vi * nu;
             bool flat;
-            z32[k] = zncc32(def, pitch, sm.off, sm.rs.r32, cn, rm, rn, sr, g.cx, g.cy, g.min_u + ui * cstep,
-                            g.min_v + vi * cstep, flat);
+            z32[k] = zncc32(dec, dpitch, soff, sm.rs.r32, cn, rm, rn, sr, 0, 0, ui, vi, flat);
             flat_bits |= flat ? 1u << k : 0u;
             best = fmaxf(best, z32[k]);
         }
@@ -251,12 +261,22 @@ coarse_kernel(const float* __restrict__ ref, const float* __restrict__ def, int 
         const int t = t0 + k * kCoarseThreads;
         if (t >= npos || !((flat_bits >> k & 1u) || z32[k] >= thr)) continue;
         const int vi = t / nu, ui = t - vi * nu;
-        const double z = zncc64(def, pitch, sm.off, sm.rs.r64, cn, sm.rs.stats[0], sm.rs.stats[1], g.cx, g.cy,
-                                g.min_u + ui * cstep, g.min_v + vi * cstep);
+        const double z = zncc64(dec, dpitch, soff, sm.rs.r64, cn, sm.rs.stats[0], sm.rs.stats[1], 0, 0, ui, vi);
         if (better(z, t, bz, bi)) { bz = z; bi = t; }
     }
     block_argmax(bz, bi, sm.sz, sm.si);
     if (threadIdx.x == 0) partial[blockIdx.y * tiles + blockIdx.x] = Best{bz, bi};
+}
+
+// The coarse lattice of the deformed image: dec[j * dw + i] = def[cstep * j][cstep * i].
+__global__ void decimate_kernel(const float* __restrict__ def, int pitch, int cstep, float* __restrict__ dec, int dw,
+                                int dh) {
+    const long long total = static_cast<long long>(dw) * dh;
+    for (long long q = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; q < total;
+         q += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int j = static_cast<int>(q / dw), i = static_cast<int>(q - static_cast<long long>(j) * dw);
+        dec[q] = __ldg(def + static_cast<size_t>(j) * cstep * pitch + static_cast<size_t>(i) * cstep);
+    }
 }
 
 // Exact block-wide argmax of circular_subset_zncc over the positions (u0 + t % nu, v0 + t / nu)
@@ -401,7 +421,24 @@ __global__ void kmeans_assign_kernel(const int2* __restrict__ pts, int m, const 
 // combine to the first centre at the smallest distance, which is the sequential scan's choice.
 constexpr int kKmeansLanes = 8;
 
-__global__ void kmeans_step_kernel(const int2* __restrict__ pts, int m, const double2* __restrict__ ctr, int k,
+//
+// FP32 filter (filter != 0, every coordinate below cb <= 2^22, points exact in float): with the
+// centres rounded to float (|c - c32| <= u |c| <= u cb, u = 2^-24) and the distance
+// d32 = dx32^2 + dy32^2 rounded in float, |d32 - d2| <= 2u cb (|dx32| + |dy32|) + 4u d32 +
+// 4u^2 cb^2 (to first order in u), where d2 is the FP64 distance.  err32 = 1e-6 (cb (|dx32| +
+// |dy32|) + d32) + kabs, kabs = 16u^2 cb^2 + 1e-6, bounds it at least four times over.  A centre
+// can hold the FP64 minimum (or tie with it) only if d32 - err32 <= U = min over the centres of
+// (d32 + err32), so only those are scored in FP64, and the FP64 scan over them gives the full
+// scan's choice.
+__device__ __forceinline__ float kmeans_d32(float x, float y, float2 c, float cb, float kabs, float& err) {
+    const float dx = __fsub_rn(x, c.x), dy = __fsub_rn(y, c.y);
+    const float d = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+    err = 1e-6f * (cb * (fabsf(dx) + fabsf(dy)) + d) + kabs;
+    return d;
+}
+
+__global__ void kmeans_step_kernel(const int2* __restrict__ pts, int m, const double2* __restrict__ ctr,
+                                   const float2* __restrict__ ctr32, int k, float cb, float kabs, int filter,
                                    unsigned long long* __restrict__ acc) {
     extern __shared__ unsigned int s_acc[];  // 3 * k
     for (int i = threadIdx.x; i < 3 * k; i += blockDim.x) s_acc[i] = 0u;
@@ -411,10 +448,25 @@ __global__ void kmeans_step_kernel(const int2* __restrict__ pts, int m, const do
     int best = -1;
     double bd = INFINITY;
     int2 pt = make_int2(0, 0);
+    if (j < m) pt = pts[j];
+    const float xf = static_cast<float>(pt.x), yf = static_cast<float>(pt.y);
+    float ub = INFINITY;  // upper bound of the FP64 minimum
+    if (filter && j < m)
+        for (int i = sub; i < k; i += kKmeansLanes) {
+            float err;
+            const float d = kmeans_d32(xf, yf, __ldg(ctr32 + i), cb, kabs, err);
+            ub = fminf(ub, d + err);
+        }
+#pragma unroll
+    for (int o = kKmeansLanes / 2; o > 0; o >>= 1) ub = fminf(ub, __shfl_xor_sync(0xffffffffu, ub, o));
     if (j < m) {
-        pt = pts[j];
         const double x = static_cast<double>(pt.x), y = static_cast<double>(pt.y);
         for (int i = sub; i < k; i += kKmeansLanes) {
+            if (filter) {
+                float err;
+                const float d = kmeans_d32(xf, yf, __ldg(ctr32 + i), cb, kabs, err);
+                if (d - err > ub) continue;
+            }
             const double2 c = __ldg(ctr + i);
             const double dx = __dsub_rn(x, c.x), dy = __dsub_rn(y, c.y);
             const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
@@ -442,13 +494,17 @@ __global__ void kmeans_step_kernel(const int2* __restrict__ pts, int m, const do
 
 // New centres (sum / count, as on the reference's host) for every centre with members; the sums
 // are cleared for the next iteration.
-__global__ void kmeans_update_kernel(double2* __restrict__ ctr, int k, unsigned long long* __restrict__ acc) {
+__global__ void kmeans_update_kernel(double2* __restrict__ ctr, float2* __restrict__ ctr32, int k,
+                                     unsigned long long* __restrict__ acc) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k) return;
     const unsigned long long n = acc[3 * i + 2];
     if (n > 0) {
         const double c = static_cast<double>(n);
-        ctr[i] = make_double2(__ddiv_rn(static_cast<double>(acc[3 * i]), c), __ddiv_rn(static_cast<double>(acc[3 * i + 1]), c));
+        const double2 v = make_double2(__ddiv_rn(static_cast<double>(acc[3 * i]), c),
+                                       __ddiv_rn(static_cast<double>(acc[3 * i + 1]), c));
+        ctr[i] = v;
+        ctr32[i] = make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
     }
     acc[3 * i] = acc[3 * i + 1] = acc[3 * i + 2] = 0ull;
 }
@@ -466,27 +522,41 @@ std::vector<short2> circle_offsets(int r, int step) {
 
 KmeansAssigner::KmeansAssigner(tdic_ctx* ctx, const int* px, const int* py, int m, int k, cudaStream_t s)
     : ctx_(ctx), s_(s), m_(m), k_(k), pts_(&ctx->pool, sizeof(int2) * std::max(m, 1)),
-      ctr_(&ctx->pool, sizeof(double2) * std::max(k, 1)), out_(&ctx->pool, sizeof(int) * std::max(m, 1)),
-      acc_(&ctx->pool, sizeof(unsigned long long) * 3 * std::max(k, 1)) {
+      ctr_(&ctx->pool, sizeof(double2) * std::max(k, 1)), ctr32_(&ctx->pool, sizeof(float2) * std::max(k, 1)),
+      out_(&ctx->pool, sizeof(int) * std::max(m, 1)), acc_(&ctx->pool, sizeof(unsigned long long) * 3 * std::max(k, 1)) {
     std::vector<int2> p(m);
-    for (int i = 0; i < m; ++i) p[i] = make_int2(px[i], py[i]);
+    long long big = 0;  // the largest |coordinate|: the centres (means of the points) lie within it
+    for (int i = 0; i < m; ++i) {
+        p[i] = make_int2(px[i], py[i]);
+        big = std::max(big, std::max(std::llabs(px[i]), std::llabs(py[i])));
+    }
+    cbound_ = static_cast<float>(big + 1);
+    const double ucb = std::ldexp(static_cast<double>(big + 1), -24);
+    kabs_ = static_cast<float>(16.0 * ucb * ucb + 1e-6);
+    filter_ = big + 1 <= (1LL << 22) ? 1 : 0;
     TDIC_CUDA_TRY(cudaMemcpyAsync(pts_.ptr, p.data(), sizeof(int2) * m, cudaMemcpyHostToDevice, s_));
     TDIC_CUDA_TRY(cudaStreamSynchronize(s_));  // p is a local
 }
 
 void KmeansAssigner::run(double* cx, double* cy, int iters) {
     std::vector<double2> c(k_);
-    for (int i = 0; i < k_; ++i) c[i] = make_double2(cx[i], cy[i]);
+    std::vector<float2> c32(k_);
+    for (int i = 0; i < k_; ++i) {
+        c[i] = make_double2(cx[i], cy[i]);
+        c32[i] = make_float2(static_cast<float>(cx[i]), static_cast<float>(cy[i]));  // round to nearest
+    }
     TDIC_CUDA_TRY(cudaMemcpyAsync(ctr_.ptr, c.data(), sizeof(double2) * k_, cudaMemcpyHostToDevice, s_));
+    TDIC_CUDA_TRY(cudaMemcpyAsync(ctr32_.ptr, c32.data(), sizeof(float2) * k_, cudaMemcpyHostToDevice, s_));
     TDIC_CUDA_TRY(cudaMemsetAsync(acc_.ptr, 0, sizeof(unsigned long long) * 3 * k_, s_));
     const size_t smem = sizeof(unsigned int) * 3 * k_;
     const long long threads = static_cast<long long>(m_) * kKmeansLanes;
     const int blocks = static_cast<int>((threads + 255) / 256);
     for (int it = 0; it < iters; ++it) {
-        kmeans_step_kernel<<<blocks, 256, smem, s_>>>(pts_.as<int2>(), m_, ctr_.as<double2>(), k_,
-                                                      acc_.as<unsigned long long>());
+        kmeans_step_kernel<<<blocks, 256, smem, s_>>>(pts_.as<int2>(), m_, ctr_.as<double2>(), ctr32_.as<float2>(),
+                                                      k_, cbound_, kabs_, filter_, acc_.as<unsigned long long>());
         TDIC_CUDA_TRY(cudaGetLastError());
-        kmeans_update_kernel<<<(k_ + 127) / 128, 128, 0, s_>>>(ctr_.as<double2>(), k_, acc_.as<unsigned long long>());
+        kmeans_update_kernel<<<(k_ + 127) / 128, 128, 0, s_>>>(ctr_.as<double2>(), ctr32_.as<float2>(), k_,
+                                                               acc_.as<unsigned long long>());
         TDIC_CUDA_TRY(cudaGetLastError());
     }
     TDIC_CUDA_TRY(cudaMemcpyAsync(c.data(), ctr_.ptr, sizeof(double2) * k_, cudaMemcpyDeviceToHost, s_));
@@ -586,13 +656,34 @@ void integer_search_batch(tdic_ctx* ctx, tdic_pair* lazy, const tdic_config& cfg
     TDIC_CUDA_TRY(cudaMemcpyAsync(d_coff.ptr, coff.data(), sizeof(short2) * coff.size(), cudaMemcpyHostToDevice, s));
     TDIC_CUDA_TRY(cudaMemcpyAsync(d_foff.ptr, foff.data(), sizeof(short2) * foff.size(), cudaMemcpyHostToDevice, s));
     TDIC_CUDA_TRY(cudaMemcpyAsync(d_cok.ptr, cok.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
-    const size_t csm = search_smem_bytes(static_cast<size_t>(cmax)), fsm = search_smem_bytes(static_cast<size_t>(fmax));
+    // lattice offsets of the coarse samples (dx = -r + cstep * a, so dx + r is a multiple of cstep)
+    std::vector<short2> doff(coff.size());
+    for (size_t i = 0; i < coff.size(); ++i)
+        doff[i] = make_short2(static_cast<short>((coff[i].x + r) / cstep), static_cast<short>((coff[i].y + r) / cstep));
+    Buffer d_doff(&ctx->pool, sizeof(short2) * doff.size());
+    TDIC_CUDA_TRY(cudaMemcpyAsync(d_doff.ptr, doff.data(), sizeof(short2) * doff.size(), cudaMemcpyHostToDevice, s));
+    const size_t csm = search_smem_bytes(static_cast<size_t>(cmax)) + sizeof(short2) * static_cast<size_t>(cmax);
+    const size_t fsm = search_smem_bytes(static_cast<size_t>(fmax));
     TDIC_CUDA_TRY(cudaFuncSetAttribute(coarse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(csm)));
     TDIC_CUDA_TRY(cudaFuncSetAttribute(fine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(fsm)));
     const float* dref = lazy->ref.as<float>();
     const float* ddef = lazy->def_f.as<float>();
-    coarse_kernel<<<dim3(tiles, n), kCoarseThreads, csm, s>>>(dref, ddef, lazy->rpitch, d_geo.as<CandGeom>(),
-                                                              d_coff.as<short2>(), static_cast<int>(coff.size()), cstep,
+    // the coarse lattice of the deformed image (the image itself when cstep is 1)
+    const int dw = (w - 1) / cstep + 1, dh = (h - 1) / cstep + 1;
+    Buffer d_dec(&ctx->pool, cstep > 1 ? sizeof(float) * static_cast<size_t>(dw) * dh : 0);
+    const float* dec = ddef;
+    int dpitch = lazy->rpitch;
+    if (cstep > 1) {
+        const long long total = static_cast<long long>(dw) * dh;
+        const int blocks = static_cast<int>(std::min<long long>((total + 255) / 256, 4096));
+        decimate_kernel<<<blocks, 256, 0, s>>>(ddef, lazy->rpitch, cstep, d_dec.as<float>(), dw, dh);
+        TDIC_CUDA_TRY(cudaGetLastError());
+        dec = d_dec.as<float>();
+        dpitch = dw;
+    }
+    coarse_kernel<<<dim3(tiles, n), kCoarseThreads, csm, s>>>(dref, lazy->rpitch, dec, dpitch, d_geo.as<CandGeom>(),
+                                                              d_coff.as<short2>(), d_doff.as<short2>(),
+                                                              static_cast<int>(coff.size()), cstep,
                                                               d_part.as<Best>(), tiles);
     TDIC_CUDA_TRY(cudaGetLastError());
     // one block per candidate: 1024 threads (the search windows' positions over every warp the

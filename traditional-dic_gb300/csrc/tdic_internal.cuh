@@ -244,7 +244,10 @@ private:
     tdic_ctx* ctx_;
     cudaStream_t s_;
     int m_, k_;
-    Buffer pts_, ctr_, out_, acc_;
+    float cbound_ = 0.0f;  // above every |coordinate| of the points
+    float kabs_ = 0.0f;    // the FP32 filter's absolute error term
+    int filter_ = 0;       // the FP32 distance filter applies (coordinates below 2^22)
+    Buffer pts_, ctr_, ctr32_, out_, acc_;
 };
 // roi (host mask of the pair's image, or NULL): the masked search of truncate_roi_subsets.
 void integer_search_batch(tdic_ctx* ctx, tdic_pair* lazy, const tdic_config& cfg, const int* cx, const int* cy,
