@@ -32,7 +32,7 @@ typedef enum tdic_status {
     TDIC_OOM = 2,           /* device allocation or admission refused */
     TDIC_CUDA_ERROR = 3,    /* a CUDA runtime error (message in tdic_last_error) */
     TDIC_TIMEOUT = 4,       /* a bounded device-side wait ran out */
-    TDIC_UNSUPPORTED = 5    /* a route or size this path does not cover (masked subsets, ...) */
+    TDIC_UNSUPPORTED = 5    /* a route or size this path does not cover (a batch of other routes, ...) */
 } tdic_status;
 
 typedef enum tdic_dtype { TDIC_U8 = 0, TDIC_U16 = 1, TDIC_F32 = 2, TDIC_F64 = 3 } tdic_dtype;
