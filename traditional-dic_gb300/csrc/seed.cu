@@ -279,33 +279,60 @@ __global__ void decimate_kernel(const float* __restrict__ def, int pitch, int cs
     }
 }
 
-// Exact block-wide argmax of circular_subset_zncc over the positions (u0 + t % nu, v0 + t / nu)
-// whose subset lies inside the image, t in scan order: FP32 maximum, then FP64 rescoring near it.
-__device__ void window_argmax(const float* __restrict__ def, int w, int h, int pitch, int r, const CandGeom& g,
-                              const SearchSmem& sm, int n, int u0, int v0, int nu, int nv, double& bz, int& bi) {
+// Exact block-wide argmaxes of circular_subset_zncc over two windows at once (either may be
+// empty): A at (ua + t % nua, va + t / nua), B at (ub + t % nub, vb + t / nub), t in scan order,
+// positions whose subset lies inside the image.  FP32 maxima of both in one sweep, then FP64
+// rescoring near each maximum in one sweep: the two windows' serial FP64 sums run on different
+// threads side by side.  Each window's result is its own argmax (the first of the best in its
+// scan order), as if it were searched alone.
+struct Window {
+    int u0, v0, nu, nv;
+    __device__ int size() const { return nu * nv; }
+};
+
+__device__ void window_argmax2(const float* __restrict__ def, int w, int h, int pitch, int r, const CandGeom& g,
+                               const SearchSmem& sm, int n, const Window& A, const Window& B, double& bza, int& bia,
+                               double& bzb, int& bib) {
     const float rm = sm.rs.fstats[0], rn = sm.rs.fstats[1], sr = sm.rs.fstats[2];
-    float best = -INFINITY;
-    for (int t = threadIdx.x; t < nu * nv; t += blockDim.x) {
-        const int u = u0 + t % nu, v = v0 + t / nu;
+    const int na = A.size(), total = na + B.size();
+    auto at = [&](int t, int& u, int& v) {  // the position of combined index t
+        if (t < na) { u = A.u0 + t % A.nu; v = A.v0 + t / A.nu; return; }
+        const int q = t - na;
+        u = B.u0 + q % B.nu;
+        v = B.v0 + q / B.nu;
+    };
+    float besta = -INFINITY, bestb = -INFINITY;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        int u, v;
+        at(t, u, v);
         const int x = g.cx + u, y = g.cy + v;
         if (!(x - r >= 0 && y - r >= 0 && x + r < w && y + r < h)) continue;
         bool flat;
-        best = fmaxf(best, zncc32(def, pitch, sm.off, sm.rs.r32, n, rm, rn, sr, g.cx, g.cy, u, v, flat));
+        const float z = zncc32(def, pitch, sm.off, sm.rs.r32, n, rm, rn, sr, g.cx, g.cy, u, v, flat);
+        if (t < na) besta = fmaxf(besta, z); else bestb = fmaxf(bestb, z);
     }
-    const float thr = block_max(best, sm.sf) - kScoreMargin;
-    bz = -INFINITY;
-    bi = 0x7fffffff;
-    for (int t = threadIdx.x; t < nu * nv; t += blockDim.x) {
-        const int u = u0 + t % nu, v = v0 + t / nu;
+    const float thra = block_max(besta, sm.sf) - kScoreMargin;
+    const float thrb = block_max(bestb, sm.sf) - kScoreMargin;
+    bza = -INFINITY; bia = 0x7fffffff;
+    bzb = -INFINITY; bib = 0x7fffffff;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        int u, v;
+        at(t, u, v);
         const int x = g.cx + u, y = g.cy + v;
         if (!(x - r >= 0 && y - r >= 0 && x + r < w && y + r < h)) continue;
         bool flat;
         const float z32 = zncc32(def, pitch, sm.off, sm.rs.r32, n, rm, rn, sr, g.cx, g.cy, u, v, flat);
-        if (!(flat || z32 >= thr)) continue;
+        if (!(flat || z32 >= (t < na ? thra : thrb))) continue;
         const double z = zncc64(def, pitch, sm.off, sm.rs.r64, n, sm.rs.stats[0], sm.rs.stats[1], g.cx, g.cy, u, v);
-        if (better(z, t, bz, bi)) { bz = z; bi = t; }
+        if (t < na) {
+            if (better(z, t, bza, bia)) { bza = z; bia = t; }
+        } else if (better(z, t - na, bzb, bib)) {
+            bzb = z;
+            bib = t - na;
+        }
     }
-    block_argmax(bz, bi, sm.sz, sm.si);
+    block_argmax(bza, bia, sm.sz, sm.si);
+    block_argmax(bzb, bib, sm.sz, sm.si);
 }
 
 // Full-sample refinement around the coarse optimum and the local +-search window, then the
@@ -352,44 +379,37 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(const float* __restr
         }
     }
     __syncthreads();
-    double best_z = s_cz;
-    int best_u = s_cu, best_v = s_cv;
-    bool have_global = coarse_ok_all && coarse_ok[blockIdx.x] && g.min_u <= g.max_u && g.min_v <= g.max_v;
-    if (have_global && isfinite(best_z) && full_ok) {
-        const int u0 = max(g.min_u, s_cu - rr), u1 = min(g.max_u, s_cu + rr);
-        const int v0 = max(g.min_v, s_cv - rr), v1 = min(g.max_v, s_cv + rr);
-        const int nu = u1 - u0 + 1, nv = v1 - v0 + 1;
-        double bz;
-        int bi;
-        window_argmax(def, w, h, pitch, r, g, sm, fn, u0, v0, nu, nv, bz, bi);
-        if (threadIdx.x == 0) {
-            s_cz = bz;
-            if (bi != 0x7fffffff) { s_cu = u0 + bi % nu; s_cv = v0 + bi / nu; } else { s_cu = 0; s_cv = 0; }
-        }
-        __syncthreads();
-        best_z = s_cz;
-        best_u = s_cu;
-        best_v = s_cv;
-    } else if (!isfinite(best_z)) {
-        best_u = s_cu;
-        best_v = s_cv;
+    // window A: the full-sample refinement around the coarse optimum; window B: the local
+    // +-search window (independent of A), searched together
+    const bool have_global = coarse_ok_all && coarse_ok[blockIdx.x] && g.min_u <= g.max_u && g.min_v <= g.max_v;
+    const bool en_a = have_global && isfinite(s_cz) && full_ok;
+    const bool en_b = search > 0 && full_ok;
+    Window A{0, 0, 0, 0}, B{0, 0, 0, 0};
+    if (en_a) {
+        A.u0 = max(g.min_u, s_cu - rr);
+        A.v0 = max(g.min_v, s_cv - rr);
+        A.nu = min(g.max_u, s_cu + rr) - A.u0 + 1;
+        A.nv = min(g.max_v, s_cv + rr) - A.v0 + 1;
     }
-    __syncthreads();
-    if (search > 0 && full_ok) {
-        const int n1 = 2 * search + 1;
-        double bz;
-        int bi;
-        window_argmax(def, w, h, pitch, r, g, sm, fn, -search, -search, n1, n1, bz, bi);
-        if (threadIdx.x == 0) {
-            const int lu = bi != 0x7fffffff ? -search + bi % n1 : 0;
-            const int lv = bi != 0x7fffffff ? -search + bi / n1 : 0;
-            // prefer_local_when_ambiguous
-            if (!isfinite(bz)) {
-            } else if (!isfinite(best_z)) { best_z = bz; best_u = lu; best_v = lv; }
-            else if (bz + 0.02 >= best_z) { best_z = bz; best_u = lu; best_v = lv; }
-            out[blockIdx.x] = SearchResult{best_u, best_v, best_z, (isfinite(best_z) && full_ok) ? 1 : 0};
+    if (en_b) B = Window{-search, -search, 2 * search + 1, 2 * search + 1};
+    double bza, bzb;
+    int bia, bib;
+    window_argmax2(def, w, h, pitch, r, g, sm, fn, A, B, bza, bia, bzb, bib);
+    if (threadIdx.x == 0) {
+        double best_z = s_cz;
+        int best_u = s_cu, best_v = s_cv;
+        if (en_a) {
+            best_z = bza;
+            if (bia != 0x7fffffff) { best_u = A.u0 + bia % A.nu; best_v = A.v0 + bia / A.nu; } else { best_u = 0; best_v = 0; }
         }
-    } else if (threadIdx.x == 0) {
+        if (en_b) {
+            const int lu = bib != 0x7fffffff ? B.u0 + bib % B.nu : 0;
+            const int lv = bib != 0x7fffffff ? B.v0 + bib / B.nu : 0;
+            // prefer_local_when_ambiguous
+            if (!isfinite(bzb)) {
+            } else if (!isfinite(best_z)) { best_z = bzb; best_u = lu; best_v = lv; }
+            else if (bzb + 0.02 >= best_z) { best_z = bzb; best_u = lu; best_v = lv; }
+        }
         out[blockIdx.x] = SearchResult{best_u, best_v, best_z, (isfinite(best_z) && full_ok) ? 1 : 0};
     }
 }
