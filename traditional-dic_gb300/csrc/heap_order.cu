@@ -29,7 +29,6 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
-#include <queue>
 
 namespace tdic {
 
@@ -115,11 +114,64 @@ struct HeapTable {
     std::vector<int> pop_step;          // pop at which a point was popped (-1: never)
     bool sim_valid = false;             // calc_step / pop_step describe the table's last simulation
 
-    struct Item {
-        double corrcoef;
-        int n;
-        bool operator<(const Item& o) const { return corrcoef > o.corrcoef; }  // QueueItem, :44-53
+    // The reference's queue: std::priority_queue<QueueItem> ordered by corrcoef, the smallest on
+    // top (reliability_propagation.cpp:44-53, 270-275).  Which of two equal keys comes out first
+    // is decided by the binary heap's layout, so the exact queue is that binary heap itself: on a
+    // push the new element rises past every parent with a larger key; on a pop the last element
+    // fills the root's place after the hole has been walked down to a leaf through, at each
+    // level, the right child unless the left one's key is smaller.  Keys are P (a float table's
+    // keys are floats: the same order and the same ties), keys and points in separate arrays.
+    struct TieHeap {
+        std::vector<P> key;
+        std::vector<int> val;
+        size_t n = 0;
+        bool empty() const { return n == 0; }
+        int top() const { return val[0]; }
+        void push(P k, int v) {
+            if (n == key.size()) {
+                key.resize(2 * n + 64);
+                val.resize(2 * n + 64);
+            }
+            rise(n++, 0, k, v);
+        }
+        void pop() {
+            if (n > 1) {
+                const P k = key[n - 1];
+                const int v = val[n - 1];
+                key[n - 1] = key[0];
+                val[n - 1] = val[0];
+                const size_t len = n - 1;
+                size_t hole = 0, child = 0;
+                while (child < (len - 1) / 2) {
+                    child = 2 * (child + 1);
+                    if (key[child] > key[child - 1]) --child;
+                    key[hole] = key[child];
+                    val[hole] = val[child];
+                    hole = child;
+                }
+                if ((len & 1) == 0 && child == (len - 2) / 2) {
+                    child = 2 * (child + 1);
+                    key[hole] = key[child - 1];
+                    val[hole] = val[child - 1];
+                    hole = child - 1;
+                }
+                rise(hole, 0, k, v);
+            }
+            --n;
+        }
+        void rise(size_t hole, size_t top, P k, int v) {
+            while (hole > top) {
+                const size_t parent = (hole - 1) / 2;
+                if (!(key[parent] > k)) break;
+                key[hole] = key[parent];
+                val[hole] = val[parent];
+                hole = parent;
+            }
+            key[hole] = k;
+            val[hole] = v;
+        }
     };
+    TieHeap pq;  // reused by every exact simulation
 
     // Bucket queue over non-negative keys (ZNSSD and SSD values): the bit pattern of a
     // non-negative double orders like the value; the span of the patterns the simulation can
@@ -127,8 +179,8 @@ struct HeapTable {
     // simulation), a bucket holds its points in a list and a three-level bitmap finds the lowest
     // non-empty bucket.  A pop takes the
     // bucket's smallest key; two equal keys in the queue at once would leave the order to
-    // std::priority_queue's tie rule, so the queue reports a tie and the caller repeats the
-    // simulation with std::priority_queue itself.
+    // the binary heap's tie rule, so the queue reports a tie and the caller repeats the
+    // simulation with the binary heap itself (TieHeap).
     struct BucketQueue {
         static constexpr int kBits = 18;
         std::vector<int> head, next;
@@ -242,7 +294,7 @@ struct HeapTable {
             accepted[seed] = 1;
             newpar[seed] = -1;
         }
-        std::priority_queue<Item> pq;
+        pq.n = 0;
         const double seed_key = std::max(0.0, static_cast<double>(corr[seed]));
         if (!exact_queue) {
             double klo = seed_key, khi = seed_key;
@@ -254,7 +306,7 @@ struct HeapTable {
             bq.init(total, klo, khi);
         }
         auto push = [&](double k, int n) -> bool {
-            if (exact_queue) { pq.push(Item{k, n}); return true; }
+            if (exact_queue) { pq.push(static_cast<P>(k), n); return true; }  // a P key: exact
             return bq.push(k, n);
         };
         int pops = 0;
@@ -268,12 +320,13 @@ struct HeapTable {
                     if (!push(i == seed ? seed_key : rec[i].corr, i)) return false;
         }
         const int dxs[4] = {0, step, 0, -step}, dys[4] = {-step, 0, step, 0};  // up, right, down, left
+        const int gdx[4] = {0, 1, 0, -1}, gdy[4] = {-1, 0, 1, 0};
         const P cutoff = static_cast<P>(step);
         for (;;) {
             int n;
             if (exact_queue) {
                 if (pq.empty()) break;
-                n = pq.top().n;
+                n = pq.top();
                 pq.pop();
             } else {
                 if (bq.empty()) break;
@@ -282,13 +335,13 @@ struct HeapTable {
             }
             const int k = pops++;
             pop_step[n] = k;
-            const int px = (n % gw) * step, py = (n / gw) * step;
+            const int gy = n / gw, gx = n - gy * gw;
             const int vn = ver[n];
             const P* pp = &p[static_cast<size_t>(n) * 6];
             for (int d = 0; d < 4; ++d) {
-                const int nx = px + dxs[d], ny = py + dys[d];
+                const int gnx = gx + gdx[d], gny = gy + gdy[d];  // the neighbour (px + dxs[d], py + dys[d])
+                const int nx = gnx * step, ny = gny * step;
                 if (nx < 0 || ny < 0 || nx >= w || ny >= h) continue;
-                const int gnx = nx / step, gny = ny / step;
                 if (gnx >= gw || gny >= gh) continue;
                 const int m = gny * gw + gnx;
                 if (calculated[m]) continue;
