@@ -262,9 +262,13 @@ struct HeapTable {
                 if (calc_step[x] >= 0) k0 = std::min(k0, calc_step[x]);  // the pop of its parent
             k0 = std::min(k0, total);
         }
-        if (simulate_from(total, k0, false)) return;
-        simulate_from(total, 0, true);  // a tie: the reference's own queue decides, from the start
+        if (!tied && simulate_from(total, k0, false)) return;
+        // a tie: the reference's own queue decides, from the start; a table whose keys tied once
+        // (a float table's often do) goes to it directly from then on
+        tied = true;
+        simulate_from(total, 0, true);
     }
+    bool tied = false;  // a simulation of this table met two equal keys in the queue
 
     // Returns false when the bucket queue met a tie (nothing usable was produced).
     bool simulate_from(int total, int k0, bool exact_queue) {
