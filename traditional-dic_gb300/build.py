@@ -45,7 +45,7 @@ def _stale(obj: str, src: str) -> bool:
     if not os.path.exists(obj):
         return True
     deps = [src, os.path.join(HERE, "..", "include", "tdic_gb300.h")]
-    deps += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
+    deps += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     return any(os.path.getmtime(d) > os.path.getmtime(obj) for d in deps)
 
 

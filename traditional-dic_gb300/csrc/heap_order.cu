@@ -23,6 +23,7 @@
 // first dirty point's parent was exact, so its new result is), so the rounds end; in practice
 // after two or three (the parent choices move only where two ZNSSD keys are close).
 #include "tdic_internal.cuh"
+#include "tie_heap.h"
 
 #include <algorithm>
 #include <chrono>
@@ -114,64 +115,7 @@ struct HeapTable {
     std::vector<int> pop_step;          // pop at which a point was popped (-1: never)
     bool sim_valid = false;             // calc_step / pop_step describe the table's last simulation
 
-    // The reference's queue: std::priority_queue<QueueItem> ordered by corrcoef, the smallest on
-    // top (reliability_propagation.cpp:44-53, 270-275).  Which of two equal keys comes out first
-    // is decided by the binary heap's layout, so the exact queue is that binary heap itself: on a
-    // push the new element rises past every parent with a larger key; on a pop the last element
-    // fills the root's place after the hole has been walked down to a leaf through, at each
-    // level, the right child unless the left one's key is smaller.  Keys are P (a float table's
-    // keys are floats: the same order and the same ties), keys and points in separate arrays.
-    struct TieHeap {
-        std::vector<P> key;
-        std::vector<int> val;
-        size_t n = 0;
-        bool empty() const { return n == 0; }
-        int top() const { return val[0]; }
-        void push(P k, int v) {
-            if (n == key.size()) {
-                key.resize(2 * n + 64);
-                val.resize(2 * n + 64);
-            }
-            rise(n++, 0, k, v);
-        }
-        void pop() {
-            if (n > 1) {
-                const P k = key[n - 1];
-                const int v = val[n - 1];
-                key[n - 1] = key[0];
-                val[n - 1] = val[0];
-                const size_t len = n - 1;
-                size_t hole = 0, child = 0;
-                while (child < (len - 1) / 2) {
-                    child = 2 * (child + 1);
-                    if (key[child] > key[child - 1]) --child;
-                    key[hole] = key[child];
-                    val[hole] = val[child];
-                    hole = child;
-                }
-                if ((len & 1) == 0 && child == (len - 2) / 2) {
-                    child = 2 * (child + 1);
-                    key[hole] = key[child - 1];
-                    val[hole] = val[child - 1];
-                    hole = child - 1;
-                }
-                rise(hole, 0, k, v);
-            }
-            --n;
-        }
-        void rise(size_t hole, size_t top, P k, int v) {
-            while (hole > top) {
-                const size_t parent = (hole - 1) / 2;
-                if (!(key[parent] > k)) break;
-                key[hole] = key[parent];
-                val[hole] = val[parent];
-                hole = parent;
-            }
-            key[hole] = k;
-            val[hole] = v;
-        }
-    };
-    TieHeap pq;  // reused by every exact simulation
+    TieHeap<P> pq;  // the reference's queue (tie_heap.h), reused by every exact simulation
 
     // Bucket queue over non-negative keys (ZNSSD and SSD values): the bit pattern of a
     // non-negative double orders like the value; the span of the patterns the simulation can
