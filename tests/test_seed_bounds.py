@@ -1,4 +1,4 @@
-"""The two arguments the seed search's kernels rest on, checked on the CPU.
+"""The arguments the seed search's kernels rest on, checked on the CPU.
 
 * Coarse lattice: with circle offsets (dx, dy) that start at -r in steps of cstep
   (circle_offsets) and positions u = r - cx + cstep * ui (min_u = r - cx), every deformed sample
@@ -8,7 +8,9 @@
 * k-means filter: for centres rounded to float and distances rounded in float (no fused
   multiply-add), |d32 - d64| stays below err32 = 1e-6 (C (|dx32| + |dy32|) + d32) + 16 (2^-24 C)^2
   + 1e-6, C above every coordinate, up to C = 2^22; err32 is what the kernel allows, so the FP64
-  minimum is always among the centres it rescores."""
+  minimum is always among the centres it rescores.
+* One-pass coarse search: rescoring near each tile's FP32 maximum picks the winner that
+  rescoring near the candidate's FP32 maximum picks."""
 import numpy as np
 import pytest
 
@@ -59,3 +61,37 @@ def test_kmeans_fp32_error_bound(big):
     ddx, ddy = px - cx, py - cy
     d64 = ddx * ddx + ddy * ddy
     assert np.all(np.abs(d32.astype(np.float64) - d64) <= 0.25 * err.astype(np.float64))   # four times over
+
+
+def _argmax_first(z, idx):
+    """The winner of the search's rule: the largest FP64 score, the first in scan order on ties."""
+    if len(idx) == 0:
+        return None
+    best = max(z[i] for i in idx)
+    return min(i for i in idx if z[i] == best)
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_one_pass_tile_threshold_picks_the_two_pass_winner(seed):
+    """The coarse search's one pass rescores, per tile, the positions within the margin of the
+    tile's FP32 maximum; the two-pass search rescores the positions within the margin of the
+    candidate's FP32 maximum.  With FP32 scores within margin / 2 of the FP64 ones, both pick the
+    same position (ties to the first in scan order), on score surfaces with plateaus and ties."""
+    rng = np.random.default_rng(seed)
+    margin, err = 1e-3, 4e-5
+    npos, per_tile = int(rng.integers(500, 20000)), int(rng.choice([64, 256, 4096]))
+    z64 = rng.uniform(-0.3, 0.6, npos)
+    peak = rng.integers(0, npos, 3)
+    z64[peak] = 0.95                                              # tied maxima
+    near = rng.integers(0, npos, 40)
+    z64[near] = 0.95 - rng.uniform(0, 2 * margin, 40)             # close runners-up
+    z64 = np.round(z64, int(rng.choice([3, 6, 12])))              # plateaus: many equal scores
+    z32 = z64 + rng.uniform(-err, err, npos)
+    two_pass = [i for i in range(npos) if z32[i] >= z32.max() - margin]
+    one_pass = []
+    for t0 in range(0, npos, per_tile):
+        tile = range(t0, min(npos, t0 + per_tile))
+        tmax = max(z32[i] for i in tile)
+        one_pass += [i for i in tile if z32[i] >= tmax - margin]
+    assert set(two_pass) <= set(one_pass)
+    assert _argmax_first(z64, one_pass) == _argmax_first(z64, two_pass) == _argmax_first(z64, range(npos))
