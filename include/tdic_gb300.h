@@ -331,7 +331,8 @@ tdic_status tdic_select_seed(tdic_ctx* ctx, tdic_pair* lazy, const float* refere
  * refinement around its optimum, the local +-search window and the local-preference rule.
  * Out, per point: the integer displacement (u, v), its ZNCC (FP64, rounded as the reference's)
  * and ok = 0 where the reference returns no estimate.  With cfg->truncate_roi_subsets the
- * masked search over roi (host H x W mask; every pixel when NULL), as seed selection uses it. */
+ * masked search over roi (host H x W mask; every pixel when NULL), as seed selection uses it.
+ * At most 65535 points per call (TDIC_INVALID_ARG beyond). */
 tdic_status tdic_integer_search(tdic_ctx* ctx, tdic_pair* pair, const tdic_config* cfg,
                                 const int32_t* x, const int32_t* y, int32_t n, const uint8_t* roi,
                                 double* u, double* v, double* zncc, uint8_t* ok, void* stream);

@@ -272,6 +272,21 @@ def test_integer_search_matches_oracle(oracle, gpu_ctx, workload0, with_roi):
         assert got["ok"][:ncand].all()
 
 
+def test_integer_search_refuses_more_points_than_a_grid_row(gpu_ctx, workload0):
+    """One coarse-grid row per point: more than 65535 points in one call is refused up front."""
+    import __graft_entry__ as G
+    from traditional_dic_gb300 import subset as S, _lib as L
+    p = workload0
+    cfg = S.config_from_dict(G.WORKLOAD0_CONFIG)
+    pair = S.Pair(gpu_ctx, p.reference, p.deformed, degree=3, exact=False)
+    pts = np.full(65536, 128, np.int32)
+    with pytest.raises(L.TdicError, match="at most 65535 points"):
+        S.integer_search(gpu_ctx, pair, cfg, pts, pts)
+    got = S.integer_search(gpu_ctx, pair, cfg, pts[:3], pts[:3])   # the context stays usable
+    assert len(set(got["ok"])) == 1 and len(set(got["u"])) == 1 and len(set(got["v"])) == 1
+    pair.close()
+
+
 def _heap(oracle, cfg):
     c = oracle.as_config(cfg)
     c.propagation_mode = 1

@@ -601,6 +601,7 @@ void KmeansAssigner::assign(const double* cx, const double* cy, int* assign_host
 void integer_search_batch(tdic_ctx* ctx, tdic_pair* lazy, const tdic_config& cfg, const int* cx, const int* cy, int n,
                           SearchResult* out_host, cudaStream_t s, const uint8_t* roi) {
     if (n <= 0) return;
+    TDIC_REQUIRE(n <= 65535, TDIC_INVALID_ARG, "integer search: at most 65535 points per call (one grid row each)");
     const int w = lazy->w, h = lazy->h;
     const int r = cfg.is_subset_radius < 1 ? 1 : cfg.is_subset_radius;
     const int search = cfg.is_search_radius < 0 ? 0 : cfg.is_search_radius;
