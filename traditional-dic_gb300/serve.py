@@ -122,9 +122,11 @@ class Server:
     # ---- client side -------------------------------------------------------------------------
     def submit(self, reference: np.ndarray, deformed: np.ndarray, config: dict | L.Config | None = None,
                roi=None) -> Request:
-        """Queue one pair.  Bad images or a bad config raise here, as ``subset.compute`` would.
-        ``config`` is a config dict, or a full ``Config`` structure as ``subset.compute_config``
-        takes (the result is then ``compute_config``'s, e.g. with masked subsets)."""
+        """Queue one pair.  Bad images or a bad config dict raise here, as ``subset.compute``
+        would.  ``config`` is a config dict, or a full ``Config`` structure as
+        ``subset.compute_config`` takes (the result is then ``compute_config``'s, e.g. with
+        masked subsets); a structure's values are checked when the request is prepared, and a
+        bad one fails that request alone."""
         ref = S._check_image(reference, "reference")
         de = S._check_image(deformed, "deformed")
         if config is not None and not isinstance(config, (dict, L.Config)):
